@@ -1,0 +1,176 @@
+"""Force-field tables and system layout in MACSIMUS cook conventions.
+
+Host-side counterpart of the parts of cook/simdef.c (``readblend``) that the
+force path consumes: per-type Lennard-Jones parameters (EvdW<0 in K, RvdW in
+Angstrom, polarizability ``alpha`` for the combining rule), site charges in
+program units (e * 408.779826922048, sim/units.h:101-108), site masses in
+program units (g/mol / 0.831446261815324, cook/simdef.c:1021) and the rigid
+bond constraints of each species.
+
+Numbers pass through the same decimal text a cook ``.ble`` file holds
+(12 significant digits for LJ parameters, cook/simdef.c:620-628), so a system
+built here and the same system read by cook from the written ``.ble`` carry
+identical doubles.  ``ble_text`` writes that file.
+"""
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+ELECTRON = 408.779826922048        # charge of e in program units
+MUNIT = 0.831446261815324          # g/mol per program mass unit
+EUNIT = 8.31446261815324           # J/mol per program energy unit (K)
+KCAL = 4184.0
+KJ_PER_KCAL = 4.184
+EUNIT_KCAL = KCAL / EUNIT          # cook's default eunit: kcal/mol -> K
+HOH = math.sqrt(8.0 / 3.0)         # SPC/E H-H distance (O-H 1 A, tetrahedral)
+
+
+def _g12(x):
+    return float("%.12g" % x)
+
+
+def rvdw_of_sigma(sigma):
+    """van der Waals radius of the .ble table: sigma * 2^(1/6) / 2."""
+    return sigma * 2.0 ** (1.0 / 6.0) / 2.0
+
+
+# LJ site types: name -> (mass g/mol, epsilon kJ/mol, sigma A)
+SITE_TYPES = {
+    "H": (1.008, 0.0, 0.0),
+    "O": (15.9994, 0.6502, 3.166),
+    "NA": (22.9898, 1.475, 2.16),
+    "CL": (35.453, 0.0535, 4.83),
+}
+TYPE_ORDER = ["H", "O", "NA", "CL"]
+
+
+def ble_type_row(name):
+    """(mass, EvdW[kcal/mol], RvdW[A]) exactly as written into the .ble."""
+    m, eps, sig = SITE_TYPES[name]
+    ev = _g12(-eps / KJ_PER_KCAL)
+    rv = _g12(rvdw_of_sigma(sig)) if sig else 0.5
+    return float("%.6f" % m), ev, rv
+
+
+def type_table():
+    """Per-type arrays in program units: EvdW [K] (<=0), RvdW [A], alpha."""
+    E, R, A, M = [], [], [], []
+    for n in TYPE_ORDER:
+        m, ev, rv = ble_type_row(n)
+        E.append(EUNIT_KCAL * ev)
+        R.append(rv)
+        A.append(0.0)
+        M.append(m)
+    return np.array(E), np.array(R), np.array(A), np.array(M)
+
+
+@dataclass
+class Species:
+    name: str
+    sites: list            # type names
+    charges: list          # e
+    geometry: np.ndarray   # reference geometry [ns,3] (A)
+    bonds: list = field(default_factory=list)  # (i, j, length)
+    drude: dict = None     # {site index: (alphapol A^3, chargepol e)}
+
+
+def spce():
+    c = math.cos(math.acos(-1.0 / 3.0))
+    s = math.sin(math.acos(-1.0 / 3.0))
+    return Species("WAT", ["O", "H", "H"], [-0.8476, 0.4238, 0.4238],
+                   np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [c, s, 0.0]]),
+                   bonds=[(0, 1, 1.0), (0, 2, 1.0), (1, 2, HOH)])
+
+
+def ion(name):
+    q = 1.0 if name == "NA" else -1.0
+    return Species(name, [name], [q], np.zeros((1, 3)))
+
+
+SPECIES = {"WAT": spce, "NA": lambda: ion("NA"), "CL": lambda: ion("CL")}
+
+
+@dataclass
+class System:
+    """Flat site arrays in cook order: species by species, molecule by
+    molecule, site by site (the layout of cook's ToInt ``rp`` arrays)."""
+    type: np.ndarray       # [ns] int32 LJ type
+    q: np.ndarray          # [ns] charge, program units
+    mass: np.ndarray       # [ns] mass, program units
+    mol: np.ndarray        # [ns] int32 molecule index
+    mol_first: np.ndarray  # [nmol+1] first site of each molecule
+    cons: np.ndarray       # [nc,2] int32 constrained site pairs (global)
+    cons_len: np.ndarray   # [nc] constraint length (A)
+    mol_cfirst: np.ndarray # [nmol+1] first constraint of each molecule
+    typeE: np.ndarray      # [ntypes] EvdW (K, <=0)
+    typeR: np.ndarray      # [ntypes] RvdW (A)
+    typeA: np.ndarray      # [ntypes] combining-rule polarizability
+    comb_rule: int = 1
+    species: list = None
+    counts: list = None
+
+    @property
+    def ns(self):
+        return len(self.type)
+
+    @property
+    def nmol(self):
+        return len(self.mol_first) - 1
+
+
+def build_system(species_names, counts):
+    E, R, A, _ = type_table()
+    tix = {n: i for i, n in enumerate(TYPE_ORDER)}
+    typ, q, mass, mol, mfirst, cons, clen, cfirst = [], [], [], [], [0], [], [], [0]
+    imol = 0
+    for sname, n in zip(species_names, counts):
+        sp = SPECIES[sname]()
+        for _ in range(n):
+            base = len(typ)
+            for k, t in enumerate(sp.sites):
+                typ.append(tix[t])
+                q.append(ELECTRON * sp.charges[k])
+                mass.append(ble_type_row(t)[0] / MUNIT)
+                mol.append(imol)
+            for (i, j, d) in sp.bonds:
+                cons.append((base + i, base + j))
+                clen.append(d)
+            imol += 1
+            mfirst.append(len(typ))
+            cfirst.append(len(cons))
+    return System(type=np.array(typ, np.int32), q=np.array(q), mass=np.array(mass),
+                  mol=np.array(mol, np.int32), mol_first=np.array(mfirst, np.int32),
+                  cons=np.array(cons, np.int32).reshape(-1, 2), cons_len=np.array(clen),
+                  mol_cfirst=np.array(cfirst, np.int32), typeE=E, typeR=R, typeA=A,
+                  comb_rule=1, species=list(species_names), counts=list(counts))
+
+
+def ble_text(species_names):
+    """The cook force-field (.ble) file of these species (test fixtures)."""
+    lines = ["! force field written by macsimus_gb300.forcefield",
+             "nspec=%d" % len(species_names),
+             "  nsites=%d  nnbfixes=0  factor14=1  distance14=0  comb_rule=1" % len(TYPE_ORDER),
+             "  polar=0  nparms=0;", "", "Lennard-Jones",
+             "! i atom mass alpha EvdW[kcal/mol] RvdW[A]"]
+    for i, n in enumerate(TYPE_ORDER):
+        m, ev, rv = ble_type_row(n)
+        lines.append("  %d %-3s %.6f 0 %.12g %.12g" % (i, n, m, ev, rv))
+    lines += ["", "nbfixes", ""]
+    for isp, sname in enumerate(species_names):
+        sp = SPECIES[sname]()
+        ns = len(sp.sites)
+        lines += ["", "species %s" % sname, "", "i=%d  N=0  config=0  water=0" % isp,
+                  "ns=%d  nc=%d  nangles=0  ndihedrals=0  nimpropers=0  naromatics=0"
+                  % (ns, len(sp.bonds)), "ndependants=0 ;", "", "sites"]
+        for k in range(ns):
+            excl = " ".join(str(j) for j in range(k))
+            x, y, z = sp.geometry[k]
+            lines.append("  %d %-3s %.4f  %.12f %.12f %.12f  %d %s"
+                         % (k, sp.sites[k], sp.charges[k], x, y, z, k, excl))
+        lines += ["", "bonds"]
+        for (i, j, d) in sp.bonds:
+            lines.append("  %d %s   %d %s   450  %.15f" % (i, sp.sites[i], j, sp.sites[j], d))
+        lines += ["", "angles", "", "dihedrals", "", "impropers", "", "aromatics", "",
+                  "dependants", "", ""]
+    return "\n".join(lines) + "\n\n"

@@ -1,0 +1,763 @@
+/*
+ * cookoracle.c -- CPU restatement of cook's force path (TEST INFRASTRUCTURE).
+ *
+ * Used only by tests/, the smoke check and the benchmark's CPU-baseline leg,
+ * as the checker.  Never part of the product path.  Each function cites the
+ * reference file:line it restates.  Plain C99, double precision, pthreads.
+ */
+#include "cookoracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define SQ(x) ((x) * (x))
+#define SQRTPI 1.772453850905516
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+/* ------------------------------------------------------------------ LJ --- */
+
+/* sim/lj/sitesite.c:37-93 (initcombrule + combrule) */
+void orc_combrule(double E0, double R0, double a0, double E1, double R1, double a1,
+                  int comb_rule, double *eps, double *sig)
+{
+  int cr0 = comb_rule | (a0 <= 0), cr1 = comb_rule | (a1 <= 0);
+  int cr = cr0 | cr1;
+  double g0, g1, r, A, B;
+  if (E0 > 0) E0 = -E0;
+  if (E1 > 0) E1 = -E1;
+  g0 = E0 != 0 ? SQ(a0) / E0 / (SQ(R0) * SQ(R0) * SQ(R0)) / -256 : 3e37;
+  g1 = E1 != 0 ? SQ(a1) / E1 / (SQ(R1) * SQ(R1) * SQ(R1)) / -256 : 3e37;
+  if (cr & 2) { double x = R0 * R1 * 4; r = x * x * x; }
+  else { double x = SQ(R0 + R1); r = x * x * x; }
+  if (cr & 1) B = sqrt(-2 * E0) * sqrt(-2 * E1) * r;
+  else B = a0 * a1 / (g0 + g1);
+  A = B * r;
+  *sig = B == 0 ? 0 : pow(A / B, 1. / 6);
+  *eps = A == 0 ? 0 : B * B / (-2 * A);
+}
+
+/* potential and force of the LJ form u=-eps[(sig/r)^12-2(sig/r)^6]
+   (SS_U / SS_F of sim/lj/sitesite.h:85-86) */
+static double ss_u(double eps, double sig, double r)
+{
+  double x = sig / r;
+  x = SQ(x) * SQ(x) * SQ(x);
+  return -eps * (x * x - 2 * x);
+}
+static double ss_f(double eps, double sig, double r)
+{
+  double x = sig / r;
+  x = SQ(x) * SQ(x) * SQ(x);
+  return -12 * eps * (x * x - x) / r;
+}
+
+/* sim/setss.c:137-300 (smooth cutoff) + 460-510 (cutoff correction) and
+   initssaux sim/lj/sitesite.c:96-112 */
+int orc_setss(double eps, double sig, double C2, orc_ss_t *ss)
+{
+  double C1, oldC1;
+  int n = 0;
+  const double meps = 2.220446049250313e-16; /* machine precision (No.eps) */
+  memset(ss, 0, sizeof(*ss));
+  ss->eps = eps;
+  ss->sig = sig;
+  /* initssaux */
+  ss->Sq = SQ(sig) * 0.7937005259840998;
+  ss->E4 = -4 * eps;
+  if (ss->Sq != 0) {
+    ss->E24 = -24 * eps / ss->Sq;
+    ss->E48 = -48 * eps / ss->Sq;
+  }
+  if (eps == 0 || C2 == 0) {
+    C1 = C2 = ss->A = 0;
+  } else {
+    if (C2 < 0) C2 = -sig * C2;
+    C1 = 0.775 * C2;
+    do {
+      double den = ss_f(eps, sig, C1);
+      if (fabs(den) < 1e-50) { C1 = -C1; break; }
+      oldC1 = C1;
+      C1 = 1 + 4 * ss_u(eps, sig, C1) / C1 / den;
+      if (n++ > 2000 || C1 < 0) { C1 = 0.775 * C2; return -1; }
+      C1 = C2 / sqrt(C1);
+    } while (fabs(1 - C1 / oldC1) > meps * n);
+    if (C1 > 0 && (C1 > 0.999 * C2 || C1 < 0.5 * C2)) return -2;
+    ss->A = ss_u(eps, sig, C1) / SQ(C2 * C2 - C1 * C1);
+  }
+  if (C1 < 0) { C1 = -C1; ss->A = ss->A4 = 0; }
+  else if (C2 > 0) ss->A4 = -ss_f(eps, sig, C1) / (C2 * C2 - C1 * C1) / C1;
+  ss->C2q = C2 * C2;
+  ss->C1q = C1 * C1;
+  /* normalized cutoff correction: analytic part + 4th order Gauss on 1/r */
+  if (eps != 0) {
+    double C14 = SQ(C1) * SQ(C1), C16 = C14 * SQ(C1), C24 = SQ(C2) * SQ(C2);
+    double corr0 = 4 * M_PI * ss->A *
+      (C1 * (C16 / 7 - 0.4 * C14 * SQ(C2) + SQ(C1) * C24 / 3) - 8.0 / 105 * pow(C2, 7));
+    double h = 1.0 / 64 / C1, corr1 = 0, r;
+    const double g4 = 0.2113248654051871;
+    for (n = 0; n < 64; n++) {
+      r = 1 / ((n + g4) * h); corr1 += SQ(r) * SQ(r) * ss_u(eps, sig, r);
+      r = 1 / ((n + (1 - g4)) * h); corr1 += SQ(r) * SQ(r) * ss_u(eps, sig, r);
+    }
+    corr1 *= 2 * M_PI * h;
+    ss->corr = corr0 + corr1;
+  }
+  return 0;
+}
+
+/* ---------------------------------------------------------------- erfc --- */
+
+/* sim/erfc.c:119-150: number of spline intervals for [0,maxr) */
+int orc_erfc_ntab(int grid, double maxr, double alpha)
+{
+  return (int)(SQ(maxr * alpha) * grid) + 1;
+}
+
+/* values at alpha=1: e=erfc(sqrt x)/sqrt x, z=(2/sqrt(pi) exp(-x)+e)/x
+   (erfcs, sim/erfc.c:76-85) */
+static void erfcs(long to, double h, double *e, double *z)
+{
+  if (to) {
+    double rr = to * h, r = sqrt(rr), er = erfc(r);
+    *e = er / r;
+    *z = ((2 / SQRTPI) * exp(-rr) + er / r) / rr;
+  } else
+    *e = *z = 9e9;
+}
+
+/* makesplines SPLINE=-2, SUBGRID=1 (sim/splines.c:23-158) followed by the
+   shifts of initerfc (sim/erfc.c:176-187).  tab: 6 doubles per interval */
+void orc_erfc_build(int grid, double maxr, double cutoff, double alpha, int shift,
+                    double *tab, double *sgrid_out)
+{
+  int ito = orc_erfc_ntab(grid, maxr, alpha), i, n = ito;
+  double h = 1.0 / grid, Du, Dd, x, xh;
+  double *fu = malloc(sizeof(double) * (n + 3)), *fd = malloc(sizeof(double) * (n + 3));
+  double a = alpha, sgrid;
+  for (i = n + 2; i >= 0; i--) erfcs(i, h, &fu[i], &fd[i]);
+  Du = (-fu[n + 2] + 8 * fu[n + 1] - 8 * fu[n - 1] + fu[n - 2]) / (12 * h);
+  Dd = (-fd[n + 2] + 8 * fd[n + 1] - 8 * fd[n - 1] + fd[n - 2]) / (12 * h);
+  x = n * h;
+  while (ito--) {
+    double *p = tab + 6 * ito;
+    double Au, Bu, Cu, Ad, Bd, Cd;
+    xh = x;
+    i = ito;
+    x = i * h;
+    Cu = (x * (fu[i + 1] - fu[i]) - xh * Du * h) / (Du * h - (fu[i + 1] - fu[i]));
+    Bu = -Du * SQ(Cu + xh);
+    Au = fu[i + 1] + Du * (Cu + xh);
+    Du = -Bu / SQ(Cu + x);
+    Cd = (x * (fd[i + 1] - fd[i]) - xh * Dd * h) / (Dd * h - (fd[i + 1] - fd[i]));
+    Bd = -Dd * SQ(Cd + xh);
+    Ad = fd[i + 1] + Dd * (Cd + xh);
+    Dd = -Bd / SQ(Cd + x);
+    p[0] = Au * a;
+    p[1] = Bu / a;
+    p[2] = Cu / SQ(a);
+    p[3] = Ad * (a * a * a);
+    p[4] = Bd * a;
+    p[5] = Cd / SQ(a);
+  }
+  sgrid = grid * SQ(a);
+  free(fu);
+  free(fd);
+  {
+    int nt = orc_erfc_ntab(grid, maxr, alpha);
+    double z = SQ(cutoff), v;
+    if (shift & 1) {
+      v = orc_eru(tab, sgrid, z);
+      for (i = 0; i < nt; i++) tab[6 * i] -= v;
+    }
+    if (shift & 2) {
+      v = orc_erd(tab, sgrid, z);
+      for (i = 0; i < nt; i++) tab[6 * i + 3] -= v;
+    }
+  }
+  *sgrid_out = sgrid;
+}
+
+/* eru/erd macros of sim/elst.h:122-130 */
+double orc_eru(const double *tab, double sgrid, double rr)
+{
+  const double *p = tab + 6 * (int)(rr * sgrid);
+  return p[1] / (p[2] + rr) + p[0];
+}
+double orc_erd(const double *tab, double sgrid, double rr)
+{
+  const double *p = tab + 6 * (int)(rr * sgrid);
+  return p[4] / (p[5] + rr) + p[3];
+}
+
+/* sim/erexact.c:25-75 (SUBGRID==1): -erf(alpha r)/r and its derivative term */
+static double exacterud_core(double rr, double alpha, double *erd, int minus1)
+{
+  double A = alpha * (-2 / SQRTPI), alphaq = SQ(alpha), B = A * alphaq * 2;
+  double err = alphaq * rr;
+  if (err < 0.01) {
+    int n = 1;
+    double su = 0, sd = 0, q = 1, r;
+    for (;;) {
+      r = q / (2 * n + 1);
+      sd += r * n;
+      su += r;
+      if (fabs(q) < (minus1 ? 1e-17 : 1e-16)) break;
+      q *= -err / ++n;
+    }
+    *erd = B * sd;
+    return minus1 ? A * (-su * err) : A * (1 - su * err);
+  } else {
+    double r = sqrt(rr);
+    double y = -erf(alpha * r) / r;
+    *erd = (y - A * exp(-err)) / rr;
+    return minus1 ? y - A : y;
+  }
+}
+double orc_exacterud_sqrt(double rr, double alpha, double *erd)
+{
+  return exacterud_core(rr, alpha, erd, 0);
+}
+double orc_exacterud_sqrt_1(double rr, double alpha, double *erd)
+{
+  return exacterud_core(rr, alpha, erd, 1);
+}
+
+/* ---------------------------------------------------------- k-vectors --- */
+
+static int almostint(double x)
+{
+  x -= (int)x;
+  return fabs(0.5 - fabs(x - 0.5)) < 1e-9;
+}
+
+/* sim/ewald.c:410-510: k-vector count with the rounding-problem guard */
+int orc_kvectors(const double L[3], double *kappa, int maxk, int *kv)
+{
+  double dK = 2e-9;
+  int nagain = 0;
+again:
+  if (nagain++ > 25) return -1;
+  {
+    double Kk = SQ(*kappa), KX = L[0] * *kappa;
+    int kx, ky, kz, kxmax = (int)KX, iQ = 0;
+    for (kx = 0; kx <= kxmax; kx++) {
+      double kxq = Kk - SQ(kx / L[0]), aux = L[1] * sqrt(kxq);
+      int kymax;
+      if (almostint(aux)) { *kappa += *kappa * dK; dK *= 1.4; goto again; }
+      kymax = (int)aux;
+      for (ky = 0; ky <= kymax; ky++) {
+        double kyq = kxq - SQ(ky / L[1]);
+        int kzmax;
+        aux = L[2] * sqrt(kyq);
+        if (almostint(aux)) { *kappa += *kappa * dK; dK *= 1.4; goto again; }
+        kzmax = (int)aux;
+        for (kz = !(kx + ky); kz <= kzmax; kz++) {
+          int c = (kx > 0) + (ky > 0) + (kz > 0), m;
+          /* sign combos in the order of sim/ewpass1.c: xyz xyZ xYz xYZ */
+          int combos[4][3] = {{kx, ky, kz}, {kx, ky, -kz}, {kx, -ky, kz}, {kx, -ky, -kz}};
+          int list[4], nl = 0;
+          if (c == 3) { list[0] = 0; list[1] = 1; list[2] = 2; list[3] = 3; nl = 4; }
+          else if (c == 2) {
+            if (kz == 0) { list[0] = 0; list[1] = 2; nl = 2; }
+            else { list[0] = 0; list[1] = 1; nl = 2; }
+          } else { list[0] = 0; nl = 1; }
+          for (m = 0; m < nl; m++) {
+            if (kv && iQ < maxk) {
+              kv[3 * iQ] = combos[list[m]][0];
+              kv[3 * iQ + 1] = combos[list[m]][1];
+              kv[3 * iQ + 2] = combos[list[m]][2];
+            }
+            iQ++;
+          }
+        }
+      }
+    }
+    return iQ;
+  }
+}
+
+/* ------------------------------------------------------------ threads --- */
+
+typedef struct {
+  const orc_sys_t *s;
+  const double *r;
+  int ith, nth;
+  double *f;            /* thread-private force array (3*ns or 6*ns) */
+  double el, lj, vir, Pvir[6];
+  /* k-space */
+  int nk;
+  const int *kv;
+  double *Sre, *Sim;    /* thread-partial structure factors */
+  const double *ekk;
+  const double *gre, *gim; /* full S for pass 2 */
+  /* cells */
+  const int *cellhead, *cellnext;
+  int nc[3];
+} orc_work_t;
+
+static void run_threads(void *(*fn)(void *), orc_work_t *w, int nth)
+{
+  pthread_t th[64];
+  int i;
+  if (nth == 1) { fn(w); return; }
+  for (i = 0; i < nth; i++) pthread_create(&th[i], NULL, fn, &w[i]);
+  for (i = 0; i < nth; i++) pthread_join(th[i], NULL);
+}
+
+/* number of charges of the Ewald sums (central + Drude) */
+static int is_polar(const orc_sys_t *s) { return s->qpol != NULL; }
+
+/* -------------------------------------------------------------- r-space --- */
+
+/* one pair (cook/ljqqnp.c LJqqm, non-polar, COULOMB=-2): dr = ri - rj with
+   nearest image, rr=|dr|^2 < cutoff^2 already checked.  Adds forces to fi
+   (and -fdr to fj when fj!=NULL).  Returns f/r. */
+static void pair_np(orc_work_t *w, int i, int j, const double dr[3], double rr,
+                    double *fi, double *fj, int measure)
+{
+  const orc_sys_t *s = w->s;
+  double f = 0, U = 0, qq = s->q[i] * s->q[j], x, y, z;
+  if (s->mol[i] == s->mol[j]) {
+    /* EXCL: no LJ; exact Ewald intramolecular correction (cook/ljqqnp.c:124-144) */
+    if (qq != 0) {
+      double fe;
+      double e = orc_exacterud_sqrt(rr, s->alpha, &fe);
+      if (measure) w->el += e * qq;
+      f = fe * qq;
+    }
+  } else {
+    const orc_ss_t *ss = s->ss + s->type[i] * s->ntypes + s->type[j];
+    if (rr < ss->C2q) {
+      if (rr < ss->C1q) {
+        x = ss->Sq / rr;
+        y = x * x * x;
+        z = y * y;
+        if (measure) {
+          U += ss->E4 * (z - y);
+          f = ss->E24 * (z + z - y) * x;
+        } else
+          f = ss->E48 * y * (y - 0.5) * x;
+      } else {
+        x = rr - ss->C2q;
+        U = x * x * ss->A;
+        f = ss->A4 * x;
+      }
+      if (measure) w->vir += rr * f;
+    }
+    if (qq != 0) {
+      const double *p = s->ertab + 6 * (int)(rr * s->sgrid);
+      f += (p[4] / (p[5] + rr) + p[3]) * qq;
+      if (measure) w->el += (p[1] / (p[2] + rr) + p[0]) * qq;
+    }
+  }
+  {
+    double fx = f * dr[0], fy = f * dr[1], fz = f * dr[2];
+    fi[0] += fx; fi[1] += fy; fi[2] += fz;
+    if (fj) { fj[0] -= fx; fj[1] -= fy; fj[2] -= fz; }
+    if (measure) {
+      w->lj += U;
+      w->Pvir[0] += dr[0] * fx;
+      w->Pvir[1] += dr[1] * fy;
+      w->Pvir[2] += dr[2] * fz;
+      w->Pvir[3] += dr[2] * fy;
+      w->Pvir[4] += dr[0] * fz;
+      w->Pvir[5] += dr[1] * fx;
+    }
+  }
+}
+
+static void nearest(const double L[3], const double *ri, const double *rj, double dr[3])
+{
+  int k;
+  for (k = 0; k < 3; k++) {
+    double d = ri[k] - rj[k], Lh = 0.5 * L[k];
+    if (d < -Lh) d += L[k];
+    else if (d > Lh) d -= L[k];
+    dr[k] = d;
+  }
+}
+
+static int cell_of(const double L[3], const int nc[3], const double *r, int k)
+{
+  double x = r[k] / L[k];
+  int c;
+  x -= floor(x);
+  c = (int)(x * nc[k]);
+  if (c >= nc[k]) c = nc[k] - 1;
+  if (c < 0) c = 0;
+  return c;
+}
+
+static int g_measure;
+
+/* r-space worker: cells ≥ cutoff, half stencil over the 27 neighbours when
+   every dimension has >=3 cells, otherwise all pairs with nearest image */
+static void *rspace_worker(void *arg)
+{
+  orc_work_t *w = arg;
+  const orc_sys_t *s = w->s;
+  int ns = s->ns, measure = g_measure;
+  const double *r = w->r;
+  if (w->cellhead == NULL) {
+    int i, j;
+    for (i = w->ith; i < ns; i += w->nth)
+      for (j = i + 1; j < ns; j++) {
+        double dr[3], rr;
+        nearest(s->L, r + 3 * i, r + 3 * j, dr);
+        rr = SQ(dr[0]) + SQ(dr[1]) + SQ(dr[2]);
+        if (rr >= SQ(s->cutoff)) continue;
+        pair_np(w, i, j, dr, rr, w->f + 3 * i, w->f + 3 * j, measure);
+      }
+  } else {
+    const int *nc = w->nc;
+    int ncell = nc[0] * nc[1] * nc[2], c;
+    for (c = w->ith; c < ncell; c += w->nth) {
+      int cx = c / (nc[1] * nc[2]), cy = (c / nc[2]) % nc[1], cz = c % nc[2];
+      int d;
+      for (d = 0; d < 27; d++) {
+        int dx = d / 9 - 1, dy = (d / 3) % 3 - 1, dz = d % 3 - 1;
+        int c2 = ((cx + dx + nc[0]) % nc[0]) * nc[1] * nc[2] +
+                 ((cy + dy + nc[1]) % nc[1]) * nc[2] + ((cz + dz + nc[2]) % nc[2]);
+        int i, j;
+        if (c2 < c) continue; /* half stencil: each unordered cell pair once */
+        for (i = w->cellhead[c]; i >= 0; i = w->cellnext[i])
+          for (j = w->cellhead[c2]; j >= 0; j = w->cellnext[j]) {
+            double dr[3], rr;
+            if (c2 == c && j <= i) continue;
+            nearest(s->L, r + 3 * i, r + 3 * j, dr);
+            rr = SQ(dr[0]) + SQ(dr[1]) + SQ(dr[2]);
+            if (rr >= SQ(s->cutoff)) continue;
+            pair_np(w, i, j, dr, rr, w->f + 3 * i, w->f + 3 * j, measure);
+          }
+      }
+    }
+  }
+  return NULL;
+}
+
+/* -------------------------------------------------------------- k-space --- */
+
+/* charge list: non-polar = sites with q != 0 (order of sim/ewald.c:632-690) */
+typedef struct { int site; double q; int drude; } qitem_t;
+
+static qitem_t *g_qlist;
+static int g_nq;
+
+static void charge_pos(const orc_sys_t *s, const double *r, const qitem_t *it, double p[3])
+{
+  int k;
+  for (k = 0; k < 3; k++) {
+    p[k] = r[3 * it->site + k];
+    if (it->drude) p[k] += r[3 * s->ns + 3 * it->site + k];
+  }
+}
+
+/* powers e^{2 pi i n x/L} for n = -nmax..nmax by incremental complex
+   products, as the reference builds its per-charge factors (sim/ewald.c:632-690,
+   sim/ewpass1.c: CxE/CxiE recurrences) */
+static void phase_powers(double x, double L, int nmax, double *pre, double *pim)
+{
+  double er = cos(2 * M_PI / L * x), ei = sin(2 * M_PI / L * x);
+  int n;
+  pre[nmax] = 1; pim[nmax] = 0;
+  for (n = 1; n <= nmax; n++) {
+    double a = pre[nmax + n - 1], b = pim[nmax + n - 1];
+    pre[nmax + n] = a * er - b * ei;
+    pim[nmax + n] = a * ei + b * er;
+    pre[nmax - n] = pre[nmax + n];
+    pim[nmax - n] = -pim[nmax + n];
+  }
+}
+
+static int g_kmax[3];
+
+/* q e^{2 pi i k.r/L} of charge j for every k-vector */
+static void charge_phases(const orc_sys_t *s, const double *r, const qitem_t *it,
+                          int nk, const int *kv, double *xr, double *xi)
+{
+  double p[3];
+  double *pw[3][2];
+  int d, m;
+  charge_pos(s, r, it, p);
+  for (d = 0; d < 3; d++) {
+    pw[d][0] = malloc(sizeof(double) * (2 * g_kmax[d] + 1));
+    pw[d][1] = malloc(sizeof(double) * (2 * g_kmax[d] + 1));
+    phase_powers(p[d], s->L[d], g_kmax[d], pw[d][0], pw[d][1]);
+  }
+  for (m = 0; m < nk; m++) {
+    const int *k = kv + 3 * m;
+    int a = k[0] + g_kmax[0], b = k[1] + g_kmax[1], c = k[2] + g_kmax[2];
+    double ar = pw[0][0][a], ai = pw[0][1][a], br = pw[1][0][b], bi = pw[1][1][b];
+    double xyr = ar * br - ai * bi, xyi = ar * bi + ai * br;
+    double cr = pw[2][0][c], ci = pw[2][1][c];
+    xr[m] = it->q * (xyr * cr - xyi * ci);
+    xi[m] = it->q * (xyr * ci + xyi * cr);
+  }
+  for (d = 0; d < 3; d++) { free(pw[d][0]); free(pw[d][1]); }
+}
+
+/* pass 1 (sim/ewpass1.c): S(k) = sum_j q_j exp(2 pi i k.r_j/L); each
+   thread sums a slice of the charges (sim/ewald.c:197-243 PARALLEL==1) */
+static void *kspace1_worker(void *arg)
+{
+  orc_work_t *w = arg;
+  int j0 = g_nq * w->ith / w->nth, j1 = g_nq * (w->ith + 1) / w->nth, j, m;
+  double *xr = malloc(sizeof(double) * (w->nk + 1)), *xi = malloc(sizeof(double) * (w->nk + 1));
+  for (j = j0; j < j1; j++) {
+    charge_phases(w->s, w->r, g_qlist + j, w->nk, w->kv, xr, xi);
+    for (m = 0; m < w->nk; m++) { w->Sre[m] += xr[m]; w->Sim[m] += xi[m]; }
+  }
+  free(xr); free(xi);
+  return NULL;
+}
+
+/* pass 2 (sim/ewpass2m.c + sim/ewaldf.c): F_j += ekk k/L Im(conj(S) q e^{ikr}) */
+static void *kspace2_worker(void *arg)
+{
+  orc_work_t *w = arg;
+  const orc_sys_t *s = w->s;
+  int j0 = g_nq * w->ith / w->nth, j1 = g_nq * (w->ith + 1) / w->nth, j, m;
+  double *xr = malloc(sizeof(double) * (w->nk + 1)), *xi = malloc(sizeof(double) * (w->nk + 1));
+  for (j = j0; j < j1; j++) {
+    double F[3] = {0, 0, 0};
+    const qitem_t *it = g_qlist + j;
+    double *fo = w->f + (it->drude ? 3 * s->ns : 0) + 3 * it->site;
+    charge_phases(s, w->r, it, w->nk, w->kv, xr, xi);
+    for (m = 0; m < w->nk; m++) {
+      const int *k = w->kv + 3 * m;
+      double FA = w->gre[m] * xi[m] - w->gim[m] * xr[m], e = w->ekk[m];
+      F[0] += e * (k[0] / s->L[0]) * FA;
+      F[1] += e * (k[1] / s->L[1]) * FA;
+      F[2] += e * (k[2] / s->L[2]) * FA;
+    }
+    fo[0] += F[0]; fo[1] += F[1]; fo[2] += F[2];
+  }
+  free(xr); free(xi);
+  return NULL;
+}
+
+/* ---------------------------------------------------------- orc_forces --- */
+
+int orc_forces(const orc_sys_t *s, const double *r, double *f, orc_en_t *en, int nthreads)
+{
+  int ns = s->ns, nf = is_polar(s) ? 6 * ns : 3 * ns, t, i, m;
+  int measure = en != NULL;
+  orc_work_t *w;
+  int *kv, nk, nc[3], usecells = 1;
+  double kappa = s->kappa, V = s->L[0] * s->L[1] * s->L[2];
+  double Energy = 0, PVIR[6] = {0, 0, 0, 0, 0, 0}, M[3] = {0, 0, 0}, sumq = 0;
+  double *Sre, *Sim, *ekk;
+  int *cellhead = NULL, *cellnext = NULL;
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 64) nthreads = 64;
+  g_measure = measure;
+  memset(f, 0, sizeof(double) * nf);
+  w = calloc(nthreads, sizeof(orc_work_t));
+
+  /* charges in the order of the reference qtab */
+  g_qlist = malloc(sizeof(qitem_t) * 2 * ns);
+  g_nq = 0;
+  for (i = 0; i < ns; i++) {
+    if (s->q[i] != 0) { g_qlist[g_nq].site = i; g_qlist[g_nq].q = s->q[i]; g_qlist[g_nq].drude = 0; g_nq++; }
+    if (is_polar(s) && s->qpol[i] != 0) {
+      g_qlist[g_nq].site = i; g_qlist[g_nq].q = s->qpol[i]; g_qlist[g_nq].drude = 1; g_nq++;
+    }
+    /* self term uses the total charge of the site (sim/ewald.c:395-410) */
+    sumq += SQ(s->q[i] + (is_polar(s) ? s->qpol[i] : 0));
+  }
+
+  /* cells for the r-space sum */
+  for (m = 0; m < 3; m++) {
+    nc[m] = (int)(s->L[m] / s->cutoff);
+    if (nc[m] < 3) usecells = 0;
+  }
+  if (is_polar(s)) usecells = 0; /* polar pair path uses all pairs (see orc_polar.c) */
+  if (usecells) {
+    int ncell = nc[0] * nc[1] * nc[2];
+    cellhead = malloc(sizeof(int) * ncell);
+    cellnext = malloc(sizeof(int) * ns);
+    for (i = 0; i < ncell; i++) cellhead[i] = -1;
+    for (i = ns - 1; i >= 0; i--) {
+      int c = (cell_of(s->L, nc, r + 3 * i, 0) * nc[1] + cell_of(s->L, nc, r + 3 * i, 1)) * nc[2] +
+              cell_of(s->L, nc, r + 3 * i, 2);
+      cellnext[i] = cellhead[c];
+      cellhead[c] = i;
+    }
+  }
+
+  /* k-vectors (count + list), ekk (sim/ewald.c:565-600) */
+  nk = orc_kvectors(s->L, &kappa, 0, NULL);
+  kv = malloc(sizeof(int) * 3 * (nk > 0 ? nk : 1));
+  kappa = s->kappa;
+  orc_kvectors(s->L, &kappa, nk, kv);
+  ekk = malloc(sizeof(double) * (nk + 1));
+  g_kmax[0] = g_kmax[1] = g_kmax[2] = 0;
+  for (m = 0; m < nk; m++) {
+    int d;
+    for (d = 0; d < 3; d++)
+      if (abs(kv[3 * m + d]) > g_kmax[d]) g_kmax[d] = abs(kv[3 * m + d]);
+  }
+  Sre = calloc(nk + 1, sizeof(double));
+  Sim = calloc(nk + 1, sizeof(double));
+  {
+    double PIaq = -SQ(M_PI / s->alpha);
+    for (m = 0; m < nk; m++) {
+      double kk = SQ(kv[3 * m + 2] / s->L[2]) + (SQ(kv[3 * m + 1] / s->L[1]) + SQ(kv[3 * m] / s->L[0]));
+      ekk[m] = 4 / (kk * V) * exp(PIaq * kk);
+    }
+  }
+
+  for (t = 0; t < nthreads; t++) {
+    w[t].s = s; w[t].r = r; w[t].ith = t; w[t].nth = nthreads;
+    w[t].f = calloc(nf, sizeof(double));
+    w[t].nk = nk; w[t].kv = kv; w[t].ekk = ekk;
+    w[t].Sre = calloc(nk + 1, sizeof(double));
+    w[t].Sim = calloc(nk + 1, sizeof(double));
+    w[t].cellhead = cellhead; w[t].cellnext = cellnext;
+    memcpy(w[t].nc, nc, sizeof(nc));
+  }
+
+  /* Ewald pass 1 */
+  run_threads(kspace1_worker, w, nthreads);
+  for (t = 0; t < nthreads; t++)
+    for (m = 0; m < nk; m++) { Sre[m] += w[t].Sre[m]; Sim[m] += w[t].Sim[m]; }
+  for (t = 0; t < nthreads; t++) { w[t].gre = Sre; w[t].gim = Sim; }
+
+  /* pass 2 energy and k-space virial (sim/ewpass2m.c measure branch) */
+  if (measure) {
+    double PIaq = -SQ(M_PI / s->alpha);
+    for (m = 0; m < nk; m++) {
+      double kx = kv[3 * m] / s->L[0], ky = kv[3 * m + 1] / s->L[1], kz = kv[3 * m + 2] / s->L[2];
+      double kk = SQ(kx) + SQ(ky) + SQ(kz), E1 = (SQ(Sre[m]) + SQ(Sim[m])) * ekk[m];
+      double ptf = 1 / kk - PIaq;
+      Energy += E1;
+      PVIR[0] += E1 * ptf * SQ(kx);
+      PVIR[1] += E1 * ptf * SQ(ky);
+      PVIR[2] += E1 * ptf * SQ(kz);
+      PVIR[3] += E1 * ptf * ky * kz;
+      PVIR[4] += E1 * ptf * kx * kz;
+      PVIR[5] += E1 * ptf * kx * ky;
+    }
+    Energy /= 4 * M_PI;
+  }
+  run_threads(kspace2_worker, w, nthreads);
+
+  /* r-space */
+  run_threads(rspace_worker, w, nthreads);
+
+  for (t = 0; t < nthreads; t++)
+    for (i = 0; i < nf; i++) f[i] += w[t].f[i];
+
+  /* dipole (epsinf) term and forces, sim/ewald.c:865-887 + sim/ewaldf.c */
+  {
+    double c, ek[3], Edip;
+    for (i = 0; i < g_nq; i++) {
+      double p[3];
+      charge_pos(s, r, g_qlist + i, p);
+      for (m = 0; m < 3; m++) M[m] += g_qlist[i].q * p[m];
+    }
+    c = 4 * M_PI / (2 * s->epsinf + 1) / V;
+    for (m = 0; m < 3; m++) ek[m] = -c * M[m];
+    Edip = c / 2 * (SQ(M[0]) + SQ(M[1]) + SQ(M[2]));
+    for (i = 0; i < g_nq; i++) {
+      const qitem_t *it = g_qlist + i;
+      double *fo = f + (it->drude ? 3 * ns : 0) + 3 * it->site, p[3];
+      for (m = 0; m < 3; m++) fo[m] += it->q * ek[m];
+      if (measure) {
+        charge_pos(s, r, it, p);
+        /* aux*ek*R (diagonal) and off-diagonal terms of ewaldf ADDFORCES */
+        w[0].Pvir[0] += it->q * ek[0] * p[0];
+        w[0].Pvir[1] += it->q * ek[1] * p[1];
+        w[0].Pvir[2] += it->q * ek[2] * p[2];
+        w[0].Pvir[3] += it->q * ek[1] * p[2];
+        w[0].Pvir[4] += it->q * ek[2] * p[0];
+        w[0].Pvir[5] += it->q * ek[0] * p[1];
+      }
+    }
+    if (measure) {
+      double el = 0, lj = 0, vir = 0, Pv[6] = {0, 0, 0, 0, 0, 0};
+      memset(en, 0, sizeof(*en));
+      for (t = 0; t < nthreads; t++) {
+        el += w[t].el; lj += w[t].lj; vir += w[t].vir;
+        for (m = 0; m < 6; m++) Pv[m] += w[t].Pvir[m];
+      }
+      en->er = el;
+      en->ek = Energy;
+      en->eself = -s->alpha / SQRTPI * sumq;
+      en->edip = Edip;
+      en->el = Energy - s->alpha / SQRTPI * sumq + Edip + el;
+      en->lj = lj;
+      en->vir = vir;
+      /* k-space tensor: +Energy on the diagonal, -2/(4 pi) PVIR (sim/ewald.c:852-856) */
+      for (m = 0; m < 3; m++) Pv[m] += Energy + Edip;
+      for (m = 0; m < 6; m++) Pv[m] -= 2 / (4 * M_PI) * PVIR[m];
+      memcpy(en->Pvir, Pv, sizeof(Pv));
+    }
+  }
+
+  for (t = 0; t < nthreads; t++) { free(w[t].f); free(w[t].Sre); free(w[t].Sim); }
+  free(w); free(kv); free(ekk); free(Sre); free(Sim); free(g_qlist);
+  free(cellhead); free(cellnext);
+  return 0;
+}
+
+/* ---------------------------------------------------------------- SHAKE --- */
+
+/* sim/constrd.c:767-839 (SHAKE=1 sweeps) with sim/verlet.c:101-104 (no
+   thermostat) and the VERLET=3 kinetic energy of sim/shakev3.c */
+int orc_shake_step(int ns, double *r, double *r1, const double *f, const double *mass,
+                   int nmol, const int *mol_first, const int *mol_nc, const int *cfirst,
+                   const int *ci, const int *cj, const double *bondq,
+                   double h, double eps, double omega, int maxit, double *ekin)
+{
+  double hh = h * h, kin = 0;
+  int n, worst = 0;
+  double *p = malloc(sizeof(double) * 3 * ns);
+  for (n = 0; n < nmol; n++) {
+    int i0 = mol_first[n], i1 = mol_first[n + 1], i, k, it = 0, al;
+    int c0 = cfirst[n], nc = mol_nc[n];
+    double maxsq;
+    for (i = i0; i < i1; i++)
+      for (k = 0; k < 3; k++)
+        p[3 * i + k] = f[3 * i + k] * (hh / mass[i]) + r[3 * i + k] + r1[3 * i + k];
+    if (nc > 0) {
+      do {
+        it++;
+        maxsq = 0;
+        for (al = c0; al < c0 + nc; al++) {
+          int a = ci[al], b = cj[al];
+          double pij[3], rij[3], sq = bondq[al], mi = 1 / mass[a], mj = 1 / mass[b];
+          for (k = 0; k < 3; k++) pij[k] = p[3 * a + k] - p[3 * b + k];
+          sq -= SQ(pij[0]) + SQ(pij[1]) + SQ(pij[2]);
+          if (fabs(sq / bondq[al]) > maxsq) maxsq = fabs(sq / bondq[al]);
+          for (k = 0; k < 3; k++) rij[k] = r[3 * a + k] - r[3 * b + k];
+          sq *= omega / (mi + mj);
+          sq /= bondq[al];
+          for (k = 0; k < 3; k++) {
+            rij[k] *= sq;
+            p[3 * a + k] += mi * rij[k];
+            p[3 * b + k] -= mj * rij[k];
+          }
+        }
+      } while (maxsq > eps && it < maxit);
+      if (it >= maxit && maxsq > eps) { free(p); return -1; }
+    }
+    if (it > worst) worst = it;
+    for (i = i0; i < i1; i++) {
+      double V2[3], V1[3];
+      for (k = 0; k < 3; k++) {
+        V1[k] = r1[3 * i + k];
+        V2[k] = p[3 * i + k] - r[3 * i + k];
+      }
+      kin += (SQ(V1[0]) + SQ(V1[1]) + SQ(V1[2]) + SQ(V2[0]) + SQ(V2[1]) + SQ(V2[2])) * mass[i];
+      for (k = 0; k < 3; k++) { r1[3 * i + k] = V2[k]; r[3 * i + k] = p[3 * i + k]; }
+    }
+  }
+  free(p);
+  if (ekin) *ekin = kin / hh / 4;
+  return worst;
+}

@@ -1,0 +1,172 @@
+"""ctypes access to the CPU oracle ``libcookoracle.so`` (TEST INFRASTRUCTURE).
+
+Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this module, as the checker.  The product path never does.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libcookoracle.so")
+
+
+class SS(C.Structure):
+    _fields_ = [(n, C.c_double) for n in
+                ("C1q", "C2q", "A", "A4", "Sq", "E4", "E24", "E48", "corr", "eps", "sig")]
+
+
+class EN(C.Structure):
+    _fields_ = [("el", C.c_double), ("lj", C.c_double), ("vir", C.c_double),
+                ("Pvir", C.c_double * 6), ("ek", C.c_double), ("er", C.c_double),
+                ("eself", C.c_double), ("edip", C.c_double), ("self", C.c_double)]
+
+    def asdict(self):
+        return dict(el=self.el, lj=self.lj, vir=self.vir, Pvir=list(self.Pvir), ek=self.ek,
+                    er=self.er, eself=self.eself, edip=self.edip, self=self.self)
+
+
+class SYS(C.Structure):
+    _fields_ = [("ns", C.c_int), ("type", C.POINTER(C.c_int)), ("q", C.POINTER(C.c_double)),
+                ("mol", C.POINTER(C.c_int)), ("ntypes", C.c_int), ("ss", C.POINTER(SS)),
+                ("L", C.c_double * 3), ("cutoff", C.c_double), ("alpha", C.c_double),
+                ("kappa", C.c_double), ("epsinf", C.c_double), ("ertab", C.POINTER(C.c_double)),
+                ("ntab", C.c_int), ("sgrid", C.c_double), ("qpol", C.POINTER(C.c_double)),
+                ("alphaqq", C.POINTER(C.c_double))]
+
+
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = C.CDLL(LIB)
+        dp = C.POINTER(C.c_double)
+        ip = C.POINTER(C.c_int)
+        L.orc_setss.argtypes = [C.c_double, C.c_double, C.c_double, C.POINTER(SS)]
+        L.orc_combrule.argtypes = [C.c_double] * 6 + [C.c_int, dp, dp]
+        L.orc_erfc_ntab.argtypes = [C.c_int, C.c_double, C.c_double]
+        L.orc_erfc_build.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, dp, dp]
+        L.orc_eru.argtypes = [dp, C.c_double, C.c_double]
+        L.orc_eru.restype = C.c_double
+        L.orc_erd.argtypes = [dp, C.c_double, C.c_double]
+        L.orc_erd.restype = C.c_double
+        L.orc_exacterud_sqrt.argtypes = [C.c_double, C.c_double, dp]
+        L.orc_exacterud_sqrt.restype = C.c_double
+        L.orc_kvectors.argtypes = [dp, dp, C.c_int, ip]
+        L.orc_forces.argtypes = [C.POINTER(SYS), dp, dp, C.POINTER(EN), C.c_int]
+        L.orc_shake_step.argtypes = [C.c_int, dp, dp, dp, dp, C.c_int, ip, ip, ip, ip, ip, dp,
+                                     C.c_double, C.c_double, C.c_double, C.c_int, dp]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def pair_tables(system, C2):
+    """per type pair setss constants (combining rule + smoothing)"""
+    L = lib()
+    nt = len(system.typeE)
+    ss = (SS * (nt * nt))()
+    for a in range(nt):
+        for b in range(nt):
+            eps, sig = C.c_double(), C.c_double()
+            L.orc_combrule(system.typeE[a], system.typeR[a], system.typeA[a],
+                           system.typeE[b], system.typeR[b], system.typeA[b],
+                           system.comb_rule, C.byref(eps), C.byref(sig))
+            rc = L.orc_setss(eps.value, sig.value, C2, C.byref(ss[a * nt + b]))
+            if rc != 0:
+                raise ValueError("setss failed for types %d,%d" % (a, b))
+    return ss
+
+
+def kvectors(Lbox, kappa):
+    L = lib()
+    Lb = np.ascontiguousarray(Lbox, dtype=np.float64)
+    kap = C.c_double(kappa)
+    n = L.orc_kvectors(_dp(Lb), C.byref(kap), 0, None)
+    kv = np.zeros((n, 3), np.int32)
+    kap = C.c_double(kappa)
+    L.orc_kvectors(_dp(Lb), C.byref(kap), n, _ip(kv))
+    return kv, kap.value
+
+
+class Oracle:
+    """The oracle's view of one system + Ewald parameters."""
+
+    def __init__(self, system, Lbox, cutoff, alpha, kappa, LJcutoff=None, grid=256,
+                 rshift=3, rplus=2.5, epsinf=3e33):
+        L = lib()
+        self.system = system
+        self.L = np.array(Lbox, dtype=np.float64)
+        self.ss = pair_tables(system, LJcutoff if LJcutoff else cutoff)
+        ntab = L.orc_erfc_ntab(grid, cutoff + rplus, alpha)
+        self.tab = np.zeros(6 * ntab)
+        sg = C.c_double()
+        L.orc_erfc_build(grid, cutoff + rplus, cutoff, alpha, rshift, _dp(self.tab), C.byref(sg))
+        self.kv, self.kappa = kvectors(self.L, kappa)
+        self.type = np.ascontiguousarray(system.type, np.int32)
+        self.q = np.ascontiguousarray(system.q, np.float64)
+        self.mol = np.ascontiguousarray(system.mol, np.int32)
+        s = SYS()
+        s.ns = system.ns
+        s.type = _ip(self.type)
+        s.q = _dp(self.q)
+        s.mol = _ip(self.mol)
+        s.ntypes = len(system.typeE)
+        s.ss = self.ss
+        for k in range(3):
+            s.L[k] = self.L[k]
+        s.cutoff = cutoff
+        s.alpha = alpha
+        s.kappa = self.kappa
+        s.epsinf = epsinf
+        s.ertab = _dp(self.tab)
+        s.ntab = ntab
+        s.sgrid = sg.value
+        s.qpol = None
+        s.alphaqq = None
+        self.sys = s
+        self.sgrid = sg.value
+        self.ntab = ntab
+
+    def forces(self, r, measure=True, nthreads=1):
+        r = np.ascontiguousarray(r, dtype=np.float64).reshape(-1)
+        f = np.zeros_like(r)
+        en = EN()
+        lib().orc_forces(C.byref(self.sys), _dp(r), _dp(f), C.byref(en) if measure else None,
+                         nthreads)
+        return f.reshape(-1, 3), (en.asdict() if measure else None)
+
+    def shake_step(self, r, r1, f, h, eps=1e-10, omega=0.6, maxit=1000):
+        s = self.system
+        r = np.ascontiguousarray(r, dtype=np.float64).copy().reshape(-1)
+        r1 = np.ascontiguousarray(r1, dtype=np.float64).copy().reshape(-1)
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+        mass = np.ascontiguousarray(s.mass, np.float64)
+        mfirst = np.ascontiguousarray(s.mol_first, np.int32)
+        cfirst = np.ascontiguousarray(s.mol_cfirst, np.int32)
+        nc = np.ascontiguousarray(np.diff(s.mol_cfirst), np.int32)
+        ci = np.ascontiguousarray(s.cons[:, 0], np.int32)
+        cj = np.ascontiguousarray(s.cons[:, 1], np.int32)
+        bq = np.ascontiguousarray(s.cons_len ** 2, np.float64)
+        ek = C.c_double()
+        it = lib().orc_shake_step(s.ns, _dp(r), _dp(r1), _dp(f), _dp(mass), s.nmol, _ip(mfirst),
+                                  _ip(nc), _ip(cfirst), _ip(ci), _ip(cj), _dp(bq), h, eps,
+                                  omega, maxit, C.byref(ek))
+        return r.reshape(-1, 3), r1.reshape(-1, 3), it, ek.value

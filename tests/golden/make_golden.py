@@ -1,0 +1,138 @@
+"""Generate the golden parity fixtures by running the reference MACSIMUS `cook`.
+
+This script is test infrastructure.  It needs the reference binaries built by
+``oracle/build_ref.sh`` (they are compiled from the reference sources into
+``oracle/_ref/``), writes hand-made force-field (.ble), parameter (.def) and
+run (.get) files into a scratch directory, runs cook with ``-v128`` (every
+``forces()`` call dumps ``r q f`` per site, sim/simils.c:2259 ``dumpall``)
+and stores the dumps as compact ``.npz`` fixtures next to this file.
+
+Reference input formats followed here: force-field tables as parsed by
+cook/simdef.c:500-1000 (``readblend``), run data as parsed by
+sim/mainget.c:67-256.  Units are cook program units: K, Angstrom, ps, charge
+unit = e/408.779826922048 (sim/units.h:101-108); masses in g/mol in the .ble.
+
+usage: python tests/golden/make_golden.py [case ...]
+"""
+import json
+import os
+import re
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REFBIN = os.path.join(REPO, "oracle", "_ref")
+
+sys.path.insert(0, REPO)
+from macsimus_gb300.forcefield import ble_text  # noqa: E402
+
+
+CASES = {
+    # 216 SPC/E waters, cutoff 9 A, alpha 0.35/A, |n|<=6
+    "spce216": dict(binary="cookew", species=["WAT"], N=[216], L=18.6206,
+                    cutoff=9.0, alpha=0.35, kn=6, steps=3, h=0.002, epsc=1e-10),
+    # the 864 SPC/E configuration: L=29.65 A, cutoff 12, alpha 0.26, |n|<=8
+    "spce864": dict(binary="cookew", species=["WAT"], N=[864], L=29.65,
+                    cutoff=12.0, alpha=0.26, kn=8, steps=2, h=0.002, epsc=1e-10),
+    # small brine: 500 SPC/E + 16 Na+ + 16 Cl-, cutoff 10, alpha 0.31, |n|<=7
+    "brine532": dict(binary="cookew", species=["WAT", "NA", "CL"], N=[500, 16, 16],
+                     L=24.97, cutoff=10.0, alpha=0.31, kn=7, steps=2, h=0.002,
+                     epsc=1e-10),
+}
+
+
+def def_text(c):
+    lines = []
+    for i, n in enumerate(c["N"]):
+        lines.append("N[%d]=%d" % (i, n))
+    L = c["L"]
+    lines += ["L[0]=%.10g L[1]=%.10g L[2]=%.10g" % (L, L, L),
+              "cutoff=%.10g LJcutoff=%.10g" % (c["cutoff"], c["cutoff"]),
+              "noint=1", "h=%.10g" % c["h"], "T=298",
+              "el.test=0 el.alpha=%.10g el.kappa=%.12g" % (c["alpha"], (c["kn"] + 1e-6) / L),
+              "epsc=%.3g" % c["epsc"], "corr=0", ";", ""]
+    return "\n".join(lines)
+
+
+def get_text(c):
+    return 'init="crystal"\nno=%d\n;\n' % c["steps"]
+
+
+def parse_dump(path):
+    with open(path) as f:
+        head = f.readline().split()
+        ns = int(head[0])
+        L = [float(x) for x in f.readline().split()[:3]]
+        rows = []
+        for _ in range(ns):
+            t = f.readline().split()
+            rows.append([float(x) for x in t[:7]] + [int(t[7]), int(t[8])])
+    a = np.array(rows)
+    return dict(L=np.array(L), r=a[:, 0:3], q=a[:, 3], f=a[:, 4:7],
+                mol=a[:, 7].astype(np.int32), site=a[:, 8].astype(np.int32))
+
+
+def run_case(name, c, keep=None):
+    binary = os.path.join(REFBIN, c["binary"])
+    if not os.path.exists(binary):
+        raise SystemExit("missing %s: run oracle/build_ref.sh first" % binary)
+    wd = keep or tempfile.mkdtemp(prefix="golden_")
+    os.makedirs(wd, exist_ok=True)
+    with open(os.path.join(wd, "ff.ble"), "w") as f:
+        f.write(ble_text(c["species"]))
+    with open(os.path.join(wd, "sim.def"), "w") as f:
+        f.write(def_text(c))
+    with open(os.path.join(wd, "sim.get"), "w") as f:
+        f.write(get_text(c))
+    p = subprocess.run([binary, "ff.ble", "sim", "-v128"], cwd=wd,
+                       stdin=subprocess.DEVNULL, capture_output=True, text=True, timeout=600)
+    if p.returncode != 0:
+        raise SystemExit("%s failed:\n%s" % (name, p.stdout[-3000:]))
+    prt = open(os.path.join(wd, "sim.prt")).read()
+    dumps = []
+    i = 0
+    while os.path.exists(os.path.join(wd, "sim.%d.dump" % i)):
+        dumps.append(parse_dump(os.path.join(wd, "sim.%d.dump" % i)))
+        i += 1
+    m = re.findall(r"En\.pot=(\S+) En\.kin=(\S+) En\.tot=(\S+)", prt)
+    m2 = re.search(r"Q->N=(\d+)", prt)
+    m3 = re.search(r"omegac=(\S+) \(optimized\)", prt)
+    meta = dict(case=name, params=c, ndumps=len(dumps),
+                Epot_last=float(m[-1][0]), Ekin_last=float(m[-1][1]), Etot_last=float(m[-1][2]),
+                QN=int(m2.group(1)) if m2 else None,
+                omegac=float(m3.group(1)) if m3 else None,
+                species=c["species"], N=c["N"])
+    if keep is None:
+        shutil.rmtree(wd)
+    return dumps, meta
+
+
+def save_case(name, dumps, meta):
+    arrays = {}
+    d0 = dumps[0]
+    arrays["q"] = d0["q"]
+    arrays["mol"] = d0["mol"]
+    arrays["site"] = d0["site"]
+    arrays["L"] = d0["L"]
+    arrays["r"] = np.stack([d["r"] for d in dumps])
+    arrays["f"] = np.stack([d["f"] for d in dumps])
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+    with open(os.path.join(HERE, name + ".json"), "w") as f:
+        json.dump(meta, f, indent=1, sort_keys=True)
+    print("wrote %s: %d dumps, %d sites" % (name, len(dumps), len(d0["q"])))
+
+
+def main(argv):
+    names = argv or list(CASES)
+    for n in names:
+        dumps, meta = run_case(n, CASES[n])
+        save_case(n, dumps, meta)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])
