@@ -1,0 +1,339 @@
+"""Benchmark of the GB300 cook force path (one JSON line on rank 0).
+
+A step is one MD step of the workload (linked-cell LJ + Ewald r-space sum,
+classical Ewald k-space sum, leap-frog + SHAKE) with the coordinates resident
+on the device.  The headline is the mixed-precision path (FP32 arithmetic,
+FP64 accumulation); the plain FP64 path runs the same steps for the ratio.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs under torchrun: independent replicas (the path does not shard),
+one box per GPU, barrier + max-over-ranks time, value = total over ranks.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "ns/day & atom-steps/s, mixed vs plain FP64 GPU path at force RMS err ≤1e-5"
+WORKLOAD = "spce32768"
+FLOP_PER_PAIR = 45          # FP32 flops per in-cutoff (half) pair
+FLOP_PER_KQ = 8             # flops per (k-vector, charge) per Ewald pass
+
+
+def env_rank():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+# ------------------------------------------------------------------ clocks --
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms (background)"""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = str(gpu_index)
+        self.proc = None
+        self.path = tempfile.mktemp(prefix="clocks_", suffix=".csv")
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", self.gpu, "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        if self.proc is None:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if p[5 + k].lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if sm:
+            out = {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                   "reasons": sorted(reasons), "samples": len(sm)}
+        return out
+
+
+# ------------------------------------------------------------ CPU baseline --
+
+def cpu_md_steps(w, nsteps_max, budget_s, nthreads):
+    """the oracle port (C, pthreads) on the host cores: MD steps of the workload"""
+    from oracle import oracle as O
+    orc = O.Oracle(w["system"], [w["L"]] * 3, w["cutoff"], w["alpha"], w["kappa"])
+    r, r1 = w["r"].copy(), w["r1"].copy()
+    t0 = time.perf_counter()
+    done = 0
+    while done < nsteps_max:
+        f, _ = orc.forces(r, measure=False, nthreads=nthreads)
+        r, r1, it, _ = orc.shake_step(r, r1, f, w["h"], eps=1e-7, omega=0.6)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    return done, time.perf_counter() - t0
+
+
+def ns_per_day(h_ps, steps, seconds):
+    return 86.4 * h_ps * steps / seconds
+
+
+# ---------------------------------------------------------------- our arm --
+
+def run_ours(args, rank, world, local):
+    import torch
+    import torch.distributed as dist
+    import macsimus_gb300 as M
+    from macsimus_gb300 import configs
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    w = configs.workload(args.workload, seed=1000 + rank)
+    system = w["system"]
+    ns = system.ns
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    fp = M.ForcePath(system, [w["L"]] * 3, w["cutoff"], w["alpha"], w["kappa"], precision="mixed",
+                     h=w["h"], epsc=1e-7)
+    fp.set_stream(stream.cuda_stream)
+    # accuracy of the mixed path against the FP64 path on the same input
+    f64 = M.ForcePath(system, [w["L"]] * 3, w["cutoff"], w["alpha"], w["kappa"],
+                      precision="fp64", h=w["h"], epsc=1e-7)
+    f64.set_stream(stream.cuda_stream)
+    fm, _ = fp.forces(w["r"])
+    fd, _ = f64.forces(w["r"])
+    force_err = float(np.sqrt(((fm - fd) ** 2).sum() / (fd ** 2).sum()))
+
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def timed_steps(path, k, warm, profile=False):
+        path.md_set_state(w["r"], w["r1"])
+        for _ in range(warm):
+            path.md_steps(1, measure=False)
+        barrier()
+        path.profile(profile)
+        path.profile_reset()
+        launches = 0
+        total_ms = 0.0
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        for _ in range(k):
+            flush.fill_(1)          # L2 flushed between timed steps (outside the events)
+            e0.record(stream)
+            path.md_steps(1, measure=False)
+            e1.record(stream)
+            e1.synchronize()
+            total_ms += e0.elapsed_time(e1)
+            launches += path.launches
+        barrier()
+        prof = path.profile_read() if profile else {}
+        path.profile(False)
+        return total_ms, launches, prof
+
+    gpu_index = local
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if vis:
+        try:
+            gpu_index = int(vis.split(",")[local])
+        except ValueError:
+            pass
+    clocks = ClockSampler(gpu_index)
+    clocks.start()
+    total_ms, launches, prof = timed_steps(fp, args.steps, args.warmup, profile=True)
+    clk = clocks.stop()
+    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    total_ms = float(t.item())
+    ms_step = total_ms / args.steps
+    value = world * ns_per_day(w["h"], args.steps, total_ms * 1e-3)
+    atom_steps = world * ns * args.steps / (total_ms * 1e-3)
+
+    # plain FP64 path, same workload (fewer steps: it is ~2 orders slower)
+    k64 = max(1, min(args.steps, args.fp64_steps))
+    ms64, _, _ = timed_steps(f64, k64, 1)
+    t = torch.tensor([ms64], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    value64 = world * ns_per_day(w["h"], k64, float(t.item()) * 1e-3)
+
+    # end to end through the C ABI with pinned host buffers: every step copies
+    # r, r1 in, runs the step, and reads r, r1 and the energies back
+    rh = torch.from_numpy(w["r"].reshape(-1).copy()).pin_memory().numpy()
+    r1h = torch.from_numpy(w["r1"].reshape(-1).copy()).pin_memory().numpy()
+    ke2e = max(3, min(args.steps, 50))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(ke2e):
+        fp.md_set_state(rh, r1h)
+        fp.md_steps(1, measure=True)
+        rr, rr1 = fp.md_get_state()
+        rh[:] = rr.reshape(-1)
+        r1h[:] = rr1.reshape(-1)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    e2e = world * ns_per_day(w["h"], ke2e, float(t.item()))
+
+    # roofline of the dominant kernel (FP32 pipe: no tensor-core contraction here)
+    peak = M.fp32_peak_tflops()
+    nq = int((system.q != 0).sum())
+    V = w["L"] ** 3
+    npairs = ns * (ns - 1) / 2 * (4.0 / 3.0 * math.pi * w["cutoff"] ** 3) / V
+    algo = {"ewald_sk": FLOP_PER_KQ * fp.nkvec * nq, "ewald_kforce": FLOP_PER_KQ * fp.nkvec * nq,
+            "pair_mixed": FLOP_PER_PAIR * npairs}
+    top = max(prof.items(), key=lambda kv: kv[1][0]) if prof else ("none", (0, 1))
+    name, (kms, kcnt) = top
+    kavg = kms / max(kcnt, 1)
+    achieved = algo.get(name, 0) / (kavg * 1e-3) / 1e12 if kavg > 0 else 0.0
+    traffic = None
+    tpath = os.path.join(REPO, "profiles", "traffic_%s.json" % args.workload)
+    if os.path.exists(tpath):
+        traffic = json.load(open(tpath)).get(name)
+    shares = {k: round(v[0] / max(sum(x[0] for x in prof.values()), 1e-30), 4)
+              for k, v in prof.items()}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        nth = os.cpu_count() or 1
+        done, secs = cpu_md_steps(w, 3, args.cpu_budget, nth)
+        cpu = {"value": ns_per_day(w["h"], done, secs), "unit": "ns/day", "cores": nth,
+               "kind": "port",
+               "sample": "%d MD step(s) of the same %d-site workload on %d host threads "
+                         "(oracle C port, pthreads), %.1f s" % (done, ns, nth, secs)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 4), "unit": "ns/day", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 5),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32+fp64acc", "data": "synthetic (seeded fcc lattice, random orientations)",
+            "config": {"workload": "%d SPC/E waters (%d sites), L=%.3f A, cutoff %.0f A, "
+                                   "alpha %.2f/A, |n|<=%d (%d k-vectors), leap-frog+SHAKE "
+                                   "dt %.0f fs" % (system.nmol, ns, w["L"], w["cutoff"],
+                                                   w["alpha"], 20, fp.nkvec, w["h"] * 1000),
+                       "model": "SPC/E rigid water, Ewald", "global_batch": world,
+                       "seq_len": ns, "parallelism": "replicas x%d" % world,
+                       "l2": "flushed between timed steps (256 MB write)"},
+            "atom_steps_per_s": round(atom_steps, 1),
+            "fp64_path": {"value": round(value64, 4), "unit": "ns/day", "steps": k64},
+            "mixed_over_fp64": round(value / value64, 3),
+            "force_rel_rms_vs_fp64": force_err,
+            "e2e": {"value": round(e2e, 4), "unit": "ns/day",
+                    "h2d_bytes_per_step": 2 * 3 * ns * 8,
+                    "d2h_bytes_per_step": 2 * 3 * ns * 8 + 18 * 8, "steps": ke2e},
+            "gpu_launches": launches,
+            "roofline": {"bound": "fp32", "kernel": name, "achieved": round(achieved, 3),
+                         "peak": round(peak, 3), "unit": "TFLOP/s",
+                         "frac": round(achieved / peak, 4) if peak else None,
+                         "traffic": traffic,
+                         "peak_source": "measured FP32 FMA loop (mg_probe_fp32_tflops); "
+                                        "MEASURED_PEAKS.json has no FP32 figure",
+                         "avg_launch_ms": round(kavg, 5)},
+            "kernel_share": shares,
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+# ---------------------------------------------------------- reference arm --
+
+def run_reference(args, rank, world):
+    """The reference's CPU algorithm on the host cores.  The reference cook
+    binaries are compiled from the reference sources, which do not exist on
+    the GPU host (and an x86 build cannot run there), so this arm times the
+    oracle's C restatement of the same algorithm with all host threads."""
+    if rank != 0:
+        return
+    from macsimus_gb300 import configs
+    w = configs.workload(args.workload, seed=1000)
+    nth = os.cpu_count() or 1
+    if args.warmup > 0:
+        cpu_md_steps(w, 1, 1e9, nth)
+    done, secs = cpu_md_steps(w, args.steps, args.ref_budget, nth)
+    v = ns_per_day(w["h"], done, secs)
+    ns = w["system"].ns
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": round(v, 6), "unit": "ns/day",
+        "n_gpus": world, "steps": args.steps, "steps_timed": done, "warmup": args.warmup,
+        "ms_per_step": round(secs / done * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+        "config": {"workload": "%d SPC/E waters (%d sites), L=%.3f A" % (w["system"].nmol, ns,
+                                                                         w["L"])},
+        "cpu_baseline": {"value": round(v, 6), "unit": "ns/day", "cores": nth, "kind": "port",
+                         "sample": "%d MD step(s) of the full workload (time box %.0f s)"
+                                   % (done, args.ref_budget)},
+        "e2e": {"value": round(v, 6), "unit": "ns/day", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--fp64-steps", type=int, default=5)
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--ref-budget", type=float, default=150.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    rank, world, local = env_rank()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

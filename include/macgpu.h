@@ -1,0 +1,161 @@
+/*
+ * macgpu.h -- C ABI of the GB300 force path for MACSIMUS cook.
+ *
+ * The library replaces cook's per-step force routine and its integrator:
+ *
+ *   mg_forces()   replaces  void forces(ToIntPtr B, ToIntPtr A)
+ *                           (cook/forces.h:1, cook/forces.c:93-224): B (forces)
+ *                           is overwritten, energies/virial are returned only
+ *                           when measure != 0, exactly as cook fills En.el,
+ *                           En.pot, En.vir, En.Pvir (sim/simglob.h:436-577).
+ *   mg_ewald()    replaces  double Ewald(int pass, vector *frp, vector *rp)
+ *                           (sim/ewald.h:60, sim/ewald.c:258) passes 1+2.
+ *   mg_md_steps() replaces  the step loop around void Shake(double eps,double prob)
+ *                           (sim/constrd.h:5, sim/constrd.c:622-1081) with
+ *                           coordinates kept on the device between steps.
+ *
+ * Arrays are cook's ``rp`` layout: contiguous site vectors in molecule order
+ * (species by species, molecule by molecule, site by site), double[3] each,
+ * Angstrom, program units (energy in K, charge e*408.779826922048, mass in
+ * g/mol/0.831446261815324).  With Drude charges (chargepol != NULL) the site
+ * vectors are followed by the Drude displacement vectors (cook's polar_off
+ * half, sim/simglob.h:912-913), so r and f hold 2*ns vectors.
+ *
+ * Errors: every call returns an int status (MG_OK = 0); mg_last_error()
+ * gives the message.  A context is used by one host thread at a time.
+ */
+#ifndef MACGPU_H
+#define MACGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mg_ctx mg_ctx;
+
+enum mg_status {
+  MG_OK = 0,
+  MG_ERR_ARG = 1,          /* invalid argument */
+  MG_ERR_CUDA = 2,         /* CUDA runtime error */
+  MG_ERR_SHAKE = 3,        /* SHAKE did not converge (cook: "too many iterations") */
+  MG_ERR_NONFINITE = 4,    /* non-finite position or force */
+  MG_ERR_SETUP = 5,        /* force-field setup failed (smooth cutoff, k-vectors) */
+  MG_ERR_SIZE = 6          /* size beyond a compiled or stated maximum */
+};
+
+enum mg_precision {
+  MG_FP64 = 0,   /* plain double precision everywhere */
+  MG_MIXED = 1   /* FP32 pair/k-space arithmetic, FP64 accumulation and reductions */
+};
+
+/* The molecular topology and force-field tables cook builds in
+   cook/simdef.c (readblend) and sim/siminit.c. */
+typedef struct {
+  int ns;                     /* number of sites (No.s) */
+  int nmol;                   /* number of molecules (No.N) */
+  const int *mol_first;       /* [nmol+1] first site of each molecule */
+  const int *site_type;       /* [ns] LJ site type (siteinfo_t.st) */
+  const double *charge;       /* [ns] site charge (Drude builds: central charge) */
+  const double *mass;         /* [ns] site mass */
+  int ntypes;                 /* number of LJ site types (nsites of the .ble) */
+  const double *type_EvdW;    /* [ntypes] LJ well depth, K, <= 0 (sitedef.LJ.EvdW) */
+  const double *type_RvdW;    /* [ntypes] van der Waals radius, A (sitedef.LJ.RvdW) */
+  const double *type_alpha;   /* [ntypes] combining-rule polarizability (sitedef.LJ.alpha) */
+  int comb_rule;              /* combining rule of the .ble (sim/lj/sitesite.c:66-93) */
+  int nc;                     /* number of bond constraints */
+  const int *cons;            /* [2*nc] constrained site pairs (global site indices) */
+  const double *cons_len;     /* [nc] constraint lengths, A */
+  const int *mol_cfirst;      /* [nmol+1] first constraint of each molecule */
+  const double *chargepol;    /* [ns] Drude charge or NULL (siteinfo_t.chargepol) */
+  const double *alphapol;     /* [ns] Drude polarizability volume, A^3, or NULL */
+} mg_topology;
+
+/* Run parameters (cook's box, el, cutoff, h, epsc ... globals). */
+typedef struct {
+  double L[3];       /* box (box.L) */
+  double cutoff;     /* r-space cutoff (box.cutoff) */
+  double LJcutoff;   /* LJ smooth cutoff C2 (LJcutoff); <=0 means cutoff */
+  double alpha;      /* Ewald separation parameter (el.alpha) */
+  double kappa;      /* k-space cutoff K/L (el.kappa) */
+  int grid;          /* erfc spline grid (el.grid, default 256) */
+  int rshift;        /* spline shift flags (el.rshift, default 3) */
+  double rplus;      /* spline table margin (el.rplus, default 2.5) */
+  double epsinf;     /* dielectric constant of surroundings (el.epsinf, 3e33 = tin foil) */
+  int precision;     /* enum mg_precision */
+  double h;          /* time step, ps */
+  double epsc;       /* SHAKE relative tolerance (epsc) */
+  double omegac;     /* SHAKE over-relaxation (cook's omegac; <=0 selects 1.2) */
+  int shake_maxit;   /* SHAKE sweep limit per molecule (<=0 selects 1000) */
+  int cells_per_cutoff; /* linked-cell subdivision (0 = automatic) */
+} mg_params;
+
+/* Energies of one force evaluation (program units, K).
+   cook: En.el = el; En.pot += lj; En.vir += vir; En.Pvir[] += Pvir[]. */
+typedef struct {
+  double el;        /* electrostatic energy: r + k + self + dipole */
+  double lj;        /* Lennard-Jones energy */
+  double vir;       /* LJ virial sum r*f */
+  double Pvir[6];   /* virial tensor xx yy zz yz zx xy */
+  double ek;        /* k-space part */
+  double er;        /* r-space part incl. Ewald exclusion corrections */
+  double eself;     /* -alpha/sqrt(pi) sum q^2 */
+  double edip;      /* dipole term */
+  double self;      /* Drude spring energy (En.self) */
+  double ekin;      /* kinetic energy (mg_md_steps only) */
+} mg_energy;
+
+/* Create a context on the current CUDA device.  Builds the smooth-cutoff LJ
+   tables (setss), the erfc spline table (initerfc) and the k-vector set
+   (Ewald(0)) from the topology and parameters; allocates device buffers.
+   Returns NULL on failure with *status set. */
+mg_ctx *mg_create(const mg_topology *top, const mg_params *par, int *status);
+int mg_destroy(mg_ctx *ctx);
+const char *mg_last_error(const mg_ctx *ctx);
+/* the k-space cutoff after cook's rounding-problem adjustment (sim/ewald.c:485-506) */
+double mg_kappa(const mg_ctx *ctx);
+/* number of k-vectors Q->N */
+int mg_nkvec(const mg_ctx *ctx);
+
+/* cook's forces(B,A): r = A->rp (host, ns or 2*ns vectors), f = B->rp
+   (host, overwritten).  measure != 0 fills *en (may be NULL otherwise). */
+int mg_forces(mg_ctx *ctx, const double *r, double *f, int measure, mg_energy *en);
+/* the same with device pointers; the call is ordered on the context stream
+   and returns after the forces are complete */
+int mg_forces_device(mg_ctx *ctx, const double *r_dev, double *f_dev, int measure,
+                     mg_energy *en);
+/* Ewald(1,...)+Ewald(2,...): k-space forces only (added to f), returns the
+   k-space + self + dipole energy in *energy when energy != NULL */
+int mg_ewald(mg_ctx *ctx, const double *r, double *f, double *energy);
+
+/* Device-resident MD (leap-frog Verlet + SHAKE, sim/constrd.c Shake with
+   SHAKE=1, VERLET=3, no thermostat): state r = r(t), r1 = r(t)-r(t-h). */
+int mg_md_set_state(mg_ctx *ctx, const double *r, const double *r1);
+int mg_md_get_state(mg_ctx *ctx, double *r, double *r1);
+/* advance nsteps; energies of the last step in *en when en != NULL */
+int mg_md_steps(mg_ctx *ctx, int nsteps, mg_energy *en);
+
+/* number of kernels launched by the last call (diagnostics) */
+int mg_last_launches(const mg_ctx *ctx);
+
+/* Run the context's work on the given CUDA stream (a cudaStream_t of the
+   caller, e.g. a framework's current stream); NULL selects the context's own
+   stream again.  No counterpart in the reference (cook has no device). */
+int mg_set_stream(mg_ctx *ctx, void *stream);
+
+/* Per-kernel timing with CUDA events recorded on the context stream around
+   every launch while enabled (diagnostics; no counterpart in the reference).
+   mg_profile_entry(ctx, i, ...) returns 0 and fills name / total ms / count
+   of entry i, or MG_ERR_ARG past the last entry. */
+int mg_profile_enable(mg_ctx *ctx, int on);
+int mg_profile_reset(mg_ctx *ctx);
+int mg_profile_entry(mg_ctx *ctx, int i, const char **name, double *ms, long *count);
+
+/* Measured FP32 FMA throughput of the current device in TFLOP/s: a long
+   chain of independent fused multiply-adds on every SM, timed with CUDA
+   events (the FP32 roofline denominator; no counterpart in the reference). */
+int mg_probe_fp32_tflops(double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,266 @@
+"""GB300 force path for MACSIMUS cook, host-side mirror of cook's interface.
+
+The compute lives in ``libmacgpu.so`` (hand-written sm_103a CUDA behind the C
+ABI declared in ``include/macgpu.h``).  This module only marshals arrays:
+
+* ``ForcePath.forces(r, measure)``  <->  cook ``forces(B,A)`` (cook/forces.c:93)
+* ``ForcePath.ewald(r)``            <->  cook ``Ewald(1,..)`` + ``Ewald(2,..)``
+                                        (sim/ewald.c:258)
+* ``ForcePath.md_steps(n)``         <->  cook's step loop around ``Shake()``
+                                        (sim/main.c:1511, sim/constrd.c:622)
+
+There is no CPU fallback: without the built library every call raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import forcefield  # noqa: F401
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(HERE, "_build", "libmacgpu.so")
+
+MG_FP64, MG_MIXED = 0, 1
+STATUS = {0: "MG_OK", 1: "MG_ERR_ARG", 2: "MG_ERR_CUDA", 3: "MG_ERR_SHAKE",
+          4: "MG_ERR_NONFINITE", 5: "MG_ERR_SETUP", 6: "MG_ERR_SIZE"}
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class MGError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (STATUS.get(code, code), msg))
+        self.code = code
+
+
+class Topology(C.Structure):
+    _fields_ = [("ns", C.c_int), ("nmol", C.c_int), ("mol_first", _ip), ("site_type", _ip),
+                ("charge", _dp), ("mass", _dp), ("ntypes", C.c_int), ("type_EvdW", _dp),
+                ("type_RvdW", _dp), ("type_alpha", _dp), ("comb_rule", C.c_int), ("nc", C.c_int),
+                ("cons", _ip), ("cons_len", _dp), ("mol_cfirst", _ip), ("chargepol", _dp),
+                ("alphapol", _dp)]
+
+
+class Params(C.Structure):
+    _fields_ = [("L", C.c_double * 3), ("cutoff", C.c_double), ("LJcutoff", C.c_double),
+                ("alpha", C.c_double), ("kappa", C.c_double), ("grid", C.c_int),
+                ("rshift", C.c_int), ("rplus", C.c_double), ("epsinf", C.c_double),
+                ("precision", C.c_int), ("h", C.c_double), ("epsc", C.c_double),
+                ("omegac", C.c_double), ("shake_maxit", C.c_int),
+                ("cells_per_cutoff", C.c_int)]
+
+
+class Energy(C.Structure):
+    _fields_ = [("el", C.c_double), ("lj", C.c_double), ("vir", C.c_double),
+                ("Pvir", C.c_double * 6), ("ek", C.c_double), ("er", C.c_double),
+                ("eself", C.c_double), ("edip", C.c_double), ("self", C.c_double),
+                ("ekin", C.c_double)]
+
+    def asdict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "Pvir"}
+        d["Pvir"] = list(self.Pvir)
+        return d
+
+
+_lib = None
+
+
+def library():
+    """Load libmacgpu.so (it must have been built: macsimus_gb300/build.py)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIBPATH):
+            raise RuntimeError("libmacgpu.so is not built (run python macsimus_gb300/build.py)")
+        L = C.CDLL(LIBPATH)
+        vp = C.c_void_p
+        L.mg_create.argtypes = [C.POINTER(Topology), C.POINTER(Params), _ip]
+        L.mg_create.restype = vp
+        L.mg_destroy.argtypes = [vp]
+        L.mg_last_error.argtypes = [vp]
+        L.mg_last_error.restype = C.c_char_p
+        L.mg_kappa.argtypes = [vp]
+        L.mg_kappa.restype = C.c_double
+        L.mg_nkvec.argtypes = [vp]
+        L.mg_last_launches.argtypes = [vp]
+        L.mg_forces.argtypes = [vp, _dp, _dp, C.c_int, C.POINTER(Energy)]
+        L.mg_forces_device.argtypes = [vp, vp, vp, C.c_int, C.POINTER(Energy)]
+        L.mg_ewald.argtypes = [vp, _dp, _dp, _dp]
+        L.mg_md_set_state.argtypes = [vp, _dp, _dp]
+        L.mg_md_get_state.argtypes = [vp, _dp, _dp]
+        L.mg_md_steps.argtypes = [vp, C.c_int, C.POINTER(Energy)]
+        L.mg_set_stream.argtypes = [vp, vp]
+        L.mg_profile_enable.argtypes = [vp, C.c_int]
+        L.mg_profile_reset.argtypes = [vp]
+        L.mg_profile_entry.argtypes = [vp, C.c_int, C.POINTER(C.c_char_p), _dp,
+                                       C.POINTER(C.c_long)]
+        L.mg_probe_fp32_tflops.argtypes = [_dp]
+        _lib = L
+    return _lib
+
+
+def fp32_peak_tflops():
+    """measured FP32 FMA throughput of the current device (TFLOP/s)"""
+    t = C.c_double()
+    rc = library().mg_probe_fp32_tflops(C.byref(t))
+    if rc:
+        raise MGError(rc, "FP32 probe failed")
+    return t.value
+
+
+def _arr(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+class ForcePath:
+    """One box on the current GPU: topology + Ewald/LJ parameters."""
+
+    def __init__(self, system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None,
+                 grid=256, rshift=3, rplus=2.5, epsinf=3e33, h=0.002, epsc=1e-7, omegac=1.2,
+                 shake_maxit=1000, cells_per_cutoff=0):
+        lib = library()
+        self.system = system
+        self.ns = system.ns
+        keep = []
+
+        def ip(a):
+            a = _arr(a, np.int32)
+            keep.append(a)
+            return a.ctypes.data_as(_ip)
+
+        def dp(a):
+            a = _arr(a, np.float64)
+            keep.append(a)
+            return a.ctypes.data_as(_dp)
+
+        t = Topology()
+        t.ns = system.ns
+        t.nmol = system.nmol
+        t.mol_first = ip(system.mol_first)
+        t.site_type = ip(system.type)
+        t.charge = dp(system.q)
+        t.mass = dp(system.mass)
+        t.ntypes = len(system.typeE)
+        t.type_EvdW = dp(system.typeE)
+        t.type_RvdW = dp(system.typeR)
+        t.type_alpha = dp(system.typeA)
+        t.comb_rule = system.comb_rule
+        t.nc = len(system.cons_len)
+        t.cons = ip(system.cons.reshape(-1))
+        t.cons_len = dp(system.cons_len)
+        t.mol_cfirst = ip(system.mol_cfirst)
+        t.chargepol = None
+        t.alphapol = None
+        p = Params()
+        Lb = np.broadcast_to(np.asarray(L, dtype=np.float64), (3,))
+        for k in range(3):
+            p.L[k] = float(Lb[k])
+        p.cutoff = cutoff
+        p.LJcutoff = LJcutoff if LJcutoff else cutoff
+        p.alpha = alpha
+        p.kappa = kappa
+        p.grid = grid
+        p.rshift = rshift
+        p.rplus = rplus
+        p.epsinf = epsinf
+        p.precision = MG_MIXED if precision == "mixed" else MG_FP64
+        p.h = h
+        p.epsc = epsc
+        p.omegac = omegac
+        p.shake_maxit = shake_maxit
+        p.cells_per_cutoff = cells_per_cutoff
+        st = C.c_int(0)
+        self._ctx = lib.mg_create(C.byref(t), C.byref(p), C.byref(st))
+        if not self._ctx:
+            raise MGError(st.value, "mg_create failed")
+        self.precision = precision
+        self.L = np.array(Lb)
+        self.kappa = lib.mg_kappa(self._ctx)
+        self.nkvec = lib.mg_nkvec(self._ctx)
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            library().mg_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            raise MGError(rc, library().mg_last_error(self._ctx).decode())
+
+    @property
+    def launches(self):
+        return library().mg_last_launches(self._ctx)
+
+    def forces(self, r, measure=False):
+        """cook forces(B,A): returns (f [ns,3], energy dict or None)."""
+        r = _arr(r, np.float64).reshape(-1)
+        f = np.empty_like(r)
+        en = Energy()
+        self._check(library().mg_forces(self._ctx, r.ctypes.data_as(_dp), f.ctypes.data_as(_dp),
+                                        int(measure), C.byref(en)))
+        return f.reshape(-1, 3), (en.asdict() if measure else None)
+
+    def forces_device(self, r_ptr, f_ptr, measure=False):
+        """forces on device arrays (raw CUDA pointers, e.g. tensor.data_ptr())."""
+        en = Energy()
+        self._check(library().mg_forces_device(self._ctx, C.c_void_p(r_ptr), C.c_void_p(f_ptr),
+                                               int(measure), C.byref(en)))
+        return en.asdict() if measure else None
+
+    def ewald(self, r):
+        """k-space forces and energy (k + self terms), cook Ewald passes 1+2."""
+        r = _arr(r, np.float64).reshape(-1)
+        f = np.zeros_like(r)
+        e = C.c_double()
+        self._check(library().mg_ewald(self._ctx, r.ctypes.data_as(_dp), f.ctypes.data_as(_dp),
+                                       C.byref(e)))
+        return f.reshape(-1, 3), e.value
+
+    def md_set_state(self, r, r1):
+        r = _arr(r, np.float64).reshape(-1)
+        r1 = _arr(r1, np.float64).reshape(-1)
+        self._check(library().mg_md_set_state(self._ctx, r.ctypes.data_as(_dp),
+                                              r1.ctypes.data_as(_dp)))
+
+    def md_get_state(self):
+        r = np.empty(3 * self.ns)
+        r1 = np.empty(3 * self.ns)
+        self._check(library().mg_md_get_state(self._ctx, r.ctypes.data_as(_dp),
+                                              r1.ctypes.data_as(_dp)))
+        return r.reshape(-1, 3), r1.reshape(-1, 3)
+
+    def set_stream(self, stream_handle):
+        """run on a caller's CUDA stream (e.g. torch.cuda.current_stream().cuda_stream)"""
+        self._check(library().mg_set_stream(self._ctx, C.c_void_p(stream_handle or None)))
+
+    def profile(self, on=True):
+        self._check(library().mg_profile_enable(self._ctx, int(on)))
+
+    def profile_reset(self):
+        self._check(library().mg_profile_reset(self._ctx))
+
+    def profile_read(self):
+        """{kernel name: (total ms, launches)} recorded while profiling was on"""
+        out = {}
+        i = 0
+        while True:
+            name = C.c_char_p()
+            ms = C.c_double()
+            cnt = C.c_long()
+            if library().mg_profile_entry(self._ctx, i, C.byref(name), C.byref(ms), C.byref(cnt)):
+                break
+            out[name.value.decode()] = (ms.value, cnt.value)
+            i += 1
+        return out
+
+    def md_steps(self, n, measure=True):
+        en = Energy()
+        self._check(library().mg_md_steps(self._ctx, int(n), C.byref(en) if measure else None))
+        return en.asdict() if measure else None

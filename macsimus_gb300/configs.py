@@ -1,0 +1,103 @@
+"""Seeded synthetic starting configurations (cook ``init="crystal"`` analogue).
+
+Molecule anchors (the first site, O for water) sit on an fcc lattice filling
+the box; each molecule gets a uniformly random orientation and rigid-body
+Maxwell velocities (centre-of-mass translation + rotation) at temperature T.
+Ions replace randomly chosen lattice molecules.  Returns cook's state pair
+r = r(t), r1 = r(t) - r(t-h) = h v, in the site order of ``forcefield``.
+"""
+import math
+
+import numpy as np
+
+from . import forcefield as ff
+
+AVOGADRO = 6.02214076e23
+
+
+def box_length(species, counts, density):
+    """cubic box edge (A) of the given composition at density (g/cm^3)"""
+    m = 0.0
+    for s, n in zip(species, counts):
+        sp = ff.SPECIES[s]()
+        m += n * sum(ff.ble_type_row(t)[0] for t in sp.sites)
+    V = m / (density * AVOGADRO * 1e-24)
+    return V ** (1.0 / 3.0)
+
+
+def _random_rotations(rng, n):
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1)[:, None]
+    w, x, y, z = q.T
+    R = np.empty((n, 3, 3))
+    R[:, 0, 0] = 1 - 2 * (y * y + z * z)
+    R[:, 0, 1] = 2 * (x * y - z * w)
+    R[:, 0, 2] = 2 * (x * z + y * w)
+    R[:, 1, 0] = 2 * (x * y + z * w)
+    R[:, 1, 1] = 1 - 2 * (x * x + z * z)
+    R[:, 1, 2] = 2 * (y * z - x * w)
+    R[:, 2, 0] = 2 * (x * z - y * w)
+    R[:, 2, 1] = 2 * (y * z + x * w)
+    R[:, 2, 2] = 1 - 2 * (x * x + y * y)
+    return R
+
+
+def build(species, counts, L, seed=0, T=298.0, h=0.002):
+    """system, r [ns,3], r1 [ns,3] for the species/counts in a cubic box L"""
+    rng = np.random.default_rng(seed)
+    system = ff.build_system(species, counts)
+    nmol = sum(counts)
+    n = 1
+    while 4 * n ** 3 < nmol:
+        n += 1
+    a = L / n
+    base = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+    cells = np.array([[i, j, k] for i in range(n) for j in range(n) for k in range(n)], float)
+    sites = ((cells[:, None, :] + base[None, :, :]).reshape(-1, 3) + 0.25) * a
+    pick = rng.permutation(len(sites))[:nmol]
+    anchors = sites[pick]
+    r = np.zeros((system.ns, 3))
+    r1 = np.zeros((system.ns, 3))
+    imol = 0
+    for s, cnt in zip(species, counts):
+        sp = ff.SPECIES[s]()
+        geo = sp.geometry - sp.geometry[0]
+        m = np.array([ff.ble_type_row(t)[0] / ff.MUNIT for t in sp.sites])
+        Rm = _random_rotations(rng, cnt)
+        for k in range(cnt):
+            i0 = system.mol_first[imol]
+            x = anchors[imol] + geo @ Rm[k].T
+            com = (m[:, None] * x).sum(0) / m.sum()
+            v = rng.normal(size=3) * math.sqrt(T / m.sum())
+            if len(m) > 1:
+                d = x - com
+                I = (m[:, None] * d * d).sum() * 2.0 / 3.0
+                omega = rng.normal(size=3) * math.sqrt(T / I)
+                v = v + np.cross(omega, d)
+            r[i0:i0 + len(m)] = x
+            r1[i0:i0 + len(m)] = h * v
+            imol += 1
+    # remove the total momentum (cook: "Remove v drifts")
+    p = (system.mass[:, None] * r1).sum(0) / system.mass.sum()
+    r1 -= p
+    return system, r, r1
+
+
+WORKLOADS = {
+    # the 864 SPC/E configuration (L = 29.65 A, cutoff 12, alpha 0.26, |n|<=8)
+    "spce864": dict(species=["WAT"], counts=[864], L=29.65, cutoff=12.0, alpha=0.26, kn=8),
+    # brine: 4096 SPC/E + 128 Na+ + 128 Cl- at 1.06 g/cm3, cutoff 10, alpha 0.31, |n|<=12
+    "brine4352": dict(species=["WAT", "NA", "CL"], counts=[4096, 128, 128], density=1.06,
+                      cutoff=10.0, alpha=0.31, kn=12),
+    # 32768 SPC/E waters at 0.997 g/cm3 (L = 99.44 A), cutoff 12, alpha 0.26, |n|<=20
+    "spce32768": dict(species=["WAT"], counts=[32768], density=0.997, cutoff=12.0, alpha=0.26,
+                      kn=20),
+}
+
+
+def workload(name, seed=0, T=298.0, h=0.002):
+    w = WORKLOADS[name]
+    L = w.get("L") or box_length(w["species"], w["counts"], w["density"])
+    system, r, r1 = build(w["species"], w["counts"], L, seed=seed, T=T, h=h)
+    return dict(name=name, system=system, r=r, r1=r1, L=L, cutoff=w["cutoff"], alpha=w["alpha"],
+                kappa=(w["kn"] + 1e-6) / L, h=h)

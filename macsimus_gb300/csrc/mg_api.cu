@@ -1,0 +1,794 @@
+// C ABI of the GB300 force path (include/macgpu.h): context set-up and the
+// per-call orchestration of the kernels in mg_kernels.cu.
+#include "../../include/macgpu.h"
+#include "mg_internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include <cub/device/device_radix_sort.cuh>
+
+using namespace mg;
+
+struct mg_ctx {
+  std::string err;
+  int precision = MG_MIXED;
+  int ns = 0, nmol = 0, nc = 0, nq = 0, nk = 0, nkind = 0, launches = 0;
+  double L[3] = {0, 0, 0};
+  double cutoff = 0, alpha = 0, kappa = 0, sgrid = 0, eself = 0, epsinf = 3e33;
+  double h = 0.002, epsc = 1e-7, omega = 0.6;
+  int shake_maxit = 1000;
+  int ncx = 0, ncy = 0, ncz = 0, ncell = 0, nstencil = 0, sort_bits = 1;
+  int Kx = 0, Ky = 0, Kz = 0, row = 0, ntask = 0, ncol = 0, nchunk = 1;
+  cudaStream_t stream = nullptr;
+  // host copies
+  std::vector<int> h_kind, h_mol;
+  // device buffers
+  double *d_r = nullptr, *d_f = nullptr, *d_r1 = nullptr, *d_p = nullptr;
+  int *d_kind = nullptr, *d_mol = nullptr;
+  int *d_key = nullptr, *d_idx = nullptr, *d_key_s = nullptr, *d_order = nullptr;
+  int* d_cell_start = nullptr;
+  void* d_sort_tmp = nullptr;
+  size_t sort_tmp_bytes = 0;
+  int4* d_pj = nullptr;
+  double4* d_pd = nullptr;
+  int4* d_stencil = nullptr;
+  PairF* d_ptabf = nullptr;
+  PairD* d_ptabd = nullptr;
+  float4 *d_erd = nullptr, *d_eru = nullptr;
+  double* d_ert = nullptr;
+  double* d_epart = nullptr;
+  // k-space
+  int* d_qsite = nullptr;
+  double* d_qval = nullptr;
+  KTask* d_task = nullptr;
+  KCol* d_col = nullptr;
+  int4* d_kvec = nullptr;
+  double* d_ekk = nullptr;
+  double* d_S = nullptr;
+  float2* d_Wf = nullptr;
+  double2* d_Wd = nullptr;
+  void* d_tab = nullptr;   // float2 or double2 rows
+  void* d_part = nullptr;  // float2 or double2 partials
+  double* d_ekpart = nullptr;
+  int nkblocks = 0;
+  // SHAKE
+  int* d_mol_first = nullptr;
+  int* d_mol_cfirst = nullptr;
+  int2* d_cons = nullptr;
+  double *d_bondq = nullptr, *d_imass = nullptr, *d_mass = nullptr;
+  double* d_kinpart = nullptr;
+  int* d_status = nullptr;
+  // reduction outputs
+  double* d_sums = nullptr;  // [0..9] pair, [10..16] k-space, [17] kinetic
+  double* h_sums = nullptr;  // pinned
+  bool have_state = false;
+  // stream ownership and per-kernel event timing
+  cudaStream_t own_stream = nullptr;
+  bool prof_on = false;
+  struct Rec { int id; cudaEvent_t a, b; };
+  std::vector<std::string> pnames;
+  std::vector<double> pms;
+  std::vector<long> pcnt;
+  std::vector<Rec> pending;
+  std::vector<cudaEvent_t> evpool;
+  size_t evused = 0;
+};
+
+namespace {
+
+int fail(mg_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define CK(call)                                                                       \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess)                                                             \
+      return fail(ctx, MG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+cudaEvent_t prof_event(mg_ctx* c) {
+  if (c->evused == c->evpool.size()) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    c->evpool.push_back(e);
+  }
+  return c->evpool[c->evused++];
+}
+
+int prof_id(mg_ctx* c, const char* name) {
+  for (size_t i = 0; i < c->pnames.size(); i++)
+    if (c->pnames[i] == name) return (int)i;
+  c->pnames.push_back(name);
+  c->pms.push_back(0);
+  c->pcnt.push_back(0);
+  return (int)c->pnames.size() - 1;
+}
+
+// fold the recorded event pairs into the per-kernel totals (after a sync)
+void prof_resolve(mg_ctx* c) {
+  for (auto& r : c->pending) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+      c->pms[r.id] += ms;
+      c->pcnt[r.id] += 1;
+    }
+  }
+  c->pending.clear();
+  c->evused = 0;
+}
+
+// launch `call`; with profiling on, bracket it by events on the context stream
+#define PROF(name, call)                                              \
+  do {                                                                \
+    cudaEvent_t a_ = nullptr;                                         \
+    if (ctx->prof_on) {                                               \
+      a_ = prof_event(ctx);                                           \
+      cudaEventRecord(a_, ctx->stream);                               \
+    }                                                                 \
+    CK(call);                                                         \
+    if (ctx->prof_on) {                                               \
+      cudaEvent_t b_ = prof_event(ctx);                               \
+      cudaEventRecord(b_, ctx->stream);                               \
+      ctx->pending.push_back(mg_ctx::Rec{prof_id(ctx, name), a_, b_}); \
+    }                                                                 \
+  } while (0)
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t n) {
+  return cudaMalloc((void**)p, sizeof(T) * (n ? n : 1));
+}
+template <typename T>
+cudaError_t upload(T** p, const T* h, size_t n) {
+  cudaError_t e = dalloc(p, n);
+  if (e != cudaSuccess || n == 0) return e;
+  return cudaMemcpy(*p, h, sizeof(T) * n, cudaMemcpyHostToDevice);
+}
+
+int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
+  if (!t || !p || t->ns <= 0 || t->nmol <= 0 || !t->mol_first || !t->site_type || !t->charge ||
+      !t->mass || t->ntypes <= 0 || !t->type_EvdW || !t->type_RvdW)
+    return fail(ctx, MG_ERR_ARG, "incomplete topology");
+  if (t->chargepol)
+    return fail(ctx, MG_ERR_ARG, "Drude charges are not supported by this build of the context");
+  if (p->precision != MG_FP64 && p->precision != MG_MIXED)
+    return fail(ctx, MG_ERR_ARG, "precision must be MG_FP64 or MG_MIXED");
+  if (!(p->cutoff > 0) || !(p->alpha > 0) || !(p->kappa > 0))
+    return fail(ctx, MG_ERR_ARG, "cutoff, alpha and kappa must be positive");
+  for (int d = 0; d < 3; d++)
+    if (!(p->L[d] > 2 * p->cutoff))
+      return fail(ctx, MG_ERR_ARG, "the cutoff must be shorter than half the box");
+  if (p->epsinf < 1e20)
+    return fail(ctx, MG_ERR_ARG, "only conducting (tin-foil) boundary conditions, epsinf>=1e20");
+  if (t->nmol >= (1 << 23)) return fail(ctx, MG_ERR_SIZE, "too many molecules (limit 2^23-1)");
+
+  ctx->precision = p->precision;
+  ctx->ns = t->ns;
+  ctx->nmol = t->nmol;
+  std::memcpy(ctx->L, p->L, sizeof(ctx->L));
+  ctx->cutoff = p->cutoff;
+  ctx->alpha = p->alpha;
+  ctx->epsinf = p->epsinf;
+  ctx->h = p->h > 0 ? p->h : 0.002;
+  ctx->epsc = p->epsc > 0 ? p->epsc : 1e-7;
+  ctx->omega = 0.5 * (p->omegac > 0 ? p->omegac : 1.2);
+  ctx->shake_maxit = p->shake_maxit > 0 ? p->shake_maxit : 1000;
+  CK(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
+  ctx->stream = ctx->own_stream;
+  const int ns = t->ns;
+
+  // ---- site kinds: distinct (LJ type, charge) combinations
+  std::map<std::pair<int, double>, int> kinds;
+  std::vector<int> kind_type;
+  std::vector<double> kind_q;
+  ctx->h_kind.resize(ns);
+  ctx->h_mol.resize(ns);
+  for (int n = 0; n < t->nmol; n++)
+    for (int i = t->mol_first[n]; i < t->mol_first[n + 1]; i++) ctx->h_mol[i] = n;
+  double sumq2 = 0;
+  for (int i = 0; i < ns; i++) {
+    if (t->site_type[i] < 0 || t->site_type[i] >= t->ntypes)
+      return fail(ctx, MG_ERR_ARG, "site type out of range");
+    auto key = std::make_pair(t->site_type[i], t->charge[i]);
+    auto it = kinds.find(key);
+    if (it == kinds.end()) {
+      int k = (int)kind_type.size();
+      kinds[key] = k;
+      kind_type.push_back(t->site_type[i]);
+      kind_q.push_back(t->charge[i]);
+      ctx->h_kind[i] = k;
+    } else {
+      ctx->h_kind[i] = it->second;
+    }
+    sumq2 += t->charge[i] * t->charge[i];
+  }
+  ctx->nkind = (int)kind_type.size();
+  if (ctx->nkind > MAX_KINDS) return fail(ctx, MG_ERR_SIZE, "more than 16 site kinds");
+  ctx->eself = -p->alpha / 1.772453850905516 * sumq2;
+
+  // ---- LJ pair tables (combining rule + smooth cutoff), per pair of kinds
+  double C2 = p->LJcutoff > 0 ? p->LJcutoff : p->cutoff;
+  std::vector<PairLJ> tp(t->ntypes * t->ntypes);
+  std::vector<double> ta(t->ntypes, 0.0);
+  for (int a = 0; a < t->ntypes; a++)
+    for (int b = 0; b < t->ntypes; b++) {
+      double eps, sig;
+      double aa = t->type_alpha ? t->type_alpha[a] : 0, ab = t->type_alpha ? t->type_alpha[b] : 0;
+      combining_rule(t->type_EvdW[a], t->type_RvdW[a], aa, t->type_EvdW[b], t->type_RvdW[b], ab,
+                     t->comb_rule, &eps, &sig);
+      if (smooth_lj(eps, sig, C2, &tp[a * t->ntypes + b]))
+        return fail(ctx, MG_ERR_SETUP, "smooth LJ cutoff cannot be determined");
+    }
+  int nk2 = ctx->nkind * ctx->nkind;
+  std::vector<PairF> pf(nk2);
+  std::vector<PairD> pd(nk2);
+  for (int a = 0; a < ctx->nkind; a++)
+    for (int b = 0; b < ctx->nkind; b++) {
+      const PairLJ& P = tp[kind_type[a] * t->ntypes + kind_type[b]];
+      double qq = kind_q[a] * kind_q[b];
+      pd[a * ctx->nkind + b] = PairD{P.C1q, P.C2q, P.A4, P.E24, P.Sq, qq, P.A, P.E4};
+      pf[a * ctx->nkind + b] = PairF{(float)P.C1q, (float)P.C2q, (float)P.A4, (float)P.E24,
+                                     (float)P.Sq,  (float)qq,    (float)P.A,  (float)P.E4};
+    }
+
+  // ---- erfc spline table over [0, cutoff + rplus)
+  std::vector<double> ert;
+  double rplus = p->rplus > 0 ? p->rplus : 2.5;
+  int grid = p->grid > 0 ? p->grid : 256;
+  erfc_table(grid, p->cutoff + rplus, p->cutoff, p->alpha, p->rshift, &ert, &ctx->sgrid);
+  int ntab = (int)(ert.size() / 6);
+
+  // ---- cells: size >= cutoff/cdiv and at least 2*cdiv+1 cells per edge
+  int cdivv = p->cells_per_cutoff > 0 ? p->cells_per_cutoff : 2;
+  int nc3[3];
+  for (;; cdivv++) {
+    if (cdivv > 8) return fail(ctx, MG_ERR_SETUP, "cannot build the linked-cell grid");
+    bool ok = true;
+    for (int d = 0; d < 3; d++) {
+      nc3[d] = (int)(p->L[d] * cdivv / p->cutoff);
+      if (nc3[d] < 2 * cdivv + 1) ok = false;
+    }
+    if (ok) break;
+  }
+  ctx->ncx = nc3[0];
+  ctx->ncy = nc3[1];
+  ctx->ncz = nc3[2];
+  ctx->ncell = nc3[0] * nc3[1] * nc3[2];
+  while ((1 << ctx->sort_bits) < ctx->ncell) ctx->sort_bits++;
+  std::vector<int4> st;
+  for (int dx = -cdivv; dx <= cdivv; dx++)
+    for (int dy = -cdivv; dy <= cdivv; dy++)
+      for (int dz = -cdivv; dz <= cdivv; dz++) {
+        double g[3] = {(double)std::max(std::abs(dx) - 1, 0) * p->L[0] / nc3[0],
+                       (double)std::max(std::abs(dy) - 1, 0) * p->L[1] / nc3[1],
+                       (double)std::max(std::abs(dz) - 1, 0) * p->L[2] / nc3[2]};
+        double dmin2 = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+        if (dmin2 < p->cutoff * p->cutoff * (1 + 1e-9)) st.push_back(make_int4(dx, dy, dz, 0));
+      }
+  ctx->nstencil = (int)st.size();
+
+  // ---- k-vectors (cook's set), sorted into (kx,ky) columns of consecutive kz
+  double kappa = p->kappa;
+  std::vector<int> kv;
+  int nk = kvector_set(p->L, &kappa, &kv);
+  if (nk <= 0) return fail(ctx, MG_ERR_SETUP, "k-vector set is empty or ill-defined");
+  ctx->kappa = kappa;
+  ctx->nk = nk;
+  std::vector<int> ordk(nk);
+  for (int i = 0; i < nk; i++) ordk[i] = i;
+  std::sort(ordk.begin(), ordk.end(), [&](int a, int b) {
+    for (int d = 0; d < 3; d++)
+      if (kv[3 * a + d] != kv[3 * b + d]) return kv[3 * a + d] < kv[3 * b + d];
+    return false;
+  });
+  std::vector<int4> kvec(nk);
+  std::vector<double> ekk(nk);
+  double V = p->L[0] * p->L[1] * p->L[2], PIaq = -std::pow(M_PI / p->alpha, 2);
+  for (int i = 0; i < nk; i++) {
+    int a = ordk[i];
+    kvec[i] = make_int4(kv[3 * a], kv[3 * a + 1], kv[3 * a + 2], 0);
+    double kk = std::pow(kvec[i].z / p->L[2], 2) +
+                (std::pow(kvec[i].y / p->L[1], 2) + std::pow(kvec[i].x / p->L[0], 2));
+    ekk[i] = 4 / (kk * V) * std::exp(PIaq * kk);
+    ctx->Kx = std::max(ctx->Kx, std::abs(kvec[i].x));
+    ctx->Ky = std::max(ctx->Ky, std::abs(kvec[i].y));
+    ctx->Kz = std::max(ctx->Kz, std::abs(kvec[i].z));
+  }
+  std::vector<KCol> cols;
+  std::vector<KTask> tasks;
+  for (int i = 0; i < nk;) {
+    int j = i + 1;
+    while (j < nk && kvec[j].x == kvec[i].x && kvec[j].y == kvec[i].y &&
+           kvec[j].z == kvec[j - 1].z + 1)
+      j++;
+    cols.push_back(KCol{kvec[i].x, kvec[i].y, kvec[i].z, j - i, i, {0, 0, 0}});
+    for (int s = i; s < j; s += KZT)
+      tasks.push_back(KTask{kvec[s].x, kvec[s].y, kvec[s].z, std::min(KZT, j - s), s, {0, 0, 0}});
+    i = j;
+  }
+  ctx->ncol = (int)cols.size();
+  ctx->ntask = (int)tasks.size();
+  ctx->row = (ctx->Kx + 1) + (2 * ctx->Ky + 1) + (2 * ctx->Kz + 1);
+
+  // ---- charges
+  std::vector<int> qsite;
+  std::vector<double> qval;
+  for (int i = 0; i < ns; i++)
+    if (t->charge[i] != 0) {
+      qsite.push_back(i);
+      qval.push_back(t->charge[i]);
+    }
+  ctx->nq = (int)qsite.size();
+  int tblocks = (ctx->ntask + 255) / 256;
+  ctx->nchunk = std::max(1, std::min(std::max(1, ctx->nq / 32), (4 * 152 + tblocks - 1) / tblocks));
+  ctx->nkblocks = (nk + 255) / 256;
+
+  // ---- constraints
+  ctx->nc = t->nc;
+  std::vector<int> mcf(t->nmol + 1, 0);
+  std::vector<int2> cons(std::max(t->nc, 0));
+  std::vector<double> bondq(std::max(t->nc, 0));
+  if (t->nc > 0) {
+    if (!t->cons || !t->cons_len || !t->mol_cfirst)
+      return fail(ctx, MG_ERR_ARG, "constraints need cons, cons_len and mol_cfirst");
+    for (int k = 0; k <= t->nmol; k++) mcf[k] = t->mol_cfirst[k];
+    for (int k = 0; k < t->nc; k++) {
+      cons[k] = make_int2(t->cons[2 * k], t->cons[2 * k + 1]);
+      bondq[k] = t->cons_len[k] * t->cons_len[k];
+    }
+  }
+  std::vector<double> imass(ns), mass(ns);
+  for (int i = 0; i < ns; i++) {
+    mass[i] = t->mass[i];
+    imass[i] = t->mass[i] > 0 ? 1 / t->mass[i] : 0;
+  }
+
+  // ---- device buffers
+  CK(dalloc(&ctx->d_r, 3 * (size_t)ns));
+  CK(dalloc(&ctx->d_f, 3 * (size_t)ns));
+  CK(dalloc(&ctx->d_r1, 3 * (size_t)ns));
+  CK(dalloc(&ctx->d_p, 3 * (size_t)ns));
+  CK(upload(&ctx->d_kind, ctx->h_kind.data(), ns));
+  CK(upload(&ctx->d_mol, ctx->h_mol.data(), ns));
+  CK(dalloc(&ctx->d_key, ns));
+  CK(dalloc(&ctx->d_idx, ns));
+  CK(dalloc(&ctx->d_key_s, ns));
+  CK(dalloc(&ctx->d_order, ns));
+  CK(dalloc(&ctx->d_cell_start, ctx->ncell + 1));
+  CK(cub::DeviceRadixSort::SortPairs(nullptr, ctx->sort_tmp_bytes, ctx->d_key, ctx->d_key_s,
+                                     ctx->d_idx, ctx->d_order, ns, 0, ctx->sort_bits));
+  CK(cudaMalloc(&ctx->d_sort_tmp, ctx->sort_tmp_bytes));
+  CK(upload(&ctx->d_stencil, st.data(), st.size()));
+  CK(dalloc(&ctx->d_epart, (size_t)ctx->ncell * 10));
+  CK(upload(&ctx->d_qsite, qsite.data(), qsite.size()));
+  CK(upload(&ctx->d_qval, qval.data(), qval.size()));
+  CK(upload(&ctx->d_task, tasks.data(), tasks.size()));
+  CK(upload(&ctx->d_col, cols.data(), cols.size()));
+  CK(upload(&ctx->d_kvec, kvec.data(), kvec.size()));
+  CK(upload(&ctx->d_ekk, ekk.data(), ekk.size()));
+  CK(dalloc(&ctx->d_S, 2 * (size_t)nk));
+  CK(dalloc(&ctx->d_ekpart, (size_t)ctx->nkblocks * 7));
+  if (ctx->precision == MG_MIXED) {
+    CK(dalloc(&ctx->d_pj, ns));
+    CK(upload(&ctx->d_ptabf, pf.data(), pf.size()));
+    std::vector<float4> erd(ntab), eru(ntab);
+    for (int i = 0; i < ntab; i++) {
+      erd[i] = make_float4((float)ert[6 * i + 3], (float)ert[6 * i + 4], (float)ert[6 * i + 5], 0);
+      eru[i] = make_float4((float)ert[6 * i], (float)ert[6 * i + 1], (float)ert[6 * i + 2], 0);
+    }
+    CK(upload(&ctx->d_erd, erd.data(), ntab));
+    CK(upload(&ctx->d_eru, eru.data(), ntab));
+    CK(dalloc((float2**)&ctx->d_tab, (size_t)ctx->nq * ctx->row));
+    CK(dalloc((float2**)&ctx->d_part, (size_t)ctx->nchunk * nk));
+    CK(dalloc(&ctx->d_Wf, nk));
+  } else {
+    CK(dalloc(&ctx->d_pd, ns));
+    CK(upload(&ctx->d_ptabd, pd.data(), pd.size()));
+    CK(upload(&ctx->d_ert, ert.data(), ert.size()));
+    CK(dalloc((double2**)&ctx->d_tab, (size_t)ctx->nq * ctx->row));
+    CK(dalloc((double2**)&ctx->d_part, (size_t)ctx->nchunk * nk));
+    CK(dalloc(&ctx->d_Wd, nk));
+  }
+  CK(upload(&ctx->d_mol_first, t->mol_first, t->nmol + 1));
+  CK(upload(&ctx->d_mol_cfirst, mcf.data(), mcf.size()));
+  CK(upload(&ctx->d_cons, cons.data(), cons.size()));
+  CK(upload(&ctx->d_bondq, bondq.data(), bondq.size()));
+  CK(upload(&ctx->d_imass, imass.data(), ns));
+  CK(upload(&ctx->d_mass, mass.data(), ns));
+  CK(dalloc(&ctx->d_kinpart, (size_t)(t->nmol + 127) / 128 + 1));
+  CK(dalloc(&ctx->d_status, 1));
+  CK(cudaMemset(ctx->d_status, 0, sizeof(int)));
+  CK(dalloc(&ctx->d_sums, 32));
+  CK(cudaMallocHost((void**)&ctx->h_sums, 32 * sizeof(double)));
+  return MG_OK;
+}
+
+Launch launch(mg_ctx* ctx) { return Launch{ctx->stream, &ctx->launches}; }
+
+// forces of the positions in r_dev (device, cook layout) into f_dev; the
+// energies are reduced into d_sums when measure
+int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) {
+  Launch L = launch(ctx);
+  const int ns = ctx->ns;
+  // linked cells
+  PROF("cell_list", k_prep_cells(L, ns, r_dev, nullptr, ctx->L[0], ctx->L[1], ctx->L[2],
+                                 ctx->ncx, ctx->ncy, ctx->ncz, ctx->d_key, ctx->d_idx));
+  PROF("cell_list", cub::DeviceRadixSort::SortPairs(ctx->d_sort_tmp, ctx->sort_tmp_bytes,
+                                                    ctx->d_key, ctx->d_key_s, ctx->d_idx,
+                                                    ctx->d_order, ns, 0, ctx->sort_bits,
+                                                    ctx->stream));
+  ctx->launches += 2;
+  PROF("cell_list", k_cell_bounds(L, ns, ctx->ncell, ctx->d_key_s, ctx->d_cell_start));
+  PairArgs pa;
+  pa.ns = ns;
+  pa.ncx = ctx->ncx;
+  pa.ncy = ctx->ncy;
+  pa.ncz = ctx->ncz;
+  pa.nstencil = ctx->nstencil;
+  pa.nkind = ctx->nkind;
+  pa.cell_start = ctx->d_cell_start;
+  pa.order = ctx->d_order;
+  pa.stencil = ctx->d_stencil;
+  pa.Lx = ctx->L[0];
+  pa.Ly = ctx->L[1];
+  pa.Lz = ctx->L[2];
+  pa.cutoff_sq = ctx->cutoff * ctx->cutoff;
+  pa.sgrid = ctx->sgrid;
+  pa.alpha = ctx->alpha;
+  pa.f = f_dev;
+  pa.epart = ctx->d_epart;
+  KArgs ka;
+  ka.nq = ctx->nq;
+  ka.nk = ctx->nk;
+  ka.ntask = ctx->ntask;
+  ka.ncol = ctx->ncol;
+  ka.nchunk = ctx->nchunk;
+  ka.Kx = ctx->Kx;
+  ka.Ky = ctx->Ky;
+  ka.Kz = ctx->Kz;
+  ka.row = ctx->row;
+  ka.Lx = ctx->L[0];
+  ka.Ly = ctx->L[1];
+  ka.Lz = ctx->L[2];
+  ka.alpha = ctx->alpha;
+  ka.qsite = ctx->d_qsite;
+  ka.qval = ctx->d_qval;
+  ka.task = ctx->d_task;
+  ka.col = ctx->d_col;
+  ka.kvec = ctx->d_kvec;
+  ka.ekk = ctx->d_ekk;
+  ka.S = ctx->d_S;
+  ka.Wf = ctx->d_Wf;
+  ka.Wd = ctx->d_Wd;
+  ka.f = f_dev;
+  ka.ek_part = ctx->d_ekpart;
+  if (ctx->precision == MG_MIXED) {
+    PROF("cell_list", k_gather_mixed(L, ns, r_dev, ctx->d_order, ctx->d_kind, ctx->d_mol, ctx->L[0], ctx->L[1],
+                      ctx->L[2], ctx->d_pj));
+    PROF("pair_mixed", k_pair_mixed(L, pa, ctx->d_pj, ctx->d_ptabf, ctx->d_erd, ctx->d_eru, measure));
+    if (ctx->nq > 0) {
+      PROF("phase_tables", k_phase_tables_mixed(L, ka, r_dev, (float2*)ctx->d_tab));
+      PROF("ewald_sk", k_sk_mixed(L, ka, (const float2*)ctx->d_tab, (float2*)ctx->d_part));
+      PROF("ewald_sk_reduce", k_sk_reduce_mixed(L, ka, (const float2*)ctx->d_part, measure));
+      PROF("ewald_kforce", k_kforce_mixed(L, ka, (const float2*)ctx->d_tab));
+    }
+  } else {
+    PROF("cell_list", k_gather_fp64(L, ns, r_dev, ctx->d_order, ctx->d_kind, ctx->d_mol, ctx->L[0], ctx->L[1],
+                     ctx->L[2], ctx->d_pd));
+    PROF("pair_fp64", k_pair_fp64(L, pa, ctx->d_pd, ctx->d_ptabd, ctx->d_ert, measure));
+    if (ctx->nq > 0) {
+      PROF("phase_tables", k_phase_tables_fp64(L, ka, r_dev, (double2*)ctx->d_tab));
+      PROF("ewald_sk", k_sk_fp64(L, ka, (const double2*)ctx->d_tab, (double2*)ctx->d_part));
+      PROF("ewald_sk_reduce", k_sk_reduce_fp64(L, ka, (const double2*)ctx->d_part, measure));
+      PROF("ewald_kforce", k_kforce_fp64(L, ka, (const double2*)ctx->d_tab));
+    }
+  }
+  if (measure) {
+    PROF("reduce", k_reduce_sum(L, ctx->d_epart, ctx->ncell, 10, ctx->d_sums));
+    if (ctx->nq > 0) PROF("reduce", k_reduce_sum(L, ctx->d_ekpart, ctx->nkblocks, 7, ctx->d_sums + 10));
+  }
+  return MG_OK;
+}
+
+// energies from the reduced sums (host, after the stream has been synchronized)
+void fill_energy(mg_ctx* ctx, mg_energy* en) {
+  const double* s = ctx->h_sums;
+  std::memset(en, 0, sizeof(*en));
+  double Ek = ctx->nq > 0 ? s[10] / (4 * M_PI) : 0;
+  en->er = s[0];
+  en->lj = s[1];
+  en->vir = s[2];
+  en->ek = Ek;
+  en->eself = ctx->eself;
+  en->edip = 0;
+  en->el = s[0] + Ek + ctx->eself;
+  for (int m = 0; m < 6; m++) en->Pvir[m] = s[3 + m];
+  if (ctx->nq > 0) {
+    for (int m = 0; m < 3; m++) en->Pvir[m] += Ek;
+    for (int m = 0; m < 6; m++) en->Pvir[m] -= 2 / (4 * M_PI) * s[11 + m];
+  }
+}
+
+int fetch_sums(mg_ctx* ctx) {
+  CK(cudaMemcpyAsync(ctx->h_sums, ctx->d_sums, 32 * sizeof(double), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  return MG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+mg_ctx* mg_create(const mg_topology* top, const mg_params* par, int* status) {
+  mg_ctx* ctx = new mg_ctx();
+  int rc = setup(ctx, top, par);
+  if (rc != MG_OK) {
+    fprintf(stderr, "mg_create: %s\n", ctx->err.c_str());
+    mg_destroy(ctx);
+    if (status) *status = rc;
+    return nullptr;
+  }
+  if (status) *status = MG_OK;
+  return ctx;
+}
+
+int mg_destroy(mg_ctx* ctx) {
+  if (!ctx) return MG_OK;
+  void* bufs[] = {ctx->d_r,      ctx->d_f,       ctx->d_r1,    ctx->d_p,      ctx->d_kind,
+                  ctx->d_mol,    ctx->d_key,     ctx->d_idx,   ctx->d_key_s,  ctx->d_order,
+                  ctx->d_cell_start, ctx->d_sort_tmp, ctx->d_pj, ctx->d_pd,  ctx->d_stencil,
+                  ctx->d_ptabf,  ctx->d_ptabd,   ctx->d_erd,   ctx->d_eru,    ctx->d_ert,
+                  ctx->d_epart,  ctx->d_qsite,   ctx->d_qval,  ctx->d_task,   ctx->d_col,
+                  ctx->d_kvec,   ctx->d_ekk,     ctx->d_S,     ctx->d_Wf,     ctx->d_Wd,
+                  ctx->d_tab,    ctx->d_part,    ctx->d_ekpart, ctx->d_mol_first,
+                  ctx->d_mol_cfirst, ctx->d_cons, ctx->d_bondq, ctx->d_imass, ctx->d_mass,
+                  ctx->d_kinpart, ctx->d_status, ctx->d_sums};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  if (ctx->h_sums) cudaFreeHost(ctx->h_sums);
+  for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+  return MG_OK;
+}
+
+const char* mg_last_error(const mg_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+double mg_kappa(const mg_ctx* ctx) { return ctx ? ctx->kappa : 0; }
+int mg_nkvec(const mg_ctx* ctx) { return ctx ? ctx->nk : 0; }
+int mg_last_launches(const mg_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int mg_forces_device(mg_ctx* ctx, const double* r_dev, double* f_dev, int measure,
+                     mg_energy* en) {
+  if (!ctx || !r_dev || !f_dev) return fail(ctx, MG_ERR_ARG, "null argument");
+  ctx->launches = 0;
+  int rc = forces_async(ctx, r_dev, f_dev, measure != 0);
+  if (rc) return rc;
+  if (measure) {
+    rc = fetch_sums(ctx);
+    if (rc) return rc;
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  prof_resolve(ctx);
+  if (measure && en) fill_energy(ctx, en);
+  return MG_OK;
+}
+
+int mg_forces(mg_ctx* ctx, const double* r, double* f, int measure, mg_energy* en) {
+  if (!ctx || !r || !f) return fail(ctx, MG_ERR_ARG, "null argument");
+  ctx->launches = 0;
+  const size_t nb = 3 * (size_t)ctx->ns * sizeof(double);
+  CK(cudaMemcpyAsync(ctx->d_r, r, nb, cudaMemcpyHostToDevice, ctx->stream));
+  int rc = forces_async(ctx, ctx->d_r, ctx->d_f, measure != 0);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(f, ctx->d_f, nb, cudaMemcpyDeviceToHost, ctx->stream));
+  if (measure) {
+    rc = fetch_sums(ctx);
+    if (rc) return rc;
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  prof_resolve(ctx);
+  if (measure && en) fill_energy(ctx, en);
+  return MG_OK;
+}
+
+int mg_ewald(mg_ctx* ctx, const double* r, double* f, double* energy) {
+  if (!ctx || !r || !f) return fail(ctx, MG_ERR_ARG, "null argument");
+  // full forces minus the r-space part is not separable cheaply here: run
+  // the k-space kernels alone on a zeroed force buffer
+  ctx->launches = 0;
+  const size_t nb = 3 * (size_t)ctx->ns * sizeof(double);
+  Launch L = launch(ctx);
+  CK(cudaMemcpyAsync(ctx->d_r, r, nb, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_f, 0, nb, ctx->stream));
+  KArgs ka;
+  std::memset(&ka, 0, sizeof(ka));
+  ka.nq = ctx->nq;
+  ka.nk = ctx->nk;
+  ka.ntask = ctx->ntask;
+  ka.ncol = ctx->ncol;
+  ka.nchunk = ctx->nchunk;
+  ka.Kx = ctx->Kx;
+  ka.Ky = ctx->Ky;
+  ka.Kz = ctx->Kz;
+  ka.row = ctx->row;
+  ka.Lx = ctx->L[0];
+  ka.Ly = ctx->L[1];
+  ka.Lz = ctx->L[2];
+  ka.alpha = ctx->alpha;
+  ka.qsite = ctx->d_qsite;
+  ka.qval = ctx->d_qval;
+  ka.task = ctx->d_task;
+  ka.col = ctx->d_col;
+  ka.kvec = ctx->d_kvec;
+  ka.ekk = ctx->d_ekk;
+  ka.S = ctx->d_S;
+  ka.Wf = ctx->d_Wf;
+  ka.Wd = ctx->d_Wd;
+  ka.f = ctx->d_f;
+  ka.ek_part = ctx->d_ekpart;
+  if (ctx->nq > 0) {
+    if (ctx->precision == MG_MIXED) {
+      CK(k_phase_tables_mixed(L, ka, ctx->d_r, (float2*)ctx->d_tab));
+      CK(k_sk_mixed(L, ka, (const float2*)ctx->d_tab, (float2*)ctx->d_part));
+      CK(k_sk_reduce_mixed(L, ka, (const float2*)ctx->d_part, true));
+      CK(k_kforce_mixed(L, ka, (const float2*)ctx->d_tab));
+    } else {
+      CK(k_phase_tables_fp64(L, ka, ctx->d_r, (double2*)ctx->d_tab));
+      CK(k_sk_fp64(L, ka, (const double2*)ctx->d_tab, (double2*)ctx->d_part));
+      CK(k_sk_reduce_fp64(L, ka, (const double2*)ctx->d_part, true));
+      CK(k_kforce_fp64(L, ka, (const double2*)ctx->d_tab));
+    }
+    CK(k_reduce_sum(L, ctx->d_ekpart, ctx->nkblocks, 7, ctx->d_sums + 10));
+  }
+  std::vector<double> fk(3 * (size_t)ctx->ns);
+  CK(cudaMemcpyAsync(fk.data(), ctx->d_f, nb, cudaMemcpyDeviceToHost, ctx->stream));
+  int rc = fetch_sums(ctx);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (size_t i = 0; i < fk.size(); i++) f[i] += fk[i];
+  if (energy) *energy = (ctx->nq > 0 ? ctx->h_sums[10] / (4 * M_PI) : 0) + ctx->eself;
+  return MG_OK;
+}
+
+int mg_md_set_state(mg_ctx* ctx, const double* r, const double* r1) {
+  if (!ctx || !r || !r1) return fail(ctx, MG_ERR_ARG, "null argument");
+  const size_t nb = 3 * (size_t)ctx->ns * sizeof(double);
+  CK(cudaMemcpyAsync(ctx->d_r, r, nb, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_r1, r1, nb, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->have_state = true;
+  return MG_OK;
+}
+
+int mg_md_get_state(mg_ctx* ctx, double* r, double* r1) {
+  if (!ctx || !ctx->have_state) return fail(ctx, MG_ERR_ARG, "no MD state");
+  const size_t nb = 3 * (size_t)ctx->ns * sizeof(double);
+  if (r) CK(cudaMemcpyAsync(r, ctx->d_r, nb, cudaMemcpyDeviceToHost, ctx->stream));
+  if (r1) CK(cudaMemcpyAsync(r1, ctx->d_r1, nb, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return MG_OK;
+}
+
+int mg_md_steps(mg_ctx* ctx, int nsteps, mg_energy* en) {
+  if (!ctx || !ctx->have_state || nsteps < 0) return fail(ctx, MG_ERR_ARG, "no MD state");
+  ctx->launches = 0;
+  Launch L = launch(ctx);
+  ShakeArgs sa;
+  sa.nmol = ctx->nmol;
+  sa.mol_first = ctx->d_mol_first;
+  sa.mol_cfirst = ctx->d_mol_cfirst;
+  sa.cons = ctx->d_cons;
+  sa.bondq = ctx->d_bondq;
+  sa.imass = ctx->d_imass;
+  sa.mass = ctx->d_mass;
+  sa.hh = ctx->h * ctx->h;
+  sa.eps = ctx->epsc;
+  sa.omega = ctx->omega;
+  sa.maxit = ctx->shake_maxit;
+  sa.r = ctx->d_r;
+  sa.r1 = ctx->d_r1;
+  sa.f = ctx->d_f;
+  sa.p = ctx->d_p;
+  sa.kin_part = ctx->d_kinpart;
+  sa.status = ctx->d_status;
+  const int nkin = (ctx->nmol + 127) / 128;
+  for (int s = 0; s < nsteps; s++) {
+    const bool last = s == nsteps - 1;
+    const bool measure = last && en != nullptr;
+    int rc = forces_async(ctx, ctx->d_r, ctx->d_f, measure);
+    if (rc) return rc;
+    PROF("shake", k_shake(L, sa));
+    if (measure) PROF("reduce", k_reduce_sum(L, ctx->d_kinpart, nkin, 1, ctx->d_sums + 17));
+  }
+  if (en) {
+    int rc = fetch_sums(ctx);
+    if (rc) return rc;
+  }
+  int hstatus = 0;
+  CK(cudaMemcpyAsync(&hstatus, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  prof_resolve(ctx);
+  if (hstatus) {
+    cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream);
+    return fail(ctx, MG_ERR_SHAKE, "SHAKE: too many iterations");
+  }
+  if (en) {
+    fill_energy(ctx, en);
+    en->ekin = ctx->h_sums[17] / (ctx->h * ctx->h) / 4;
+  }
+  return MG_OK;
+}
+
+int mg_set_stream(mg_ctx* ctx, void* stream) {
+  if (!ctx) return MG_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+  return MG_OK;
+}
+
+int mg_profile_enable(mg_ctx* ctx, int on) {
+  if (!ctx) return MG_ERR_ARG;
+  ctx->prof_on = on != 0;
+  return MG_OK;
+}
+
+int mg_profile_reset(mg_ctx* ctx) {
+  if (!ctx) return MG_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  prof_resolve(ctx);
+  for (size_t i = 0; i < ctx->pms.size(); i++) {
+    ctx->pms[i] = 0;
+    ctx->pcnt[i] = 0;
+  }
+  return MG_OK;
+}
+
+int mg_profile_entry(mg_ctx* ctx, int i, const char** name, double* ms, long* count) {
+  if (!ctx || i < 0 || i >= (int)ctx->pnames.size()) return MG_ERR_ARG;
+  if (name) *name = ctx->pnames[i].c_str();
+  if (ms) *ms = ctx->pms[i];
+  if (count) *count = ctx->pcnt[i];
+  return MG_OK;
+}
+
+int mg_probe_fp32_tflops(double* tflops) {
+  mg_ctx* ctx = nullptr;
+  if (!tflops) return MG_ERR_ARG;
+  int dev = 0, nsm = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  float* buf = nullptr;
+  cudaStream_t s;
+  cudaEvent_t a, b;
+  CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  const int blocks = nsm * 8, threads = 256, iters = 1 << 14;
+  CK(cudaMalloc(&buf, sizeof(float) * blocks * threads));
+  double best = 0;
+  for (int rep = 0; rep < 4; rep++) {
+    CK(cudaEventRecord(a, s));
+    CK(k_fma_probe(s, blocks, threads, iters, buf));
+    CK(cudaEventRecord(b, s));
+    CK(cudaEventSynchronize(b));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, a, b));
+    double fl = 2.0 * 8 * (double)iters * blocks * threads;
+    if (rep > 0 && ms > 0) best = std::max(best, fl / (ms * 1e-3) / 1e12);
+  }
+  cudaFree(buf);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaStreamDestroy(s);
+  *tflops = best;
+  return MG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,134 @@
+// Internal declarations shared by the host tables, the kernels and the C ABI.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+namespace mg {
+
+// smoothed LJ constants of one type pair (cook's sitesite_t)
+struct PairLJ {
+  double C1q, C2q, A, A4, Sq, E4, E24, E48;
+};
+
+void combining_rule(double E0, double R0, double a0, double E1, double R1, double a1,
+                    int comb_rule, double* eps, double* sig);
+int smooth_lj(double eps, double sig, double C2, PairLJ* p);
+int erfc_table_size(int grid, double maxr, double alpha);
+void erfc_table(int grid, double maxr, double cutoff, double alpha, int shift,
+                std::vector<double>* tab, double* sgrid);
+int kvector_set(const double L[3], double* kappa, std::vector<int>* kv);
+
+// ---------------------------------------------------------------- device --
+
+// per pair-of-kinds constants (kind = LJ type x charge class); FP32 copy
+struct PairF {
+  float C1q, C2q, A4, E24;   // force
+  float Sq, qq, A, E4;       // + energy
+};
+struct PairD {
+  double C1q, C2q, A4, E24, Sq, qq, A, E4;
+};
+
+// one k-space task: a run of <=KZT consecutive kz of one (kx,ky) column
+struct KTask {
+  int kx, ky, kz0, n;   // first kz and count
+  int k0;               // index of (kx,ky,kz0) in the k list
+  int pad[3];
+};
+// a (kx,ky) column of the k list
+struct KCol {
+  int kx, ky, kz0, n, k0, pad[3];
+};
+
+constexpr int KZT = 4;          // kz per pass-1 thread
+constexpr int PAIR_THREADS = 128;
+constexpr int MAX_KINDS = 16;
+
+struct Launch {
+  cudaStream_t s;
+  int* counter;  // number of kernel launches (diagnostics)
+};
+
+// kernels (mg_kernels.cu); each returns cudaGetLastError()
+cudaError_t k_prep_cells(const Launch& L, int ns, const double* r, const double* Lbox,
+                         double Lx, double Ly, double Lz, int ncx, int ncy, int ncz,
+                         int* cellkey, int* idx);
+cudaError_t k_cell_bounds(const Launch& L, int ns, int ncell, const int* key_sorted,
+                          int* cell_start);
+cudaError_t k_gather_mixed(const Launch& L, int ns, const double* r, const int* order,
+                           const int* kind, const int* mol, double Lx, double Ly, double Lz,
+                           int4* pj);
+cudaError_t k_gather_fp64(const Launch& L, int ns, const double* r, const int* order,
+                          const int* kind, const int* mol, double Lx, double Ly, double Lz,
+                          double4* pd);
+
+struct PairArgs {
+  int ns, ncx, ncy, ncz, nstencil, nkind;
+  const int* cell_start;
+  const int* order;         // sorted -> site
+  const int4* stencil;      // dx,dy,dz
+  double Lx, Ly, Lz;
+  double cutoff_sq;
+  double sgrid;
+  double alpha;
+  double* f;                // [3*ns] output (original order), overwritten
+  double* epart;            // [nblocks*10] partial energies (measure)
+};
+cudaError_t k_pair_mixed(const Launch& L, const PairArgs& a, const int4* pj,
+                         const PairF* ptab, const float4* erd, const float4* eru,
+                         bool measure);
+cudaError_t k_pair_fp64(const Launch& L, const PairArgs& a, const double4* pd,
+                        const PairD* ptab, const double* ertab, bool measure);
+
+struct KArgs {
+  int nq, nk, ntask, ncol, nchunk;
+  int Kx, Ky, Kz, row;      // table extents; row = (Kx+1)+(2Ky+1)+(2Kz+1)
+  double Lx, Ly, Lz;
+  double alpha;
+  const int* qsite;         // [nq] site of each charge
+  const double* qval;       // [nq]
+  const KTask* task;
+  const KCol* col;
+  const int4* kvec;         // [nk] kx,ky,kz
+  const double* ekk;        // [nk]
+  double* S;                // [2*nk] structure factor (FP64)
+  float2* Wf;               // [nk] ekk conj(S) for the mixed back-transform (or NULL)
+  double2* Wd;              // [nk] the same in FP64 (or NULL)
+  double* f;                // forces (added)
+  double* ek_part;          // [nk-blocks * 7] energy + virial partials
+};
+cudaError_t k_phase_tables_mixed(const Launch& L, const KArgs& a, const double* r, float2* tab);
+cudaError_t k_phase_tables_fp64(const Launch& L, const KArgs& a, const double* r, double2* tab);
+cudaError_t k_sk_mixed(const Launch& L, const KArgs& a, const float2* tab, float2* part);
+cudaError_t k_sk_fp64(const Launch& L, const KArgs& a, const double2* tab, double2* part);
+cudaError_t k_sk_reduce_mixed(const Launch& L, const KArgs& a, const float2* part, bool measure);
+cudaError_t k_sk_reduce_fp64(const Launch& L, const KArgs& a, const double2* part, bool measure);
+cudaError_t k_kforce_mixed(const Launch& L, const KArgs& a, const float2* tab);
+cudaError_t k_kforce_fp64(const Launch& L, const KArgs& a, const double2* tab);
+cudaError_t k_reduce_sum(const Launch& L, const double* part, int nrows, int width, double* out);
+
+struct ShakeArgs {
+  int nmol;
+  const int* mol_first;
+  const int* mol_cfirst;
+  const int2* cons;
+  const double* bondq;
+  const double* imass;
+  const double* mass;
+  double hh, eps, omega;
+  int maxit;
+  double* r;
+  double* r1;
+  const double* f;
+  double* p;           // scratch [3*ns]
+  double* kin_part;    // [nblocks]
+  int* status;         // set to 1 on non-convergence
+};
+cudaError_t k_shake(const Launch& L, const ShakeArgs& a);
+cudaError_t k_fma_probe(cudaStream_t s, int blocks, int threads, int iters, float* out);
+
+}  // namespace mg

@@ -1,0 +1,845 @@
+// sm_103a kernels of the cook force path.
+//
+//   cell list      k_prep_cells + (CUB radix sort) + k_cell_bounds + k_gather_*
+//   r-space sum    k_pair_mixed / k_pair_fp64: one CTA per home cell, its warps
+//                  split the neighbour-cell stencil; neighbour cells are staged
+//                  per warp in shared memory (16-byte loads) and every lane owns
+//                  one home-cell site (full shell: each pair is evaluated from
+//                  both ends, so no atomics and a fixed summation order).
+//   k-space        k_phase_tables_* (per-charge e^{2 pi i n x/L} rows),
+//                  k_sk_* (structure factor, FP32 partial sums per charge chunk),
+//                  k_sk_reduce_* (FP64 sum of the partials, energy, virial),
+//                  k_kforce_* (force back-transform, one thread per charge)
+//   integrator     k_shake: leap-frog + SHAKE sweeps, one thread per molecule
+//
+// Mixed precision: positions enter the pair kernel as 32-bit fixed-point
+// fractions of the box, so the nearest-image difference is an exact integer
+// subtraction; pair arithmetic is FP32; per-site sums are carried in FP32
+// within a neighbour-cell batch and folded into FP64; all global reductions
+// are FP64 in a fixed order.
+#include "mg_internal.h"
+
+#include <cub/device/device_radix_sort.cuh>
+
+namespace mg {
+
+#define LAUNCHED(L) (++*(L).counter)
+
+static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
+
+// ------------------------------------------------------------- cell list --
+
+__device__ __forceinline__ double wrap01(double s) { return s - floor(s); }
+
+__global__ void prep_cells_kernel(int ns, const double* __restrict__ r, double Lx, double Ly,
+                                  double Lz, int ncx, int ncy, int ncz, int* __restrict__ key,
+                                  int* __restrict__ idx) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ns) return;
+  double sx = wrap01(r[3 * i] / Lx), sy = wrap01(r[3 * i + 1] / Ly), sz = wrap01(r[3 * i + 2] / Lz);
+  int cx = min((int)(sx * ncx), ncx - 1), cy = min((int)(sy * ncy), ncy - 1),
+      cz = min((int)(sz * ncz), ncz - 1);
+  key[i] = (cx * ncy + cy) * ncz + cz;
+  idx[i] = i;
+}
+
+cudaError_t k_prep_cells(const Launch& L, int ns, const double* r, const double*, double Lx,
+                         double Ly, double Lz, int ncx, int ncy, int ncz, int* cellkey, int* idx) {
+  prep_cells_kernel<<<cdiv(ns, 256), 256, 0, L.s>>>(ns, r, Lx, Ly, Lz, ncx, ncy, ncz, cellkey, idx);
+  LAUNCHED(L);
+  return cudaGetLastError();
+}
+
+__global__ void cell_bounds_kernel(int ns, int ncell, const int* __restrict__ key,
+                                   int* __restrict__ start) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ns) return;
+  int k = key[t];
+  int prev = t ? key[t - 1] : -1;
+  for (int c = prev + 1; c <= k; c++) start[c] = t;
+  if (t == ns - 1)
+    for (int c = k + 1; c <= ncell; c++) start[c] = ns;
+}
+
+cudaError_t k_cell_bounds(const Launch& L, int ns, int ncell, const int* key_sorted,
+                          int* cell_start) {
+  cell_bounds_kernel<<<cdiv(ns, 256), 256, 0, L.s>>>(ns, ncell, key_sorted, cell_start);
+  LAUNCHED(L);
+  return cudaGetLastError();
+}
+
+__device__ __forceinline__ int fixed32(double x, double Lb) {
+  double s = wrap01(x / Lb);
+  long long v = llrint(s * 4294967296.0);
+  return (int)(unsigned int)(v & 0xffffffffLL);
+}
+
+__global__ void gather_mixed_kernel(int ns, const double* __restrict__ r,
+                                    const int* __restrict__ order, const int* __restrict__ kind,
+                                    const int* __restrict__ mol, double Lx, double Ly, double Lz,
+                                    int4* __restrict__ pj) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ns) return;
+  int i = order[t];
+  pj[t] = make_int4(fixed32(r[3 * i], Lx), fixed32(r[3 * i + 1], Ly), fixed32(r[3 * i + 2], Lz),
+                    (mol[i] << 8) | kind[i]);
+}
+
+cudaError_t k_gather_mixed(const Launch& L, int ns, const double* r, const int* order,
+                           const int* kind, const int* mol, double Lx, double Ly, double Lz,
+                           int4* pj) {
+  gather_mixed_kernel<<<cdiv(ns, 256), 256, 0, L.s>>>(ns, r, order, kind, mol, Lx, Ly, Lz, pj);
+  LAUNCHED(L);
+  return cudaGetLastError();
+}
+
+__global__ void gather_fp64_kernel(int ns, const double* __restrict__ r,
+                                   const int* __restrict__ order, const int* __restrict__ kind,
+                                   const int* __restrict__ mol, double Lx, double Ly, double Lz,
+                                   double4* __restrict__ pd) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ns) return;
+  int i = order[t];
+  double x = r[3 * i], y = r[3 * i + 1], z = r[3 * i + 2];
+  x -= Lx * floor(x / Lx);
+  y -= Ly * floor(y / Ly);
+  z -= Lz * floor(z / Lz);
+  pd[t] = make_double4(x, y, z, __longlong_as_double((long long)((mol[i] << 8) | kind[i])));
+}
+
+cudaError_t k_gather_fp64(const Launch& L, int ns, const double* r, const int* order,
+                          const int* kind, const int* mol, double Lx, double Ly, double Lz,
+                          double4* pd) {
+  gather_fp64_kernel<<<cdiv(ns, 256), 256, 0, L.s>>>(ns, r, order, kind, mol, Lx, Ly, Lz, pd);
+  LAUNCHED(L);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------- pair kernels --
+
+constexpr int NWARP = PAIR_THREADS / 32;
+constexpr int FOLD = 8;   // stencil cells per FP32 batch before the FP64 fold
+constexpr int NEN = 10;   // er, lj, vir, Pvir[6], (spare)
+
+// Ewald exclusion term -erf(alpha r)/r and its f/r (cook's exacterud_sqrt)
+template <typename T>
+__device__ __forceinline__ T excl_term(T rr, T alpha, T* erd) {
+  const T A = alpha * (T)(-1.1283791670955126);  // -2 alpha/sqrt(pi)
+  T aq = alpha * alpha, err = aq * rr;
+  if (err < (T)0.01) {
+    // Taylor series of erf(x)/x in x^2, as the reference does for short pairs
+    T su = 0, sd = 0, q = 1;
+    for (int n = 1; n < 40; n++) {
+      T rn = q / (T)(2 * n + 1);
+      sd += rn * (T)n;
+      su += rn;
+      if (fabs(q) < (T)1e-16) break;
+      q *= -err / (T)(n + 1);
+    }
+    *erd = A * aq * 2 * sd;
+    return A * (1 - su * err);
+  }
+  T r = sqrt(rr);
+  T y = -erf(alpha * r) / r;
+  *erd = (y - A * exp(-err)) / rr;
+  return y;
+}
+
+template <bool MEASURE>
+__global__ void __launch_bounds__(PAIR_THREADS)
+    pair_mixed_kernel(PairArgs a, const int4* __restrict__ pj, const PairF* __restrict__ ptab_g,
+                      const float4* __restrict__ erd, const float4* __restrict__ eru, float sx,
+                      float sy, float sz, float cq, float sgrid, float alpha) {
+  __shared__ PairF ptab[MAX_KINDS * MAX_KINDS];
+  __shared__ int4 sj[NWARP][32];
+  __shared__ double red[NWARP][32][3];
+  __shared__ double ered[PAIR_THREADS];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nk = a.nkind;
+  for (int t = threadIdx.x; t < nk * nk; t += PAIR_THREADS) ptab[t] = ptab_g[t];
+  __syncthreads();
+
+  const int c = blockIdx.x;
+  const int cz = c % a.ncz, cy = (c / a.ncz) % a.ncy, cx = c / (a.ncy * a.ncz);
+  const int i0 = a.cell_start[c], ni = a.cell_start[c + 1] - i0;
+  double en[NEN];
+#pragma unroll
+  for (int k = 0; k < NEN; k++) en[k] = 0;
+
+  for (int ib = 0; ib < ni; ib += 32) {
+    const bool vi = ib + lane < ni;
+    const int ti = i0 + ib + lane;
+    const int4 me = vi ? pj[ti] : make_int4(0, 0, 0, 0);
+    const int kind_i = me.w & 255, mol_i = me.w >> 8;
+    double fx = 0, fy = 0, fz = 0;
+    float ax = 0, ay = 0, az = 0;
+    float e_el = 0, e_lj = 0, e_vir = 0, p0 = 0, p1 = 0, p2 = 0, p3 = 0, p4 = 0, p5 = 0;
+    int nb = 0;
+    for (int s = warp; s < a.nstencil; s += NWARP) {
+      const int4 o = a.stencil[s];
+      int x2 = cx + o.x, y2 = cy + o.y, z2 = cz + o.z;
+      x2 += (x2 < 0) ? a.ncx : (x2 >= a.ncx ? -a.ncx : 0);
+      y2 += (y2 < 0) ? a.ncy : (y2 >= a.ncy ? -a.ncy : 0);
+      z2 += (z2 < 0) ? a.ncz : (z2 >= a.ncz ? -a.ncz : 0);
+      const int c2 = (x2 * a.ncy + y2) * a.ncz + z2;
+      const int j0 = a.cell_start[c2], nj = a.cell_start[c2 + 1] - j0;
+      for (int jb = 0; jb < nj; jb += 32) {
+        if (jb + lane < nj) sj[warp][lane] = pj[j0 + jb + lane];
+        __syncwarp();
+        const int cnt = min(32, nj - jb);
+        for (int jj = 0; jj < cnt; jj++) {
+          const int4 q = sj[warp][jj];
+          const float dx = (float)(me.x - q.x) * sx;
+          const float dy = (float)(me.y - q.y) * sy;
+          const float dz = (float)(me.z - q.z) * sz;
+          const float rr = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+          if (!vi || rr >= cq || j0 + jb + jj == ti) continue;
+          const PairF P = ptab[kind_i * nk + (q.w & 255)];
+          float f = 0;
+          if ((q.w >> 8) == mol_i) {
+            if (P.qq != 0.f) {
+              float fe;
+              float e = excl_term<float>(rr, alpha, &fe);
+              f = fe * P.qq;
+              if (MEASURE) e_el += e * P.qq;
+            }
+          } else {
+            if (rr < P.C2q) {
+              float U;
+              if (rr < P.C1q) {
+                const float x = P.Sq / rr, y = x * x * x;
+                f = P.E24 * fmaf(2.f * y, y, -y) * x;
+                U = P.E4 * fmaf(y, y, -y);
+              } else {
+                const float x = rr - P.C2q;
+                f = P.A4 * x;
+                U = P.A * x * x;
+              }
+              if (MEASURE) {
+                e_lj += U;
+                e_vir += rr * f;
+              }
+            }
+            if (P.qq != 0.f) {
+              const int ix = (int)(rr * sgrid);
+              const float4 d = __ldg(erd + ix);
+              f = fmaf(__fdividef(d.y, d.z + rr) + d.x, P.qq, f);
+              if (MEASURE) {
+                const float4 u = __ldg(eru + ix);
+                e_el += (__fdividef(u.y, u.z + rr) + u.x) * P.qq;
+              }
+            }
+          }
+          const float fdx = f * dx, fdy = f * dy, fdz = f * dz;
+          ax += fdx;
+          ay += fdy;
+          az += fdz;
+          if (MEASURE) {
+            p0 = fmaf(dx, fdx, p0);
+            p1 = fmaf(dy, fdy, p1);
+            p2 = fmaf(dz, fdz, p2);
+            p3 = fmaf(dz, fdy, p3);
+            p4 = fmaf(dx, fdz, p4);
+            p5 = fmaf(dy, fdx, p5);
+          }
+        }
+        __syncwarp();
+      }
+      if (++nb == FOLD) {
+        nb = 0;
+        fx += ax; fy += ay; fz += az;
+        ax = ay = az = 0;
+        if (MEASURE) {
+          en[0] += e_el; en[1] += e_lj; en[2] += e_vir;
+          en[3] += p0; en[4] += p1; en[5] += p2; en[6] += p3; en[7] += p4; en[8] += p5;
+          e_el = e_lj = e_vir = p0 = p1 = p2 = p3 = p4 = p5 = 0;
+        }
+      }
+    }
+    fx += ax; fy += ay; fz += az;
+    if (MEASURE) {
+      en[0] += e_el; en[1] += e_lj; en[2] += e_vir;
+      en[3] += p0; en[4] += p1; en[5] += p2; en[6] += p3; en[7] += p4; en[8] += p5;
+    }
+    red[warp][lane][0] = fx;
+    red[warp][lane][1] = fy;
+    red[warp][lane][2] = fz;
+    __syncthreads();
+    if (warp == 0 && vi) {
+      double gx = 0, gy = 0, gz = 0;
+#pragma unroll
+      for (int w = 0; w < NWARP; w++) {
+        gx += red[w][lane][0];
+        gy += red[w][lane][1];
+        gz += red[w][lane][2];
+      }
+      const int site = a.order[ti];
+      a.f[3 * site] = gx;
+      a.f[3 * site + 1] = gy;
+      a.f[3 * site + 2] = gz;
+    }
+    __syncthreads();
+  }
+  if (MEASURE) {
+    // each unordered pair was visited from both ends
+    for (int k = 0; k < 9; k++) {
+      ered[threadIdx.x] = 0.5 * en[k];
+      __syncthreads();
+      for (int w = PAIR_THREADS / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) ered[threadIdx.x] += ered[threadIdx.x + w];
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) a.epart[blockIdx.x * NEN + k] = ered[0];
+      __syncthreads();
+    }
+  }
+}
+
+cudaError_t k_pair_mixed(const Launch& L, const PairArgs& a, const int4* pj, const PairF* ptab,
+                         const float4* erd, const float4* eru, bool measure) {
+  int ncell = a.ncx * a.ncy * a.ncz;
+  float sx = (float)(a.Lx / 4294967296.0), sy = (float)(a.Ly / 4294967296.0),
+        sz = (float)(a.Lz / 4294967296.0);
+  if (measure)
+    pair_mixed_kernel<true><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pj, ptab, erd, eru, sx, sy, sz,
+                                                             (float)a.cutoff_sq, (float)a.sgrid,
+                                                             (float)a.alpha);
+  else
+    pair_mixed_kernel<false><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pj, ptab, erd, eru, sx, sy, sz,
+                                                              (float)a.cutoff_sq, (float)a.sgrid,
+                                                              (float)a.alpha);
+  LAUNCHED(L);
+  return cudaGetLastError();
+}
+
+template <bool MEASURE>
+__global__ void __launch_bounds__(PAIR_THREADS)
+    pair_fp64_kernel(PairArgs a, const double4* __restrict__ pd, const PairD* __restrict__ ptab_g,
+                     const double* __restrict__ ert) {
+  __shared__ PairD ptab[MAX_KINDS * MAX_KINDS];
+  __shared__ double4 sj[NWARP][32];
+  __shared__ double red[NWARP][32][3];
+  __shared__ double ered[PAIR_THREADS];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nk = a.nkind;
+  for (int t = threadIdx.x; t < nk * nk; t += PAIR_THREADS) ptab[t] = ptab_g[t];
+  __syncthreads();
+  const int c = blockIdx.x;
+  const int cz = c % a.ncz, cy = (c / a.ncz) % a.ncy, cx = c / (a.ncy * a.ncz);
+  const int i0 = a.cell_start[c], ni = a.cell_start[c + 1] - i0;
+  const double cq = a.cutoff_sq, sgrid = a.sgrid, alpha = a.alpha;
+  double en[NEN];
+#pragma unroll
+  for (int k = 0; k < NEN; k++) en[k] = 0;
+  for (int ib = 0; ib < ni; ib += 32) {
+    const bool vi = ib + lane < ni;
+    const int ti = i0 + ib + lane;
+    const double4 me = vi ? pd[ti] : make_double4(0, 0, 0, 0);
+    const long long wi = __double_as_longlong(me.w);
+    const int kind_i = (int)(wi & 255), mol_i = (int)(wi >> 8);
+    double fx = 0, fy = 0, fz = 0;
+    for (int s = warp; s < a.nstencil; s += NWARP) {
+      const int4 o = a.stencil[s];
+      int x2 = cx + o.x, y2 = cy + o.y, z2 = cz + o.z;
+      double shx = 0, shy = 0, shz = 0;
+      if (x2 < 0) { x2 += a.ncx; shx = -a.Lx; } else if (x2 >= a.ncx) { x2 -= a.ncx; shx = a.Lx; }
+      if (y2 < 0) { y2 += a.ncy; shy = -a.Ly; } else if (y2 >= a.ncy) { y2 -= a.ncy; shy = a.Ly; }
+      if (z2 < 0) { z2 += a.ncz; shz = -a.Lz; } else if (z2 >= a.ncz) { z2 -= a.ncz; shz = a.Lz; }
+      const double xs = me.x - shx, ys = me.y - shy, zs = me.z - shz;
+      const int c2 = (x2 * a.ncy + y2) * a.ncz + z2;
+      const int j0 = a.cell_start[c2], nj = a.cell_start[c2 + 1] - j0;
+      for (int jb = 0; jb < nj; jb += 32) {
+        if (jb + lane < nj) sj[warp][lane] = pd[j0 + jb + lane];
+        __syncwarp();
+        const int cnt = min(32, nj - jb);
+        for (int jj = 0; jj < cnt; jj++) {
+          const double4 q = sj[warp][jj];
+          const double dx = xs - q.x, dy = ys - q.y, dz = zs - q.z;
+          const double rr = dx * dx + dy * dy + dz * dz;
+          if (!vi || rr >= cq || j0 + jb + jj == ti) continue;
+          const long long wj = __double_as_longlong(q.w);
+          const PairD& P = ptab[kind_i * nk + (int)(wj & 255)];
+          double f = 0;
+          if ((int)(wj >> 8) == mol_i) {
+            if (P.qq != 0) {
+              double fe;
+              double e = excl_term<double>(rr, alpha, &fe);
+              f = fe * P.qq;
+              if (MEASURE) en[0] += e * P.qq;
+            }
+          } else {
+            if (rr < P.C2q) {
+              double U;
+              if (rr < P.C1q) {
+                const double x = P.Sq / rr, y = x * x * x, z = y * y;
+                f = P.E24 * (z + z - y) * x;
+                U = P.E4 * (z - y);
+              } else {
+                const double x = rr - P.C2q;
+                f = P.A4 * x;
+                U = x * x * P.A;
+              }
+              if (MEASURE) {
+                en[1] += U;
+                en[2] += rr * f;
+              }
+            }
+            if (P.qq != 0) {
+              const double* e = ert + 6 * (int)(rr * sgrid);
+              f += (e[4] / (e[5] + rr) + e[3]) * P.qq;
+              if (MEASURE) en[0] += (e[1] / (e[2] + rr) + e[0]) * P.qq;
+            }
+          }
+          const double fdx = f * dx, fdy = f * dy, fdz = f * dz;
+          fx += fdx;
+          fy += fdy;
+          fz += fdz;
+          if (MEASURE) {
+            en[3] += dx * fdx;
+            en[4] += dy * fdy;
+            en[5] += dz * fdz;
+            en[6] += dz * fdy;
+            en[7] += dx * fdz;
+            en[8] += dy * fdx;
+          }
+        }
+        __syncwarp();
+      }
+    }
+    red[warp][lane][0] = fx;
+    red[warp][lane][1] = fy;
+    red[warp][lane][2] = fz;
+    __syncthreads();
+    if (warp == 0 && vi) {
+      double gx = 0, gy = 0, gz = 0;
+#pragma unroll
+      for (int w = 0; w < NWARP; w++) {
+        gx += red[w][lane][0];
+        gy += red[w][lane][1];
+        gz += red[w][lane][2];
+      }
+      const int site = a.order[ti];
+      a.f[3 * site] = gx;
+      a.f[3 * site + 1] = gy;
+      a.f[3 * site + 2] = gz;
+    }
+    __syncthreads();
+  }
+  if (MEASURE) {
+    for (int k = 0; k < 9; k++) {
+      ered[threadIdx.x] = 0.5 * en[k];
+      __syncthreads();
+      for (int w = PAIR_THREADS / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) ered[threadIdx.x] += ered[threadIdx.x + w];
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) a.epart[blockIdx.x * NEN + k] = ered[0];
+      __syncthreads();
+    }
+  }
+}
+
+cudaError_t k_pair_fp64(const Launch& L, const PairArgs& a, const double4* pd, const PairD* ptab,
+                        const double* ertab, bool measure) {
+  int ncell = a.ncx * a.ncy * a.ncz;
+  if (measure)
+    pair_fp64_kernel<true><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pd, ptab, ertab);
+  else
+    pair_fp64_kernel<false><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pd, ptab, ertab);
+  LAUNCHED(L);
+  return cudaGetLastError();
+}
+
+// --------------------------------------------------------------- k-space --
+
+// Row of charge j: [q e^{2 pi i kx sx}, kx=0..Kx | e^{2 pi i ky sy}, ky=-Ky..Ky |
+//                   e^{2 pi i kz sz}, kz=-Kz..Kz]
+__global__ void phase_tables_mixed_kernel(KArgs a, const double* __restrict__ r,
+                                          float2* __restrict__ tab) {
+  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)a.nq * a.row) return;
+  int j = (int)(t / a.row), e = (int)(t % a.row);
+  int site = a.qsite[j];
+  int d, n;
+  if (e <= a.Kx) { d = 0; n = e; }
+  else if (e <= a.Kx + 2 * a.Ky + 1) { d = 1; n = e - (a.Kx + 1) - a.Ky; }
+  else { d = 2; n = e - (a.Kx + 2 * a.Ky + 2) - a.Kz; }
+  double Lb = d == 0 ? a.Lx : (d == 1 ? a.Ly : a.Lz);
+  // exact integer phase n*s mod 1 in units of 2^-32
+  unsigned int S = (unsigned int)fixed32(r[3 * site + d], Lb);
+  int ph = (int)(S * (unsigned int)n);
+  float tt = (float)ph * 2.3283064365386963e-10f;   // in [-0.5, 0.5)
+  float sn, cs;
+  sincospif(2.f * tt, &sn, &cs);
+  if (d == 0) {
+    float q = (float)a.qval[j];
+    cs *= q;
+    sn *= q;
+  }
+  tab[t] = make_float2(cs, sn);
+}
+
+__global__ void phase_tables_fp64_kernel(KArgs a, const double* __restrict__ r,
+                                         double2* __restrict__ tab) {
+  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)a.nq * a.row) return;
+  int j = (int)(t / a.row), e = (int)(t % a.row);
+  int site = a.qsite[j];
+  int d, n;
+  if (e <= a.Kx) { d = 0; n = e; }
+  else if (e <= a.Kx + 2 * a.Ky + 1) { d = 1; n = e - (a.Kx + 1) - a.Ky; }
+  else { d = 2; n = e - (a.Kx + 2 * a.Ky + 2) - a.Kz; }
+  double Lb = d == 0 ? a.Lx : (d == 1 ? a.Ly : a.Lz);
+  double s = r[3 * site + d] / Lb;
+  double ph = n * s;
+  ph -= rint(ph);
+  double sn, cs;
+  sincospi(2.0 * ph, &sn, &cs);
+  if (d == 0) {
+    cs *= a.qval[j];
+    sn *= a.qval[j];
+  }
+  tab[t] = make_double2(cs, sn);
+}
+
+cudaError_t k_phase_tables_mixed(const Launch& L, const KArgs& a, const double* r, float2* tab) {
+  long n = (long)a.nq * a.row;
+  phase_tables_mixed_kernel<<<(int)((n + 255) / 256), 256, 0, L.s>>>(a, r, tab);
+  LAUNCHED(L);
+  return cudaGetLastError();
+}
+cudaError_t k_phase_tables_fp64(const Launch& L, const KArgs& a, const double* r, double2* tab) {
+  long n = (long)a.nq * a.row;
+  phase_tables_fp64_kernel<<<(int)((n + 255) / 256), 256, 0, L.s>>>(a, r, tab);
+  LAUNCHED(L);
+  return cudaGetLastError();
+}
+
+template <typename T2>
+struct CplxOps;
+template <>
+struct CplxOps<float2> {
+  typedef float T;
+  static __device__ __forceinline__ float2 mul(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+  }
+};
+template <>
+struct CplxOps<double2> {
+  typedef double T;
+  static __device__ __forceinline__ double2 mul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+  }
+};
+
+constexpr int SK_THREADS = 256;
+
+// pass 1: each thread owns one task (<=KZT consecutive kz of a column) and
+// sums q X Y Z over the charges of its chunk; charge rows are staged in
+// shared memory STAGE at a time.
+template <typename T2>
+__global__ void __launch_bounds__(SK_THREADS)
+    sk_kernel(KArgs a, const T2* __restrict__ tab, T2* __restrict__ part, int stage) {
+  extern __shared__ unsigned char smem_raw[];
+  T2* rows = reinterpret_cast<T2*>(smem_raw);
+  const int ch = blockIdx.y;
+  const int j0 = (int)((long)a.nq * ch / a.nchunk), j1 = (int)((long)a.nq * (ch + 1) / a.nchunk);
+  const int tk = blockIdx.x * SK_THREADS + threadIdx.x;
+  const bool valid = tk < a.ntask;
+  KTask tsk = valid ? a.task[tk] : KTask{0, 0, 0, 0, 0, {0, 0, 0}};
+  const int ix = tsk.kx, iy = a.Kx + 1 + a.Ky + tsk.ky,
+            iz = a.Kx + 2 * a.Ky + 2 + a.Kz + tsk.kz0;
+  T2 S[KZT];
+#pragma unroll
+  for (int m = 0; m < KZT; m++) S[m] = T2{0, 0};
+  for (int js = j0; js < j1; js += stage) {
+    const int nst = min(stage, j1 - js);
+    __syncthreads();
+    for (int t = threadIdx.x; t < nst * a.row; t += SK_THREADS)
+      rows[t] = tab[(long)js * a.row + t];
+    __syncthreads();
+    if (valid) {
+      for (int jj = 0; jj < nst; jj++) {
+        const T2* R = rows + jj * a.row;
+        const T2 U = CplxOps<T2>::mul(R[ix], R[iy]);
+#pragma unroll
+        for (int m = 0; m < KZT; m++) {
+          if (m < tsk.n) {
+            const T2 Z = R[iz + m];
+            const T2 p = CplxOps<T2>::mul(U, Z);
+            S[m].x += p.x;
+            S[m].y += p.y;
+          }
+        }
+      }
+    }
+  }
+  if (valid) {
+#pragma unroll
+    for (int m = 0; m < KZT; m++)
+      if (m < tsk.n) part[(long)ch * a.nk + tsk.k0 + m] = S[m];
+  }
+}
+
+template <typename T2>
+static cudaError_t launch_sk(const Launch& L, const KArgs& a, const T2* tab, T2* part) {
+  int stage = (int)(40960 / (a.row * sizeof(T2)));
+  if (stage < 1) stage = 1;
+  if (stage > 64) stage = 64;
+  size_t smem = (size_t)stage * a.row * sizeof(T2);
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(sk_kernel<T2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  dim3 grid(cdiv(a.ntask, SK_THREADS), a.nchunk);
+  sk_kernel<T2><<<grid, SK_THREADS, smem, L.s>>>(a, tab, part, stage);
+  LAUNCHED(L);
+  return cudaGetLastError();
+}
+
+cudaError_t k_sk_mixed(const Launch& L, const KArgs& a, const float2* tab, float2* part) {
+  return launch_sk<float2>(L, a, tab, part);
+}
+cudaError_t k_sk_fp64(const Launch& L, const KArgs& a, const double2* tab, double2* part) {
+  return launch_sk<double2>(L, a, tab, part);
+}
+
+// S(k) = sum over chunks (FP64, fixed order); energy and virial per k
+// (sim/ewpass2m.c: E1 = |S|^2 ekk, ptf = 1/kk + (pi/alpha)^2) reduced per block
+template <typename T2>
+__global__ void sk_reduce_kernel(KArgs a, const T2* __restrict__ part, bool measure,
+                                 double pi2_over_a2) {
+  __shared__ double red[256][7];
+  const int k = blockIdx.x * 256 + threadIdx.x;
+  double e[7] = {0, 0, 0, 0, 0, 0, 0};
+  if (k < a.nk) {
+    double sr = 0, si = 0;
+    for (int c = 0; c < a.nchunk; c++) {
+      T2 v = part[(long)c * a.nk + k];
+      sr += v.x;
+      si += v.y;
+    }
+    a.S[2 * k] = sr;
+    a.S[2 * k + 1] = si;
+    const double ek = a.ekk[k];
+    if (a.Wf) a.Wf[k] = make_float2((float)(ek * sr), (float)(-ek * si));
+    if (a.Wd) a.Wd[k] = make_double2(ek * sr, -ek * si);
+    if (measure) {
+      const int4 kv = a.kvec[k];
+      const double kx = kv.x / a.Lx, ky = kv.y / a.Ly, kz = kv.z / a.Lz;
+      const double kk = kx * kx + ky * ky + kz * kz;
+      const double E1 = (sr * sr + si * si) * a.ekk[k];
+      const double ptf = 1 / kk + pi2_over_a2;
+      e[0] = E1;
+      e[1] = E1 * ptf * kx * kx;
+      e[2] = E1 * ptf * ky * ky;
+      e[3] = E1 * ptf * kz * kz;
+      e[4] = E1 * ptf * ky * kz;
+      e[5] = E1 * ptf * kx * kz;
+      e[6] = E1 * ptf * kx * ky;
+    }
+  }
+  if (!measure) return;
+  for (int m = 0; m < 7; m++) red[threadIdx.x][m] = e[m];
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int m = 0; m < 7; m++) red[threadIdx.x][m] += red[threadIdx.x + w][m];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int m = 0; m < 7; m++) a.ek_part[blockIdx.x * 7 + m] = red[0][m];
+}
+
+cudaError_t k_sk_reduce_mixed(const Launch& L, const KArgs& a, const float2* part, bool measure) {
+  const double pa = 9.869604401089358 / (a.alpha * a.alpha);
+  sk_reduce_kernel<float2><<<cdiv(a.nk, 256), 256, 0, L.s>>>(a, part, measure, pa);
+  LAUNCHED(L);
+  return cudaGetLastError();
+}
+cudaError_t k_sk_reduce_fp64(const Launch& L, const KArgs& a, const double2* part, bool measure) {
+  const double pa = 9.869604401089358 / (a.alpha * a.alpha);
+  sk_reduce_kernel<double2><<<cdiv(a.nk, 256), 256, 0, L.s>>>(a, part, measure, pa);
+  LAUNCHED(L);
+  return cudaGetLastError();
+}
+
+// pass 2 (sim/ewpass2.c + sim/ewaldf.c): F_j += sum_k ekk (k/L) Im(conj(S_k) q_j e^{2 pi i k.r_j/L}).
+// One thread per charge; the k list is walked column by column ((kx,ky) with
+// consecutive kz): the phase at the first kz of a column comes from the
+// per-charge rows (X Y Z products), later ones from the recurrence
+// P <- P e^{2 pi i z/L}.  Column sums are FP32, folded into FP64 every
+// KFOLD columns.
+constexpr int KF_THREADS = 128;
+constexpr int KFOLD = 16;
+
+template <typename T2>
+__global__ void __launch_bounds__(KF_THREADS)
+    kforce_kernel(KArgs a, const T2* __restrict__ tab, const T2* __restrict__ W) {
+  typedef typename CplxOps<T2>::T T;
+  const int j = blockIdx.x * KF_THREADS + threadIdx.x;
+  if (j >= a.nq) return;
+  const T2* R = tab + (long)j * a.row;
+  const int oy = a.Kx + 1 + a.Ky, oz = a.Kx + 2 * a.Ky + 2 + a.Kz;
+  const T2 ez = R[oz + 1];
+  double Fx = 0, Fy = 0, Fz = 0;
+  T gx = 0, gy = 0, gz = 0;
+  int nf = 0;
+  for (int c = 0; c < a.ncol; c++) {
+    const KCol col = a.col[c];
+    T2 P = CplxOps<T2>::mul(CplxOps<T2>::mul(R[col.kx], R[oy + col.ky]), R[oz + col.kz0]);
+    T G = 0, Gz = 0;
+    for (int m = 0; m < col.n; m++) {
+      // W_k = ekk conj(S_k): g = ekk Im(conj(S) P)
+      const T2 Wk = W[col.k0 + m];
+      const T g = Wk.x * P.y + Wk.y * P.x;
+      G += g;
+      Gz += (T)(col.kz0 + m) * g;
+      P = CplxOps<T2>::mul(P, ez);
+    }
+    gx += (T)col.kx * G;
+    gy += (T)col.ky * G;
+    gz += Gz;
+    if (++nf == KFOLD) {
+      nf = 0;
+      Fx += gx; Fy += gy; Fz += gz;
+      gx = gy = gz = 0;
+    }
+  }
+  Fx += gx; Fy += gy; Fz += gz;
+  const int site = a.qsite[j];
+  a.f[3 * site] += Fx / a.Lx;
+  a.f[3 * site + 1] += Fy / a.Ly;
+  a.f[3 * site + 2] += Fz / a.Lz;
+}
+
+cudaError_t k_kforce_mixed(const Launch& L, const KArgs& a, const float2* tab) {
+  kforce_kernel<float2><<<cdiv(a.nq, KF_THREADS), KF_THREADS, 0, L.s>>>(a, tab, a.Wf);
+  LAUNCHED(L);
+  return cudaGetLastError();
+}
+cudaError_t k_kforce_fp64(const Launch& L, const KArgs& a, const double2* tab) {
+  kforce_kernel<double2><<<cdiv(a.nq, KF_THREADS), KF_THREADS, 0, L.s>>>(a, tab, a.Wd);
+  LAUNCHED(L);
+  return cudaGetLastError();
+}
+
+// out[k] = sum over rows of part[row*width+k], fixed order (one CTA)
+__global__ void reduce_rows_kernel(const double* __restrict__ part, int nrows, int width,
+                                   double* __restrict__ out) {
+  __shared__ double red[256];
+  for (int k = 0; k < width; k++) {
+    double s = 0;
+    for (int r = threadIdx.x; r < nrows; r += 256) s += part[(long)r * width + k];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+      if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[k] = red[0];
+    __syncthreads();
+  }
+}
+
+cudaError_t k_reduce_sum(const Launch& L, const double* part, int nrows, int width, double* out) {
+  reduce_rows_kernel<<<1, 256, 0, L.s>>>(part, nrows, width, out);
+  LAUNCHED(L);
+  return cudaGetLastError();
+}
+
+// -------------------------------------------------------------- SHAKE --
+
+// sim/constrd.c:767-839 + sim/verlet.c:101-104 + sim/shakev3.c (SHAKE=1,
+// VERLET=3, no thermostat), one thread per molecule, FP64.
+constexpr int SH_THREADS = 128;
+
+__global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
+  __shared__ double red[SH_THREADS];
+  const int n = blockIdx.x * SH_THREADS + threadIdx.x;
+  double kin = 0;
+  if (n < a.nmol) {
+    const int i0 = a.mol_first[n], i1 = a.mol_first[n + 1];
+    const int c0 = a.mol_cfirst[n], c1 = a.mol_cfirst[n + 1];
+    double* p = a.p;
+    for (int i = i0; i < i1; i++)
+      for (int k = 0; k < 3; k++)
+        p[3 * i + k] = a.f[3 * i + k] * (a.hh * a.imass[i]) + a.r[3 * i + k] + a.r1[3 * i + k];
+    if (c1 > c0) {
+      int it = 0;
+      double maxsq;
+      do {
+        it++;
+        maxsq = 0;
+        for (int al = c0; al < c1; al++) {
+          const int2 ij = a.cons[al];
+          const double bq = a.bondq[al];
+          const double mi = a.imass[ij.x], mj = a.imass[ij.y];
+          double px = p[3 * ij.x] - p[3 * ij.y], py = p[3 * ij.x + 1] - p[3 * ij.y + 1],
+                 pz = p[3 * ij.x + 2] - p[3 * ij.y + 2];
+          double sq = bq - (px * px + py * py + pz * pz);
+          maxsq = fmax(maxsq, fabs(sq / bq));
+          sq *= a.omega / (mi + mj);
+          sq /= bq;
+          const double rx = (a.r[3 * ij.x] - a.r[3 * ij.y]) * sq,
+                       ry = (a.r[3 * ij.x + 1] - a.r[3 * ij.y + 1]) * sq,
+                       rz = (a.r[3 * ij.x + 2] - a.r[3 * ij.y + 2]) * sq;
+          p[3 * ij.x] += mi * rx;
+          p[3 * ij.x + 1] += mi * ry;
+          p[3 * ij.x + 2] += mi * rz;
+          p[3 * ij.y] -= mj * rx;
+          p[3 * ij.y + 1] -= mj * ry;
+          p[3 * ij.y + 2] -= mj * rz;
+        }
+      } while (maxsq > a.eps && it < a.maxit);
+      if (maxsq > a.eps) atomicExch(a.status, 1);
+    }
+    for (int i = i0; i < i1; i++) {
+      double v1s = 0, v2s = 0;
+      for (int k = 0; k < 3; k++) {
+        const double v1 = a.r1[3 * i + k], v2 = p[3 * i + k] - a.r[3 * i + k];
+        v1s += v1 * v1;
+        v2s += v2 * v2;
+        a.r1[3 * i + k] = v2;
+        a.r[3 * i + k] = p[3 * i + k];
+      }
+      kin += (v1s + v2s) * a.mass[i];
+    }
+  }
+  red[threadIdx.x] = kin;
+  __syncthreads();
+  for (int w = SH_THREADS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) a.kin_part[blockIdx.x] = red[0];
+}
+
+cudaError_t k_shake(const Launch& L, const ShakeArgs& a) {
+  shake_kernel<<<cdiv(a.nmol, SH_THREADS), SH_THREADS, 0, L.s>>>(a);
+  LAUNCHED(L);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------- FP32 probe --
+
+// 8 independent FMA chains per thread: the FP32 issue rate of the device
+__global__ void fma_probe_kernel(int iters, float* __restrict__ out) {
+  float x[8];
+  const float a = 0.999999f, b = 1e-7f;
+#pragma unroll
+  for (int k = 0; k < 8; k++) x[k] = (float)(threadIdx.x + k);
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int k = 0; k < 8; k++) x[k] = fmaf(x[k], a, b);
+  }
+  float s = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) s += x[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+cudaError_t k_fma_probe(cudaStream_t s, int blocks, int threads, int iters, float* out) {
+  fma_probe_kernel<<<blocks, threads, 0, s>>>(iters, out);
+  return cudaGetLastError();
+}
+
+}  // namespace mg

@@ -1,0 +1,114 @@
+"""GPU force path (through the C ABI) against the CPU oracle and the
+reference dumps.  Tolerances: FP64 path 1e-10 relative force RMS (the
+oracle itself matches cook's dumps to ~1e-12); mixed path 1e-5 relative
+force RMS against FP64, the bound the force path is specified to."""
+import numpy as np
+import pytest
+
+import macsimus_gb300 as M
+from golden_cases import CASES, load
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+MIXED_TOL = 1e-5
+
+
+def rel_rms(a, b):
+    return float(np.sqrt(((a - b) ** 2).sum() / (b ** 2).sum()))
+
+
+def make(case, precision, **kw):
+    g, meta, system, ew = load(case)
+    fp = M.ForcePath(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"],
+                     precision=precision, h=meta["params"]["h"], epsc=meta["params"]["epsc"],
+                     omegac=meta["omegac"], **kw)
+    return g, meta, system, ew, fp
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_forces_vs_oracle_and_reference(case, precision):
+    g, meta, system, ew, fp = make(case, precision)
+    assert fp.nkvec == meta["QN"]
+    orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
+    for d in (0, g["r"].shape[0] - 1):
+        f, en = fp.forces(g["r"][d], measure=True)
+        fo, eo = orc.forces(g["r"][d], nthreads=4)
+        tol = 1e-10 if precision == "fp64" else MIXED_TOL
+        assert rel_rms(f, fo) < tol
+        assert rel_rms(f, g["f"][d]) < max(tol, 2e-10)
+        etol = 1e-10 if precision == "fp64" else 1e-6
+        for k in ("el", "lj", "er", "ek"):
+            assert abs(en[k] - eo[k]) <= etol * max(abs(eo[k]), abs(eo["el"])), k
+        assert abs(en["vir"] - eo["vir"]) <= etol * abs(eo["vir"]) * 10
+        for m in range(6):
+            assert abs(en["Pvir"][m] - eo["Pvir"][m]) <= 10 * etol * abs(eo["Pvir"][0]), m
+    # total potential energy printed by cook for the last step
+    assert abs((en["el"] + en["lj"]) / meta["Epot_last"] - 1) < (5e-9 if precision == "fp64" else 1e-6)
+
+
+@pytest.mark.parametrize("cells", [1, 2, 3])
+def test_cell_subdivision_does_not_change_forces(cells):
+    g, meta, system, ew, fp = make("spce864", "fp64", cells_per_cutoff=cells)
+    f, _ = fp.forces(g["r"][0])
+    assert rel_rms(f, g["f"][0]) < 2e-10
+
+
+def test_ewald_kspace_part():
+    g, meta, system, ew, fp = make("spce216", "fp64")
+    fk, e = fp.ewald(g["r"][0])
+    orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
+    _, eo = orc.forces(g["r"][0])
+    assert abs(e - (eo["ek"] + eo["eself"])) < 1e-9 * abs(eo["eself"])
+    # k-space forces sum to zero (conj(S) S is real)
+    assert np.abs(fk.sum(axis=0)).max() < 1e-8 * np.abs(fk).max() * len(fk)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_md_step_matches_reference_trajectory(precision):
+    g, meta, system, ew, fp = make("spce216", precision)
+    R = g["r"]
+    fp.md_set_state(R[2], R[2] - R[1])
+    en = fp.md_steps(1)
+    r, r1 = fp.md_get_state()
+    tol = 1e-9 if precision == "fp64" else 1e-6
+    assert np.abs(r - R[3]).max() < tol
+    assert np.isfinite(en["ekin"]) and en["ekin"] > 0
+
+
+def test_md_many_steps_conserve_energy():
+    """leap-frog + SHAKE NVE on 216 SPC/E: total energy drift stays small"""
+    g, meta, system, ew, fp = make("spce216", "mixed")
+    R = g["r"]
+    fp.md_set_state(R[2], R[2] - R[1])
+    E = []
+    for _ in range(10):
+        en = fp.md_steps(20)
+        E.append(en["el"] + en["lj"] + en["ekin"])
+    E = np.array(E)
+    assert np.all(np.isfinite(E))
+    assert np.abs(E - E[0]).max() < 2e-3 * abs(en["ekin"])
+
+
+def test_shake_failure_is_reported_not_fatal():
+    g, meta, system, ew, fp = make("spce216", "fp64", shake_maxit=2)
+    fp2 = M.ForcePath(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"], precision="fp64",
+                      epsc=1e-30, shake_maxit=2)
+    fp2.md_set_state(g["r"][2], g["r"][2] - g["r"][1])
+    with pytest.raises(M.MGError) as e:
+        fp2.md_steps(1)
+    assert e.value.code == 3
+    # the context stays usable
+    f, _ = fp2.forces(g["r"][0])
+    assert rel_rms(f, g["f"][0]) < 2e-10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_translation_invariance(precision):
+    g, meta, system, ew, fp = make("brine532", precision)
+    f0, e0 = fp.forces(g["r"][0], measure=True)
+    f1, e1 = fp.forces(g["r"][0] + np.array([3.3, -7.1, 11.9]), measure=True)
+    tol = 1e-10 if precision == "fp64" else MIXED_TOL
+    assert rel_rms(f1, f0) < tol
+    assert abs(e1["el"] - e0["el"]) < 10 * tol * abs(e0["eself"])
