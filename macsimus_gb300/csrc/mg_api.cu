@@ -418,7 +418,7 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
   Launch L = launch(ctx);
   const int ns = ctx->ns;
   // linked cells
-  PROF("cell_list", k_prep_cells(L, ns, r_dev, nullptr, ctx->L[0], ctx->L[1], ctx->L[2],
+  PROF("cell_list", k_prep_cells(L, ns, r_dev, ctx->d_status, ctx->L[0], ctx->L[1], ctx->L[2],
                                  ctx->ncx, ctx->ncy, ctx->ncz, ctx->d_key, ctx->d_idx));
   PROF("cell_list", cub::DeviceRadixSort::SortPairs(ctx->d_sort_tmp, ctx->sort_tmp_bytes,
                                                     ctx->d_key, ctx->d_key_s, ctx->d_idx,
@@ -522,6 +522,24 @@ int fetch_sums(mg_ctx* ctx) {
   return MG_OK;
 }
 
+// device status word: bit 0 SHAKE did not converge, bit 1 non-finite position.
+// Copied into the pinned block behind the sums; read after the stream sync.
+int fetch_status(mg_ctx* ctx) {
+  CK(cudaMemcpyAsync(ctx->h_sums + 31, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  return MG_OK;
+}
+
+int check_status(mg_ctx* ctx) {
+  int st;
+  std::memcpy(&st, ctx->h_sums + 31, sizeof(int));
+  if (!st) return MG_OK;
+  CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (st & 2) return fail(ctx, MG_ERR_NONFINITE, "non-finite site position");
+  return fail(ctx, MG_ERR_SHAKE, "SHAKE: too many iterations");
+}
+
 }  // namespace
 
 extern "C" {
@@ -574,8 +592,12 @@ int mg_forces_device(mg_ctx* ctx, const double* r_dev, double* f_dev, int measur
     rc = fetch_sums(ctx);
     if (rc) return rc;
   }
+  rc = fetch_status(ctx);
+  if (rc) return rc;
   CK(cudaStreamSynchronize(ctx->stream));
   prof_resolve(ctx);
+  rc = check_status(ctx);
+  if (rc) return rc;
   if (measure && en) fill_energy(ctx, en);
   return MG_OK;
 }
@@ -592,8 +614,12 @@ int mg_forces(mg_ctx* ctx, const double* r, double* f, int measure, mg_energy* e
     rc = fetch_sums(ctx);
     if (rc) return rc;
   }
+  rc = fetch_status(ctx);
+  if (rc) return rc;
   CK(cudaStreamSynchronize(ctx->stream));
   prof_resolve(ctx);
+  rc = check_status(ctx);
+  if (rc) return rc;
   if (measure && en) fill_energy(ctx, en);
   return MG_OK;
 }
@@ -711,14 +737,12 @@ int mg_md_steps(mg_ctx* ctx, int nsteps, mg_energy* en) {
     int rc = fetch_sums(ctx);
     if (rc) return rc;
   }
-  int hstatus = 0;
-  CK(cudaMemcpyAsync(&hstatus, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  int rc = fetch_status(ctx);
+  if (rc) return rc;
   CK(cudaStreamSynchronize(ctx->stream));
   prof_resolve(ctx);
-  if (hstatus) {
-    cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream);
-    return fail(ctx, MG_ERR_SHAKE, "SHAKE: too many iterations");
-  }
+  rc = check_status(ctx);
+  if (rc) return rc;
   if (en) {
     fill_energy(ctx, en);
     en->ekin = ctx->h_sums[17] / (ctx->h * ctx->h) / 4;

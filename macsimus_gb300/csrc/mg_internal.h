@@ -54,7 +54,7 @@ struct Launch {
 };
 
 // kernels (mg_kernels.cu); each returns cudaGetLastError()
-cudaError_t k_prep_cells(const Launch& L, int ns, const double* r, const double* Lbox,
+cudaError_t k_prep_cells(const Launch& L, int ns, const double* r, int* status,
                          double Lx, double Ly, double Lz, int ncx, int ncy, int ncz,
                          int* cellkey, int* idx);
 cudaError_t k_cell_bounds(const Launch& L, int ns, int ncell, const int* key_sorted,

@@ -31,21 +31,35 @@ static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 
 __device__ __forceinline__ double wrap01(double s) { return s - floor(s); }
 
+__device__ __forceinline__ int cell_coord(double s, int n) {
+  int c = (int)(s * n);
+  return c < 0 ? 0 : (c >= n ? n - 1 : c);
+}
+
+// cell key of every site; a non-finite coordinate sets bit 1 of *status and
+// the site is binned into cell 0 so that every later index stays in range
 __global__ void prep_cells_kernel(int ns, const double* __restrict__ r, double Lx, double Ly,
                                   double Lz, int ncx, int ncy, int ncz, int* __restrict__ key,
-                                  int* __restrict__ idx) {
+                                  int* __restrict__ idx, int* __restrict__ status) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ns) return;
-  double sx = wrap01(r[3 * i] / Lx), sy = wrap01(r[3 * i + 1] / Ly), sz = wrap01(r[3 * i + 2] / Lz);
-  int cx = min((int)(sx * ncx), ncx - 1), cy = min((int)(sy * ncy), ncy - 1),
-      cz = min((int)(sz * ncz), ncz - 1);
-  key[i] = (cx * ncy + cy) * ncz + cz;
+  const double x = r[3 * i], y = r[3 * i + 1], z = r[3 * i + 2];
+  int k = 0;
+  if (isfinite(x) && isfinite(y) && isfinite(z)) {
+    const int cx = cell_coord(wrap01(x / Lx), ncx), cy = cell_coord(wrap01(y / Ly), ncy),
+              cz = cell_coord(wrap01(z / Lz), ncz);
+    k = (cx * ncy + cy) * ncz + cz;
+  } else {
+    atomicOr(status, 2);
+  }
+  key[i] = k;
   idx[i] = i;
 }
 
-cudaError_t k_prep_cells(const Launch& L, int ns, const double* r, const double*, double Lx,
+cudaError_t k_prep_cells(const Launch& L, int ns, const double* r, int* status, double Lx,
                          double Ly, double Lz, int ncx, int ncy, int ncz, int* cellkey, int* idx) {
-  prep_cells_kernel<<<cdiv(ns, 256), 256, 0, L.s>>>(ns, r, Lx, Ly, Lz, ncx, ncy, ncz, cellkey, idx);
+  prep_cells_kernel<<<cdiv(ns, 256), 256, 0, L.s>>>(ns, r, Lx, Ly, Lz, ncx, ncy, ncz, cellkey, idx,
+                                                    status);
   LAUNCHED(L);
   return cudaGetLastError();
 }
@@ -189,9 +203,10 @@ __global__ void __launch_bounds__(PAIR_THREADS)
         const int cnt = min(32, nj - jb);
         for (int jj = 0; jj < cnt; jj++) {
           const int4 q = sj[warp][jj];
-          const float dx = (float)(me.x - q.x) * sx;
-          const float dy = (float)(me.y - q.y) * sy;
-          const float dz = (float)(me.z - q.z) * sz;
+          // nearest image: 32-bit wrap-around of the fixed-point difference
+          const float dx = (float)(int)((unsigned)me.x - (unsigned)q.x) * sx;
+          const float dy = (float)(int)((unsigned)me.y - (unsigned)q.y) * sy;
+          const float dz = (float)(int)((unsigned)me.z - (unsigned)q.z) * sz;
           const float rr = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
           if (!vi || rr >= cq || j0 + jb + jj == ti) continue;
           const PairF P = ptab[kind_i * nk + (q.w & 255)];
@@ -679,7 +694,7 @@ __global__ void __launch_bounds__(KF_THREADS)
   if (j >= a.nq) return;
   const T2* R = tab + (long)j * a.row;
   const int oy = a.Kx + 1 + a.Ky, oz = a.Kx + 2 * a.Ky + 2 + a.Kz;
-  const T2 ez = R[oz + 1];
+  const T2 ez = a.Kz >= 1 ? R[oz + 1] : T2{1, 0};
   double Fx = 0, Fy = 0, Fz = 0;
   T gx = 0, gy = 0, gz = 0;
   int nf = 0;
