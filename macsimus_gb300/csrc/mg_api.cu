@@ -24,6 +24,7 @@ struct mg_ctx {
   double h = 0.002, epsc = 1e-7, omega = 0.6;
   int shake_maxit = 1000;
   int ncx = 0, ncy = 0, ncz = 0, ncell = 0, nstencil = 0, sort_bits = 1;
+  bool allpairs = false;
   int Kx = 0, Ky = 0, Kz = 0, row = 0, ntask = 0, ncol = 0, nchunk = 1;
   cudaStream_t stream = nullptr;
   // host copies
@@ -235,7 +236,8 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
       double qq = kind_q[a] * kind_q[b];
       pd[a * ctx->nkind + b] = PairD{P.C1q, P.C2q, P.A4, P.E24, P.Sq, qq, P.A, P.E4};
       pf[a * ctx->nkind + b] = PairF{(float)P.C1q, (float)P.C2q, (float)P.A4, (float)P.E24,
-                                     (float)P.Sq,  (float)qq,    (float)P.A,  (float)P.E4};
+                                     (float)P.Sq,  (float)qq,    (float)P.A,  (float)P.E4,
+                                     qq,           0.0};
     }
 
   // ---- erfc spline table over [0, cutoff + rplus)
@@ -247,9 +249,16 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
 
   // ---- cells: size >= cutoff/cdiv and at least 2*cdiv+1 cells per edge
   int cdivv = p->cells_per_cutoff > 0 ? p->cells_per_cutoff : 2;
-  int nc3[3];
+  int nc3[3] = {1, 1, 1};
+  bool allpairs = false;
   for (;; cdivv++) {
-    if (cdivv > 8) return fail(ctx, MG_ERR_SETUP, "cannot build the linked-cell grid");
+    if (cdivv > 8) {
+      // box barely larger than twice the cutoff: one cell holding every
+      // site, pairs taken with the nearest image
+      allpairs = true;
+      nc3[0] = nc3[1] = nc3[2] = 1;
+      break;
+    }
     bool ok = true;
     for (int d = 0; d < 3; d++) {
       nc3[d] = (int)(p->L[d] * cdivv / p->cutoff);
@@ -257,21 +266,26 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
     }
     if (ok) break;
   }
+  ctx->allpairs = allpairs;
   ctx->ncx = nc3[0];
   ctx->ncy = nc3[1];
   ctx->ncz = nc3[2];
   ctx->ncell = nc3[0] * nc3[1] * nc3[2];
   while ((1 << ctx->sort_bits) < ctx->ncell) ctx->sort_bits++;
   std::vector<int4> st;
-  for (int dx = -cdivv; dx <= cdivv; dx++)
-    for (int dy = -cdivv; dy <= cdivv; dy++)
-      for (int dz = -cdivv; dz <= cdivv; dz++) {
-        double g[3] = {(double)std::max(std::abs(dx) - 1, 0) * p->L[0] / nc3[0],
-                       (double)std::max(std::abs(dy) - 1, 0) * p->L[1] / nc3[1],
-                       (double)std::max(std::abs(dz) - 1, 0) * p->L[2] / nc3[2]};
-        double dmin2 = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
-        if (dmin2 < p->cutoff * p->cutoff * (1 + 1e-9)) st.push_back(make_int4(dx, dy, dz, 0));
-      }
+  if (allpairs) {
+    st.push_back(make_int4(0, 0, 0, 0));
+  } else {
+    for (int dx = -cdivv; dx <= cdivv; dx++)
+      for (int dy = -cdivv; dy <= cdivv; dy++)
+        for (int dz = -cdivv; dz <= cdivv; dz++) {
+          double g[3] = {(double)std::max(std::abs(dx) - 1, 0) * p->L[0] / nc3[0],
+                         (double)std::max(std::abs(dy) - 1, 0) * p->L[1] / nc3[1],
+                         (double)std::max(std::abs(dz) - 1, 0) * p->L[2] / nc3[2]};
+          double dmin2 = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+          if (dmin2 < p->cutoff * p->cutoff * (1 + 1e-9)) st.push_back(make_int4(dx, dy, dz, 0));
+        }
+  }
   ctx->nstencil = (int)st.size();
 
   // ---- k-vectors (cook's set), sorted into (kx,ky) columns of consecutive kz
@@ -432,6 +446,7 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
   pa.ncy = ctx->ncy;
   pa.ncz = ctx->ncz;
   pa.nstencil = ctx->nstencil;
+  pa.allpairs = ctx->allpairs ? 1 : 0;
   pa.nkind = ctx->nkind;
   pa.cell_start = ctx->d_cell_start;
   pa.order = ctx->d_order;

@@ -28,6 +28,8 @@ int kvector_set(const double L[3], double* kappa, std::vector<int>* kv);
 struct PairF {
   float C1q, C2q, A4, E24;   // force
   float Sq, qq, A, E4;       // + energy
+  double qqd;                // qq in FP64 (excluded intramolecular pairs)
+  double pad;
 };
 struct PairD {
   double C1q, C2q, A4, E24, Sq, qq, A, E4;
@@ -68,6 +70,7 @@ cudaError_t k_gather_fp64(const Launch& L, int ns, const double* r, const int* o
 
 struct PairArgs {
   int ns, ncx, ncy, ncz, nstencil, nkind;
+  int allpairs;             // one cell: nearest image taken per pair (FP64 path)
   const int* cell_start;
   const int* order;         // sorted -> site
   const int4* stencil;      // dx,dy,dz

@@ -212,12 +212,31 @@ __global__ void __launch_bounds__(PAIR_THREADS)
           const PairF P = ptab[kind_i * nk + (q.w & 255)];
           float f = 0;
           if ((q.w >> 8) == mol_i) {
+            // excluded intramolecular pair: its Ewald correction is large and
+            // cancels the self term, so it is evaluated and summed in FP64
             if (P.qq != 0.f) {
-              float fe;
-              float e = excl_term<float>(rr, alpha, &fe);
-              f = fe * P.qq;
-              if (MEASURE) e_el += e * P.qq;
+              const double ex = (double)(int)((unsigned)me.x - (unsigned)q.x) * (a.Lx * 2.3283064365386963e-10);
+              const double ey = (double)(int)((unsigned)me.y - (unsigned)q.y) * (a.Ly * 2.3283064365386963e-10);
+              const double ez = (double)(int)((unsigned)me.z - (unsigned)q.z) * (a.Lz * 2.3283064365386963e-10);
+              const double err = ex * ex + ey * ey + ez * ez;
+              double fe;
+              const double e = excl_term<double>(err, a.alpha, &fe);
+              const double qq = P.qqd;
+              fe *= qq;
+              fx += fe * ex;
+              fy += fe * ey;
+              fz += fe * ez;
+              if (MEASURE) {
+                en[0] += e * qq;
+                en[3] += ex * fe * ex;
+                en[4] += ey * fe * ey;
+                en[5] += ez * fe * ez;
+                en[6] += ez * fe * ey;
+                en[7] += ex * fe * ez;
+                en[8] += ey * fe * ex;
+              }
             }
+            continue;
           } else {
             if (rr < P.C2q) {
               float U;
@@ -369,7 +388,12 @@ __global__ void __launch_bounds__(PAIR_THREADS)
         const int cnt = min(32, nj - jb);
         for (int jj = 0; jj < cnt; jj++) {
           const double4 q = sj[warp][jj];
-          const double dx = xs - q.x, dy = ys - q.y, dz = zs - q.z;
+          double dx = xs - q.x, dy = ys - q.y, dz = zs - q.z;
+          if (a.allpairs) {
+            dx -= a.Lx * rint(dx / a.Lx);
+            dy -= a.Ly * rint(dy / a.Ly);
+            dz -= a.Lz * rint(dz / a.Lz);
+          }
           const double rr = dx * dx + dy * dy + dz * dz;
           if (!vi || rr >= cq || j0 + jb + jj == ti) continue;
           const long long wj = __double_as_longlong(q.w);

@@ -112,3 +112,20 @@ def test_translation_invariance(precision):
     tol = 1e-10 if precision == "fp64" else MIXED_TOL
     assert rel_rms(f1, f0) < tol
     assert abs(e1["el"] - e0["el"]) < 10 * tol * abs(e0["eself"])
+
+
+def test_full_size_mixed_within_tolerance_of_fp64():
+    """32768 SPC/E waters (the benchmark workload): the mixed path stays within
+    the 1e-5 relative force RMS bound of the FP64 path; Newton's third law and
+    conj(S)S real make the total force vanish; energies agree."""
+    from macsimus_gb300 import configs
+    w = configs.workload("spce32768", seed=3)
+    args = (w["system"], [w["L"]] * 3, w["cutoff"], w["alpha"], w["kappa"])
+    fm, em = M.ForcePath(*args, precision="mixed").forces(w["r"], measure=True)
+    fd, ed = M.ForcePath(*args, precision="fp64").forces(w["r"], measure=True)
+    assert rel_rms(fm, fd) < MIXED_TOL
+    scale = np.sqrt((fd ** 2).sum(axis=1).mean())
+    assert np.abs(fd.sum(axis=0)).max() < 1e-6 * scale * np.sqrt(len(fd))
+    assert np.abs(fm.sum(axis=0)).max() < 1e-3 * scale * np.sqrt(len(fd))
+    assert abs(em["lj"] - ed["lj"]) < 1e-6 * abs(ed["lj"])
+    assert abs(em["el"] - ed["el"]) < 1e-6 * abs(ed["eself"])

@@ -53,6 +53,18 @@ def test_shake_step_matches_reference_trajectory():
     assert np.abs(rn - R[3]).max() < 1e-9
 
 
+def test_leapfrog_kinetic_energy_matches_reference():
+    """VERLET=3 kinetic energy m (V1^2+V2^2)/(4 h^2) of sim/shakev3.c; cook
+    prints En.kin of the last step (9 significant digits)"""
+    g, meta, system, ew = load("spce216")
+    p = meta["params"]
+    orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
+    R, F = g["r"], g["f"]
+    _, _, it, ek = orc.shake_step(R[3], R[3] - R[2], F[3], p["h"], eps=p["epsc"],
+                                  omega=meta["omegac"] / 2)
+    assert abs(ek / meta["Ekin_last"] - 1) < 5e-9
+
+
 def test_virial_is_volume_derivative():
     """trace(Pvir) = -dE/dln(s) for an affine scaling r->s r, L->s L with the
     Ewald parameters and the integer k-vector set fixed.  Central finite
