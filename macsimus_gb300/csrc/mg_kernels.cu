@@ -279,15 +279,16 @@ __global__ void __launch_bounds__(PAIR_THREADS)
         }
         __syncwarp();
       }
+      // energies fold into FP64 after every neighbour cell, forces every FOLD
+      if (MEASURE) {
+        en[0] += e_el; en[1] += e_lj; en[2] += e_vir;
+        en[3] += p0; en[4] += p1; en[5] += p2; en[6] += p3; en[7] += p4; en[8] += p5;
+        e_el = e_lj = e_vir = p0 = p1 = p2 = p3 = p4 = p5 = 0;
+      }
       if (++nb == FOLD) {
         nb = 0;
         fx += ax; fy += ay; fz += az;
         ax = ay = az = 0;
-        if (MEASURE) {
-          en[0] += e_el; en[1] += e_lj; en[2] += e_vir;
-          en[3] += p0; en[4] += p1; en[5] += p2; en[6] += p3; en[7] += p4; en[8] += p5;
-          e_el = e_lj = e_vir = p0 = p1 = p2 = p3 = p4 = p5 = 0;
-        }
       }
     }
     fx += ax; fy += ay; fz += az;
