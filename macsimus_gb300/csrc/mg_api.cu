@@ -58,6 +58,10 @@ struct mg_ctx {
   void* d_part = nullptr;  // float2 or double2 partials
   double* d_ekpart = nullptr;
   int nkblocks = 0;
+  KRow* d_krows = nullptr;
+  KTile* d_tiles = nullptr;
+  int2* d_p1job = nullptr;
+  int ntile = 0, np1job = 0;
   // SHAKE
   int* d_mol_first = nullptr;
   int* d_mol_cfirst = nullptr;
@@ -329,6 +333,22 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   }
   ctx->ncol = (int)cols.size();
   ctx->ntask = (int)tasks.size();
+  // rows of the tiled k-space kernels: sorted by kz extent, KTR per tile
+  std::vector<KRow> krows;
+  for (const KCol& c : cols) krows.push_back(KRow{c.kx, c.ky, c.kz0, c.kz0 + c.n - 1, c.k0, {0, 0, 0}});
+  auto extent = [](const KRow& r) { return std::max(std::abs(r.kzlo), std::abs(r.kzhi)); };
+  std::stable_sort(krows.begin(), krows.end(),
+                   [&](const KRow& x, const KRow& y) { return extent(x) > extent(y); });
+  std::vector<KTile> tiles;
+  std::vector<int2> p1job;
+  for (int r0 = 0; r0 < (int)krows.size(); r0 += KTR) {
+    int n = std::min(KTR, (int)krows.size() - r0), R = 0;
+    for (int i = r0; i < r0 + n; i++) R = std::max(R, extent(krows[i]));
+    for (int kz0 = -R; kz0 <= R; kz0 += 16) p1job.push_back(make_int2((int)tiles.size(), kz0));
+    tiles.push_back(KTile{r0, n, R, 0});
+  }
+  ctx->ntile = (int)tiles.size();
+  ctx->np1job = (int)p1job.size();
   ctx->row = (ctx->Kx + 1) + (2 * ctx->Ky + 1) + (2 * ctx->Kz + 1);
 
   // ---- charges
@@ -340,8 +360,9 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
       qval.push_back(t->charge[i]);
     }
   ctx->nq = (int)qsite.size();
-  int tblocks = (ctx->ntask + 255) / 256;
-  ctx->nchunk = std::max(1, std::min(std::max(1, ctx->nq / 32), (4 * 152 + tblocks - 1) / tblocks));
+  // charge chunks of pass 1: about 8 CTAs per SM, at least 64 charges each
+  ctx->nchunk = std::max(1, std::min(std::max(1, ctx->nq / 64),
+                                     (8 * 152 + ctx->np1job - 1) / ctx->np1job));
   ctx->nkblocks = (nk + 255) / 256;
 
   // ---- constraints
@@ -386,6 +407,9 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   CK(upload(&ctx->d_task, tasks.data(), tasks.size()));
   CK(upload(&ctx->d_col, cols.data(), cols.size()));
   CK(upload(&ctx->d_kvec, kvec.data(), kvec.size()));
+  CK(upload(&ctx->d_krows, krows.data(), krows.size()));
+  CK(upload(&ctx->d_tiles, tiles.data(), tiles.size()));
+  CK(upload(&ctx->d_p1job, p1job.data(), p1job.size()));
   CK(upload(&ctx->d_ekk, ekk.data(), ekk.size()));
   CK(dalloc(&ctx->d_S, 2 * (size_t)nk));
   CK(dalloc(&ctx->d_ekpart, (size_t)ctx->nkblocks * 7));
@@ -484,15 +508,22 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
   ka.Wd = ctx->d_Wd;
   ka.f = f_dev;
   ka.ek_part = ctx->d_ekpart;
+  ka.krows = ctx->d_krows;
+  ka.tiles = ctx->d_tiles;
+  ka.ntile = ctx->ntile;
+  ka.p1job = ctx->d_p1job;
+  ka.np1job = ctx->np1job;
+  ka.qdrude = nullptr;
+  ka.ns = ctx->ns;
   if (ctx->precision == MG_MIXED) {
     PROF("cell_list", k_gather_mixed(L, ns, r_dev, ctx->d_order, ctx->d_kind, ctx->d_mol, ctx->L[0], ctx->L[1],
                       ctx->L[2], ctx->d_pj));
     PROF("pair_mixed", k_pair_mixed(L, pa, ctx->d_pj, ctx->d_ptabf, ctx->d_erd, ctx->d_eru, measure));
     if (ctx->nq > 0) {
       PROF("phase_tables", k_phase_tables_mixed(L, ka, r_dev, (float2*)ctx->d_tab));
-      PROF("ewald_sk", k_sk_mixed(L, ka, (const float2*)ctx->d_tab, (float2*)ctx->d_part));
+      PROF("ewald_sk", k_sk_gemm_mixed(L, ka, (const float2*)ctx->d_tab, (float2*)ctx->d_part));
       PROF("ewald_sk_reduce", k_sk_reduce_mixed(L, ka, (const float2*)ctx->d_part, measure));
-      PROF("ewald_kforce", k_kforce_mixed(L, ka, (const float2*)ctx->d_tab));
+      PROF("ewald_kforce", k_kf_gemm_mixed(L, ka, (const float2*)ctx->d_tab));
     }
   } else {
     PROF("cell_list", k_gather_fp64(L, ns, r_dev, ctx->d_order, ctx->d_kind, ctx->d_mol, ctx->L[0], ctx->L[1],
@@ -500,9 +531,9 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
     PROF("pair_fp64", k_pair_fp64(L, pa, ctx->d_pd, ctx->d_ptabd, ctx->d_ert, measure));
     if (ctx->nq > 0) {
       PROF("phase_tables", k_phase_tables_fp64(L, ka, r_dev, (double2*)ctx->d_tab));
-      PROF("ewald_sk", k_sk_fp64(L, ka, (const double2*)ctx->d_tab, (double2*)ctx->d_part));
+      PROF("ewald_sk", k_sk_gemm_fp64(L, ka, (const double2*)ctx->d_tab, (double2*)ctx->d_part));
       PROF("ewald_sk_reduce", k_sk_reduce_fp64(L, ka, (const double2*)ctx->d_part, measure));
-      PROF("ewald_kforce", k_kforce_fp64(L, ka, (const double2*)ctx->d_tab));
+      PROF("ewald_kforce", k_kf_gemm_fp64(L, ka, (const double2*)ctx->d_tab));
     }
   }
   if (measure) {
@@ -582,7 +613,8 @@ int mg_destroy(mg_ctx* ctx) {
                   ctx->d_kvec,   ctx->d_ekk,     ctx->d_S,     ctx->d_Wf,     ctx->d_Wd,
                   ctx->d_tab,    ctx->d_part,    ctx->d_ekpart, ctx->d_mol_first,
                   ctx->d_mol_cfirst, ctx->d_cons, ctx->d_bondq, ctx->d_imass, ctx->d_mass,
-                  ctx->d_kinpart, ctx->d_status, ctx->d_sums};
+                  ctx->d_kinpart, ctx->d_status, ctx->d_sums, ctx->d_krows,
+                  ctx->d_tiles, ctx->d_p1job};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ctx->h_sums) cudaFreeHost(ctx->h_sums);
@@ -674,17 +706,24 @@ int mg_ewald(mg_ctx* ctx, const double* r, double* f, double* energy) {
   ka.Wd = ctx->d_Wd;
   ka.f = ctx->d_f;
   ka.ek_part = ctx->d_ekpart;
+  ka.krows = ctx->d_krows;
+  ka.tiles = ctx->d_tiles;
+  ka.ntile = ctx->ntile;
+  ka.p1job = ctx->d_p1job;
+  ka.np1job = ctx->np1job;
+  ka.qdrude = nullptr;
+  ka.ns = ctx->ns;
   if (ctx->nq > 0) {
     if (ctx->precision == MG_MIXED) {
       CK(k_phase_tables_mixed(L, ka, ctx->d_r, (float2*)ctx->d_tab));
-      CK(k_sk_mixed(L, ka, (const float2*)ctx->d_tab, (float2*)ctx->d_part));
+      CK(k_sk_gemm_mixed(L, ka, (const float2*)ctx->d_tab, (float2*)ctx->d_part));
       CK(k_sk_reduce_mixed(L, ka, (const float2*)ctx->d_part, true));
-      CK(k_kforce_mixed(L, ka, (const float2*)ctx->d_tab));
+      CK(k_kf_gemm_mixed(L, ka, (const float2*)ctx->d_tab));
     } else {
       CK(k_phase_tables_fp64(L, ka, ctx->d_r, (double2*)ctx->d_tab));
-      CK(k_sk_fp64(L, ka, (const double2*)ctx->d_tab, (double2*)ctx->d_part));
+      CK(k_sk_gemm_fp64(L, ka, (const double2*)ctx->d_tab, (double2*)ctx->d_part));
       CK(k_sk_reduce_fp64(L, ka, (const double2*)ctx->d_part, true));
-      CK(k_kforce_fp64(L, ka, (const double2*)ctx->d_tab));
+      CK(k_kf_gemm_fp64(L, ka, (const double2*)ctx->d_tab));
     }
     CK(k_reduce_sum(L, ctx->d_ekpart, ctx->nkblocks, 7, ctx->d_sums + 10));
   }

@@ -46,6 +46,16 @@ struct KCol {
   int kx, ky, kz0, n, k0, pad[3];
 };
 
+// a (kx,ky) row of the k set: kz in [kzlo,kzhi], k index kstart+(kz-kzlo)
+struct KRow {
+  int kx, ky, kzlo, kzhi, kstart, pad[3];
+};
+// KTR rows sharing the kz span [-R,R]
+struct KTile {
+  int row0, nrows, R, pad;
+};
+constexpr int KTR = 64;         // rows per k-space tile
+
 constexpr int KZT = 4;          // kz per pass-1 thread
 constexpr int PAIR_THREADS = 128;
 constexpr int MAX_KINDS = 16;
@@ -103,6 +113,13 @@ struct KArgs {
   double2* Wd;              // [nk] the same in FP64 (or NULL)
   double* f;                // forces (added)
   double* ek_part;          // [nk-blocks * 7] energy + virial partials
+  const KRow* krows;        // rows sorted by kz extent
+  const KTile* tiles;
+  int ntile;
+  const int2* p1job;        // pass-1 CTA jobs: (tile, first kz)
+  int np1job;
+  const int* qdrude;        // [nq] 1 if the charge is a Drude charge (or NULL)
+  int ns;
 };
 cudaError_t k_phase_tables_mixed(const Launch& L, const KArgs& a, const double* r, float2* tab);
 cudaError_t k_phase_tables_fp64(const Launch& L, const KArgs& a, const double* r, double2* tab);
@@ -112,6 +129,10 @@ cudaError_t k_sk_reduce_mixed(const Launch& L, const KArgs& a, const float2* par
 cudaError_t k_sk_reduce_fp64(const Launch& L, const KArgs& a, const double2* part, bool measure);
 cudaError_t k_kforce_mixed(const Launch& L, const KArgs& a, const float2* tab);
 cudaError_t k_kforce_fp64(const Launch& L, const KArgs& a, const double2* tab);
+cudaError_t k_sk_gemm_mixed(const Launch& L, const KArgs& a, const float2* tab, float2* part);
+cudaError_t k_sk_gemm_fp64(const Launch& L, const KArgs& a, const double2* tab, double2* part);
+cudaError_t k_kf_gemm_mixed(const Launch& L, const KArgs& a, const float2* tab);
+cudaError_t k_kf_gemm_fp64(const Launch& L, const KArgs& a, const double2* tab);
 cudaError_t k_reduce_sum(const Launch& L, const double* part, int nrows, int width, double* out);
 
 struct ShakeArgs {
