@@ -41,8 +41,14 @@ SITE_TYPES = {
     "O": (15.9994, 0.6502, 3.166),
     "NA": (22.9898, 1.475, 2.16),
     "CL": (35.453, 0.0535, 4.83),
+    "OD": (15.9994, 0.6502, 3.166),   # oxygen carrying a Drude charge
 }
-TYPE_ORDER = ["H", "O", "NA", "CL"]
+TYPE_ORDER = ["H", "O", "NA", "CL", "OD"]
+
+# Drude parameters of a site type: (alphapol A^3, chargepol e).  The Drude
+# water takes the polarizability 1.44 A^3 and the shell charge -1.8 e; the
+# spring constant follows, k = q^2/(4 pi eps0 alpha) = 3126 kJ/mol/A^2.
+TYPE_DRUDE = {"OD": (1.44, -1.8)}
 
 
 def ble_type_row(name):
@@ -88,7 +94,15 @@ def ion(name):
     return Species(name, [name], [q], np.zeros((1, 3)))
 
 
-SPECIES = {"WAT": spce, "NA": lambda: ion("NA"), "CL": lambda: ion("CL")}
+def spce_drude():
+    """SPC/E geometry and total charges with a Drude shell on the oxygen"""
+    sp = spce()
+    sp.name = "WATD"
+    sp.sites = ["OD", "H", "H"]
+    return sp
+
+
+SPECIES = {"WAT": spce, "NA": lambda: ion("NA"), "CL": lambda: ion("CL"), "WATD": spce_drude}
 
 
 @dataclass
@@ -109,6 +123,20 @@ class System:
     comb_rule: int = 1
     species: list = None
     counts: list = None
+    qpol: np.ndarray = None     # [ns] Drude charge (program units) or None
+    alphapol: np.ndarray = None # [ns] Drude polarizability volume (A^3) or None
+
+    @property
+    def polar(self):
+        return self.qpol is not None
+
+    @property
+    def alpha_qq(self):
+        """cook's si->alpha_qq = alphapol/qpol^2 (cook/simdef.c:1008-1010)"""
+        a = np.zeros(len(self.type))
+        m = self.qpol != 0
+        a[m] = self.alphapol[m] / self.qpol[m] ** 2
+        return a
 
     @property
     def ns(self):
@@ -123,6 +151,8 @@ def build_system(species_names, counts):
     E, R, A, _ = type_table()
     tix = {n: i for i, n in enumerate(TYPE_ORDER)}
     typ, q, mass, mol, mfirst, cons, clen, cfirst = [], [], [], [], [0], [], [], [0]
+    qpol, apol = [], []
+    polar = any(t in TYPE_DRUDE for s in species_names for t in SPECIES[s]().sites)
     imol = 0
     for sname, n in zip(species_names, counts):
         sp = SPECIES[sname]()
@@ -130,7 +160,12 @@ def build_system(species_names, counts):
             base = len(typ)
             for k, t in enumerate(sp.sites):
                 typ.append(tix[t])
-                q.append(ELECTRON * sp.charges[k])
+                qt = ELECTRON * sp.charges[k]
+                ap, cp = TYPE_DRUDE.get(t, (0.0, 0.0))
+                qp = cp * ELECTRON
+                q.append(qt - qp)          # central charge = total - Drude
+                qpol.append(qp)
+                apol.append(ap)
                 mass.append(ble_type_row(t)[0] / MUNIT)
                 mol.append(imol)
             for (i, j, d) in sp.bonds:
@@ -143,19 +178,29 @@ def build_system(species_names, counts):
                   mol=np.array(mol, np.int32), mol_first=np.array(mfirst, np.int32),
                   cons=np.array(cons, np.int32).reshape(-1, 2), cons_len=np.array(clen),
                   mol_cfirst=np.array(cfirst, np.int32), typeE=E, typeR=R, typeA=A,
-                  comb_rule=1, species=list(species_names), counts=list(counts))
+                  comb_rule=1, species=list(species_names), counts=list(counts),
+                  qpol=np.array(qpol) if polar else None,
+                  alphapol=np.array(apol) if polar else None)
 
 
 def ble_text(species_names):
-    """The cook force-field (.ble) file of these species (test fixtures)."""
+    """The cook force-field (.ble) file of these species (test fixtures);
+    with a Drude species the table carries cook's POLAR columns
+    alphapol chargepol Esat kappa (cook/simdef.c:638-700)."""
+    polar = any(t in TYPE_DRUDE for s in species_names for t in SPECIES[s]().sites)
     lines = ["! force field written by macsimus_gb300.forcefield",
              "nspec=%d" % len(species_names),
              "  nsites=%d  nnbfixes=0  factor14=1  distance14=0  comb_rule=1" % len(TYPE_ORDER),
-             "  polar=0  nparms=0;", "", "Lennard-Jones",
-             "! i atom mass alpha EvdW[kcal/mol] RvdW[A]"]
+             "  polar=%d  nparms=0;" % (1 if polar else 0), "", "Lennard-Jones",
+             "! i atom mass alpha EvdW[kcal/mol] RvdW[A]" +
+             (" alphapol chargepol Esat kappa" if polar else "")]
     for i, n in enumerate(TYPE_ORDER):
         m, ev, rv = ble_type_row(n)
-        lines.append("  %d %-3s %.6f 0 %.12g %.12g" % (i, n, m, ev, rv))
+        extra = ""
+        if polar:
+            ap, cp = TYPE_DRUDE.get(n, (0.0, 0.0))
+            extra = " %.12g %.12g 0 0" % (ap, cp)
+        lines.append("  %d %-3s %.6f 0 %.12g %.12g%s" % (i, n, m, ev, rv, extra))
     lines += ["", "nbfixes", ""]
     for isp, sname in enumerate(species_names):
         sp = SPECIES[sname]()

@@ -282,6 +282,8 @@ again:
 
 /* ------------------------------------------------------------ threads --- */
 
+static int is_polar(const orc_sys_t *s) { return s->qpol != NULL; }
+
 typedef struct {
   const orc_sys_t *s;
   const double *r;
@@ -308,8 +310,6 @@ static void run_threads(void *(*fn)(void *), orc_work_t *w, int nth)
   for (i = 0; i < nth; i++) pthread_join(th[i], NULL);
 }
 
-/* number of charges of the Ewald sums (central + Drude) */
-static int is_polar(const orc_sys_t *s) { return s->qpol != NULL; }
 
 /* -------------------------------------------------------------- r-space --- */
 
@@ -370,6 +370,70 @@ static void pair_np(orc_work_t *w, int i, int j, const double dr[3], double rr,
   }
 }
 
+/* one pair of polarizable sites (cook/ljqqpol.c polarLJqqm, POLAR=0,
+   COULOMB=-2): centre-centre LJ + charge, Drude(i)-centre(j),
+   centre(i)-Drude(j), Drude-Drude terms, each at its own separation; an
+   intramolecular pair takes the exact Ewald exclusion term for all four.
+   dr = centre(i) - centre(j) (nearest image).  Centre forces go to
+   f[3*ns..], Drude forces to the second half (cook's polar_off half). */
+static void pair_pol(orc_work_t *w, int i, int j, const double dr0[3], double rr0,
+                     double *fo, int measure)
+{
+  const orc_sys_t *s = w->s;
+  const int ns = s->ns;
+  const double *di = w->r + 3 * ns + 3 * i, *dj = w->r + 3 * ns + 3 * j;
+  double *fci = fo + 3 * i, *fcj = fo + 3 * j, *fpi = fo + 3 * ns + 3 * i, *fpj = fo + 3 * ns + 3 * j;
+  const double qi = s->q[i], qj = s->q[j], pi_ = s->qpol[i], pj_ = s->qpol[j];
+  const int excl = s->mol[i] == s->mol[j];
+  double U = 0, f = 0, x, y, z;
+  int k, m;
+  struct { double q; double sgn_i, sgn_j; double *fa, *fb; } t[4] = {
+    {qi * qj, 0, 0, fci, fcj}, {pi_ * qj, 1, 0, fpi, fcj},
+    {qi * pj_, 0, 1, fci, fpj}, {pi_ * pj_, 1, 1, fpi, fpj}};
+  if (!excl) {
+    const orc_ss_t *ss = s->ss + s->type[i] * s->ntypes + s->type[j];
+    if (rr0 < ss->C2q) {
+      if (rr0 < ss->C1q) {
+        x = ss->Sq / rr0; y = x * x * x; z = y * y;
+        U = ss->E4 * (z - y);
+        f = ss->E24 * (z + z - y) * x;
+      } else {
+        x = rr0 - ss->C2q;
+        U = x * x * ss->A;
+        f = ss->A4 * x;
+      }
+      if (measure) { w->vir += rr0 * f; w->lj += U; }
+    }
+  }
+  for (m = 0; m < 4; m++) {
+    double d[3], rr, fe = 0, e = 0;
+    if (t[m].q == 0 && !(m == 0 && f != 0)) continue;
+    for (k = 0; k < 3; k++) d[k] = dr0[k] + (t[m].sgn_i ? di[k] : 0) - (t[m].sgn_j ? dj[k] : 0);
+    rr = SQ(d[0]) + SQ(d[1]) + SQ(d[2]);
+    if (t[m].q != 0) {
+      if (excl) {
+        e = orc_exacterud_sqrt(rr, s->alpha, &fe) * t[m].q;
+        fe *= t[m].q;
+      } else {
+        const double *p = s->ertab + 6 * (int)(rr * s->sgrid);
+        fe = (p[4] / (p[5] + rr) + p[3]) * t[m].q;
+        e = (p[1] / (p[2] + rr) + p[0]) * t[m].q;
+      }
+    }
+    if (m == 0) fe += f;
+    if (measure) w->el += e;
+    {
+      double fx = fe * d[0], fy = fe * d[1], fz = fe * d[2];
+      t[m].fa[0] += fx; t[m].fa[1] += fy; t[m].fa[2] += fz;
+      t[m].fb[0] -= fx; t[m].fb[1] -= fy; t[m].fb[2] -= fz;
+      if (measure) {
+        w->Pvir[0] += d[0] * fx; w->Pvir[1] += d[1] * fy; w->Pvir[2] += d[2] * fz;
+        w->Pvir[3] += d[2] * fy; w->Pvir[4] += d[0] * fz; w->Pvir[5] += d[1] * fx;
+      }
+    }
+  }
+}
+
 static void nearest(const double L[3], const double *ri, const double *rj, double dr[3])
 {
   int k;
@@ -410,7 +474,8 @@ static void *rspace_worker(void *arg)
         nearest(s->L, r + 3 * i, r + 3 * j, dr);
         rr = SQ(dr[0]) + SQ(dr[1]) + SQ(dr[2]);
         if (rr >= SQ(s->cutoff)) continue;
-        pair_np(w, i, j, dr, rr, w->f + 3 * i, w->f + 3 * j, measure);
+        if (is_polar(s)) pair_pol(w, i, j, dr, rr, w->f, measure);
+        else pair_np(w, i, j, dr, rr, w->f + 3 * i, w->f + 3 * j, measure);
       }
   } else {
     const int *nc = w->nc;
@@ -431,7 +496,8 @@ static void *rspace_worker(void *arg)
             nearest(s->L, r + 3 * i, r + 3 * j, dr);
             rr = SQ(dr[0]) + SQ(dr[1]) + SQ(dr[2]);
             if (rr >= SQ(s->cutoff)) continue;
-            pair_np(w, i, j, dr, rr, w->f + 3 * i, w->f + 3 * j, measure);
+            if (is_polar(s)) pair_pol(w, i, j, dr, rr, w->f, measure);
+            else pair_np(w, i, j, dr, rr, w->f + 3 * i, w->f + 3 * j, measure);
           }
       }
     }
@@ -575,7 +641,6 @@ int orc_forces(const orc_sys_t *s, const double *r, double *f, orc_en_t *en, int
     nc[m] = (int)(s->L[m] / s->cutoff);
     if (nc[m] < 3) usecells = 0;
   }
-  if (is_polar(s)) usecells = 0; /* polar pair path uses all pairs (see orc_polar.c) */
   if (usecells) {
     int ncell = nc[0] * nc[1] * nc[2];
     cellhead = malloc(sizeof(int) * ncell);
@@ -760,4 +825,69 @@ int orc_shake_step(int ns, double *r, double *r1, const double *f, const double 
   free(p);
   if (ekin) *ekin = kin / hh / 4;
   return worst;
+}
+
+/* ------------------------------------------------------------- Drude --- */
+
+/* sim/scf.c:12-300 selffield (POLAR=0, no saturation): Ewald correction of
+   the centre-Drude pair of each site (exacterud_sqrt_1), relaxation
+   rpol <- (1-omega) rpol + omega alpha_qq fpol, Drude force folded into the
+   centre, spring energy and virial.  Returns the max |rpol change|/omega. */
+double orc_selffield(const orc_sys_t *s, double *r, double *f, orc_en_t *en, double omega)
+{
+  int ns = s->ns, i, k;
+  double self = 0, maxd = 0;
+  for (i = 0; i < ns; i++) {
+    double *rp = r + 3 * ns + 3 * i, *fp = f + 3 * ns + 3 * i, *fc = f + 3 * i;
+    double rr, byerd, fq, old[3], dd = 0;
+    if (s->qpol[i] == 0) continue;
+    rr = SQ(rp[0]) + SQ(rp[1]) + SQ(rp[2]);
+    fq = s->q[i] * s->qpol[i];
+    {
+      double e = orc_exacterud_sqrt_1(rr, s->alpha, &byerd);
+      double ff = fq * byerd;
+      if (en) en->el += fq * e;
+      for (k = 0; k < 3; k++) {
+        double fdr = ff * rp[k];
+        fp[k] += fdr;
+        fc[k] -= fdr;
+      }
+      if (en) {
+        en->Pvir[0] += rp[0] * ff * rp[0]; en->Pvir[1] += rp[1] * ff * rp[1];
+        en->Pvir[2] += rp[2] * ff * rp[2]; en->Pvir[3] += rp[2] * ff * rp[1];
+        en->Pvir[4] += rp[0] * ff * rp[2]; en->Pvir[5] += rp[1] * ff * rp[0];
+      }
+    }
+    for (k = 0; k < 3; k++) {
+      old[k] = rp[k];
+      rp[k] = (1 - omega) * rp[k] + omega * s->alphaqq[i] * fp[k];
+      dd += SQ(old[k] - rp[k]);
+      fc[k] += fp[k];
+    }
+    if (dd > maxd) maxd = dd;
+    self += rp[0] * fp[0] + rp[1] * fp[1] + rp[2] * fp[2];
+    if (en) {
+      en->Pvir[0] -= rp[0] * fp[0]; en->Pvir[1] -= rp[1] * fp[1]; en->Pvir[2] -= rp[2] * fp[2];
+      en->Pvir[3] -= rp[1] * fp[2]; en->Pvir[4] -= rp[2] * fp[0]; en->Pvir[5] -= rp[0] * fp[1];
+    }
+  }
+  if (en) en->self = self / 2;
+  return sqrt(maxd) / omega;
+}
+
+/* ASPC coefficients of sim/pred2.c:70-97 (Kolafa 2004) for predictor length
+   k: B[0..k+1] and the stabilizing mixing omega=(k+2)/(2k+3); k=0 gives the
+   linear predictor {2,-1} */
+void orc_aspc_coef(int k, double *B, double *omega)
+{
+  int i;
+  if (k == 0) { B[0] = 2; B[1] = -1; *omega = 2.0 / 3.0; return; }
+  {
+    double o = (double)(4 * k + 6) / (double)(k + 3);
+    for (i = 0; i < k + 2; i++) {
+      B[i] = o * (i + 1);
+      o *= (double)(i - k - 1) / (double)(k + i + 4);
+    }
+  }
+  *omega = (k + 2) / (double)(2 * k + 3);
 }

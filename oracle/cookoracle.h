@@ -107,6 +107,13 @@ int orc_shake_step(int ns, double *r, double *r1, const double *f, const double 
                    const int *ci, const int *cj, const double *bondq,
                    double h, double eps, double omega, int maxit, double *ekin);
 
+/* one Drude relaxation iteration (sim/scf.c selffield): r and f hold 2*ns
+   vectors (sites, then Drude displacements / Drude forces); energies added
+   to *en (el, self, Pvir) when en != NULL; returns max |d rpol|/omega */
+double orc_selffield(const orc_sys_t *s, double *r, double *f, orc_en_t *en, double omega);
+/* ASPC predictor B[0..k+1] and mixing omega (sim/pred2.c:70-97) */
+void orc_aspc_coef(int k, double *B, double *omega);
+
 #ifdef __cplusplus
 }
 #endif

@@ -66,6 +66,9 @@ def lib():
         L.orc_forces.argtypes = [C.POINTER(SYS), dp, dp, C.POINTER(EN), C.c_int]
         L.orc_shake_step.argtypes = [C.c_int, dp, dp, dp, dp, C.c_int, ip, ip, ip, ip, ip, dp,
                                      C.c_double, C.c_double, C.c_double, C.c_int, dp]
+        L.orc_selffield.argtypes = [C.POINTER(SYS), dp, dp, C.POINTER(EN), C.c_double]
+        L.orc_selffield.restype = C.c_double
+        L.orc_aspc_coef.argtypes = [C.c_int, dp, dp]
         _lib = L
     return _lib
 
@@ -139,8 +142,15 @@ class Oracle:
         s.ertab = _dp(self.tab)
         s.ntab = ntab
         s.sgrid = sg.value
-        s.qpol = None
-        s.alphaqq = None
+        if getattr(system, "polar", False):
+            self.qpol = np.ascontiguousarray(system.qpol, np.float64)
+            self.alphaqq = np.ascontiguousarray(system.alpha_qq, np.float64)
+            s.qpol = _dp(self.qpol)
+            s.alphaqq = _dp(self.alphaqq)
+        else:
+            s.qpol = None
+            s.alphaqq = None
+        self.polar = getattr(system, "polar", False)
         self.sys = s
         self.sgrid = sg.value
         self.ntab = ntab
@@ -152,6 +162,25 @@ class Oracle:
         lib().orc_forces(C.byref(self.sys), _dp(r), _dp(f), C.byref(en) if measure else None,
                          nthreads)
         return f.reshape(-1, 3), (en.asdict() if measure else None)
+
+    def selffield(self, r2, f2, omega, en=None):
+        """one Drude iteration: r2/f2 [2ns,3] updated in place; en dict
+        (from forces) updated with the self-pair Ewald term, En.self, Pvir"""
+        r2 = np.ascontiguousarray(r2, dtype=np.float64)
+        f2 = np.ascontiguousarray(f2, dtype=np.float64)
+        e = EN()
+        if en is not None:
+            e.el = en["el"]
+            for m in range(6):
+                e.Pvir[m] = en["Pvir"][m]
+        d = lib().orc_selffield(C.byref(self.sys), _dp(r2.reshape(-1)), _dp(f2.reshape(-1)),
+                                C.byref(e), omega)
+        if en is not None:
+            en = dict(en)
+            en["el"] = e.el
+            en["self"] = e.self
+            en["Pvir"] = list(e.Pvir)
+        return r2, f2, en, d
 
     def shake_step(self, r, r1, f, h, eps=1e-10, omega=0.6, maxit=1000):
         s = self.system
@@ -170,3 +199,10 @@ class Oracle:
                                   _ip(nc), _ip(cfirst), _ip(ci), _ip(cj), _dp(bq), h, eps,
                                   omega, maxit, C.byref(ek))
         return r.reshape(-1, 3), r1.reshape(-1, 3), it, ek.value
+
+
+def aspc_coef(k):
+    B = np.zeros(k + 2)
+    om = C.c_double()
+    lib().orc_aspc_coef(k, _dp(B), C.byref(om))
+    return B, om.value

@@ -43,6 +43,11 @@ CASES = {
     "brine532": dict(binary="cookew", species=["WAT", "NA", "CL"], N=[500, 16, 16],
                      L=24.97, cutoff=10.0, alpha=0.31, kn=7, steps=2, h=0.002,
                      epsc=1e-10),
+    # 216 Drude waters (SPC/E + Drude shell on O, alpha 1.44 A^3, q_D -1.8 e),
+    # ASPC k=2 (-p220) with one SCF iteration per step (scf.eps=-1)
+    "drude216": dict(binary="cookpol", species=["WATD"], N=[216], L=18.6206,
+                     cutoff=9.0, alpha=0.35, kn=6, steps=6, h=0.001, epsc=1e-10,
+                     options=["-p220"], extra_def=["scf.eps=-1"]),
 }
 
 
@@ -55,7 +60,7 @@ def def_text(c):
               "cutoff=%.10g LJcutoff=%.10g" % (c["cutoff"], c["cutoff"]),
               "noint=1", "h=%.10g" % c["h"], "T=298",
               "el.test=0 el.alpha=%.10g el.kappa=%.12g" % (c["alpha"], (c["kn"] + 1e-6) / L),
-              "epsc=%.3g" % c["epsc"], "corr=0", ";", ""]
+              "epsc=%.3g" % c["epsc"], "corr=0"] + c.get("extra_def", []) + [";", ""]
     return "\n".join(lines)
 
 
@@ -71,8 +76,16 @@ def parse_dump(path):
         rows = []
         for _ in range(ns):
             t = f.readline().split()
-            rows.append([float(x) for x in t[:7]] + [int(t[7]), int(t[8])])
+            if "rDrude[]" in t:
+                # r q rDrude qDrude f fDrude mol site (POLAR dump)
+                rows.append([float(x) for x in t[:14]] + [int(t[14]), int(t[15])])
+            else:
+                rows.append([float(x) for x in t[:7]] + [int(t[7]), int(t[8])])
     a = np.array(rows)
+    if a.shape[1] == 16:
+        return dict(L=np.array(L), r=a[:, 0:3], q=a[:, 3], rD=a[:, 4:7], qD=a[:, 7],
+                    f=a[:, 8:11], fD=a[:, 11:14], mol=a[:, 14].astype(np.int32),
+                    site=a[:, 15].astype(np.int32))
     return dict(L=np.array(L), r=a[:, 0:3], q=a[:, 3], f=a[:, 4:7],
                 mol=a[:, 7].astype(np.int32), site=a[:, 8].astype(np.int32))
 
@@ -89,7 +102,7 @@ def run_case(name, c, keep=None):
         f.write(def_text(c))
     with open(os.path.join(wd, "sim.get"), "w") as f:
         f.write(get_text(c))
-    p = subprocess.run([binary, "ff.ble", "sim", "-v128"], cwd=wd,
+    p = subprocess.run([binary, "ff.ble", "sim", "-v128"] + c.get("options", []), cwd=wd,
                        stdin=subprocess.DEVNULL, capture_output=True, text=True, timeout=600)
     if p.returncode != 0:
         raise SystemExit("%s failed:\n%s" % (name, p.stdout[-3000:]))
@@ -121,6 +134,10 @@ def save_case(name, dumps, meta):
     arrays["L"] = d0["L"]
     arrays["r"] = np.stack([d["r"] for d in dumps])
     arrays["f"] = np.stack([d["f"] for d in dumps])
+    if "rD" in d0:
+        arrays["qD"] = d0["qD"]
+        arrays["rD"] = np.stack([d["rD"] for d in dumps])
+        arrays["fD"] = np.stack([d["fD"] for d in dumps])
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
     with open(os.path.join(HERE, name + ".json"), "w") as f:
         json.dump(meta, f, indent=1, sort_keys=True)

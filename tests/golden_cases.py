@@ -8,6 +8,7 @@ from macsimus_gb300 import forcefield as ff
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ["spce216", "brine532", "spce864"]
+POLAR_CASES = ["drude216"]
 
 
 def load(case):

@@ -105,3 +105,35 @@ def test_erfc_spline_against_libm():
         rr = r * r
         exact = math.erfc(alpha * r) / r
         assert abs(L.orc_eru(O._dp(tab), sg.value, rr) - exact) < 1e-7 * exact
+
+
+def test_drude_forces_match_reference_dumps():
+    """POLAR build of cook (cook/ljqqpol.c pair terms, Drude charges in the
+    Ewald sums): centre and Drude forces at cook's predicted shell positions"""
+    g, meta, system, ew = load("drude216")
+    assert np.allclose(system.qpol, g["qD"], rtol=1e-11, atol=1e-9)
+    orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
+    for d in range(g["r"].shape[0]):
+        r2 = np.vstack([g["r"][d], g["rD"][d]])
+        f2, _ = orc.forces(r2, nthreads=4)
+        fr = np.vstack([g["f"][d], g["fD"][d]])
+        assert rel_rms(f2, fr) < 1e-10
+
+
+def test_aspc_scf_chain_matches_reference():
+    """ASPC k=2 predictor (sim/pred2.c) over SCF-corrected shell positions
+    (sim/scf.c selffield, omega=4/7) reproduces cook's predicted positions"""
+    g, meta, system, ew = load("drude216")
+    orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
+    ns = system.ns
+    B, om = O.aspc_coef(2)
+    assert np.allclose(B, [2.8, -2.8, 1.2, -0.2]) and abs(om - 4 / 7) < 1e-15
+    corr = {}
+    for t in range(1, g["r"].shape[0]):
+        r2 = np.vstack([g["r"][t], g["rD"][t]])
+        f2 = np.vstack([g["f"][t], g["fD"][t]])
+        r2c, _, _, _ = orc.selffield(r2, f2, om if t > 1 else 0.6)
+        corr[t] = r2c[ns:]
+    for t in range(5, g["r"].shape[0]):
+        pred = sum(B[i] * corr[t - 1 - i] for i in range(4))
+        assert np.abs(pred - g["rD"][t]).max() < 1e-10
