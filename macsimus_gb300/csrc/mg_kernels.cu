@@ -213,27 +213,24 @@ __global__ void __launch_bounds__(PAIR_THREADS)
           float f = 0;
           if ((q.w >> 8) == mol_i) {
             // excluded intramolecular pair: its Ewald correction is large and
-            // cancels the self term, so it is evaluated and summed in FP64
+            // cancels the self term; the term is evaluated in FP32 (an FP64
+            // erf on a divergent lane would stall the warp on the slow FP64
+            // pipe) and summed straight into the FP64 accumulators
             if (P.qq != 0.f) {
-              const double ex = (double)(int)((unsigned)me.x - (unsigned)q.x) * (a.Lx * 2.3283064365386963e-10);
-              const double ey = (double)(int)((unsigned)me.y - (unsigned)q.y) * (a.Ly * 2.3283064365386963e-10);
-              const double ez = (double)(int)((unsigned)me.z - (unsigned)q.z) * (a.Lz * 2.3283064365386963e-10);
-              const double err = ex * ex + ey * ey + ez * ez;
-              double fe;
-              const double e = excl_term<double>(err, a.alpha, &fe);
-              const double qq = P.qqd;
-              fe *= qq;
-              fx += fe * ex;
-              fy += fe * ey;
-              fz += fe * ez;
+              float fe;
+              const float e = excl_term<float>(rr, alpha, &fe);
+              const double fq = (double)fe * P.qqd;
+              fx += fq * dx;
+              fy += fq * dy;
+              fz += fq * dz;
               if (MEASURE) {
-                en[0] += e * qq;
-                en[3] += ex * fe * ex;
-                en[4] += ey * fe * ey;
-                en[5] += ez * fe * ez;
-                en[6] += ez * fe * ey;
-                en[7] += ex * fe * ez;
-                en[8] += ey * fe * ex;
+                en[0] += (double)e * P.qqd;
+                en[3] += fq * dx * dx;
+                en[4] += fq * dy * dy;
+                en[5] += fq * dz * dz;
+                en[6] += fq * dz * dy;
+                en[7] += fq * dx * dz;
+                en[8] += fq * dy * dx;
               }
             }
             continue;
