@@ -155,6 +155,31 @@ int mg_profile_entry(mg_ctx *ctx, int i, const char **name, double *ms, long *co
    events (the FP32 roofline denominator; no counterpart in the reference). */
 int mg_probe_fp32_tflops(double *tflops);
 
+/* k-space Ewald forces and energy without any memory allocation.
+   No counterpart in the reference (cook allocates its Ewald tables per call).
+   For callers that cannot allocate device memory -- a host program that hands
+   all device memory out from its own fixed pool, or a time-critical loop that
+   cannot afford cudaMalloc/cudaFree and the device-wide synchronization they
+   can imply -- this variant keeps all of its scratch in a fixed array inside
+   the library: every GPU that loads the library holds it (about 4.4 MB) until
+   the process exits.  Inputs and outputs stay the caller's: r_dev [3*nq]
+   charge positions and q_dev [nq] charges (device), f_dev [3*nq] forces
+   (device, overwritten), *energy (host: k-space + self term, may be NULL);
+   L, alpha, kappa as in mg_params; stream is a cudaStream_t (NULL: default
+   stream); the call returns after the work is done.  Limits: at most
+   MG_NOALLOC_MAX_CHARGES charges, MG_NOALLOC_MAX_KVEC k-vectors, phase rows
+   of at most MG_NOALLOC_MAX_ROW entries ((Kx+1)+(2Ky+1)+(2Kz+1)); larger
+   inputs return MG_ERR_SIZE.  The first call on a device looks up the
+   array's device address (make it before any stream capture).  All calls
+   share the array and keep the last call's data in it: calls that overlap on
+   the GPU (or run concurrently from several host threads) race. */
+#define MG_NOALLOC_MAX_CHARGES 4096
+#define MG_NOALLOC_MAX_KVEC 4096
+#define MG_NOALLOC_MAX_ROW 96
+int mg_ewald_kspace_noalloc(const double *r_dev, const double *q_dev, int nq, const double L[3],
+                            double alpha, double kappa, double *f_dev, double *energy,
+                            void *stream);
+
 #ifdef __cplusplus
 }
 #endif

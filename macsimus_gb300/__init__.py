@@ -96,6 +96,8 @@ def library():
         L.mg_profile_entry.argtypes = [vp, C.c_int, C.POINTER(C.c_char_p), _dp,
                                        C.POINTER(C.c_long)]
         L.mg_probe_fp32_tflops.argtypes = [_dp]
+        L.mg_ewald_kspace_noalloc.argtypes = [vp, vp, C.c_int, _dp, C.c_double, C.c_double, vp,
+                                              _dp, vp]
         _lib = L
     return _lib
 
