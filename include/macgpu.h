@@ -87,6 +87,10 @@ typedef struct {
   double omegac;     /* SHAKE over-relaxation (cook's omegac; <=0 selects 1.2) */
   int shake_maxit;   /* SHAKE sweep limit per molecule (<=0 selects 1000) */
   int cells_per_cutoff; /* linked-cell subdivision (0 = automatic) */
+  /* Drude builds (cook option -p2K0 and scf.eps<=-1, sim/pred2.c, sim/scf.c) */
+  int aspc_k;        /* ASPC predictor length k (0..9; cook -p2K0) */
+  int scf_iter;      /* force evaluations + SCF iterations per step (|scf.eps|, >=1) */
+  double scf_omega;  /* SCF mixing when aspc_k == 0 (ASPC sets (k+2)/(2k+3) itself) */
 } mg_params;
 
 /* Energies of one force evaluation (program units, K).
@@ -127,8 +131,21 @@ int mg_forces_device(mg_ctx *ctx, const double *r_dev, double *f_dev, int measur
    k-space + self + dipole energy in *energy when energy != NULL */
 int mg_ewald(mg_ctx *ctx, const double *r, double *f, double *energy);
 
+/* One SCF iteration of the Drude displacements, cook's
+   int selffield(ToIntPtr B, ToIntPtr A, eps, omega, run) (sim/scf.c:12,
+   sim/constrd.h:8): on host arrays r (2*ns vectors, Drude half updated) and
+   f (2*ns vectors as returned by mg_forces; the Drude force is folded into
+   the centre); with measure, *en gets the self-pair Ewald term added to el,
+   the spring energy in self and its virial added to Pvir (*en must hold the
+   energies of the forces call). */
+int mg_selffield(mg_ctx *ctx, double *r, double *f, double omega, int measure, mg_energy *en);
+
 /* Device-resident MD (leap-frog Verlet + SHAKE, sim/constrd.c Shake with
-   SHAKE=1, VERLET=3, no thermostat): state r = r(t), r1 = r(t)-r(t-h). */
+   SHAKE=1, VERLET=3, no thermostat): state r = r(t), r1 = r(t)-r(t-h).
+   Drude builds: r holds the Drude displacements after the sites, r1 the
+   displacements of the previous step (cook's cfg[0], cfg[1] polar halves);
+   every step runs the ASPC predictor, scf_iter force + SCF iterations and
+   SHAKE (sim/constrd.c:726-736). */
 int mg_md_set_state(mg_ctx *ctx, const double *r, const double *r1);
 int mg_md_get_state(mg_ctx *ctx, double *r, double *r1);
 /* advance nsteps; energies of the last step in *en when en != NULL */

@@ -49,7 +49,8 @@ class Params(C.Structure):
                 ("rshift", C.c_int), ("rplus", C.c_double), ("epsinf", C.c_double),
                 ("precision", C.c_int), ("h", C.c_double), ("epsc", C.c_double),
                 ("omegac", C.c_double), ("shake_maxit", C.c_int),
-                ("cells_per_cutoff", C.c_int)]
+                ("cells_per_cutoff", C.c_int), ("aspc_k", C.c_int), ("scf_iter", C.c_int),
+                ("scf_omega", C.c_double)]
 
 
 class Energy(C.Structure):
@@ -90,6 +91,7 @@ def library():
         L.mg_md_set_state.argtypes = [vp, _dp, _dp]
         L.mg_md_get_state.argtypes = [vp, _dp, _dp]
         L.mg_md_steps.argtypes = [vp, C.c_int, C.POINTER(Energy)]
+        L.mg_selffield.argtypes = [vp, _dp, _dp, C.c_double, C.c_int, C.POINTER(Energy)]
         L.mg_set_stream.argtypes = [vp, vp]
         L.mg_profile_enable.argtypes = [vp, C.c_int]
         L.mg_profile_reset.argtypes = [vp]
@@ -120,7 +122,7 @@ class ForcePath:
 
     def __init__(self, system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None,
                  grid=256, rshift=3, rplus=2.5, epsinf=3e33, h=0.002, epsc=1e-7, omegac=1.2,
-                 shake_maxit=1000, cells_per_cutoff=0):
+                 shake_maxit=1000, cells_per_cutoff=0, aspc_k=2, scf_iter=1, scf_omega=0.6):
         lib = library()
         self.system = system
         self.ns = system.ns
@@ -152,8 +154,13 @@ class ForcePath:
         t.cons = ip(system.cons.reshape(-1))
         t.cons_len = dp(system.cons_len)
         t.mol_cfirst = ip(system.mol_cfirst)
-        t.chargepol = None
-        t.alphapol = None
+        self.polar = getattr(system, "polar", False)
+        if self.polar:
+            t.chargepol = dp(system.qpol)
+            t.alphapol = dp(system.alphapol)
+        else:
+            t.chargepol = None
+            t.alphapol = None
         p = Params()
         Lb = np.broadcast_to(np.asarray(L, dtype=np.float64), (3,))
         for k in range(3):
@@ -172,6 +179,9 @@ class ForcePath:
         p.omegac = omegac
         p.shake_maxit = shake_maxit
         p.cells_per_cutoff = cells_per_cutoff
+        p.aspc_k = aspc_k
+        p.scf_iter = scf_iter
+        p.scf_omega = scf_omega
         st = C.c_int(0)
         self._ctx = lib.mg_create(C.byref(t), C.byref(p), C.byref(st))
         if not self._ctx:
@@ -225,6 +235,24 @@ class ForcePath:
                                        C.byref(e)))
         return f.reshape(-1, 3), e.value
 
+    def selffield(self, r, f, omega, en=None):
+        """cook selffield(): one SCF iteration; r, f with 2*ns vectors.
+        Returns (r, f, en) with en the energies of the forces call updated"""
+        r = _arr(r, np.float64).reshape(-1).copy()
+        f = _arr(f, np.float64).reshape(-1).copy()
+        e = Energy()
+        if en is not None:
+            for k, v in en.items():
+                if k == "Pvir":
+                    for m in range(6):
+                        e.Pvir[m] = v[m]
+                else:
+                    setattr(e, k, v)
+        self._check(library().mg_selffield(self._ctx, r.ctypes.data_as(_dp),
+                                           f.ctypes.data_as(_dp), omega, int(en is not None),
+                                           C.byref(e)))
+        return r.reshape(-1, 3), f.reshape(-1, 3), (e.asdict() if en is not None else None)
+
     def md_set_state(self, r, r1):
         r = _arr(r, np.float64).reshape(-1)
         r1 = _arr(r1, np.float64).reshape(-1)
@@ -232,8 +260,9 @@ class ForcePath:
                                               r1.ctypes.data_as(_dp)))
 
     def md_get_state(self):
-        r = np.empty(3 * self.ns)
-        r1 = np.empty(3 * self.ns)
+        nv = 3 * self.ns * (2 if self.polar else 1)
+        r = np.empty(nv)
+        r1 = np.empty(nv)
         self._check(library().mg_md_get_state(self._ctx, r.ctypes.data_as(_dp),
                                               r1.ctypes.data_as(_dp)))
         return r.reshape(-1, 3), r1.reshape(-1, 3)

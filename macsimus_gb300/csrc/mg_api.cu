@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -25,6 +26,7 @@ struct mg_ctx {
   int shake_maxit = 1000;
   int ncx = 0, ncy = 0, ncz = 0, ncell = 0, nstencil = 0, sort_bits = 1;
   bool allpairs = false;
+  int ntab = 0;
   int Kx = 0, Ky = 0, Kz = 0, row = 0, ntask = 0, ncol = 0, nchunk = 1;
   cudaStream_t stream = nullptr;
   // host copies
@@ -73,6 +75,15 @@ struct mg_ctx {
   double* d_sums = nullptr;  // [0..9] pair, [10..16] k-space, [17] kinetic
   double* h_sums = nullptr;  // pinned
   bool have_state = false;
+  // Drude
+  bool polar = false;
+  int nd = 0, ndblocks = 0, aspc_k = 2, aspc_kk = 0, scf_iter = 1, hist_h = 0;
+  double scf_omega = 0.6, cur_omega = 0.6;
+  int *d_dsite = nullptr, *d_qdrude = nullptr;
+  double *d_qc = nullptr, *d_qp = nullptr, *d_aqq = nullptr, *d_hist = nullptr,
+         *d_drpart = nullptr;
+  float4* d_pdj = nullptr;
+  double4* d_pdd = nullptr;
   // stream ownership and per-kernel event timing
   cudaStream_t own_stream = nullptr;
   bool prof_on = false;
@@ -161,8 +172,8 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   if (!t || !p || t->ns <= 0 || t->nmol <= 0 || !t->mol_first || !t->site_type || !t->charge ||
       !t->mass || t->ntypes <= 0 || !t->type_EvdW || !t->type_RvdW)
     return fail(ctx, MG_ERR_ARG, "incomplete topology");
-  if (t->chargepol)
-    return fail(ctx, MG_ERR_ARG, "Drude charges are not supported by this build of the context");
+  if (t->chargepol && !t->alphapol)
+    return fail(ctx, MG_ERR_ARG, "Drude charges need alphapol");
   if (p->precision != MG_FP64 && p->precision != MG_MIXED)
     return fail(ctx, MG_ERR_ARG, "precision must be MG_FP64 or MG_MIXED");
   if (!(p->cutoff > 0) || !(p->alpha > 0) || !(p->kappa > 0))
@@ -185,14 +196,19 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   ctx->epsc = p->epsc > 0 ? p->epsc : 1e-7;
   ctx->omega = 0.5 * (p->omegac > 0 ? p->omegac : 1.2);
   ctx->shake_maxit = p->shake_maxit > 0 ? p->shake_maxit : 1000;
+  ctx->polar = t->chargepol != nullptr;
+  ctx->aspc_k = p->aspc_k;
+  if (ctx->aspc_k < 0 || ctx->aspc_k > 9) return fail(ctx, MG_ERR_ARG, "aspc_k must be 0..9");
+  ctx->scf_iter = p->scf_iter > 0 ? p->scf_iter : 1;
+  ctx->scf_omega = p->scf_omega > 0 ? p->scf_omega : 0.6;
   CK(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
   ctx->stream = ctx->own_stream;
   const int ns = t->ns;
 
-  // ---- site kinds: distinct (LJ type, charge) combinations
-  std::map<std::pair<int, double>, int> kinds;
+  // ---- site kinds: distinct (LJ type, charge, Drude charge) combinations
+  std::map<std::tuple<int, double, double>, int> kinds;
   std::vector<int> kind_type;
-  std::vector<double> kind_q;
+  std::vector<double> kind_q, kind_qp;
   ctx->h_kind.resize(ns);
   ctx->h_mol.resize(ns);
   for (int n = 0; n < t->nmol; n++)
@@ -201,18 +217,21 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   for (int i = 0; i < ns; i++) {
     if (t->site_type[i] < 0 || t->site_type[i] >= t->ntypes)
       return fail(ctx, MG_ERR_ARG, "site type out of range");
-    auto key = std::make_pair(t->site_type[i], t->charge[i]);
+    const double qp = ctx->polar ? t->chargepol[i] : 0.0;
+    auto key = std::make_tuple(t->site_type[i], t->charge[i], qp);
     auto it = kinds.find(key);
     if (it == kinds.end()) {
       int k = (int)kind_type.size();
       kinds[key] = k;
       kind_type.push_back(t->site_type[i]);
       kind_q.push_back(t->charge[i]);
+      kind_qp.push_back(qp);
       ctx->h_kind[i] = k;
     } else {
       ctx->h_kind[i] = it->second;
     }
-    sumq2 += t->charge[i] * t->charge[i];
+    // the self term takes the total charge of the site (sim/ewald.c:395-410)
+    sumq2 += (t->charge[i] + qp) * (t->charge[i] + qp);
   }
   ctx->nkind = (int)kind_type.size();
   if (ctx->nkind > MAX_KINDS) return fail(ctx, MG_ERR_SIZE, "more than 16 site kinds");
@@ -237,11 +256,14 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   for (int a = 0; a < ctx->nkind; a++)
     for (int b = 0; b < ctx->nkind; b++) {
       const PairLJ& P = tp[kind_type[a] * t->ntypes + kind_type[b]];
-      double qq = kind_q[a] * kind_q[b];
-      pd[a * ctx->nkind + b] = PairD{P.C1q, P.C2q, P.A4, P.E24, P.Sq, qq, P.A, P.E4};
+      const double qq = kind_q[a] * kind_q[b], qpc = kind_qp[a] * kind_q[b],
+                   qcp = kind_q[a] * kind_qp[b], qpp = kind_qp[a] * kind_qp[b];
+      pd[a * ctx->nkind + b] =
+          PairD{P.C1q, P.C2q, P.A4, P.E24, P.Sq, qq, P.A, P.E4, qpc, qcp, qpp, 0.0};
       pf[a * ctx->nkind + b] = PairF{(float)P.C1q, (float)P.C2q, (float)P.A4, (float)P.E24,
                                      (float)P.Sq,  (float)qq,    (float)P.A,  (float)P.E4,
-                                     qq,           0.0};
+                                     (float)qpc,   (float)qcp,   (float)qpp,  0.f,
+                                     qq,           qpc,          qcp,         qpp};
     }
 
   // ---- erfc spline table over [0, cutoff + rplus)
@@ -271,6 +293,7 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
     if (ok) break;
   }
   ctx->allpairs = allpairs;
+  ctx->ntab = (int)(ert.size() / 6);
   ctx->ncx = nc3[0];
   ctx->ncy = nc3[1];
   ctx->ncz = nc3[2];
@@ -351,15 +374,29 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   ctx->np1job = (int)p1job.size();
   ctx->row = (ctx->Kx + 1) + (2 * ctx->Ky + 1) + (2 * ctx->Kz + 1);
 
-  // ---- charges
-  std::vector<int> qsite;
-  std::vector<double> qval;
-  for (int i = 0; i < ns; i++)
+  // ---- charges of the Ewald sums: centres, then the site's Drude charge
+  std::vector<int> qsite, qdrude, dsite;
+  std::vector<double> qval, dqc, dqp, daqq;
+  for (int i = 0; i < ns; i++) {
     if (t->charge[i] != 0) {
       qsite.push_back(i);
       qval.push_back(t->charge[i]);
+      qdrude.push_back(0);
     }
+    if (ctx->polar && t->chargepol[i] != 0) {
+      qsite.push_back(i);
+      qval.push_back(t->chargepol[i]);
+      qdrude.push_back(1);
+      dsite.push_back(i);
+      dqc.push_back(t->charge[i]);
+      dqp.push_back(t->chargepol[i]);
+      // cook: si->alpha_qq = alphapol / chargepol^2 (cook/simdef.c:1008-1010)
+      daqq.push_back(t->alphapol[i] / (t->chargepol[i] * t->chargepol[i]));
+    }
+  }
   ctx->nq = (int)qsite.size();
+  ctx->nd = (int)dsite.size();
+  ctx->ndblocks = (ctx->nd + 127) / 128;
   // charge chunks of pass 1: about 8 CTAs per SM, at least 64 charges each
   ctx->nchunk = std::max(1, std::min(std::max(1, ctx->nq / 64),
                                      (8 * 152 + ctx->np1job - 1) / ctx->np1job));
@@ -385,11 +422,23 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
     imass[i] = t->mass[i] > 0 ? 1 / t->mass[i] : 0;
   }
 
-  // ---- device buffers
-  CK(dalloc(&ctx->d_r, 3 * (size_t)ns));
-  CK(dalloc(&ctx->d_f, 3 * (size_t)ns));
-  CK(dalloc(&ctx->d_r1, 3 * (size_t)ns));
+  // ---- device buffers (Drude builds: 2*ns vectors, cook's polar half)
+  const size_t nvec = 3 * (size_t)ns * (ctx->polar ? 2 : 1);
+  CK(dalloc(&ctx->d_r, nvec));
+  CK(dalloc(&ctx->d_f, nvec));
+  CK(dalloc(&ctx->d_r1, nvec));
   CK(dalloc(&ctx->d_p, 3 * (size_t)ns));
+  if (ctx->polar) {
+    CK(upload(&ctx->d_dsite, dsite.data(), dsite.size()));
+    CK(upload(&ctx->d_qc, dqc.data(), dqc.size()));
+    CK(upload(&ctx->d_qp, dqp.data(), dqp.size()));
+    CK(upload(&ctx->d_aqq, daqq.data(), daqq.size()));
+    CK(upload(&ctx->d_qdrude, qdrude.data(), qdrude.size()));
+    CK(dalloc(&ctx->d_hist, (size_t)(ctx->aspc_k + 2) * 3 * std::max(ctx->nd, 1)));
+    CK(dalloc(&ctx->d_drpart, (size_t)std::max(ctx->ndblocks, 1) * 8));
+    if (p->precision == MG_MIXED) CK(dalloc(&ctx->d_pdj, ns));
+    else CK(dalloc(&ctx->d_pdd, ns));
+  }
   CK(upload(&ctx->d_kind, ctx->h_kind.data(), ns));
   CK(upload(&ctx->d_mol, ctx->h_mol.data(), ns));
   CK(dalloc(&ctx->d_key, ns));
@@ -483,6 +532,9 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
   pa.alpha = ctx->alpha;
   pa.f = f_dev;
   pa.epart = ctx->d_epart;
+  pa.ntab = ctx->ntab;
+  pa.pdj = ctx->d_pdj;
+  pa.pdd = ctx->d_pdd;
   KArgs ka;
   ka.nq = ctx->nq;
   ka.nk = ctx->nk;
@@ -513,12 +565,14 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
   ka.ntile = ctx->ntile;
   ka.p1job = ctx->d_p1job;
   ka.np1job = ctx->np1job;
-  ka.qdrude = nullptr;
+  ka.qdrude = ctx->d_qdrude;
   ka.ns = ctx->ns;
   if (ctx->precision == MG_MIXED) {
     PROF("cell_list", k_gather_mixed(L, ns, r_dev, ctx->d_order, ctx->d_kind, ctx->d_mol, ctx->L[0], ctx->L[1],
                       ctx->L[2], ctx->d_pj));
-    PROF("pair_mixed", k_pair_mixed(L, pa, ctx->d_pj, ctx->d_ptabf, ctx->d_erd, ctx->d_eru, measure));
+    if (ctx->polar) PROF("cell_list", k_gather_drude(L, ns, r_dev, ctx->d_order, ctx->d_pdj, nullptr));
+    PROF("pair_mixed", k_pair_mixed(L, pa, ctx->d_pj, ctx->d_ptabf, ctx->d_erd, ctx->d_eru, measure,
+                                    ctx->polar));
     if (ctx->nq > 0) {
       PROF("phase_tables", k_phase_tables_mixed(L, ka, r_dev, (float2*)ctx->d_tab));
       PROF("ewald_sk", k_sk_gemm_mixed(L, ka, (const float2*)ctx->d_tab, (float2*)ctx->d_part));
@@ -528,7 +582,8 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
   } else {
     PROF("cell_list", k_gather_fp64(L, ns, r_dev, ctx->d_order, ctx->d_kind, ctx->d_mol, ctx->L[0], ctx->L[1],
                      ctx->L[2], ctx->d_pd));
-    PROF("pair_fp64", k_pair_fp64(L, pa, ctx->d_pd, ctx->d_ptabd, ctx->d_ert, measure));
+    if (ctx->polar) PROF("cell_list", k_gather_drude(L, ns, r_dev, ctx->d_order, nullptr, ctx->d_pdd));
+    PROF("pair_fp64", k_pair_fp64(L, pa, ctx->d_pd, ctx->d_ptabd, ctx->d_ert, measure, ctx->polar));
     if (ctx->nq > 0) {
       PROF("phase_tables", k_phase_tables_fp64(L, ka, r_dev, (double2*)ctx->d_tab));
       PROF("ewald_sk", k_sk_gemm_fp64(L, ka, (const double2*)ctx->d_tab, (double2*)ctx->d_part));
@@ -541,6 +596,37 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
     if (ctx->nq > 0) PROF("reduce", k_reduce_sum(L, ctx->d_ekpart, ctx->nkblocks, 7, ctx->d_sums + 10));
   }
   return MG_OK;
+}
+
+DrudeArgs drude_args(mg_ctx* ctx) {
+  DrudeArgs d;
+  d.nd = ctx->nd;
+  d.ns = ctx->ns;
+  d.dsite = ctx->d_dsite;
+  d.qc = ctx->d_qc;
+  d.qp = ctx->d_qp;
+  d.aqq = ctx->d_aqq;
+  d.alpha = ctx->alpha;
+  d.part = ctx->d_drpart;
+  return d;
+}
+
+// one SCF iteration on the device arrays r, f; with measure its energy
+// partials are reduced into d_sums[20..27] (el, 2*self, Pvir)
+int selffield_async(mg_ctx* ctx, double* r, double* f, double omega, bool measure,
+                    double* hist_out) {
+  Launch L = launch(ctx);
+  DrudeArgs d = drude_args(ctx);
+  PROF("drude_scf", k_selffield(L, d, omega, r, f, hist_out));
+  if (measure) PROF("reduce", k_reduce_sum(L, ctx->d_drpart, ctx->ndblocks, 8, ctx->d_sums + 20));
+  return MG_OK;
+}
+
+void add_drude_energy(mg_ctx* ctx, mg_energy* en) {
+  const double* s = ctx->h_sums;
+  en->el += s[20];
+  en->self = s[21] / 2;
+  for (int m = 0; m < 6; m++) en->Pvir[m] += s[22 + m];
 }
 
 // energies from the reduced sums (host, after the stream has been synchronized)
@@ -614,7 +700,8 @@ int mg_destroy(mg_ctx* ctx) {
                   ctx->d_tab,    ctx->d_part,    ctx->d_ekpart, ctx->d_mol_first,
                   ctx->d_mol_cfirst, ctx->d_cons, ctx->d_bondq, ctx->d_imass, ctx->d_mass,
                   ctx->d_kinpart, ctx->d_status, ctx->d_sums, ctx->d_krows,
-                  ctx->d_tiles, ctx->d_p1job};
+                  ctx->d_tiles, ctx->d_p1job, ctx->d_dsite, ctx->d_qdrude, ctx->d_qc,
+                  ctx->d_qp, ctx->d_aqq, ctx->d_hist, ctx->d_drpart, ctx->d_pdj, ctx->d_pdd};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ctx->h_sums) cudaFreeHost(ctx->h_sums);
@@ -652,7 +739,7 @@ int mg_forces_device(mg_ctx* ctx, const double* r_dev, double* f_dev, int measur
 int mg_forces(mg_ctx* ctx, const double* r, double* f, int measure, mg_energy* en) {
   if (!ctx || !r || !f) return fail(ctx, MG_ERR_ARG, "null argument");
   ctx->launches = 0;
-  const size_t nb = 3 * (size_t)ctx->ns * sizeof(double);
+  const size_t nb = 3 * (size_t)ctx->ns * (ctx->polar ? 2 : 1) * sizeof(double);
   CK(cudaMemcpyAsync(ctx->d_r, r, nb, cudaMemcpyHostToDevice, ctx->stream));
   int rc = forces_async(ctx, ctx->d_r, ctx->d_f, measure != 0);
   if (rc) return rc;
@@ -676,7 +763,7 @@ int mg_ewald(mg_ctx* ctx, const double* r, double* f, double* energy) {
   // full forces minus the r-space part is not separable cheaply here: run
   // the k-space kernels alone on a zeroed force buffer
   ctx->launches = 0;
-  const size_t nb = 3 * (size_t)ctx->ns * sizeof(double);
+  const size_t nb = 3 * (size_t)ctx->ns * (ctx->polar ? 2 : 1) * sizeof(double);
   Launch L = launch(ctx);
   CK(cudaMemcpyAsync(ctx->d_r, r, nb, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemsetAsync(ctx->d_f, 0, nb, ctx->stream));
@@ -711,7 +798,7 @@ int mg_ewald(mg_ctx* ctx, const double* r, double* f, double* energy) {
   ka.ntile = ctx->ntile;
   ka.p1job = ctx->d_p1job;
   ka.np1job = ctx->np1job;
-  ka.qdrude = nullptr;
+  ka.qdrude = ctx->d_qdrude;
   ka.ns = ctx->ns;
   if (ctx->nq > 0) {
     if (ctx->precision == MG_MIXED) {
@@ -739,9 +826,23 @@ int mg_ewald(mg_ctx* ctx, const double* r, double* f, double* energy) {
 
 int mg_md_set_state(mg_ctx* ctx, const double* r, const double* r1) {
   if (!ctx || !r || !r1) return fail(ctx, MG_ERR_ARG, "null argument");
-  const size_t nb = 3 * (size_t)ctx->ns * sizeof(double);
+  const size_t nb = 3 * (size_t)ctx->ns * (ctx->polar ? 2 : 1) * sizeof(double);
   CK(cudaMemcpyAsync(ctx->d_r, r, nb, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->d_r1, r1, nb, cudaMemcpyHostToDevice, ctx->stream));
+  if (ctx->polar && ctx->nd > 0) {
+    // ASPC history as cook starts it (sim/pred2.c:45-55): the latest slot is
+    // rpol(t) from r, the previous one rpol(t-h) from r1, older slots zero
+    Launch L = launch(ctx);
+    DrudeArgs d = drude_args(ctx);
+    const int K2 = ctx->aspc_k + 2;
+    const size_t slot = 3 * (size_t)ctx->nd;
+    CK(cudaMemsetAsync(ctx->d_hist, 0, sizeof(double) * slot * K2, ctx->stream));
+    CK(k_drude_take(L, d, ctx->d_r, ctx->d_hist));
+    CK(k_drude_take(L, d, ctx->d_r1, ctx->d_hist + slot * (K2 - 1)));
+    ctx->hist_h = 0;
+    ctx->aspc_kk = 0;
+    ctx->cur_omega = ctx->scf_omega;
+  }
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->have_state = true;
   return MG_OK;
@@ -749,7 +850,7 @@ int mg_md_set_state(mg_ctx* ctx, const double* r, const double* r1) {
 
 int mg_md_get_state(mg_ctx* ctx, double* r, double* r1) {
   if (!ctx || !ctx->have_state) return fail(ctx, MG_ERR_ARG, "no MD state");
-  const size_t nb = 3 * (size_t)ctx->ns * sizeof(double);
+  const size_t nb = 3 * (size_t)ctx->ns * (ctx->polar ? 2 : 1) * sizeof(double);
   if (r) CK(cudaMemcpyAsync(r, ctx->d_r, nb, cudaMemcpyDeviceToHost, ctx->stream));
   if (r1) CK(cudaMemcpyAsync(r1, ctx->d_r1, nb, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -782,8 +883,36 @@ int mg_md_steps(mg_ctx* ctx, int nsteps, mg_energy* en) {
   for (int s = 0; s < nsteps; s++) {
     const bool last = s == nsteps - 1;
     const bool measure = last && en != nullptr;
-    int rc = forces_async(ctx, ctx->d_r, ctx->d_f, measure);
-    if (rc) return rc;
+    if (ctx->polar && ctx->nd > 0) {
+      // ASPC predictor, then scf_iter force evaluations each followed by one
+      // SCF iteration (sim/constrd.c:726-736, sim/pred2.c:56-97)
+      const int K2 = ctx->aspc_k + 2;
+      const size_t slot = 3 * (size_t)ctx->nd;
+      AspcCoef B;
+      double om;
+      aspc_coefficients(ctx->aspc_kk, B.b, &om);
+      B.n = ctx->aspc_kk + 2;
+      DrudeArgs d = drude_args(ctx);
+      PROF("drude_aspc", k_aspc_predict(L, d, ctx->d_hist, K2, ctx->hist_h, B, ctx->d_r));
+      if (ctx->aspc_kk < ctx->aspc_k) {
+        ctx->aspc_kk++;
+        aspc_coefficients(ctx->aspc_kk, B.b, &om);
+        ctx->cur_omega = om;
+      }
+      const int hn = (ctx->hist_h + 1) % K2;
+      for (int it = 0; it < ctx->scf_iter; it++) {
+        const bool lastit = it == ctx->scf_iter - 1;
+        int rc = forces_async(ctx, ctx->d_r, ctx->d_f, measure && lastit);
+        if (rc) return rc;
+        rc = selffield_async(ctx, ctx->d_r, ctx->d_f, ctx->cur_omega, measure && lastit,
+                             lastit ? ctx->d_hist + slot * hn : nullptr);
+        if (rc) return rc;
+      }
+      ctx->hist_h = hn;
+    } else {
+      int rc = forces_async(ctx, ctx->d_r, ctx->d_f, measure);
+      if (rc) return rc;
+    }
     PROF("shake", k_shake(L, sa));
     if (measure) PROF("reduce", k_reduce_sum(L, ctx->d_kinpart, nkin, 1, ctx->d_sums + 17));
   }
@@ -799,8 +928,30 @@ int mg_md_steps(mg_ctx* ctx, int nsteps, mg_energy* en) {
   if (rc) return rc;
   if (en) {
     fill_energy(ctx, en);
+    if (ctx->polar && ctx->nd > 0) add_drude_energy(ctx, en);
     en->ekin = ctx->h_sums[17] / (ctx->h * ctx->h) / 4;
   }
+  return MG_OK;
+}
+
+int mg_selffield(mg_ctx* ctx, double* r, double* f, double omega, int measure, mg_energy* en) {
+  if (!ctx || !r || !f) return fail(ctx, MG_ERR_ARG, "null argument");
+  if (!ctx->polar) return fail(ctx, MG_ERR_ARG, "no Drude charges in this context");
+  ctx->launches = 0;
+  const size_t nb = 6 * (size_t)ctx->ns * sizeof(double);
+  CK(cudaMemcpyAsync(ctx->d_r, r, nb, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_f, f, nb, cudaMemcpyHostToDevice, ctx->stream));
+  int rc = selffield_async(ctx, ctx->d_r, ctx->d_f, omega, measure && en, nullptr);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(r, ctx->d_r, nb, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(f, ctx->d_f, nb, cudaMemcpyDeviceToHost, ctx->stream));
+  if (measure && en) {
+    rc = fetch_sums(ctx);
+    if (rc) return rc;
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  prof_resolve(ctx);
+  if (measure && en) add_drude_energy(ctx, en);
   return MG_OK;
 }
 

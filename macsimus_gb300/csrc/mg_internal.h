@@ -21,18 +21,21 @@ int erfc_table_size(int grid, double maxr, double alpha);
 void erfc_table(int grid, double maxr, double cutoff, double alpha, int shift,
                 std::vector<double>* tab, double* sgrid);
 int kvector_set(const double L[3], double* kappa, std::vector<int>* kv);
+void aspc_coefficients(int k, double* B, double* omega);
 
 // ---------------------------------------------------------------- device --
 
 // per pair-of-kinds constants (kind = LJ type x charge class); FP32 copy
+// charge products: qq centre-centre, qpc Drude(i)-centre(j), qcp centre(i)-
+// Drude(j), qpp Drude-Drude (zero without Drude charges)
 struct PairF {
-  float C1q, C2q, A4, E24;   // force
-  float Sq, qq, A, E4;       // + energy
-  double qqd;                // qq in FP64 (excluded intramolecular pairs)
-  double pad;
+  float C1q, C2q, A4, E24;        // LJ force
+  float Sq, qq, A, E4;            // LJ energy, centre-centre charge product
+  float qpc, qcp, qpp, pad;
+  double qqd, qpcd, qcpd, qppd;   // the charge products in FP64 (exclusions)
 };
 struct PairD {
-  double C1q, C2q, A4, E24, Sq, qq, A, E4;
+  double C1q, C2q, A4, E24, Sq, qq, A, E4, qpc, qcp, qpp, pad;
 };
 
 // one k-space task: a run of <=KZT consecutive kz of one (kx,ky) column
@@ -77,6 +80,9 @@ cudaError_t k_gather_mixed(const Launch& L, int ns, const double* r, const int* 
 cudaError_t k_gather_fp64(const Launch& L, int ns, const double* r, const int* order,
                           const int* kind, const int* mol, double Lx, double Ly, double Lz,
                           double4* pd);
+// Drude builds: sorted Drude displacements (second half of r)
+cudaError_t k_gather_drude(const Launch& L, int ns, const double* r, const int* order,
+                           float4* pdj, double4* pdd);
 
 struct PairArgs {
   int ns, ncx, ncy, ncz, nstencil, nkind;
@@ -90,12 +96,15 @@ struct PairArgs {
   double alpha;
   double* f;                // [3*ns] output (original order), overwritten
   double* epart;            // [nblocks*10] partial energies (measure)
+  int ntab;                 // erfc spline intervals (lookups are clamped)
+  const float4* pdj;        // mixed, Drude builds: sorted Drude displacements
+  const double4* pdd;       // FP64, Drude builds: sorted Drude displacements
 };
 cudaError_t k_pair_mixed(const Launch& L, const PairArgs& a, const int4* pj,
                          const PairF* ptab, const float4* erd, const float4* eru,
-                         bool measure);
+                         bool measure, bool polar);
 cudaError_t k_pair_fp64(const Launch& L, const PairArgs& a, const double4* pd,
-                        const PairD* ptab, const double* ertab, bool measure);
+                        const PairD* ptab, const double* ertab, bool measure, bool polar);
 
 struct KArgs {
   int nq, nk, ntask, ncol, nchunk;
@@ -153,6 +162,26 @@ struct ShakeArgs {
   int* status;         // set to 1 on non-convergence
 };
 cudaError_t k_shake(const Launch& L, const ShakeArgs& a);
+
+// Drude sites (mg_drude.cu)
+struct DrudeArgs {
+  int nd, ns;
+  const int* dsite;    // [nd] sites carrying a Drude charge
+  const double* qc;    // [nd] central charge of the site
+  const double* qp;    // [nd] Drude charge
+  const double* aqq;   // [nd] alpha_qq = alphapol/qp^2
+  double alpha;        // Ewald alpha
+  double* part;        // [nblocks*8] el, self, Pvir0..5
+};
+struct AspcCoef {
+  int n;
+  double b[12];
+};
+cudaError_t k_selffield(const Launch& L, const DrudeArgs& a, double omega, double* r, double* f,
+                        double* hist_out);
+cudaError_t k_aspc_predict(const Launch& L, const DrudeArgs& a, const double* hist, int K2, int h,
+                           const AspcCoef& B, double* r);
+cudaError_t k_drude_take(const Launch& L, const DrudeArgs& a, const double* r, double* out);
 cudaError_t k_fma_probe(cudaStream_t s, int blocks, int threads, int iters, float* out);
 
 }  // namespace mg

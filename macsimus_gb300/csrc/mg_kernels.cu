@@ -132,12 +132,14 @@ cudaError_t k_gather_fp64(const Launch& L, int ns, const double* r, const int* o
 // ---------------------------------------------------------- pair kernels --
 
 constexpr int NWARP = PAIR_THREADS / 32;
-constexpr int FOLD = 8;   // stencil cells per FP32 batch before the FP64 fold
+constexpr int FOLD = 8;   // stencil cells per FP32 force batch before the FP64 fold
 constexpr int NEN = 10;   // er, lj, vir, Pvir[6], (spare)
 
-// Ewald exclusion term -erf(alpha r)/r and its f/r (cook's exacterud_sqrt)
+// Ewald exclusion term -erf(alpha r)/r and its f/r (cook's exacterud_sqrt);
+// with minus_const the constant 2 alpha/sqrt(pi) is taken off the energy
+// (exacterud_sqrt_1, the centre-Drude pair of one site)
 template <typename T>
-__device__ __forceinline__ T excl_term(T rr, T alpha, T* erd) {
+__device__ __forceinline__ T excl_term(T rr, T alpha, T* erd, bool minus_const = false) {
   const T A = alpha * (T)(-1.1283791670955126);  // -2 alpha/sqrt(pi)
   T aq = alpha * alpha, err = aq * rr;
   if (err < (T)0.01) {
@@ -147,29 +149,86 @@ __device__ __forceinline__ T excl_term(T rr, T alpha, T* erd) {
       T rn = q / (T)(2 * n + 1);
       sd += rn * (T)n;
       su += rn;
-      if (fabs(q) < (T)1e-16) break;
+      if (fabs(q) < (T)1e-17) break;
       q *= -err / (T)(n + 1);
     }
     *erd = A * aq * 2 * sd;
-    return A * (1 - su * err);
+    return minus_const ? A * (-su * err) : A * (1 - su * err);
   }
   T r = sqrt(rr);
   T y = -erf(alpha * r) / r;
   *erd = (y - A * exp(-err)) / rr;
-  return y;
+  return minus_const ? y - A : y;
 }
 
+// f/r of a spline term (erd), energy (eru) added to e when MEASURE
 template <bool MEASURE>
+__device__ __forceinline__ float spline_term(const float4* __restrict__ erd,
+                                             const float4* __restrict__ eru, float r2, float sgrid,
+                                             int ntab, float qq, float& e) {
+  const int ix = min((int)(r2 * sgrid), ntab - 1);
+  const float4 d = __ldg(erd + ix);
+  if (MEASURE) {
+    const float4 u = __ldg(eru + ix);
+    e += (__fdividef(u.y, u.z + r2) + u.x) * qq;
+  }
+  return (__fdividef(d.y, d.z + r2) + d.x) * qq;
+}
+
+// excluded intramolecular term: its Ewald correction is large and cancels
+// the self term; evaluated in FP32 (an FP64 erf on a divergent lane would
+// stall the warp on the slow FP64 pipe) and summed into FP64
+template <bool MEASURE>
+__device__ __forceinline__ void excl_acc(float dx, float dy, float dz, double qq, float alpha,
+                                         double& fx, double& fy, double& fz, double* en) {
+  float fe;
+  const float e = excl_term<float>(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), alpha, &fe);
+  const double fq = (double)fe * qq;
+  fx += fq * dx;
+  fy += fq * dy;
+  fz += fq * dz;
+  if (MEASURE) {
+    en[0] += (double)e * qq;
+    en[3] += fq * dx * dx;
+    en[4] += fq * dy * dy;
+    en[5] += fq * dz * dz;
+    en[6] += fq * dz * dy;
+    en[7] += fq * dx * dz;
+    en[8] += fq * dy * dx;
+  }
+}
+
+struct PvF {
+  float p0, p1, p2, p3, p4, p5;
+  __device__ __forceinline__ void zero() { p0 = p1 = p2 = p3 = p4 = p5 = 0.f; }
+  __device__ __forceinline__ void add(float dx, float dy, float dz, float f) {
+    const float fdx = f * dx, fdy = f * dy, fdz = f * dz;
+    p0 = fmaf(dx, fdx, p0);
+    p1 = fmaf(dy, fdy, p1);
+    p2 = fmaf(dz, fdz, p2);
+    p3 = fmaf(dz, fdy, p3);
+    p4 = fmaf(dx, fdz, p4);
+    p5 = fmaf(dy, fdx, p5);
+  }
+};
+
+// One CTA per home cell; its 4 warps split the neighbour-cell stencil, each
+// staging 32 neighbour sites at a time in shared memory; lane = home site.
+// Full shell: forces only on the home site.  POLAR adds the Drude terms of
+// cook/ljqqpol.c (centre-Drude, Drude-centre, Drude-Drude, each at its own
+// separation); Drude forces go to the second half of f.
+template <bool MEASURE, bool POLAR>
 __global__ void __launch_bounds__(PAIR_THREADS)
     pair_mixed_kernel(PairArgs a, const int4* __restrict__ pj, const PairF* __restrict__ ptab_g,
                       const float4* __restrict__ erd, const float4* __restrict__ eru, float sx,
                       float sy, float sz, float cq, float sgrid, float alpha) {
   __shared__ PairF ptab[MAX_KINDS * MAX_KINDS];
   __shared__ int4 sj[NWARP][32];
-  __shared__ double red[NWARP][32][3];
+  __shared__ float4 sjd[POLAR ? NWARP : 1][32];
+  __shared__ double red[NWARP][32][POLAR ? 6 : 3];
   __shared__ double ered[PAIR_THREADS];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nk = a.nkind;
+  const int nk = a.nkind, ntab = a.ntab;
   for (int t = threadIdx.x; t < nk * nk; t += PAIR_THREADS) ptab[t] = ptab_g[t];
   __syncthreads();
 
@@ -184,10 +243,13 @@ __global__ void __launch_bounds__(PAIR_THREADS)
     const bool vi = ib + lane < ni;
     const int ti = i0 + ib + lane;
     const int4 me = vi ? pj[ti] : make_int4(0, 0, 0, 0);
+    const float4 md = (POLAR && vi) ? a.pdj[ti] : make_float4(0.f, 0.f, 0.f, 0.f);
     const int kind_i = me.w & 255, mol_i = me.w >> 8;
-    double fx = 0, fy = 0, fz = 0;
-    float ax = 0, ay = 0, az = 0;
-    float e_el = 0, e_lj = 0, e_vir = 0, p0 = 0, p1 = 0, p2 = 0, p3 = 0, p4 = 0, p5 = 0;
+    double fx = 0, fy = 0, fz = 0, gx = 0, gy = 0, gz = 0;
+    float ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;
+    float e_el = 0, e_lj = 0, e_vir = 0;
+    PvF pv;
+    pv.zero();
     int nb = 0;
     for (int s = warp; s < a.nstencil; s += NWARP) {
       const int4 o = a.stencil[s];
@@ -198,7 +260,10 @@ __global__ void __launch_bounds__(PAIR_THREADS)
       const int c2 = (x2 * a.ncy + y2) * a.ncz + z2;
       const int j0 = a.cell_start[c2], nj = a.cell_start[c2 + 1] - j0;
       for (int jb = 0; jb < nj; jb += 32) {
-        if (jb + lane < nj) sj[warp][lane] = pj[j0 + jb + lane];
+        if (jb + lane < nj) {
+          sj[warp][lane] = pj[j0 + jb + lane];
+          if (POLAR) sjd[warp][lane] = a.pdj[j0 + jb + lane];
+        }
         __syncwarp();
         const int cnt = min(32, nj - jb);
         for (int jj = 0; jj < cnt; jj++) {
@@ -210,68 +275,71 @@ __global__ void __launch_bounds__(PAIR_THREADS)
           const float rr = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
           if (!vi || rr >= cq || j0 + jb + jj == ti) continue;
           const PairF P = ptab[kind_i * nk + (q.w & 255)];
-          float f = 0;
+          float4 qd = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (POLAR) qd = sjd[warp][jj];
           if ((q.w >> 8) == mol_i) {
-            // excluded intramolecular pair: its Ewald correction is large and
-            // cancels the self term; the term is evaluated in FP32 (an FP64
-            // erf on a divergent lane would stall the warp on the slow FP64
-            // pipe) and summed straight into the FP64 accumulators
-            if (P.qq != 0.f) {
-              float fe;
-              const float e = excl_term<float>(rr, alpha, &fe);
-              const double fq = (double)fe * P.qqd;
-              fx += fq * dx;
-              fy += fq * dy;
-              fz += fq * dz;
-              if (MEASURE) {
-                en[0] += (double)e * P.qqd;
-                en[3] += fq * dx * dx;
-                en[4] += fq * dy * dy;
-                en[5] += fq * dz * dz;
-                en[6] += fq * dz * dy;
-                en[7] += fq * dx * dz;
-                en[8] += fq * dy * dx;
-              }
+            if (P.qq != 0.f) excl_acc<MEASURE>(dx, dy, dz, P.qqd, alpha, fx, fy, fz, en);
+            if (POLAR) {
+              if (P.qpc != 0.f)
+                excl_acc<MEASURE>(dx + md.x, dy + md.y, dz + md.z, P.qpcd, alpha, gx, gy, gz, en);
+              if (P.qcp != 0.f)
+                excl_acc<MEASURE>(dx - qd.x, dy - qd.y, dz - qd.z, P.qcpd, alpha, fx, fy, fz, en);
+              if (P.qpp != 0.f)
+                excl_acc<MEASURE>(dx + md.x - qd.x, dy + md.y - qd.y, dz + md.z - qd.z, P.qppd,
+                                  alpha, gx, gy, gz, en);
             }
             continue;
-          } else {
-            if (rr < P.C2q) {
-              float U;
-              if (rr < P.C1q) {
-                const float x = P.Sq / rr, y = x * x * x;
-                f = P.E24 * fmaf(2.f * y, y, -y) * x;
-                U = P.E4 * fmaf(y, y, -y);
-              } else {
-                const float x = rr - P.C2q;
-                f = P.A4 * x;
-                U = P.A * x * x;
-              }
-              if (MEASURE) {
-                e_lj += U;
-                e_vir += rr * f;
-              }
+          }
+          float f = 0;
+          if (rr < P.C2q) {
+            float U;
+            if (rr < P.C1q) {
+              const float x = P.Sq / rr, y = x * x * x;
+              f = P.E24 * fmaf(2.f * y, y, -y) * x;
+              U = P.E4 * fmaf(y, y, -y);
+            } else {
+              const float x = rr - P.C2q;
+              f = P.A4 * x;
+              U = P.A * x * x;
             }
-            if (P.qq != 0.f) {
-              const int ix = (int)(rr * sgrid);
-              const float4 d = __ldg(erd + ix);
-              f = fmaf(__fdividef(d.y, d.z + rr) + d.x, P.qq, f);
-              if (MEASURE) {
-                const float4 u = __ldg(eru + ix);
-                e_el += (__fdividef(u.y, u.z + rr) + u.x) * P.qq;
-              }
+            if (MEASURE) {
+              e_lj += U;
+              e_vir += rr * f;
             }
           }
-          const float fdx = f * dx, fdy = f * dy, fdz = f * dz;
-          ax += fdx;
-          ay += fdy;
-          az += fdz;
-          if (MEASURE) {
-            p0 = fmaf(dx, fdx, p0);
-            p1 = fmaf(dy, fdy, p1);
-            p2 = fmaf(dz, fdz, p2);
-            p3 = fmaf(dz, fdy, p3);
-            p4 = fmaf(dx, fdz, p4);
-            p5 = fmaf(dy, fdx, p5);
+          if (P.qq != 0.f) f += spline_term<MEASURE>(erd, eru, rr, sgrid, ntab, P.qq, e_el);
+          ax = fmaf(f, dx, ax);
+          ay = fmaf(f, dy, ay);
+          az = fmaf(f, dz, az);
+          if (MEASURE) pv.add(dx, dy, dz, f);
+          if (POLAR) {
+            if (P.qpc != 0.f) {  // Drude(i) - centre(j)
+              const float ex = dx + md.x, ey = dy + md.y, ez = dz + md.z;
+              const float fp = spline_term<MEASURE>(erd, eru, fmaf(ex, ex, fmaf(ey, ey, ez * ez)),
+                                                    sgrid, ntab, P.qpc, e_el);
+              bx = fmaf(fp, ex, bx);
+              by = fmaf(fp, ey, by);
+              bz = fmaf(fp, ez, bz);
+              if (MEASURE) pv.add(ex, ey, ez, fp);
+            }
+            if (P.qcp != 0.f) {  // centre(i) - Drude(j)
+              const float ex = dx - qd.x, ey = dy - qd.y, ez = dz - qd.z;
+              const float fp = spline_term<MEASURE>(erd, eru, fmaf(ex, ex, fmaf(ey, ey, ez * ez)),
+                                                    sgrid, ntab, P.qcp, e_el);
+              ax = fmaf(fp, ex, ax);
+              ay = fmaf(fp, ey, ay);
+              az = fmaf(fp, ez, az);
+              if (MEASURE) pv.add(ex, ey, ez, fp);
+            }
+            if (P.qpp != 0.f) {  // Drude(i) - Drude(j)
+              const float ex = dx + md.x - qd.x, ey = dy + md.y - qd.y, ez = dz + md.z - qd.z;
+              const float fp = spline_term<MEASURE>(erd, eru, fmaf(ex, ex, fmaf(ey, ey, ez * ez)),
+                                                    sgrid, ntab, P.qpp, e_el);
+              bx = fmaf(fp, ex, bx);
+              by = fmaf(fp, ey, by);
+              bz = fmaf(fp, ez, bz);
+              if (MEASURE) pv.add(ex, ey, ez, fp);
+            }
           }
         }
         __syncwarp();
@@ -279,36 +347,47 @@ __global__ void __launch_bounds__(PAIR_THREADS)
       // energies fold into FP64 after every neighbour cell, forces every FOLD
       if (MEASURE) {
         en[0] += e_el; en[1] += e_lj; en[2] += e_vir;
-        en[3] += p0; en[4] += p1; en[5] += p2; en[6] += p3; en[7] += p4; en[8] += p5;
-        e_el = e_lj = e_vir = p0 = p1 = p2 = p3 = p4 = p5 = 0;
+        en[3] += pv.p0; en[4] += pv.p1; en[5] += pv.p2;
+        en[6] += pv.p3; en[7] += pv.p4; en[8] += pv.p5;
+        e_el = e_lj = e_vir = 0;
+        pv.zero();
       }
       if (++nb == FOLD) {
         nb = 0;
         fx += ax; fy += ay; fz += az;
         ax = ay = az = 0;
+        if (POLAR) {
+          gx += bx; gy += by; gz += bz;
+          bx = by = bz = 0;
+        }
       }
     }
     fx += ax; fy += ay; fz += az;
-    if (MEASURE) {
-      en[0] += e_el; en[1] += e_lj; en[2] += e_vir;
-      en[3] += p0; en[4] += p1; en[5] += p2; en[6] += p3; en[7] += p4; en[8] += p5;
-    }
     red[warp][lane][0] = fx;
     red[warp][lane][1] = fy;
     red[warp][lane][2] = fz;
+    if (POLAR) {
+      gx += bx; gy += by; gz += bz;
+      red[warp][lane][POLAR ? 3 : 0] = gx;
+      red[warp][lane][POLAR ? 4 : 0] = gy;
+      red[warp][lane][POLAR ? 5 : 0] = gz;
+    }
     __syncthreads();
     if (warp == 0 && vi) {
-      double gx = 0, gy = 0, gz = 0;
+      double g[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll
-      for (int w = 0; w < NWARP; w++) {
-        gx += red[w][lane][0];
-        gy += red[w][lane][1];
-        gz += red[w][lane][2];
-      }
+      for (int w = 0; w < NWARP; w++)
+#pragma unroll
+        for (int k = 0; k < (POLAR ? 6 : 3); k++) g[k] += red[w][lane][k];
       const int site = a.order[ti];
-      a.f[3 * site] = gx;
-      a.f[3 * site + 1] = gy;
-      a.f[3 * site + 2] = gz;
+      a.f[3 * site] = g[0];
+      a.f[3 * site + 1] = g[1];
+      a.f[3 * site + 2] = g[2];
+      if (POLAR) {
+        a.f[3 * (long)a.ns + 3 * site] = g[3];
+        a.f[3 * (long)a.ns + 3 * site + 1] = g[4];
+        a.f[3 * (long)a.ns + 3 * site + 2] = g[5];
+      }
     }
     __syncthreads();
   }
@@ -328,32 +407,73 @@ __global__ void __launch_bounds__(PAIR_THREADS)
 }
 
 cudaError_t k_pair_mixed(const Launch& L, const PairArgs& a, const int4* pj, const PairF* ptab,
-                         const float4* erd, const float4* eru, bool measure) {
+                         const float4* erd, const float4* eru, bool measure, bool polar) {
   int ncell = a.ncx * a.ncy * a.ncz;
   float sx = (float)(a.Lx / 4294967296.0), sy = (float)(a.Ly / 4294967296.0),
         sz = (float)(a.Lz / 4294967296.0);
-  if (measure)
-    pair_mixed_kernel<true><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pj, ptab, erd, eru, sx, sy, sz,
-                                                             (float)a.cutoff_sq, (float)a.sgrid,
-                                                             (float)a.alpha);
-  else
-    pair_mixed_kernel<false><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pj, ptab, erd, eru, sx, sy, sz,
-                                                              (float)a.cutoff_sq, (float)a.sgrid,
-                                                              (float)a.alpha);
+  const float cq = (float)a.cutoff_sq, sg = (float)a.sgrid, al = (float)a.alpha;
+  if (polar) {
+    if (measure)
+      pair_mixed_kernel<true, true><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pj, ptab, erd, eru, sx,
+                                                                     sy, sz, cq, sg, al);
+    else
+      pair_mixed_kernel<false, true><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pj, ptab, erd, eru, sx,
+                                                                      sy, sz, cq, sg, al);
+  } else {
+    if (measure)
+      pair_mixed_kernel<true, false><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pj, ptab, erd, eru, sx,
+                                                                      sy, sz, cq, sg, al);
+    else
+      pair_mixed_kernel<false, false><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pj, ptab, erd, eru, sx,
+                                                                       sy, sz, cq, sg, al);
+  }
   LAUNCHED(L);
   return cudaGetLastError();
 }
 
+// FP64 term at separation (dx,dy,dz): spline or exact exclusion; adds the
+// force to (fx,fy,fz) and energy/virial to en
 template <bool MEASURE>
+__device__ __forceinline__ void term64(double dx, double dy, double dz, double qq, bool excl,
+                                       const double* __restrict__ ert, double sgrid, int ntab,
+                                       double alpha, double& fx, double& fy, double& fz,
+                                       double* en) {
+  const double r2 = dx * dx + dy * dy + dz * dz;
+  double f, e;
+  if (excl) {
+    e = excl_term<double>(r2, alpha, &f);
+  } else {
+    const double* p = ert + 6 * min((int)(r2 * sgrid), ntab - 1);
+    f = p[4] / (p[5] + r2) + p[3];
+    e = p[1] / (p[2] + r2) + p[0];
+  }
+  f *= qq;
+  const double fdx = f * dx, fdy = f * dy, fdz = f * dz;
+  fx += fdx;
+  fy += fdy;
+  fz += fdz;
+  if (MEASURE) {
+    en[0] += e * qq;
+    en[3] += dx * fdx;
+    en[4] += dy * fdy;
+    en[5] += dz * fdz;
+    en[6] += dz * fdy;
+    en[7] += dx * fdz;
+    en[8] += dy * fdx;
+  }
+}
+
+template <bool MEASURE, bool POLAR>
 __global__ void __launch_bounds__(PAIR_THREADS)
     pair_fp64_kernel(PairArgs a, const double4* __restrict__ pd, const PairD* __restrict__ ptab_g,
                      const double* __restrict__ ert) {
   __shared__ PairD ptab[MAX_KINDS * MAX_KINDS];
   __shared__ double4 sj[NWARP][32];
-  __shared__ double red[NWARP][32][3];
+  __shared__ double4 sjd[POLAR ? NWARP : 1][32];
+  __shared__ double red[NWARP][32][POLAR ? 6 : 3];
   __shared__ double ered[PAIR_THREADS];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nk = a.nkind;
+  const int nk = a.nkind, ntab = a.ntab;
   for (int t = threadIdx.x; t < nk * nk; t += PAIR_THREADS) ptab[t] = ptab_g[t];
   __syncthreads();
   const int c = blockIdx.x;
@@ -367,9 +487,10 @@ __global__ void __launch_bounds__(PAIR_THREADS)
     const bool vi = ib + lane < ni;
     const int ti = i0 + ib + lane;
     const double4 me = vi ? pd[ti] : make_double4(0, 0, 0, 0);
+    const double4 md = (POLAR && vi) ? a.pdd[ti] : make_double4(0, 0, 0, 0);
     const long long wi = __double_as_longlong(me.w);
     const int kind_i = (int)(wi & 255), mol_i = (int)(wi >> 8);
-    double fx = 0, fy = 0, fz = 0;
+    double fx = 0, fy = 0, fz = 0, gx = 0, gy = 0, gz = 0;
     for (int s = warp; s < a.nstencil; s += NWARP) {
       const int4 o = a.stencil[s];
       int x2 = cx + o.x, y2 = cy + o.y, z2 = cz + o.z;
@@ -381,7 +502,10 @@ __global__ void __launch_bounds__(PAIR_THREADS)
       const int c2 = (x2 * a.ncy + y2) * a.ncz + z2;
       const int j0 = a.cell_start[c2], nj = a.cell_start[c2 + 1] - j0;
       for (int jb = 0; jb < nj; jb += 32) {
-        if (jb + lane < nj) sj[warp][lane] = pd[j0 + jb + lane];
+        if (jb + lane < nj) {
+          sj[warp][lane] = pd[j0 + jb + lane];
+          if (POLAR) sjd[warp][lane] = a.pdd[j0 + jb + lane];
+        }
         __syncwarp();
         const int cnt = min(32, nj - jb);
         for (int jj = 0; jj < cnt; jj++) {
@@ -396,48 +520,45 @@ __global__ void __launch_bounds__(PAIR_THREADS)
           if (!vi || rr >= cq || j0 + jb + jj == ti) continue;
           const long long wj = __double_as_longlong(q.w);
           const PairD& P = ptab[kind_i * nk + (int)(wj & 255)];
-          double f = 0;
-          if ((int)(wj >> 8) == mol_i) {
-            if (P.qq != 0) {
-              double fe;
-              double e = excl_term<double>(rr, alpha, &fe);
-              f = fe * P.qq;
-              if (MEASURE) en[0] += e * P.qq;
+          const bool excl = (int)(wj >> 8) == mol_i;
+          if (!excl && rr < P.C2q) {
+            double f, U;
+            if (rr < P.C1q) {
+              const double x = P.Sq / rr, y = x * x * x, z = y * y;
+              f = P.E24 * (z + z - y) * x;
+              U = P.E4 * (z - y);
+            } else {
+              const double x = rr - P.C2q;
+              f = P.A4 * x;
+              U = x * x * P.A;
             }
-          } else {
-            if (rr < P.C2q) {
-              double U;
-              if (rr < P.C1q) {
-                const double x = P.Sq / rr, y = x * x * x, z = y * y;
-                f = P.E24 * (z + z - y) * x;
-                U = P.E4 * (z - y);
-              } else {
-                const double x = rr - P.C2q;
-                f = P.A4 * x;
-                U = x * x * P.A;
-              }
-              if (MEASURE) {
-                en[1] += U;
-                en[2] += rr * f;
-              }
-            }
-            if (P.qq != 0) {
-              const double* e = ert + 6 * (int)(rr * sgrid);
-              f += (e[4] / (e[5] + rr) + e[3]) * P.qq;
-              if (MEASURE) en[0] += (e[1] / (e[2] + rr) + e[0]) * P.qq;
+            fx += f * dx;
+            fy += f * dy;
+            fz += f * dz;
+            if (MEASURE) {
+              en[1] += U;
+              en[2] += rr * f;
+              en[3] += dx * f * dx;
+              en[4] += dy * f * dy;
+              en[5] += dz * f * dz;
+              en[6] += dz * f * dy;
+              en[7] += dx * f * dz;
+              en[8] += dy * f * dx;
             }
           }
-          const double fdx = f * dx, fdy = f * dy, fdz = f * dz;
-          fx += fdx;
-          fy += fdy;
-          fz += fdz;
-          if (MEASURE) {
-            en[3] += dx * fdx;
-            en[4] += dy * fdy;
-            en[5] += dz * fdz;
-            en[6] += dz * fdy;
-            en[7] += dx * fdz;
-            en[8] += dy * fdx;
+          if (P.qq != 0)
+            term64<MEASURE>(dx, dy, dz, P.qq, excl, ert, sgrid, ntab, alpha, fx, fy, fz, en);
+          if (POLAR) {
+            const double4 qd = sjd[warp][jj];
+            if (P.qpc != 0)
+              term64<MEASURE>(dx + md.x, dy + md.y, dz + md.z, P.qpc, excl, ert, sgrid, ntab,
+                              alpha, gx, gy, gz, en);
+            if (P.qcp != 0)
+              term64<MEASURE>(dx - qd.x, dy - qd.y, dz - qd.z, P.qcp, excl, ert, sgrid, ntab,
+                              alpha, fx, fy, fz, en);
+            if (P.qpp != 0)
+              term64<MEASURE>(dx + md.x - qd.x, dy + md.y - qd.y, dz + md.z - qd.z, P.qpp, excl,
+                              ert, sgrid, ntab, alpha, gx, gy, gz, en);
           }
         }
         __syncwarp();
@@ -446,19 +567,27 @@ __global__ void __launch_bounds__(PAIR_THREADS)
     red[warp][lane][0] = fx;
     red[warp][lane][1] = fy;
     red[warp][lane][2] = fz;
+    if (POLAR) {
+      red[warp][lane][POLAR ? 3 : 0] = gx;
+      red[warp][lane][POLAR ? 4 : 0] = gy;
+      red[warp][lane][POLAR ? 5 : 0] = gz;
+    }
     __syncthreads();
     if (warp == 0 && vi) {
-      double gx = 0, gy = 0, gz = 0;
+      double g[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll
-      for (int w = 0; w < NWARP; w++) {
-        gx += red[w][lane][0];
-        gy += red[w][lane][1];
-        gz += red[w][lane][2];
-      }
+      for (int w = 0; w < NWARP; w++)
+#pragma unroll
+        for (int k = 0; k < (POLAR ? 6 : 3); k++) g[k] += red[w][lane][k];
       const int site = a.order[ti];
-      a.f[3 * site] = gx;
-      a.f[3 * site + 1] = gy;
-      a.f[3 * site + 2] = gz;
+      a.f[3 * site] = g[0];
+      a.f[3 * site + 1] = g[1];
+      a.f[3 * site + 2] = g[2];
+      if (POLAR) {
+        a.f[3 * (long)a.ns + 3 * site] = g[3];
+        a.f[3 * (long)a.ns + 3 * site + 1] = g[4];
+        a.f[3 * (long)a.ns + 3 * site + 2] = g[5];
+      }
     }
     __syncthreads();
   }
@@ -477,12 +606,37 @@ __global__ void __launch_bounds__(PAIR_THREADS)
 }
 
 cudaError_t k_pair_fp64(const Launch& L, const PairArgs& a, const double4* pd, const PairD* ptab,
-                        const double* ertab, bool measure) {
+                        const double* ertab, bool measure, bool polar) {
   int ncell = a.ncx * a.ncy * a.ncz;
-  if (measure)
-    pair_fp64_kernel<true><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pd, ptab, ertab);
-  else
-    pair_fp64_kernel<false><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pd, ptab, ertab);
+  if (polar) {
+    if (measure)
+      pair_fp64_kernel<true, true><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pd, ptab, ertab);
+    else
+      pair_fp64_kernel<false, true><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pd, ptab, ertab);
+  } else {
+    if (measure)
+      pair_fp64_kernel<true, false><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pd, ptab, ertab);
+    else
+      pair_fp64_kernel<false, false><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pd, ptab, ertab);
+  }
+  LAUNCHED(L);
+  return cudaGetLastError();
+}
+
+__global__ void gather_drude_kernel(int ns, const double* __restrict__ r,
+                                    const int* __restrict__ order, float4* __restrict__ pdj,
+                                    double4* __restrict__ pdd) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ns) return;
+  const int i = order[t];
+  const double* d = r + 3 * (long)ns + 3 * i;
+  if (pdj) pdj[t] = make_float4((float)d[0], (float)d[1], (float)d[2], 0.f);
+  if (pdd) pdd[t] = make_double4(d[0], d[1], d[2], 0.0);
+}
+
+cudaError_t k_gather_drude(const Launch& L, int ns, const double* r, const int* order,
+                           float4* pdj, double4* pdd) {
+  gather_drude_kernel<<<cdiv(ns, 256), 256, 0, L.s>>>(ns, r, order, pdj, pdd);
   LAUNCHED(L);
   return cudaGetLastError();
 }
@@ -503,7 +657,9 @@ __global__ void phase_tables_mixed_kernel(KArgs a, const double* __restrict__ r,
   else { d = 2; n = e - (a.Kx + 2 * a.Ky + 2) - a.Kz; }
   double Lb = d == 0 ? a.Lx : (d == 1 ? a.Ly : a.Lz);
   // exact integer phase n*s mod 1 in units of 2^-32
-  unsigned int S = (unsigned int)fixed32(r[3 * site + d], Lb);
+  double xd = r[3 * site + d];
+  if (a.qdrude && a.qdrude[j]) xd += r[3 * (long)a.ns + 3 * site + d];
+  unsigned int S = (unsigned int)fixed32(xd, Lb);
   int ph = (int)(S * (unsigned int)n);
   float tt = (float)ph * 2.3283064365386963e-10f;   // in [-0.5, 0.5)
   float sn, cs;
@@ -527,7 +683,9 @@ __global__ void phase_tables_fp64_kernel(KArgs a, const double* __restrict__ r,
   else if (e <= a.Kx + 2 * a.Ky + 1) { d = 1; n = e - (a.Kx + 1) - a.Ky; }
   else { d = 2; n = e - (a.Kx + 2 * a.Ky + 2) - a.Kz; }
   double Lb = d == 0 ? a.Lx : (d == 1 ? a.Ly : a.Lz);
-  double s = r[3 * site + d] / Lb;
+  double xd = r[3 * site + d];
+  if (a.qdrude && a.qdrude[j]) xd += r[3 * (long)a.ns + 3 * site + d];
+  double s = xd / Lb;
   double ph = n * s;
   ph -= rint(ph);
   double sn, cs;

@@ -202,4 +202,22 @@ int kvector_set(const double L[3], double* kappa, std::vector<int>* kv) {
   return -1;
 }
 
+// ASPC predictor of Kolafa (J. Comput. Chem. 25, 335 (2004)) as set up in
+// sim/pred2.c:70-97: B[0..k+1] for predictor length k (k=0: the linear
+// predictor 2, -1) and the mixing omega = (k+2)/(2k+3) that keeps it stable
+void aspc_coefficients(int k, double* B, double* omega) {
+  if (k == 0) {
+    B[0] = 2;
+    B[1] = -1;
+    *omega = 2.0 / 3.0;
+    return;
+  }
+  double o = (double)(4 * k + 6) / (double)(k + 3);
+  for (int i = 0; i < k + 2; i++) {
+    B[i] = o * (i + 1);
+    o *= (double)(i - k - 1) / (double)(k + i + 4);
+  }
+  *omega = (k + 2) / (double)(2 * k + 3);
+}
+
 }  // namespace mg
