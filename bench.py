@@ -94,15 +94,29 @@ class ClockSampler:
 # ------------------------------------------------------------ CPU baseline --
 
 def cpu_md_steps(w, nsteps_max, budget_s, nthreads):
-    """the oracle port (C, pthreads) on the host cores: MD steps of the workload"""
+    """the oracle port (C, pthreads) on the host cores: MD steps of the
+    workload (Drude systems: linear predictor + one SCF iteration per step)"""
     from oracle import oracle as O
-    orc = O.Oracle(w["system"], [w["L"]] * 3, w["cutoff"], w["alpha"], w["kappa"])
+    system = w["system"]
+    ns = system.ns
+    orc = O.Oracle(system, [w["L"]] * 3, w["cutoff"], w["alpha"], w["kappa"])
     r, r1 = w["r"].copy(), w["r1"].copy()
     t0 = time.perf_counter()
     done = 0
+    prev = r[ns:].copy() if system.polar else None
     while done < nsteps_max:
-        f, _ = orc.forces(r, measure=False, nthreads=nthreads)
-        r, r1, it, _ = orc.shake_step(r, r1, f, w["h"], eps=1e-7, omega=0.6)
+        if system.polar:
+            cur = r[ns:].copy()
+            r = np.vstack([r[:ns], 2 * cur - prev])
+            prev = cur
+            f, _ = orc.forces(r, measure=False, nthreads=nthreads)
+            r, f, _, _ = orc.selffield(r, f, 4.0 / 7.0)
+            rs, r1s, it, _ = orc.shake_step(r[:ns], r1[:ns], f[:ns], w["h"], eps=1e-7, omega=0.6)
+            r = np.vstack([rs, r[ns:]])
+            r1 = np.vstack([r1s, r1[ns:]])
+        else:
+            f, _ = orc.forces(r, measure=False, nthreads=nthreads)
+            r, r1, it, _ = orc.shake_step(r, r1, f, w["h"], eps=1e-7, omega=0.6)
         done += 1
         if time.perf_counter() - t0 > budget_s:
             break
@@ -134,12 +148,13 @@ def run_ours(args, rank, world, local):
             dist.barrier()
         torch.cuda.synchronize()
 
+    kw = dict(h=w["h"], epsc=1e-7, aspc_k=w["aspc_k"], scf_iter=w["scf_iter"])
     fp = M.ForcePath(system, [w["L"]] * 3, w["cutoff"], w["alpha"], w["kappa"], precision="mixed",
-                     h=w["h"], epsc=1e-7)
+                     **kw)
     fp.set_stream(stream.cuda_stream)
     # accuracy of the mixed path against the FP64 path on the same input
     f64 = M.ForcePath(system, [w["L"]] * 3, w["cutoff"], w["alpha"], w["kappa"],
-                      precision="fp64", h=w["h"], epsc=1e-7)
+                      precision="fp64", **kw)
     f64.set_stream(stream.cuda_stream)
     fm, _ = fp.forces(w["r"])
     fd, _ = f64.forces(w["r"])
@@ -220,7 +235,7 @@ def run_ours(args, rank, world, local):
 
     # roofline of the dominant kernel (FP32 pipe: no tensor-core contraction here)
     peak = M.fp32_peak_tflops()
-    nq = int((system.q != 0).sum())
+    nq = int((system.q != 0).sum()) + (int((system.qpol != 0).sum()) if system.polar else 0)
     V = w["L"] ** 3
     npairs = ns * (ns - 1) / 2 * (4.0 / 3.0 * math.pi * w["cutoff"] ** 3) / V
     algo = {"ewald_sk": FLOP_PER_KQ * fp.nkvec * nq, "ewald_kforce": FLOP_PER_KQ * fp.nkvec * nq,
@@ -251,11 +266,18 @@ def run_ours(args, rank, world, local):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 5),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "fp32+fp64acc", "data": "synthetic (seeded fcc lattice, random orientations)",
-            "config": {"workload": "%d SPC/E waters (%d sites), L=%.3f A, cutoff %.0f A, "
+            "config": {"workload": "%d %s waters (%d sites%s), L=%.3f A, cutoff %.0f A, "
                                    "alpha %.2f/A, |n|<=%d (%d k-vectors), leap-frog+SHAKE "
-                                   "dt %.0f fs" % (system.nmol, ns, w["L"], w["cutoff"],
-                                                   w["alpha"], 20, fp.nkvec, w["h"] * 1000),
-                       "model": "SPC/E rigid water, Ewald", "global_batch": world,
+                                   "dt %.0f fs%s" % (
+                                       system.nmol, "Drude" if system.polar else "SPC/E", ns,
+                                       " + %d Drude shells" % int((system.qpol != 0).sum())
+                                       if system.polar else "", w["L"], w["cutoff"], w["alpha"],
+                                       w["kn"], fp.nkvec, w["h"] * 1000,
+                                       ", ASPC k=%d + %d SCF iteration(s)" % (w["aspc_k"],
+                                                                               w["scf_iter"])
+                                       if system.polar else ""),
+                       "model": ("SPC/E + Drude shell water" if system.polar else
+                                 "SPC/E rigid water") + ", Ewald", "global_batch": world,
                        "seq_len": ns, "parallelism": "replicas x%d" % world,
                        "l2": "flushed between timed steps (256 MB write)"},
             "atom_steps_per_s": round(atom_steps, 1),
@@ -263,8 +285,8 @@ def run_ours(args, rank, world, local):
             "mixed_over_fp64": round(value / value64, 3),
             "force_rel_rms_vs_fp64": force_err,
             "e2e": {"value": round(e2e, 4), "unit": "ns/day",
-                    "h2d_bytes_per_step": 2 * 3 * ns * 8,
-                    "d2h_bytes_per_step": 2 * 3 * ns * 8 + 18 * 8, "steps": ke2e},
+                    "h2d_bytes_per_step": rh.nbytes + r1h.nbytes,
+                    "d2h_bytes_per_step": rh.nbytes + r1h.nbytes + 18 * 8, "steps": ke2e},
             "gpu_launches": launches,
             "roofline": {"bound": "fp32", "kernel": name, "achieved": round(achieved, 3),
                          "peak": round(peak, 3), "unit": "TFLOP/s",
@@ -304,8 +326,8 @@ def run_reference(args, rank, world):
         "n_gpus": world, "steps": args.steps, "steps_timed": done, "warmup": args.warmup,
         "ms_per_step": round(secs / done * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
-        "config": {"workload": "%d SPC/E waters (%d sites), L=%.3f A" % (w["system"].nmol, ns,
-                                                                         w["L"])},
+        "config": {"workload": "%s: %d molecules (%d sites), L=%.3f A" % (
+            args.workload, w["system"].nmol, ns, w["L"])},
         "cpu_baseline": {"value": round(v, 6), "unit": "ns/day", "cores": nth, "kind": "port",
                          "sample": "%d MD step(s) of the full workload (time box %.0f s)"
                                    % (done, args.ref_budget)},

@@ -92,12 +92,22 @@ WORKLOADS = {
     # 32768 SPC/E waters at 0.997 g/cm3 (L = 99.44 A), cutoff 12, alpha 0.26, |n|<=20
     "spce32768": dict(species=["WAT"], counts=[32768], density=0.997, cutoff=12.0, alpha=0.26,
                       kn=20),
+    # the same box of Drude-polarizable waters (shell on O, alpha 1.44 A^3,
+    # q_D -1.8 e); ASPC k=2 with one SCF iteration per step
+    "drude32768": dict(species=["WATD"], counts=[32768], density=0.997, cutoff=12.0,
+                       alpha=0.26, kn=20, aspc_k=2, scf_iter=1),
 }
 
 
 def workload(name, seed=0, T=298.0, h=0.002):
+    """a named workload; for Drude systems r and r1 carry the shell
+    displacements (zero: shells start on their sites) after the sites"""
     w = WORKLOADS[name]
     L = w.get("L") or box_length(w["species"], w["counts"], w["density"])
     system, r, r1 = build(w["species"], w["counts"], L, seed=seed, T=T, h=h)
+    if system.polar:
+        r = np.vstack([r, np.zeros_like(r)])
+        r1 = np.vstack([r1, np.zeros_like(r1)])
     return dict(name=name, system=system, r=r, r1=r1, L=L, cutoff=w["cutoff"], alpha=w["alpha"],
-                kappa=(w["kn"] + 1e-6) / L, h=h)
+                kappa=(w["kn"] + 1e-6) / L, h=h, kn=w["kn"], aspc_k=w.get("aspc_k", 2),
+                scf_iter=w.get("scf_iter", 1))
