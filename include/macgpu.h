@@ -40,7 +40,8 @@ enum mg_status {
   MG_ERR_SHAKE = 3,        /* SHAKE did not converge (cook: "too many iterations") */
   MG_ERR_NONFINITE = 4,    /* non-finite position or force */
   MG_ERR_SETUP = 5,        /* force-field setup failed (smooth cutoff, k-vectors) */
-  MG_ERR_SIZE = 6          /* size beyond a compiled or stated maximum */
+  MG_ERR_SIZE = 6,         /* size beyond a compiled or stated maximum */
+  MG_ERR_SCF = 7           /* Drude displacement beyond el.minqq (sim/scf.c:142,253) */
 };
 
 enum mg_precision {
@@ -91,6 +92,7 @@ typedef struct {
   int aspc_k;        /* ASPC predictor length k (0..9; cook -p2K0) */
   int scf_iter;      /* force evaluations + SCF iterations per step (|scf.eps|, >=1) */
   double scf_omega;  /* SCF mixing when aspc_k == 0 (ASPC sets (k+2)/(2k+3) itself) */
+  double minqq;      /* largest allowed Drude displacement (el.minqq, default 1 A) */
 } mg_params;
 
 /* Energies of one force evaluation (program units, K).

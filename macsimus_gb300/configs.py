@@ -111,3 +111,40 @@ def workload(name, seed=0, T=298.0, h=0.002):
     return dict(name=name, system=system, r=r, r1=r1, L=L, cutoff=w["cutoff"], alpha=w["alpha"],
                 kappa=(w["kn"] + 1e-6) / L, h=h, kn=w["kn"], aspc_k=w.get("aspc_k", 2),
                 scf_iter=w.get("scf_iter", 1))
+
+
+def equilibrate(w, steps=400, T=298.0, every=20, h=None, **kw):
+    """Relax a lattice start with rigid (non-polarizable) molecules on the
+    GPU: leap-frog + SHAKE with the half-step velocities rescaled to T every
+    ``every`` steps.  Drude systems are relaxed as their SPC/E parents and
+    get their shells back on the sites.  Returns the workload with new r, r1."""
+    import macsimus_gb300 as M
+    system = w["system"]
+    ns = system.ns
+    rigid = system
+    if system.polar:
+        rigid = ff.build_system([s.replace("WATD", "WAT") for s in system.species],
+                                system.counts)
+    hh = h or w["h"]
+    fp = M.ForcePath(rigid, [w["L"]] * 3, w["cutoff"], w["alpha"], w["kappa"],
+                     precision="mixed", h=hh, epsc=1e-7, **kw)
+    r, r1 = w["r"][:ns].copy(), w["r1"][:ns].copy() * (hh / w["h"])
+    nf = 6 * rigid.nmol - 3 if len(rigid.cons_len) else 3 * ns - 3
+    m = rigid.mass[:, None]
+    for _ in range(steps // every):
+        fp.md_set_state(r, r1)
+        fp.md_steps(every, measure=False)
+        r, r1 = fp.md_get_state()
+        ekin = 0.5 * (m * (r1 / hh) ** 2).sum()
+        Tnow = 2 * ekin / nf
+        r1 *= np.sqrt(T / max(Tnow, 1e-6))
+    fp.close()
+    out = dict(w)
+    r1 *= w["h"] / hh
+    if system.polar:
+        out["r"] = np.vstack([r, np.zeros_like(r)])
+        out["r1"] = np.vstack([r1, np.zeros_like(r1)])
+    else:
+        out["r"], out["r1"] = r, r1
+    out["equilibrated"] = steps
+    return out

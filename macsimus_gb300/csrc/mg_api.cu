@@ -78,7 +78,7 @@ struct mg_ctx {
   // Drude
   bool polar = false;
   int nd = 0, ndblocks = 0, aspc_k = 2, aspc_kk = 0, scf_iter = 1, hist_h = 0;
-  double scf_omega = 0.6, cur_omega = 0.6;
+  double scf_omega = 0.6, cur_omega = 0.6, minqq = 1.0;
   int *d_dsite = nullptr, *d_qdrude = nullptr;
   double *d_qc = nullptr, *d_qp = nullptr, *d_aqq = nullptr, *d_hist = nullptr,
          *d_drpart = nullptr;
@@ -201,6 +201,7 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   if (ctx->aspc_k < 0 || ctx->aspc_k > 9) return fail(ctx, MG_ERR_ARG, "aspc_k must be 0..9");
   ctx->scf_iter = p->scf_iter > 0 ? p->scf_iter : 1;
   ctx->scf_omega = p->scf_omega > 0 ? p->scf_omega : 0.6;
+  ctx->minqq = p->minqq > 0 ? p->minqq : 1.0;
   CK(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
   ctx->stream = ctx->own_stream;
   const int ns = t->ns;
@@ -608,6 +609,8 @@ DrudeArgs drude_args(mg_ctx* ctx) {
   d.aqq = ctx->d_aqq;
   d.alpha = ctx->alpha;
   d.part = ctx->d_drpart;
+  d.minqq2 = ctx->minqq * ctx->minqq;
+  d.status = ctx->d_status;
   return d;
 }
 
@@ -669,6 +672,7 @@ int check_status(mg_ctx* ctx) {
   CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   if (st & 2) return fail(ctx, MG_ERR_NONFINITE, "non-finite site position");
+  if (st & 4) return fail(ctx, MG_ERR_SCF, "Drude displacement beyond el.minqq");
   return fail(ctx, MG_ERR_SHAKE, "SHAKE: too many iterations");
 }
 
@@ -949,8 +953,12 @@ int mg_selffield(mg_ctx* ctx, double* r, double* f, double omega, int measure, m
     rc = fetch_sums(ctx);
     if (rc) return rc;
   }
+  rc = fetch_status(ctx);
+  if (rc) return rc;
   CK(cudaStreamSynchronize(ctx->stream));
   prof_resolve(ctx);
+  rc = check_status(ctx);
+  if (rc) return rc;
   if (measure && en) add_drude_energy(ctx, en);
   return MG_OK;
 }

@@ -71,6 +71,9 @@ __global__ void __launch_bounds__(DR_THREADS)
     acc[5] -= n1 * p2;
     acc[6] -= n2 * p0;
     acc[7] -= n0 * p1;
+    // cook stops when a shell leaves the sphere of radius el.minqq around
+    // its site (sim/scf.c:253): flag it, the host reports MG_ERR_SCF
+    if (!(n0 * n0 + n1 * n1 + n2 * n2 < a.minqq2)) atomicOr(a.status, 4);
     rp[0] = n0;
     rp[1] = n1;
     rp[2] = n2;

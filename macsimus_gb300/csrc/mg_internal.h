@@ -172,6 +172,8 @@ struct DrudeArgs {
   const double* aqq;   // [nd] alpha_qq = alphapol/qp^2
   double alpha;        // Ewald alpha
   double* part;        // [nblocks*8] el, self, Pvir0..5
+  double minqq2;       // squared limit of the Drude displacement
+  int* status;         // bit 2 set when a displacement reaches it
 };
 struct AspcCoef {
   int n;

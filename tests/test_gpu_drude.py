@@ -107,3 +107,19 @@ def test_aspc_md_matches_oracle(precision):
     assert np.abs(rg[:ns] - ro[:ns]).max() < tol
     assert np.abs(rg[ns:] - ro[ns:]).max() < tol
     assert np.isfinite(en["self"]) and en["self"] > 0
+
+
+def test_shell_escape_is_reported_not_fatal():
+    """a shell pushed beyond el.minqq (1 A) is reported as MG_ERR_SCF, as
+    cook stops with "DRUDE new cfg" (sim/scf.c:253); the context stays usable"""
+    g, meta, system, ew, fp, orc = setup("fp64")
+    ns = system.ns
+    r2 = np.vstack([g["r"][3], g["rD"][3]])
+    f2, en = fp.forces(r2, measure=True)
+    bad = f2.copy()
+    bad[ns:] *= 1e4          # a huge field on the shells
+    with pytest.raises(M.MGError) as e:
+        fp.selffield(r2, bad, 0.6)
+    assert e.value.code == 7
+    f3, _ = fp.forces(r2)
+    assert rel_rms(f3, f2) < 1e-12
