@@ -41,7 +41,8 @@ enum mg_status {
   MG_ERR_NONFINITE = 4,    /* non-finite position or force */
   MG_ERR_SETUP = 5,        /* force-field setup failed (smooth cutoff, k-vectors) */
   MG_ERR_SIZE = 6,         /* size beyond a compiled or stated maximum */
-  MG_ERR_SCF = 7           /* Drude displacement beyond el.minqq (sim/scf.c:142,253) */
+  MG_ERR_SCF = 7,          /* Drude displacement beyond el.minqq (sim/scf.c:142,253) */
+  MG_ERR_LIST = 8          /* a site moved more than skin/2 between neighbour-list builds */
 };
 
 enum mg_precision {
@@ -93,6 +94,11 @@ typedef struct {
   int scf_iter;      /* force evaluations + SCF iterations per step (|scf.eps|, >=1) */
   double scf_omega;  /* SCF mixing when aspc_k == 0 (ASPC sets (k+2)/(2k+3) itself) */
   double minqq;      /* largest allowed Drude displacement (el.minqq, default 1 A) */
+  /* pair search: Verlet lists of radius cutoff+skin rebuilt every nl_every MD
+     steps (and at every mg_forces call); skin < 0 re-bins the linked cells at
+     every force evaluation as cook does (cook/lc.c) */
+  double skin;       /* A; 0 selects 1.5 */
+  int nl_every;      /* MD steps between list builds; <=0 selects 5 */
 } mg_params;
 
 /* Energies of one force evaluation (program units, K).

@@ -23,7 +23,8 @@ LIBPATH = os.path.join(HERE, "_build", "libmacgpu.so")
 
 MG_FP64, MG_MIXED = 0, 1
 STATUS = {0: "MG_OK", 1: "MG_ERR_ARG", 2: "MG_ERR_CUDA", 3: "MG_ERR_SHAKE",
-          4: "MG_ERR_NONFINITE", 5: "MG_ERR_SETUP", 6: "MG_ERR_SIZE", 7: "MG_ERR_SCF"}
+          4: "MG_ERR_NONFINITE", 5: "MG_ERR_SETUP", 6: "MG_ERR_SIZE", 7: "MG_ERR_SCF",
+          8: "MG_ERR_LIST"}
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -50,7 +51,8 @@ class Params(C.Structure):
                 ("precision", C.c_int), ("h", C.c_double), ("epsc", C.c_double),
                 ("omegac", C.c_double), ("shake_maxit", C.c_int),
                 ("cells_per_cutoff", C.c_int), ("aspc_k", C.c_int), ("scf_iter", C.c_int),
-                ("scf_omega", C.c_double), ("minqq", C.c_double)]
+                ("scf_omega", C.c_double), ("minqq", C.c_double), ("skin", C.c_double),
+                ("nl_every", C.c_int)]
 
 
 class Energy(C.Structure):
@@ -123,7 +125,7 @@ class ForcePath:
     def __init__(self, system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None,
                  grid=256, rshift=3, rplus=2.5, epsinf=3e33, h=0.002, epsc=1e-7, omegac=1.2,
                  shake_maxit=1000, cells_per_cutoff=0, aspc_k=2, scf_iter=1, scf_omega=0.6,
-                 minqq=1.0):
+                 minqq=1.0, skin=1.5, nl_every=5):
         lib = library()
         self.system = system
         self.ns = system.ns
@@ -184,6 +186,8 @@ class ForcePath:
         p.scf_iter = scf_iter
         p.scf_omega = scf_omega
         p.minqq = minqq
+        p.skin = skin
+        p.nl_every = nl_every
         st = C.c_int(0)
         self._ctx = lib.mg_create(C.byref(t), C.byref(p), C.byref(st))
         if not self._ctx:

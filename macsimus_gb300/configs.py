@@ -92,8 +92,9 @@ WORKLOADS = {
     # 32768 SPC/E waters at 0.997 g/cm3 (L = 99.44 A), cutoff 12, alpha 0.26, |n|<=20
     "spce32768": dict(species=["WAT"], counts=[32768], density=0.997, cutoff=12.0, alpha=0.26,
                       kn=20),
-    # the same box of Drude-polarizable waters (shell on O, alpha 1.44 A^3,
-    # q_D -1.8 e); ASPC k=2 with one SCF iteration per step
+    # the same box of Drude-polarizable waters (shell on O, q_D -1.8 e,
+    # k 4184 kJ/mol/A^2, alpha 1.0759 A^3); ASPC k=2 with one SCF iteration
+    # per step
     "drude32768": dict(species=["WATD"], counts=[32768], density=0.997, cutoff=12.0,
                        alpha=0.26, kn=20, aspc_k=2, scf_iter=1),
 }
@@ -113,7 +114,7 @@ def workload(name, seed=0, T=298.0, h=0.002):
                 scf_iter=w.get("scf_iter", 1))
 
 
-def equilibrate(w, steps=400, T=298.0, every=20, h=None, **kw):
+def equilibrate(w, steps=400, T=298.0, every=20, h=None, polar_steps=200, **kw):
     """Relax a lattice start with rigid (non-polarizable) molecules on the
     GPU: leap-frog + SHAKE with the half-step velocities rescaled to T every
     ``every`` steps.  Drude systems are relaxed as their SPC/E parents and
@@ -140,11 +141,23 @@ def equilibrate(w, steps=400, T=298.0, every=20, h=None, **kw):
         r1 *= np.sqrt(T / max(Tnow, 1e-6))
     fp.close()
     out = dict(w)
-    r1 *= w["h"] / hh
     if system.polar:
-        out["r"] = np.vstack([r, np.zeros_like(r)])
-        out["r1"] = np.vstack([r1, np.zeros_like(r1)])
-    else:
-        out["r"], out["r1"] = r, r1
-    out["equilibrated"] = steps
+        # then the polarizable system itself, still with velocity rescaling,
+        # to absorb the polarization energy released when shells switch on
+        r = np.vstack([r, np.zeros_like(r)])
+        r1 = np.vstack([r1, np.zeros_like(r1)])
+        fpp = M.ForcePath(system, [w["L"]] * 3, w["cutoff"], w["alpha"], w["kappa"],
+                          precision="mixed", h=hh, epsc=1e-7, aspc_k=w.get("aspc_k", 2),
+                          scf_iter=w.get("scf_iter", 1), **kw)
+        for _ in range(polar_steps // every):
+            fpp.md_set_state(r, r1)
+            fpp.md_steps(every, measure=False)
+            r, r1 = fpp.md_get_state()
+            ekin = 0.5 * (m * (r1[:ns] / hh) ** 2).sum()
+            Tnow = 2 * ekin / nf
+            r1[:ns] *= np.sqrt(T / max(Tnow, 1e-6))
+        fpp.close()
+    r1[:ns] *= w["h"] / hh
+    out["r"], out["r1"] = r, r1
+    out["equilibrated"] = steps + (polar_steps if system.polar else 0)
     return out

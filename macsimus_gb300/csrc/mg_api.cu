@@ -33,6 +33,7 @@ struct mg_ctx {
   std::vector<int> h_kind, h_mol;
   // device buffers
   double *d_r = nullptr, *d_f = nullptr, *d_r1 = nullptr, *d_p = nullptr;
+  double *d_rs = nullptr, *d_fs = nullptr;  // staging of the host-array calls
   int *d_kind = nullptr, *d_mol = nullptr;
   int *d_key = nullptr, *d_idx = nullptr, *d_key_s = nullptr, *d_order = nullptr;
   int* d_cell_start = nullptr;
@@ -75,6 +76,14 @@ struct mg_ctx {
   double* d_sums = nullptr;  // [0..9] pair, [10..16] k-space, [17] kinetic
   double* h_sums = nullptr;  // pinned
   bool have_state = false;
+  // neighbour lists
+  bool use_list = true, need_build = true;
+  double skin = 1.5;
+  int nl_every = 5, since_build = 0, nl_cap = 0;
+  long nl_pitch = 0;
+  int *d_nlist = nullptr, *d_ncount = nullptr;
+  double* d_rbuild = nullptr;
+  int nepart = 0;
   // Drude
   bool polar = false;
   int nd = 0, ndblocks = 0, aspc_k = 2, aspc_kk = 0, scf_iter = 1, hist_h = 0;
@@ -202,6 +211,9 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   ctx->scf_iter = p->scf_iter > 0 ? p->scf_iter : 1;
   ctx->scf_omega = p->scf_omega > 0 ? p->scf_omega : 0.6;
   ctx->minqq = p->minqq > 0 ? p->minqq : 1.0;
+  ctx->use_list = p->skin >= 0;
+  ctx->skin = p->skin > 0 ? p->skin : 1.5;
+  ctx->nl_every = p->nl_every > 0 ? p->nl_every : 5;
   CK(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
   ctx->stream = ctx->own_stream;
   const int ns = t->ns;
@@ -276,6 +288,8 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
 
   // ---- cells: size >= cutoff/cdiv and at least 2*cdiv+1 cells per edge
   int cdivv = p->cells_per_cutoff > 0 ? p->cells_per_cutoff : 2;
+  // cells cover the list radius cutoff+skin (or the cutoff without lists)
+  const double rgrid = ctx->use_list ? p->cutoff + ctx->skin : p->cutoff;
   int nc3[3] = {1, 1, 1};
   bool allpairs = false;
   for (;; cdivv++) {
@@ -288,7 +302,7 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
     }
     bool ok = true;
     for (int d = 0; d < 3; d++) {
-      nc3[d] = (int)(p->L[d] * cdivv / p->cutoff);
+      nc3[d] = (int)(p->L[d] * cdivv / rgrid);
       if (nc3[d] < 2 * cdivv + 1) ok = false;
     }
     if (ok) break;
@@ -311,7 +325,7 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
                          (double)std::max(std::abs(dy) - 1, 0) * p->L[1] / nc3[1],
                          (double)std::max(std::abs(dz) - 1, 0) * p->L[2] / nc3[2]};
           double dmin2 = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
-          if (dmin2 < p->cutoff * p->cutoff * (1 + 1e-9)) st.push_back(make_int4(dx, dy, dz, 0));
+          if (dmin2 < rgrid * rgrid * (1 + 1e-9)) st.push_back(make_int4(dx, dy, dz, 0));
         }
   }
   ctx->nstencil = (int)st.size();
@@ -428,6 +442,8 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   CK(dalloc(&ctx->d_r, nvec));
   CK(dalloc(&ctx->d_f, nvec));
   CK(dalloc(&ctx->d_r1, nvec));
+  CK(dalloc(&ctx->d_rs, nvec));
+  CK(dalloc(&ctx->d_fs, nvec));
   CK(dalloc(&ctx->d_p, 3 * (size_t)ns));
   if (ctx->polar) {
     CK(upload(&ctx->d_dsite, dsite.data(), dsite.size()));
@@ -451,7 +467,20 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
                                      ctx->d_idx, ctx->d_order, ns, 0, ctx->sort_bits));
   CK(cudaMalloc(&ctx->d_sort_tmp, ctx->sort_tmp_bytes));
   CK(upload(&ctx->d_stencil, st.data(), st.size()));
-  CK(dalloc(&ctx->d_epart, (size_t)ctx->ncell * 10));
+  ctx->nepart = std::max(ctx->ncell, list_blocks(ns));
+  CK(dalloc(&ctx->d_epart, (size_t)ctx->nepart * 10));
+  if (ctx->use_list) {
+    // capacity: the largest expected count in a sphere of the list radius at
+    // 1.5 times the mean site density, in multiples of 32 (grown on overflow)
+    const double V = p->L[0] * p->L[1] * p->L[2], rl = p->cutoff + ctx->skin;
+    ctx->nl_cap = ((int)(1.5 * ns / V * 4.18879 * rl * rl * rl) + 64 + 31) / 32 * 32;
+    ctx->nl_cap = std::min(ctx->nl_cap, ns);
+    ctx->nl_pitch = ((long)ns + 31) / 32 * 32;
+    CK(dalloc(&ctx->d_nlist, (size_t)ctx->nl_cap * ctx->nl_pitch));
+    CK(dalloc(&ctx->d_ncount, ns));
+    CK(dalloc(&ctx->d_rbuild, 3 * (size_t)ns));
+    if (p->precision != MG_MIXED) CK(dalloc(&ctx->d_pj, ns));
+  }
   CK(upload(&ctx->d_qsite, qsite.data(), qsite.size()));
   CK(upload(&ctx->d_qval, qval.data(), qval.size()));
   CK(upload(&ctx->d_task, tasks.data(), tasks.size()));
@@ -502,18 +531,68 @@ Launch launch(mg_ctx* ctx) { return Launch{ctx->stream, &ctx->launches}; }
 
 // forces of the positions in r_dev (device, cook layout) into f_dev; the
 // energies are reduced into d_sums when measure
+ListArgs list_args(mg_ctx* ctx) {
+  ListArgs l;
+  l.ncx = ctx->ncx;
+  l.ncy = ctx->ncy;
+  l.ncz = ctx->ncz;
+  l.nstencil = ctx->nstencil;
+  l.cell_start = ctx->d_cell_start;
+  l.stencil = ctx->d_stencil;
+  l.sx = (float)(ctx->L[0] / 4294967296.0);
+  l.sy = (float)(ctx->L[1] / 4294967296.0);
+  l.sz = (float)(ctx->L[2] / 4294967296.0);
+  const double rl = ctx->cutoff + ctx->skin;
+  l.rlist2 = (float)(rl * rl);
+  l.cap = ctx->nl_cap;
+  l.pitch = ctx->nl_pitch;
+  l.nlist = ctx->d_nlist;
+  l.ncount = ctx->d_ncount;
+  l.status = ctx->d_status;
+  return l;
+}
+
+// Verlet lists of the positions r_dev (cells binned and sorted here): the
+// build is followed by a synchronous overflow check that grows the lists
+int build_lists(mg_ctx* ctx, const double* r_dev) {
+  Launch L = launch(ctx);
+  for (int attempt = 0; attempt < 4; attempt++) {
+    ListArgs l = list_args(ctx);
+    PROF("neighbour_list", k_build_list(L, l, ctx->d_pj));
+    PROF("neighbour_list", k_save_build(L, ctx->ns, r_dev, ctx->d_rbuild));
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (!(st & 16)) {
+      ctx->need_build = false;
+      ctx->since_build = 0;
+      return MG_OK;
+    }
+    st &= ~16;
+    CK(cudaMemcpyAsync(ctx->d_status, &st, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaFree(ctx->d_nlist));
+    ctx->d_nlist = nullptr;
+    ctx->nl_cap = std::min(ctx->ns, ctx->nl_cap * 3 / 2 + 32);
+    CK(dalloc(&ctx->d_nlist, (size_t)ctx->nl_cap * ctx->nl_pitch));
+  }
+  return fail(ctx, MG_ERR_SIZE, "neighbour list capacity");
+}
+
 int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) {
   Launch L = launch(ctx);
   const int ns = ctx->ns;
-  // linked cells
-  PROF("cell_list", k_prep_cells(L, ns, r_dev, ctx->d_status, ctx->L[0], ctx->L[1], ctx->L[2],
-                                 ctx->ncx, ctx->ncy, ctx->ncz, ctx->d_key, ctx->d_idx));
-  PROF("cell_list", cub::DeviceRadixSort::SortPairs(ctx->d_sort_tmp, ctx->sort_tmp_bytes,
-                                                    ctx->d_key, ctx->d_key_s, ctx->d_idx,
-                                                    ctx->d_order, ns, 0, ctx->sort_bits,
-                                                    ctx->stream));
-  ctx->launches += 2;
-  PROF("cell_list", k_cell_bounds(L, ns, ctx->ncell, ctx->d_key_s, ctx->d_cell_start));
+  const bool rebuild = !ctx->use_list || ctx->need_build || ctx->since_build >= ctx->nl_every;
+  if (rebuild) {
+    // linked cells
+    PROF("cell_list", k_prep_cells(L, ns, r_dev, ctx->d_status, ctx->L[0], ctx->L[1], ctx->L[2],
+                                   ctx->ncx, ctx->ncy, ctx->ncz, ctx->d_key, ctx->d_idx));
+    PROF("cell_list", cub::DeviceRadixSort::SortPairs(ctx->d_sort_tmp, ctx->sort_tmp_bytes,
+                                                      ctx->d_key, ctx->d_key_s, ctx->d_idx,
+                                                      ctx->d_order, ns, 0, ctx->sort_bits,
+                                                      ctx->stream));
+    ctx->launches += 2;
+    PROF("cell_list", k_cell_bounds(L, ns, ctx->ncell, ctx->d_key_s, ctx->d_cell_start));
+  }
   PairArgs pa;
   pa.ns = ns;
   pa.ncx = ctx->ncx;
@@ -568,12 +647,25 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
   ka.np1job = ctx->np1job;
   ka.qdrude = ctx->d_qdrude;
   ka.ns = ctx->ns;
+  ListArgs la = list_args(ctx);
+  int nerows = ctx->ncell;
   if (ctx->precision == MG_MIXED) {
-    PROF("cell_list", k_gather_mixed(L, ns, r_dev, ctx->d_order, ctx->d_kind, ctx->d_mol, ctx->L[0], ctx->L[1],
-                      ctx->L[2], ctx->d_pj));
-    if (ctx->polar) PROF("cell_list", k_gather_drude(L, ns, r_dev, ctx->d_order, ctx->d_pdj, nullptr));
-    PROF("pair_mixed", k_pair_mixed(L, pa, ctx->d_pj, ctx->d_ptabf, ctx->d_erd, ctx->d_eru, measure,
-                                    ctx->polar));
+    PROF("gather", k_gather_mixed(L, ns, r_dev, ctx->d_order, ctx->d_kind, ctx->d_mol, ctx->L[0],
+                                  ctx->L[1], ctx->L[2], ctx->d_pj));
+    if (ctx->polar) PROF("gather", k_gather_drude(L, ns, r_dev, ctx->d_order, ctx->d_pdj, nullptr));
+    if (ctx->use_list) {
+      if (rebuild) {
+        int rc = build_lists(ctx, r_dev);
+        if (rc) return rc;
+        la = list_args(ctx);
+      }
+      PROF("pair_mixed", k_pair_list_mixed(L, pa, la, ctx->d_pj, ctx->d_ptabf, ctx->d_erd,
+                                           ctx->d_eru, measure, ctx->polar));
+      nerows = list_blocks(ns);
+    } else {
+      PROF("pair_mixed", k_pair_mixed(L, pa, ctx->d_pj, ctx->d_ptabf, ctx->d_erd, ctx->d_eru,
+                                      measure, ctx->polar));
+    }
     if (ctx->nq > 0) {
       PROF("phase_tables", k_phase_tables_mixed(L, ka, r_dev, (float2*)ctx->d_tab));
       PROF("ewald_sk", k_sk_gemm_mixed(L, ka, (const float2*)ctx->d_tab, (float2*)ctx->d_part));
@@ -581,10 +673,24 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
       PROF("ewald_kforce", k_kf_gemm_mixed(L, ka, (const float2*)ctx->d_tab));
     }
   } else {
-    PROF("cell_list", k_gather_fp64(L, ns, r_dev, ctx->d_order, ctx->d_kind, ctx->d_mol, ctx->L[0], ctx->L[1],
-                     ctx->L[2], ctx->d_pd));
-    if (ctx->polar) PROF("cell_list", k_gather_drude(L, ns, r_dev, ctx->d_order, nullptr, ctx->d_pdd));
-    PROF("pair_fp64", k_pair_fp64(L, pa, ctx->d_pd, ctx->d_ptabd, ctx->d_ert, measure, ctx->polar));
+    PROF("gather", k_gather_fp64(L, ns, r_dev, ctx->d_order, ctx->d_kind, ctx->d_mol, ctx->L[0],
+                                 ctx->L[1], ctx->L[2], ctx->d_pd));
+    if (ctx->polar) PROF("gather", k_gather_drude(L, ns, r_dev, ctx->d_order, nullptr, ctx->d_pdd));
+    if (ctx->use_list) {
+      if (rebuild) {
+        PROF("gather", k_gather_mixed(L, ns, r_dev, ctx->d_order, ctx->d_kind, ctx->d_mol,
+                                      ctx->L[0], ctx->L[1], ctx->L[2], ctx->d_pj));
+        int rc = build_lists(ctx, r_dev);
+        if (rc) return rc;
+        la = list_args(ctx);
+      }
+      PROF("pair_fp64", k_pair_list_fp64(L, pa, la, ctx->d_pd, ctx->d_ptabd, ctx->d_ert, measure,
+                                         ctx->polar));
+      nerows = list_blocks(ns);
+    } else {
+      PROF("pair_fp64", k_pair_fp64(L, pa, ctx->d_pd, ctx->d_ptabd, ctx->d_ert, measure,
+                                    ctx->polar));
+    }
     if (ctx->nq > 0) {
       PROF("phase_tables", k_phase_tables_fp64(L, ka, r_dev, (double2*)ctx->d_tab));
       PROF("ewald_sk", k_sk_gemm_fp64(L, ka, (const double2*)ctx->d_tab, (double2*)ctx->d_part));
@@ -593,7 +699,7 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
     }
   }
   if (measure) {
-    PROF("reduce", k_reduce_sum(L, ctx->d_epart, ctx->ncell, 10, ctx->d_sums));
+    PROF("reduce", k_reduce_sum(L, ctx->d_epart, nerows, 10, ctx->d_sums));
     if (ctx->nq > 0) PROF("reduce", k_reduce_sum(L, ctx->d_ekpart, ctx->nkblocks, 7, ctx->d_sums + 10));
   }
   return MG_OK;
@@ -673,6 +779,10 @@ int check_status(mg_ctx* ctx) {
   CK(cudaStreamSynchronize(ctx->stream));
   if (st & 2) return fail(ctx, MG_ERR_NONFINITE, "non-finite site position");
   if (st & 4) return fail(ctx, MG_ERR_SCF, "Drude displacement beyond el.minqq");
+  if (st & 8)
+    return fail(ctx, MG_ERR_LIST,
+                "a site moved more than skin/2 between neighbour-list builds (larger skin or "
+                "smaller nl_every)");
   return fail(ctx, MG_ERR_SHAKE, "SHAKE: too many iterations");
 }
 
@@ -695,7 +805,7 @@ mg_ctx* mg_create(const mg_topology* top, const mg_params* par, int* status) {
 
 int mg_destroy(mg_ctx* ctx) {
   if (!ctx) return MG_OK;
-  void* bufs[] = {ctx->d_r,      ctx->d_f,       ctx->d_r1,    ctx->d_p,      ctx->d_kind,
+  void* bufs[] = {ctx->d_rs, ctx->d_fs, ctx->d_r,      ctx->d_f,       ctx->d_r1,    ctx->d_p,      ctx->d_kind,
                   ctx->d_mol,    ctx->d_key,     ctx->d_idx,   ctx->d_key_s,  ctx->d_order,
                   ctx->d_cell_start, ctx->d_sort_tmp, ctx->d_pj, ctx->d_pd,  ctx->d_stencil,
                   ctx->d_ptabf,  ctx->d_ptabd,   ctx->d_erd,   ctx->d_eru,    ctx->d_ert,
@@ -705,7 +815,8 @@ int mg_destroy(mg_ctx* ctx) {
                   ctx->d_mol_cfirst, ctx->d_cons, ctx->d_bondq, ctx->d_imass, ctx->d_mass,
                   ctx->d_kinpart, ctx->d_status, ctx->d_sums, ctx->d_krows,
                   ctx->d_tiles, ctx->d_p1job, ctx->d_dsite, ctx->d_qdrude, ctx->d_qc,
-                  ctx->d_qp, ctx->d_aqq, ctx->d_hist, ctx->d_drpart, ctx->d_pdj, ctx->d_pdd};
+                  ctx->d_qp, ctx->d_aqq, ctx->d_hist, ctx->d_drpart, ctx->d_pdj, ctx->d_pdd,
+                  ctx->d_nlist, ctx->d_ncount, ctx->d_rbuild};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ctx->h_sums) cudaFreeHost(ctx->h_sums);
@@ -724,6 +835,7 @@ int mg_forces_device(mg_ctx* ctx, const double* r_dev, double* f_dev, int measur
                      mg_energy* en) {
   if (!ctx || !r_dev || !f_dev) return fail(ctx, MG_ERR_ARG, "null argument");
   ctx->launches = 0;
+  ctx->need_build = true;
   int rc = forces_async(ctx, r_dev, f_dev, measure != 0);
   if (rc) return rc;
   if (measure) {
@@ -736,6 +848,7 @@ int mg_forces_device(mg_ctx* ctx, const double* r_dev, double* f_dev, int measur
   prof_resolve(ctx);
   rc = check_status(ctx);
   if (rc) return rc;
+  ctx->need_build = true;  // the lists now describe these positions, not the MD state
   if (measure && en) fill_energy(ctx, en);
   return MG_OK;
 }
@@ -743,11 +856,12 @@ int mg_forces_device(mg_ctx* ctx, const double* r_dev, double* f_dev, int measur
 int mg_forces(mg_ctx* ctx, const double* r, double* f, int measure, mg_energy* en) {
   if (!ctx || !r || !f) return fail(ctx, MG_ERR_ARG, "null argument");
   ctx->launches = 0;
+  ctx->need_build = true;
   const size_t nb = 3 * (size_t)ctx->ns * (ctx->polar ? 2 : 1) * sizeof(double);
-  CK(cudaMemcpyAsync(ctx->d_r, r, nb, cudaMemcpyHostToDevice, ctx->stream));
-  int rc = forces_async(ctx, ctx->d_r, ctx->d_f, measure != 0);
+  CK(cudaMemcpyAsync(ctx->d_rs, r, nb, cudaMemcpyHostToDevice, ctx->stream));
+  int rc = forces_async(ctx, ctx->d_rs, ctx->d_fs, measure != 0);
   if (rc) return rc;
-  CK(cudaMemcpyAsync(f, ctx->d_f, nb, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(f, ctx->d_fs, nb, cudaMemcpyDeviceToHost, ctx->stream));
   if (measure) {
     rc = fetch_sums(ctx);
     if (rc) return rc;
@@ -758,6 +872,7 @@ int mg_forces(mg_ctx* ctx, const double* r, double* f, int measure, mg_energy* e
   prof_resolve(ctx);
   rc = check_status(ctx);
   if (rc) return rc;
+  ctx->need_build = true;  // the lists now describe these positions, not the MD state
   if (measure && en) fill_energy(ctx, en);
   return MG_OK;
 }
@@ -769,8 +884,8 @@ int mg_ewald(mg_ctx* ctx, const double* r, double* f, double* energy) {
   ctx->launches = 0;
   const size_t nb = 3 * (size_t)ctx->ns * (ctx->polar ? 2 : 1) * sizeof(double);
   Launch L = launch(ctx);
-  CK(cudaMemcpyAsync(ctx->d_r, r, nb, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemsetAsync(ctx->d_f, 0, nb, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_rs, r, nb, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_fs, 0, nb, ctx->stream));
   KArgs ka;
   std::memset(&ka, 0, sizeof(ka));
   ka.nq = ctx->nq;
@@ -795,7 +910,7 @@ int mg_ewald(mg_ctx* ctx, const double* r, double* f, double* energy) {
   ka.S = ctx->d_S;
   ka.Wf = ctx->d_Wf;
   ka.Wd = ctx->d_Wd;
-  ka.f = ctx->d_f;
+  ka.f = ctx->d_fs;
   ka.ek_part = ctx->d_ekpart;
   ka.krows = ctx->d_krows;
   ka.tiles = ctx->d_tiles;
@@ -806,12 +921,12 @@ int mg_ewald(mg_ctx* ctx, const double* r, double* f, double* energy) {
   ka.ns = ctx->ns;
   if (ctx->nq > 0) {
     if (ctx->precision == MG_MIXED) {
-      CK(k_phase_tables_mixed(L, ka, ctx->d_r, (float2*)ctx->d_tab));
+      CK(k_phase_tables_mixed(L, ka, ctx->d_rs, (float2*)ctx->d_tab));
       CK(k_sk_gemm_mixed(L, ka, (const float2*)ctx->d_tab, (float2*)ctx->d_part));
       CK(k_sk_reduce_mixed(L, ka, (const float2*)ctx->d_part, true));
       CK(k_kf_gemm_mixed(L, ka, (const float2*)ctx->d_tab));
     } else {
-      CK(k_phase_tables_fp64(L, ka, ctx->d_r, (double2*)ctx->d_tab));
+      CK(k_phase_tables_fp64(L, ka, ctx->d_rs, (double2*)ctx->d_tab));
       CK(k_sk_gemm_fp64(L, ka, (const double2*)ctx->d_tab, (double2*)ctx->d_part));
       CK(k_sk_reduce_fp64(L, ka, (const double2*)ctx->d_part, true));
       CK(k_kf_gemm_fp64(L, ka, (const double2*)ctx->d_tab));
@@ -819,7 +934,7 @@ int mg_ewald(mg_ctx* ctx, const double* r, double* f, double* energy) {
     CK(k_reduce_sum(L, ctx->d_ekpart, ctx->nkblocks, 7, ctx->d_sums + 10));
   }
   std::vector<double> fk(3 * (size_t)ctx->ns);
-  CK(cudaMemcpyAsync(fk.data(), ctx->d_f, nb, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(fk.data(), ctx->d_fs, nb, cudaMemcpyDeviceToHost, ctx->stream));
   int rc = fetch_sums(ctx);
   if (rc) return rc;
   CK(cudaStreamSynchronize(ctx->stream));
@@ -849,6 +964,7 @@ int mg_md_set_state(mg_ctx* ctx, const double* r, const double* r1) {
   }
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->have_state = true;
+  ctx->need_build = true;
   return MG_OK;
 }
 
@@ -918,6 +1034,11 @@ int mg_md_steps(mg_ctx* ctx, int nsteps, mg_energy* en) {
       if (rc) return rc;
     }
     PROF("shake", k_shake(L, sa));
+    if (ctx->use_list) {
+      ctx->since_build++;
+      PROF("neighbour_list", k_check_skin(L, ctx->ns, ctx->d_r, ctx->d_rbuild,
+                                          0.25 * ctx->skin * ctx->skin, ctx->d_status));
+    }
     if (measure) PROF("reduce", k_reduce_sum(L, ctx->d_kinpart, nkin, 1, ctx->d_sums + 17));
   }
   if (en) {
@@ -943,12 +1064,12 @@ int mg_selffield(mg_ctx* ctx, double* r, double* f, double omega, int measure, m
   if (!ctx->polar) return fail(ctx, MG_ERR_ARG, "no Drude charges in this context");
   ctx->launches = 0;
   const size_t nb = 6 * (size_t)ctx->ns * sizeof(double);
-  CK(cudaMemcpyAsync(ctx->d_r, r, nb, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->d_f, f, nb, cudaMemcpyHostToDevice, ctx->stream));
-  int rc = selffield_async(ctx, ctx->d_r, ctx->d_f, omega, measure && en, nullptr);
+  CK(cudaMemcpyAsync(ctx->d_rs, r, nb, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_fs, f, nb, cudaMemcpyHostToDevice, ctx->stream));
+  int rc = selffield_async(ctx, ctx->d_rs, ctx->d_fs, omega, measure && en, nullptr);
   if (rc) return rc;
-  CK(cudaMemcpyAsync(r, ctx->d_r, nb, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaMemcpyAsync(f, ctx->d_f, nb, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(r, ctx->d_rs, nb, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(f, ctx->d_fs, nb, cudaMemcpyDeviceToHost, ctx->stream));
   if (measure && en) {
     rc = fetch_sums(ctx);
     if (rc) return rc;

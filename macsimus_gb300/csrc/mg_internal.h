@@ -163,6 +163,31 @@ struct ShakeArgs {
 };
 cudaError_t k_shake(const Launch& L, const ShakeArgs& a);
 
+// neighbour lists (mg_nlist.cu)
+struct ListArgs {
+  int ncx, ncy, ncz, nstencil;   // build grid (cells >= (cutoff+skin)/cdiv)
+  const int* cell_start;
+  const int4* stencil;
+  float sx, sy, sz;              // fixed-point -> A
+  float rlist2;                  // (cutoff+skin)^2
+  int cap;                       // list capacity per site
+  long pitch;                    // column stride of nlist
+  int* nlist;                    // [cap*pitch]
+  int* ncount;                   // [ns]
+  int* status;                   // bit 4: capacity exceeded
+};
+cudaError_t k_build_list(const Launch& L, const ListArgs& a, const int4* pj);
+cudaError_t k_save_build(const Launch& L, int ns, const double* r, double* rb);
+cudaError_t k_check_skin(const Launch& L, int ns, const double* r, const double* rb, double lim2,
+                         int* status);
+cudaError_t k_pair_list_mixed(const Launch& L, const PairArgs& a, const ListArgs& l,
+                              const int4* pj, const PairF* ptab, const float4* erd,
+                              const float4* eru, bool measure, bool polar);
+cudaError_t k_pair_list_fp64(const Launch& L, const PairArgs& a, const ListArgs& l,
+                             const double4* pd, const PairD* ptab, const double* ertab,
+                             bool measure, bool polar);
+int list_blocks(int ns);
+
 // Drude sites (mg_drude.cu)
 struct DrudeArgs {
   int nd, ns;

@@ -46,9 +46,12 @@ SITE_TYPES = {
 TYPE_ORDER = ["H", "O", "NA", "CL", "OD"]
 
 # Drude parameters of a site type: (alphapol A^3, chargepol e).  The Drude
-# water takes the polarizability 1.44 A^3 and the shell charge -1.8 e; the
-# spring constant follows, k = q^2/(4 pi eps0 alpha) = 3126 kJ/mol/A^2.
-TYPE_DRUDE = {"OD": (1.44, -1.8)}
+# water has the shell charge -1.8 e on a spring of 4184 kJ/mol/A^2
+# (1000 kcal/mol/A^2); its polarizability follows as
+# alpha = q^2/(4 pi eps0 k) = 1.8^2 * 332.06371330/1000 A^3 (sim/units.h:90).
+DRUDE_QD = -1.8
+DRUDE_K_KCAL = 1000.0
+TYPE_DRUDE = {"OD": (DRUDE_QD ** 2 * 332.06371330 / DRUDE_K_KCAL, DRUDE_QD)}
 
 
 def ble_type_row(name):

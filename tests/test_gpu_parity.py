@@ -140,3 +140,42 @@ def test_full_size_mixed_within_tolerance_of_fp64():
     assert np.abs(fm.sum(axis=0)).max() < 1e-3 * scale * np.sqrt(len(fd))
     assert abs(em["lj"] - ed["lj"]) < 1e-6 * abs(ed["lj"])
     assert abs(em["el"] - ed["el"]) < 1e-6 * abs(ed["eself"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_neighbour_lists_match_direct_cells(precision):
+    """Verlet lists (cutoff+skin) give the same forces as re-binned cells"""
+    g, meta, system, ew = load("spce864")
+    args = (system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
+    fl, el = M.ForcePath(*args, precision=precision, skin=1.5).forces(g["r"][0], measure=True)
+    fc, ec = M.ForcePath(*args, precision=precision, skin=-1).forces(g["r"][0], measure=True)
+    assert rel_rms(fl, fc) < (1e-12 if precision == "fp64" else 1e-6)
+    assert abs(el["lj"] - ec["lj"]) < 1e-6 * abs(ec["lj"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_md_with_lists_matches_md_with_cells(precision):
+    """20 MD steps with lists rebuilt every 5 steps track the cook-style
+    re-binning at every step"""
+    g, meta, system, ew = load("spce216")
+    kw = dict(precision=precision, h=meta["params"]["h"], epsc=meta["params"]["epsc"],
+              omegac=meta["omegac"])
+    args = (system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
+    out = []
+    for skin in (1.5, -1):
+        fp = M.ForcePath(*args, skin=skin, nl_every=5, **kw)
+        fp.md_set_state(g["r"][2], g["r"][2] - g["r"][1])
+        fp.md_steps(20)
+        out.append(fp.md_get_state()[0])
+    assert np.abs(out[0] - out[1]).max() < (1e-9 if precision == "fp64" else 1e-5)
+
+
+def test_skin_violation_is_reported():
+    """a list kept for too many steps with a tiny skin is detected"""
+    g, meta, system, ew = load("spce216")
+    fp = M.ForcePath(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"], precision="fp64",
+                     skin=1e-4, nl_every=1000, h=meta["params"]["h"])
+    fp.md_set_state(g["r"][2], g["r"][2] - g["r"][1])
+    with pytest.raises(M.MGError) as e:
+        fp.md_steps(5)
+    assert e.value.code == 8
