@@ -94,11 +94,12 @@ typedef struct {
   int scf_iter;      /* force evaluations + SCF iterations per step (|scf.eps|, >=1) */
   double scf_omega;  /* SCF mixing when aspc_k == 0 (ASPC sets (k+2)/(2k+3) itself) */
   double minqq;      /* largest allowed Drude displacement (el.minqq, default 1 A) */
-  /* pair search: Verlet lists of radius cutoff+skin rebuilt every nl_every MD
-     steps (and at every mg_forces call); skin < 0 re-bins the linked cells at
-     every force evaluation as cook does (cook/lc.c) */
-  double skin;       /* A; 0 selects 1.5 */
-  int nl_every;      /* MD steps between list builds; <=0 selects 5 */
+  /* pair search: skin <= 0 re-bins the linked cells at every force
+     evaluation as cook does (cook/lc.c); skin > 0 selects per-site Verlet
+     lists of radius cutoff+skin, rebuilt at every mg_forces call and, in MD,
+     once a site has moved skin/4 since the build (or after nl_every steps) */
+  double skin;       /* A */
+  int nl_every;      /* most MD steps between list builds; <=0 selects 50 */
 } mg_params;
 
 /* Energies of one force evaluation (program units, K).

@@ -125,7 +125,7 @@ class ForcePath:
     def __init__(self, system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None,
                  grid=256, rshift=3, rplus=2.5, epsinf=3e33, h=0.002, epsc=1e-7, omegac=1.2,
                  shake_maxit=1000, cells_per_cutoff=0, aspc_k=2, scf_iter=1, scf_omega=0.6,
-                 minqq=1.0, skin=1.5, nl_every=5):
+                 minqq=1.0, skin=0.0, nl_every=50):
         lib = library()
         self.system = system
         self.ns = system.ns

@@ -83,6 +83,10 @@ struct mg_ctx {
   long nl_pitch = 0;
   int *d_nlist = nullptr, *d_ncount = nullptr;
   double* d_rbuild = nullptr;
+  int* d_dmax = nullptr;        // max squared displacement since the build (float bits)
+  int* h_dmax = nullptr;        // pinned copy, read before the next step
+  cudaEvent_t ev_dmax = nullptr;
+  bool dmax_pending = false;
   int nepart = 0;
   // Drude
   bool polar = false;
@@ -211,9 +215,9 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   ctx->scf_iter = p->scf_iter > 0 ? p->scf_iter : 1;
   ctx->scf_omega = p->scf_omega > 0 ? p->scf_omega : 0.6;
   ctx->minqq = p->minqq > 0 ? p->minqq : 1.0;
-  ctx->use_list = p->skin >= 0;
-  ctx->skin = p->skin > 0 ? p->skin : 1.5;
-  ctx->nl_every = p->nl_every > 0 ? p->nl_every : 5;
+  ctx->use_list = p->skin > 0;
+  ctx->skin = p->skin > 0 ? p->skin : 0;
+  ctx->nl_every = p->nl_every > 0 ? p->nl_every : 50;
   CK(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
   ctx->stream = ctx->own_stream;
   const int ns = t->ns;
@@ -479,6 +483,11 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
     CK(dalloc(&ctx->d_nlist, (size_t)ctx->nl_cap * ctx->nl_pitch));
     CK(dalloc(&ctx->d_ncount, ns));
     CK(dalloc(&ctx->d_rbuild, 3 * (size_t)ns));
+    CK(dalloc(&ctx->d_dmax, 1));
+    CK(cudaMemset(ctx->d_dmax, 0, sizeof(int)));
+    CK(cudaMallocHost((void**)&ctx->h_dmax, sizeof(int)));
+    *ctx->h_dmax = 0;
+    CK(cudaEventCreateWithFlags(&ctx->ev_dmax, cudaEventDisableTiming));
     if (p->precision != MG_MIXED) CK(dalloc(&ctx->d_pj, ns));
   }
   CK(upload(&ctx->d_qsite, qsite.data(), qsite.size()));
@@ -566,6 +575,8 @@ int build_lists(mg_ctx* ctx, const double* r_dev) {
     if (!(st & 16)) {
       ctx->need_build = false;
       ctx->since_build = 0;
+      CK(cudaMemsetAsync(ctx->d_dmax, 0, sizeof(int), ctx->stream));
+      ctx->dmax_pending = false;
       return MG_OK;
     }
     st &= ~16;
@@ -816,10 +827,12 @@ int mg_destroy(mg_ctx* ctx) {
                   ctx->d_kinpart, ctx->d_status, ctx->d_sums, ctx->d_krows,
                   ctx->d_tiles, ctx->d_p1job, ctx->d_dsite, ctx->d_qdrude, ctx->d_qc,
                   ctx->d_qp, ctx->d_aqq, ctx->d_hist, ctx->d_drpart, ctx->d_pdj, ctx->d_pdd,
-                  ctx->d_nlist, ctx->d_ncount, ctx->d_rbuild};
+                  ctx->d_nlist, ctx->d_ncount, ctx->d_rbuild, ctx->d_dmax};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ctx->h_sums) cudaFreeHost(ctx->h_sums);
+  if (ctx->h_dmax) cudaFreeHost(ctx->h_dmax);
+  if (ctx->ev_dmax) cudaEventDestroy(ctx->ev_dmax);
   for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
@@ -971,6 +984,15 @@ int mg_md_set_state(mg_ctx* ctx, const double* r, const double* r1) {
 int mg_md_get_state(mg_ctx* ctx, double* r, double* r1) {
   if (!ctx || !ctx->have_state) return fail(ctx, MG_ERR_ARG, "no MD state");
   const size_t nb = 3 * (size_t)ctx->ns * (ctx->polar ? 2 : 1) * sizeof(double);
+  if (ctx->polar && ctx->nd > 0) {
+    // cook keeps rpol(t-h) in cfg[1]'s polar half: the previous corrected
+    // shells, so that a get/set round trip restarts ASPC from them
+    Launch L = launch(ctx);
+    DrudeArgs d = drude_args(ctx);
+    const int K2 = ctx->aspc_k + 2;
+    const size_t slot = 3 * (size_t)ctx->nd;
+    CK(k_drude_put(L, d, ctx->d_hist + slot * ((ctx->hist_h - 1 + K2) % K2), ctx->d_r1));
+  }
   if (r) CK(cudaMemcpyAsync(r, ctx->d_r, nb, cudaMemcpyDeviceToHost, ctx->stream));
   if (r1) CK(cudaMemcpyAsync(r1, ctx->d_r1, nb, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -1003,6 +1025,16 @@ int mg_md_steps(mg_ctx* ctx, int nsteps, mg_energy* en) {
   for (int s = 0; s < nsteps; s++) {
     const bool last = s == nsteps - 1;
     const bool measure = last && en != nullptr;
+    if (ctx->use_list && ctx->dmax_pending) {
+      // the previous step's largest displacement since the build: rebuild
+      // once half of the skin/2 budget is used (one more step cannot spend
+      // the other half at any physical speed)
+      CK(cudaEventSynchronize(ctx->ev_dmax));
+      ctx->dmax_pending = false;
+      float d2;
+      std::memcpy(&d2, ctx->h_dmax, sizeof(float));
+      if (d2 > 0.0625 * ctx->skin * ctx->skin) ctx->need_build = true;
+    }
     if (ctx->polar && ctx->nd > 0) {
       // ASPC predictor, then scf_iter force evaluations each followed by one
       // SCF iteration (sim/constrd.c:726-736, sim/pred2.c:56-97)
@@ -1037,7 +1069,12 @@ int mg_md_steps(mg_ctx* ctx, int nsteps, mg_energy* en) {
     if (ctx->use_list) {
       ctx->since_build++;
       PROF("neighbour_list", k_check_skin(L, ctx->ns, ctx->d_r, ctx->d_rbuild,
-                                          0.25 * ctx->skin * ctx->skin, ctx->d_status));
+                                          0.25 * ctx->skin * ctx->skin, ctx->d_status,
+                                          ctx->d_dmax));
+      CK(cudaMemcpyAsync(ctx->h_dmax, ctx->d_dmax, sizeof(int), cudaMemcpyDeviceToHost,
+                         ctx->stream));
+      CK(cudaEventRecord(ctx->ev_dmax, ctx->stream));
+      ctx->dmax_pending = true;
     }
     if (measure) PROF("reduce", k_reduce_sum(L, ctx->d_kinpart, nkin, 1, ctx->d_sums + 17));
   }

@@ -71,9 +71,10 @@ __global__ void __launch_bounds__(DR_THREADS)
     acc[5] -= n1 * p2;
     acc[6] -= n2 * p0;
     acc[7] -= n0 * p1;
-    // cook stops when a shell leaves the sphere of radius el.minqq around
-    // its site (sim/scf.c:253): flag it, the host reports MG_ERR_SCF
-    if (!(n0 * n0 + n1 * n1 + n2 * n2 < a.minqq2)) atomicOr(a.status, 4);
+    // cook stops when a shell, before or after the iteration, is outside
+    // the sphere of radius el.minqq around its site (sim/scf.c:137 and
+    // :255): flag it, the host reports MG_ERR_SCF
+    if (!(rr < a.minqq2) || !(n0 * n0 + n1 * n1 + n2 * n2 < a.minqq2)) atomicOr(a.status, 4);
     rp[0] = n0;
     rp[1] = n1;
     rp[2] = n2;
@@ -136,6 +137,20 @@ __global__ void drude_take_kernel(DrudeArgs a, const double* __restrict__ r,
 
 cudaError_t k_drude_take(const Launch& L, const DrudeArgs& a, const double* r, double* out) {
   drude_take_kernel<<<(3 * a.nd + 255) / 256, 256, 0, L.s>>>(a, r, out);
+  ++*L.counter;
+  return cudaGetLastError();
+}
+
+// the inverse: shell displacements of the Drude sites into r's second half
+__global__ void drude_put_kernel(DrudeArgs a, const double* __restrict__ in,
+                                 double* __restrict__ r) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 3 * a.nd) return;
+  r[3 * (long)a.ns + 3 * a.dsite[t / 3] + t % 3] = in[t];
+}
+
+cudaError_t k_drude_put(const Launch& L, const DrudeArgs& a, const double* in, double* r) {
+  drude_put_kernel<<<(3 * a.nd + 255) / 256, 256, 0, L.s>>>(a, in, r);
   ++*L.counter;
   return cudaGetLastError();
 }

@@ -179,7 +179,7 @@ struct ListArgs {
 cudaError_t k_build_list(const Launch& L, const ListArgs& a, const int4* pj);
 cudaError_t k_save_build(const Launch& L, int ns, const double* r, double* rb);
 cudaError_t k_check_skin(const Launch& L, int ns, const double* r, const double* rb, double lim2,
-                         int* status);
+                         int* status, int* dmax);
 cudaError_t k_pair_list_mixed(const Launch& L, const PairArgs& a, const ListArgs& l,
                               const int4* pj, const PairF* ptab, const float4* erd,
                               const float4* eru, bool measure, bool polar);
@@ -209,6 +209,7 @@ cudaError_t k_selffield(const Launch& L, const DrudeArgs& a, double omega, doubl
 cudaError_t k_aspc_predict(const Launch& L, const DrudeArgs& a, const double* hist, int K2, int h,
                            const AspcCoef& B, double* r);
 cudaError_t k_drude_take(const Launch& L, const DrudeArgs& a, const double* r, double* out);
+cudaError_t k_drude_put(const Launch& L, const DrudeArgs& a, const double* in, double* r);
 cudaError_t k_fma_probe(cudaStream_t s, int blocks, int threads, int iters, float* out);
 
 }  // namespace mg

@@ -49,6 +49,16 @@ __device__ __forceinline__ T2 cmul(const T2 b, const T2 c) {
   return r;
 }
 
+// s + c += v, c carrying the low-order part lost by s (Kahan summation); the
+// FP64 path adds directly
+__device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
+  const float y = v - c;
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+__device__ __forceinline__ void kahan_add(double& s, double&, double v) { s += v; }
+
 // ------------------------------------------------------------ pass 1 --
 
 constexpr int P1_THREADS = 128;
@@ -156,7 +166,8 @@ __global__ void __launch_bounds__(P2_THREADS)
   T2* Zs = reinterpret_cast<T2*>(smem_raw);            // [nz][P2_NJ]
   T2* Ws = Zs + (size_t)nz * P2_NJ;                     // [nz][KTR]
   KRow* rows = reinterpret_cast<KRow*>(Ws + (size_t)nz * KTR);  // [KTR]
-  double* red = reinterpret_cast<double*>(rows + KTR);  // [P2_THREADS][12]
+  float2* kxy = reinterpret_cast<float2*>(rows + KTR);  // [KTR] (kx, ky) as floats
+  double* red = reinterpret_cast<double*>(kxy + KTR);   // [P2_THREADS][12]
   const int tid = threadIdx.x;
   const int tw = tid & 15, tj = tid >> 4;
   const int jbase = blockIdx.x * P2_NJ;
@@ -165,15 +176,22 @@ __global__ void __launch_bounds__(P2_THREADS)
     const int z = t / P2_NJ, c = t % P2_NJ, j = jbase + c;
     Zs[t] = j < a.nq ? tab[(long)j * a.row + oz - a.Kz + z] : Cx<T2>::zero();
   }
-  double F[4][3];
+  // per-charge force sums over the tiles: compensated (Kahan) in the FP32
+  // path, so that the fold costs FP32 and not FP64 instructions
+  T F[4][3], Fc[4][3];
 #pragma unroll
-  for (int c = 0; c < 4; c++) F[c][0] = F[c][1] = F[c][2] = 0;
+  for (int c = 0; c < 4; c++)
+#pragma unroll
+    for (int d = 0; d < 3; d++) F[c][d] = Fc[c][d] = 0;
   for (int ti = 0; ti < a.ntile; ti++) {
     const KTile tile = a.tiles[ti];
     const int R = tile.R;
     __syncthreads();
-    for (int t = tid; t < KTR; t += P2_THREADS)
-      rows[t] = t < tile.nrows ? a.krows[tile.row0 + t] : KRow{0, 0, 1, 0, 0, 0, 0, 0};
+    for (int t = tid; t < KTR; t += P2_THREADS) {
+      const KRow rw = t < tile.nrows ? a.krows[tile.row0 + t] : KRow{0, 0, 1, 0, 0, 0, 0, 0};
+      rows[t] = rw;
+      kxy[t] = make_float2((float)rw.kx, (float)rw.ky);
+    }
     __syncthreads();
     for (int t = tid; t < (2 * R + 1) * KTR; t += P2_THREADS) {
       const int z = t / KTR, rr = t % KTR, kz = z - R;
@@ -186,8 +204,8 @@ __global__ void __launch_bounds__(P2_THREADS)
     for (int c = 0; c < 4; c++)
 #pragma unroll
       for (int i = 0; i < 4; i++) H[c][i] = Hz[c][i] = Cx<T2>::zero();
-    for (int z = 0; z < 2 * R + 1; z++) {
-      const T kz = (T)(z - R);
+    T kz = (T)(-R);
+    for (int z = 0; z < 2 * R + 1; z++, kz += (T)1) {
       const T2* Zrow = Zs + (size_t)(z - R + a.Kz) * P2_NJ + 4 * tj;
       const T2* Wrow = Ws + (size_t)z * KTR + tw;
       T2 zv[4], wv[4];
@@ -212,28 +230,28 @@ __global__ void __launch_bounds__(P2_THREADS)
       const int j = jbase + 4 * tj + c;
       if (j >= a.nq) continue;
       const T2* Rj = tab + (long)j * a.row;
-      T gx = 0, gy = 0, gz = 0;
+      T g3[3] = {0, 0, 0};
 #pragma unroll
       for (int i = 0; i < 4; i++) {
         const int rr = tw + 16 * i;
         if (rr >= tile.nrows) continue;
         const KRow rw = rows[rr];
+        const float2 kf = kxy[rr];
         const T2 A = cmul(Rj[rw.kx], Rj[oy + rw.ky]);
         const T g = A.x * H[c][i].y + A.y * H[c][i].x;
-        gx = fma((T)rw.kx, g, gx);
-        gy = fma((T)rw.ky, g, gy);
-        gz += A.x * Hz[c][i].y + A.y * Hz[c][i].x;
+        g3[0] = fma((T)kf.x, g, g3[0]);
+        g3[1] = fma((T)kf.y, g, g3[1]);
+        g3[2] += A.x * Hz[c][i].y + A.y * Hz[c][i].x;
       }
-      F[c][0] += gx;
-      F[c][1] += gy;
-      F[c][2] += gz;
+#pragma unroll
+      for (int d = 0; d < 3; d++) kahan_add(F[c][d], Fc[c][d], g3[d]);
     }
   }
   // sum over the 16 row slots of each charge
 #pragma unroll
   for (int c = 0; c < 4; c++)
 #pragma unroll
-    for (int d = 0; d < 3; d++) red[tid * 12 + c * 3 + d] = F[c][d];
+    for (int d = 0; d < 3; d++) red[tid * 12 + c * 3 + d] = (double)F[c][d] + (double)Fc[c][d];
   __syncthreads();
   if (tw == 0) {
 #pragma unroll
@@ -256,7 +274,7 @@ template <typename T2>
 static cudaError_t launch_kf_gemm(const Launch& L, const KArgs& a, const T2* tab, const T2* W) {
   const int nz = 2 * a.Kz + 1;
   size_t smem = (size_t)nz * P2_NJ * sizeof(T2) + (size_t)nz * KTR * sizeof(T2) +
-                KTR * sizeof(KRow) + (size_t)P2_THREADS * 12 * sizeof(double);
+                KTR * (sizeof(KRow) + sizeof(float2)) + (size_t)P2_THREADS * 12 * sizeof(double);
   cudaError_t e = cudaFuncSetAttribute(kf_gemm_kernel<T2>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;

@@ -84,19 +84,34 @@ cudaError_t k_save_build(const Launch& L, int ns, const double* r, double* rb) {
   return cudaGetLastError();
 }
 
+// largest squared displacement since the build (as the bits of a float,
+// which order like the floats for non-negative values) into *dmax; a site
+// beyond skin/2 sets bit 3 of *status (the lists may have missed a pair)
 __global__ void check_skin_kernel(int ns, const double* __restrict__ r,
                                   const double* __restrict__ rb, double lim2,
-                                  int* __restrict__ status) {
+                                  int* __restrict__ status, int* __restrict__ dmax) {
+  __shared__ float red[256];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= ns) return;
-  const double dx = r[3 * i] - rb[3 * i], dy = r[3 * i + 1] - rb[3 * i + 1],
-               dz = r[3 * i + 2] - rb[3 * i + 2];
-  if (!(dx * dx + dy * dy + dz * dz < lim2)) atomicOr(status, 8);
+  float d2 = 0.f;
+  if (i < ns) {
+    const double dx = r[3 * i] - rb[3 * i], dy = r[3 * i + 1] - rb[3 * i + 1],
+                 dz = r[3 * i + 2] - rb[3 * i + 2];
+    const double dd = dx * dx + dy * dy + dz * dz;
+    if (!(dd < lim2)) atomicOr(status, 8);
+    d2 = (float)fmin(dd, 1e30);
+  }
+  red[threadIdx.x] = d2;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicMax(dmax, __float_as_int(red[0]));
 }
 
 cudaError_t k_check_skin(const Launch& L, int ns, const double* r, const double* rb, double lim2,
-                         int* status) {
-  check_skin_kernel<<<(ns + 255) / 256, 256, 0, L.s>>>(ns, r, rb, lim2, status);
+                         int* status, int* dmax) {
+  check_skin_kernel<<<(ns + 255) / 256, 256, 0, L.s>>>(ns, r, rb, lim2, status, dmax);
   ++*L.counter;
   return cudaGetLastError();
 }

@@ -97,11 +97,22 @@ def ion(name):
     return Species(name, [name], [q], np.zeros((1, 3)))
 
 
+# permanent charges of the Drude water: the SPC/E geometry carrying the
+# gas-phase dipole 1.85 D (q_H = 0.3336 e).  With the SPC/E charges (which
+# already include the liquid-phase polarization) the added shells polarize
+# without bound: O...H contacts close to 1.26 A and the shells run away
+# within 60 steps at 298 K even with a fully converged SCF.
+DRUDE_WATER_QH = 0.3336
+
+
 def spce_drude():
-    """SPC/E geometry and total charges with a Drude shell on the oxygen"""
+    """SPC/E geometry with a Drude shell on the oxygen; permanent charges
+    q_H = DRUDE_WATER_QH, q_O = -2 q_H (total site charges; the O core
+    carries q_O - q_D)"""
     sp = spce()
     sp.name = "WATD"
     sp.sites = ["OD", "H", "H"]
+    sp.charges = [-2 * DRUDE_WATER_QH, DRUDE_WATER_QH, DRUDE_WATER_QH]
     return sp
 
 

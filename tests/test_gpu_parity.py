@@ -155,7 +155,7 @@ def test_neighbour_lists_match_direct_cells(precision):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_md_with_lists_matches_md_with_cells(precision):
-    """20 MD steps with lists rebuilt every 5 steps track the cook-style
+    """20 MD steps with lists (rebuilt on displacement) track the cook-style
     re-binning at every step"""
     g, meta, system, ew = load("spce216")
     kw = dict(precision=precision, h=meta["params"]["h"], epsc=meta["params"]["epsc"],
@@ -163,7 +163,7 @@ def test_md_with_lists_matches_md_with_cells(precision):
     args = (system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
     out = []
     for skin in (1.5, -1):
-        fp = M.ForcePath(*args, skin=skin, nl_every=5, **kw)
+        fp = M.ForcePath(*args, skin=skin, **kw)
         fp.md_set_state(g["r"][2], g["r"][2] - g["r"][1])
         fp.md_steps(20)
         out.append(fp.md_get_state()[0])
