@@ -206,6 +206,39 @@ int mg_ewald_kspace_noalloc(const double *r_dev, const double *q_dev, int nq, co
                             double alpha, double kappa, double *f_dev, double *energy,
                             void *stream);
 
+/* ---- Widom test-particle insertion ----
+   Replaces Einsert (cook/forces.h:3, cook/widom.c:175-288) and the averaging
+   of Widom (sim/simmeas.c:1821-1958) with the cutoff correction of
+   Widomcutcorr (sim/siminit.c:762-808).  ninsert ghost molecules are placed
+   at random into the configuration of the last force evaluation (mg_forces,
+   mg_forces_device or the last step of mg_md_steps -- cook's "last cell
+   list"); each one's energy U against the box (LJ with the smooth cutoff +
+   q q erfc r-space terms within the cutoff; the ghost is not part of the
+   box) enters exp(-U/T), a term skipped when -U/T <= -700.  Insertion k
+   takes its point and (for more than one site) a uniform rotation from a
+   counter-based stream of `seed`, so the result is reproducible and does
+   not depend on the launch.  Not available for Drude systems. */
+#define MG_WIDOM_MAX_SITES 8
+typedef struct {
+  int ns;                  /* ghost sites, 1..MG_WIDOM_MAX_SITES */
+  const int *site_type;    /* LJ type of each site (index into the topology's types) */
+  const double *charge;    /* site charges in program units, or NULL (neutral) */
+  const double *geometry;  /* [3*ns] site offsets from the insertion point, A */
+} mg_probe;
+
+typedef struct {
+  double sum;     /* sum of exp(-U/T) */
+  double raw;     /* sum / ninsert (cook's "Widom raw") */
+  double corr;    /* cutoff correction numerator (cook's widom.corr), K A^3 */
+  double factor;  /* exp(-corr/(V T)) */
+  double widom;   /* raw * factor (cook's "Widom") */
+  double mu;      /* -T ln(widom): residual chemical potential, K */
+} mg_widom_result;
+
+/* U (optional, [ninsert]) receives every insertion energy (K) */
+int mg_widom(mg_ctx *ctx, const mg_probe *probe, long long ninsert, unsigned long long seed,
+             double T, mg_widom_result *out, double *U);
+
 #ifdef __cplusplus
 }
 #endif

@@ -67,6 +67,17 @@ class Energy(C.Structure):
         return d
 
 
+class Probe(C.Structure):
+    _fields_ = [("ns", C.c_int), ("site_type", _ip), ("charge", _dp), ("geometry", _dp)]
+
+
+class WidomResult(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("sum", "raw", "corr", "factor", "widom", "mu")]
+
+    def asdict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 _lib = None
 
 
@@ -100,6 +111,8 @@ def library():
         L.mg_profile_entry.argtypes = [vp, C.c_int, C.POINTER(C.c_char_p), _dp,
                                        C.POINTER(C.c_long)]
         L.mg_probe_fp32_tflops.argtypes = [_dp]
+        L.mg_widom.argtypes = [vp, C.POINTER(Probe), C.c_longlong, C.c_ulonglong, C.c_double,
+                               C.POINTER(WidomResult), _dp]
         L.mg_ewald_kspace_noalloc.argtypes = [vp, vp, C.c_int, _dp, C.c_double, C.c_double, vp,
                                               _dp, vp]
         _lib = L
@@ -301,3 +314,23 @@ class ForcePath:
         en = Energy()
         self._check(library().mg_md_steps(self._ctx, int(n), C.byref(en) if measure else None))
         return en.asdict() if measure else None
+
+    def widom(self, site_types, geometry=None, charges=None, n=100000, seed=1, T=298.0,
+              energies=False):
+        """Widom insertions of a ghost molecule (cook's Einsert + Widom) into
+        the configuration of the last force evaluation; returns a dict with
+        sum, raw, corr, factor, widom, mu (K) and, with energies=True, the
+        insertion energies U [n] (K)"""
+        st = _arr(site_types, np.int32).reshape(-1)
+        g = _arr(np.zeros((len(st), 3)) if geometry is None else geometry, np.float64).reshape(-1)
+        q = None if charges is None else _arr(charges, np.float64).reshape(-1)
+        pr = Probe(len(st), st.ctypes.data_as(_ip), q.ctypes.data_as(_dp) if q is not None else None,
+                   g.ctypes.data_as(_dp))
+        res = WidomResult()
+        U = np.zeros(int(n)) if energies else None
+        self._check(library().mg_widom(self._ctx, C.byref(pr), int(n), int(seed), float(T),
+                                       C.byref(res), U.ctypes.data_as(_dp) if energies else None))
+        out = res.asdict()
+        if energies:
+            out["U"] = U
+        return out

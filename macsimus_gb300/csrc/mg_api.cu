@@ -88,6 +88,18 @@ struct mg_ctx {
   cudaEvent_t ev_dmax = nullptr;
   bool dmax_pending = false;
   int nepart = 0;
+  // Widom: the type table, the site kinds, sites per type; cell data of the
+  // last force evaluation (cook's lastlist)
+  int ntypes = 0, comb_rule = 1;
+  double C2 = 0;
+  std::vector<double> h_tE, h_tR, h_tA;
+  std::vector<int> kind_type;
+  std::vector<double> kind_q;
+  std::vector<long> type_count;
+  bool have_cells = false;
+  PairF* d_wtabf = nullptr;
+  PairD* d_wtabd = nullptr;
+  double *d_wgeom = nullptr, *d_wpart = nullptr;
   // Drude
   bool polar = false;
   int nd = 0, ndblocks = 0, aspc_k = 2, aspc_kk = 0, scf_iter = 1, hist_h = 0;
@@ -252,10 +264,21 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   }
   ctx->nkind = (int)kind_type.size();
   if (ctx->nkind > MAX_KINDS) return fail(ctx, MG_ERR_SIZE, "more than 16 site kinds");
+  ctx->kind_type = kind_type;
+  ctx->kind_q = kind_q;
+  ctx->ntypes = t->ntypes;
+  ctx->comb_rule = t->comb_rule;
+  ctx->h_tE.assign(t->type_EvdW, t->type_EvdW + t->ntypes);
+  ctx->h_tR.assign(t->type_RvdW, t->type_RvdW + t->ntypes);
+  ctx->h_tA.assign(t->ntypes, 0.0);
+  if (t->type_alpha) ctx->h_tA.assign(t->type_alpha, t->type_alpha + t->ntypes);
+  ctx->type_count.assign(t->ntypes, 0);
+  for (int i = 0; i < ns; i++) ctx->type_count[t->site_type[i]]++;
   ctx->eself = -p->alpha / 1.772453850905516 * sumq2;
 
   // ---- LJ pair tables (combining rule + smooth cutoff), per pair of kinds
   double C2 = p->LJcutoff > 0 ? p->LJcutoff : p->cutoff;
+  ctx->C2 = C2;
   std::vector<PairLJ> tp(t->ntypes * t->ntypes);
   std::vector<double> ta(t->ntypes, 0.0);
   for (int a = 0; a < t->ntypes; a++)
@@ -709,6 +732,7 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
       PROF("ewald_kforce", k_kf_gemm_fp64(L, ka, (const double2*)ctx->d_tab));
     }
   }
+  ctx->have_cells = true;
   if (measure) {
     PROF("reduce", k_reduce_sum(L, ctx->d_epart, nerows, 10, ctx->d_sums));
     if (ctx->nq > 0) PROF("reduce", k_reduce_sum(L, ctx->d_ekpart, ctx->nkblocks, 7, ctx->d_sums + 10));
@@ -827,7 +851,8 @@ int mg_destroy(mg_ctx* ctx) {
                   ctx->d_kinpart, ctx->d_status, ctx->d_sums, ctx->d_krows,
                   ctx->d_tiles, ctx->d_p1job, ctx->d_dsite, ctx->d_qdrude, ctx->d_qc,
                   ctx->d_qp, ctx->d_aqq, ctx->d_hist, ctx->d_drpart, ctx->d_pdj, ctx->d_pdd,
-                  ctx->d_nlist, ctx->d_ncount, ctx->d_rbuild, ctx->d_dmax};
+                  ctx->d_nlist, ctx->d_ncount, ctx->d_rbuild, ctx->d_dmax,
+                  ctx->d_wtabf, ctx->d_wtabd, ctx->d_wgeom, ctx->d_wpart};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ctx->h_sums) cudaFreeHost(ctx->h_sums);
@@ -1093,6 +1118,123 @@ int mg_md_steps(mg_ctx* ctx, int nsteps, mg_energy* en) {
     if (ctx->polar && ctx->nd > 0) add_drude_energy(ctx, en);
     en->ekin = ctx->h_sums[17] / (ctx->h * ctx->h) / 4;
   }
+  return MG_OK;
+}
+
+int mg_widom(mg_ctx* ctx, const mg_probe* probe, long long ninsert, unsigned long long seed,
+             double T, mg_widom_result* out, double* U) {
+  if (!ctx || !probe || !out) return fail(ctx, MG_ERR_ARG, "null argument");
+  const int nps = probe->ns;
+  if (nps < 1 || nps > MG_WIDOM_MAX_SITES || !probe->site_type || !probe->geometry)
+    return fail(ctx, MG_ERR_ARG, "the ghost needs 1..8 sites with types and geometry");
+  if (ninsert < 1 || !(T > 0)) return fail(ctx, MG_ERR_ARG, "ninsert >= 1 and T > 0 required");
+  if (ctx->polar)
+    return fail(ctx, MG_ERR_ARG, "Widom insertion into a Drude system is not supported");
+  if (!ctx->have_cells)
+    return fail(ctx, MG_ERR_ARG, "no cell list yet: evaluate forces first");
+  const double Lmin = std::min(ctx->L[0], std::min(ctx->L[1], ctx->L[2]));
+  for (int s = 0; s < nps; s++) {
+    if (probe->site_type[s] < 0 || probe->site_type[s] >= ctx->ntypes)
+      return fail(ctx, MG_ERR_ARG, "ghost site type out of range");
+    const double* g = probe->geometry + 3 * s;
+    if (!(std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]) < Lmin / 4))
+      return fail(ctx, MG_ERR_ARG, "ghost geometry larger than a quarter of the box");
+  }
+  // pair constants of every ghost site with every site kind of the box, and
+  // the cutoff correction over all (ghost site, box site) pairs
+  std::vector<PairF> tf(MAX_WPROBE * MAX_KINDS);
+  std::vector<PairD> td(MAX_WPROBE * MAX_KINDS);
+  double corr = 0;
+  for (int s = 0; s < nps; s++) {
+    const int ta = probe->site_type[s];
+    const double qs = probe->charge ? probe->charge[s] : 0.0;
+    for (int tb = 0; tb < ctx->ntypes; tb++) {
+      if (!ctx->type_count[tb]) continue;
+      double eps, sig;
+      PairLJ P;
+      combining_rule(ctx->h_tE[ta], ctx->h_tR[ta], ctx->h_tA[ta], ctx->h_tE[tb], ctx->h_tR[tb],
+                     ctx->h_tA[tb], ctx->comb_rule, &eps, &sig);
+      if (smooth_lj(eps, sig, ctx->C2, &P))
+        return fail(ctx, MG_ERR_SETUP, "smooth LJ cutoff cannot be determined");
+      corr += ctx->type_count[tb] * lj_tail_correction(eps, sig, P);
+    }
+    for (int b = 0; b < ctx->nkind; b++) {
+      const int tb = ctx->kind_type[b];
+      double eps, sig;
+      PairLJ P;
+      combining_rule(ctx->h_tE[ta], ctx->h_tR[ta], ctx->h_tA[ta], ctx->h_tE[tb], ctx->h_tR[tb],
+                     ctx->h_tA[tb], ctx->comb_rule, &eps, &sig);
+      smooth_lj(eps, sig, ctx->C2, &P);
+      const double qq = qs * ctx->kind_q[b];
+      td[s * ctx->nkind + b] = PairD{P.C1q, P.C2q, P.A4, P.E24, P.Sq, qq, P.A, P.E4, 0, 0, 0, 0};
+      tf[s * ctx->nkind + b] = PairF{(float)P.C1q, (float)P.C2q, (float)P.A4, (float)P.E24,
+                                     (float)P.Sq,  (float)qq,    (float)P.A,  (float)P.E4,
+                                     0.f, 0.f, 0.f, 0.f, qq, 0, 0, 0};
+    }
+  }
+  const int nblk = widom_blocks(ninsert);
+  if (!ctx->d_wgeom) {
+    CK(dalloc(&ctx->d_wgeom, 3 * MAX_WPROBE));
+    CK(dalloc(&ctx->d_wpart, 152 * 8));
+    CK(dalloc(&ctx->d_wtabf, MAX_WPROBE * MAX_KINDS));
+    CK(dalloc(&ctx->d_wtabd, MAX_WPROBE * MAX_KINDS));
+  }
+  CK(cudaMemcpyAsync(ctx->d_wgeom, probe->geometry, sizeof(double) * 3 * nps,
+                     cudaMemcpyHostToDevice, ctx->stream));
+  double* d_U = nullptr;
+  if (U) CK(cudaMalloc((void**)&d_U, sizeof(double) * ninsert));
+  WidomArgs w;
+  w.n = ninsert;
+  w.seed = seed;
+  w.T = T;
+  w.nps = nps;
+  w.nkind = ctx->nkind;
+  w.ncx = ctx->ncx;
+  w.ncy = ctx->ncy;
+  w.ncz = ctx->ncz;
+  w.nstencil = ctx->nstencil;
+  w.lanes_sites = ctx->nstencil < 16 ? 1 : 0;
+  w.ntab = ctx->ntab;
+  w.cell_start = ctx->d_cell_start;
+  w.stencil = ctx->d_stencil;
+  w.Lx = ctx->L[0];
+  w.Ly = ctx->L[1];
+  w.Lz = ctx->L[2];
+  w.cutoff_sq = ctx->cutoff * ctx->cutoff;
+  w.sgrid = ctx->sgrid;
+  w.geom = ctx->d_wgeom;
+  w.U = d_U;
+  w.part = ctx->d_wpart;
+  Launch L = launch(ctx);
+  cudaError_t e;
+  if (ctx->precision == MG_MIXED) {
+    CK(cudaMemcpyAsync(ctx->d_wtabf, tf.data(), sizeof(PairF) * tf.size(), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    e = k_widom_mixed(L, w, ctx->d_pj, ctx->d_wtabf, ctx->d_eru);
+  } else {
+    CK(cudaMemcpyAsync(ctx->d_wtabd, td.data(), sizeof(PairD) * td.size(), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    e = k_widom_fp64(L, w, ctx->d_pd, ctx->d_wtabd, ctx->d_ert);
+  }
+  if (e != cudaSuccess) {
+    if (d_U) cudaFree(d_U);
+    return fail(ctx, MG_ERR_CUDA, std::string("widom: ") + cudaGetErrorString(e));
+  }
+  std::vector<double> part(nblk);
+  CK(cudaMemcpyAsync(part.data(), ctx->d_wpart, sizeof(double) * nblk, cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  if (U) CK(cudaMemcpyAsync(U, d_U, sizeof(double) * ninsert, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (d_U) CK(cudaFree(d_U));
+  double sum = 0;
+  for (double v : part) sum += v;
+  const double V = ctx->L[0] * ctx->L[1] * ctx->L[2];
+  out->sum = sum;
+  out->raw = sum / (double)ninsert;
+  out->corr = corr;
+  out->factor = std::exp(-corr / (V * T));
+  out->widom = out->raw * out->factor;
+  out->mu = -T * std::log(out->widom);
   return MG_OK;
 }
 

@@ -17,6 +17,7 @@ struct PairLJ {
 void combining_rule(double E0, double R0, double a0, double E1, double R1, double a1,
                     int comb_rule, double* eps, double* sig);
 int smooth_lj(double eps, double sig, double C2, PairLJ* p);
+double lj_tail_correction(double eps, double sig, const PairLJ& p);
 int erfc_table_size(int grid, double maxr, double alpha);
 void erfc_table(int grid, double maxr, double cutoff, double alpha, int shift,
                 std::vector<double>* tab, double* sgrid);
@@ -208,6 +209,27 @@ cudaError_t k_selffield(const Launch& L, const DrudeArgs& a, double omega, doubl
                         double* hist_out);
 cudaError_t k_aspc_predict(const Launch& L, const DrudeArgs& a, const double* hist, int K2, int h,
                            const AspcCoef& B, double* r);
+// Widom insertions: nps ghost sites against the cell list of the last force
+// evaluation; per-CTA sums of exp(-U/T) into part[], energies into U[]
+constexpr int MAX_WPROBE = 8;
+struct WidomArgs {
+  long long n;
+  unsigned long long seed;
+  double T;
+  int nps, nkind, ncx, ncy, ncz, nstencil, lanes_sites, ntab;
+  const int* cell_start;
+  const int4* stencil;
+  double Lx, Ly, Lz, cutoff_sq, sgrid;
+  const double* geom;  // [3*nps] site offsets of the ghost
+  double* U;           // [n] or null
+  double* part;        // [nblocks]
+};
+int widom_blocks(long long n);
+cudaError_t k_widom_mixed(const Launch& L, const WidomArgs& a, const int4* pj, const PairF* tab,
+                          const float4* eru);
+cudaError_t k_widom_fp64(const Launch& L, const WidomArgs& a, const double4* pd, const PairD* tab,
+                         const double* ert);
+
 cudaError_t k_drude_take(const Launch& L, const DrudeArgs& a, const double* r, double* out);
 cudaError_t k_drude_put(const Launch& L, const DrudeArgs& a, const double* in, double* r);
 cudaError_t k_fma_probe(cudaStream_t s, int blocks, int threads, int iters, float* out);

@@ -90,6 +90,27 @@ int smooth_lj(double eps, double sig, double C2, PairLJ* p) {
   return 0;
 }
 
+// Cutoff correction of one type pair for a homogeneous fluid (the integral
+// of the missing tail, sim/setss.c:454-500): the smoothing region C1..C2
+// analytically, r > C1 by 4th-order Gauss on 64 intervals in 1/r
+double lj_tail_correction(double eps, double sig, const PairLJ& p) {
+  if (eps == 0 || p.C1q == 0) return 0;
+  const double C1 = std::sqrt(p.C1q), C2 = std::sqrt(p.C2q);
+  const double C14 = sq(C1) * sq(C1), C16 = C14 * sq(C1), C24 = sq(C2) * sq(C2);
+  const double pi = 3.14159265358979323846;
+  double c0 = 4 * pi * p.A *
+              (C1 * (C16 / 7 - 0.4 * C14 * sq(C2) + sq(C1) * C24 / 3) - 8.0 / 105 * std::pow(C2, 7));
+  const double h = 1.0 / 64 / C1, g = 0.2113248654051871;
+  double c1 = 0;
+  for (int n = 0; n < 64; n++) {
+    double r = 1 / ((n + g) * h);
+    c1 += sq(r) * sq(r) * lj_u(eps, sig, r);
+    r = 1 / ((n + (1 - g)) * h);
+    c1 += sq(r) * sq(r) * lj_u(eps, sig, r);
+  }
+  return c0 + c1 * 2 * pi * h;
+}
+
 int erfc_table_size(int grid, double maxr, double alpha) {
   return (int)(sq(maxr * alpha) * grid) + 1;
 }

@@ -42,8 +42,13 @@ SITE_TYPES = {
     "NA": (22.9898, 1.475, 2.16),
     "CL": (35.453, 0.0535, 4.83),
     "OD": (15.9994, 0.6502, 3.166),   # oxygen carrying a Drude charge
+    # a model ionic fluid (LJ spheres with +-1 e) and a neutral LJ probe for
+    # Widom insertions (sigma 3.2 A, epsilon 0.65 kJ/mol)
+    "AP": (22.9898, 0.5, 3.3),
+    "AM": (35.453, 0.7, 4.1),
+    "PRB": (39.948, 0.65, 3.2),
 }
-TYPE_ORDER = ["H", "O", "NA", "CL", "OD"]
+TYPE_ORDER = ["H", "O", "NA", "CL", "OD", "AP", "AM", "PRB"]
 
 # Drude parameters of a site type: (alphapol A^3, chargepol e).  The Drude
 # water has the shell charge -1.8 e on a spring of 4184 kJ/mol/A^2
@@ -92,8 +97,9 @@ def spce():
                    bonds=[(0, 1, 1.0), (0, 2, 1.0), (1, 2, HOH)])
 
 
-def ion(name):
-    q = 1.0 if name == "NA" else -1.0
+def ion(name, q=None):
+    if q is None:
+        q = 1.0 if name == "NA" else -1.0
     return Species(name, [name], [q], np.zeros((1, 3)))
 
 
@@ -116,7 +122,9 @@ def spce_drude():
     return sp
 
 
-SPECIES = {"WAT": spce, "NA": lambda: ion("NA"), "CL": lambda: ion("CL"), "WATD": spce_drude}
+SPECIES = {"WAT": spce, "NA": lambda: ion("NA"), "CL": lambda: ion("CL"), "WATD": spce_drude,
+           "AP": lambda: ion("AP", 1.0), "AM": lambda: ion("AM", -1.0),
+           "PRB": lambda: ion("PRB", 0.0)}
 
 
 @dataclass

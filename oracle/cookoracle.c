@@ -9,6 +9,7 @@
 
 #include <math.h>
 #include <pthread.h>
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -890,4 +891,159 @@ void orc_aspc_coef(int k, double *B, double *omega)
     }
   }
   *omega = (k + 2) / (double)(2 * k + 3);
+}
+
+/* --------------------------------------------------------------- Widom --- */
+
+/* The insertion stream.  The reference draws rnd() (gen/rndgen.h); the
+   insertion points are inputs of the method, so the oracle and the GPU path
+   share one counter-based stream instead: word c of insertion k is the
+   SplitMix64 output function (Steele, Lea and Flood, "Fast splittable
+   pseudorandom number generators", OOPSLA 2014) of seed + (8k+c+1)*gamma. */
+static uint64_t mix64(uint64_t z)
+{
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+unsigned long long orc_widom_word(unsigned long long seed, long long k, int c)
+{
+  return mix64(seed + (uint64_t)(8 * k + c + 1) * 0x9E3779B97F4A7C15ULL);
+}
+
+/* probe sites of insertion k: the point is (w_c >> 32)/2^32 * L_c for words
+   c = 0,1,2; for more than one site the geometry is turned by the uniform
+   random rotation of Shoemake ("Uniform random rotations", Graphics Gems
+   III, 1992) from u_c = (w_c >> 11)/2^53, c = 3,4,5 (cook/simils.c
+   rndorientation plays this part in the reference) */
+void orc_widom_sites(unsigned long long seed, long long k, const double L[3], int nps, const double *geom,
+                     double *out)
+{
+  double p[3], R[9];
+  int c, i;
+  for (c = 0; c < 3; c++)
+    p[c] = (double)(uint32_t)(orc_widom_word(seed, k, c) >> 32) * (1.0 / 4294967296.0) * L[c];
+  if (nps > 1) {
+    double u1 = (double)(orc_widom_word(seed, k, 3) >> 11) * (1.0 / 9007199254740992.0);
+    double u2 = (double)(orc_widom_word(seed, k, 4) >> 11) * (1.0 / 9007199254740992.0);
+    double u3 = (double)(orc_widom_word(seed, k, 5) >> 11) * (1.0 / 9007199254740992.0);
+    double a = sqrt(1 - u1), b = sqrt(u1);
+    double x = a * sin(2 * M_PI * u2), y = a * cos(2 * M_PI * u2);
+    double z = b * sin(2 * M_PI * u3), w = b * cos(2 * M_PI * u3);
+    R[0] = 1 - 2 * (y * y + z * z); R[1] = 2 * (x * y - z * w);     R[2] = 2 * (x * z + y * w);
+    R[3] = 2 * (x * y + z * w);     R[4] = 1 - 2 * (x * x + z * z); R[5] = 2 * (y * z - x * w);
+    R[6] = 2 * (x * z - y * w);     R[7] = 2 * (y * z + x * w);     R[8] = 1 - 2 * (x * x + y * y);
+  } else {
+    R[0] = R[4] = R[8] = 1;
+    R[1] = R[2] = R[3] = R[5] = R[6] = R[7] = 0;
+  }
+  for (i = 0; i < nps; i++)
+    for (c = 0; c < 3; c++)
+      out[3 * i + c] = p[c] + R[3 * c] * geom[3 * i] + R[3 * c + 1] * geom[3 * i + 1] +
+                       R[3 * c + 2] * geom[3 * i + 2];
+}
+
+/* Einsert (cook/widom.c:175-288): energy of a ghost molecule with sites at
+   ppos against every site of the box within the cutoff (nearest image):
+   the pair function of cook/ljqqnp.c (LJ with the smooth cutoff + q q eru,
+   r-space only); no intramolecular exclusion applies to the ghost
+   (lsloc.n = No.s, cook/widom.c:195) */
+double orc_einsert(const orc_sys_t *s, const double *r, int nps, const int *ptype,
+                   const double *pq, const double *ppos)
+{
+  double U = 0, El = 0;
+  const double cq = SQ(s->cutoff);
+  int a, j;
+  for (a = 0; a < nps; a++)
+    for (j = 0; j < s->ns; j++) {
+      double dr[3], rr, x, y;
+      const orc_ss_t *ss = s->ss + ptype[a] * s->ntypes + s->type[j];
+      const double qq = (pq ? pq[a] : 0) * s->q[j];
+      nearest(s->L, ppos + 3 * a, r + 3 * j, dr);
+      rr = SQ(dr[0]) + SQ(dr[1]) + SQ(dr[2]);
+      if (rr >= cq) continue;
+      if (rr < ss->C2q) {
+        if (rr < ss->C1q) {
+          x = ss->Sq / rr;
+          y = x * x * x;
+          U += ss->E4 * (y * y - y);
+        } else {
+          x = rr - ss->C2q;
+          U += x * x * ss->A;
+        }
+      }
+      if (qq != 0) {
+        const double *p = s->ertab + 6 * (int)(rr * s->sgrid);
+        El += (p[1] / (p[2] + rr) + p[0]) * qq;
+      }
+    }
+  return U + El;
+}
+
+typedef struct {
+  const orc_sys_t *s;
+  const double *r, *geom, *pq;
+  const int *ptype;
+  int nps;
+  long long k0, k1;
+  uint64_t seed;
+  double T, sum;
+  double *U;
+} widom_work_t;
+
+static void *widom_worker(void *arg)
+{
+  widom_work_t *w = (widom_work_t *)arg;
+  double pos[3 * 16];
+  long long k;
+  w->sum = 0;
+  for (k = w->k0; k < w->k1; k++) {
+    double U, e;
+    orc_widom_sites(w->seed, k, w->s->L, w->nps, w->geom, pos);
+    U = orc_einsert(w->s, w->r, w->nps, w->ptype, w->pq, pos);
+    if (w->U) w->U[k] = U;
+    e = -U / w->T;
+    if (e > -700) w->sum += exp(e);
+  }
+  return NULL;
+}
+
+/* Widom (sim/simmeas.c:1821-1958): sum over n insertions of exp(-U/T),
+   a term skipped when -U/T <= -700; per-insertion energies into U when
+   U != NULL.  The caller divides by n and applies exp(-corr/(V T)). */
+double orc_widom(const orc_sys_t *s, const double *r, int nps, const int *ptype,
+                 const double *pq, const double *geom, long long n, unsigned long long seed, double T,
+                 double *U, int nthreads)
+{
+  widom_work_t w[64];
+  pthread_t th[64];
+  double sum = 0;
+  int t;
+  if (nps > 16) return -1;
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 64) nthreads = 64;
+  for (t = 0; t < nthreads; t++) {
+    w[t].s = s; w[t].r = r; w[t].geom = geom; w[t].pq = pq; w[t].ptype = ptype;
+    w[t].nps = nps; w[t].seed = seed; w[t].T = T; w[t].U = U;
+    w[t].k0 = n * t / nthreads;
+    w[t].k1 = n * (t + 1) / nthreads;
+    pthread_create(&th[t], NULL, widom_worker, &w[t]);
+  }
+  for (t = 0; t < nthreads; t++) {
+    pthread_join(th[t], NULL);
+    sum += w[t].sum;
+  }
+  return sum;
+}
+
+/* Widomcutcorr (sim/siminit.c:762-808): sum of the pair cutoff corrections
+   (setss, sim/setss.c:454-500) over the ghost's sites x every box site */
+double orc_widom_corr(const orc_sys_t *s, int nps, const int *ptype)
+{
+  double c = 0;
+  int a, j;
+  for (a = 0; a < nps; a++)
+    for (j = 0; j < s->ns; j++) c += s->ss[ptype[a] * s->ntypes + s->type[j]].corr;
+  return c;
 }

@@ -17,6 +17,8 @@
  *                                   sim/shakev3.c:1-33
  *   Drude SCF + ASPC                sim/scf.c:12-393, sim/pred2.c:26-100,
  *                                   cook/ljqqpol.c:15-698
+ *   Widom insertions                cook/widom.c:175-288, sim/simmeas.c:1821-1958,
+ *                                   sim/siminit.c:762-808
  * Parity is pinned against dumps of the reference binary (tests/golden).
  */
 #ifndef COOKORACLE_H
@@ -113,6 +115,19 @@ int orc_shake_step(int ns, double *r, double *r1, const double *f, const double 
 double orc_selffield(const orc_sys_t *s, double *r, double *f, orc_en_t *en, double omega);
 /* ASPC predictor B[0..k+1] and mixing omega (sim/pred2.c:70-97) */
 void orc_aspc_coef(int k, double *B, double *omega);
+
+/* Widom insertions (cook/widom.c:175-288 Einsert, sim/simmeas.c:1821-1958
+   Widom, sim/siminit.c:762-808 Widomcutcorr).  The insertion points come
+   from a counter-based stream shared with the GPU path (orc_widom_word). */
+unsigned long long orc_widom_word(unsigned long long seed, long long k, int c);
+void orc_widom_sites(unsigned long long seed, long long k, const double L[3], int nps,
+                     const double *geom, double *out);
+double orc_einsert(const orc_sys_t *s, const double *r, int nps, const int *ptype,
+                   const double *pq, const double *ppos);
+double orc_widom(const orc_sys_t *s, const double *r, int nps, const int *ptype,
+                 const double *pq, const double *geom, long long n, unsigned long long seed,
+                 double T, double *U, int nthreads);
+double orc_widom_corr(const orc_sys_t *s, int nps, const int *ptype);
 
 #ifdef __cplusplus
 }

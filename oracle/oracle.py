@@ -69,6 +69,17 @@ def lib():
         L.orc_selffield.argtypes = [C.POINTER(SYS), dp, dp, C.POINTER(EN), C.c_double]
         L.orc_selffield.restype = C.c_double
         L.orc_aspc_coef.argtypes = [C.c_int, dp, dp]
+        u64 = C.c_ulonglong
+        L.orc_widom_word.argtypes = [u64, C.c_longlong, C.c_int]
+        L.orc_widom_word.restype = u64
+        L.orc_widom_sites.argtypes = [u64, C.c_longlong, dp, C.c_int, dp, dp]
+        L.orc_einsert.argtypes = [C.POINTER(SYS), dp, C.c_int, ip, dp, dp]
+        L.orc_einsert.restype = C.c_double
+        L.orc_widom.argtypes = [C.POINTER(SYS), dp, C.c_int, ip, dp, dp, C.c_longlong, u64,
+                                C.c_double, dp, C.c_int]
+        L.orc_widom.restype = C.c_double
+        L.orc_widom_corr.argtypes = [C.POINTER(SYS), C.c_int, ip]
+        L.orc_widom_corr.restype = C.c_double
         _lib = L
     return _lib
 
@@ -199,6 +210,33 @@ class Oracle:
                                   _ip(nc), _ip(cfirst), _ip(ci), _ip(cj), _dp(bq), h, eps,
                                   omega, maxit, C.byref(ek))
         return r.reshape(-1, 3), r1.reshape(-1, 3), it, ek.value
+
+
+    # ------------------------------------------------------------ Widom --
+    def widom_sites(self, seed, k, geometry):
+        g = np.ascontiguousarray(geometry, np.float64).reshape(-1, 3)
+        out = np.zeros_like(g)
+        lib().orc_widom_sites(seed, k, _dp(self.L), len(g), _dp(g), _dp(out))
+        return out
+
+    def einsert(self, r, probe_types, probe_q, positions):
+        r = np.ascontiguousarray(r, np.float64).reshape(-1)
+        pt = np.ascontiguousarray(probe_types, np.int32)
+        pq = np.ascontiguousarray(probe_q, np.float64)
+        pp = np.ascontiguousarray(positions, np.float64).reshape(-1)
+        return lib().orc_einsert(C.byref(self.sys), _dp(r), len(pt), _ip(pt), _dp(pq), _dp(pp))
+
+    def widom(self, r, probe_types, probe_q, geometry, n, seed, T, energies=False, nthreads=8):
+        """(sum of exp(-U/T), corr, U or None) over n insertions"""
+        r = np.ascontiguousarray(r, np.float64).reshape(-1)
+        pt = np.ascontiguousarray(probe_types, np.int32)
+        pq = np.ascontiguousarray(probe_q, np.float64)
+        g = np.ascontiguousarray(geometry, np.float64).reshape(-1)
+        U = np.zeros(n) if energies else None
+        s = lib().orc_widom(C.byref(self.sys), _dp(r), len(pt), _ip(pt), _dp(pq), _dp(g), n,
+                            seed, T, _dp(U) if energies else None, nthreads)
+        corr = lib().orc_widom_corr(C.byref(self.sys), len(pt), _ip(pt))
+        return s, corr, U
 
 
 def aspc_coef(k):

@@ -48,6 +48,13 @@ CASES = {
     "drude216": dict(binary="cookpol", species=["WATD"], N=[216], L=18.6206,
                      cutoff=9.0, alpha=0.35, kn=6, steps=6, h=0.001, epsc=1e-10,
                      options=["-p220"], extra_def=["scf.eps=-1"]),
+    # Widom insertions of a neutral LJ probe (sigma 3.2 A, epsilon 0.65
+    # kJ/mol) into 250 + 250 LJ ions of charge +-1 e, L = 37 A (reduced
+    # density 0.5 at sigma 3.7 A), cutoff 10, alpha 0.31, |n|<=8; 1e7
+    # insertions into the configuration of the last force evaluation
+    "widom500": dict(binary="cookwidom", species=["AP", "AM", "PRB"], N=[250, 250, 0],
+                     L=37.0, cutoff=10.0, alpha=0.31, kn=8, steps=1, h=0.002, epsc=1e-10,
+                     extra_def=["corr=1"], extra_get=["widom.sp=2", "widom.n=10000000"]),
 }
 
 
@@ -65,7 +72,8 @@ def def_text(c):
 
 
 def get_text(c):
-    return 'init="crystal"\nno=%d\n;\n' % c["steps"]
+    return "\n".join(['init="crystal"', "no=%d" % c["steps"]] + c.get("extra_get", []) +
+                     [";", ""])
 
 
 def parse_dump(path):
@@ -120,6 +128,13 @@ def run_case(name, c, keep=None):
                 QN=int(m2.group(1)) if m2 else None,
                 omegac=float(m3.group(1)) if m3 else None,
                 species=c["species"], N=c["N"])
+    mw = re.search(r"mu = (\S+) \+- \S+ K \(raw value without cutoff correction\)", prt)
+    if mw:
+        mc = re.search(r"corr = (\S+)/V = (\S+)", prt)
+        mk = re.search(r"mu = (\S+) \+- \S+ kT \(corrected\)", prt)
+        meta["widom"] = dict(mu_raw_K=float(mw.group(1)), corr=float(mc.group(1)),
+                             mu_kT=float(mk.group(1)),
+                             n=int(re.search(r"widom\.n=(\d+)", get_text(c)).group(1)))
     if keep is None:
         shutil.rmtree(wd)
     return dumps, meta

@@ -1,0 +1,96 @@
+"""Widom insertions on the GPU (through the C ABI) against the oracle on the
+same insertion stream: per-insertion energies and the Boltzmann sum, both
+precisions; a multi-site charged ghost (SPC/E water into SPC/E water)."""
+import numpy as np
+import pytest
+
+import macsimus_gb300 as M
+from golden_cases import load
+from macsimus_gb300 import forcefield as ff
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+PRB = [ff.TYPE_ORDER.index("PRB")]
+T = 298.0
+
+
+def ctx(case, precision, **kw):
+    g, meta, system, ew = load(case)
+    fp = M.ForcePath(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"],
+                     precision=precision, **kw)
+    orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
+    return g, meta, system, ew, fp, orc
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("cells", [1, 2])
+def test_lj_probe_energies_and_average(precision, cells):
+    g, meta, system, ew, fp, orc = ctx("widom500", precision, cells_per_cutoff=cells)
+    r = g["r"][-1]
+    fp.forces(r)
+    n = 40000
+    res = fp.widom(PRB, n=n, seed=4242, T=T, energies=True)
+    s, corr, Uo = orc.widom(r, PRB, [0.0], [0, 0, 0], n, 4242, T, energies=True)
+    U = res["U"]
+    ok = Uo < 50 * T
+    if precision == "fp64":
+        assert np.abs(U[ok] - Uo[ok]).max() < 1e-9 * (np.abs(Uo[ok]).max() + 1)
+        assert abs(res["sum"] - s) <= 1e-11 * s
+    else:
+        # FP32 pair energies: ~1e-6 of the largest terms of the sum
+        assert np.abs(U[ok] - Uo[ok]).max() < 1e-2 + 1e-6 * np.abs(Uo[ok]).max()
+        assert abs(res["sum"] - s) <= 2e-6 * s
+    assert abs(res["corr"] - corr) <= 1e-10 * abs(corr)
+    V = float(np.prod(ew["L"]))
+    assert abs(res["factor"] - np.exp(-corr / (V * T))) < 1e-14
+    assert abs(res["mu"] + T * np.log(s / n * res["factor"])) < (1e-8 if precision == "fp64" else 1e-3)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_water_ghost_into_water(precision):
+    """a rigid SPC/E ghost (3 charged sites, random orientations) into the
+    864-water box"""
+    g, meta, system, ew, fp, orc = ctx("spce864", precision)
+    r = g["r"][0]
+    fp.forces(r)
+    sp = ff.spce()
+    types = [ff.TYPE_ORDER.index(t) for t in sp.sites]
+    q = np.array(sp.charges) * ff.ELECTRON
+    geo = sp.geometry - sp.geometry[0]
+    n = 8000
+    res = fp.widom(types, geometry=geo, charges=q, n=n, seed=77, T=T, energies=True)
+    s, corr, Uo = orc.widom(r, types, q, geo, n, 77, T, energies=True)
+    ok = Uo < 50 * T
+    tol = 1e-8 if precision == "fp64" else 5e-3
+    assert np.abs(res["U"][ok] - Uo[ok]).max() < tol * (1 + np.abs(Uo[ok]).max() / 1e3)
+    assert abs(res["sum"] - s) <= (1e-10 if precision == "fp64" else 1e-5) * s
+
+
+def test_reproducible_and_uses_last_force_configuration():
+    g, meta, system, ew, fp, orc = ctx("widom500", "mixed", h=0.002)
+    r0 = g["r"][-1]
+    fp.forces(r0)
+    a = fp.widom(PRB, n=20000, seed=3, T=T)
+    b = fp.widom(PRB, n=20000, seed=3, T=T)
+    assert a["sum"] == b["sum"]
+    # after one MD step the last force evaluation was at the starting point
+    fp.md_set_state(r0, np.zeros_like(r0))
+    fp.md_steps(1, measure=False)
+    c = fp.widom(PRB, n=20000, seed=3, T=T)
+    assert abs(c["sum"] - a["sum"]) <= 1e-12 * a["sum"]
+
+
+def test_errors_are_reported():
+    g, meta, system, ew = load("widom500")
+    fp = M.ForcePath(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
+    with pytest.raises(M.MGError):
+        fp.widom(PRB, n=10)          # no force evaluation yet
+    fp.forces(g["r"][-1])
+    with pytest.raises(M.MGError):
+        fp.widom([99], n=10)         # type out of range
+    gd, md, sd, ed = load("drude216")
+    fd = M.ForcePath(sd, ed["L"], ed["cutoff"], ed["alpha"], ed["kappa"])
+    fd.forces(np.vstack([gd["r"][0], gd["rD"][0]]))
+    with pytest.raises(M.MGError):
+        fd.widom([0], n=10)          # Drude systems are not supported
