@@ -239,6 +239,30 @@ typedef struct {
 int mg_widom(mg_ctx *ctx, const mg_probe *probe, long long ninsert, unsigned long long seed,
              double T, mg_widom_result *out, double *U);
 
+/* ---- batches of independent boxes ----
+   No reference counterpart (cook runs one box per process).  A batch owns
+   nbox contexts whose kernels run on nlanes streams; mg_batch_md_steps
+   replays one captured CUDA graph per MD step of all boxes (non-polar boxes
+   with cells re-binned at every step); mg_batch_widom inserts into every
+   box in one kernel launch (box i draws from seed + i * 0x632BE59BD9B4E019).
+   Per-box state, forces and single-box calls go through mg_batch_box(). */
+typedef struct mg_batch mg_batch;
+
+mg_batch *mg_batch_create(int nbox, const mg_topology *tops, const mg_params *params,
+                          int nlanes, int *status);
+int mg_batch_destroy(mg_batch *b);
+const char *mg_batch_last_error(const mg_batch *b);
+int mg_batch_size(const mg_batch *b);
+mg_ctx *mg_batch_box(mg_batch *b, int i);
+/* kernels launched by the last batch call (graph nodes counted per step) */
+int mg_batch_last_launches(const mg_batch *b);
+/* en: NULL or [nbox] energies of the last step */
+int mg_batch_md_steps(mg_batch *b, int nsteps, mg_energy *en);
+/* probes: one ghost for all boxes (probe_per_box = 0) or [nbox];
+   out: [nbox] */
+int mg_batch_widom(mg_batch *b, const mg_probe *probes, int probe_per_box, long long ninsert,
+                   unsigned long long seed, double T, mg_widom_result *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -113,6 +113,18 @@ def library():
         L.mg_probe_fp32_tflops.argtypes = [_dp]
         L.mg_widom.argtypes = [vp, C.POINTER(Probe), C.c_longlong, C.c_ulonglong, C.c_double,
                                C.POINTER(WidomResult), _dp]
+        L.mg_batch_create.argtypes = [C.c_int, C.POINTER(Topology), C.POINTER(Params), C.c_int,
+                                      _ip]
+        L.mg_batch_create.restype = vp
+        L.mg_batch_destroy.argtypes = [vp]
+        L.mg_batch_last_error.argtypes = [vp]
+        L.mg_batch_last_error.restype = C.c_char_p
+        L.mg_batch_box.argtypes = [vp, C.c_int]
+        L.mg_batch_box.restype = vp
+        L.mg_batch_last_launches.argtypes = [vp]
+        L.mg_batch_md_steps.argtypes = [vp, C.c_int, C.POINTER(Energy)]
+        L.mg_batch_widom.argtypes = [vp, C.POINTER(Probe), C.c_int, C.c_longlong, C.c_ulonglong,
+                                     C.c_double, C.POINTER(WidomResult)]
         L.mg_ewald_kspace_noalloc.argtypes = [vp, vp, C.c_int, _dp, C.c_double, C.c_double, vp,
                                               _dp, vp]
         _lib = L
@@ -132,6 +144,72 @@ def _arr(a, dt):
     return np.ascontiguousarray(a, dtype=dt)
 
 
+def describe(system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None, grid=256,
+             rshift=3, rplus=2.5, epsinf=3e33, h=0.002, epsc=1e-7, omegac=1.2, shake_maxit=1000,
+             cells_per_cutoff=0, aspc_k=2, scf_iter=1, scf_omega=0.6, minqq=1.0, skin=0.0,
+             nl_every=50):
+    """(mg_topology, mg_params, arrays to keep alive) of one box"""
+    keep = []
+
+    def ip(a):
+        a = _arr(a, np.int32)
+        keep.append(a)
+        return a.ctypes.data_as(_ip)
+
+    def dp(a):
+        a = _arr(a, np.float64)
+        keep.append(a)
+        return a.ctypes.data_as(_dp)
+
+    t = Topology()
+    t.ns = system.ns
+    t.nmol = system.nmol
+    t.mol_first = ip(system.mol_first)
+    t.site_type = ip(system.type)
+    t.charge = dp(system.q)
+    t.mass = dp(system.mass)
+    t.ntypes = len(system.typeE)
+    t.type_EvdW = dp(system.typeE)
+    t.type_RvdW = dp(system.typeR)
+    t.type_alpha = dp(system.typeA)
+    t.comb_rule = system.comb_rule
+    t.nc = len(system.cons_len)
+    t.cons = ip(system.cons.reshape(-1))
+    t.cons_len = dp(system.cons_len)
+    t.mol_cfirst = ip(system.mol_cfirst)
+    if getattr(system, "polar", False):
+        t.chargepol = dp(system.qpol)
+        t.alphapol = dp(system.alphapol)
+    else:
+        t.chargepol = None
+        t.alphapol = None
+    p = Params()
+    Lb = np.broadcast_to(np.asarray(L, dtype=np.float64), (3,))
+    for k in range(3):
+        p.L[k] = float(Lb[k])
+    p.cutoff = cutoff
+    p.LJcutoff = LJcutoff if LJcutoff else cutoff
+    p.alpha = alpha
+    p.kappa = kappa
+    p.grid = grid
+    p.rshift = rshift
+    p.rplus = rplus
+    p.epsinf = epsinf
+    p.precision = MG_MIXED if precision == "mixed" else MG_FP64
+    p.h = h
+    p.epsc = epsc
+    p.omegac = omegac
+    p.shake_maxit = shake_maxit
+    p.cells_per_cutoff = cells_per_cutoff
+    p.aspc_k = aspc_k
+    p.scf_iter = scf_iter
+    p.scf_omega = scf_omega
+    p.minqq = minqq
+    p.skin = skin
+    p.nl_every = nl_every
+    return t, p, keep
+
+
 class ForcePath:
     """One box on the current GPU: topology + Ewald/LJ parameters."""
 
@@ -142,77 +220,44 @@ class ForcePath:
         lib = library()
         self.system = system
         self.ns = system.ns
-        keep = []
-
-        def ip(a):
-            a = _arr(a, np.int32)
-            keep.append(a)
-            return a.ctypes.data_as(_ip)
-
-        def dp(a):
-            a = _arr(a, np.float64)
-            keep.append(a)
-            return a.ctypes.data_as(_dp)
-
-        t = Topology()
-        t.ns = system.ns
-        t.nmol = system.nmol
-        t.mol_first = ip(system.mol_first)
-        t.site_type = ip(system.type)
-        t.charge = dp(system.q)
-        t.mass = dp(system.mass)
-        t.ntypes = len(system.typeE)
-        t.type_EvdW = dp(system.typeE)
-        t.type_RvdW = dp(system.typeR)
-        t.type_alpha = dp(system.typeA)
-        t.comb_rule = system.comb_rule
-        t.nc = len(system.cons_len)
-        t.cons = ip(system.cons.reshape(-1))
-        t.cons_len = dp(system.cons_len)
-        t.mol_cfirst = ip(system.mol_cfirst)
+        t, p, self._keep = describe(system, L, cutoff, alpha, kappa, precision=precision,
+                                    LJcutoff=LJcutoff, grid=grid, rshift=rshift, rplus=rplus,
+                                    epsinf=epsinf, h=h, epsc=epsc, omegac=omegac,
+                                    shake_maxit=shake_maxit, cells_per_cutoff=cells_per_cutoff,
+                                    aspc_k=aspc_k, scf_iter=scf_iter, scf_omega=scf_omega,
+                                    minqq=minqq, skin=skin, nl_every=nl_every)
         self.polar = getattr(system, "polar", False)
-        if self.polar:
-            t.chargepol = dp(system.qpol)
-            t.alphapol = dp(system.alphapol)
-        else:
-            t.chargepol = None
-            t.alphapol = None
-        p = Params()
         Lb = np.broadcast_to(np.asarray(L, dtype=np.float64), (3,))
-        for k in range(3):
-            p.L[k] = float(Lb[k])
-        p.cutoff = cutoff
-        p.LJcutoff = LJcutoff if LJcutoff else cutoff
-        p.alpha = alpha
-        p.kappa = kappa
-        p.grid = grid
-        p.rshift = rshift
-        p.rplus = rplus
-        p.epsinf = epsinf
-        p.precision = MG_MIXED if precision == "mixed" else MG_FP64
-        p.h = h
-        p.epsc = epsc
-        p.omegac = omegac
-        p.shake_maxit = shake_maxit
-        p.cells_per_cutoff = cells_per_cutoff
-        p.aspc_k = aspc_k
-        p.scf_iter = scf_iter
-        p.scf_omega = scf_omega
-        p.minqq = minqq
-        p.skin = skin
-        p.nl_every = nl_every
         st = C.c_int(0)
         self._ctx = lib.mg_create(C.byref(t), C.byref(p), C.byref(st))
         if not self._ctx:
             raise MGError(st.value, "mg_create failed")
+        self._owned = True
         self.precision = precision
         self.L = np.array(Lb)
         self.kappa = lib.mg_kappa(self._ctx)
         self.nkvec = lib.mg_nkvec(self._ctx)
 
+    @classmethod
+    def _borrow(cls, ctx, system, L, precision, owner):
+        """a view of a context owned by a Batch (not destroyed by close())"""
+        fp = cls.__new__(cls)
+        fp._ctx = ctx
+        fp._owned = False
+        fp._owner = owner
+        fp.system = system
+        fp.ns = system.ns
+        fp.polar = getattr(system, "polar", False)
+        fp.precision = precision
+        fp.L = np.array(np.broadcast_to(np.asarray(L, dtype=np.float64), (3,)))
+        fp.kappa = library().mg_kappa(ctx)
+        fp.nkvec = library().mg_nkvec(ctx)
+        return fp
+
     def close(self):
         if getattr(self, "_ctx", None):
-            library().mg_destroy(self._ctx)
+            if getattr(self, "_owned", True):
+                library().mg_destroy(self._ctx)
             self._ctx = None
 
     def __del__(self):
@@ -334,3 +379,74 @@ class ForcePath:
         if energies:
             out["U"] = U
         return out
+
+
+class Batch:
+    """Independent boxes on the current GPU, stepped together: one captured
+    CUDA graph per MD step of all boxes, one kernel launch for the Widom
+    insertions of all boxes.  boxes: list of dicts with the ForcePath
+    arguments (system, L, cutoff, alpha, kappa, and keywords)."""
+
+    def __init__(self, boxes, precision="mixed", lanes=16):
+        lib = library()
+        self.nbox = len(boxes)
+        tops = (Topology * self.nbox)()
+        pars = (Params * self.nbox)()
+        self._keep = []
+        self.systems = []
+        for i, b in enumerate(boxes):
+            b = dict(b)
+            system = b.pop("system")
+            t, p, keep = describe(system, b.pop("L"), b.pop("cutoff"), b.pop("alpha"),
+                                  b.pop("kappa"), precision=precision, **b)
+            tops[i] = t
+            pars[i] = p
+            self._keep.append(keep)
+            self.systems.append(system)
+        st = C.c_int(0)
+        self._b = lib.mg_batch_create(self.nbox, tops, pars, int(lanes), C.byref(st))
+        if not self._b:
+            raise MGError(st.value, "mg_batch_create failed")
+        self.precision = precision
+        self.box = [ForcePath._borrow(lib.mg_batch_box(self._b, i), self.systems[i],
+                                      [pars[i].L[0], pars[i].L[1], pars[i].L[2]], precision, self)
+                    for i in range(self.nbox)]
+
+    def _check(self, rc):
+        if rc != 0:
+            raise MGError(rc, library().mg_batch_last_error(self._b).decode())
+
+    @property
+    def launches(self):
+        return library().mg_batch_last_launches(self._b)
+
+    def md_steps(self, n, measure=True):
+        en = (Energy * self.nbox)()
+        self._check(library().mg_batch_md_steps(self._b, int(n), en if measure else None))
+        return [e.asdict() for e in en] if measure else None
+
+    def widom(self, site_types, geometry=None, charges=None, n=100000, seed=1, T=298.0):
+        """the same ghost inserted n times into every box (box i uses the
+        stream of seed + i * 0x632BE59BD9B4E019); list of result dicts"""
+        st = _arr(site_types, np.int32).reshape(-1)
+        g = _arr(np.zeros((len(st), 3)) if geometry is None else geometry, np.float64).reshape(-1)
+        q = None if charges is None else _arr(charges, np.float64).reshape(-1)
+        pr = Probe(len(st), st.ctypes.data_as(_ip), q.ctypes.data_as(_dp) if q is not None else None,
+                   g.ctypes.data_as(_dp))
+        out = (WidomResult * self.nbox)()
+        self._check(library().mg_batch_widom(self._b, C.byref(pr), 0, int(n), int(seed), float(T),
+                                             out))
+        return [o.asdict() for o in out]
+
+    def close(self):
+        if getattr(self, "_b", None):
+            for fp in self.box:
+                fp._ctx = None
+            library().mg_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

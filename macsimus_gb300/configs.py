@@ -161,3 +161,38 @@ def equilibrate(w, steps=400, T=298.0, every=20, h=None, polar_steps=200, **kw):
     out["r"], out["r1"] = r, r1
     out["equilibrated"] = steps + (polar_steps if system.polar else 0)
     return out
+
+
+def ionic_boxes(nbox=256, seed=0, T=298.0, h=0.002, nmin=500, nmax=4000, rho_star=0.8):
+    """Independent LJ + point-charge ionic-fluid boxes: per box N uniform in
+    [nmin, nmax] (even, equimolar +-1 e), sigma uniform in [3.0, 4.5] A and
+    epsilon in [0.1, 1.0] kJ/mol for each ion type, number density
+    rho_star / sigma_mean^3, cutoff 2.5 sigma_max (at most 0.49 L), Ewald
+    alpha = 3.1/cutoff and |n| <= 1.08 alpha L (erfc and Gaussian tails
+    ~1e-5 at the cutoffs).  Ions start on a simple cubic lattice, randomly
+    assigned, with Maxwell velocities at T (zero total momentum)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for b in range(nbox):
+        n = 2 * int(rng.integers(nmin // 2, nmax // 2 + 1))
+        sp, sm = rng.uniform(3.0, 4.5, 2)
+        ep, em = rng.uniform(0.1, 1.0, 2)
+        system = ff.ionic_system(n, sp, ep, sm, em)
+        smean = 0.5 * (sp + sm)
+        L = (n * smean ** 3 / rho_star) ** (1.0 / 3.0)
+        cutoff = min(2.5 * max(sp, sm), 0.49 * L)
+        alpha = 3.1 / cutoff
+        kn = int(math.ceil(1.08 * alpha * L))
+        m = 1
+        while m ** 3 < n:
+            m += 1
+        grid = (np.array([[i, j, k] for i in range(m) for j in range(m) for k in range(m)], float)
+                + 0.5) * (L / m)
+        pick = rng.permutation(len(grid))[:n]
+        r = grid[pick][rng.permutation(n)]
+        v = rng.normal(size=(n, 3)) * np.sqrt(T / system.mass)[:, None]
+        v -= (system.mass[:, None] * v).sum(0) / system.mass.sum()
+        out.append(dict(name="ionic%d" % b, system=system, r=r, r1=h * v, L=L, cutoff=cutoff,
+                        alpha=alpha, kappa=(kn + 1e-6) / L, kn=kn, h=h, sigma=(sp, sm),
+                        epsilon=(ep, em)))
+    return out

@@ -100,6 +100,10 @@ struct mg_ctx {
   PairF* d_wtabf = nullptr;
   PairD* d_wtabd = nullptr;
   double *d_wgeom = nullptr, *d_wpart = nullptr;
+  WidomBox* d_wbox = nullptr;
+  std::vector<PairF> h_wtabf;
+  std::vector<PairD> h_wtabd;
+  std::vector<double> h_wgeom;
   // Drude
   bool polar = false;
   int nd = 0, ndblocks = 0, aspc_k = 2, aspc_kk = 0, scf_iter = 1, hist_h = 0;
@@ -792,6 +796,39 @@ void fill_energy(mg_ctx* ctx, mg_energy* en) {
   }
 }
 
+ShakeArgs shake_args(mg_ctx* ctx) {
+  ShakeArgs sa;
+  sa.nmol = ctx->nmol;
+  sa.mol_first = ctx->d_mol_first;
+  sa.mol_cfirst = ctx->d_mol_cfirst;
+  sa.cons = ctx->d_cons;
+  sa.bondq = ctx->d_bondq;
+  sa.imass = ctx->d_imass;
+  sa.mass = ctx->d_mass;
+  sa.hh = ctx->h * ctx->h;
+  sa.eps = ctx->epsc;
+  sa.omega = ctx->omega;
+  sa.maxit = ctx->shake_maxit;
+  sa.r = ctx->d_r;
+  sa.r1 = ctx->d_r1;
+  sa.f = ctx->d_f;
+  sa.p = ctx->d_p;
+  sa.kin_part = ctx->d_kinpart;
+  sa.status = ctx->d_status;
+  return sa;
+}
+
+// one leap-frog + SHAKE step of a non-polar box with cells re-binned at the
+// force evaluation: kernels only, no host synchronisation (graph capture)
+int md_step_enqueue(mg_ctx* ctx, bool measure) {
+  Launch L = launch(ctx);
+  int rc = forces_async(ctx, ctx->d_r, ctx->d_f, measure);
+  if (rc) return rc;
+  CK(k_shake(L, shake_args(ctx)));
+  if (measure) CK(k_reduce_sum(L, ctx->d_kinpart, (ctx->nmol + 127) / 128, 1, ctx->d_sums + 17));
+  return MG_OK;
+}
+
 int fetch_sums(mg_ctx* ctx) {
   CK(cudaMemcpyAsync(ctx->h_sums, ctx->d_sums, 32 * sizeof(double), cudaMemcpyDeviceToHost,
                      ctx->stream));
@@ -852,7 +889,7 @@ int mg_destroy(mg_ctx* ctx) {
                   ctx->d_tiles, ctx->d_p1job, ctx->d_dsite, ctx->d_qdrude, ctx->d_qc,
                   ctx->d_qp, ctx->d_aqq, ctx->d_hist, ctx->d_drpart, ctx->d_pdj, ctx->d_pdd,
                   ctx->d_nlist, ctx->d_ncount, ctx->d_rbuild, ctx->d_dmax,
-                  ctx->d_wtabf, ctx->d_wtabd, ctx->d_wgeom, ctx->d_wpart};
+                  ctx->d_wtabf, ctx->d_wtabd, ctx->d_wgeom, ctx->d_wpart, ctx->d_wbox};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ctx->h_sums) cudaFreeHost(ctx->h_sums);
@@ -1028,24 +1065,7 @@ int mg_md_steps(mg_ctx* ctx, int nsteps, mg_energy* en) {
   if (!ctx || !ctx->have_state || nsteps < 0) return fail(ctx, MG_ERR_ARG, "no MD state");
   ctx->launches = 0;
   Launch L = launch(ctx);
-  ShakeArgs sa;
-  sa.nmol = ctx->nmol;
-  sa.mol_first = ctx->d_mol_first;
-  sa.mol_cfirst = ctx->d_mol_cfirst;
-  sa.cons = ctx->d_cons;
-  sa.bondq = ctx->d_bondq;
-  sa.imass = ctx->d_imass;
-  sa.mass = ctx->d_mass;
-  sa.hh = ctx->h * ctx->h;
-  sa.eps = ctx->epsc;
-  sa.omega = ctx->omega;
-  sa.maxit = ctx->shake_maxit;
-  sa.r = ctx->d_r;
-  sa.r1 = ctx->d_r1;
-  sa.f = ctx->d_f;
-  sa.p = ctx->d_p;
-  sa.kin_part = ctx->d_kinpart;
-  sa.status = ctx->d_status;
+  const ShakeArgs sa = shake_args(ctx);
   const int nkin = (ctx->nmol + 127) / 128;
   for (int s = 0; s < nsteps; s++) {
     const bool last = s == nsteps - 1;
@@ -1121,9 +1141,14 @@ int mg_md_steps(mg_ctx* ctx, int nsteps, mg_energy* en) {
   return MG_OK;
 }
 
-int mg_widom(mg_ctx* ctx, const mg_probe* probe, long long ninsert, unsigned long long seed,
-             double T, mg_widom_result* out, double* U) {
-  if (!ctx || !probe || !out) return fail(ctx, MG_ERR_ARG, "null argument");
+namespace {
+
+// Widom set-up of one box: checks, the ghost-site x site-kind pair table and
+// the ghost geometry uploaded (on the context's stream), the cutoff
+// correction, and the launch descriptor
+int widom_prepare(mg_ctx* ctx, const mg_probe* probe, long long ninsert, unsigned long long seed,
+                  double T, double* d_U, WidomBox* box, double* corr_out) {
+  if (!ctx || !probe) return fail(ctx, MG_ERR_ARG, "null argument");
   const int nps = probe->ns;
   if (nps < 1 || nps > MG_WIDOM_MAX_SITES || !probe->site_type || !probe->geometry)
     return fail(ctx, MG_ERR_ARG, "the ghost needs 1..8 sites with types and geometry");
@@ -1142,8 +1167,10 @@ int mg_widom(mg_ctx* ctx, const mg_probe* probe, long long ninsert, unsigned lon
   }
   // pair constants of every ghost site with every site kind of the box, and
   // the cutoff correction over all (ghost site, box site) pairs
-  std::vector<PairF> tf(MAX_WPROBE * MAX_KINDS);
-  std::vector<PairD> td(MAX_WPROBE * MAX_KINDS);
+  std::vector<PairF>& tf = ctx->h_wtabf;
+  std::vector<PairD>& td = ctx->h_wtabd;
+  tf.assign(MAX_WPROBE * MAX_KINDS, PairF{});
+  td.assign(MAX_WPROBE * MAX_KINDS, PairD{});
   double corr = 0;
   for (int s = 0; s < nps; s++) {
     const int ta = probe->site_type[s];
@@ -1172,18 +1199,23 @@ int mg_widom(mg_ctx* ctx, const mg_probe* probe, long long ninsert, unsigned lon
                                      0.f, 0.f, 0.f, 0.f, qq, 0, 0, 0};
     }
   }
-  const int nblk = widom_blocks(ninsert);
   if (!ctx->d_wgeom) {
     CK(dalloc(&ctx->d_wgeom, 3 * MAX_WPROBE));
     CK(dalloc(&ctx->d_wpart, 152 * 8));
     CK(dalloc(&ctx->d_wtabf, MAX_WPROBE * MAX_KINDS));
     CK(dalloc(&ctx->d_wtabd, MAX_WPROBE * MAX_KINDS));
+    CK(dalloc(&ctx->d_wbox, 1));
   }
-  CK(cudaMemcpyAsync(ctx->d_wgeom, probe->geometry, sizeof(double) * 3 * nps,
+  ctx->h_wgeom.assign(probe->geometry, probe->geometry + 3 * nps);
+  CK(cudaMemcpyAsync(ctx->d_wgeom, ctx->h_wgeom.data(), sizeof(double) * 3 * nps,
                      cudaMemcpyHostToDevice, ctx->stream));
-  double* d_U = nullptr;
-  if (U) CK(cudaMalloc((void**)&d_U, sizeof(double) * ninsert));
-  WidomArgs w;
+  if (ctx->precision == MG_MIXED)
+    CK(cudaMemcpyAsync(ctx->d_wtabf, tf.data(), sizeof(PairF) * tf.size(), cudaMemcpyHostToDevice,
+                       ctx->stream));
+  else
+    CK(cudaMemcpyAsync(ctx->d_wtabd, td.data(), sizeof(PairD) * td.size(), cudaMemcpyHostToDevice,
+                       ctx->stream));
+  WidomArgs& w = box->a;
   w.n = ninsert;
   w.seed = seed;
   w.T = T;
@@ -1205,17 +1237,47 @@ int mg_widom(mg_ctx* ctx, const mg_probe* probe, long long ninsert, unsigned lon
   w.geom = ctx->d_wgeom;
   w.U = d_U;
   w.part = ctx->d_wpart;
-  Launch L = launch(ctx);
-  cudaError_t e;
-  if (ctx->precision == MG_MIXED) {
-    CK(cudaMemcpyAsync(ctx->d_wtabf, tf.data(), sizeof(PairF) * tf.size(), cudaMemcpyHostToDevice,
-                       ctx->stream));
-    e = k_widom_mixed(L, w, ctx->d_pj, ctx->d_wtabf, ctx->d_eru);
-  } else {
-    CK(cudaMemcpyAsync(ctx->d_wtabd, td.data(), sizeof(PairD) * td.size(), cudaMemcpyHostToDevice,
-                       ctx->stream));
-    e = k_widom_fp64(L, w, ctx->d_pd, ctx->d_wtabd, ctx->d_ert);
+  box->pj = ctx->d_pj;
+  box->pd = ctx->d_pd;
+  box->tabf = ctx->d_wtabf;
+  box->tabd = ctx->d_wtabd;
+  box->eru = ctx->d_eru;
+  box->ert = ctx->d_ert;
+  *corr_out = corr;
+  return MG_OK;
+}
+
+void widom_result(const mg_ctx* ctx, const double* part, int nblk, long long n, double T,
+                  double corr, mg_widom_result* out) {
+  double sum = 0;
+  for (int b = 0; b < nblk; b++) sum += part[b];
+  const double V = ctx->L[0] * ctx->L[1] * ctx->L[2];
+  out->sum = sum;
+  out->raw = sum / (double)n;
+  out->corr = corr;
+  out->factor = std::exp(-corr / (V * T));
+  out->widom = out->raw * out->factor;
+  out->mu = -T * std::log(out->widom);
+}
+
+}  // namespace
+
+int mg_widom(mg_ctx* ctx, const mg_probe* probe, long long ninsert, unsigned long long seed,
+             double T, mg_widom_result* out, double* U) {
+  if (!ctx || !out) return fail(ctx, MG_ERR_ARG, "null argument");
+  double* d_U = nullptr;
+  if (U) CK(cudaMalloc((void**)&d_U, sizeof(double) * std::max(ninsert, 1LL)));
+  WidomBox box;
+  double corr = 0;
+  int rc = widom_prepare(ctx, probe, ninsert, seed, T, d_U, &box, &corr);
+  if (rc) {
+    if (d_U) cudaFree(d_U);
+    return rc;
   }
+  const int nblk = widom_blocks(ninsert);
+  CK(cudaMemcpyAsync(ctx->d_wbox, &box, sizeof(WidomBox), cudaMemcpyHostToDevice, ctx->stream));
+  Launch L = launch(ctx);
+  cudaError_t e = k_widom(L, ctx->d_wbox, 1, ninsert, ctx->precision != MG_MIXED);
   if (e != cudaSuccess) {
     if (d_U) cudaFree(d_U);
     return fail(ctx, MG_ERR_CUDA, std::string("widom: ") + cudaGetErrorString(e));
@@ -1226,15 +1288,7 @@ int mg_widom(mg_ctx* ctx, const mg_probe* probe, long long ninsert, unsigned lon
   if (U) CK(cudaMemcpyAsync(U, d_U, sizeof(double) * ninsert, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   if (d_U) CK(cudaFree(d_U));
-  double sum = 0;
-  for (double v : part) sum += v;
-  const double V = ctx->L[0] * ctx->L[1] * ctx->L[2];
-  out->sum = sum;
-  out->raw = sum / (double)ninsert;
-  out->corr = corr;
-  out->factor = std::exp(-corr / (V * T));
-  out->widom = out->raw * out->factor;
-  out->mu = -T * std::log(out->widom);
+  widom_result(ctx, part.data(), nblk, ninsert, T, corr, out);
   return MG_OK;
 }
 
@@ -1329,3 +1383,218 @@ int mg_probe_fp32_tflops(double* tflops) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------- batches --
+
+struct mg_batch {
+  std::string err;
+  std::vector<mg_ctx*> box;
+  cudaStream_t main = nullptr;
+  std::vector<cudaStream_t> lanes;
+  std::vector<cudaEvent_t> ev_join;
+  cudaEvent_t ev_fork = nullptr;
+  cudaGraphExec_t g_step = nullptr, g_meas = nullptr;
+  int launches_step = 0, launches = 0;
+  WidomBox* d_wbox = nullptr;
+  int wcap = 0;
+};
+
+namespace {
+
+int bfail(mg_batch* b, int code, const std::string& msg) {
+  if (b) b->err = msg;
+  return code;
+}
+
+#define BCK(call)                                                                     \
+  do {                                                                                \
+    cudaError_t e_ = (call);                                                          \
+    if (e_ != cudaSuccess)                                                            \
+      return bfail(b, MG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// one MD step of every box as a graph: fork from the main stream onto the
+// lanes (boxes round-robin), each box's kernels on its lane, join
+int capture_step(mg_batch* b, bool measure, cudaGraphExec_t* out) {
+  BCK(cudaStreamBeginCapture(b->main, cudaStreamCaptureModeRelaxed));
+  int rc = MG_OK;
+  cudaEventRecord(b->ev_fork, b->main);
+  for (cudaStream_t s : b->lanes) cudaStreamWaitEvent(s, b->ev_fork, 0);
+  int nl = 0;
+  for (size_t i = 0; i < b->box.size() && !rc; i++) {
+    mg_ctx* c = b->box[i];
+    c->launches = 0;
+    rc = md_step_enqueue(c, measure);
+    if (rc) b->err = "box " + std::to_string(i) + ": " + c->err;
+    nl += c->launches;
+  }
+  for (size_t l = 0; l < b->lanes.size(); l++) {
+    cudaEventRecord(b->ev_join[l], b->lanes[l]);
+    cudaStreamWaitEvent(b->main, b->ev_join[l], 0);
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(b->main, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return bfail(b, MG_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess)
+    return bfail(b, MG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  b->launches_step = nl;
+  return MG_OK;
+}
+
+}  // namespace
+
+mg_batch* mg_batch_create(int nbox, const mg_topology* tops, const mg_params* params, int nlanes,
+                          int* status) {
+  int dummy;
+  int* st = status ? status : &dummy;
+  if (nbox < 1 || !tops || !params) {
+    *st = MG_ERR_ARG;
+    return nullptr;
+  }
+  mg_batch* b = new mg_batch;
+  const int nl = std::max(1, std::min(nlanes > 0 ? nlanes : 16, nbox));
+  if (cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess) {
+    *st = MG_ERR_CUDA;
+    mg_batch_destroy(b);
+    return nullptr;
+  }
+  b->lanes.resize(nl);
+  b->ev_join.resize(nl);
+  for (int l = 0; l < nl; l++) {
+    if (cudaStreamCreateWithFlags(&b->lanes[l], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_join[l], cudaEventDisableTiming) != cudaSuccess) {
+      *st = MG_ERR_CUDA;
+      mg_batch_destroy(b);
+      return nullptr;
+    }
+  }
+  for (int i = 0; i < nbox; i++) {
+    int s = 0;
+    mg_ctx* c = mg_create(&tops[i], &params[i], &s);
+    if (!c) {
+      *st = s ? s : MG_ERR_SETUP;
+      mg_batch_destroy(b);
+      return nullptr;
+    }
+    c->stream = b->lanes[i % nl];
+    b->box.push_back(c);
+  }
+  *st = MG_OK;
+  return b;
+}
+
+int mg_batch_destroy(mg_batch* b) {
+  if (!b) return MG_OK;
+  if (b->main) cudaStreamSynchronize(b->main);
+  for (mg_ctx* c : b->box) {
+    cudaStreamSynchronize(c->stream);
+    c->stream = c->own_stream;
+    mg_destroy(c);
+  }
+  if (b->g_step) cudaGraphExecDestroy(b->g_step);
+  if (b->g_meas) cudaGraphExecDestroy(b->g_meas);
+  if (b->d_wbox) cudaFree(b->d_wbox);
+  for (cudaEvent_t e : b->ev_join)
+    if (e) cudaEventDestroy(e);
+  for (cudaStream_t s : b->lanes)
+    if (s) cudaStreamDestroy(s);
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  if (b->main) cudaStreamDestroy(b->main);
+  delete b;
+  return MG_OK;
+}
+
+const char* mg_batch_last_error(const mg_batch* b) { return b ? b->err.c_str() : "null batch"; }
+int mg_batch_size(const mg_batch* b) { return b ? (int)b->box.size() : 0; }
+mg_ctx* mg_batch_box(mg_batch* b, int i) {
+  return (b && i >= 0 && i < (int)b->box.size()) ? b->box[i] : nullptr;
+}
+int mg_batch_last_launches(const mg_batch* b) { return b ? b->launches : 0; }
+
+int mg_batch_md_steps(mg_batch* b, int nsteps, mg_energy* en) {
+  if (!b || nsteps < 0) return bfail(b, MG_ERR_ARG, "bad arguments");
+  for (size_t i = 0; i < b->box.size(); i++) {
+    const mg_ctx* c = b->box[i];
+    if (!c->have_state) return bfail(b, MG_ERR_ARG, "box " + std::to_string(i) + ": no MD state");
+    if (c->polar || c->use_list || c->prof_on)
+      return bfail(b, MG_ERR_ARG, "box " + std::to_string(i) +
+                                      ": batched MD needs non-polar boxes, cells re-binned "
+                                      "every step and profiling off");
+  }
+  // the lanes must have finished what the per-box calls queued on them
+  for (cudaStream_t s : b->lanes) BCK(cudaStreamSynchronize(s));
+  b->launches = 0;
+  for (int s = 0; s < nsteps; s++) {
+    const bool meas = en && s == nsteps - 1;
+    cudaGraphExec_t& g = meas ? b->g_meas : b->g_step;
+    if (!g) {
+      int rc = capture_step(b, meas, &g);
+      if (rc) return rc;
+    }
+    BCK(cudaGraphLaunch(g, b->main));
+    b->launches += b->launches_step;
+  }
+  BCK(cudaStreamSynchronize(b->main));
+  for (size_t i = 0; i < b->box.size(); i++) {
+    mg_ctx* c = b->box[i];
+    int rc = fetch_status(c);
+    if (!rc && en) rc = fetch_sums(c);
+    if (!rc) {
+      cudaError_t e = cudaStreamSynchronize(c->stream);
+      if (e != cudaSuccess) rc = fail(c, MG_ERR_CUDA, cudaGetErrorString(e));
+    }
+    if (!rc) rc = check_status(c);
+    if (rc) return bfail(b, rc, "box " + std::to_string(i) + ": " + c->err);
+    if (en) {
+      fill_energy(c, &en[i]);
+      en[i].ekin = c->h_sums[17] / (c->h * c->h) / 4;
+    }
+  }
+  return MG_OK;
+}
+
+int mg_batch_widom(mg_batch* b, const mg_probe* probes, int probe_per_box, long long ninsert,
+                   unsigned long long seed, double T, mg_widom_result* out) {
+  if (!b || !probes || !out) return bfail(b, MG_ERR_ARG, "null argument");
+  const int nbox = (int)b->box.size();
+  std::vector<WidomBox> desc(nbox);
+  std::vector<double> corr(nbox);
+  for (int i = 0; i < nbox; i++) {
+    mg_ctx* c = b->box[i];
+    int rc = widom_prepare(c, probe_per_box ? &probes[i] : probes, ninsert,
+                           seed + 0x632BE59BD9B4E019ULL * (unsigned long long)i, T, nullptr,
+                           &desc[i], &corr[i]);
+    if (rc) return bfail(b, rc, "box " + std::to_string(i) + ": " + c->err);
+    if (c->precision != b->box[0]->precision)
+      return bfail(b, MG_ERR_ARG, "all boxes of a batch need the same precision");
+  }
+  for (cudaStream_t s : b->lanes) BCK(cudaStreamSynchronize(s));
+  if (b->wcap < nbox) {
+    if (b->d_wbox) cudaFree(b->d_wbox);
+    b->d_wbox = nullptr;
+    BCK(cudaMalloc((void**)&b->d_wbox, sizeof(WidomBox) * nbox));
+    b->wcap = nbox;
+  }
+  BCK(cudaMemcpyAsync(b->d_wbox, desc.data(), sizeof(WidomBox) * nbox, cudaMemcpyHostToDevice,
+                      b->main));
+  int cnt = 0;
+  Launch L{b->main, &cnt};
+  BCK(k_widom(L, b->d_wbox, nbox, ninsert, b->box[0]->precision != MG_MIXED));
+  b->launches = cnt;
+  const int nblk = widom_blocks(ninsert);
+  std::vector<double> part((size_t)nblk * nbox);
+  for (int i = 0; i < nbox; i++)
+    BCK(cudaMemcpyAsync(part.data() + (size_t)i * nblk, b->box[i]->d_wpart, sizeof(double) * nblk,
+                        cudaMemcpyDeviceToHost, b->main));
+  BCK(cudaStreamSynchronize(b->main));
+  for (int i = 0; i < nbox; i++)
+    widom_result(b->box[i], part.data() + (size_t)i * nblk, nblk, ninsert, T, corr[i], &out[i]);
+  return MG_OK;
+}

@@ -224,11 +224,18 @@ struct WidomArgs {
   double* U;           // [n] or null
   double* part;        // [nblocks]
 };
+// one box of a Widom launch (blockIdx.y): its arguments and data
+struct WidomBox {
+  WidomArgs a;
+  const int4* pj;       // mixed: sorted fixed-point sites
+  const double4* pd;    // FP64: sorted sites
+  const PairF* tabf;    // [nps*nkind] ghost-site x site-kind constants
+  const PairD* tabd;
+  const float4* eru;    // erfc energy spline (mixed)
+  const double* ert;    // erfc splines (FP64)
+};
 int widom_blocks(long long n);
-cudaError_t k_widom_mixed(const Launch& L, const WidomArgs& a, const int4* pj, const PairF* tab,
-                          const float4* eru);
-cudaError_t k_widom_fp64(const Launch& L, const WidomArgs& a, const double4* pd, const PairD* tab,
-                         const double* ert);
+cudaError_t k_widom(const Launch& L, const WidomBox* boxes, int nbox, long long n, bool fp64);
 
 cudaError_t k_drude_take(const Launch& L, const DrudeArgs& a, const double* r, double* out);
 cudaError_t k_drude_put(const Launch& L, const DrudeArgs& a, const double* in, double* r);

@@ -876,7 +876,7 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
           p[3 * ij.y + 2] -= mj * rz;
         }
       } while (maxsq > a.eps && it < a.maxit);
-      if (maxsq > a.eps) atomicExch(a.status, 1);
+      if (maxsq > a.eps) atomicOr(a.status, 1);
     }
     for (int i = i0; i < i1; i++) {
       double v1s = 0, v2s = 0;

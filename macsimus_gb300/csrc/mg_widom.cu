@@ -9,7 +9,9 @@
 // list the same way), and lane 0 adds exp(-U/T) (skipped when -U/T <= -700,
 // sim/simmeas.c:1934) to the warp's sum.  Lanes take stencil cells (or, for
 // grids of few cells, the sites of one cell).  Sums per CTA in FP64, in a
-// fixed order, so the result does not depend on scheduling.
+// fixed order, so the result does not depend on scheduling.  blockIdx.y
+// selects the box: one launch serves a whole batch of boxes, each with its
+// own cell list, pair table and ghost.
 #include "mg_internal.h"
 
 namespace mg {
@@ -68,11 +70,13 @@ __device__ __forceinline__ void wd_block_sum(double wacc, double* part) {
 }
 
 // mixed path: fixed-point ghost sites, FP32 pair energies, FP64 sums per cell
-__global__ void __launch_bounds__(WD_THREADS)
-    widom_mixed_kernel(WidomArgs a, const int4* __restrict__ pj, const PairF* __restrict__ tab_g,
-                       const float4* __restrict__ eru) {
+__global__ void __launch_bounds__(WD_THREADS) widom_mixed_kernel(const WidomBox* __restrict__ boxes) {
   __shared__ PairF tab[MAX_WPROBE * MAX_KINDS];
-  for (int t = threadIdx.x; t < a.nps * a.nkind; t += WD_THREADS) tab[t] = tab_g[t];
+  const WidomBox& B = boxes[blockIdx.y];
+  const WidomArgs a = B.a;
+  const int4* __restrict__ pj = B.pj;
+  const float4* __restrict__ eru = B.eru;
+  for (int t = threadIdx.x; t < a.nps * a.nkind; t += WD_THREADS) tab[t] = B.tabf[t];
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const long long nw = (long long)gridDim.x * WD_WARPS;
@@ -140,11 +144,13 @@ __global__ void __launch_bounds__(WD_THREADS)
 }
 
 // FP64 path: the same in double, nearest image by rint
-__global__ void __launch_bounds__(WD_THREADS)
-    widom_fp64_kernel(WidomArgs a, const double4* __restrict__ pd, const PairD* __restrict__ tab_g,
-                      const double* __restrict__ ert) {
+__global__ void __launch_bounds__(WD_THREADS) widom_fp64_kernel(const WidomBox* __restrict__ boxes) {
   __shared__ PairD tab[MAX_WPROBE * MAX_KINDS];
-  for (int t = threadIdx.x; t < a.nps * a.nkind; t += WD_THREADS) tab[t] = tab_g[t];
+  const WidomBox& B = boxes[blockIdx.y];
+  const WidomArgs a = B.a;
+  const double4* __restrict__ pd = B.pd;
+  const double* __restrict__ ert = B.ert;
+  for (int t = threadIdx.x; t < a.nps * a.nkind; t += WD_THREADS) tab[t] = B.tabd[t];
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const long long nw = (long long)gridDim.x * WD_WARPS;
@@ -213,16 +219,12 @@ int widom_blocks(long long n) {
   return (int)(b < 152 * 8 ? (b > 0 ? b : 1) : 152 * 8);
 }
 
-cudaError_t k_widom_mixed(const Launch& L, const WidomArgs& a, const int4* pj, const PairF* tab,
-                          const float4* eru) {
-  widom_mixed_kernel<<<widom_blocks(a.n), WD_THREADS, 0, L.s>>>(a, pj, tab, eru);
-  ++*L.counter;
-  return cudaGetLastError();
-}
-
-cudaError_t k_widom_fp64(const Launch& L, const WidomArgs& a, const double4* pd, const PairD* tab,
-                         const double* ert) {
-  widom_fp64_kernel<<<widom_blocks(a.n), WD_THREADS, 0, L.s>>>(a, pd, tab, ert);
+cudaError_t k_widom(const Launch& L, const WidomBox* boxes, int nbox, long long n, bool fp64) {
+  const dim3 grid(widom_blocks(n), nbox);
+  if (fp64)
+    widom_fp64_kernel<<<grid, WD_THREADS, 0, L.s>>>(boxes);
+  else
+    widom_mixed_kernel<<<grid, WD_THREADS, 0, L.s>>>(boxes);
   ++*L.counter;
   return cudaGetLastError();
 }

@@ -241,3 +241,22 @@ def ble_text(species_names):
         lines += ["", "angles", "", "dihedrals", "", "impropers", "", "aromatics", "",
                   "dependants", "", ""]
     return "\n".join(lines) + "\n\n"
+
+
+def ionic_system(n, sig_p, eps_p, sig_m, eps_m, probe=(3.2, 0.65), masses=(22.9898, 35.453, 39.948)):
+    """n/2 cations (+1 e) and n/2 anions (-1 e), LJ spheres (sigma A, epsilon
+    kJ/mol), each its own molecule; the type table has a third type, the LJ
+    ghost (probe = (sigma, epsilon)) used by Widom insertions, with no site"""
+    if n % 2:
+        raise ValueError("an equimolar ionic box needs an even number of ions")
+    types = [(masses[0], eps_p, sig_p), (masses[1], eps_m, sig_m), (masses[2], probe[1], probe[0])]
+    E = np.array([EUNIT_KCAL * _g12(-e / KJ_PER_KCAL) for _, e, _ in types])
+    R = np.array([_g12(rvdw_of_sigma(sg)) for _, _, sg in types])
+    typ = np.array([0] * (n // 2) + [1] * (n // 2), np.int32)
+    q = np.where(typ == 0, ELECTRON, -ELECTRON).astype(np.float64)
+    mass = np.array([float("%.6f" % types[t][0]) / MUNIT for t in typ])
+    return System(type=typ, q=q, mass=mass, mol=np.arange(n, dtype=np.int32),
+                  mol_first=np.arange(n + 1, dtype=np.int32), cons=np.zeros((0, 2), np.int32),
+                  cons_len=np.zeros(0), mol_cfirst=np.zeros(n + 1, np.int32), typeE=E, typeR=R,
+                  typeA=np.zeros(3), comb_rule=1, species=["ion+", "ion-"],
+                  counts=[n // 2, n // 2])

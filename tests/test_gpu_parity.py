@@ -22,7 +22,7 @@ def make(case, precision, **kw):
     g, meta, system, ew = load(case)
     fp = M.ForcePath(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"],
                      precision=precision, h=meta["params"]["h"], epsc=meta["params"]["epsc"],
-                     omegac=meta["omegac"], **kw)
+                     omegac=meta["omegac"] or 1.2, **kw)
     return g, meta, system, ew, fp
 
 
@@ -159,7 +159,7 @@ def test_md_with_lists_matches_md_with_cells(precision):
     re-binning at every step"""
     g, meta, system, ew = load("spce216")
     kw = dict(precision=precision, h=meta["params"]["h"], epsc=meta["params"]["epsc"],
-              omegac=meta["omegac"])
+              omegac=meta["omegac"] or 1.2)
     args = (system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
     out = []
     for skin in (1.5, -1):
