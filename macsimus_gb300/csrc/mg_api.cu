@@ -413,12 +413,18 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   for (int r0 = 0; r0 < (int)krows.size(); r0 += KTR) {
     int n = std::min(KTR, (int)krows.size() - r0), R = 0;
     for (int i = r0; i < r0 + n; i++) R = std::max(R, extent(krows[i]));
-    for (int kz0 = -R; kz0 <= R; kz0 += 16) p1job.push_back(make_int2((int)tiles.size(), kz0));
+    // pass-1 jobs: |kz| chunks of KZC_MIXED over [0, R] (FP32 kernel, both
+    // signs at once) or kz chunks of 16 over [-R, R] (FP64 kernel)
+    if (ctx->precision == MG_MIXED)
+      for (int kz0 = 0; kz0 <= R; kz0 += KZC_MIXED) p1job.push_back(make_int2((int)tiles.size(), kz0));
+    else
+      for (int kz0 = -R; kz0 <= R; kz0 += 16) p1job.push_back(make_int2((int)tiles.size(), kz0));
     tiles.push_back(KTile{r0, n, R, 0});
   }
   ctx->ntile = (int)tiles.size();
   ctx->np1job = (int)p1job.size();
-  ctx->row = (ctx->Kx + 1) + (2 * ctx->Ky + 1) + (2 * ctx->Kz + 1);
+  ctx->row = ctx->precision == MG_MIXED ? phase_row_mixed(ctx->Kx, ctx->Ky, ctx->Kz)
+                                         : (ctx->Kx + 1) + (2 * ctx->Ky + 1) + (2 * ctx->Kz + 1);
 
   // ---- charges of the Ewald sums: centres, then the site's Drude charge
   std::vector<int> qsite, qdrude, dsite;
@@ -443,9 +449,11 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   ctx->nq = (int)qsite.size();
   ctx->nd = (int)dsite.size();
   ctx->ndblocks = (ctx->nd + 127) / 128;
-  // charge chunks of pass 1: about 8 CTAs per SM, at least 64 charges each
+  // charge chunks of pass 1: about 8 (FP64 kernel) or 6 (FP32 kernel) CTAs
+  // per SM, at least 64 charges each
+  const int p1ctas = (ctx->precision == MG_MIXED ? 16 : 8) * 152;
   ctx->nchunk = std::max(1, std::min(std::max(1, ctx->nq / 64),
-                                     (8 * 152 + ctx->np1job - 1) / ctx->np1job));
+                                     (p1ctas + ctx->np1job - 1) / ctx->np1job));
   ctx->nkblocks = (nk + 255) / 256;
 
   // ---- constraints

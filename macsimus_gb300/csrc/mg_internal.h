@@ -59,6 +59,11 @@ struct KTile {
   int row0, nrows, R, pad;
 };
 constexpr int KTR = 64;         // rows per k-space tile
+// FP32 path: phase rows [X(0..Kx) | Y(-Ky..Ky) | Z(0..Kz)] (Z(-kz) is the
+// conjugate of Z(kz), so one product serves +kz and -kz); pass-1 jobs cover
+// kz in [kz0, kz0+KZC_MIXED) of [0, R]
+constexpr int KZC_MIXED = 32;
+inline int phase_row_mixed(int Kx, int Ky, int Kz) { return (Kx + 1) + (2 * Ky + 1) + (Kz + 1); }
 
 constexpr int KZT = 4;          // kz per pass-1 thread
 constexpr int PAIR_THREADS = 128;

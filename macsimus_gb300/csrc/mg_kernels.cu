@@ -545,7 +545,7 @@ __global__ void phase_tables_mixed_kernel(KArgs a, const double* __restrict__ r,
   int d, n;
   if (e <= a.Kx) { d = 0; n = e; }
   else if (e <= a.Kx + 2 * a.Ky + 1) { d = 1; n = e - (a.Kx + 1) - a.Ky; }
-  else { d = 2; n = e - (a.Kx + 2 * a.Ky + 2) - a.Kz; }
+  else { d = 2; n = e - (a.Kx + 2 * a.Ky + 2); }   // Z(0..Kz) only
   double Lb = d == 0 ? a.Lx : (d == 1 ? a.Ly : a.Lz);
   // exact integer phase n*s mod 1 in units of 2^-32
   double xd = r[3 * site + d];

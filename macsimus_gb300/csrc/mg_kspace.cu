@@ -142,8 +142,175 @@ static cudaError_t launch_sk_gemm(const Launch& L, const KArgs& a, const T2* tab
   return cudaGetLastError();
 }
 
+// ---------------------------------------------- pass 1, FP32 pipelined --
+//
+// Z(-kz) = conj(Z(kz)), so with A = X(kx) Y(ky) = (ax, ay) and Z(kz) = (c, s)
+//   S(row, kz) = sum (ax c - ay s, ax s + ay c),  S(row,-kz) = sum (ax c + ay s, ay c - ax s)
+// share the four sums P = (sum ax c, sum ax s), Q = (sum ay s, sum ay c):
+// two FFMA2 per (row, |kz|) give both signs.  CTA = (tile, |kz| chunk of
+// <= 32) x charge chunk; thread (tr, tz) holds rows tr+16i (i<4) x
+// |kz| = kz0+tz+8m (m < MZ <= 4).  The A products staged for a block of 16
+// charges serve every kz of the tile; the phase values of the next block
+// stream into shared memory with cp.async while the current one is
+// multiplied (two buffers).  Each thread stages one fixed row rr = tid&63
+// (and one fixed kz slot) for charges (tid>>6)+2u, so its gather offsets are
+// constants.
+
+constexpr int Q1_THREADS = 128;
+constexpr int Q1_KC = 16;
+constexpr int Q1_NZ = KZC_MIXED;
+
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem, bool valid) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  const int n = valid ? 8 : 0;  // 0: nothing is read, the 8 bytes are zero-filled
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa), "l"(gmem), "r"(n)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+struct SkSmem {
+  float2 X[2][Q1_KC][KTR];
+  float2 Y[2][Q1_KC][KTR];
+  float2 Z[2][Q1_KC][Q1_NZ];
+};
+
+// the multiply loop of one stage for MZ kz groups (no per-group branches, so
+// the compiler interleaves all 4 x MZ accumulator chains)
+template <int MZ>
+__device__ __forceinline__ void sk_stage_mac(const float2 (*X)[KTR], const float2 (*Z)[Q1_NZ],
+                                             int tr, int tz, float2 (&P)[4][4],
+                                             float2 (&Q)[4][4]) {
+#pragma unroll 2
+  for (int jj = 0; jj < Q1_KC; jj++) {
+    float2 ax[4], ay[4], zv[MZ], zs[MZ];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const float2 v = X[jj][tr + 16 * i];
+      ax[i] = make_float2(v.x, v.x);
+      ay[i] = make_float2(v.y, v.y);
+    }
+#pragma unroll
+    for (int m = 0; m < MZ; m++) {
+      zv[m] = Z[jj][tz + 8 * m];
+      zs[m] = make_float2(zv[m].y, zv[m].x);
+    }
+#pragma unroll
+    for (int m = 0; m < MZ; m++)
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        P[i][m] = __ffma2_rn(ax[i], zv[m], P[i][m]);
+        Q[i][m] = __ffma2_rn(ay[i], zs[m], Q[i][m]);
+      }
+  }
+}
+
+template <int MZ>
+__device__ __forceinline__ void sk_gemm_mixed_body(const KArgs& a, const float2* __restrict__ tab,
+                                                   float2* __restrict__ part, const KTile& tile,
+                                                   int kz0, int nz, SkSmem& sm) {
+  auto& Xs = sm.X;
+  auto& Ys = sm.Y;
+  auto& Zs = sm.Z;
+  const int ch = blockIdx.y;
+  const int j0 = (int)((long)a.nq * ch / a.nchunk), j1 = (int)((long)a.nq * (ch + 1) / a.nchunk);
+  const int tid = threadIdx.x, tr = tid >> 3, tz = tid & 7;
+  const int oy = a.Kx + 1 + a.Ky, oz = a.Kx + 2 * a.Ky + 2;
+  // this thread's staging slots: row rr for charges jb + 2u; kz slot zz for
+  // charges zb + 4u
+  const int rr = tid & (KTR - 1), jb = tid >> 6;
+  const int zz = tid & (Q1_NZ - 1), zb = tid / Q1_NZ;
+  const bool vr = rr < tile.nrows, vz = zz < nz;
+  const KRow myrow = vr ? a.krows[tile.row0 + rr] : KRow{0, 0, 1, 0, 0, 0, 0, 0};
+  const int xoff = myrow.kx, yoff = oy + myrow.ky, zoff = oz + kz0 + zz;
+  const int nstage = (j1 - j0 + Q1_KC - 1) / Q1_KC;
+  auto issue = [&](int st, int buf) {
+    const int js = j0 + st * Q1_KC;
+#pragma unroll
+    for (int u = 0; u < Q1_KC / 2; u++) {
+      const int jj = jb + 2 * u;
+      const bool vj = js + jj < j1;
+      const float2* base = vj ? tab + (long)(js + jj) * a.row : tab;
+      cp_async8(&Xs[buf][jj][rr], base + (vj && vr ? xoff : 0), vj && vr);
+      cp_async8(&Ys[buf][jj][rr], base + (vj && vr ? yoff : 0), vj && vr);
+    }
+#pragma unroll
+    for (int u = 0; u < Q1_KC * Q1_NZ / Q1_THREADS; u++) {
+      const int jj = zb + (Q1_THREADS / Q1_NZ) * u;
+      const bool vj = js + jj < j1;
+      const float2* base = vj ? tab + (long)(js + jj) * a.row : tab;
+      cp_async8(&Zs[buf][jj][zz], base + (vj && vz ? zoff : 0), vj && vz);
+    }
+    cp_async_commit();
+  };
+  float2 P[4][4], Q[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int m = 0; m < 4; m++) P[i][m] = Q[i][m] = make_float2(0.f, 0.f);
+  if (nstage > 0) issue(0, 0);
+  for (int st = 0; st < nstage; st++) {
+    const int buf = st & 1;
+    if (st + 1 < nstage) {
+      issue(st + 1, buf ^ 1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    // A = X Y for the entries this thread staged (its own copies are complete)
+#pragma unroll
+    for (int u = 0; u < Q1_KC / 2; u++) {
+      const int jj = jb + 2 * u;
+      const float2 x = Xs[buf][jj][rr], y = Ys[buf][jj][rr];
+      Xs[buf][jj][rr] = make_float2(x.x * y.x - x.y * y.y, x.x * y.y + x.y * y.x);
+    }
+    __syncthreads();
+    sk_stage_mac<MZ>(Xs[buf], Zs[buf], tr, tz, P, Q);
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const int r = tr + 16 * i;
+    if (r >= tile.nrows) continue;
+    const KRow rw = a.krows[tile.row0 + r];
+#pragma unroll
+    for (int m = 0; m < MZ; m++) {
+      const int kz = kz0 + tz + 8 * m;
+      if (tz + 8 * m >= nz) continue;
+      const float2 p = P[i][m], q = Q[i][m];
+      if (kz >= rw.kzlo && kz <= rw.kzhi)
+        part[(long)ch * a.nk + rw.kstart + (kz - rw.kzlo)] = make_float2(p.x - q.x, p.y + q.y);
+      if (kz > 0 && -kz >= rw.kzlo && -kz <= rw.kzhi)
+        part[(long)ch * a.nk + rw.kstart + (-kz - rw.kzlo)] = make_float2(p.x + q.x, q.y - p.y);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(Q1_THREADS)
+    sk_gemm_mixed_kernel(KArgs a, const float2* __restrict__ tab, float2* __restrict__ part) {
+  __shared__ __align__(16) SkSmem sm;
+  const int2 job = a.p1job[blockIdx.x];
+  const KTile tile = a.tiles[job.x];
+  const int kz0 = job.y;
+  const int nz = min(Q1_NZ, tile.R - kz0 + 1);
+  switch ((nz + 7) >> 3) {
+    case 1: sk_gemm_mixed_body<1>(a, tab, part, tile, kz0, nz, sm); break;
+    case 2: sk_gemm_mixed_body<2>(a, tab, part, tile, kz0, nz, sm); break;
+    case 3: sk_gemm_mixed_body<3>(a, tab, part, tile, kz0, nz, sm); break;
+    default: sk_gemm_mixed_body<4>(a, tab, part, tile, kz0, nz, sm); break;
+  }
+}
+
 cudaError_t k_sk_gemm_mixed(const Launch& L, const KArgs& a, const float2* tab, float2* part) {
-  return launch_sk_gemm<float2>(L, a, tab, part);
+  dim3 grid(a.np1job, a.nchunk);
+  sk_gemm_mixed_kernel<<<grid, Q1_THREADS, 0, L.s>>>(a, tab, part);
+  ++*L.counter;
+  return cudaGetLastError();
 }
 cudaError_t k_sk_gemm_fp64(const Launch& L, const KArgs& a, const double2* tab, double2* part) {
   return launch_sk_gemm<double2>(L, a, tab, part);
@@ -284,8 +451,159 @@ static cudaError_t launch_kf_gemm(const Launch& L, const KArgs& a, const T2* tab
   return cudaGetLastError();
 }
 
+// ---------------------------------------------- pass 2, FP32 pipelined --
+//
+// CTA = 32 charges; thread (tj, tw) = (warp, lane): charges 4tj..4tj+3,
+// rows tw and tw+32 of the current tile.  With W+- = W(row, +-kz),
+// P = W+ + W-, M = W+ - W- and Z(kz) = (c, s):
+//   H  = W(row,0) + sum_{kz>0} (P.x c - M.y s,  M.x s + P.y c)
+//   Hz =            sum_{kz>0} kz (M.x c - P.y s,  P.x s + M.y c)
+// (Z(-kz) = conj Z(kz)): four FFMA2 per (charge, row, |kz|).  Z(0..Kz) and the
+// X|Y phase values of the CTA's charges stay in shared memory for the whole
+// kernel (the epilogue's A = X(kx) Y(ky) products read them there); W of the
+// next tile streams in with cp.async while the current tile is multiplied.
+// A warp owns whole charges, so the sum over its 32 row slots is a shuffle
+// reduction.
+
+constexpr int Q2_THREADS = 256;
+constexpr int Q2_NJ = 32;
+
+size_t kf_mixed_smem(const KArgs& a) {
+  const int nz = a.Kz + 1, nw = 2 * a.Kz + 1, nxy = a.Kx + 1 + 2 * a.Ky + 1;
+  return sizeof(float2) * ((size_t)nz * Q2_NJ + (size_t)Q2_NJ * nxy + 2 * (size_t)nw * KTR);
+}
+
+__global__ void __launch_bounds__(Q2_THREADS, 2)
+    kf_gemm_mixed_kernel(KArgs a, const float2* __restrict__ tab, const float2* __restrict__ W) {
+  extern __shared__ __align__(16) unsigned char smem_kf[];
+  const int nz = a.Kz + 1, nw = 2 * a.Kz + 1, nxy = a.Kx + 1 + 2 * a.Ky + 1;
+  float2* Zs = reinterpret_cast<float2*>(smem_kf);  // [nz][Q2_NJ]: Z(0..Kz)
+  float2* XYs = Zs + (size_t)nz * Q2_NJ;            // [Q2_NJ][nxy]
+  float2* Ws = XYs + (size_t)Q2_NJ * nxy;           // [2][nw][KTR]: W(kz = z - R)
+  const int tid = threadIdx.x, tw = tid & 31, tj = tid >> 5;
+  const int jbase = blockIdx.x * Q2_NJ;
+  const int oz = a.Kx + 2 * a.Ky + 2, oyl = a.Kx + 1 + a.Ky;
+  for (int t = tid; t < nz * Q2_NJ; t += Q2_THREADS) {
+    const int z = t / Q2_NJ, c = t % Q2_NJ, j = jbase + c;
+    Zs[t] = j < a.nq ? tab[(long)j * a.row + oz + z] : make_float2(0.f, 0.f);
+  }
+  for (int t = tid; t < Q2_NJ * nxy; t += Q2_THREADS) {
+    const int c = t / nxy, e = t % nxy, j = jbase + c;
+    XYs[t] = j < a.nq ? tab[(long)j * a.row + e] : make_float2(0.f, 0.f);
+  }
+  // W staging: this thread copies row wr = tid&63, kz slots (tid>>6)+4u
+  const int wr = tid & (KTR - 1), wz = tid >> 6;
+  auto issue = [&](int ti, int buf) {
+    const KTile tl = a.tiles[ti];
+    const KRow rw = wr < tl.nrows ? a.krows[tl.row0 + wr] : KRow{0, 0, 1, 0, 0, 0, 0, 0};
+    float2* dst = Ws + (size_t)buf * nw * KTR;
+    for (int z = wz; z < 2 * tl.R + 1; z += Q2_THREADS / KTR) {
+      const int kz = z - tl.R;
+      const bool v = kz >= rw.kzlo && kz <= rw.kzhi;
+      cp_async8(dst + z * KTR + wr, v ? W + rw.kstart + (kz - rw.kzlo) : W, v);
+    }
+    cp_async_commit();
+  };
+  float F[4][3], Fc[4][3];
+#pragma unroll
+  for (int c = 0; c < 4; c++)
+#pragma unroll
+    for (int d = 0; d < 3; d++) F[c][d] = Fc[c][d] = 0.f;
+  if (a.ntile > 0) issue(0, 0);
+  for (int ti = 0; ti < a.ntile; ti++) {
+    const int buf = ti & 1;
+    if (ti + 1 < a.ntile) {
+      issue(ti + 1, buf ^ 1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    const KTile tile = a.tiles[ti];
+    const int R = tile.R;
+    const float2* W0 = Ws + (size_t)buf * nw * KTR + (size_t)R * KTR;  // kz = 0
+    float2 H[4][2], Hz[4][2];
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+      const float2 w0 = W0[tw + 32 * i];
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        H[c][i] = w0;
+        Hz[c][i] = make_float2(0.f, 0.f);
+      }
+    }
+    float kz = 1.f;
+    for (int z = 1; z <= R; z++, kz += 1.f) {
+      const float4* zp = reinterpret_cast<const float4*>(Zs + (size_t)z * Q2_NJ + 4 * tj);
+      const float4 z01 = zp[0], z23 = zp[1];
+      const float2 zv[4] = {make_float2(z01.x, z01.y), make_float2(z01.z, z01.w),
+                            make_float2(z23.x, z23.y), make_float2(z23.z, z23.w)};
+#pragma unroll
+      for (int i = 0; i < 2; i++) {
+        const float2 wp = W0[z * KTR + tw + 32 * i], wm = W0[-z * KTR + tw + 32 * i];
+        const float Px = wp.x + wm.x, Py = wp.y + wm.y, Mx = wp.x - wm.x, My = wp.y - wm.y;
+        const float2 h1 = make_float2(Px, Mx), h2 = make_float2(-My, Py);
+        const float2 g1 = make_float2(kz * Mx, kz * Px), g2 = make_float2(-kz * Py, kz * My);
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const float2 zs = make_float2(zv[c].y, zv[c].x);
+          H[c][i] = __ffma2_rn(h1, zv[c], H[c][i]);
+          H[c][i] = __ffma2_rn(h2, zs, H[c][i]);
+          Hz[c][i] = __ffma2_rn(g1, zv[c], Hz[c][i]);
+          Hz[c][i] = __ffma2_rn(g2, zs, Hz[c][i]);
+        }
+      }
+    }
+    // epilogue: A_j(row) = X(kx) Y(ky) from shared memory, Im(A H) weighted by k
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+      const int r = tw + 32 * i;
+      if (r >= tile.nrows) continue;
+      const KRow rw = a.krows[tile.row0 + r];
+      const float kxf = (float)rw.kx, kyf = (float)rw.ky;
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const float2* xy = XYs + (size_t)(4 * tj + c) * nxy;
+        const float2 X = xy[rw.kx], Y = xy[oyl + rw.ky];
+        const float2 A = make_float2(X.x * Y.x - X.y * Y.y, X.x * Y.y + X.y * Y.x);
+        const float g = A.x * H[c][i].y + A.y * H[c][i].x;
+        kahan_add(F[c][0], Fc[c][0], kxf * g);
+        kahan_add(F[c][1], Fc[c][1], kyf * g);
+        kahan_add(F[c][2], Fc[c][2], A.x * Hz[c][i].y + A.y * Hz[c][i].x);
+      }
+    }
+    __syncthreads();
+  }
+  // sum over the 32 row slots of the warp (FP64), lane 0 stores
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    double s[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      double v = (double)F[c][d] + (double)Fc[c][d];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      s[d] = v;
+    }
+    const int j = jbase + 4 * tj + c;
+    if (tw == 0 && j < a.nq) {
+      const int site = a.qsite[j];
+      double* fo = a.f + 3 * (long)site + (a.qdrude && a.qdrude[j] ? 3 * (long)a.ns : 0);
+      fo[0] += s[0] / a.Lx;
+      fo[1] += s[1] / a.Ly;
+      fo[2] += s[2] / a.Lz;
+    }
+  }
+}
+
 cudaError_t k_kf_gemm_mixed(const Launch& L, const KArgs& a, const float2* tab) {
-  return launch_kf_gemm<float2>(L, a, tab, a.Wf);
+  const size_t smem = kf_mixed_smem(a);
+  cudaError_t e = cudaFuncSetAttribute(kf_gemm_mixed_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  kf_gemm_mixed_kernel<<<(a.nq + Q2_NJ - 1) / Q2_NJ, Q2_THREADS, smem, L.s>>>(a, tab, a.Wf);
+  ++*L.counter;
+  return cudaGetLastError();
 }
 cudaError_t k_kf_gemm_fp64(const Launch& L, const KArgs& a, const double2* tab) {
   return launch_kf_gemm<double2>(L, a, tab, a.Wd);

@@ -178,7 +178,7 @@ extern "C" int mg_ewald_kspace_noalloc(const double* r_dev, const double* q_dev,
     Ky = std::max(Ky, std::abs(h_kvec[i].y));
     Kz = std::max(Kz, std::abs(h_kvec[i].z));
   }
-  const int rowlen = (Kx + 1) + (2 * Ky + 1) + (2 * Kz + 1);
+  const int rowlen = phase_row_mixed(Kx, Ky, Kz);
   if (rowlen > MAXROW)
     return fail_na(MG_ERR_SIZE, "mg_ewald_kspace_noalloc: phase row longer than MG_NOALLOC_MAX_ROW");
   int nrows = 0;
@@ -198,7 +198,7 @@ extern "C" int mg_ewald_kspace_noalloc(const double* r_dev, const double* q_dev,
     const int n = std::min(KTR, nrows - r0);
     int R = 0;
     for (int i = r0; i < r0 + n; i++) R = std::max(R, ext(h_rows[i]));
-    for (int kz0 = -R; kz0 <= R; kz0 += 16) {
+    for (int kz0 = 0; kz0 <= R; kz0 += KZC_MIXED) {
       if (njob >= MAXJOB) return fail_na(MG_ERR_SIZE, "mg_ewald_kspace_noalloc: k tiling too large");
       h_jobs[njob++] = make_int2(ntile, kz0);
     }
