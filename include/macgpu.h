@@ -187,7 +187,7 @@ int mg_probe_fp32_tflops(double *tflops);
    all device memory out from its own fixed pool, or a time-critical loop that
    cannot afford cudaMalloc/cudaFree and the device-wide synchronization they
    can imply -- this variant keeps all of its scratch in a fixed array inside
-   the library: every GPU that loads the library holds it (about 4.4 MB) until
+   the library: every GPU that loads the library holds it (about 4.6 MB) until
    the process exits.  Inputs and outputs stay the caller's: r_dev [3*nq]
    charge positions and q_dev [nq] charges (device), f_dev [3*nq] forces
    (device, overwritten), *energy (host: k-space + self term, may be NULL);

@@ -58,6 +58,7 @@ struct mg_ctx {
   float2* d_Wf = nullptr;
   double2* d_Wd = nullptr;
   void* d_tab = nullptr;   // float2 or double2 rows
+  uint4* d_qfix = nullptr; // FP32 path: fixed-point coordinates of the charges
   void* d_part = nullptr;  // float2 or double2 partials
   double* d_ekpart = nullptr;
   int nkblocks = 0;
@@ -451,7 +452,7 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   ctx->ndblocks = (ctx->nd + 127) / 128;
   // charge chunks of pass 1: about 8 (FP64 kernel) or 6 (FP32 kernel) CTAs
   // per SM, at least 64 charges each
-  const int p1ctas = (ctx->precision == MG_MIXED ? 16 : 8) * 152;
+  const int p1ctas = (ctx->precision == MG_MIXED ? 10 : 8) * 152;
   ctx->nchunk = std::max(1, std::min(std::max(1, ctx->nq / 64),
                                      (p1ctas + ctx->np1job - 1) / ctx->np1job));
   ctx->nkblocks = (nk + 255) / 256;
@@ -547,6 +548,7 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
     CK(upload(&ctx->d_erd, erd.data(), ntab));
     CK(upload(&ctx->d_eru, eru.data(), ntab));
     CK(dalloc((float2**)&ctx->d_tab, (size_t)ctx->nq * ctx->row));
+    CK(dalloc(&ctx->d_qfix, std::max(1, ctx->nq)));
     CK(dalloc((float2**)&ctx->d_part, (size_t)ctx->nchunk * nk));
     CK(dalloc(&ctx->d_Wf, nk));
   } else {
@@ -713,7 +715,7 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
                                       measure, ctx->polar));
     }
     if (ctx->nq > 0) {
-      PROF("phase_tables", k_phase_tables_mixed(L, ka, r_dev, (float2*)ctx->d_tab));
+      PROF("phase_tables", k_phase_tables_mixed(L, ka, r_dev, (float2*)ctx->d_tab, ctx->d_qfix));
       PROF("ewald_sk", k_sk_gemm_mixed(L, ka, (const float2*)ctx->d_tab, (float2*)ctx->d_part));
       PROF("ewald_sk_reduce", k_sk_reduce_mixed(L, ka, (const float2*)ctx->d_part, measure));
       PROF("ewald_kforce", k_kf_gemm_mixed(L, ka, (const float2*)ctx->d_tab));
@@ -897,7 +899,8 @@ int mg_destroy(mg_ctx* ctx) {
                   ctx->d_tiles, ctx->d_p1job, ctx->d_dsite, ctx->d_qdrude, ctx->d_qc,
                   ctx->d_qp, ctx->d_aqq, ctx->d_hist, ctx->d_drpart, ctx->d_pdj, ctx->d_pdd,
                   ctx->d_nlist, ctx->d_ncount, ctx->d_rbuild, ctx->d_dmax,
-                  ctx->d_wtabf, ctx->d_wtabd, ctx->d_wgeom, ctx->d_wpart, ctx->d_wbox};
+                  ctx->d_wtabf, ctx->d_wtabd, ctx->d_wgeom, ctx->d_wpart, ctx->d_wbox,
+                  ctx->d_qfix};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ctx->h_sums) cudaFreeHost(ctx->h_sums);
@@ -1004,7 +1007,7 @@ int mg_ewald(mg_ctx* ctx, const double* r, double* f, double* energy) {
   ka.ns = ctx->ns;
   if (ctx->nq > 0) {
     if (ctx->precision == MG_MIXED) {
-      CK(k_phase_tables_mixed(L, ka, ctx->d_rs, (float2*)ctx->d_tab));
+      CK(k_phase_tables_mixed(L, ka, ctx->d_rs, (float2*)ctx->d_tab, ctx->d_qfix));
       CK(k_sk_gemm_mixed(L, ka, (const float2*)ctx->d_tab, (float2*)ctx->d_part));
       CK(k_sk_reduce_mixed(L, ka, (const float2*)ctx->d_part, true));
       CK(k_kf_gemm_mixed(L, ka, (const float2*)ctx->d_tab));

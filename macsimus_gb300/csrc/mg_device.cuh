@@ -38,7 +38,10 @@ template <bool MEASURE>
 __device__ __forceinline__ float spline_term(const float4* __restrict__ erd,
                                              const float4* __restrict__ eru, float r2, float sgrid,
                                              int ntab, float qq, float& e) {
-  const int ix = min((int)(r2 * sgrid), ntab - 1);
+  // floor(r2 sgrid) without a float-to-int conversion: r2 sgrid - 1/2 rounded
+  // to an integer in the mantissa of 1.5 * 2^23 (0 <= r2 sgrid < 2^22; at an
+  // exact knot either neighbouring interval gives the same value)
+  const int ix = min(__float_as_int(fmaf(r2, sgrid, 12582911.5f)) - 0x4B400000, ntab - 1);
   const float4 d = __ldg(erd + ix);
   if (MEASURE) {
     const float4 u = __ldg(eru + ix);

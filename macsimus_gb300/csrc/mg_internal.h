@@ -136,7 +136,9 @@ struct KArgs {
   const int* qdrude;        // [nq] 1 if the charge is a Drude charge (or NULL)
   int ns;
 };
-cudaError_t k_phase_tables_mixed(const Launch& L, const KArgs& a, const double* r, float2* tab);
+// qf: [nq] scratch for the charges' fixed-point coordinates
+cudaError_t k_phase_tables_mixed(const Launch& L, const KArgs& a, const double* r, float2* tab,
+                                 uint4* qf);
 cudaError_t k_phase_tables_fp64(const Launch& L, const KArgs& a, const double* r, double2* tab);
 cudaError_t k_sk_mixed(const Launch& L, const KArgs& a, const float2* tab, float2* part);
 cudaError_t k_sk_fp64(const Launch& L, const KArgs& a, const double2* tab, double2* part);

@@ -140,7 +140,16 @@ constexpr int FOLD = 8;   // stencil cells per FP32 force batch before the FP64 
 // Full shell: forces only on the home site.  POLAR adds the Drude terms of
 // cook/ljqqpol.c (centre-Drude, Drude-centre, Drude-Drude, each at its own
 // separation); Drude forces go to the second half of f.
-template <bool MEASURE, bool POLAR>
+//
+// REL (every grid of at least 2 cdiv + 1 cells per edge): a staged site is
+// converted once, as the float offset of its nearest image from the centre
+// of the home cell (exact 32-bit fixed-point difference, then one rounding);
+// a pair then costs three subtractions and no int-to-float conversion
+// (conversions are slow on this GPU).  Every stencil cell lies within half a
+// box of the home-cell centre, so the image taken is the nearest one for
+// every pair inside the cutoff.  Without REL (one cell: all pairs) each pair
+// takes its nearest image from its own fixed-point difference.
+template <bool MEASURE, bool POLAR, bool REL>
 __global__ void __launch_bounds__(PAIR_THREADS)
     pair_mixed_kernel(PairArgs a, const int4* __restrict__ pj, const PairF* __restrict__ ptab_g,
                       const float4* __restrict__ erd, const float4* __restrict__ eru, float sx,
@@ -158,6 +167,10 @@ __global__ void __launch_bounds__(PAIR_THREADS)
   const int c = blockIdx.x;
   const int cz = c % a.ncz, cy = (c / a.ncz) % a.ncy, cx = c / (a.ncy * a.ncz);
   const int i0 = a.cell_start[c], ni = a.cell_start[c + 1] - i0;
+  // fixed-point centre of the home cell
+  const unsigned refx = (unsigned)((((unsigned long long)(2 * cx + 1)) << 31) / a.ncx),
+                 refy = (unsigned)((((unsigned long long)(2 * cy + 1)) << 31) / a.ncy),
+                 refz = (unsigned)((((unsigned long long)(2 * cz + 1)) << 31) / a.ncz);
   double en[NEN];
 #pragma unroll
   for (int k = 0; k < NEN; k++) en[k] = 0;
@@ -168,6 +181,9 @@ __global__ void __launch_bounds__(PAIR_THREADS)
     const int4 me = vi ? pj[ti] : make_int4(0, 0, 0, 0);
     const float4 md = (POLAR && vi) ? a.pdj[ti] : make_float4(0.f, 0.f, 0.f, 0.f);
     const int kind_i = me.w & 255, mol_i = me.w >> 8;
+    const float xi = (float)(int)((unsigned)me.x - refx) * sx,
+                yi = (float)(int)((unsigned)me.y - refy) * sy,
+                zi = (float)(int)((unsigned)me.z - refz) * sz;
     double fx = 0, fy = 0, fz = 0, gx = 0, gy = 0, gz = 0;
     float ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;
     float e_el = 0, e_lj = 0, e_vir = 0;
@@ -184,17 +200,33 @@ __global__ void __launch_bounds__(PAIR_THREADS)
       const int j0 = a.cell_start[c2], nj = a.cell_start[c2 + 1] - j0;
       for (int jb = 0; jb < nj; jb += 32) {
         if (jb + lane < nj) {
-          sj[warp][lane] = pj[j0 + jb + lane];
+          int4 q = pj[j0 + jb + lane];
+          if (REL) {
+            // offset of the neighbour's nearest image from the home-cell centre
+            const float4 f = make_float4((float)(int)((unsigned)q.x - refx) * sx,
+                                         (float)(int)((unsigned)q.y - refy) * sy,
+                                         (float)(int)((unsigned)q.z - refz) * sz,
+                                         __int_as_float(q.w));
+            q = make_int4(__float_as_int(f.x), __float_as_int(f.y), __float_as_int(f.z), q.w);
+          }
+          sj[warp][lane] = q;
           if (POLAR) sjd[warp][lane] = a.pdj[j0 + jb + lane];
         }
         __syncwarp();
         const int cnt = min(32, nj - jb);
         for (int jj = 0; jj < cnt; jj++) {
           const int4 q = sj[warp][jj];
-          // nearest image: 32-bit wrap-around of the fixed-point difference
-          const float dx = (float)(int)((unsigned)me.x - (unsigned)q.x) * sx;
-          const float dy = (float)(int)((unsigned)me.y - (unsigned)q.y) * sy;
-          const float dz = (float)(int)((unsigned)me.z - (unsigned)q.z) * sz;
+          float dx, dy, dz;
+          if (REL) {
+            dx = xi - __int_as_float(q.x);
+            dy = yi - __int_as_float(q.y);
+            dz = zi - __int_as_float(q.z);
+          } else {
+            // nearest image: 32-bit wrap-around of the fixed-point difference
+            dx = (float)(int)((unsigned)me.x - (unsigned)q.x) * sx;
+            dy = (float)(int)((unsigned)me.y - (unsigned)q.y) * sy;
+            dz = (float)(int)((unsigned)me.z - (unsigned)q.z) * sz;
+          }
           const float rr = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
           if (!vi || rr >= cq || j0 + jb + jj == ti) continue;
           const PairF P = ptab[kind_i * nk + (q.w & 255)];
@@ -217,7 +249,7 @@ __global__ void __launch_bounds__(PAIR_THREADS)
           if (rr < P.C2q) {
             float U;
             if (rr < P.C1q) {
-              const float x = P.Sq / rr, y = x * x * x;
+              const float x = __fdividef(P.Sq, rr), y = x * x * x;
               f = P.E24 * fmaf(2.f * y, y, -y) * x;
               U = P.E4 * fmaf(y, y, -y);
             } else {
@@ -335,21 +367,18 @@ cudaError_t k_pair_mixed(const Launch& L, const PairArgs& a, const int4* pj, con
   float sx = (float)(a.Lx / 4294967296.0), sy = (float)(a.Ly / 4294967296.0),
         sz = (float)(a.Lz / 4294967296.0);
   const float cq = (float)a.cutoff_sq, sg = (float)a.sgrid, al = (float)a.alpha;
+#define PAIR_MIXED(M, P, R)                                                                   \
+  pair_mixed_kernel<M, P, R><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pj, ptab, erd, eru, sx, sy, sz, \
+                                                              cq, sg, al)
+  const bool rel = !a.allpairs;
   if (polar) {
-    if (measure)
-      pair_mixed_kernel<true, true><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pj, ptab, erd, eru, sx,
-                                                                     sy, sz, cq, sg, al);
-    else
-      pair_mixed_kernel<false, true><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pj, ptab, erd, eru, sx,
-                                                                      sy, sz, cq, sg, al);
+    if (measure) { if (rel) PAIR_MIXED(true, true, true); else PAIR_MIXED(true, true, false); }
+    else { if (rel) PAIR_MIXED(false, true, true); else PAIR_MIXED(false, true, false); }
   } else {
-    if (measure)
-      pair_mixed_kernel<true, false><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pj, ptab, erd, eru, sx,
-                                                                      sy, sz, cq, sg, al);
-    else
-      pair_mixed_kernel<false, false><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pj, ptab, erd, eru, sx,
-                                                                       sy, sz, cq, sg, al);
+    if (measure) { if (rel) PAIR_MIXED(true, false, true); else PAIR_MIXED(true, false, false); }
+    else { if (rel) PAIR_MIXED(false, false, true); else PAIR_MIXED(false, false, false); }
   }
+#undef PAIR_MIXED
   LAUNCHED(L);
   return cudaGetLastError();
 }
@@ -536,21 +565,33 @@ cudaError_t k_gather_drude(const Launch& L, int ns, const double* r, const int* 
 
 // Row of charge j: [q e^{2 pi i kx sx}, kx=0..Kx | e^{2 pi i ky sy}, ky=-Ky..Ky |
 //                   e^{2 pi i kz sz}, kz=-Kz..Kz]
-__global__ void phase_tables_mixed_kernel(KArgs a, const double* __restrict__ r,
+// fixed-point coordinates of every charge (Drude charges at r + rpol)
+__global__ void charge_fixed_kernel(KArgs a, const double* __restrict__ r, uint4* __restrict__ qf) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.nq) return;
+  const int site = a.qsite[j];
+  double x = r[3 * site], y = r[3 * site + 1], z = r[3 * site + 2];
+  if (a.qdrude && a.qdrude[j]) {
+    x += r[3 * (long)a.ns + 3 * site];
+    y += r[3 * (long)a.ns + 3 * site + 1];
+    z += r[3 * (long)a.ns + 3 * site + 2];
+  }
+  qf[j] = make_uint4((unsigned)fixed32(x, a.Lx), (unsigned)fixed32(y, a.Ly),
+                     (unsigned)fixed32(z, a.Lz), 0u);
+}
+
+__global__ void phase_tables_mixed_kernel(KArgs a, const uint4* __restrict__ qf,
                                           float2* __restrict__ tab) {
   long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long)a.nq * a.row) return;
   int j = (int)(t / a.row), e = (int)(t % a.row);
-  int site = a.qsite[j];
   int d, n;
   if (e <= a.Kx) { d = 0; n = e; }
   else if (e <= a.Kx + 2 * a.Ky + 1) { d = 1; n = e - (a.Kx + 1) - a.Ky; }
   else { d = 2; n = e - (a.Kx + 2 * a.Ky + 2); }   // Z(0..Kz) only
-  double Lb = d == 0 ? a.Lx : (d == 1 ? a.Ly : a.Lz);
+  const uint4 S4 = qf[j];
+  const unsigned S = d == 0 ? S4.x : (d == 1 ? S4.y : S4.z);
   // exact integer phase n*s mod 1 in units of 2^-32
-  double xd = r[3 * site + d];
-  if (a.qdrude && a.qdrude[j]) xd += r[3 * (long)a.ns + 3 * site + d];
-  unsigned int S = (unsigned int)fixed32(xd, Lb);
   int ph = (int)(S * (unsigned int)n);
   float tt = (float)ph * 2.3283064365386963e-10f;   // in [-0.5, 0.5)
   float sn, cs;
@@ -588,9 +629,12 @@ __global__ void phase_tables_fp64_kernel(KArgs a, const double* __restrict__ r,
   tab[t] = make_double2(cs, sn);
 }
 
-cudaError_t k_phase_tables_mixed(const Launch& L, const KArgs& a, const double* r, float2* tab) {
+cudaError_t k_phase_tables_mixed(const Launch& L, const KArgs& a, const double* r, float2* tab,
+                                 uint4* qf) {
+  charge_fixed_kernel<<<cdiv(a.nq, 256), 256, 0, L.s>>>(a, r, qf);
+  LAUNCHED(L);
   long n = (long)a.nq * a.row;
-  phase_tables_mixed_kernel<<<(int)((n + 255) / 256), 256, 0, L.s>>>(a, r, tab);
+  phase_tables_mixed_kernel<<<(int)((n + 255) / 256), 256, 0, L.s>>>(a, qf, tab);
   LAUNCHED(L);
   return cudaGetLastError();
 }

@@ -48,7 +48,8 @@ constexpr size_t OFF_JOBS = OFF_TILES + al(sizeof(KTile) * MAXTILE);
 constexpr size_t OFF_QSITE = OFF_JOBS + al(sizeof(int2) * MAXJOB);
 constexpr size_t OFF_EKPART = OFF_QSITE + al(sizeof(int) * MAXQ);
 constexpr size_t OFF_SUMS = OFF_EKPART + al(sizeof(double) * 7 * MAXKB);
-constexpr size_t SCRATCH_BYTES = OFF_SUMS + al(sizeof(double) * 32);
+constexpr size_t OFF_QFIX = OFF_SUMS + al(sizeof(double) * 32);
+constexpr size_t SCRATCH_BYTES = OFF_QFIX + al(sizeof(uint4) * MAXQ);
 
 }  // namespace
 
@@ -220,6 +221,7 @@ extern "C" int mg_ewald_kspace_noalloc(const double* r_dev, const double* q_dev,
   int* qsite = (int*)(base + OFF_QSITE);
   double* ekpart = (double*)(base + OFF_EKPART);
   double* sums = (double*)(base + OFF_SUMS);
+  uint4* qfix = (uint4*)(base + OFF_QFIX);
 
 #define NA_CK(call)                                                     \
   do {                                                                  \
@@ -267,7 +269,7 @@ extern "C" int mg_ewald_kspace_noalloc(const double* r_dev, const double* q_dev,
   ka.np1job = njob;
   ka.qdrude = nullptr;
   ka.ns = nq;
-  NA_CK(k_phase_tables_mixed(Lc, ka, r_dev, tab));
+  NA_CK(k_phase_tables_mixed(Lc, ka, r_dev, tab, qfix));
   NA_CK(k_sk_gemm_mixed(Lc, ka, tab, part));
   NA_CK(k_sk_reduce_mixed(Lc, ka, part, true));
   NA_CK(k_kf_gemm_mixed(Lc, ka, tab));

@@ -1047,3 +1047,156 @@ double orc_widom_corr(const orc_sys_t *s, int nps, const int *ptype)
     for (j = 0; j < s->ns; j++) c += s->ss[ptype[a] * s->ntypes + s->type[j]].corr;
   return c;
 }
+
+/* ------------------------------------------------------------- adjoint --- */
+
+/* d/d sigma of the smoothed LJ pair terms: u = E4 (y^2 - y), y = (Sq/r^2)^3
+   below C1 (sigma^2 = Sq), u = A (r^2 - C2^2)^2 above; f = -2 du/d(r^2).
+   dA[0], dA[1]: dA/dsigma, dA4/dsigma of the smoothing constants. */
+static void lj_terms(const orc_ss_t *ss, const double *dA, double rr, double *u, double *f,
+                     double *du, double *df)
+{
+  *u = *f = *du = *df = 0;
+  if (rr >= ss->C2q || ss->E4 == 0) return;
+  if (rr < ss->C1q) {
+    double sig = sqrt(ss->Sq), y = ss->Sq / rr;
+    y = y * y * y;
+    *u = ss->E4 * (y * y - y);
+    *f = 6 * ss->E4 * (2 * y * y - y) / rr;
+    *du = ss->E4 / sig * (12 * y * y - 6 * y);
+    *df = 36 * ss->E4 * y * (4 * y - 1) / (sig * rr);
+  } else {
+    double x = rr - ss->C2q;
+    *u = ss->A * x * x;
+    *f = ss->A4 * x;
+    *du = dA[0] * x * x;
+    *df = dA[1] * x;
+  }
+}
+
+/* Gradients of the energy E, the scalar virial W = sum r.f (LJ) + E_el, and
+   (with g = dLoss/dF, [3 ns]) of a loss of the forces, with respect to the
+   LJ parameters of every type pair (epsilon > 0 and sigma of
+   4 eps [(sigma/r)^12 - (sigma/r)^6]) and to every site charge.  The
+   restatement of the adjoint: all pairs by nearest image, k-space by direct
+   sums over the k set of orc_forces, tin-foil boundary (no dipole term).
+   Per type pair (a <= b) arrays [nt*nt*2]: (d/d eps_ab, d/d sigma_ab). */
+int orc_adjoint(const orc_sys_t *s, const double *r, const double *g, const double *dA,
+                double *E, double *W, double *dEp, double *dWp, double *dLp, double *dEq,
+                double *dLq)
+{
+  const int ns = s->ns, nt = s->ntypes;
+  int i, j, m, d, nk;
+  int *kv;
+  double kappa = s->kappa, V = s->L[0] * s->L[1] * s->L[2], cq = SQ(s->cutoff);
+  double Elj = 0, Eel = 0, vir = 0;
+  double *ekk, *Sre, *Sim, *Tre, *Tim, *pr, *pi;
+  if (is_polar(s)) return -1;
+  memset(dEp, 0, sizeof(double) * nt * nt * 2);
+  memset(dWp, 0, sizeof(double) * nt * nt * 2);
+  memset(dLp, 0, sizeof(double) * nt * nt * 2);
+  memset(dEq, 0, sizeof(double) * ns);
+  memset(dLq, 0, sizeof(double) * ns);
+  /* r-space pairs */
+  for (i = 0; i < ns; i++)
+    for (j = i + 1; j < ns; j++) {
+      double dr[3], rr, qq = s->q[i] * s->q[j], phi = 0, e = 0, gd = 0;
+      nearest(s->L, r + 3 * i, r + 3 * j, dr);
+      rr = SQ(dr[0]) + SQ(dr[1]) + SQ(dr[2]);
+      if (rr >= cq) continue;
+      if (g)
+        for (d = 0; d < 3; d++) gd += (g[3 * i + d] - g[3 * j + d]) * dr[d];
+      if (s->mol[i] == s->mol[j]) {
+        phi = orc_exacterud_sqrt(rr, s->alpha, &e);
+      } else {
+        int a = s->type[i], b = s->type[j], lo = a < b ? a : b, hi = a < b ? b : a;
+        const orc_ss_t *ss = s->ss + a * nt + b;
+        double u, f, du, df, eps = -ss->eps;
+        lj_terms(ss, dA + 2 * (a * nt + b), rr, &u, &f, &du, &df);
+        Elj += u;
+        vir += rr * f;
+        if (eps > 0) {
+          dEp[2 * (lo * nt + hi)] += u / eps;
+          dWp[2 * (lo * nt + hi)] += rr * f / eps;
+          dLp[2 * (lo * nt + hi)] += gd * f / eps;
+        }
+        dEp[2 * (lo * nt + hi) + 1] += du;
+        dWp[2 * (lo * nt + hi) + 1] += rr * df;
+        dLp[2 * (lo * nt + hi) + 1] += gd * df;
+        if (qq != 0 || s->q[i] != 0 || s->q[j] != 0) {
+          const double *p = s->ertab + 6 * (int)(rr * s->sgrid);
+          phi = p[1] / (p[2] + rr) + p[0];
+          e = p[4] / (p[5] + rr) + p[3];
+        }
+      }
+      Eel += qq * phi;
+      dEq[i] += s->q[j] * phi;
+      dEq[j] += s->q[i] * phi;
+      dLq[i] += gd * e * s->q[j];
+      dLq[j] += gd * e * s->q[i];
+    }
+  /* k-space: S, T_d = sum_j q_j g_jd Phi_j, then per charge */
+  nk = orc_kvectors(s->L, &kappa, 0, NULL);
+  kv = malloc(sizeof(int) * 3 * (nk > 0 ? nk : 1));
+  kappa = s->kappa;
+  orc_kvectors(s->L, &kappa, nk, kv);
+  ekk = malloc(sizeof(double) * (nk + 1));
+  Sre = calloc(nk + 1, sizeof(double)); Sim = calloc(nk + 1, sizeof(double));
+  Tre = calloc(nk + 1, sizeof(double)); Tim = calloc(nk + 1, sizeof(double));
+  pr = malloc(sizeof(double) * (nk + 1)); pi = malloc(sizeof(double) * (nk + 1));
+  g_kmax[0] = g_kmax[1] = g_kmax[2] = 0;
+  for (m = 0; m < nk; m++)
+    for (d = 0; d < 3; d++)
+      if (abs(kv[3 * m + d]) > g_kmax[d]) g_kmax[d] = abs(kv[3 * m + d]);
+  {
+    double PIaq = -SQ(M_PI / s->alpha);
+    for (m = 0; m < nk; m++) {
+      double kk = SQ(kv[3 * m + 2] / s->L[2]) + (SQ(kv[3 * m + 1] / s->L[1]) + SQ(kv[3 * m] / s->L[0]));
+      ekk[m] = 4 / (kk * V) * exp(PIaq * kk);
+    }
+  }
+  for (j = 0; j < ns; j++) {
+    qitem_t it = {j, s->q[j], 0};
+    if (s->q[j] == 0) continue;
+    charge_phases(s, r, &it, nk, kv, pr, pi);       /* q_j Phi_j(k) */
+    for (m = 0; m < nk; m++) {
+      double w = 0;
+      Sre[m] += pr[m]; Sim[m] += pi[m];
+      if (g)
+        for (d = 0; d < 3; d++) w += g[3 * j + d] * kv[3 * m + d] / s->L[d];
+      Tre[m] += w * pr[m]; Tim[m] += w * pi[m];
+    }
+  }
+  {
+    double Ek = 0;
+    for (m = 0; m < nk; m++) Ek += ekk[m] * (SQ(Sre[m]) + SQ(Sim[m]));
+    Eel += Ek / (4 * M_PI);
+  }
+  for (j = 0; j < ns; j++) {
+    qitem_t it = {j, 1.0, 0};
+    double psi = 0, fk[3] = {0, 0, 0}, kl = 0;
+    if (s->q[j] == 0) continue;
+    charge_phases(s, r, &it, nk, kv, pr, pi);       /* Phi_j(k) */
+    for (m = 0; m < nk; m++) {
+      /* conj(S) Phi and conj(Phi) T */
+      double re = Sre[m] * pr[m] + Sim[m] * pi[m], im = Sre[m] * pi[m] - Sim[m] * pr[m];
+      double tim = pr[m] * Tim[m] - pi[m] * Tre[m];
+      psi += ekk[m] * re;
+      for (d = 0; d < 3; d++) fk[d] += ekk[m] * kv[3 * m + d] / s->L[d] * im;
+      kl += ekk[m] * tim;
+    }
+    dEq[j] += psi / (2 * M_PI) - 2 * s->alpha / SQRTPI * s->q[j];
+    if (g) dLq[j] += g[3 * j] * fk[0] + g[3 * j + 1] * fk[1] + g[3 * j + 2] * fk[2] + kl;
+  }
+  {
+    double sq2 = 0;
+    for (j = 0; j < ns; j++) sq2 += SQ(s->q[j]);
+    Eel += -s->alpha / SQRTPI * sq2;
+  }
+  /* the electrostatic virial equals the electrostatic energy */
+  for (i = 0; i < nt * nt * 2; i++) dWp[i] += 0;
+  *E = Elj + Eel;
+  *W = vir + Eel;
+  free(kv); free(ekk); free(Sre); free(Sim); free(Tre); free(Tim); free(pr); free(pi);
+  return 0;
+}

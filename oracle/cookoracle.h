@@ -129,6 +129,14 @@ double orc_widom(const orc_sys_t *s, const double *r, int nps, const int *ptype,
                  double T, double *U, int nthreads);
 double orc_widom_corr(const orc_sys_t *s, int nps, const int *ptype);
 
+/* Adjoint: gradients of E, W = LJ sum r.f + E_el and (g = dLoss/dF) of a
+   force loss with respect to the LJ (epsilon, sigma) of every type pair a<=b
+   ([nt*nt*2]) and to every site charge ([ns]); dA: [nt*nt*2] dA/dsigma,
+   dA4/dsigma of the smoothing constants.  Non-polar, tin-foil. */
+int orc_adjoint(const orc_sys_t *s, const double *r, const double *g, const double *dA,
+                double *E, double *W, double *dEp, double *dWp, double *dLp, double *dEq,
+                double *dLq);
+
 #ifdef __cplusplus
 }
 #endif
