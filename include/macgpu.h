@@ -239,6 +239,27 @@ typedef struct {
 int mg_widom(mg_ctx *ctx, const mg_probe *probe, long long ninsert, unsigned long long seed,
              double T, mg_widom_result *out, double *U);
 
+/* ---- adjoint ----
+   No reference counterpart.  Gradients, at the configuration r, of the
+   energy E, the scalar virial W = LJ sum r.f + electrostatic energy, and of
+   a loss of the forces through its weights g = dLoss/dF ([3 ns], or NULL),
+   with respect to the LJ parameters (epsilon > 0 and sigma of
+   4 eps[(sigma/r)^12 - (sigma/r)^6], combined as in the topology) of every
+   pair of types and to every site charge.  FP64 contexts without Drude
+   shells, cells re-binned (skin <= 0); tin-foil boundary.  Pair terms are
+   recomputed (nothing stored but S(k)); the type-pair sums use shared-memory
+   atomics, so their last bits may vary between calls. */
+typedef struct {
+  double E, W;        /* energy, scalar virial at r (K) */
+  double *dE_pair;    /* [ntypes*ntypes*2] or NULL: (d/d eps, d/d sigma) of the */
+  double *dW_pair;    /*   type pair (a, b), a <= b, at 2*(a*ntypes + b)        */
+  double *dL_pair;
+  double *dE_dq;      /* [ns] or NULL: dE/dq_i (= dW/dq_i) */
+  double *dL_dq;      /* [ns] or NULL: dLoss/dq_i */
+} mg_adjoint_out;
+
+int mg_adjoint(mg_ctx *ctx, const double *r, const double *g, mg_adjoint_out *out);
+
 /* ---- batches of independent boxes ----
    No reference counterpart (cook runs one box per process).  A batch owns
    nbox contexts whose kernels run on nlanes streams; mg_batch_md_steps

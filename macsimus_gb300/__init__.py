@@ -67,6 +67,11 @@ class Energy(C.Structure):
         return d
 
 
+class AdjointOut(C.Structure):
+    _fields_ = [("E", C.c_double), ("W", C.c_double), ("dE_pair", _dp), ("dW_pair", _dp),
+                ("dL_pair", _dp), ("dE_dq", _dp), ("dL_dq", _dp)]
+
+
 class Probe(C.Structure):
     _fields_ = [("ns", C.c_int), ("site_type", _ip), ("charge", _dp), ("geometry", _dp)]
 
@@ -111,6 +116,7 @@ def library():
         L.mg_profile_entry.argtypes = [vp, C.c_int, C.POINTER(C.c_char_p), _dp,
                                        C.POINTER(C.c_long)]
         L.mg_probe_fp32_tflops.argtypes = [_dp]
+        L.mg_adjoint.argtypes = [vp, _dp, _dp, C.POINTER(AdjointOut)]
         L.mg_widom.argtypes = [vp, C.POINTER(Probe), C.c_longlong, C.c_ulonglong, C.c_double,
                                C.POINTER(WidomResult), _dp]
         L.mg_batch_create.argtypes = [C.c_int, C.POINTER(Topology), C.POINTER(Params), C.c_int,
@@ -359,6 +365,24 @@ class ForcePath:
         en = Energy()
         self._check(library().mg_md_steps(self._ctx, int(n), C.byref(en) if measure else None))
         return en.asdict() if measure else None
+
+    def adjoint(self, r, g=None):
+        """gradients of E, W = LJ sum r.f + E_el and (g = dLoss/dF, [ns,3]) of
+        a force loss w.r.t. the LJ (eps, sigma) of every type pair a <= b
+        ([nt,nt,2]) and every site charge ([ns]); FP64 contexts"""
+        nt = len(self.system.typeE)
+        r = _arr(r, np.float64).reshape(-1)
+        gg = None if g is None else _arr(g, np.float64).reshape(-1)
+        dEp, dWp, dLp = (np.zeros(nt * nt * 2) for _ in range(3))
+        dEq, dLq = np.zeros(self.ns), np.zeros(self.ns)
+        out = AdjointOut(0.0, 0.0, dEp.ctypes.data_as(_dp), dWp.ctypes.data_as(_dp),
+                         dLp.ctypes.data_as(_dp), dEq.ctypes.data_as(_dp), dLq.ctypes.data_as(_dp))
+        self._check(library().mg_adjoint(self._ctx, r.ctypes.data_as(_dp),
+                                         gg.ctypes.data_as(_dp) if gg is not None else None,
+                                         C.byref(out)))
+        sh = (nt, nt, 2)
+        return dict(E=out.E, W=out.W, dEp=dEp.reshape(sh), dWp=dWp.reshape(sh),
+                    dLp=dLp.reshape(sh), dEq=dEq, dLq=dLq)
 
     def widom(self, site_types, geometry=None, charges=None, n=100000, seed=1, T=298.0,
               energies=False):

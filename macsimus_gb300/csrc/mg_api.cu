@@ -102,6 +102,13 @@ struct mg_ctx {
   PairD* d_wtabd = nullptr;
   double *d_wgeom = nullptr, *d_wpart = nullptr;
   WidomBox* d_wbox = nullptr;
+  // adjoint scratch (FP64 contexts)
+  AdjPair* d_adjtab = nullptr;
+  double *d_ag = nullptr, *d_aq = nullptr, *d_apart = nullptr, *d_adEq = nullptr,
+         *d_adLq = nullptr;
+  double4* d_ags = nullptr;
+  double2 *d_atpart = nullptr, *d_aT = nullptr;
+  int adj_ntch = 0;
   std::vector<PairF> h_wtabf;
   std::vector<PairD> h_wtabd;
   std::vector<double> h_wgeom;
@@ -900,7 +907,8 @@ int mg_destroy(mg_ctx* ctx) {
                   ctx->d_qp, ctx->d_aqq, ctx->d_hist, ctx->d_drpart, ctx->d_pdj, ctx->d_pdd,
                   ctx->d_nlist, ctx->d_ncount, ctx->d_rbuild, ctx->d_dmax,
                   ctx->d_wtabf, ctx->d_wtabd, ctx->d_wgeom, ctx->d_wpart, ctx->d_wbox,
-                  ctx->d_qfix};
+                  ctx->d_qfix, ctx->d_adjtab, ctx->d_ag, ctx->d_aq, ctx->d_apart, ctx->d_adEq,
+                  ctx->d_adLq, ctx->d_ags, ctx->d_atpart, ctx->d_aT};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ctx->h_sums) cudaFreeHost(ctx->h_sums);
@@ -1300,6 +1308,156 @@ int mg_widom(mg_ctx* ctx, const mg_probe* probe, long long ninsert, unsigned lon
   CK(cudaStreamSynchronize(ctx->stream));
   if (d_U) CK(cudaFree(d_U));
   widom_result(ctx, part.data(), nblk, ninsert, T, corr, out);
+  return MG_OK;
+}
+
+namespace {
+
+PairArgs pair_args(mg_ctx* ctx) {
+  PairArgs pa;
+  pa.ns = ctx->ns;
+  pa.ncx = ctx->ncx;
+  pa.ncy = ctx->ncy;
+  pa.ncz = ctx->ncz;
+  pa.nstencil = ctx->nstencil;
+  pa.allpairs = ctx->allpairs ? 1 : 0;
+  pa.nkind = ctx->nkind;
+  pa.cell_start = ctx->d_cell_start;
+  pa.order = ctx->d_order;
+  pa.stencil = ctx->d_stencil;
+  pa.Lx = ctx->L[0];
+  pa.Ly = ctx->L[1];
+  pa.Lz = ctx->L[2];
+  pa.cutoff_sq = ctx->cutoff * ctx->cutoff;
+  pa.sgrid = ctx->sgrid;
+  pa.alpha = ctx->alpha;
+  pa.f = nullptr;
+  pa.epart = nullptr;
+  pa.ntab = ctx->ntab;
+  pa.pdj = nullptr;
+  pa.pdd = nullptr;
+  return pa;
+}
+
+KArgs kspace_args(mg_ctx* ctx) {
+  KArgs ka;
+  std::memset(&ka, 0, sizeof(ka));
+  ka.nq = ctx->nq;
+  ka.nk = ctx->nk;
+  ka.nchunk = ctx->nchunk;
+  ka.Kx = ctx->Kx;
+  ka.Ky = ctx->Ky;
+  ka.Kz = ctx->Kz;
+  ka.row = ctx->row;
+  ka.Lx = ctx->L[0];
+  ka.Ly = ctx->L[1];
+  ka.Lz = ctx->L[2];
+  ka.alpha = ctx->alpha;
+  ka.qsite = ctx->d_qsite;
+  ka.qval = ctx->d_qval;
+  ka.kvec = ctx->d_kvec;
+  ka.ekk = ctx->d_ekk;
+  ka.S = ctx->d_S;
+  ka.ns = ctx->ns;
+  return ka;
+}
+
+}  // namespace
+
+int mg_adjoint(mg_ctx* ctx, const double* r, const double* g, mg_adjoint_out* out) {
+  if (!ctx || !r || !out) return fail(ctx, MG_ERR_ARG, "null argument");
+  if (ctx->precision != MG_FP64 || ctx->polar || ctx->use_list)
+    return fail(ctx, MG_ERR_ARG,
+                "the adjoint needs an FP64, non-polar context with cells re-binned (skin <= 0)");
+  const int ns = ctx->ns, nk2 = ctx->nkind * ctx->nkind, nt = ctx->ntypes;
+  if (!ctx->d_adjtab) {
+    // per pair of kinds: the smoothed-LJ constants, their sigma derivatives
+    // (central differences of the set-up, step 1e-5 sigma) and eps, sigma
+    std::vector<AdjPair> tab(nk2);
+    const double c6 = 1.122462048309373;  // 2^(1/6): r_min = c6 sigma
+    for (int ka = 0; ka < ctx->nkind; ka++)
+      for (int kb = 0; kb < ctx->nkind; kb++) {
+        const int ta = ctx->kind_type[ka], tb = ctx->kind_type[kb];
+        double eps, sig;
+        PairLJ P{}, Pp{}, Pm{};
+        combining_rule(ctx->h_tE[ta], ctx->h_tR[ta], ctx->h_tA[ta], ctx->h_tE[tb], ctx->h_tR[tb],
+                       ctx->h_tA[tb], ctx->comb_rule, &eps, &sig);
+        smooth_lj(eps, sig, ctx->C2, &P);
+        AdjPair& A = tab[ka * ctx->nkind + kb];
+        A = AdjPair{P.C1q, P.C2q, P.Sq, P.E4, P.A, P.A4, 0, 0, 1, 1};
+        if (eps != 0) {
+          const double h = 1e-5 * sig;
+          smooth_lj(eps, sig + h, ctx->C2, &Pp);
+          smooth_lj(eps, sig - h, ctx->C2, &Pm);
+          A.dA = (Pp.A - Pm.A) / (2 * h) * c6;
+          A.dA4 = (Pp.A4 - Pm.A4) / (2 * h) * c6;
+          A.eps = -eps;
+          A.sig = sig / c6;
+        }
+      }
+    CK(upload(&ctx->d_adjtab, tab.data(), tab.size()));
+    std::vector<double> q(ns);
+    for (int i = 0; i < ns; i++) q[i] = ctx->kind_q[ctx->h_kind[i]];
+    CK(upload(&ctx->d_aq, q.data(), q.size()));
+    CK(dalloc(&ctx->d_ag, 3 * (size_t)ns));
+    CK(dalloc(&ctx->d_ags, (size_t)ns));
+    CK(dalloc(&ctx->d_apart, (size_t)ctx->ncell * nk2 * 6));
+    CK(dalloc(&ctx->d_adEq, (size_t)ns));
+    CK(dalloc(&ctx->d_adLq, (size_t)ns));
+    ctx->adj_ntch = std::max(1, std::min(64, ctx->nq / 256));
+    CK(dalloc(&ctx->d_atpart, (size_t)ctx->adj_ntch * std::max(1, ctx->nk) * 3));
+    CK(dalloc(&ctx->d_aT, (size_t)std::max(1, ctx->nk)));
+  }
+  ctx->launches = 0;
+  const size_t nb = 3 * (size_t)ns * sizeof(double);
+  CK(cudaMemcpyAsync(ctx->d_rs, r, nb, cudaMemcpyHostToDevice, ctx->stream));
+  if (g) CK(cudaMemcpyAsync(ctx->d_ag, g, nb, cudaMemcpyHostToDevice, ctx->stream));
+  int rc = forces_async(ctx, ctx->d_rs, ctx->d_fs, true);
+  if (rc) return rc;
+  ctx->need_build = true;
+  Launch L = launch(ctx);
+  CK(k_adjoint(L, pair_args(ctx), kspace_args(ctx), ctx->d_pd, ctx->d_adjtab, ctx->d_ert,
+               (const double2*)ctx->d_tab, g ? ctx->d_ag : nullptr, ctx->d_aq, ctx->d_ags,
+               ctx->d_apart, ctx->d_adEq, ctx->d_adLq, ctx->d_atpart, ctx->adj_ntch, ctx->d_aT));
+  std::vector<double> part((size_t)ctx->ncell * nk2 * 6);
+  CK(cudaMemcpyAsync(part.data(), ctx->d_apart, sizeof(double) * part.size(),
+                     cudaMemcpyDeviceToHost, ctx->stream));
+  if (out->dE_dq)
+    CK(cudaMemcpyAsync(out->dE_dq, ctx->d_adEq, sizeof(double) * ns, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+  if (out->dL_dq)
+    CK(cudaMemcpyAsync(out->dL_dq, ctx->d_adLq, sizeof(double) * ns, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+  rc = fetch_sums(ctx);
+  if (rc) return rc;
+  rc = fetch_status(ctx);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  rc = check_status(ctx);
+  if (rc) return rc;
+  mg_energy en;
+  fill_energy(ctx, &en);
+  out->E = en.el + en.lj;
+  out->W = en.vir + en.el;
+  // kind pairs (both orders, halves from the kernel) -> type pairs a <= b,
+  // summed over the cell CTAs in a fixed order
+  std::vector<double> kp((size_t)nk2 * 6, 0.0);
+  for (int c = 0; c < ctx->ncell; c++)
+    for (int t = 0; t < nk2 * 6; t++) kp[t] += part[(size_t)c * nk2 * 6 + t];
+  double* dst[3] = {out->dE_pair, out->dW_pair, out->dL_pair};
+  for (int m = 0; m < 3; m++)
+    if (dst[m]) std::memset(dst[m], 0, sizeof(double) * nt * nt * 2);
+  for (int ka = 0; ka < ctx->nkind; ka++)
+    for (int kb = 0; kb < ctx->nkind; kb++) {
+      const int ta = ctx->kind_type[ka], tb = ctx->kind_type[kb];
+      const int lo = std::min(ta, tb), hi = std::max(ta, tb);
+      const double* v = kp.data() + 6 * (ka * ctx->nkind + kb);
+      for (int m = 0; m < 3; m++)
+        if (dst[m]) {
+          dst[m][2 * (lo * nt + hi)] += v[2 * m];
+          dst[m][2 * (lo * nt + hi) + 1] += v[2 * m + 1];
+        }
+    }
   return MG_OK;
 }
 

@@ -231,6 +231,19 @@ struct WidomArgs {
   double* U;           // [n] or null
   double* part;        // [nblocks]
 };
+// adjoint constants of one pair of site kinds (FP64)
+struct AdjPair {
+  double C1q, C2q, Sq, E4, A, A4;
+  double dA, dA4;   // d/dsigma of the smoothing constants
+  double eps, sig;  // epsilon > 0 (1 when the pair has no LJ), sigma
+};
+// per cell CTA: kind-pair sums [ncell][nkind^2][6]; per site dE/dq, dLoss/dq;
+// k-space: tpart [ntch][nk][3], T [nk]
+cudaError_t k_adjoint(const Launch& L, const PairArgs& pa, const KArgs& ka, const double4* pd,
+                      const AdjPair* tab, const double* ert, const double2* ptab, const double* g,
+                      const double* q, double4* gs, double* part, double* dEq, double* dLq,
+                      double2* tpart, int ntch, double2* T);
+
 // one box of a Widom launch (blockIdx.y): its arguments and data
 struct WidomBox {
   WidomArgs a;

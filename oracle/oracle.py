@@ -78,6 +78,7 @@ def lib():
         L.orc_widom.argtypes = [C.POINTER(SYS), dp, C.c_int, ip, dp, dp, C.c_longlong, u64,
                                 C.c_double, dp, C.c_int]
         L.orc_widom.restype = C.c_double
+        L.orc_adjoint.argtypes = [C.POINTER(SYS), dp, dp, dp, dp, dp, dp, dp, dp, dp, dp]
         L.orc_widom_corr.argtypes = [C.POINTER(SYS), C.c_int, ip]
         L.orc_widom_corr.restype = C.c_double
         _lib = L
@@ -107,6 +108,32 @@ def pair_tables(system, C2):
             if rc != 0:
                 raise ValueError("setss failed for types %d,%d" % (a, b))
     return ss
+
+
+def smoothing_derivatives(system, C2):
+    """dA/dsigma and dA4/dsigma (sigma of 4 eps[(s/r)^12-(s/r)^6]) of the smooth
+    cutoff constants of every type pair, [nt*nt*2], by central differences
+    of setss"""
+    L = lib()
+    nt = len(system.typeE)
+    out = np.zeros(nt * nt * 2)
+    c6 = 2.0 ** (1.0 / 6.0)
+    for a in range(nt):
+        for b in range(nt):
+            eps, sig = C.c_double(), C.c_double()
+            L.orc_combrule(system.typeE[a], system.typeR[a], system.typeA[a],
+                           system.typeE[b], system.typeR[b], system.typeA[b],
+                           system.comb_rule, C.byref(eps), C.byref(sig))
+            if eps.value == 0:
+                continue
+            h = 1e-5 * sig.value
+            sp, sm = SS(), SS()
+            L.orc_setss(eps.value, sig.value + h, C2, C.byref(sp))
+            L.orc_setss(eps.value, sig.value - h, C2, C.byref(sm))
+            # d/d sigma_LJ = c6 d/d r_min
+            out[2 * (a * nt + b)] = (sp.A - sm.A) / (2 * h) * c6
+            out[2 * (a * nt + b) + 1] = (sp.A4 - sm.A4) / (2 * h) * c6
+    return out
 
 
 def kvectors(Lbox, kappa):
@@ -211,6 +238,27 @@ class Oracle:
                                   omega, maxit, C.byref(ek))
         return r.reshape(-1, 3), r1.reshape(-1, 3), it, ek.value
 
+
+    # ---------------------------------------------------------- adjoint --
+    def adjoint(self, r, g=None, C2=None):
+        """gradients of E, W and (g = dLoss/dF) a force loss w.r.t. the LJ
+        (eps, sigma) of every type pair a<=b and every site charge"""
+        s = self.system
+        nt = len(s.typeE)
+        r = np.ascontiguousarray(r, np.float64).reshape(-1)
+        gg = None if g is None else np.ascontiguousarray(g, np.float64).reshape(-1)
+        dA = smoothing_derivatives(s, C2 if C2 else self.sys.cutoff)
+        E, W = C.c_double(), C.c_double()
+        dEp, dWp, dLp = (np.zeros(nt * nt * 2) for _ in range(3))
+        dEq, dLq = np.zeros(s.ns), np.zeros(s.ns)
+        rc = lib().orc_adjoint(C.byref(self.sys), _dp(r), _dp(gg) if gg is not None else None,
+                               _dp(dA), C.byref(E), C.byref(W), _dp(dEp), _dp(dWp), _dp(dLp),
+                               _dp(dEq), _dp(dLq))
+        if rc:
+            raise ValueError("orc_adjoint: polar systems are not supported")
+        sh = (nt, nt, 2)
+        return dict(E=E.value, W=W.value, dEp=dEp.reshape(sh), dWp=dWp.reshape(sh),
+                    dLp=dLp.reshape(sh), dEq=dEq, dLq=dLq)
 
     # ------------------------------------------------------------ Widom --
     def widom_sites(self, seed, k, geometry):
