@@ -100,6 +100,9 @@ typedef struct {
      once a site has moved skin/4 since the build (or after nl_every steps) */
   double skin;       /* A */
   int nl_every;      /* most MD steps between list builds; <=0 selects 50 */
+  /* Ewald pass 1 work split: charge chunks sized for this many CTAs per SM;
+     <=0 selects 10 (FP32) / 8 (FP64).  mg_autotune picks it. */
+  int kspace_ctas_per_sm;
 } mg_params;
 
 /* Energies of one force evaluation (program units, K).
@@ -238,6 +241,15 @@ typedef struct {
 /* U (optional, [ninsert]) receives every insertion energy (K) */
 int mg_widom(mg_ctx *ctx, const mg_probe *probe, long long ninsert, unsigned long long seed,
              double T, mg_widom_result *out, double *U);
+
+/* ---- autotuner ----
+   No reference counterpart.  Times the force evaluation of the configuration
+   r for every cell subdivision (cells_per_cutoff 1..3) and Ewald pass-1
+   split (kspace_ctas_per_sm 6, 10, 16) and writes the fastest pair into
+   *par.  Builds and frees its own trial contexts; ms[9] (optional) gets the
+   time per evaluation of each trial (cdiv-major, -1 if that grid is not
+   possible). */
+int mg_autotune(const mg_topology *top, mg_params *par, const double *r, int nrep, double *ms);
 
 /* ---- adjoint ----
    No reference counterpart.  Gradients, at the configuration r, of the

@@ -52,7 +52,7 @@ class Params(C.Structure):
                 ("omegac", C.c_double), ("shake_maxit", C.c_int),
                 ("cells_per_cutoff", C.c_int), ("aspc_k", C.c_int), ("scf_iter", C.c_int),
                 ("scf_omega", C.c_double), ("minqq", C.c_double), ("skin", C.c_double),
-                ("nl_every", C.c_int)]
+                ("nl_every", C.c_int), ("kspace_ctas_per_sm", C.c_int)]
 
 
 class Energy(C.Structure):
@@ -116,6 +116,7 @@ def library():
         L.mg_profile_entry.argtypes = [vp, C.c_int, C.POINTER(C.c_char_p), _dp,
                                        C.POINTER(C.c_long)]
         L.mg_probe_fp32_tflops.argtypes = [_dp]
+        L.mg_autotune.argtypes = [C.POINTER(Topology), C.POINTER(Params), _dp, C.c_int, _dp]
         L.mg_adjoint.argtypes = [vp, _dp, _dp, C.POINTER(AdjointOut)]
         L.mg_widom.argtypes = [vp, C.POINTER(Probe), C.c_longlong, C.c_ulonglong, C.c_double,
                                C.POINTER(WidomResult), _dp]
@@ -137,6 +138,20 @@ def library():
     return _lib
 
 
+def autotune(system, L, cutoff, alpha, kappa, r, nrep=3, **kw):
+    """the fastest (cells_per_cutoff, kspace_ctas_per_sm) for this box and
+    configuration (mg_autotune); returns them with the 3x3 timing table"""
+    t, p, keep = describe(system, L, cutoff, alpha, kappa, **kw)
+    ms = np.zeros(9)
+    rr = _arr(r, np.float64).reshape(-1)
+    rc = library().mg_autotune(C.byref(t), C.byref(p), rr.ctypes.data_as(_dp), int(nrep),
+                               ms.ctypes.data_as(_dp))
+    if rc:
+        raise MGError(rc, "mg_autotune failed")
+    return dict(cells_per_cutoff=p.cells_per_cutoff, kspace_ctas_per_sm=p.kspace_ctas_per_sm,
+                ms=ms.reshape(3, 3))
+
+
 def fp32_peak_tflops():
     """measured FP32 FMA throughput of the current device (TFLOP/s)"""
     t = C.c_double()
@@ -153,7 +168,7 @@ def _arr(a, dt):
 def describe(system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None, grid=256,
              rshift=3, rplus=2.5, epsinf=3e33, h=0.002, epsc=1e-7, omegac=1.2, shake_maxit=1000,
              cells_per_cutoff=0, aspc_k=2, scf_iter=1, scf_omega=0.6, minqq=1.0, skin=0.0,
-             nl_every=50):
+             nl_every=50, kspace_ctas_per_sm=0):
     """(mg_topology, mg_params, arrays to keep alive) of one box"""
     keep = []
 
@@ -213,6 +228,7 @@ def describe(system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None, 
     p.minqq = minqq
     p.skin = skin
     p.nl_every = nl_every
+    p.kspace_ctas_per_sm = kspace_ctas_per_sm
     return t, p, keep
 
 
@@ -222,7 +238,7 @@ class ForcePath:
     def __init__(self, system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None,
                  grid=256, rshift=3, rplus=2.5, epsinf=3e33, h=0.002, epsc=1e-7, omegac=1.2,
                  shake_maxit=1000, cells_per_cutoff=0, aspc_k=2, scf_iter=1, scf_omega=0.6,
-                 minqq=1.0, skin=0.0, nl_every=50):
+                 minqq=1.0, skin=0.0, nl_every=50, kspace_ctas_per_sm=0):
         lib = library()
         self.system = system
         self.ns = system.ns
@@ -231,7 +247,8 @@ class ForcePath:
                                     epsinf=epsinf, h=h, epsc=epsc, omegac=omegac,
                                     shake_maxit=shake_maxit, cells_per_cutoff=cells_per_cutoff,
                                     aspc_k=aspc_k, scf_iter=scf_iter, scf_omega=scf_omega,
-                                    minqq=minqq, skin=skin, nl_every=nl_every)
+                                    minqq=minqq, skin=skin, nl_every=nl_every,
+                                    kspace_ctas_per_sm=kspace_ctas_per_sm)
         self.polar = getattr(system, "polar", False)
         Lb = np.broadcast_to(np.asarray(L, dtype=np.float64), (3,))
         st = C.c_int(0)

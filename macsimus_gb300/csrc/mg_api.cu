@@ -459,7 +459,8 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   ctx->ndblocks = (ctx->nd + 127) / 128;
   // charge chunks of pass 1: about 8 (FP64 kernel) or 6 (FP32 kernel) CTAs
   // per SM, at least 64 charges each
-  const int p1ctas = (ctx->precision == MG_MIXED ? 10 : 8) * 152;
+  const int p1ctas = (p->kspace_ctas_per_sm > 0 ? p->kspace_ctas_per_sm
+                                                : (ctx->precision == MG_MIXED ? 10 : 8)) * 152;
   ctx->nchunk = std::max(1, std::min(std::max(1, ctx->nq / 64),
                                      (p1ctas + ctx->np1job - 1) / ctx->np1job));
   ctx->nkblocks = (nk + 255) / 256;
@@ -1765,5 +1766,65 @@ int mg_batch_widom(mg_batch* b, const mg_probe* probes, int probe_per_box, long 
   BCK(cudaStreamSynchronize(b->main));
   for (int i = 0; i < nbox; i++)
     widom_result(b->box[i], part.data() + (size_t)i * nblk, nblk, ninsert, T, corr[i], &out[i]);
+  return MG_OK;
+}
+
+// ------------------------------------------------------------- autotuner --
+
+int mg_autotune(const mg_topology* top, mg_params* par, const double* r, int nrep, double* ms) {
+  if (!top || !par || !r) return MG_ERR_ARG;
+  const int cd[3] = {1, 2, 3}, kc[3] = {6, 10, 16};
+  nrep = std::max(1, nrep);
+  const bool polar = top->chargepol != nullptr;
+  const size_t nv = 3 * (size_t)top->ns * (polar ? 2 : 1);
+  double *r_dev = nullptr, *f_dev = nullptr;
+  if (cudaMalloc((void**)&r_dev, nv * sizeof(double)) != cudaSuccess) return MG_ERR_CUDA;
+  if (cudaMalloc((void**)&f_dev, nv * sizeof(double)) != cudaSuccess) {
+    cudaFree(r_dev);
+    return MG_ERR_CUDA;
+  }
+  cudaMemcpy(r_dev, r, nv * sizeof(double), cudaMemcpyHostToDevice);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  double best = 1e300;
+  int bc = 0, bk = 0, rc = MG_OK;
+  for (int a = 0; a < 3 && rc == MG_OK; a++)
+    for (int b = 0; b < 3; b++) {
+      mg_params p2 = *par;
+      p2.cells_per_cutoff = cd[a];
+      p2.kspace_ctas_per_sm = kc[b];
+      int st = 0;
+      mg_ctx* c = mg_create(top, &p2, &st);
+      double t = -1;
+      if (c) {
+        int e = mg_forces_device(c, r_dev, f_dev, 0, nullptr);  // warm-up
+        if (!e) {
+          cudaEventRecord(e0, c->stream);
+          for (int k = 0; k < nrep && !e; k++) e = mg_forces_device(c, r_dev, f_dev, 0, nullptr);
+          cudaEventRecord(e1, c->stream);
+          cudaEventSynchronize(e1);
+          float f = 0;
+          cudaEventElapsedTime(&f, e0, e1);
+          if (!e) t = f / nrep;
+        }
+        if (e) rc = e;
+        mg_destroy(c);
+      }
+      if (ms) ms[3 * a + b] = t;
+      if (t > 0 && t < best) {
+        best = t;
+        bc = cd[a];
+        bk = kc[b];
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(r_dev);
+  cudaFree(f_dev);
+  if (rc) return rc;
+  if (bc == 0) return MG_ERR_SETUP;
+  par->cells_per_cutoff = bc;
+  par->kspace_ctas_per_sm = bk;
   return MG_OK;
 }

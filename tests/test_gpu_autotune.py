@@ -1,0 +1,27 @@
+"""The autotuner (mg_autotune) returns a valid cell subdivision and pass-1
+split, and the tuned path gives the same forces."""
+import numpy as np
+import pytest
+
+import macsimus_gb300 as M
+from golden_cases import load
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_autotune_choice_and_forces(precision):
+    g, meta, system, ew = load("spce864")
+    args = (system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
+    best = M.autotune(*args, g["r"][0], precision=precision)
+    assert best["cells_per_cutoff"] in (1, 2, 3)
+    assert best["kspace_ctas_per_sm"] in (6, 10, 16)
+    ms = best["ms"]
+    assert (ms[ms > 0] > 0).any()
+    assert ms[best["cells_per_cutoff"] - 1, [6, 10, 16].index(best["kspace_ctas_per_sm"])] == \
+        ms[ms > 0].min()
+    f0, _ = M.ForcePath(*args, precision=precision).forces(g["r"][0])
+    f1, _ = M.ForcePath(*args, precision=precision, cells_per_cutoff=best["cells_per_cutoff"],
+                        kspace_ctas_per_sm=best["kspace_ctas_per_sm"]).forces(g["r"][0])
+    tol = 1e-12 if precision == "fp64" else 1e-6
+    assert np.sqrt(((f1 - f0) ** 2).sum() / (f0 ** 2).sum()) < tol
