@@ -169,6 +169,10 @@ int mg_last_launches(const mg_ctx *ctx);
 /* Run the context's work on the given CUDA stream (a cudaStream_t of the
    caller, e.g. a framework's current stream); NULL selects the context's own
    stream again.  No counterpart in the reference (cook has no device). */
+/* FP32 path: run the Ewald k-space chain on a second stream beside the
+   r-space chain (on by default; off serialises them, e.g. to time kernels
+   one by one).  No reference counterpart. */
+int mg_set_overlap(mg_ctx *ctx, int on);
 int mg_set_stream(mg_ctx *ctx, void *stream);
 
 /* Per-kernel timing with CUDA events recorded on the context stream around

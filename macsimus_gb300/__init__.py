@@ -111,6 +111,7 @@ def library():
         L.mg_md_steps.argtypes = [vp, C.c_int, C.POINTER(Energy)]
         L.mg_selffield.argtypes = [vp, _dp, _dp, C.c_double, C.c_int, C.POINTER(Energy)]
         L.mg_set_stream.argtypes = [vp, vp]
+        L.mg_set_overlap.argtypes = [vp, C.c_int]
         L.mg_profile_enable.argtypes = [vp, C.c_int]
         L.mg_profile_reset.argtypes = [vp]
         L.mg_profile_entry.argtypes = [vp, C.c_int, C.POINTER(C.c_char_p), _dp,
@@ -353,6 +354,10 @@ class ForcePath:
         self._check(library().mg_md_get_state(self._ctx, r.ctypes.data_as(_dp),
                                               r1.ctypes.data_as(_dp)))
         return r.reshape(-1, 3), r1.reshape(-1, 3)
+
+    def set_overlap(self, on):
+        """FP32 path: k-space chain concurrent with the r-space chain (default on)"""
+        self._check(library().mg_set_overlap(self._ctx, 1 if on else 0))
 
     def set_stream(self, stream_handle):
         """run on a caller's CUDA stream (e.g. torch.cuda.current_stream().cuda_stream)"""

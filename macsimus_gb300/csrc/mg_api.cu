@@ -123,6 +123,12 @@ struct mg_ctx {
   double4* d_pdd = nullptr;
   // stream ownership and per-kernel event timing
   cudaStream_t own_stream = nullptr;
+  // FP32 path: the Ewald k-space chain runs on kstream beside the r-space
+  // chain (forks and joins on events, k-space forces into d_fk, added at the join)
+  bool overlap = true;
+  cudaStream_t kstream = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  double* d_fk = nullptr;
   bool prof_on = false;
   struct Rec { int id; cudaEvent_t a, b; };
   std::vector<std::string> pnames;
@@ -178,21 +184,23 @@ void prof_resolve(mg_ctx* c) {
   c->evused = 0;
 }
 
-// launch `call`; with profiling on, bracket it by events on the context stream
-#define PROF(name, call)                                              \
+// launch `call` on stream `strm`; with profiling on, bracket it by events
+// on that stream
+#define PROFS(name, strm, call)                                       \
   do {                                                                \
     cudaEvent_t a_ = nullptr;                                         \
     if (ctx->prof_on) {                                               \
       a_ = prof_event(ctx);                                           \
-      cudaEventRecord(a_, ctx->stream);                               \
+      cudaEventRecord(a_, strm);                                      \
     }                                                                 \
     CK(call);                                                         \
     if (ctx->prof_on) {                                               \
       cudaEvent_t b_ = prof_event(ctx);                               \
-      cudaEventRecord(b_, ctx->stream);                               \
+      cudaEventRecord(b_, strm);                                      \
       ctx->pending.push_back(mg_ctx::Rec{prof_id(ctx, name), a_, b_}); \
     }                                                                 \
   } while (0)
+#define PROF(name, call) PROFS(name, ctx->stream, call)
 
 template <typename T>
 cudaError_t dalloc(T** p, size_t n) {
@@ -244,6 +252,9 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   ctx->nl_every = p->nl_every > 0 ? p->nl_every : 50;
   CK(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
   ctx->stream = ctx->own_stream;
+  CK(cudaStreamCreateWithFlags(&ctx->kstream, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
   const int ns = t->ns;
 
   // ---- site kinds: distinct (LJ type, charge, Drude charge) combinations
@@ -515,7 +526,7 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
                                      ctx->d_idx, ctx->d_order, ns, 0, ctx->sort_bits));
   CK(cudaMalloc(&ctx->d_sort_tmp, ctx->sort_tmp_bytes));
   CK(upload(&ctx->d_stencil, st.data(), st.size()));
-  ctx->nepart = std::max(ctx->ncell, list_blocks(ns));
+  ctx->nepart = std::max(ctx->ncell, std::max(list_blocks(ns, true), list_blocks(ns, false)));
   CK(dalloc(&ctx->d_epart, (size_t)ctx->nepart * 10));
   if (ctx->use_list) {
     // capacity: the largest expected count in a sphere of the list radius at
@@ -523,8 +534,8 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
     const double V = p->L[0] * p->L[1] * p->L[2], rl = p->cutoff + ctx->skin;
     ctx->nl_cap = ((int)(1.5 * ns / V * 4.18879 * rl * rl * rl) + 64 + 31) / 32 * 32;
     ctx->nl_cap = std::min(ctx->nl_cap, ns);
-    ctx->nl_pitch = ((long)ns + 31) / 32 * 32;
-    CK(dalloc(&ctx->d_nlist, (size_t)ctx->nl_cap * ctx->nl_pitch));
+    ctx->nl_pitch = ctx->nl_cap;
+    CK(dalloc(&ctx->d_nlist, (size_t)ctx->nl_cap * ns));
     CK(dalloc(&ctx->d_ncount, ns));
     CK(dalloc(&ctx->d_rbuild, 3 * (size_t)ns));
     CK(dalloc(&ctx->d_dmax, 1));
@@ -557,6 +568,7 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
     CK(upload(&ctx->d_eru, eru.data(), ntab));
     CK(dalloc((float2**)&ctx->d_tab, (size_t)ctx->nq * ctx->row));
     CK(dalloc(&ctx->d_qfix, std::max(1, ctx->nq)));
+    CK(dalloc(&ctx->d_fk, 3 * (size_t)ns * (ctx->polar ? 2 : 1)));
     CK(dalloc((float2**)&ctx->d_part, (size_t)ctx->nchunk * nk));
     CK(dalloc(&ctx->d_Wf, nk));
   } else {
@@ -612,7 +624,7 @@ int build_lists(mg_ctx* ctx, const double* r_dev) {
   Launch L = launch(ctx);
   for (int attempt = 0; attempt < 4; attempt++) {
     ListArgs l = list_args(ctx);
-    PROF("neighbour_list", k_build_list(L, l, ctx->d_pj));
+    PROF("list_build", k_build_list(L, l, ctx->ns, ctx->d_key_s, ctx->d_pj));
     PROF("neighbour_list", k_save_build(L, ctx->ns, r_dev, ctx->d_rbuild));
     int st = 0;
     CK(cudaMemcpyAsync(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -629,7 +641,8 @@ int build_lists(mg_ctx* ctx, const double* r_dev) {
     CK(cudaFree(ctx->d_nlist));
     ctx->d_nlist = nullptr;
     ctx->nl_cap = std::min(ctx->ns, ctx->nl_cap * 3 / 2 + 32);
-    CK(dalloc(&ctx->d_nlist, (size_t)ctx->nl_cap * ctx->nl_pitch));
+    ctx->nl_pitch = ctx->nl_cap;
+    CK(dalloc(&ctx->d_nlist, (size_t)ctx->nl_cap * ctx->ns));
   }
   return fail(ctx, MG_ERR_SIZE, "neighbour list capacity");
 }
@@ -637,6 +650,10 @@ int build_lists(mg_ctx* ctx, const double* r_dev) {
 int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) {
   Launch L = launch(ctx);
   const int ns = ctx->ns;
+  // fork point of the concurrent k-space chain (FP32 path): everything
+  // queued before, nothing of this evaluation's r-space work
+  if (ctx->precision == MG_MIXED && ctx->overlap && ctx->nq > 0)
+    CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
   const bool rebuild = !ctx->use_list || ctx->need_build || ctx->since_build >= ctx->nl_every;
   if (rebuild) {
     // linked cells
@@ -706,6 +723,23 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
   ListArgs la = list_args(ctx);
   int nerows = ctx->ncell;
   if (ctx->precision == MG_MIXED) {
+    // the k-space chain on kstream, concurrent with the r-space chain below;
+    // its forces go to d_fk and are added at the join
+    const bool fork = ctx->overlap && ctx->nq > 0;
+    const size_t nf = 3 * (size_t)ns * (ctx->polar ? 2 : 1);
+    if (fork) {
+      cudaStream_t ks = ctx->kstream;
+      Launch LK{ks, &ctx->launches};
+      KArgs kk = ka;
+      kk.f = ctx->d_fk;
+      CK(cudaStreamWaitEvent(ks, ctx->ev_fork, 0));
+      CK(cudaMemsetAsync(ctx->d_fk, 0, nf * sizeof(double), ks));
+      PROFS("phase_tables", ks, k_phase_tables_mixed(LK, kk, r_dev, (float2*)ctx->d_tab, ctx->d_qfix));
+      PROFS("ewald_sk", ks, k_sk_gemm_mixed(LK, kk, (const float2*)ctx->d_tab, (float2*)ctx->d_part));
+      PROFS("ewald_sk_reduce", ks, k_sk_reduce_mixed(LK, kk, (const float2*)ctx->d_part, measure));
+      PROFS("ewald_kforce", ks, k_kf_gemm_mixed(LK, kk, (const float2*)ctx->d_tab));
+      CK(cudaEventRecord(ctx->ev_join, ks));
+    }
     PROF("gather", k_gather_mixed(L, ns, r_dev, ctx->d_order, ctx->d_kind, ctx->d_mol, ctx->L[0],
                                   ctx->L[1], ctx->L[2], ctx->d_pj));
     if (ctx->polar) PROF("gather", k_gather_drude(L, ns, r_dev, ctx->d_order, ctx->d_pdj, nullptr));
@@ -717,12 +751,15 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
       }
       PROF("pair_mixed", k_pair_list_mixed(L, pa, la, ctx->d_pj, ctx->d_ptabf, ctx->d_erd,
                                            ctx->d_eru, measure, ctx->polar));
-      nerows = list_blocks(ns);
+      nerows = list_blocks(ns, true);
     } else {
       PROF("pair_mixed", k_pair_mixed(L, pa, ctx->d_pj, ctx->d_ptabf, ctx->d_erd, ctx->d_eru,
                                       measure, ctx->polar));
     }
-    if (ctx->nq > 0) {
+    if (fork) {
+      CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
+      PROF("ewald_kforce", k_add_forces(L, nf, ctx->d_fk, f_dev));
+    } else if (ctx->nq > 0) {
       PROF("phase_tables", k_phase_tables_mixed(L, ka, r_dev, (float2*)ctx->d_tab, ctx->d_qfix));
       PROF("ewald_sk", k_sk_gemm_mixed(L, ka, (const float2*)ctx->d_tab, (float2*)ctx->d_part));
       PROF("ewald_sk_reduce", k_sk_reduce_mixed(L, ka, (const float2*)ctx->d_part, measure));
@@ -742,7 +779,7 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
       }
       PROF("pair_fp64", k_pair_list_fp64(L, pa, la, ctx->d_pd, ctx->d_ptabd, ctx->d_ert, measure,
                                          ctx->polar));
-      nerows = list_blocks(ns);
+      nerows = list_blocks(ns, false);
     } else {
       PROF("pair_fp64", k_pair_fp64(L, pa, ctx->d_pd, ctx->d_ptabd, ctx->d_ert, measure,
                                     ctx->polar));
@@ -909,7 +946,7 @@ int mg_destroy(mg_ctx* ctx) {
                   ctx->d_nlist, ctx->d_ncount, ctx->d_rbuild, ctx->d_dmax,
                   ctx->d_wtabf, ctx->d_wtabd, ctx->d_wgeom, ctx->d_wpart, ctx->d_wbox,
                   ctx->d_qfix, ctx->d_adjtab, ctx->d_ag, ctx->d_aq, ctx->d_apart, ctx->d_adEq,
-                  ctx->d_adLq, ctx->d_ags, ctx->d_atpart, ctx->d_aT};
+                  ctx->d_adLq, ctx->d_ags, ctx->d_atpart, ctx->d_aT, ctx->d_fk};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ctx->h_sums) cudaFreeHost(ctx->h_sums);
@@ -917,6 +954,9 @@ int mg_destroy(mg_ctx* ctx) {
   if (ctx->ev_dmax) cudaEventDestroy(ctx->ev_dmax);
   for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  if (ctx->kstream) cudaStreamDestroy(ctx->kstream);
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
   delete ctx;
   return MG_OK;
 }
@@ -1487,6 +1527,12 @@ int mg_selffield(mg_ctx* ctx, double* r, double* f, double omega, int measure, m
   return MG_OK;
 }
 
+int mg_set_overlap(mg_ctx* ctx, int on) {
+  if (!ctx) return MG_ERR_ARG;
+  ctx->overlap = on != 0;
+  return MG_OK;
+}
+
 int mg_set_stream(mg_ctx* ctx, void* stream) {
   if (!ctx) return MG_ERR_ARG;
   CK(cudaStreamSynchronize(ctx->stream));
@@ -1654,6 +1700,7 @@ mg_batch* mg_batch_create(int nbox, const mg_topology* tops, const mg_params* pa
       return nullptr;
     }
     c->stream = b->lanes[i % nl];
+    c->overlap = false;
     b->box.push_back(c);
   }
   *st = MG_OK;

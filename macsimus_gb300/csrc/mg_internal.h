@@ -136,6 +136,7 @@ struct KArgs {
   const int* qdrude;        // [nq] 1 if the charge is a Drude charge (or NULL)
   int ns;
 };
+cudaError_t k_add_forces(const Launch& L, size_t n, const double* fk, double* f);
 // qf: [nq] scratch for the charges' fixed-point coordinates
 cudaError_t k_phase_tables_mixed(const Launch& L, const KArgs& a, const double* r, float2* tab,
                                  uint4* qf);
@@ -179,12 +180,14 @@ struct ListArgs {
   float sx, sy, sz;              // fixed-point -> A
   float rlist2;                  // (cutoff+skin)^2
   int cap;                       // list capacity per site
-  long pitch;                    // column stride of nlist
-  int* nlist;                    // [cap*pitch]
+  long pitch;                    // row stride of nlist (= cap)
+  int* nlist;                    // [ns*cap]: entry k of sorted site t at t*cap + k
   int* ncount;                   // [ns]
   int* status;                   // bit 4: capacity exceeded
 };
-cudaError_t k_build_list(const Launch& L, const ListArgs& a, const int4* pj);
+// cell_of: [ns] cell of every sorted site (the sorted cell keys)
+cudaError_t k_build_list(const Launch& L, const ListArgs& a, int ns, const int* cell_of,
+                         const int4* pj);
 cudaError_t k_save_build(const Launch& L, int ns, const double* r, double* rb);
 cudaError_t k_check_skin(const Launch& L, int ns, const double* r, const double* rb, double lim2,
                          int* status, int* dmax);
@@ -194,7 +197,7 @@ cudaError_t k_pair_list_mixed(const Launch& L, const PairArgs& a, const ListArgs
 cudaError_t k_pair_list_fp64(const Launch& L, const PairArgs& a, const ListArgs& l,
                              const double4* pd, const PairD* ptab, const double* ertab,
                              bool measure, bool polar);
-int list_blocks(int ns);
+int list_blocks(int ns, bool mixed);  // CTAs of the list pair kernels
 
 // Drude sites (mg_drude.cu)
 struct DrudeArgs {

@@ -565,6 +565,18 @@ cudaError_t k_gather_drude(const Launch& L, int ns, const double* r, const int* 
 
 // Row of charge j: [q e^{2 pi i kx sx}, kx=0..Kx | e^{2 pi i ky sy}, ky=-Ky..Ky |
 //                   e^{2 pi i kz sz}, kz=-Kz..Kz]
+// f += fk (the k-space forces of the concurrent chain)
+__global__ void add_forces_kernel(size_t n, const double* __restrict__ fk, double* __restrict__ f) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) f[i] += fk[i];
+}
+
+cudaError_t k_add_forces(const Launch& L, size_t n, const double* fk, double* f) {
+  add_forces_kernel<<<(unsigned)((n + 255) / 256), 256, 0, L.s>>>(n, fk, f);
+  LAUNCHED(L);
+  return cudaGetLastError();
+}
+
 // fixed-point coordinates of every charge (Drude charges at r + rpol)
 __global__ void charge_fixed_kernel(KArgs a, const double* __restrict__ r, uint4* __restrict__ qf) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -882,6 +894,20 @@ cudaError_t k_reduce_sum(const Launch& L, const double* part, int nrows, int wid
 // VERLET=3, no thermostat), one thread per molecule, FP64.
 constexpr int SH_THREADS = 128;
 
+// three-site, three-constraint molecules (rigid water) with the positions in
+// registers: the same sweeps, in the same order and with the same roundings,
+// as the general path below (which works on the global array p)
+__device__ __forceinline__ double3 sh_get(int k, const double3& a, const double3& b,
+                                          const double3& c) {
+  return k == 0 ? a : (k == 1 ? b : c);
+}
+__device__ __forceinline__ void sh_add(int k, double3& a, double3& b, double3& c, double s,
+                                       double x, double y, double z) {
+  if (k == 0) { a.x += s * x; a.y += s * y; a.z += s * z; }
+  else if (k == 1) { b.x += s * x; b.y += s * y; b.z += s * z; }
+  else { c.x += s * x; c.y += s * y; c.z += s * z; }
+}
+
 __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
   __shared__ double red[SH_THREADS];
   const int n = blockIdx.x * SH_THREADS + threadIdx.x;
@@ -889,6 +915,73 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
   if (n < a.nmol) {
     const int i0 = a.mol_first[n], i1 = a.mol_first[n + 1];
     const int c0 = a.mol_cfirst[n], c1 = a.mol_cfirst[n + 1];
+    if (i1 - i0 == 3 && c1 - c0 == 3) {
+      double3 P[3], R[3];
+      double im[3];
+#pragma unroll
+      for (int s = 0; s < 3; s++) {
+        const int i = i0 + s;
+        R[s] = make_double3(a.r[3 * i], a.r[3 * i + 1], a.r[3 * i + 2]);
+        im[s] = a.imass[i];
+        P[s] = make_double3(a.f[3 * i] * (a.hh * im[s]) + R[s].x + a.r1[3 * i],
+                            a.f[3 * i + 1] * (a.hh * im[s]) + R[s].y + a.r1[3 * i + 1],
+                            a.f[3 * i + 2] * (a.hh * im[s]) + R[s].z + a.r1[3 * i + 2]);
+      }
+      int ci[3], cj[3];
+      double bq[3], rx[3], ry[3], rz[3], mi[3], mj[3];
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        const int2 ij = a.cons[c0 + q];
+        ci[q] = ij.x - i0;
+        cj[q] = ij.y - i0;
+        bq[q] = a.bondq[c0 + q];
+        mi[q] = a.imass[ij.x];
+        mj[q] = a.imass[ij.y];
+        const double3 ri = sh_get(ci[q], R[0], R[1], R[2]), rj = sh_get(cj[q], R[0], R[1], R[2]);
+        rx[q] = ri.x - rj.x;
+        ry[q] = ri.y - rj.y;
+        rz[q] = ri.z - rj.z;
+      }
+      int it = 0;
+      double maxsq;
+      do {
+        it++;
+        maxsq = 0;
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+          const double3 pi = sh_get(ci[q], P[0], P[1], P[2]), pj = sh_get(cj[q], P[0], P[1], P[2]);
+          const double px = pi.x - pj.x, py = pi.y - pj.y, pz = pi.z - pj.z;
+          double sq = bq[q] - (px * px + py * py + pz * pz);
+          maxsq = fmax(maxsq, fabs(sq / bq[q]));
+          sq *= a.omega / (mi[q] + mj[q]);
+          sq /= bq[q];
+          const double sx = rx[q] * sq, sy = ry[q] * sq, sz = rz[q] * sq;
+          sh_add(ci[q], P[0], P[1], P[2], mi[q], sx, sy, sz);
+          sh_add(cj[q], P[0], P[1], P[2], -mj[q], sx, sy, sz);
+        }
+      } while (maxsq > a.eps && it < a.maxit);
+      if (maxsq > a.eps) atomicOr(a.status, 1);
+#pragma unroll
+      for (int s = 0; s < 3; s++) {
+        const int i = i0 + s;
+        const double v1x = a.r1[3 * i], v1y = a.r1[3 * i + 1], v1z = a.r1[3 * i + 2];
+        const double v2x = P[s].x - R[s].x, v2y = P[s].y - R[s].y, v2z = P[s].z - R[s].z;
+        double v1s = 0, v2s = 0;
+        v1s += v1x * v1x;
+        v2s += v2x * v2x;
+        v1s += v1y * v1y;
+        v2s += v2y * v2y;
+        v1s += v1z * v1z;
+        v2s += v2z * v2z;
+        kin += (v1s + v2s) * a.mass[i];
+        a.r1[3 * i] = v2x;
+        a.r1[3 * i + 1] = v2y;
+        a.r1[3 * i + 2] = v2z;
+        a.r[3 * i] = P[s].x;
+        a.r[3 * i + 1] = P[s].y;
+        a.r[3 * i + 2] = P[s].z;
+      }
+    } else {
     double* p = a.p;
     for (int i = i0; i < i1; i++)
       for (int k = 0; k < 3; k++)
@@ -932,6 +1025,7 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
         a.r[3 * i + k] = p[3 * i + k];
       }
       kin += (v1s + v2s) * a.mass[i];
+    }
     }
   }
   red[threadIdx.x] = kin;

@@ -7,67 +7,67 @@
 // more than skin/2 since the build; a kernel checks that every step and
 // raises a status bit otherwise.
 //
-// Lists are stored column-major, entry k of sorted site t at
-// nlist[k*pitch + t], so that a warp of consecutive sites reads consecutive
-// words.  Entries are sorted-site indices; sites keep their sorted slot (and
-// the fixed-point/FP64 gathers reuse the build's order) until the next build.
+// Lists are stored row-major, entry k of sorted site t at nlist[t*cap + k],
+// so that the warp that walks site t's list reads consecutive words.
+// Entries are sorted-site indices; sites keep their sorted slot (and the
+// fixed-point/FP64 gathers reuse the build's order) until the next build.
 #include "mg_internal.h"
 #include "mg_device.cuh"
 
 namespace mg {
 
-constexpr int NB_THREADS = 32;  // one warp per home cell: deterministic list order
+constexpr int NB_THREADS = 128;
+constexpr int NB_WARPS = NB_THREADS / 32;
 
-// One warp per home cell; lane = home site (chunks of 32).  Candidates come
-// from the stencil cells of the build grid; kept if |d| < cutoff+skin.
+// One warp per sorted site: the lanes take 32 candidates of a stencil cell
+// at a time (the cell's sites are contiguous in the sorted order), and the
+// ones within cutoff+skin are compacted with a ballot and appended to the
+// site's row in one coalesced store.  Entry order: stencil order, then
+// sorted order within a cell (deterministic).
 __global__ void __launch_bounds__(NB_THREADS)
-    build_list_kernel(ListArgs a, const int4* __restrict__ pj) {
-  __shared__ int4 sj[32];
-  const int lane = threadIdx.x;
-  const int c = blockIdx.x;
+    build_list_kernel(ListArgs a, int ns, const int* __restrict__ cell_of,
+                      const int4* __restrict__ pj) {
+  const int lane = threadIdx.x & 31;
+  const int ti = blockIdx.x * NB_WARPS + (threadIdx.x >> 5);
+  if (ti >= ns) return;
+  const int c = cell_of[ti];
   const int cz = c % a.ncz, cy = (c / a.ncz) % a.ncy, cx = c / (a.ncy * a.ncz);
-  const int i0 = a.cell_start[c], ni = a.cell_start[c + 1] - i0;
-  for (int ib = 0; ib < ni; ib += 32) {
-    const bool vi = ib + lane < ni;
-    const int ti = i0 + ib + lane;
-    const int4 me = vi ? pj[ti] : make_int4(0, 0, 0, 0);
-    int cnt = 0;
-    for (int s = 0; s < a.nstencil; s++) {
-      const int4 o = a.stencil[s];
-      int x2 = cx + o.x, y2 = cy + o.y, z2 = cz + o.z;
-      x2 += (x2 < 0) ? a.ncx : (x2 >= a.ncx ? -a.ncx : 0);
-      y2 += (y2 < 0) ? a.ncy : (y2 >= a.ncy ? -a.ncy : 0);
-      z2 += (z2 < 0) ? a.ncz : (z2 >= a.ncz ? -a.ncz : 0);
-      const int c2 = (x2 * a.ncy + y2) * a.ncz + z2;
-      const int j0 = a.cell_start[c2], nj = a.cell_start[c2 + 1] - j0;
-      for (int jb = 0; jb < nj; jb += 32) {
-        if (jb + lane < nj) sj[lane] = pj[j0 + jb + lane];
-        __syncwarp();
-        const int n = min(32, nj - jb);
-        for (int jj = 0; jj < n; jj++) {
-          const int4 q = sj[jj];
-          const float dx = (float)(int)((unsigned)me.x - (unsigned)q.x) * a.sx;
-          const float dy = (float)(int)((unsigned)me.y - (unsigned)q.y) * a.sy;
-          const float dz = (float)(int)((unsigned)me.z - (unsigned)q.z) * a.sz;
-          const float rr = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          const int tj = j0 + jb + jj;
-          if (vi && rr < a.rlist2 && tj != ti) {
-            if (cnt < a.cap) a.nlist[(long)cnt * a.pitch + ti] = tj;
-            cnt++;
-          }
-        }
-        __syncwarp();
+  const int4 me = pj[ti];
+  int* row = a.nlist + (long)ti * a.cap;
+  int cnt = 0;
+  for (int s = 0; s < a.nstencil; s++) {
+    const int4 o = a.stencil[s];
+    int x2 = cx + o.x, y2 = cy + o.y, z2 = cz + o.z;
+    x2 += (x2 < 0) ? a.ncx : (x2 >= a.ncx ? -a.ncx : 0);
+    y2 += (y2 < 0) ? a.ncy : (y2 >= a.ncy ? -a.ncy : 0);
+    z2 += (z2 < 0) ? a.ncz : (z2 >= a.ncz ? -a.ncz : 0);
+    const int c2 = (x2 * a.ncy + y2) * a.ncz + z2;
+    const int j0 = a.cell_start[c2], j1 = a.cell_start[c2 + 1];
+    for (int jb = j0; jb < j1; jb += 32) {
+      const int tj = jb + lane;
+      bool in = false;
+      if (tj < j1 && tj != ti) {
+        const int4 q = pj[tj];
+        const float dx = (float)(int)((unsigned)me.x - (unsigned)q.x) * a.sx;
+        const float dy = (float)(int)((unsigned)me.y - (unsigned)q.y) * a.sy;
+        const float dz = (float)(int)((unsigned)me.z - (unsigned)q.z) * a.sz;
+        in = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < a.rlist2;
       }
+      const unsigned m = __ballot_sync(0xffffffffu, in);
+      const int pos = cnt + __popc(m & ((1u << lane) - 1u));
+      if (in && pos < a.cap) row[pos] = tj;
+      cnt += __popc(m);
     }
-    if (vi) {
-      a.ncount[ti] = min(cnt, a.cap);
-      if (cnt > a.cap) atomicOr(a.status, 16);
-    }
+  }
+  if (lane == 0) {
+    a.ncount[ti] = min(cnt, a.cap);
+    if (cnt > a.cap) atomicOr(a.status, 16);
   }
 }
 
-cudaError_t k_build_list(const Launch& L, const ListArgs& a, const int4* pj) {
-  build_list_kernel<<<a.ncx * a.ncy * a.ncz, NB_THREADS, 0, L.s>>>(a, pj);
+cudaError_t k_build_list(const Launch& L, const ListArgs& a, int ns, const int* cell_of,
+                         const int4* pj) {
+  build_list_kernel<<<(ns + NB_WARPS - 1) / NB_WARPS, NB_THREADS, 0, L.s>>>(a, ns, cell_of, pj);
   ++*L.counter;
   return cudaGetLastError();
 }
@@ -119,10 +119,13 @@ cudaError_t k_check_skin(const Launch& L, int ns, const double* r, const double*
 // --------------------------------------------------------- list kernels --
 
 constexpr int NL_THREADS = 128;
-constexpr int NL_FOLD = 64;  // neighbours per FP32 force batch before the FP64 fold
+constexpr int NL_WARPS = NL_THREADS / 32;
 
-// Mixed precision pair sum over the lists: one thread per sorted site.
-// Same pair arithmetic as pair_mixed_kernel (cook/ljqqnp.c, ljqqpol.c).
+// Mixed precision pair sum over the lists: one warp per sorted site, the
+// lanes walk its list 32 entries at a time (coalesced list reads, every lane
+// busy); per-lane FP32 sums (FP64 for the excluded intramolecular terms),
+// reduced over the warp in FP64.  Same pair arithmetic as pair_mixed_kernel
+// (cook/ljqqnp.c, ljqqpol.c).
 template <bool MEASURE, bool POLAR>
 __global__ void __launch_bounds__(NL_THREADS)
     pair_list_mixed_kernel(PairArgs a, ListArgs l, const int4* __restrict__ pj,
@@ -134,122 +137,120 @@ __global__ void __launch_bounds__(NL_THREADS)
   const int nk = a.nkind, ntab = a.ntab;
   for (int t = threadIdx.x; t < nk * nk; t += NL_THREADS) ptab[t] = ptab_g[t];
   __syncthreads();
-  const int ti = blockIdx.x * NL_THREADS + threadIdx.x;
-  const bool vi = ti < a.ns;
+  const int lane = threadIdx.x & 31;
+  const int ti = blockIdx.x * NL_WARPS + (threadIdx.x >> 5);
   double en[NEN];
 #pragma unroll
   for (int k = 0; k < NEN; k++) en[k] = 0;
-  if (vi) {
+  if (ti < a.ns) {
     const int4 me = pj[ti];
     const float4 md = POLAR ? a.pdj[ti] : make_float4(0.f, 0.f, 0.f, 0.f);
     const int kind_i = me.w & 255, mol_i = me.w >> 8;
     const int cnt = l.ncount[ti];
+    const int* row = l.nlist + (long)ti * l.cap;
     double fx = 0, fy = 0, fz = 0, gx = 0, gy = 0, gz = 0;
     float ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;
     float e_el = 0, e_lj = 0, e_vir = 0;
     PvF pv;
     pv.zero();
     const PairF* prow = ptab + kind_i * nk;
-    for (int k0 = 0; k0 < cnt; k0 += NL_FOLD) {
-      const int k1 = min(cnt, k0 + NL_FOLD);
-      for (int k = k0; k < k1; k++) {
-        const int tj = l.nlist[(long)k * l.pitch + ti];
-        const int4 q = pj[tj];
-        const float dx = (float)(int)((unsigned)me.x - (unsigned)q.x) * sx;
-        const float dy = (float)(int)((unsigned)me.y - (unsigned)q.y) * sy;
-        const float dz = (float)(int)((unsigned)me.z - (unsigned)q.z) * sz;
-        const float rr = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        if (rr >= cq) continue;
-        const PairF P = prow[q.w & 255];
-        float4 qd = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (POLAR) qd = a.pdj[tj];
-        if ((q.w >> 8) == mol_i) {
-          if (P.qq != 0.f) excl_acc<MEASURE>(dx, dy, dz, P.qqd, alpha, fx, fy, fz, en);
-          if (POLAR) {
-            if (P.qpc != 0.f)
-              excl_acc<MEASURE>(dx + md.x, dy + md.y, dz + md.z, P.qpcd, alpha, gx, gy, gz, en);
-            if (P.qcp != 0.f)
-              excl_acc<MEASURE>(dx - qd.x, dy - qd.y, dz - qd.z, P.qcpd, alpha, fx, fy, fz, en);
-            if (P.qpp != 0.f)
-              excl_acc<MEASURE>(dx + md.x - qd.x, dy + md.y - qd.y, dz + md.z - qd.z, P.qppd,
-                                  alpha, gx, gy, gz, en);
-          }
-          continue;
-        }
-        float f = 0;
-        if (rr < P.C2q) {
-          float U;
-          if (rr < P.C1q) {
-            const float x = P.Sq / rr, y = x * x * x;
-            f = P.E24 * fmaf(2.f * y, y, -y) * x;
-            U = P.E4 * fmaf(y, y, -y);
-          } else {
-            const float x = rr - P.C2q;
-            f = P.A4 * x;
-            U = P.A * x * x;
-          }
-          if (MEASURE) {
-            e_lj += U;
-            e_vir += rr * f;
-          }
-        }
-        if (P.qq != 0.f) f += spline_term<MEASURE>(erd, eru, rr, sgrid, ntab, P.qq, e_el);
-        ax = fmaf(f, dx, ax);
-        ay = fmaf(f, dy, ay);
-        az = fmaf(f, dz, az);
-        if (MEASURE) pv.add(dx, dy, dz, f);
+    for (int k = lane; k < cnt; k += 32) {
+      const int tj = row[k];
+      const int4 q = pj[tj];
+      const float dx = (float)(int)((unsigned)me.x - (unsigned)q.x) * sx;
+      const float dy = (float)(int)((unsigned)me.y - (unsigned)q.y) * sy;
+      const float dz = (float)(int)((unsigned)me.z - (unsigned)q.z) * sz;
+      const float rr = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      if (rr >= cq) continue;
+      const PairF P = prow[q.w & 255];
+      float4 qd = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (POLAR) qd = a.pdj[tj];
+      if ((q.w >> 8) == mol_i) {
+        if (P.qq != 0.f) excl_acc<MEASURE>(dx, dy, dz, P.qqd, alpha, fx, fy, fz, en);
         if (POLAR) {
-          if (P.qpc != 0.f) {
-            const float ex = dx + md.x, ey = dy + md.y, ez = dz + md.z;
-            const float fp = spline_term<MEASURE>(erd, eru, fmaf(ex, ex, fmaf(ey, ey, ez * ez)),
-                                                    sgrid, ntab, P.qpc, e_el);
-            bx = fmaf(fp, ex, bx);
-            by = fmaf(fp, ey, by);
-            bz = fmaf(fp, ez, bz);
-            if (MEASURE) pv.add(ex, ey, ez, fp);
-          }
-          if (P.qcp != 0.f) {
-            const float ex = dx - qd.x, ey = dy - qd.y, ez = dz - qd.z;
-            const float fp = spline_term<MEASURE>(erd, eru, fmaf(ex, ex, fmaf(ey, ey, ez * ez)),
-                                                    sgrid, ntab, P.qcp, e_el);
-            ax = fmaf(fp, ex, ax);
-            ay = fmaf(fp, ey, ay);
-            az = fmaf(fp, ez, az);
-            if (MEASURE) pv.add(ex, ey, ez, fp);
-          }
-          if (P.qpp != 0.f) {
-            const float ex = dx + md.x - qd.x, ey = dy + md.y - qd.y, ez = dz + md.z - qd.z;
-            const float fp = spline_term<MEASURE>(erd, eru, fmaf(ex, ex, fmaf(ey, ey, ez * ez)),
-                                                    sgrid, ntab, P.qpp, e_el);
-            bx = fmaf(fp, ex, bx);
-            by = fmaf(fp, ey, by);
-            bz = fmaf(fp, ez, bz);
-            if (MEASURE) pv.add(ex, ey, ez, fp);
-          }
+          if (P.qpc != 0.f)
+            excl_acc<MEASURE>(dx + md.x, dy + md.y, dz + md.z, P.qpcd, alpha, gx, gy, gz, en);
+          if (P.qcp != 0.f)
+            excl_acc<MEASURE>(dx - qd.x, dy - qd.y, dz - qd.z, P.qcpd, alpha, fx, fy, fz, en);
+          if (P.qpp != 0.f)
+            excl_acc<MEASURE>(dx + md.x - qd.x, dy + md.y - qd.y, dz + md.z - qd.z, P.qppd,
+                              alpha, gx, gy, gz, en);
+        }
+        continue;
+      }
+      float f = 0;
+      if (rr < P.C2q) {
+        float U;
+        if (rr < P.C1q) {
+          const float x = __fdividef(P.Sq, rr), y = x * x * x;
+          f = P.E24 * fmaf(2.f * y, y, -y) * x;
+          U = P.E4 * fmaf(y, y, -y);
+        } else {
+          const float x = rr - P.C2q;
+          f = P.A4 * x;
+          U = P.A * x * x;
+        }
+        if (MEASURE) {
+          e_lj += U;
+          e_vir += rr * f;
         }
       }
-      fx += ax; fy += ay; fz += az;
-      ax = ay = az = 0;
+      if (P.qq != 0.f) f += spline_term<MEASURE>(erd, eru, rr, sgrid, ntab, P.qq, e_el);
+      ax = fmaf(f, dx, ax);
+      ay = fmaf(f, dy, ay);
+      az = fmaf(f, dz, az);
+      if (MEASURE) pv.add(dx, dy, dz, f);
       if (POLAR) {
-        gx += bx; gy += by; gz += bz;
-        bx = by = bz = 0;
-      }
-      if (MEASURE) {
-        en[0] += e_el; en[1] += e_lj; en[2] += e_vir;
-        en[3] += pv.p0; en[4] += pv.p1; en[5] += pv.p2;
-        en[6] += pv.p3; en[7] += pv.p4; en[8] += pv.p5;
-        e_el = e_lj = e_vir = 0;
-        pv.zero();
+        if (P.qpc != 0.f) {
+          const float ex = dx + md.x, ey = dy + md.y, ez = dz + md.z;
+          const float fp = spline_term<MEASURE>(erd, eru, fmaf(ex, ex, fmaf(ey, ey, ez * ez)),
+                                                sgrid, ntab, P.qpc, e_el);
+          bx = fmaf(fp, ex, bx);
+          by = fmaf(fp, ey, by);
+          bz = fmaf(fp, ez, bz);
+          if (MEASURE) pv.add(ex, ey, ez, fp);
+        }
+        if (P.qcp != 0.f) {
+          const float ex = dx - qd.x, ey = dy - qd.y, ez = dz - qd.z;
+          const float fp = spline_term<MEASURE>(erd, eru, fmaf(ex, ex, fmaf(ey, ey, ez * ez)),
+                                                sgrid, ntab, P.qcp, e_el);
+          ax = fmaf(fp, ex, ax);
+          ay = fmaf(fp, ey, ay);
+          az = fmaf(fp, ez, az);
+          if (MEASURE) pv.add(ex, ey, ez, fp);
+        }
+        if (P.qpp != 0.f) {
+          const float ex = dx + md.x - qd.x, ey = dy + md.y - qd.y, ez = dz + md.z - qd.z;
+          const float fp = spline_term<MEASURE>(erd, eru, fmaf(ex, ex, fmaf(ey, ey, ez * ez)),
+                                                sgrid, ntab, P.qpp, e_el);
+          bx = fmaf(fp, ex, bx);
+          by = fmaf(fp, ey, by);
+          bz = fmaf(fp, ez, bz);
+          if (MEASURE) pv.add(ex, ey, ez, fp);
+        }
       }
     }
-    const int site = a.order[ti];
-    a.f[3 * site] = fx;
-    a.f[3 * site + 1] = fy;
-    a.f[3 * site + 2] = fz;
-    if (POLAR) {
-      a.f[3 * (long)a.ns + 3 * site] = gx;
-      a.f[3 * (long)a.ns + 3 * site + 1] = gy;
-      a.f[3 * (long)a.ns + 3 * site + 2] = gz;
+    if (MEASURE) {
+      en[0] += e_el; en[1] += e_lj; en[2] += e_vir;
+      en[3] += pv.p0; en[4] += pv.p1; en[5] += pv.p2;
+      en[6] += pv.p3; en[7] += pv.p4; en[8] += pv.p5;
+    }
+    // the site's force: lane sums (about cnt/32 terms each) reduced in FP64
+    double v[6] = {fx + ax, fy + ay, fz + az, gx + bx, gy + by, gz + bz};
+#pragma unroll
+    for (int d = 0; d < (POLAR ? 6 : 3); d++)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[d] += __shfl_xor_sync(0xffffffffu, v[d], o);
+    if (lane == 0) {
+      const int site = a.order[ti];
+      a.f[3 * site] = v[0];
+      a.f[3 * site + 1] = v[1];
+      a.f[3 * site + 2] = v[2];
+      if (POLAR) {
+        a.f[3 * (long)a.ns + 3 * site] = v[3];
+        a.f[3 * (long)a.ns + 3 * site + 1] = v[4];
+        a.f[3 * (long)a.ns + 3 * site + 2] = v[5];
+      }
     }
   }
   if (MEASURE) {
@@ -269,7 +270,7 @@ __global__ void __launch_bounds__(NL_THREADS)
 cudaError_t k_pair_list_mixed(const Launch& L, const PairArgs& a, const ListArgs& l,
                               const int4* pj, const PairF* ptab, const float4* erd,
                               const float4* eru, bool measure, bool polar) {
-  const int grid = (a.ns + NL_THREADS - 1) / NL_THREADS;
+  const int grid = list_blocks(a.ns, true);
   const float sx = (float)(a.Lx / 4294967296.0), sy = (float)(a.Ly / 4294967296.0),
               sz = (float)(a.Lz / 4294967296.0);
   const float cq = (float)a.cutoff_sq, sg = (float)a.sgrid, al = (float)a.alpha;
@@ -311,7 +312,7 @@ __global__ void __launch_bounds__(NL_THREADS)
     const int cnt = l.ncount[ti];
     double fx = 0, fy = 0, fz = 0, gx = 0, gy = 0, gz = 0;
     for (int k = 0; k < cnt; k++) {
-      const int tj = l.nlist[(long)k * l.pitch + ti];
+      const int tj = l.nlist[(long)ti * l.cap + k];
       const double4 q = pd[tj];
       double dx = me.x - q.x, dy = me.y - q.y, dz = me.z - q.z;
       dx -= a.Lx * rint(dx / a.Lx);
@@ -404,6 +405,8 @@ cudaError_t k_pair_list_fp64(const Launch& L, const PairArgs& a, const ListArgs&
   return cudaGetLastError();
 }
 
-int list_blocks(int ns) { return (ns + NL_THREADS - 1) / NL_THREADS; }
+int list_blocks(int ns, bool mixed) {
+  return mixed ? (ns + NL_WARPS - 1) / NL_WARPS : (ns + NL_THREADS - 1) / NL_THREADS;
+}
 
 }  // namespace mg
