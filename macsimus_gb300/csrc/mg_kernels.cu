@@ -896,7 +896,9 @@ constexpr int SH_THREADS = 128;
 
 // three-site, three-constraint molecules (rigid water) with the positions in
 // registers: the same sweeps, in the same order and with the same roundings,
-// as the general path below (which works on the global array p)
+// as the general path below (which works on the global array p).  The
+// per-constraint factors omega/(m_i^-1 + m_j^-1)/d^2 and 1/d^2 are formed
+// once per call: FP64 divisions are slow on this GPU.
 __device__ __forceinline__ double3 sh_get(int k, const double3& a, const double3& b,
                                           const double3& c) {
   return k == 0 ? a : (k == 1 ? b : c);
@@ -928,7 +930,7 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
                             a.f[3 * i + 2] * (a.hh * im[s]) + R[s].z + a.r1[3 * i + 2]);
       }
       int ci[3], cj[3];
-      double bq[3], rx[3], ry[3], rz[3], mi[3], mj[3];
+      double bq[3], ibq[3], wq[3], rx[3], ry[3], rz[3], mi[3], mj[3];
 #pragma unroll
       for (int q = 0; q < 3; q++) {
         const int2 ij = a.cons[c0 + q];
@@ -937,6 +939,8 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
         bq[q] = a.bondq[c0 + q];
         mi[q] = a.imass[ij.x];
         mj[q] = a.imass[ij.y];
+        ibq[q] = 1.0 / bq[q];
+        wq[q] = a.omega / (mi[q] + mj[q]) * ibq[q];
         const double3 ri = sh_get(ci[q], R[0], R[1], R[2]), rj = sh_get(cj[q], R[0], R[1], R[2]);
         rx[q] = ri.x - rj.x;
         ry[q] = ri.y - rj.y;
@@ -951,10 +955,9 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
         for (int q = 0; q < 3; q++) {
           const double3 pi = sh_get(ci[q], P[0], P[1], P[2]), pj = sh_get(cj[q], P[0], P[1], P[2]);
           const double px = pi.x - pj.x, py = pi.y - pj.y, pz = pi.z - pj.z;
-          double sq = bq[q] - (px * px + py * py + pz * pz);
-          maxsq = fmax(maxsq, fabs(sq / bq[q]));
-          sq *= a.omega / (mi[q] + mj[q]);
-          sq /= bq[q];
+          const double d = bq[q] - (px * px + py * py + pz * pz);
+          maxsq = fmax(maxsq, fabs(d) * ibq[q]);
+          const double sq = d * wq[q];
           const double sx = rx[q] * sq, sy = ry[q] * sq, sz = rz[q] * sq;
           sh_add(ci[q], P[0], P[1], P[2], mi[q], sx, sy, sz);
           sh_add(cj[q], P[0], P[1], P[2], -mj[q], sx, sy, sz);
@@ -996,12 +999,12 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
           const int2 ij = a.cons[al];
           const double bq = a.bondq[al];
           const double mi = a.imass[ij.x], mj = a.imass[ij.y];
+          const double ibq = 1.0 / bq, wq = a.omega / (mi + mj) * ibq;
           double px = p[3 * ij.x] - p[3 * ij.y], py = p[3 * ij.x + 1] - p[3 * ij.y + 1],
                  pz = p[3 * ij.x + 2] - p[3 * ij.y + 2];
-          double sq = bq - (px * px + py * py + pz * pz);
-          maxsq = fmax(maxsq, fabs(sq / bq));
-          sq *= a.omega / (mi + mj);
-          sq /= bq;
+          const double d = bq - (px * px + py * py + pz * pz);
+          maxsq = fmax(maxsq, fabs(d) * ibq);
+          const double sq = d * wq;
           const double rx = (a.r[3 * ij.x] - a.r[3 * ij.y]) * sq,
                        ry = (a.r[3 * ij.x + 1] - a.r[3 * ij.y + 1]) * sq,
                        rz = (a.r[3 * ij.x + 2] - a.r[3 * ij.y + 2]) * sq;

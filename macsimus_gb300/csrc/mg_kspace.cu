@@ -574,24 +574,35 @@ __global__ void __launch_bounds__(Q2_THREADS, 2)
     }
     __syncthreads();
   }
-  // sum over the 32 row slots of the warp (FP64), lane 0 stores
+  // sum over the 32 row slots of the warp as compensated FP32 pairs (s, e)
+  // (Knuth's TwoSum), so that only lane 0 touches the slow FP64 pipe
 #pragma unroll
   for (int c = 0; c < 4; c++) {
     double s[3];
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-      double v = (double)F[c][d] + (double)Fc[c][d];
+      float hi = F[c][d], lo = -Fc[c][d];
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      s[d] = v;
+      for (int o = 16; o > 0; o >>= 1) {
+        const float h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+        const float l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+        const float t = hi + h2, bb = t - hi;
+        const float err = (hi - (t - bb)) + (h2 - bb);
+        hi = t;
+        lo = lo + l2 + err;
+      }
+      s[d] = (double)hi + (double)lo;
     }
     const int j = jbase + 4 * tj + c;
     if (tw == 0 && j < a.nq) {
       const int site = a.qsite[j];
       double* fo = a.f + 3 * (long)site + (a.qdrude && a.qdrude[j] ? 3 * (long)a.ns : 0);
-      fo[0] += s[0] / a.Lx;
-      fo[1] += s[1] / a.Ly;
-      fo[2] += s[2] / a.Lz;
+      // the product rounded on its own (no fused multiply-add with the
+      // running force), so that adding to the r-space forces here or in a
+      // separate buffer gives the same bits
+      fo[0] += __dmul_rn(s[0], 1.0 / a.Lx);
+      fo[1] += __dmul_rn(s[1], 1.0 / a.Ly);
+      fo[2] += __dmul_rn(s[2], 1.0 / a.Lz);
     }
   }
 }

@@ -179,3 +179,15 @@ def test_skin_violation_is_reported():
     with pytest.raises(M.MGError) as e:
         fp.md_steps(5)
     assert e.value.code == 8
+
+
+@pytest.mark.parametrize("case", ["spce864", "brine532"])
+def test_concurrent_kspace_chain_gives_identical_forces(case):
+    """the k-space chain on its own stream (default) and serialised give the
+    same forces bit for bit (the k-space part is added once either way)"""
+    g, meta, system, ew, fp = make(case, "mixed")
+    f1, e1 = fp.forces(g["r"][0], measure=True)
+    fp.set_overlap(False)
+    f2, e2 = fp.forces(g["r"][0], measure=True)
+    assert np.array_equal(f1, f2)
+    assert e1["el"] == e2["el"] and e1["lj"] == e2["lj"]
