@@ -158,7 +158,8 @@ def run_ours(args, rank, world, local):
         best = M.autotune(system, [w["L"]] * 3, w["cutoff"], w["alpha"], w["kappa"], w["r"],
                           precision="mixed", **kw)
         tuned = dict(cells_per_cutoff=best["cells_per_cutoff"],
-                     kspace_ctas_per_sm=best["kspace_ctas_per_sm"])
+                     kspace_ctas_per_sm=best["kspace_ctas_per_sm"],
+                     pair_variant=best["pair_variant"])
     fp = M.ForcePath(system, [w["L"]] * 3, w["cutoff"], w["alpha"], w["kappa"], precision="mixed",
                      **kw, **tuned)
     fp.set_stream(stream.cuda_stream)

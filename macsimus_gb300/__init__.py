@@ -52,7 +52,7 @@ class Params(C.Structure):
                 ("omegac", C.c_double), ("shake_maxit", C.c_int),
                 ("cells_per_cutoff", C.c_int), ("aspc_k", C.c_int), ("scf_iter", C.c_int),
                 ("scf_omega", C.c_double), ("minqq", C.c_double), ("skin", C.c_double),
-                ("nl_every", C.c_int), ("kspace_ctas_per_sm", C.c_int)]
+                ("nl_every", C.c_int), ("kspace_ctas_per_sm", C.c_int), ("pair_variant", C.c_int)]
 
 
 class Energy(C.Structure):
@@ -140,17 +140,18 @@ def library():
 
 
 def autotune(system, L, cutoff, alpha, kappa, r, nrep=3, **kw):
-    """the fastest (cells_per_cutoff, kspace_ctas_per_sm) for this box and
-    configuration (mg_autotune); returns them with the 3x3 timing table"""
+    """the fastest (cells_per_cutoff, kspace_ctas_per_sm, pair_variant) for
+    this box and configuration (mg_autotune), with the timings (3x3 grid x
+    split, then the 4 pair variants)"""
     t, p, keep = describe(system, L, cutoff, alpha, kappa, **kw)
-    ms = np.zeros(9)
+    ms = np.zeros(13)
     rr = _arr(r, np.float64).reshape(-1)
     rc = library().mg_autotune(C.byref(t), C.byref(p), rr.ctypes.data_as(_dp), int(nrep),
                                ms.ctypes.data_as(_dp))
     if rc:
         raise MGError(rc, "mg_autotune failed")
     return dict(cells_per_cutoff=p.cells_per_cutoff, kspace_ctas_per_sm=p.kspace_ctas_per_sm,
-                ms=ms.reshape(3, 3))
+                pair_variant=p.pair_variant, ms=ms[:9].reshape(3, 3), ms_pair=ms[9:])
 
 
 def fp32_peak_tflops():
@@ -169,7 +170,7 @@ def _arr(a, dt):
 def describe(system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None, grid=256,
              rshift=3, rplus=2.5, epsinf=3e33, h=0.002, epsc=1e-7, omegac=1.2, shake_maxit=1000,
              cells_per_cutoff=0, aspc_k=2, scf_iter=1, scf_omega=0.6, minqq=1.0, skin=0.0,
-             nl_every=50, kspace_ctas_per_sm=0):
+             nl_every=50, kspace_ctas_per_sm=0, pair_variant=0):
     """(mg_topology, mg_params, arrays to keep alive) of one box"""
     keep = []
 
@@ -230,6 +231,7 @@ def describe(system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None, 
     p.skin = skin
     p.nl_every = nl_every
     p.kspace_ctas_per_sm = kspace_ctas_per_sm
+    p.pair_variant = pair_variant
     return t, p, keep
 
 
@@ -239,7 +241,7 @@ class ForcePath:
     def __init__(self, system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None,
                  grid=256, rshift=3, rplus=2.5, epsinf=3e33, h=0.002, epsc=1e-7, omegac=1.2,
                  shake_maxit=1000, cells_per_cutoff=0, aspc_k=2, scf_iter=1, scf_omega=0.6,
-                 minqq=1.0, skin=0.0, nl_every=50, kspace_ctas_per_sm=0):
+                 minqq=1.0, skin=0.0, nl_every=50, kspace_ctas_per_sm=0, pair_variant=0):
         lib = library()
         self.system = system
         self.ns = system.ns
@@ -249,7 +251,8 @@ class ForcePath:
                                     shake_maxit=shake_maxit, cells_per_cutoff=cells_per_cutoff,
                                     aspc_k=aspc_k, scf_iter=scf_iter, scf_omega=scf_omega,
                                     minqq=minqq, skin=skin, nl_every=nl_every,
-                                    kspace_ctas_per_sm=kspace_ctas_per_sm)
+                                    kspace_ctas_per_sm=kspace_ctas_per_sm,
+                                    pair_variant=pair_variant)
         self.polar = getattr(system, "polar", False)
         Lb = np.broadcast_to(np.asarray(L, dtype=np.float64), (3,))
         st = C.c_int(0)

@@ -89,6 +89,7 @@ struct mg_ctx {
   cudaEvent_t ev_dmax = nullptr;
   bool dmax_pending = false;
   int nepart = 0;
+  int pair_variant = 0;
   // Widom: the type table, the site kinds, sites per type; cell data of the
   // last force evaluation (cook's lastlist)
   int ntypes = 0, comb_rule = 1;
@@ -248,6 +249,7 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   ctx->scf_omega = p->scf_omega > 0 ? p->scf_omega : 0.6;
   ctx->minqq = p->minqq > 0 ? p->minqq : 1.0;
   ctx->use_list = p->skin > 0;
+  ctx->pair_variant = p->pair_variant;
   ctx->skin = p->skin > 0 ? p->skin : 0;
   ctx->nl_every = p->nl_every > 0 ? p->nl_every : 50;
   CK(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
@@ -688,6 +690,8 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
   pa.ntab = ctx->ntab;
   pa.pdj = ctx->d_pdj;
   pa.pdd = ctx->d_pdd;
+  pa.pair_warps = (ctx->pair_variant & 1) ? 8 : 4;
+  pa.spline_smem = (ctx->pair_variant & 2) && ctx->ntab * 16 <= 200 * 1024 ? 1 : 0;
   KArgs ka;
   ka.nq = ctx->nq;
   ka.nk = ctx->nk;
@@ -1377,6 +1381,8 @@ PairArgs pair_args(mg_ctx* ctx) {
   pa.ntab = ctx->ntab;
   pa.pdj = nullptr;
   pa.pdd = nullptr;
+  pa.pair_warps = 4;
+  pa.spline_smem = 0;
   return pa;
 }
 
@@ -1865,6 +1871,39 @@ int mg_autotune(const mg_topology* top, mg_params* par, const double* r, int nre
         bk = kc[b];
       }
     }
+  // the pair-kernel variants at the best grid and split
+  int bv = par->pair_variant;
+  if (!rc && bc) {
+    double bestv = 1e300;
+    for (int v = 0; v < 4 && rc == MG_OK; v++) {
+      mg_params p2 = *par;
+      p2.cells_per_cutoff = bc;
+      p2.kspace_ctas_per_sm = bk;
+      p2.pair_variant = v;
+      int st = 0;
+      mg_ctx* c = mg_create(top, &p2, &st);
+      double t = -1;
+      if (c) {
+        int e = mg_forces_device(c, r_dev, f_dev, 0, nullptr);
+        if (!e) {
+          cudaEventRecord(e0, c->stream);
+          for (int k = 0; k < nrep && !e; k++) e = mg_forces_device(c, r_dev, f_dev, 0, nullptr);
+          cudaEventRecord(e1, c->stream);
+          cudaEventSynchronize(e1);
+          float f = 0;
+          cudaEventElapsedTime(&f, e0, e1);
+          if (!e) t = f / nrep;
+        }
+        if (e) rc = e;
+        mg_destroy(c);
+      }
+      if (ms) ms[9 + v] = t;
+      if (t > 0 && t < bestv) {
+        bestv = t;
+        bv = v;
+      }
+    }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(r_dev);
@@ -1873,5 +1912,6 @@ int mg_autotune(const mg_topology* top, mg_params* par, const double* r, int nre
   if (bc == 0) return MG_ERR_SETUP;
   par->cells_per_cutoff = bc;
   par->kspace_ctas_per_sm = bk;
+  par->pair_variant = bv;
   return MG_OK;
 }

@@ -50,6 +50,20 @@ __device__ __forceinline__ float spline_term(const float4* __restrict__ erd,
   return (__fdividef(d.y, d.z + r2) + d.x) * qq;
 }
 
+// the same through any pointer (LDG: read-only path; else plain loads, e.g.
+// from a copy of the table in shared memory)
+template <bool MEASURE, bool LDG>
+__device__ __forceinline__ float spline_any(const float4* erd, const float4* __restrict__ eru,
+                                            float r2, float sgrid, int ntab, float qq, float& e) {
+  const int ix = min(__float_as_int(fmaf(r2, sgrid, 12582911.5f)) - 0x4B400000, ntab - 1);
+  const float4 d = LDG ? __ldg(erd + ix) : erd[ix];
+  if (MEASURE) {
+    const float4 u = __ldg(eru + ix);
+    e += (__fdividef(u.y, u.z + r2) + u.x) * qq;
+  }
+  return (__fdividef(d.y, d.z + r2) + d.x) * qq;
+}
+
 // excluded intramolecular term: its Ewald correction is large and cancels
 // the self term; evaluated in FP32 (an FP64 erf on a divergent lane would
 // stall the warp on the slow FP64 pipe) and summed into FP64

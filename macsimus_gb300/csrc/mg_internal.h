@@ -104,6 +104,8 @@ struct PairArgs {
   double* epart;            // [nblocks*10] partial energies (measure)
   int ntab;                 // erfc spline intervals (lookups are clamped)
   const float4* pdj;        // mixed, Drude builds: sorted Drude displacements
+  int pair_warps;           // mixed cell kernel: warps per CTA (4 or 8)
+  int spline_smem;          // mixed cell kernel: force spline in shared memory
   const double4* pdd;       // FP64, Drude builds: sorted Drude displacements
 };
 cudaError_t k_pair_mixed(const Launch& L, const PairArgs& a, const int4* pj,

@@ -149,19 +149,26 @@ constexpr int FOLD = 8;   // stencil cells per FP32 force batch before the FP64 
 // box of the home-cell centre, so the image taken is the nearest one for
 // every pair inside the cutoff.  Without REL (one cell: all pairs) each pair
 // takes its nearest image from its own fixed-point difference.
-template <bool MEASURE, bool POLAR, bool REL>
-__global__ void __launch_bounds__(PAIR_THREADS)
+// NW warps per CTA (the autotuner picks 4 or 8); STAB: the force spline in
+// shared memory (dynamic, ntab float4) instead of read through L1.
+template <bool MEASURE, bool POLAR, bool REL, int NW, bool STAB>
+__global__ void __launch_bounds__(NW * 32)
     pair_mixed_kernel(PairArgs a, const int4* __restrict__ pj, const PairF* __restrict__ ptab_g,
-                      const float4* __restrict__ erd, const float4* __restrict__ eru, float sx,
+                      const float4* __restrict__ erd_g, const float4* __restrict__ eru, float sx,
                       float sy, float sz, float cq, float sgrid, float alpha) {
+  constexpr int NT = NW * 32;
+  extern __shared__ float4 s_erd[];
   __shared__ PairF ptab[MAX_KINDS * MAX_KINDS];
-  __shared__ int4 sj[NWARP][32];
-  __shared__ float4 sjd[POLAR ? NWARP : 1][32];
-  __shared__ double red[NWARP][32][POLAR ? 6 : 3];
-  __shared__ double ered[PAIR_THREADS];
+  __shared__ int4 sj[NW][32];
+  __shared__ float4 sjd[POLAR ? NW : 1][32];
+  __shared__ double red[NW][32][POLAR ? 6 : 3];
+  __shared__ double ered[NT];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nk = a.nkind, ntab = a.ntab;
-  for (int t = threadIdx.x; t < nk * nk; t += PAIR_THREADS) ptab[t] = ptab_g[t];
+  for (int t = threadIdx.x; t < nk * nk; t += NT) ptab[t] = ptab_g[t];
+  if (STAB)
+    for (int t = threadIdx.x; t < ntab; t += NT) s_erd[t] = erd_g[t];
+  const float4* erd = STAB ? s_erd : erd_g;
   __syncthreads();
 
   const int c = blockIdx.x;
@@ -190,7 +197,7 @@ __global__ void __launch_bounds__(PAIR_THREADS)
     PvF pv;
     pv.zero();
     int nb = 0;
-    for (int s = warp; s < a.nstencil; s += NWARP) {
+    for (int s = warp; s < a.nstencil; s += NW) {
       const int4 o = a.stencil[s];
       int x2 = cx + o.x, y2 = cy + o.y, z2 = cz + o.z;
       x2 += (x2 < 0) ? a.ncx : (x2 >= a.ncx ? -a.ncx : 0);
@@ -262,7 +269,7 @@ __global__ void __launch_bounds__(PAIR_THREADS)
               e_vir += rr * f;
             }
           }
-          if (P.qq != 0.f) f += spline_term<MEASURE>(erd, eru, rr, sgrid, ntab, P.qq, e_el);
+          if (P.qq != 0.f) f += spline_any<MEASURE, !STAB>(erd, eru, rr, sgrid, ntab, P.qq, e_el);
           ax = fmaf(f, dx, ax);
           ay = fmaf(f, dy, ay);
           az = fmaf(f, dz, az);
@@ -270,7 +277,7 @@ __global__ void __launch_bounds__(PAIR_THREADS)
           if (POLAR) {
             if (P.qpc != 0.f) {  // Drude(i) - centre(j)
               const float ex = dx + md.x, ey = dy + md.y, ez = dz + md.z;
-              const float fp = spline_term<MEASURE>(erd, eru, fmaf(ex, ex, fmaf(ey, ey, ez * ez)),
+              const float fp = spline_any<MEASURE, !STAB>(erd, eru, fmaf(ex, ex, fmaf(ey, ey, ez * ez)),
                                                     sgrid, ntab, P.qpc, e_el);
               bx = fmaf(fp, ex, bx);
               by = fmaf(fp, ey, by);
@@ -279,7 +286,7 @@ __global__ void __launch_bounds__(PAIR_THREADS)
             }
             if (P.qcp != 0.f) {  // centre(i) - Drude(j)
               const float ex = dx - qd.x, ey = dy - qd.y, ez = dz - qd.z;
-              const float fp = spline_term<MEASURE>(erd, eru, fmaf(ex, ex, fmaf(ey, ey, ez * ez)),
+              const float fp = spline_any<MEASURE, !STAB>(erd, eru, fmaf(ex, ex, fmaf(ey, ey, ez * ez)),
                                                     sgrid, ntab, P.qcp, e_el);
               ax = fmaf(fp, ex, ax);
               ay = fmaf(fp, ey, ay);
@@ -288,7 +295,7 @@ __global__ void __launch_bounds__(PAIR_THREADS)
             }
             if (P.qpp != 0.f) {  // Drude(i) - Drude(j)
               const float ex = dx + md.x - qd.x, ey = dy + md.y - qd.y, ez = dz + md.z - qd.z;
-              const float fp = spline_term<MEASURE>(erd, eru, fmaf(ex, ex, fmaf(ey, ey, ez * ez)),
+              const float fp = spline_any<MEASURE, !STAB>(erd, eru, fmaf(ex, ex, fmaf(ey, ey, ez * ez)),
                                                     sgrid, ntab, P.qpp, e_el);
               bx = fmaf(fp, ex, bx);
               by = fmaf(fp, ey, by);
@@ -331,7 +338,7 @@ __global__ void __launch_bounds__(PAIR_THREADS)
     if (warp == 0 && vi) {
       double g[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll
-      for (int w = 0; w < NWARP; w++)
+      for (int w = 0; w < NW; w++)
 #pragma unroll
         for (int k = 0; k < (POLAR ? 6 : 3); k++) g[k] += red[w][lane][k];
       const int site = a.order[ti];
@@ -351,7 +358,7 @@ __global__ void __launch_bounds__(PAIR_THREADS)
     for (int k = 0; k < 9; k++) {
       ered[threadIdx.x] = 0.5 * en[k];
       __syncthreads();
-      for (int w = PAIR_THREADS / 2; w > 0; w >>= 1) {
+      for (int w = NT / 2; w > 0; w >>= 1) {
         if (threadIdx.x < w) ered[threadIdx.x] += ered[threadIdx.x + w];
         __syncthreads();
       }
@@ -367,18 +374,39 @@ cudaError_t k_pair_mixed(const Launch& L, const PairArgs& a, const int4* pj, con
   float sx = (float)(a.Lx / 4294967296.0), sy = (float)(a.Ly / 4294967296.0),
         sz = (float)(a.Lz / 4294967296.0);
   const float cq = (float)a.cutoff_sq, sg = (float)a.sgrid, al = (float)a.alpha;
-#define PAIR_MIXED(M, P, R)                                                                   \
-  pair_mixed_kernel<M, P, R><<<ncell, PAIR_THREADS, 0, L.s>>>(a, pj, ptab, erd, eru, sx, sy, sz, \
-                                                              cq, sg, al)
   const bool rel = !a.allpairs;
+  const int nw = a.pair_warps == 8 ? 8 : 4;
+  const bool stab = a.spline_smem && !measure;
+  const size_t dsm = stab ? sizeof(float4) * (size_t)a.ntab : 0;
+  cudaError_t e = cudaSuccess;
+#define PAIR_MIXED(M, P, R, W, S)                                                               \
+  do {                                                                                          \
+    if (S) e = cudaFuncSetAttribute(pair_mixed_kernel<M, P, R, W, S>,                           \
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);     \
+    if (e == cudaSuccess)                                                                       \
+      pair_mixed_kernel<M, P, R, W, S><<<ncell, W * 32, dsm, L.s>>>(a, pj, ptab, erd, eru, sx,  \
+                                                                     sy, sz, cq, sg, al);       \
+  } while (0)
+#define PAIR_MIXED_W(M, P, R)                              \
+  do {                                                     \
+    if (nw == 8) {                                         \
+      if (stab) PAIR_MIXED(M, P, R, 8, true);              \
+      else PAIR_MIXED(M, P, R, 8, false);                  \
+    } else {                                               \
+      if (stab) PAIR_MIXED(M, P, R, 4, true);              \
+      else PAIR_MIXED(M, P, R, 4, false);                  \
+    }                                                      \
+  } while (0)
   if (polar) {
-    if (measure) { if (rel) PAIR_MIXED(true, true, true); else PAIR_MIXED(true, true, false); }
-    else { if (rel) PAIR_MIXED(false, true, true); else PAIR_MIXED(false, true, false); }
+    if (measure) { if (rel) PAIR_MIXED_W(true, true, true); else PAIR_MIXED_W(true, true, false); }
+    else { if (rel) PAIR_MIXED_W(false, true, true); else PAIR_MIXED_W(false, true, false); }
   } else {
-    if (measure) { if (rel) PAIR_MIXED(true, false, true); else PAIR_MIXED(true, false, false); }
-    else { if (rel) PAIR_MIXED(false, false, true); else PAIR_MIXED(false, false, false); }
+    if (measure) { if (rel) PAIR_MIXED_W(true, false, true); else PAIR_MIXED_W(true, false, false); }
+    else { if (rel) PAIR_MIXED_W(false, false, true); else PAIR_MIXED_W(false, false, false); }
   }
+#undef PAIR_MIXED_W
 #undef PAIR_MIXED
+  if (e != cudaSuccess) return e;
   LAUNCHED(L);
   return cudaGetLastError();
 }
