@@ -107,6 +107,13 @@ typedef struct {
      the erfc force spline in shared memory (else read through L1).
      mg_autotune picks it. */
   int pair_variant;
+  /* thermostat after every SHAKE step (sim/thermo.c): 0 none, 1 Berendsen,
+     2 Bussi (stochastic velocity rescaling); temperature T (K), time
+     constant tau_T (ps), degrees of freedom thermo_f (<=0: 3 ns - nc - 3),
+     seed of the Bussi stream */
+  int thermostat;
+  double T, tau_T, thermo_f;
+  unsigned long long seed;
 } mg_params;
 
 /* Energies of one force evaluation (program units, K).
@@ -173,6 +180,10 @@ int mg_last_launches(const mg_ctx *ctx);
 /* Run the context's work on the given CUDA stream (a cudaStream_t of the
    caller, e.g. a framework's current stream); NULL selects the context's own
    stream again.  No counterpart in the reference (cook has no device). */
+/* factor by which the last thermostat call scaled the velocities (1 if
+   none); a synchronising read */
+double mg_thermostat_factor(mg_ctx *ctx);
+
 /* FP32 path: run the Ewald k-space chain on a second stream beside the
    r-space chain (on by default; off serialises them, e.g. to time kernels
    one by one).  No reference counterpart. */

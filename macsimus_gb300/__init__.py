@@ -52,7 +52,9 @@ class Params(C.Structure):
                 ("omegac", C.c_double), ("shake_maxit", C.c_int),
                 ("cells_per_cutoff", C.c_int), ("aspc_k", C.c_int), ("scf_iter", C.c_int),
                 ("scf_omega", C.c_double), ("minqq", C.c_double), ("skin", C.c_double),
-                ("nl_every", C.c_int), ("kspace_ctas_per_sm", C.c_int), ("pair_variant", C.c_int)]
+                ("nl_every", C.c_int), ("kspace_ctas_per_sm", C.c_int), ("pair_variant", C.c_int),
+                ("thermostat", C.c_int), ("T", C.c_double), ("tau_T", C.c_double),
+                ("thermo_f", C.c_double), ("seed", C.c_ulonglong)]
 
 
 class Energy(C.Structure):
@@ -112,6 +114,8 @@ def library():
         L.mg_selffield.argtypes = [vp, _dp, _dp, C.c_double, C.c_int, C.POINTER(Energy)]
         L.mg_set_stream.argtypes = [vp, vp]
         L.mg_set_overlap.argtypes = [vp, C.c_int]
+        L.mg_thermostat_factor.argtypes = [vp]
+        L.mg_thermostat_factor.restype = C.c_double
         L.mg_profile_enable.argtypes = [vp, C.c_int]
         L.mg_profile_reset.argtypes = [vp]
         L.mg_profile_entry.argtypes = [vp, C.c_int, C.POINTER(C.c_char_p), _dp,
@@ -170,7 +174,8 @@ def _arr(a, dt):
 def describe(system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None, grid=256,
              rshift=3, rplus=2.5, epsinf=3e33, h=0.002, epsc=1e-7, omegac=1.2, shake_maxit=1000,
              cells_per_cutoff=0, aspc_k=2, scf_iter=1, scf_omega=0.6, minqq=1.0, skin=0.0,
-             nl_every=50, kspace_ctas_per_sm=0, pair_variant=0):
+             nl_every=50, kspace_ctas_per_sm=0, pair_variant=0, thermostat=0, T=298.0,
+             tau_T=0.1, thermo_f=0.0, seed=0):
     """(mg_topology, mg_params, arrays to keep alive) of one box"""
     keep = []
 
@@ -232,6 +237,11 @@ def describe(system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None, 
     p.nl_every = nl_every
     p.kspace_ctas_per_sm = kspace_ctas_per_sm
     p.pair_variant = pair_variant
+    p.thermostat = {"none": 0, "berendsen": 1, "bussi": 2}.get(thermostat, thermostat) or 0
+    p.T = T
+    p.tau_T = tau_T
+    p.thermo_f = thermo_f
+    p.seed = seed
     return t, p, keep
 
 
@@ -241,7 +251,8 @@ class ForcePath:
     def __init__(self, system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None,
                  grid=256, rshift=3, rplus=2.5, epsinf=3e33, h=0.002, epsc=1e-7, omegac=1.2,
                  shake_maxit=1000, cells_per_cutoff=0, aspc_k=2, scf_iter=1, scf_omega=0.6,
-                 minqq=1.0, skin=0.0, nl_every=50, kspace_ctas_per_sm=0, pair_variant=0):
+                 minqq=1.0, skin=0.0, nl_every=50, kspace_ctas_per_sm=0, pair_variant=0,
+                 thermostat=0, T=298.0, tau_T=0.1, thermo_f=0.0, seed=0):
         lib = library()
         self.system = system
         self.ns = system.ns
@@ -252,7 +263,8 @@ class ForcePath:
                                     aspc_k=aspc_k, scf_iter=scf_iter, scf_omega=scf_omega,
                                     minqq=minqq, skin=skin, nl_every=nl_every,
                                     kspace_ctas_per_sm=kspace_ctas_per_sm,
-                                    pair_variant=pair_variant)
+                                    pair_variant=pair_variant, thermostat=thermostat, T=T,
+                                    tau_T=tau_T, thermo_f=thermo_f, seed=seed)
         self.polar = getattr(system, "polar", False)
         Lb = np.broadcast_to(np.asarray(L, dtype=np.float64), (3,))
         st = C.c_int(0)
@@ -357,6 +369,10 @@ class ForcePath:
         self._check(library().mg_md_get_state(self._ctx, r.ctypes.data_as(_dp),
                                               r1.ctypes.data_as(_dp)))
         return r.reshape(-1, 3), r1.reshape(-1, 3)
+
+    def thermostat_factor(self):
+        """velocity factor of the last thermostat call"""
+        return library().mg_thermostat_factor(self._ctx)
 
     def set_overlap(self, on):
         """FP32 path: k-space chain concurrent with the r-space chain (default on)"""

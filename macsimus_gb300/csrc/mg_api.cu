@@ -90,6 +90,12 @@ struct mg_ctx {
   bool dmax_pending = false;
   int nepart = 0;
   int pair_variant = 0;
+  // thermostat
+  int thermostat = 0, nchi = 0;
+  double T = 298, tau_T = 0.1, thermo_f = 0;
+  unsigned long long seed = 0;
+  long long* d_step = nullptr;
+  double *d_chi = nullptr, *d_zth = nullptr;
   // Widom: the type table, the site kinds, sites per type; cell data of the
   // last force evaluation (cook's lastlist)
   int ntypes = 0, comb_rule = 1;
@@ -250,6 +256,14 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   ctx->minqq = p->minqq > 0 ? p->minqq : 1.0;
   ctx->use_list = p->skin > 0;
   ctx->pair_variant = p->pair_variant;
+  ctx->thermostat = p->thermostat;
+  if (ctx->thermostat < 0 || ctx->thermostat > 2)
+    return fail(ctx, MG_ERR_ARG, "thermostat: 0 none, 1 Berendsen, 2 Bussi");
+  if (ctx->thermostat && !(p->T > 0 && p->tau_T > 0))
+    return fail(ctx, MG_ERR_ARG, "thermostat needs T > 0 and tau_T > 0");
+  ctx->T = p->T;
+  ctx->tau_T = p->tau_T;
+  ctx->seed = p->seed;
   ctx->skin = p->skin > 0 ? p->skin : 0;
   ctx->nl_every = p->nl_every > 0 ? p->nl_every : 50;
   CK(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
@@ -588,6 +602,16 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   CK(upload(&ctx->d_imass, imass.data(), ns));
   CK(upload(&ctx->d_mass, mass.data(), ns));
   CK(dalloc(&ctx->d_kinpart, (size_t)(t->nmol + 127) / 128 + 1));
+  ctx->thermo_f = p->thermo_f > 0 ? p->thermo_f : 3.0 * ns - t->nc - 3;
+  ctx->nchi = 2 * 152;
+  CK(dalloc(&ctx->d_chi, (size_t)ctx->nchi));
+  CK(dalloc(&ctx->d_zth, 1));
+  CK(dalloc(&ctx->d_step, 1));
+  CK(cudaMemset(ctx->d_step, 0, sizeof(long long)));
+  {
+    const double one = 1;
+    CK(cudaMemcpy(ctx->d_zth, &one, sizeof(double), cudaMemcpyHostToDevice));
+  }
   CK(dalloc(&ctx->d_status, 1));
   CK(cudaMemset(ctx->d_status, 0, sizeof(int)));
   CK(dalloc(&ctx->d_sums, 32));
@@ -877,6 +901,22 @@ ShakeArgs shake_args(mg_ctx* ctx) {
   return sa;
 }
 
+ThermoArgs thermo_args(mg_ctx* ctx) {
+  ThermoArgs t;
+  t.kind = ctx->thermostat;
+  t.ns = ctx->ns;
+  t.nkin = (ctx->nmol + 127) / 128;
+  t.nchi = ctx->nchi;
+  t.nf = ctx->thermo_f;
+  t.T = ctx->T;
+  t.tau = ctx->tau_T;
+  t.h = ctx->h;
+  t.seed = ctx->seed;
+  t.step = ctx->d_step;
+  t.zout = ctx->d_zth;
+  return t;
+}
+
 // one leap-frog + SHAKE step of a non-polar box with cells re-binned at the
 // force evaluation: kernels only, no host synchronisation (graph capture)
 int md_step_enqueue(mg_ctx* ctx, bool measure) {
@@ -885,6 +925,8 @@ int md_step_enqueue(mg_ctx* ctx, bool measure) {
   if (rc) return rc;
   CK(k_shake(L, shake_args(ctx)));
   if (measure) CK(k_reduce_sum(L, ctx->d_kinpart, (ctx->nmol + 127) / 128, 1, ctx->d_sums + 17));
+  if (ctx->thermostat)
+    CK(k_thermostat(L, thermo_args(ctx), ctx->d_kinpart, ctx->d_chi, ctx->d_r1));
   return MG_OK;
 }
 
@@ -950,7 +992,8 @@ int mg_destroy(mg_ctx* ctx) {
                   ctx->d_nlist, ctx->d_ncount, ctx->d_rbuild, ctx->d_dmax,
                   ctx->d_wtabf, ctx->d_wtabd, ctx->d_wgeom, ctx->d_wpart, ctx->d_wbox,
                   ctx->d_qfix, ctx->d_adjtab, ctx->d_ag, ctx->d_aq, ctx->d_apart, ctx->d_adEq,
-                  ctx->d_adLq, ctx->d_ags, ctx->d_atpart, ctx->d_aT, ctx->d_fk};
+                  ctx->d_adLq, ctx->d_ags, ctx->d_atpart, ctx->d_aT, ctx->d_fk,
+                  ctx->d_chi, ctx->d_zth, ctx->d_step};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ctx->h_sums) cudaFreeHost(ctx->h_sums);
@@ -1186,6 +1229,8 @@ int mg_md_steps(mg_ctx* ctx, int nsteps, mg_energy* en) {
       ctx->dmax_pending = true;
     }
     if (measure) PROF("reduce", k_reduce_sum(L, ctx->d_kinpart, nkin, 1, ctx->d_sums + 17));
+    if (ctx->thermostat)
+      PROF("thermostat", k_thermostat(L, thermo_args(ctx), ctx->d_kinpart, ctx->d_chi, ctx->d_r1));
   }
   if (en) {
     int rc = fetch_sums(ctx);
@@ -1531,6 +1576,14 @@ int mg_selffield(mg_ctx* ctx, double* r, double* f, double omega, int measure, m
   if (rc) return rc;
   if (measure && en) add_drude_energy(ctx, en);
   return MG_OK;
+}
+
+double mg_thermostat_factor(mg_ctx* ctx) {
+  if (!ctx) return 0;
+  double z = 1;
+  cudaMemcpyAsync(&z, ctx->d_zth, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaStreamSynchronize(ctx->stream);
+  return z;
 }
 
 int mg_set_overlap(mg_ctx* ctx, int on) {

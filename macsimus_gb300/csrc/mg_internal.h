@@ -236,6 +236,19 @@ struct WidomArgs {
   double* U;           // [n] or null
   double* part;        // [nblocks]
 };
+// thermostat after SHAKE (mg_thermo.cu)
+struct ThermoArgs {
+  int kind;              // 1 Berendsen, 2 Bussi
+  int ns, nkin, nchi;    // sites, SHAKE kinetic partials, Bussi chi^2 partials
+  double nf;             // degrees of freedom
+  double T, tau, h;
+  unsigned long long seed;
+  long long* step;       // device step counter (Bussi stream), advanced per call
+  double* zout;          // the factor of the step, or null
+};
+cudaError_t k_thermostat(const Launch& L, const ThermoArgs& a, const double* kin_part,
+                         double* chi_part, double* r1);
+
 // adjoint constants of one pair of site kinds (FP64)
 struct AdjPair {
   double C1q, C2q, Sq, E4, A, A4;

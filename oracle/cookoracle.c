@@ -1200,3 +1200,42 @@ int orc_adjoint(const orc_sys_t *s, const double *r, const double *g, const doub
   free(kv); free(ekk); free(Sre); free(Sim); free(Tre); free(Tim); free(pr); free(pi);
   return 0;
 }
+
+/* ---------------------------------------------------------- thermostats --- */
+
+/* Gaussian number i of step `step` of the thermostat stream: Box-Muller on
+   the SplitMix64 words 2i, 2i+1 of seed + (step*2^40 + n + 1)*gamma (the
+   stream of the GPU path; the reference draws rndgauss()) */
+double orc_thermo_gauss(unsigned long long seed, long long step, long long i)
+{
+  unsigned long long base = (unsigned long long)step << 40;
+  double u1 = ((double)(mix64(seed + (base + 2 * i + 1) * 0x9E3779B97F4A7C15ULL) >> 11) + 1.0) /
+              9007199254740992.0;
+  double u2 = (double)(mix64(seed + (base + 2 * i + 2) * 0x9E3779B97F4A7C15ULL) >> 11) /
+              9007199254740992.0;
+  return sqrt(-2.0 * log(u1)) * cos(2 * M_PI * u2);
+}
+
+/* the velocity factor of sim/thermo.c after a SHAKE step: kin2 = sum m
+   (V1^2 + V2^2) (V = h v), En.T = kin2/(2 h^2)/f; kind 1 Berendsen
+   (:157-163, blogT of sim/constrd.c:98-107), kind 2 Bussi (:165-179) */
+double orc_thermostat(int kind, double kin2, double h, double nf, double T, double tau,
+                      unsigned long long seed, long long step)
+{
+  double ET = kin2 / (2 * h * h) / nf;
+  if (kind == 1) {
+    const double e2 = 7.38905609893065022723;
+    double bl = ET > T * e2 ? 1 : (ET * e2 < T ? -1 : log(ET / T) / 2);
+    return exp(bl * -h / tau);
+  }
+  if (kind == 2) {
+    double e = exp(-h / tau), c = T / (nf * ET), u1 = orc_thermo_gauss(seed, step, 0), uf = 0;
+    long long i;
+    for (i = 1; i < (long long)nf; i++) {
+      double g = orc_thermo_gauss(seed, step, i);
+      uf += g * g;
+    }
+    return sqrt(e + c * (1 - e) * (u1 * u1 + uf) + 2 * e * sqrt(c * (1 - e)) * u1);
+  }
+  return 1;
+}

@@ -103,7 +103,7 @@ int orc_forces(const orc_sys_t *s, const double *r, double *f, orc_en_t *en, int
    VERLET=3).  r, r1 updated in place (r1 = r(t)-r(t-h)); f = forces at r.
    Constraints: nc pairs (ci,cj) with squared lengths bondq; imass per site.
    omega = half of cook's omegac.  Returns the number of sweeps of the worst
-   molecule (or -1 when maxit is exceeded).  ekin: sum m (V1^2+V2^2)/2/h^2 */
+   molecule (or -1 when maxit is exceeded).  ekin: sum m (V1^2+V2^2)/(4 h^2), the kinetic energy */
 int orc_shake_step(int ns, double *r, double *r1, const double *f, const double *mass,
                    int nmol, const int *mol_first, const int *mol_nc, const int *cfirst,
                    const int *ci, const int *cj, const double *bondq,
@@ -136,6 +136,12 @@ double orc_widom_corr(const orc_sys_t *s, int nps, const int *ptype);
 int orc_adjoint(const orc_sys_t *s, const double *r, const double *g, const double *dA,
                 double *E, double *W, double *dEp, double *dWp, double *dLp, double *dEq,
                 double *dLq);
+
+/* thermostats of sim/thermo.c (Berendsen 1, Bussi 2): the velocity factor
+   after a SHAKE step from kin2 = sum m (V1^2+V2^2), V = h v */
+double orc_thermo_gauss(unsigned long long seed, long long step, long long i);
+double orc_thermostat(int kind, double kin2, double h, double nf, double T, double tau,
+                      unsigned long long seed, long long step);
 
 #ifdef __cplusplus
 }

@@ -80,6 +80,9 @@ def lib():
         L.orc_widom.restype = C.c_double
         L.orc_adjoint.argtypes = [C.POINTER(SYS), dp, dp, dp, dp, dp, dp, dp, dp, dp, dp]
         L.orc_widom_corr.argtypes = [C.POINTER(SYS), C.c_int, ip]
+        L.orc_thermostat.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                     C.c_double, C.c_ulonglong, C.c_longlong]
+        L.orc_thermostat.restype = C.c_double
         L.orc_widom_corr.restype = C.c_double
         _lib = L
     return _lib
@@ -292,3 +295,8 @@ def aspc_coef(k):
     om = C.c_double()
     lib().orc_aspc_coef(k, _dp(B), C.byref(om))
     return B, om.value
+
+
+def thermostat_factor(kind, kin2, h, nf, T, tau, seed=0, step=0):
+    """velocity factor of cook's Berendsen (1) / Bussi (2) thermostat"""
+    return lib().orc_thermostat(kind, kin2, h, nf, T, tau, seed, step)
