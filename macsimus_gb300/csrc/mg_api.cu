@@ -549,7 +549,7 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
     // 1.5 times the mean site density, in multiples of 32 (grown on overflow)
     const double V = p->L[0] * p->L[1] * p->L[2], rl = p->cutoff + ctx->skin;
     ctx->nl_cap = ((int)(1.5 * ns / V * 4.18879 * rl * rl * rl) + 64 + 31) / 32 * 32;
-    ctx->nl_cap = std::min(ctx->nl_cap, ns);
+    ctx->nl_cap = (std::min(ctx->nl_cap, ns) + 7) / 8 * 8;  // rows 16-byte aligned
     ctx->nl_pitch = ctx->nl_cap;
     CK(dalloc(&ctx->d_nlist, (size_t)ctx->nl_cap * ns));
     CK(dalloc(&ctx->d_ncount, ns));
@@ -650,7 +650,10 @@ int build_lists(mg_ctx* ctx, const double* r_dev) {
   Launch L = launch(ctx);
   for (int attempt = 0; attempt < 4; attempt++) {
     ListArgs l = list_args(ctx);
-    PROF("list_build", k_build_list(L, l, ctx->ns, ctx->d_key_s, ctx->d_pj));
+    if (ctx->allpairs)
+      PROF("list_build", k_build_list(L, l, ctx->ns, ctx->d_key_s, ctx->d_pj));
+    else
+      PROF("list_build", k_build_list_cells(L, l, ctx->d_pj));
     PROF("neighbour_list", k_save_build(L, ctx->ns, r_dev, ctx->d_rbuild));
     int st = 0;
     CK(cudaMemcpyAsync(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -666,7 +669,7 @@ int build_lists(mg_ctx* ctx, const double* r_dev) {
     CK(cudaMemcpyAsync(ctx->d_status, &st, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaFree(ctx->d_nlist));
     ctx->d_nlist = nullptr;
-    ctx->nl_cap = std::min(ctx->ns, ctx->nl_cap * 3 / 2 + 32);
+    ctx->nl_cap = (std::min(ctx->ns, ctx->nl_cap * 3 / 2 + 32) + 7) / 8 * 8;
     ctx->nl_pitch = ctx->nl_cap;
     CK(dalloc(&ctx->d_nlist, (size_t)ctx->nl_cap * ctx->ns));
   }

@@ -190,6 +190,9 @@ struct ListArgs {
 // cell_of: [ns] cell of every sorted site (the sorted cell keys)
 cudaError_t k_build_list(const Launch& L, const ListArgs& a, int ns, const int* cell_of,
                          const int4* pj);
+// the same by warp per home cell with staged appends (grids of >= 2 cdiv + 1
+// cells per edge; cap a multiple of 8)
+cudaError_t k_build_list_cells(const Launch& L, const ListArgs& a, const int4* pj);
 cudaError_t k_save_build(const Launch& L, int ns, const double* r, double* rb);
 cudaError_t k_check_skin(const Launch& L, int ns, const double* r, const double* rb, double lim2,
                          int* status, int* dmax);

@@ -65,6 +65,88 @@ __global__ void __launch_bounds__(NB_THREADS)
   }
 }
 
+// One warp per home cell, lane = home site (grids of at least 2 cdiv + 1
+// cells per edge): the neighbours of a stencil cell are staged once as float
+// offsets of their nearest image from the home-cell centre (the pair
+// kernel's scheme), and every lane appends its hits to a private buffer of 8
+// entries in shared memory that goes to its row as two 16-byte stores.
+// Entry order: stencil order, then sorted order (deterministic).
+constexpr int NBC_BUF = 8;
+__global__ void __launch_bounds__(32)
+    build_list_cell_kernel(ListArgs a, const int4* __restrict__ pj) {
+  __shared__ float4 sj[32];
+  __shared__ int sidx[32];
+  __shared__ __align__(16) int buf[32][NBC_BUF];
+  const int lane = threadIdx.x;
+  const int c = blockIdx.x;
+  const int cz = c % a.ncz, cy = (c / a.ncz) % a.ncy, cx = c / (a.ncy * a.ncz);
+  const unsigned refx = (unsigned)((((unsigned long long)(2 * cx + 1)) << 31) / a.ncx),
+                 refy = (unsigned)((((unsigned long long)(2 * cy + 1)) << 31) / a.ncy),
+                 refz = (unsigned)((((unsigned long long)(2 * cz + 1)) << 31) / a.ncz);
+  const int i0 = a.cell_start[c], ni = a.cell_start[c + 1] - i0;
+  for (int ib = 0; ib < ni; ib += 32) {
+    const bool vi = ib + lane < ni;
+    const int ti = i0 + ib + lane;
+    const int4 me = vi ? pj[ti] : make_int4(0, 0, 0, 0);
+    const float xi = (float)(int)((unsigned)me.x - refx) * a.sx,
+                yi = (float)(int)((unsigned)me.y - refy) * a.sy,
+                zi = (float)(int)((unsigned)me.z - refz) * a.sz;
+    int* row = a.nlist + (long)ti * a.cap;
+    int cnt = 0, nb = 0;
+    for (int s = 0; s < a.nstencil; s++) {
+      const int4 o = a.stencil[s];
+      int x2 = cx + o.x, y2 = cy + o.y, z2 = cz + o.z;
+      x2 += (x2 < 0) ? a.ncx : (x2 >= a.ncx ? -a.ncx : 0);
+      y2 += (y2 < 0) ? a.ncy : (y2 >= a.ncy ? -a.ncy : 0);
+      z2 += (z2 < 0) ? a.ncz : (z2 >= a.ncz ? -a.ncz : 0);
+      const int c2 = (x2 * a.ncy + y2) * a.ncz + z2;
+      const int j0 = a.cell_start[c2], nj = a.cell_start[c2 + 1] - j0;
+      for (int jb = 0; jb < nj; jb += 32) {
+        if (jb + lane < nj) {
+          const int4 q = pj[j0 + jb + lane];
+          sj[lane] = make_float4((float)(int)((unsigned)q.x - refx) * a.sx,
+                                 (float)(int)((unsigned)q.y - refy) * a.sy,
+                                 (float)(int)((unsigned)q.z - refz) * a.sz, 0.f);
+          sidx[lane] = j0 + jb + lane;
+        }
+        __syncwarp();
+        const int n = min(32, nj - jb);
+        for (int jj = 0; jj < n; jj++) {
+          const float4 q = sj[jj];
+          const float dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
+          const int tj = sidx[jj];
+          if (vi && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < a.rlist2 && tj != ti) {
+            buf[lane][nb++] = tj;
+            if (nb == NBC_BUF) {
+              if (cnt + NBC_BUF <= a.cap) {
+                int4* d = reinterpret_cast<int4*>(row + cnt);
+                d[0] = *reinterpret_cast<const int4*>(&buf[lane][0]);
+                d[1] = *reinterpret_cast<const int4*>(&buf[lane][4]);
+              }
+              cnt += NBC_BUF;
+              nb = 0;
+            }
+          }
+        }
+        __syncwarp();
+      }
+    }
+    if (vi) {
+      for (int k = 0; k < nb; k++)
+        if (cnt + k < a.cap) row[cnt + k] = buf[lane][k];
+      cnt += nb;
+      a.ncount[ti] = min(cnt, a.cap);
+      if (cnt > a.cap) atomicOr(a.status, 16);
+    }
+  }
+}
+
+cudaError_t k_build_list_cells(const Launch& L, const ListArgs& a, const int4* pj) {
+  build_list_cell_kernel<<<a.ncx * a.ncy * a.ncz, 32, 0, L.s>>>(a, pj);
+  ++*L.counter;
+  return cudaGetLastError();
+}
+
 cudaError_t k_build_list(const Launch& L, const ListArgs& a, int ns, const int* cell_of,
                          const int4* pj) {
   build_list_kernel<<<(ns + NB_WARPS - 1) / NB_WARPS, NB_THREADS, 0, L.s>>>(a, ns, cell_of, pj);
