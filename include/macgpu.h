@@ -70,6 +70,18 @@ typedef struct {
   const int *mol_cfirst;      /* [nmol+1] first constraint of each molecule */
   const double *chargepol;    /* [ns] Drude charge or NULL (siteinfo_t.chargepol) */
   const double *alphapol;     /* [ns] Drude polarizability volume, A^3, or NULL */
+  /* linear ("Middle") dependants, cook's depend_t of type DEP_M
+     (cook/simdef.c:322-432): massless site dep_site[k] at
+     sum_p dep_w[p] r[dep_parent[p]], p in [dep_first[k], dep_first[k+1]);
+     mg_md_steps places them before and redistributes their forces after
+     every force evaluation (sim/norm.c:1161-1276 depend_r / depend_f, as
+     sim/constrd.c:722,747 call them); mg_forces returns the raw forces like
+     cook's forces().  ndep = 0: none. */
+  int ndep;
+  const int *dep_site;        /* [ndep], dependants of a molecule consecutive */
+  const int *dep_first;       /* [ndep+1] */
+  const int *dep_parent;      /* [dep_first[ndep]] */
+  const double *dep_w;        /* [dep_first[ndep]] */
 } mg_topology;
 
 /* Run parameters (cook's box, el, cutoff, h, epsc ... globals). */
@@ -109,11 +121,19 @@ typedef struct {
   int pair_variant;
   /* thermostat after every SHAKE step (sim/thermo.c): 0 none, 1 Berendsen,
      2 Bussi (stochastic velocity rescaling); temperature T (K), time
-     constant tau_T (ps), degrees of freedom thermo_f (<=0: 3 ns - nc - 3),
-     seed of the Bussi stream */
+     constant tau_T (ps), degrees of freedom thermo_f (<=0: cook's No.f,
+     3 (ns - ndep) - nc - 3), seed of the Bussi stream */
   int thermostat;
   double T, tau_T, thermo_f;
   unsigned long long seed;
+  /* molecule wrapping after every MD step, cook's normalize(-1)
+     (sim/norm.c:356-447, called at sim/main.c:1607): a molecule whose lowest
+     coordinate over its massive sites leaves [r0, r0 + L) moves by one box
+     length.  box_rmin as cook's box.rmin (cook/linklist.c:363-377): > 0 sets
+     r0, < 0 gives r0 = 0, 0 gives cook's Verlet/SHAKE choice r0 = 0.15 A.
+     no_normalize != 0 leaves the positions unwrapped. */
+  double box_rmin;
+  int no_normalize;
 } mg_params;
 
 /* Energies of one force evaluation (program units, K).
@@ -171,6 +191,17 @@ int mg_selffield(mg_ctx *ctx, double *r, double *f, double omega, int measure, m
    SHAKE (sim/constrd.c:726-736). */
 int mg_md_set_state(mg_ctx *ctx, const double *r, const double *r1);
 int mg_md_get_state(mg_ctx *ctx, double *r, double *r1);
+
+/* One playback frame of the MD state as cook's writeplayback writes it
+   (sim/simils.c:1646-1697): frame[0..2] = L, then ns float triples of
+     what = MG_PLB_POS:   r                  (.plb)
+            MG_PLB_VEL:   r1 / h             (.vlb, leap-frog v(t - h/2))
+            MG_PLB_DRUDE: r + Drude offset   (.dlb, Drude builds only)
+   flags are cook's option -n bits for positions: 2 = r - r1/2 (t - h/2),
+   4 = centred, r - L/2.  The file layout (float header ns, -3 or -6 when
+   centred, then the frames) is the caller's; the Python package writes it. */
+enum { MG_PLB_POS = 0, MG_PLB_VEL = 1, MG_PLB_DRUDE = 2 };
+int mg_playback_frame(mg_ctx *ctx, int what, int flags, float *frame);
 /* advance nsteps; energies of the last step in *en when en != NULL */
 int mg_md_steps(mg_ctx *ctx, int nsteps, mg_energy *en);
 

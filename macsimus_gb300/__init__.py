@@ -41,7 +41,8 @@ class Topology(C.Structure):
                 ("charge", _dp), ("mass", _dp), ("ntypes", C.c_int), ("type_EvdW", _dp),
                 ("type_RvdW", _dp), ("type_alpha", _dp), ("comb_rule", C.c_int), ("nc", C.c_int),
                 ("cons", _ip), ("cons_len", _dp), ("mol_cfirst", _ip), ("chargepol", _dp),
-                ("alphapol", _dp)]
+                ("alphapol", _dp), ("ndep", C.c_int), ("dep_site", _ip), ("dep_first", _ip),
+                ("dep_parent", _ip), ("dep_w", _dp)]
 
 
 class Params(C.Structure):
@@ -54,7 +55,8 @@ class Params(C.Structure):
                 ("scf_omega", C.c_double), ("minqq", C.c_double), ("skin", C.c_double),
                 ("nl_every", C.c_int), ("kspace_ctas_per_sm", C.c_int), ("pair_variant", C.c_int),
                 ("thermostat", C.c_int), ("T", C.c_double), ("tau_T", C.c_double),
-                ("thermo_f", C.c_double), ("seed", C.c_ulonglong)]
+                ("thermo_f", C.c_double), ("seed", C.c_ulonglong), ("box_rmin", C.c_double),
+                ("no_normalize", C.c_int)]
 
 
 class Energy(C.Structure):
@@ -110,6 +112,7 @@ def library():
         L.mg_ewald.argtypes = [vp, _dp, _dp, _dp]
         L.mg_md_set_state.argtypes = [vp, _dp, _dp]
         L.mg_md_get_state.argtypes = [vp, _dp, _dp]
+        L.mg_playback_frame.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_float)]
         L.mg_md_steps.argtypes = [vp, C.c_int, C.POINTER(Energy)]
         L.mg_selffield.argtypes = [vp, _dp, _dp, C.c_double, C.c_int, C.POINTER(Energy)]
         L.mg_set_stream.argtypes = [vp, vp]
@@ -175,7 +178,7 @@ def describe(system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None, 
              rshift=3, rplus=2.5, epsinf=3e33, h=0.002, epsc=1e-7, omegac=1.2, shake_maxit=1000,
              cells_per_cutoff=0, aspc_k=2, scf_iter=1, scf_omega=0.6, minqq=1.0, skin=0.0,
              nl_every=50, kspace_ctas_per_sm=0, pair_variant=0, thermostat=0, T=298.0,
-             tau_T=0.1, thermo_f=0.0, seed=0):
+             tau_T=0.1, thermo_f=0.0, seed=0, box_rmin=0.0, normalize=True):
     """(mg_topology, mg_params, arrays to keep alive) of one box"""
     keep = []
 
@@ -205,6 +208,14 @@ def describe(system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None, 
     t.cons = ip(system.cons.reshape(-1))
     t.cons_len = dp(system.cons_len)
     t.mol_cfirst = ip(system.mol_cfirst)
+    if getattr(system, "ndep", 0):
+        t.ndep = system.ndep
+        t.dep_site = ip(system.dep_site)
+        t.dep_first = ip(system.dep_first)
+        t.dep_parent = ip(system.dep_parent)
+        t.dep_w = dp(system.dep_w)
+    else:
+        t.ndep = 0
     if getattr(system, "polar", False):
         t.chargepol = dp(system.qpol)
         t.alphapol = dp(system.alphapol)
@@ -242,6 +253,8 @@ def describe(system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None, 
     p.tau_T = tau_T
     p.thermo_f = thermo_f
     p.seed = seed
+    p.box_rmin = box_rmin
+    p.no_normalize = 0 if normalize else 1
     return t, p, keep
 
 
@@ -252,7 +265,8 @@ class ForcePath:
                  grid=256, rshift=3, rplus=2.5, epsinf=3e33, h=0.002, epsc=1e-7, omegac=1.2,
                  shake_maxit=1000, cells_per_cutoff=0, aspc_k=2, scf_iter=1, scf_omega=0.6,
                  minqq=1.0, skin=0.0, nl_every=50, kspace_ctas_per_sm=0, pair_variant=0,
-                 thermostat=0, T=298.0, tau_T=0.1, thermo_f=0.0, seed=0):
+                 thermostat=0, T=298.0, tau_T=0.1, thermo_f=0.0, seed=0, box_rmin=0.0,
+                 normalize=True):
         lib = library()
         self.system = system
         self.ns = system.ns
@@ -264,7 +278,8 @@ class ForcePath:
                                     minqq=minqq, skin=skin, nl_every=nl_every,
                                     kspace_ctas_per_sm=kspace_ctas_per_sm,
                                     pair_variant=pair_variant, thermostat=thermostat, T=T,
-                                    tau_T=tau_T, thermo_f=thermo_f, seed=seed)
+                                    tau_T=tau_T, thermo_f=thermo_f, seed=seed,
+                                    box_rmin=box_rmin, normalize=normalize)
         self.polar = getattr(system, "polar", False)
         Lb = np.broadcast_to(np.asarray(L, dtype=np.float64), (3,))
         st = C.c_int(0)
@@ -369,6 +384,17 @@ class ForcePath:
         self._check(library().mg_md_get_state(self._ctx, r.ctypes.data_as(_dp),
                                               r1.ctypes.data_as(_dp)))
         return r.reshape(-1, 3), r1.reshape(-1, 3)
+
+    def playback_frame(self, what="plb", flags=0):
+        """(L[3], float32 [ns, 3]) of the MD state as cook writes it into
+        SIMNAME.plb ("plb": r), .vlb ("vlb": r1/h) or .dlb ("dlb": r + the
+        Drude offset); flags are cook's -n bits 2 (r - r1/2) and 4 (r - L/2)"""
+        w = {"plb": 0, "vlb": 1, "dlb": 2}[what]
+        fr = np.empty(3 * (self.ns + 1), np.float32)
+        self._check(library().mg_playback_frame(self._ctx, w, int(flags),
+                                                fr.ctypes.data_as(C.POINTER(C.c_float))))
+        fr = fr.reshape(-1, 3)
+        return fr[0].copy(), fr[1:]
 
     def thermostat_factor(self):
         """velocity factor of the last thermostat call"""

@@ -73,6 +73,11 @@ struct mg_ctx {
   double *d_bondq = nullptr, *d_imass = nullptr, *d_mass = nullptr;
   double* d_kinpart = nullptr;
   int* d_status = nullptr;
+  // linear dependant sites
+  int ndep = 0;
+  int *d_dep_site = nullptr, *d_dep_first = nullptr, *d_dep_parent = nullptr;
+  double* d_dep_w = nullptr;
+  float* d_plb = nullptr;  // playback frame staging
   // reduction outputs
   double* d_sums = nullptr;  // [0..9] pair, [10..16] k-space, [17] kinetic
   double* h_sums = nullptr;  // pinned
@@ -91,6 +96,8 @@ struct mg_ctx {
   int nepart = 0;
   int pair_variant = 0;
   // thermostat
+  int normalize = 1;
+  double box_r0 = 0.15;
   int thermostat = 0, nchi = 0;
   double T = 298, tau_T = 0.1, thermo_f = 0;
   unsigned long long seed = 0;
@@ -265,6 +272,8 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   ctx->tau_T = p->tau_T;
   ctx->seed = p->seed;
   ctx->skin = p->skin > 0 ? p->skin : 0;
+  ctx->normalize = p->no_normalize ? 0 : 1;
+  ctx->box_r0 = p->box_rmin > 0 ? p->box_rmin : (p->box_rmin < 0 ? 0.0 : 0.15);
   ctx->nl_every = p->nl_every > 0 ? p->nl_every : 50;
   CK(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
   ctx->stream = ctx->own_stream;
@@ -602,7 +611,45 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   CK(upload(&ctx->d_imass, imass.data(), ns));
   CK(upload(&ctx->d_mass, mass.data(), ns));
   CK(dalloc(&ctx->d_kinpart, (size_t)(t->nmol + 127) / 128 + 1));
-  ctx->thermo_f = p->thermo_f > 0 ? p->thermo_f : 3.0 * ns - t->nc - 3;
+  // dependants: parents and dependants of one molecule, consecutive per
+  // molecule, no dependant a parent, weights summing to 1 (cook fixes
+  // other sums with a warning, cook/simdef.c:390)
+  if (t->ndep < 0) return fail(ctx, MG_ERR_ARG, "ndep < 0");
+  ctx->ndep = t->ndep;
+  if (t->ndep > 0) {
+    if (!t->dep_site || !t->dep_first || !t->dep_parent || !t->dep_w)
+      return fail(ctx, MG_ERR_ARG, "incomplete dependant tables");
+    std::vector<char> isdep(ns, 0);
+    for (int k = 0; k < t->ndep; k++) {
+      const int d = t->dep_site[k];
+      if (d < 0 || d >= ns || isdep[d]) return fail(ctx, MG_ERR_ARG, "bad dependant site");
+      isdep[d] = 1;
+      if (t->mass[d] != 0) return fail(ctx, MG_ERR_ARG, "a dependant site must be massless");
+      if (k > 0 && ctx->h_mol[t->dep_site[k - 1]] > ctx->h_mol[d])
+        return fail(ctx, MG_ERR_ARG, "dependants must be ordered by molecule");
+    }
+    if (t->dep_first[0] != 0) return fail(ctx, MG_ERR_ARG, "dep_first[0] must be 0");
+    for (int k = 0; k < t->ndep; k++) {
+      if (t->dep_first[k + 1] <= t->dep_first[k])
+        return fail(ctx, MG_ERR_ARG, "a dependant without parents");
+      double sw = 0;
+      for (int q = t->dep_first[k]; q < t->dep_first[k + 1]; q++) {
+        const int a = t->dep_parent[q];
+        if (a < 0 || a >= ns || isdep[a] || ctx->h_mol[a] != ctx->h_mol[t->dep_site[k]])
+          return fail(ctx, MG_ERR_ARG, "a dependant's parent must be a site of its molecule");
+        sw += t->dep_w[q];
+      }
+      if (std::fabs(sw - 1) > 1e-5) return fail(ctx, MG_ERR_ARG, "dependant weights must sum to 1");
+    }
+    const int npar = t->dep_first[t->ndep];
+    CK(upload(&ctx->d_dep_site, t->dep_site, t->ndep));
+    CK(upload(&ctx->d_dep_first, t->dep_first, t->ndep + 1));
+    CK(upload(&ctx->d_dep_parent, t->dep_parent, npar));
+    CK(upload(&ctx->d_dep_w, t->dep_w, npar));
+  }
+  // cook's No.f: 3 per site less constraints, dependants and the conserved
+  // momentum (sim/siminit.c:518-530)
+  ctx->thermo_f = p->thermo_f > 0 ? p->thermo_f : 3.0 * (ns - t->ndep) - t->nc - 3;
   ctx->nchi = 2 * 152;
   CK(dalloc(&ctx->d_chi, (size_t)ctx->nchi));
   CK(dalloc(&ctx->d_zth, 1));
@@ -901,7 +948,21 @@ ShakeArgs shake_args(mg_ctx* ctx) {
   sa.p = ctx->d_p;
   sa.kin_part = ctx->d_kinpart;
   sa.status = ctx->d_status;
+  sa.normalize = ctx->normalize;
+  sa.r0 = ctx->box_r0;
+  for (int d = 0; d < 3; d++) sa.Lb[d] = ctx->L[d];
   return sa;
+}
+
+DependArgs depend_args(mg_ctx* ctx) {
+  DependArgs a;
+  a.ndep = ctx->ndep;
+  a.site = ctx->d_dep_site;
+  a.first = ctx->d_dep_first;
+  a.parent = ctx->d_dep_parent;
+  a.w = ctx->d_dep_w;
+  a.mol = ctx->d_mol;
+  return a;
 }
 
 ThermoArgs thermo_args(mg_ctx* ctx) {
@@ -926,7 +987,9 @@ int md_step_enqueue(mg_ctx* ctx, bool measure) {
   Launch L = launch(ctx);
   int rc = forces_async(ctx, ctx->d_r, ctx->d_f, measure);
   if (rc) return rc;
+  CK(k_depend_f(L, depend_args(ctx), ctx->d_f));
   CK(k_shake(L, shake_args(ctx)));
+  CK(k_depend_r(L, depend_args(ctx), ctx->d_r));
   if (measure) CK(k_reduce_sum(L, ctx->d_kinpart, (ctx->nmol + 127) / 128, 1, ctx->d_sums + 17));
   if (ctx->thermostat)
     CK(k_thermostat(L, thermo_args(ctx), ctx->d_kinpart, ctx->d_chi, ctx->d_r1));
@@ -996,7 +1059,8 @@ int mg_destroy(mg_ctx* ctx) {
                   ctx->d_wtabf, ctx->d_wtabd, ctx->d_wgeom, ctx->d_wpart, ctx->d_wbox,
                   ctx->d_qfix, ctx->d_adjtab, ctx->d_ag, ctx->d_aq, ctx->d_apart, ctx->d_adEq,
                   ctx->d_adLq, ctx->d_ags, ctx->d_atpart, ctx->d_aT, ctx->d_fk,
-                  ctx->d_chi, ctx->d_zth, ctx->d_step};
+                  ctx->d_chi, ctx->d_zth, ctx->d_step, ctx->d_dep_site, ctx->d_dep_first,
+                  ctx->d_dep_parent, ctx->d_dep_w, ctx->d_plb};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ctx->h_sums) cudaFreeHost(ctx->h_sums);
@@ -1133,6 +1197,12 @@ int mg_md_set_state(mg_ctx* ctx, const double* r, const double* r1) {
   const size_t nb = 3 * (size_t)ctx->ns * (ctx->polar ? 2 : 1) * sizeof(double);
   CK(cudaMemcpyAsync(ctx->d_r, r, nb, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->d_r1, r1, nb, cudaMemcpyHostToDevice, ctx->stream));
+  if (ctx->ndep > 0) {
+    // dependant positions from their parents, as cook's depend_r before the
+    // first force evaluation (sim/constrd.c:722)
+    Launch L = launch(ctx);
+    CK(k_depend_r(L, depend_args(ctx), ctx->d_r));
+  }
   if (ctx->polar && ctx->nd > 0) {
     // ASPC history as cook starts it (sim/pred2.c:45-55): the latest slot is
     // rpol(t) from r, the previous one rpol(t-h) from r1, older slots zero
@@ -1167,6 +1237,24 @@ int mg_md_get_state(mg_ctx* ctx, double* r, double* r1) {
   }
   if (r) CK(cudaMemcpyAsync(r, ctx->d_r, nb, cudaMemcpyDeviceToHost, ctx->stream));
   if (r1) CK(cudaMemcpyAsync(r1, ctx->d_r1, nb, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return MG_OK;
+}
+
+int mg_playback_frame(mg_ctx* ctx, int what, int flags, float* frame) {
+  if (!ctx || !frame) return fail(ctx, MG_ERR_ARG, "null argument");
+  if (!ctx->have_state) return fail(ctx, MG_ERR_ARG, "no MD state");
+  if (what < MG_PLB_POS || what > MG_PLB_DRUDE || (flags & ~6))
+    return fail(ctx, MG_ERR_ARG, "what: MG_PLB_POS/VEL/DRUDE; flags: bits 2 and 4");
+  if (what == MG_PLB_DRUDE && !ctx->polar)
+    return fail(ctx, MG_ERR_ARG, "Drude playback of a build without Drude charges");
+  if (!ctx->d_plb) CK(dalloc(&ctx->d_plb, 3 * (size_t)ctx->ns));
+  Launch L = launch(ctx);
+  CK(k_playback_frame(L, ctx->ns, what, flags, ctx->d_r, ctx->d_r1, 1. / ctx->h, ctx->L,
+                      ctx->d_plb));
+  for (int d = 0; d < 3; d++) frame[d] = (float)ctx->L[d];
+  CK(cudaMemcpyAsync(frame + 3, ctx->d_plb, 3 * sizeof(float) * (size_t)ctx->ns,
+                     cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return MG_OK;
 }
@@ -1220,11 +1308,16 @@ int mg_md_steps(mg_ctx* ctx, int nsteps, mg_energy* en) {
       int rc = forces_async(ctx, ctx->d_r, ctx->d_f, measure);
       if (rc) return rc;
     }
+    // forces on dependants to their parents (sim/constrd.c:747), the step,
+    // and dependant positions for the next force evaluation: the same
+    // positions cook's depend_r makes at the start of its next step
+    if (ctx->ndep > 0) PROF("depend", k_depend_f(L, depend_args(ctx), ctx->d_f));
     PROF("shake", k_shake(L, sa));
+    if (ctx->ndep > 0) PROF("depend", k_depend_r(L, depend_args(ctx), ctx->d_r));
     if (ctx->use_list) {
       ctx->since_build++;
       PROF("neighbour_list", k_check_skin(L, ctx->ns, ctx->d_r, ctx->d_rbuild,
-                                          0.25 * ctx->skin * ctx->skin, ctx->d_status,
+                                          0.25 * ctx->skin * ctx->skin, ctx->L, ctx->d_status,
                                           ctx->d_dmax));
       CK(cudaMemcpyAsync(ctx->h_dmax, ctx->d_dmax, sizeof(int), cudaMemcpyDeviceToHost,
                          ctx->stream));

@@ -171,6 +171,10 @@ struct ShakeArgs {
   double* p;           // scratch [3*ns]
   double* kin_part;    // [nblocks]
   int* status;         // set to 1 on non-convergence
+  // molecule wrapping after the step (cook's normalize): a molecule whose
+  // lowest massive-site coordinate is outside [r0, r0 + L) moves by L
+  int normalize;
+  double r0, Lb[3];
 };
 cudaError_t k_shake(const Launch& L, const ShakeArgs& a);
 
@@ -195,7 +199,7 @@ cudaError_t k_build_list(const Launch& L, const ListArgs& a, int ns, const int* 
 cudaError_t k_build_list_cells(const Launch& L, const ListArgs& a, const int4* pj);
 cudaError_t k_save_build(const Launch& L, int ns, const double* r, double* rb);
 cudaError_t k_check_skin(const Launch& L, int ns, const double* r, const double* rb, double lim2,
-                         int* status, int* dmax);
+                         const double Lb[3], int* status, int* dmax);
 cudaError_t k_pair_list_mixed(const Launch& L, const PairArgs& a, const ListArgs& l,
                               const int4* pj, const PairF* ptab, const float4* erd,
                               const float4* eru, bool measure, bool polar);
@@ -281,5 +285,20 @@ cudaError_t k_widom(const Launch& L, const WidomBox* boxes, int nbox, long long 
 cudaError_t k_drude_take(const Launch& L, const DrudeArgs& a, const double* r, double* out);
 cudaError_t k_drude_put(const Launch& L, const DrudeArgs& a, const double* in, double* r);
 cudaError_t k_fma_probe(cudaStream_t s, int blocks, int threads, int iters, float* out);
+
+// linear dependant sites (r_d = sum_p w_p r_p; f_p += w_p f_d)
+struct DependArgs {
+  int ndep;
+  const int* site;    // [ndep] dependant site, those of a molecule consecutive
+  const int* first;   // [ndep+1] parent range
+  const int* parent;  // parent sites
+  const double* w;    // parent weights
+  const int* mol;     // [ns] molecule of each site
+};
+cudaError_t k_depend_r(const Launch& L, const DependArgs& a, double* r);
+cudaError_t k_depend_f(const Launch& L, const DependArgs& a, double* f);
+// one playback frame (float triples of ns sites) from the MD state
+cudaError_t k_playback_frame(const Launch& L, int ns, int what, int flags, const double* r,
+                             const double* r1, double ih, const double Lb[3], float* out);
 
 }  // namespace mg

@@ -919,8 +919,15 @@ cudaError_t k_reduce_sum(const Launch& L, const double* part, int nrows, int wid
 // -------------------------------------------------------------- SHAKE --
 
 // sim/constrd.c:767-839 + sim/verlet.c:101-104 + sim/shakev3.c (SHAKE=1,
-// VERLET=3, no thermostat), one thread per molecule, FP64.
+// VERLET=3, no thermostat), one thread per molecule, FP64.  The new
+// positions are then wrapped as cook's normalize(-1) does after the step
+// (sim/norm.c:415-444): the molecule's lowest coordinate over its massive
+// sites decides a shift of +L (below r0), -L (at or above r0 + L) or none.
 constexpr int SH_THREADS = 128;
+
+__device__ __forceinline__ double wrap_shift(double lo, double r0, double L) {
+  return lo < r0 ? L : (lo >= r0 + L ? -L : 0.0);
+}
 
 // three-site, three-constraint molecules (rigid water) with the positions in
 // registers: the same sweeps, in the same order and with the same roundings,
@@ -992,6 +999,20 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
         }
       } while (maxsq > a.eps && it < a.maxit);
       if (maxsq > a.eps) atomicOr(a.status, 1);
+      double sx = 0, sy = 0, sz = 0;
+      if (a.normalize) {
+        double lx = 9e9, ly = 9e9, lz = 9e9;
+#pragma unroll
+        for (int s = 0; s < 3; s++)
+          if (a.mass[i0 + s] != 0) {
+            lx = fmin(lx, P[s].x);
+            ly = fmin(ly, P[s].y);
+            lz = fmin(lz, P[s].z);
+          }
+        sx = wrap_shift(lx, a.r0, a.Lb[0]);
+        sy = wrap_shift(ly, a.r0, a.Lb[1]);
+        sz = wrap_shift(lz, a.r0, a.Lb[2]);
+      }
 #pragma unroll
       for (int s = 0; s < 3; s++) {
         const int i = i0 + s;
@@ -1008,9 +1029,9 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
         a.r1[3 * i] = v2x;
         a.r1[3 * i + 1] = v2y;
         a.r1[3 * i + 2] = v2z;
-        a.r[3 * i] = P[s].x;
-        a.r[3 * i + 1] = P[s].y;
-        a.r[3 * i + 2] = P[s].z;
+        a.r[3 * i] = P[s].x + sx;
+        a.r[3 * i + 1] = P[s].y + sy;
+        a.r[3 * i + 2] = P[s].z + sz;
       }
     } else {
     double* p = a.p;
@@ -1046,6 +1067,14 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
       } while (maxsq > a.eps && it < a.maxit);
       if (maxsq > a.eps) atomicOr(a.status, 1);
     }
+    double sh[3] = {0, 0, 0};
+    if (a.normalize)
+      for (int k = 0; k < 3; k++) {
+        double lo = 9e9;
+        for (int i = i0; i < i1; i++)
+          if (a.mass[i] != 0) lo = fmin(lo, p[3 * i + k]);
+        sh[k] = wrap_shift(lo, a.r0, a.Lb[k]);
+      }
     for (int i = i0; i < i1; i++) {
       double v1s = 0, v2s = 0;
       for (int k = 0; k < 3; k++) {
@@ -1053,7 +1082,7 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
         v1s += v1 * v1;
         v2s += v2 * v2;
         a.r1[3 * i + k] = v2;
-        a.r[3 * i + k] = p[3 * i + k];
+        a.r[3 * i + k] = p[3 * i + k] + sh[k];
       }
       kin += (v1s + v2s) * a.mass[i];
     }

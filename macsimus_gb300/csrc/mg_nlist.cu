@@ -169,15 +169,22 @@ cudaError_t k_save_build(const Launch& L, int ns, const double* r, double* rb) {
 // largest squared displacement since the build (as the bits of a float,
 // which order like the floats for non-negative values) into *dmax; a site
 // beyond skin/2 sets bit 3 of *status (the lists may have missed a pair)
+// displacement since the build taken to the nearest image: the per-step
+// molecule wrapping moves sites by whole box lengths
+__device__ __forceinline__ double near_image(double d, double L, double iL) {
+  return d - L * rint(d * iL);
+}
+
 __global__ void check_skin_kernel(int ns, const double* __restrict__ r,
-                                  const double* __restrict__ rb, double lim2,
-                                  int* __restrict__ status, int* __restrict__ dmax) {
+                                  const double* __restrict__ rb, double lim2, double3 Lb,
+                                  double3 iL, int* __restrict__ status, int* __restrict__ dmax) {
   __shared__ float red[256];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   float d2 = 0.f;
   if (i < ns) {
-    const double dx = r[3 * i] - rb[3 * i], dy = r[3 * i + 1] - rb[3 * i + 1],
-                 dz = r[3 * i + 2] - rb[3 * i + 2];
+    const double dx = near_image(r[3 * i] - rb[3 * i], Lb.x, iL.x),
+                 dy = near_image(r[3 * i + 1] - rb[3 * i + 1], Lb.y, iL.y),
+                 dz = near_image(r[3 * i + 2] - rb[3 * i + 2], Lb.z, iL.z);
     const double dd = dx * dx + dy * dy + dz * dz;
     if (!(dd < lim2)) atomicOr(status, 8);
     d2 = (float)fmin(dd, 1e30);
@@ -192,8 +199,10 @@ __global__ void check_skin_kernel(int ns, const double* __restrict__ r,
 }
 
 cudaError_t k_check_skin(const Launch& L, int ns, const double* r, const double* rb, double lim2,
-                         int* status, int* dmax) {
-  check_skin_kernel<<<(ns + 255) / 256, 256, 0, L.s>>>(ns, r, rb, lim2, status, dmax);
+                         const double Lb[3], int* status, int* dmax) {
+  check_skin_kernel<<<(ns + 255) / 256, 256, 0, L.s>>>(
+      ns, r, rb, lim2, make_double3(Lb[0], Lb[1], Lb[2]),
+      make_double3(1 / Lb[0], 1 / Lb[1], 1 / Lb[2]), status, dmax);
   ++*L.counter;
   return cudaGetLastError();
 }

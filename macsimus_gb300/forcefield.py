@@ -47,8 +47,11 @@ SITE_TYPES = {
     "AP": (22.9898, 0.5, 3.3),
     "AM": (35.453, 0.7, 4.1),
     "PRB": (39.948, 0.65, 3.2),
+    # TIP4P/2005: the LJ oxygen and the massless charge site M
+    "OT": (15.9994, 0.774908, 3.1589),
+    "MW": (0.0, 0.0, 0.0),
 }
-TYPE_ORDER = ["H", "O", "NA", "CL", "OD", "AP", "AM", "PRB"]
+TYPE_ORDER = ["H", "O", "NA", "CL", "OD", "AP", "AM", "PRB", "OT", "MW"]
 
 # Drude parameters of a site type: (alphapol A^3, chargepol e).  The Drude
 # water has the shell charge -1.8 e on a spring of 4184 kJ/mol/A^2
@@ -87,6 +90,8 @@ class Species:
     geometry: np.ndarray   # reference geometry [ns,3] (A)
     bonds: list = field(default_factory=list)  # (i, j, length)
     drude: dict = None     # {site index: (alphapol A^3, chargepol e)}
+    # linear ("Middle") dependants: (site, [(parent, weight), ...])
+    dependants: list = field(default_factory=list)
 
 
 def spce():
@@ -95,6 +100,24 @@ def spce():
     return Species("WAT", ["O", "H", "H"], [-0.8476, 0.4238, 0.4238],
                    np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [c, s, 0.0]]),
                    bonds=[(0, 1, 1.0), (0, 2, 1.0), (1, 2, HOH)])
+
+
+def tip4p2005():
+    """TIP4P/2005 water: O (LJ), H, H, and the massless charge site M on the
+    bisector, 0.1546 A from O, a linear dependant of O, H, H"""
+    a = math.radians(104.52)
+    doh = 0.9572
+    h1 = np.array([doh, 0.0, 0.0])
+    h2 = np.array([doh * math.cos(a), doh * math.sin(a), 0.0])
+    bis = 0.5 * (h1 + h2)
+    w = 0.1546 / (2 * np.linalg.norm(bis))
+    m = w * (h1 + h2)
+    dhh = float(np.linalg.norm(h1 - h2))
+    sp = Species("T4P", ["OT", "H", "H", "MW"], [0.0, 0.5564, 0.5564, -1.1128],
+                 np.array([[0.0, 0.0, 0.0], h1, h2, m]),
+                 bonds=[(0, 1, doh), (0, 2, doh), (1, 2, dhh)])
+    sp.dependants = [(3, [(0, 1 - 2 * w), (1, w), (2, w)])]
+    return sp
 
 
 def ion(name, q=None):
@@ -124,7 +147,7 @@ def spce_drude():
 
 SPECIES = {"WAT": spce, "NA": lambda: ion("NA"), "CL": lambda: ion("CL"), "WATD": spce_drude,
            "AP": lambda: ion("AP", 1.0), "AM": lambda: ion("AM", -1.0),
-           "PRB": lambda: ion("PRB", 0.0)}
+           "PRB": lambda: ion("PRB", 0.0), "T4P": tip4p2005}
 
 
 @dataclass
@@ -147,6 +170,15 @@ class System:
     counts: list = None
     qpol: np.ndarray = None     # [ns] Drude charge (program units) or None
     alphapol: np.ndarray = None # [ns] Drude polarizability volume (A^3) or None
+    # linear dependants (massless sites): site, parents [dep_first[k]:dep_first[k+1]]
+    dep_site: np.ndarray = None   # [ndep] int32
+    dep_first: np.ndarray = None  # [ndep+1] int32
+    dep_parent: np.ndarray = None # [np] int32 (global site indices)
+    dep_w: np.ndarray = None      # [np] weights
+
+    @property
+    def ndep(self):
+        return 0 if self.dep_site is None else len(self.dep_site)
 
     @property
     def polar(self):
@@ -174,6 +206,7 @@ def build_system(species_names, counts):
     tix = {n: i for i, n in enumerate(TYPE_ORDER)}
     typ, q, mass, mol, mfirst, cons, clen, cfirst = [], [], [], [], [0], [], [], [0]
     qpol, apol = [], []
+    dsite, dfirst, dpar, dw = [], [0], [], []
     polar = any(t in TYPE_DRUDE for s in species_names for t in SPECIES[s]().sites)
     imol = 0
     for sname, n in zip(species_names, counts):
@@ -193,6 +226,12 @@ def build_system(species_names, counts):
             for (i, j, d) in sp.bonds:
                 cons.append((base + i, base + j))
                 clen.append(d)
+            for (k, parents) in sp.dependants:
+                dsite.append(base + k)
+                for (pi, w) in parents:
+                    dpar.append(base + pi)
+                    dw.append(w)
+                dfirst.append(len(dpar))
             imol += 1
             mfirst.append(len(typ))
             cfirst.append(len(cons))
@@ -202,7 +241,11 @@ def build_system(species_names, counts):
                   mol_cfirst=np.array(cfirst, np.int32), typeE=E, typeR=R, typeA=A,
                   comb_rule=1, species=list(species_names), counts=list(counts),
                   qpol=np.array(qpol) if polar else None,
-                  alphapol=np.array(apol) if polar else None)
+                  alphapol=np.array(apol) if polar else None,
+                  dep_site=np.array(dsite, np.int32) if dsite else None,
+                  dep_first=np.array(dfirst, np.int32) if dsite else None,
+                  dep_parent=np.array(dpar, np.int32) if dsite else None,
+                  dep_w=np.array(dw) if dsite else None)
 
 
 def ble_text(species_names):
@@ -229,7 +272,8 @@ def ble_text(species_names):
         ns = len(sp.sites)
         lines += ["", "species %s" % sname, "", "i=%d  N=0  config=0  water=0" % isp,
                   "ns=%d  nc=%d  nangles=0  ndihedrals=0  nimpropers=0  naromatics=0"
-                  % (ns, len(sp.bonds)), "ndependants=0 ;", "", "sites"]
+                  % (ns, len(sp.bonds)), "ndependants=%d ;" % len(sp.dependants), "",
+                  "sites"]
         for k in range(ns):
             excl = " ".join(str(j) for j in range(k))
             x, y, z = sp.geometry[k]
@@ -239,7 +283,13 @@ def ble_text(species_names):
         for (i, j, d) in sp.bonds:
             lines.append("  %d %s   %d %s   450  %.15f" % (i, sp.sites[i], j, sp.sites[j], d))
         lines += ["", "angles", "", "dihedrals", "", "impropers", "", "aromatics", "",
-                  "dependants", "", ""]
+                  "dependants"]
+        # cook/simdef.c readdependants: M site name n (parent name weight)... e
+        for (k, parents) in sp.dependants:
+            lines.append("  M %d %s %d " % (k, sp.sites[k], len(parents)) +
+                         " ".join("%d %s %.12f" % (pi, sp.sites[pi], w) for pi, w in parents) +
+                         " e")
+        lines += ["", ""]
     return "\n".join(lines) + "\n\n"
 
 

@@ -789,7 +789,9 @@ int orc_shake_step(int ns, double *r, double *r1, const double *f, const double 
     double maxsq;
     for (i = i0; i < i1; i++)
       for (k = 0; k < 3; k++)
-        p[3 * i + k] = f[3 * i + k] * (hh / mass[i]) + r[3 * i + k] + r1[3 * i + k];
+        /* a massless site is a dependant, placed by depend_r after the step */
+        p[3 * i + k] = f[3 * i + k] * (mass[i] > 0 ? hh / mass[i] : 0) + r[3 * i + k] +
+                       r1[3 * i + k];
     if (nc > 0) {
       do {
         it++;

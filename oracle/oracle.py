@@ -47,7 +47,8 @@ def build():
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB):
+        src = [os.path.join(HERE, n) for n in ("cookoracle.c", "cookoracle.h")]
+        if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(map(os.path.getmtime, src)):
             build()
         L = C.CDLL(LIB)
         dp = C.POINTER(C.c_double)
@@ -288,6 +289,43 @@ class Oracle:
                             seed, T, _dp(U) if energies else None, nthreads)
         corr = lib().orc_widom_corr(C.byref(self.sys), len(pt), _ip(pt))
         return s, corr, U
+
+
+def depend_r(system, r):
+    """positions of the linear ("Middle") dependants from their parents,
+    r_d = sum_p w_p r_p (sim/norm.c:1188-1193, depend_r for d->type<=DEP_M);
+    returns a copy"""
+    r = np.array(r, dtype=np.float64, copy=True)
+    for k in range(system.ndep):
+        a, b = system.dep_first[k], system.dep_first[k + 1]
+        r[system.dep_site[k]] = (system.dep_w[a:b, None] * r[system.dep_parent[a:b]]).sum(0)
+    return r
+
+
+def depend_f(system, f):
+    """forces on the linear dependants added to their parents, f_p += w_p f_d,
+    in table order (sim/norm.c:1296-1299, depend_f for d->type<=DEP_M); the
+    dependant keeps its force, as in cook; returns a copy"""
+    f = np.array(f, dtype=np.float64, copy=True)
+    for k in range(system.ndep):
+        fd = f[system.dep_site[k]].copy()
+        for q in range(system.dep_first[k], system.dep_first[k + 1]):
+            f[system.dep_parent[q]] += system.dep_w[q] * fd
+    return f
+
+
+def normalize(system, r, L, r0=0.15):
+    """cook's normalize(-1) (sim/norm.c:415-444): per molecule and axis, the
+    lowest coordinate over the massive sites below r0 shifts the molecule by
+    +L, at or above r0 + L by -L; returns a copy"""
+    r = np.array(r, dtype=np.float64, copy=True)
+    L = np.broadcast_to(np.asarray(L, dtype=np.float64), (3,))
+    for n in range(system.nmol):
+        a, b = system.mol_first[n], system.mol_first[n + 1]
+        heavy = system.mass[a:b] != 0
+        lo = r[a:b][heavy].min(axis=0)
+        r[a:b] += np.where(lo < r0, L, np.where(lo >= r0 + L, -L, 0.0))
+    return r
 
 
 def aspc_coef(k):

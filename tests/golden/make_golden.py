@@ -48,6 +48,12 @@ CASES = {
     "drude216": dict(binary="cookpol", species=["WATD"], N=[216], L=18.6206,
                      cutoff=9.0, alpha=0.35, kn=6, steps=6, h=0.001, epsc=1e-10,
                      options=["-p220"], extra_def=["scf.eps=-1"]),
+    # 216 TIP4P/2005 waters: the charge site M is a massless linear
+    # dependant of O, H, H (cook's depend_r / depend_f)
+    # with a playback (-y) and velocity playback (-n1) frame after every step
+    "tip4p216": dict(binary="cookew", species=["T4P"], N=[216], L=18.6206,
+                     cutoff=9.0, alpha=0.35, kn=6, steps=3, h=0.002, epsc=1e-10,
+                     options=["-y99999", "-n1"], extra_get=["dt.plb=0.002"]),
     # Widom insertions of a neutral LJ probe (sigma 3.2 A, epsilon 0.65
     # kJ/mol) into 250 + 250 LJ ions of charge +-1 e, L = 37 A (reduced
     # density 0.5 at sigma 3.7 A), cutoff 10, alpha 0.31, |n|<=8; 1e7
@@ -135,6 +141,17 @@ def run_case(name, c, keep=None):
         meta["widom"] = dict(mu_raw_K=float(mw.group(1)), corr=float(mc.group(1)),
                              mu_kT=float(mk.group(1)),
                              n=int(re.search(r"widom\.n=(\d+)", get_text(c)).group(1)))
+    # playback files (sim/simils.c:1554-1697): float32 header (ns, -3), then
+    # per frame L[3] and ns positions (.plb) or velocities (.vlb)
+    for ext in ("plb", "vlb"):
+        fn = os.path.join(wd, "sim." + ext)
+        if os.path.exists(fn):
+            raw = np.fromfile(fn, dtype=np.float32)
+            ns = int(raw[0])
+            assert raw[1] == -3
+            fr = raw[2:].reshape(-1, ns + 1, 3)
+            dumps[0][ext + "_L"] = fr[:, 0].copy()
+            dumps[0][ext + "_r"] = fr[:, 1:].copy()
     if keep is None:
         shutil.rmtree(wd)
     return dumps, meta
@@ -149,6 +166,9 @@ def save_case(name, dumps, meta):
     arrays["L"] = d0["L"]
     arrays["r"] = np.stack([d["r"] for d in dumps])
     arrays["f"] = np.stack([d["f"] for d in dumps])
+    for k in ("plb_L", "plb_r", "vlb_L", "vlb_r"):
+        if k in d0:
+            arrays[k] = d0[k]
     if "rD" in d0:
         arrays["qD"] = d0["qD"]
         arrays["rD"] = np.stack([d["rD"] for d in dumps])

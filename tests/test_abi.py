@@ -45,3 +45,29 @@ def test_product_does_not_reference_oracle():
             if fn.endswith((".py", ".cu", ".cpp", ".h")):
                 src = open(os.path.join(root, fn)).read()
                 assert "cookoracle" not in src and "from oracle" not in src, fn
+
+
+@pytest.mark.parametrize("cname,pyname", [
+    ("mg_topology", "Topology"), ("mg_params", "Params"), ("mg_energy", "Energy"),
+    ("mg_probe", "Probe"), ("mg_widom_result", "WidomResult"),
+    ("mg_adjoint_out", "AdjointOut")])
+def test_ctypes_layout_matches_header(cname, pyname, tmp_path):
+    """the Python mirror's structs have the header's size and field offsets
+    (a C program built with the host compiler prints them)"""
+    import ctypes
+    import macsimus_gb300 as M
+    cls = getattr(M, pyname)
+    fields = [f[0] for f in cls._fields_]
+    src = ['#include <stdio.h>', '#include <stddef.h>', '#include "macgpu.h"', 'int main(void){',
+           'printf("%%zu\\n", sizeof(%s));' % cname]
+    src += ['printf("%%zu\\n", offsetof(%s, %s));' % (cname, f) for f in fields]
+    src.append('return 0;}')
+    c = tmp_path / "layout.c"
+    c.write_text("\n".join(src))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(REPO, "include"), str(c), "-o", str(exe)],
+                   check=True)
+    out = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    assert out[0] == ctypes.sizeof(cls)
+    assert out[1:] == [getattr(cls, f).offset for f in fields]

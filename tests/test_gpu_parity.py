@@ -72,8 +72,11 @@ def test_ewald_kspace_part():
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_md_step_matches_reference_trajectory(precision):
-    g, meta, system, ew, fp = make("spce216", precision)
+@pytest.mark.parametrize("case", ["spce216", "tip4p216"])
+def test_md_step_matches_reference_trajectory(precision, case):
+    """one step from cook's dumps; for TIP4P/2005 the M-site forces go to
+    O, H, H before SHAKE and M is placed after it"""
+    g, meta, system, ew, fp = make(case, precision)
     R = g["r"]
     fp.md_set_state(R[2], R[2] - R[1])
     en = fp.md_steps(1)
@@ -191,3 +194,54 @@ def test_concurrent_kspace_chain_gives_identical_forces(case):
     f2, e2 = fp.forces(g["r"][0], measure=True)
     assert np.array_equal(f1, f2)
     assert e1["el"] == e2["el"] and e1["lj"] == e2["lj"]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_dependant_md_chain_matches_oracle(precision):
+    """five TIP4P/2005 steps on the device against the oracle's chain of
+    forces, depend_f, SHAKE and depend_r from the same start"""
+    g, meta, system, ew, fp = make("tip4p216", precision)
+    p = meta["params"]
+    orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
+    R = g["r"]
+    r, r1 = R[2].copy(), R[2] - R[1]
+    fp.md_set_state(r, r1)
+    fp.md_steps(5)
+    rg, _ = fp.md_get_state()
+    for _ in range(5):
+        f, _ = orc.forces(r, measure=False, nthreads=4)
+        r, r1, it, _ = orc.shake_step(r, r1, O.depend_f(system, f), p["h"], eps=p["epsc"],
+                                      omega=meta["omegac"] / 2)
+        r = O.depend_r(system, O.normalize(system, r, ew["L"]))
+    assert np.abs(rg - r).max() < (1e-9 if precision == "fp64" else 2e-6)
+
+
+@pytest.mark.parametrize("case", ["spce216", "tip4p216"])
+def test_step_wraps_molecules_like_normalize(case):
+    """cook wraps molecules after every step (normalize(-1)): the
+    configuration translated by -1 A in x and y leaves molecules below
+    r0 = 0.15, which the step moves by +L, the dependants with them"""
+    g, meta, system, ew, fp = make(case, "fp64")
+    p = meta["params"]
+    orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
+    R = g["r"]
+    r = R[2] + np.array([-1.0, -1.0, 0.0])
+    r1 = R[2] - R[1]
+    fp.md_set_state(r, r1)
+    fp.md_steps(1)
+    rg, _ = fp.md_get_state()
+    f, _ = orc.forces(r, measure=False, nthreads=4)
+    ro, _, _, _ = orc.shake_step(r, r1, O.depend_f(system, f), p["h"], eps=p["epsc"],
+                                 omega=meta["omegac"] / 2)
+    ro = O.depend_r(system, O.normalize(system, ro, ew["L"]))
+    moved = np.abs(ro - (r + r1)).max(axis=1) > 1.0
+    assert moved.sum() > 100         # molecules did wrap
+    assert np.abs(rg - ro).max() < 1e-9
+    # without the wrapping the same step leaves them where they are
+    g, meta, system, ew, fp = make(case, "fp64", normalize=False)
+    fp.md_set_state(r, r1)
+    fp.md_steps(1)
+    rn, _ = fp.md_get_state()
+    ro2, _, _, _ = orc.shake_step(r, r1, O.depend_f(system, f), p["h"], eps=p["epsc"],
+                                  omega=meta["omegac"] / 2)
+    assert np.abs(rn - O.depend_r(system, ro2)).max() < 1e-9

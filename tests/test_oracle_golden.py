@@ -137,3 +137,44 @@ def test_aspc_scf_chain_matches_reference():
     for t in range(5, g["r"].shape[0]):
         pred = sum(B[i] * corr[t - 1 - i] for i in range(4))
         assert np.abs(pred - g["rD"][t]).max() < 1e-10
+
+
+def test_dependant_positions_in_reference_dumps():
+    """cook dumps r after depend_r: every TIP4P/2005 charge site M sits at
+    (1-2w) O + w H1 + w H2 (sim/norm.c:1188-1193)"""
+    g, meta, system, ew = load("tip4p216")
+    assert system.ndep == 216
+    for d in range(g["r"].shape[0]):
+        assert np.abs(O.depend_r(system, g["r"][d]) - g["r"][d]).max() < 1e-10
+
+
+def test_dependant_step_matches_reference_trajectory():
+    """leap-frog + SHAKE of TIP4P/2005 with the M-site force moved onto O, H,
+    H before the step (sim/constrd.c:747) and M placed after it"""
+    g, meta, system, ew = load("tip4p216")
+    p = meta["params"]
+    orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
+    R, F = g["r"], g["f"]
+    f = O.depend_f(system, F[2])
+    # the redistribution keeps the total force and the torque about any point
+    dep = system.dep_site
+    assert np.allclose(f.sum(0) - f[dep].sum(0), F[2].sum(0), atol=1e-7)
+    rn, r1n, it, ek = orc.shake_step(R[2], R[2] - R[1], f, p["h"], eps=p["epsc"],
+                                     omega=meta["omegac"] / 2)
+    rn = O.depend_r(system, rn)
+    assert it > 0
+    assert np.abs(rn - R[3]).max() < 1e-9
+    # VERLET=3 kinetic energy of the last step (massless M contributes none)
+    _, _, _, ek = orc.shake_step(R[3], R[3] - R[2], O.depend_f(system, F[3]), p["h"],
+                                 eps=p["epsc"], omega=meta["omegac"] / 2)
+    assert abs(ek / meta["Ekin_last"] - 1) < 5e-9
+
+
+def test_reference_states_are_normalized():
+    """cook's dumped positions are normalized: every molecule's lowest
+    massive-site coordinate lies in [r0, r0 + L) with r0 = 0.15 (the value
+    cook picks for Verlet/SHAKE), so the oracle's normalize leaves them alone"""
+    for case in ("spce216", "brine532", "tip4p216"):
+        g, meta, system, ew = load(case)
+        for d in range(g["r"].shape[0]):
+            assert np.array_equal(O.normalize(system, g["r"][d], ew["L"]), g["r"][d])
