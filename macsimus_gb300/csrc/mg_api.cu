@@ -77,6 +77,11 @@ struct mg_ctx {
   int ndep = 0;
   int *d_dep_site = nullptr, *d_dep_first = nullptr, *d_dep_parent = nullptr;
   double* d_dep_w = nullptr;
+  // intramolecular (excluded) charge pairs of the mixed cell path
+  int* d_xfirst = nullptr;
+  int2* d_xpair = nullptr;
+  double4* d_xq = nullptr;
+  int nxblocks = 0;
   float* d_plb = nullptr;  // playback frame staging
   // reduction outputs
   double* d_sums = nullptr;  // [0..9] pair, [10..16] k-space, [17] kinetic
@@ -551,7 +556,9 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
                                      ctx->d_idx, ctx->d_order, ns, 0, ctx->sort_bits));
   CK(cudaMalloc(&ctx->d_sort_tmp, ctx->sort_tmp_bytes));
   CK(upload(&ctx->d_stencil, st.data(), st.size()));
-  ctx->nepart = std::max(ctx->ncell, std::max(list_blocks(ns, true), list_blocks(ns, false)));
+  ctx->nxblocks = (t->nmol + EXCL_THREADS - 1) / EXCL_THREADS;
+  ctx->nepart = std::max(ctx->ncell + ctx->nxblocks,
+                         std::max(list_blocks(ns, true), list_blocks(ns, false)));
   CK(dalloc(&ctx->d_epart, (size_t)ctx->nepart * 10));
   if (ctx->use_list) {
     // capacity: the largest expected count in a sphere of the list radius at
@@ -605,6 +612,26 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
     CK(dalloc(&ctx->d_Wd, nk));
   }
   CK(upload(&ctx->d_mol_first, t->mol_first, t->nmol + 1));
+  {
+    // every pair of sites of one molecule with a charge product is an Ewald
+    // exclusion (the r-space term of a rigid molecule is not counted)
+    std::vector<int> xfirst(t->nmol + 1, 0);
+    std::vector<int2> xpair;
+    std::vector<double4> xq;
+    for (int n = 0; n < t->nmol; n++) {
+      for (int i = t->mol_first[n]; i < t->mol_first[n + 1]; i++)
+        for (int j = i + 1; j < t->mol_first[n + 1]; j++) {
+          const PairD& P = pd[ctx->h_kind[i] * ctx->nkind + ctx->h_kind[j]];
+          if (P.qq == 0 && P.qpc == 0 && P.qcp == 0 && P.qpp == 0) continue;
+          xpair.push_back(make_int2(i, j));
+          xq.push_back(make_double4(P.qq, P.qpc, P.qcp, P.qpp));
+        }
+      xfirst[n + 1] = (int)xpair.size();
+    }
+    CK(upload(&ctx->d_xfirst, xfirst.data(), xfirst.size()));
+    CK(upload(&ctx->d_xpair, xpair.data(), xpair.size()));
+    CK(upload(&ctx->d_xq, xq.data(), xq.size()));
+  }
   CK(upload(&ctx->d_mol_cfirst, mcf.data(), mcf.size()));
   CK(upload(&ctx->d_cons, cons.data(), cons.size()));
   CK(upload(&ctx->d_bondq, bondq.data(), bondq.size()));
@@ -723,6 +750,28 @@ int build_lists(mg_ctx* ctx, const double* r_dev) {
   return fail(ctx, MG_ERR_SIZE, "neighbour list capacity");
 }
 
+ExclArgs excl_args(mg_ctx* ctx, const double* r_dev, double* f) {
+  ExclArgs a;
+  a.nmol = ctx->nmol;
+  a.ns = ctx->ns;
+  a.xfirst = ctx->d_xfirst;
+  a.xpair = ctx->d_xpair;
+  a.xq = ctx->d_xq;
+  a.Lx = ctx->L[0];
+  a.Ly = ctx->L[1];
+  a.Lz = ctx->L[2];
+  a.iLx = 1 / ctx->L[0];
+  a.iLy = 1 / ctx->L[1];
+  a.iLz = 1 / ctx->L[2];
+  a.cutoff_sq = ctx->cutoff * ctx->cutoff;
+  a.alpha = (float)ctx->alpha;
+  a.r = r_dev;
+  a.f = f;
+  // energy rows after the cell kernel's
+  a.epart = ctx->d_epart + (size_t)ctx->ncell * 10;
+  return a;
+}
+
 int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) {
   Launch L = launch(ctx);
   const int ns = ctx->ns;
@@ -833,6 +882,11 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
     } else {
       PROF("pair_mixed", k_pair_mixed(L, pa, ctx->d_pj, ctx->d_ptabf, ctx->d_erd, ctx->d_eru,
                                       measure, ctx->polar));
+      // after the pair kernel, before the k-space forces are added: the same
+      // summation order with and without the concurrent k-space chain
+      ExclArgs xa = excl_args(ctx, r_dev, f_dev);
+      PROF("exclusions", k_excl_mixed(L, xa, measure, ctx->polar));
+      nerows = ctx->ncell + ctx->nxblocks;
     }
     if (fork) {
       CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
@@ -1060,7 +1114,8 @@ int mg_destroy(mg_ctx* ctx) {
                   ctx->d_qfix, ctx->d_adjtab, ctx->d_ag, ctx->d_aq, ctx->d_apart, ctx->d_adEq,
                   ctx->d_adLq, ctx->d_ags, ctx->d_atpart, ctx->d_aT, ctx->d_fk,
                   ctx->d_chi, ctx->d_zth, ctx->d_step, ctx->d_dep_site, ctx->d_dep_first,
-                  ctx->d_dep_parent, ctx->d_dep_w, ctx->d_plb};
+                  ctx->d_dep_parent, ctx->d_dep_w, ctx->d_plb, ctx->d_xfirst, ctx->d_xpair,
+                  ctx->d_xq};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ctx->h_sums) cudaFreeHost(ctx->h_sums);

@@ -87,6 +87,19 @@ __device__ __forceinline__ void excl_acc(float dx, float dy, float dz, double qq
   }
 }
 
+// FP32 sum with a compensation term: s + c carries the sum of the added
+// values to about FP64 accuracy for the few hundred terms of a site
+// (Knuth's TwoSum, exact error of each addition into c)
+struct CSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float t = s + x, bb = t - s;
+    c += (s - (t - bb)) + (x - bb);
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
 struct PvF {
   float p0, p1, p2, p3, p4, p5;
   __device__ __forceinline__ void zero() { p0 = p1 = p2 = p3 = p4 = p5 = 0.f; }

@@ -38,6 +38,14 @@ struct PairF {
 struct PairD {
   double C1q, C2q, A4, E24, Sq, qq, A, E4, qpc, qcp, qpp, pad;
 };
+// the FP32 fields of PairF alone (the first 48 bytes), as the cell pair
+// kernel keeps them in shared memory
+struct PairFS {
+  float C1q, C2q, A4, E24;
+  float Sq, qq, A, E4;
+  float qpc, qcp, qpp, pad;
+};
+static_assert(sizeof(PairF) == 80 && sizeof(PairFS) == 48, "PairFS is the head of PairF");
 
 // one k-space task: a run of <=KZT consecutive kz of one (kx,ky) column
 struct KTask {
@@ -177,6 +185,23 @@ struct ShakeArgs {
   double r0, Lb[3];
 };
 cudaError_t k_shake(const Launch& L, const ShakeArgs& a);
+
+// Ewald exclusion corrections of the intramolecular pairs, one thread per
+// molecule (mixed cell path: the pair kernel skips these pairs)
+struct ExclArgs {
+  int nmol, ns;
+  const int* xfirst;    // [nmol+1] pair range of each molecule
+  const int2* xpair;    // (i, j), i < j, sites of one molecule
+  const double4* xq;    // charge products: centre-centre, Drude(i)-centre(j),
+                        // centre(i)-Drude(j), Drude-Drude
+  double Lx, Ly, Lz, iLx, iLy, iLz, cutoff_sq;
+  float alpha;
+  const double* r;      // positions (+ Drude offsets in the second half)
+  double* f;            // forces, added to
+  double* epart;        // [nblocks * 10] energy rows (measure)
+};
+constexpr int EXCL_THREADS = 128;
+cudaError_t k_excl_mixed(const Launch& L, const ExclArgs& a, bool measure, bool polar);
 
 // neighbour lists (mg_nlist.cu)
 struct ListArgs {

@@ -151,21 +151,30 @@ constexpr int FOLD = 8;   // stencil cells per FP32 force batch before the FP64 
 // takes its nearest image from its own fixed-point difference.
 // NW warps per CTA (the autotuner picks 4 or 8); STAB: the force spline in
 // shared memory (dynamic, ntab float4) instead of read through L1.
+// Intramolecular pairs are skipped: their Ewald exclusion terms come from
+// excl_mixed_kernel, once per pair.  Forces are summed in FP32 per batch of
+// FOLD stencil cells and folded into an FP32 sum with a compensation term
+// (Knuth's TwoSum): no FP64 instruction in the loop (the FP64 pipe of this
+// GPU is narrow and also serves the float/double conversions).
 template <bool MEASURE, bool POLAR, bool REL, int NW, bool STAB>
 __global__ void __launch_bounds__(NW * 32)
     pair_mixed_kernel(PairArgs a, const int4* __restrict__ pj, const PairF* __restrict__ ptab_g,
                       const float4* __restrict__ erd_g, const float4* __restrict__ eru, float sx,
                       float sy, float sz, float cq, float sgrid, float alpha) {
   constexpr int NT = NW * 32;
-  extern __shared__ float4 s_erd[];
-  __shared__ PairF ptab[MAX_KINDS * MAX_KINDS];
+  // dynamic shared memory: the nk x nk FP32 pair table, then (STAB) the
+  // force spline
+  extern __shared__ float4 dyn_smem[];
   __shared__ int4 sj[NW][32];
   __shared__ float4 sjd[POLAR ? NW : 1][32];
   __shared__ double red[NW][32][POLAR ? 6 : 3];
   __shared__ double ered[NT];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nk = a.nkind, ntab = a.ntab;
-  for (int t = threadIdx.x; t < nk * nk; t += NT) ptab[t] = ptab_g[t];
+  PairFS* ptab = reinterpret_cast<PairFS*>(dyn_smem);
+  float4* s_erd = dyn_smem + 3 * nk * nk;
+  for (int t = threadIdx.x; t < 3 * nk * nk; t += NT)
+    dyn_smem[t] = reinterpret_cast<const float4*>(ptab_g + t / 3)[t % 3];
   if (STAB)
     for (int t = threadIdx.x; t < ntab; t += NT) s_erd[t] = erd_g[t];
   const float4* erd = STAB ? s_erd : erd_g;
@@ -191,7 +200,7 @@ __global__ void __launch_bounds__(NW * 32)
     const float xi = (float)(int)((unsigned)me.x - refx) * sx,
                 yi = (float)(int)((unsigned)me.y - refy) * sy,
                 zi = (float)(int)((unsigned)me.z - refz) * sz;
-    double fx = 0, fy = 0, fz = 0, gx = 0, gy = 0, gz = 0;
+    CSum fx, fy, fz, gx, gy, gz;
     float ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;
     float e_el = 0, e_lj = 0, e_vir = 0;
     PvF pv;
@@ -235,23 +244,11 @@ __global__ void __launch_bounds__(NW * 32)
             dz = (float)(int)((unsigned)me.z - (unsigned)q.z) * sz;
           }
           const float rr = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          if (!vi || rr >= cq || j0 + jb + jj == ti) continue;
-          const PairF P = ptab[kind_i * nk + (q.w & 255)];
+          // the site itself and its own molecule (exclusions) are skipped
+          if (!vi || rr >= cq || (q.w >> 8) == mol_i) continue;
+          const PairFS P = ptab[kind_i * nk + (q.w & 255)];
           float4 qd = make_float4(0.f, 0.f, 0.f, 0.f);
           if (POLAR) qd = sjd[warp][jj];
-          if ((q.w >> 8) == mol_i) {
-            if (P.qq != 0.f) excl_acc<MEASURE>(dx, dy, dz, P.qqd, alpha, fx, fy, fz, en);
-            if (POLAR) {
-              if (P.qpc != 0.f)
-                excl_acc<MEASURE>(dx + md.x, dy + md.y, dz + md.z, P.qpcd, alpha, gx, gy, gz, en);
-              if (P.qcp != 0.f)
-                excl_acc<MEASURE>(dx - qd.x, dy - qd.y, dz - qd.z, P.qcpd, alpha, fx, fy, fz, en);
-              if (P.qpp != 0.f)
-                excl_acc<MEASURE>(dx + md.x - qd.x, dy + md.y - qd.y, dz + md.z - qd.z, P.qppd,
-                                  alpha, gx, gy, gz, en);
-            }
-            continue;
-          }
           float f = 0;
           if (rr < P.C2q) {
             float U;
@@ -316,23 +313,23 @@ __global__ void __launch_bounds__(NW * 32)
       }
       if (++nb == FOLD) {
         nb = 0;
-        fx += ax; fy += ay; fz += az;
+        fx.add(ax); fy.add(ay); fz.add(az);
         ax = ay = az = 0;
         if (POLAR) {
-          gx += bx; gy += by; gz += bz;
+          gx.add(bx); gy.add(by); gz.add(bz);
           bx = by = bz = 0;
         }
       }
     }
-    fx += ax; fy += ay; fz += az;
-    red[warp][lane][0] = fx;
-    red[warp][lane][1] = fy;
-    red[warp][lane][2] = fz;
+    fx.add(ax); fy.add(ay); fz.add(az);
+    red[warp][lane][0] = fx.value();
+    red[warp][lane][1] = fy.value();
+    red[warp][lane][2] = fz.value();
     if (POLAR) {
-      gx += bx; gy += by; gz += bz;
-      red[warp][lane][POLAR ? 3 : 0] = gx;
-      red[warp][lane][POLAR ? 4 : 0] = gy;
-      red[warp][lane][POLAR ? 5 : 0] = gz;
+      gx.add(bx); gy.add(by); gz.add(bz);
+      red[warp][lane][POLAR ? 3 : 0] = gx.value();
+      red[warp][lane][POLAR ? 4 : 0] = gy.value();
+      red[warp][lane][POLAR ? 5 : 0] = gz.value();
     }
     __syncthreads();
     if (warp == 0 && vi) {
@@ -377,12 +374,14 @@ cudaError_t k_pair_mixed(const Launch& L, const PairArgs& a, const int4* pj, con
   const bool rel = !a.allpairs;
   const int nw = a.pair_warps == 8 ? 8 : 4;
   const bool stab = a.spline_smem && !measure;
-  const size_t dsm = stab ? sizeof(float4) * (size_t)a.ntab : 0;
+  const size_t dsm = sizeof(PairFS) * (size_t)a.nkind * a.nkind +
+                     (stab ? sizeof(float4) * (size_t)a.ntab : 0);
   cudaError_t e = cudaSuccess;
 #define PAIR_MIXED(M, P, R, W, S)                                                               \
   do {                                                                                          \
-    if (S) e = cudaFuncSetAttribute(pair_mixed_kernel<M, P, R, W, S>,                           \
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);     \
+    if (dsm > 48 * 1024)                                                                        \
+      e = cudaFuncSetAttribute(pair_mixed_kernel<M, P, R, W, S>,                                \
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);          \
     if (e == cudaSuccess)                                                                       \
       pair_mixed_kernel<M, P, R, W, S><<<ncell, W * 32, dsm, L.s>>>(a, pj, ptab, erd, eru, sx,  \
                                                                      sy, sz, cq, sg, al);       \
@@ -551,6 +550,109 @@ __global__ void __launch_bounds__(PAIR_THREADS)
       __syncthreads();
     }
   }
+}
+
+// ------------------------------------------------ Ewald exclusion terms --
+
+// -erf(alpha r)/r of the intramolecular pairs (cook/ljqqnp.c:131-141, its
+// Drude forms cook/ljqqpol.c) for the mixed cell path: each pair once, from
+// the FP64 positions (nearest image), the term in FP32 as in the pair
+// kernels, forces and energy summed in FP64.  Pairs beyond the cutoff are
+// skipped, as the cell traversal never meets them.
+template <bool MEASURE>
+__device__ __forceinline__ void excl_pair(double dx, double dy, double dz, double qq, float alpha,
+                                          double* fi, double* fj, double* en) {
+  float fe;
+  const float e = excl_term<float>((float)(dx * dx + dy * dy + dz * dz), alpha, &fe);
+  const double fq = (double)fe * qq;
+  const double Fx = fq * dx, Fy = fq * dy, Fz = fq * dz;
+  fi[0] += Fx;
+  fi[1] += Fy;
+  fi[2] += Fz;
+  fj[0] -= Fx;
+  fj[1] -= Fy;
+  fj[2] -= Fz;
+  if (MEASURE) {
+    en[0] += (double)e * qq;
+    en[1] += Fx * dx;
+    en[2] += Fy * dy;
+    en[3] += Fz * dz;
+    en[4] += Fz * dy;
+    en[5] += Fx * dz;
+    en[6] += Fy * dx;
+  }
+}
+
+__device__ __forceinline__ double near_img(double d, double L, double iL) {
+  return d - L * rint(d * iL);
+}
+
+template <bool MEASURE, bool POLAR>
+__global__ void __launch_bounds__(EXCL_THREADS) excl_mixed_kernel(ExclArgs a) {
+  __shared__ double red[EXCL_THREADS];
+  const int n = blockIdx.x * EXCL_THREADS + threadIdx.x;
+  double en[7] = {0, 0, 0, 0, 0, 0, 0};
+  if (n < a.nmol) {
+    const long ns3 = 3 * (long)a.ns;
+    for (int p = a.xfirst[n]; p < a.xfirst[n + 1]; p++) {
+      const int2 ij = a.xpair[p];
+      const double4 q = a.xq[p];
+      const double* ri = a.r + 3 * (long)ij.x;
+      const double* rj = a.r + 3 * (long)ij.y;
+      const double dx = near_img(ri[0] - rj[0], a.Lx, a.iLx),
+                   dy = near_img(ri[1] - rj[1], a.Ly, a.iLy),
+                   dz = near_img(ri[2] - rj[2], a.Lz, a.iLz);
+      if (!(dx * dx + dy * dy + dz * dz < a.cutoff_sq)) continue;
+      double* fi = a.f + 3 * (long)ij.x;
+      double* fj = a.f + 3 * (long)ij.y;
+      if (q.x != 0) excl_pair<MEASURE>(dx, dy, dz, q.x, a.alpha, fi, fj, en);
+      if (POLAR) {
+        const double* mi = ri + ns3;
+        const double* mj = rj + ns3;
+        double* gi = fi + ns3;
+        double* gj = fj + ns3;
+        if (q.y != 0)  // Drude(i) - centre(j)
+          excl_pair<MEASURE>(dx + mi[0], dy + mi[1], dz + mi[2], q.y, a.alpha, gi, fj, en);
+        if (q.z != 0)  // centre(i) - Drude(j)
+          excl_pair<MEASURE>(dx - mj[0], dy - mj[1], dz - mj[2], q.z, a.alpha, fi, gj, en);
+        if (q.w != 0)  // Drude(i) - Drude(j)
+          excl_pair<MEASURE>(dx + mi[0] - mj[0], dy + mi[1] - mj[1], dz + mi[2] - mj[2], q.w,
+                             a.alpha, gi, gj, en);
+      }
+    }
+  }
+  if (MEASURE) {
+    // row layout of the pair kernels: el, lj, vir, Pvir[6], spare
+    constexpr int slot[7] = {0, 3, 4, 5, 6, 7, 8};
+    for (int k = 0; k < 10; k++) {
+      double v = 0;
+#pragma unroll
+      for (int m = 0; m < 7; m++)
+        if (slot[m] == k) v = en[m];
+      red[threadIdx.x] = v;
+      __syncthreads();
+      for (int w = EXCL_THREADS / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) a.epart[blockIdx.x * NEN + k] = red[0];
+      __syncthreads();
+    }
+  }
+}
+
+cudaError_t k_excl_mixed(const Launch& L, const ExclArgs& a, bool measure, bool polar) {
+  if (a.nmol <= 0) return cudaSuccess;
+  const int nb = cdiv(a.nmol, EXCL_THREADS);
+  if (measure) {
+    if (polar) excl_mixed_kernel<true, true><<<nb, EXCL_THREADS, 0, L.s>>>(a);
+    else excl_mixed_kernel<true, false><<<nb, EXCL_THREADS, 0, L.s>>>(a);
+  } else {
+    if (polar) excl_mixed_kernel<false, true><<<nb, EXCL_THREADS, 0, L.s>>>(a);
+    else excl_mixed_kernel<false, false><<<nb, EXCL_THREADS, 0, L.s>>>(a);
+  }
+  LAUNCHED(L);
+  return cudaGetLastError();
 }
 
 cudaError_t k_pair_fp64(const Launch& L, const PairArgs& a, const double4* pd, const PairD* ptab,
