@@ -134,6 +134,10 @@ typedef struct {
      no_normalize != 0 leaves the positions unwrapped. */
   double box_rmin;
   int no_normalize;
+  /* Ewald pass 2 of the FP32 path: 0 = the tensor cores when their shared
+     memory tiles fit (else the FP32 cores), 1 = FP32 cores, 2 = tensor cores
+     (TF32 split into three products, FP32 accuracy) */
+  int kspace_engine;
 } mg_params;
 
 /* Energies of one force evaluation (program units, K).
@@ -201,6 +205,12 @@ int mg_md_get_state(mg_ctx *ctx, double *r, double *r1);
    4 = centred, r - L/2.  The file layout (float header ns, -3 or -6 when
    centred, then the frames) is the caller's; the Python package writes it. */
 enum { MG_PLB_POS = 0, MG_PLB_VEL = 1, MG_PLB_DRUDE = 2 };
+
+/* Diagnostic: C[128 x n] = A[128 x k] B[n x k]^T (row-major FP32 host
+   arrays) on the tensor cores in TF32 with the descriptors, TMEM accumulator
+   and completion protocol of the tensor-core Ewald kernels; n a multiple of
+   16 in 16..256, k a multiple of 8 up to 64. */
+int mg_tc_selftest(const float *A, const float *B, float *C, int n, int k);
 int mg_playback_frame(mg_ctx *ctx, int what, int flags, float *frame);
 /* advance nsteps; energies of the last step in *en when en != NULL */
 int mg_md_steps(mg_ctx *ctx, int nsteps, mg_energy *en);

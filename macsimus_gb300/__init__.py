@@ -56,7 +56,7 @@ class Params(C.Structure):
                 ("nl_every", C.c_int), ("kspace_ctas_per_sm", C.c_int), ("pair_variant", C.c_int),
                 ("thermostat", C.c_int), ("T", C.c_double), ("tau_T", C.c_double),
                 ("thermo_f", C.c_double), ("seed", C.c_ulonglong), ("box_rmin", C.c_double),
-                ("no_normalize", C.c_int)]
+                ("no_normalize", C.c_int), ("kspace_engine", C.c_int)]
 
 
 class Energy(C.Structure):
@@ -113,6 +113,8 @@ def library():
         L.mg_md_set_state.argtypes = [vp, _dp, _dp]
         L.mg_md_get_state.argtypes = [vp, _dp, _dp]
         L.mg_playback_frame.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_float)]
+        _fp = C.POINTER(C.c_float)
+        L.mg_tc_selftest.argtypes = [_fp, _fp, _fp, C.c_int, C.c_int]
         L.mg_md_steps.argtypes = [vp, C.c_int, C.POINTER(Energy)]
         L.mg_selffield.argtypes = [vp, _dp, _dp, C.c_double, C.c_int, C.POINTER(Energy)]
         L.mg_set_stream.argtypes = [vp, vp]
@@ -178,7 +180,7 @@ def describe(system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None, 
              rshift=3, rplus=2.5, epsinf=3e33, h=0.002, epsc=1e-7, omegac=1.2, shake_maxit=1000,
              cells_per_cutoff=0, aspc_k=2, scf_iter=1, scf_omega=0.6, minqq=1.0, skin=0.0,
              nl_every=50, kspace_ctas_per_sm=0, pair_variant=0, thermostat=0, T=298.0,
-             tau_T=0.1, thermo_f=0.0, seed=0, box_rmin=0.0, normalize=True):
+             tau_T=0.1, thermo_f=0.0, seed=0, box_rmin=0.0, normalize=True, kspace_engine=0):
     """(mg_topology, mg_params, arrays to keep alive) of one box"""
     keep = []
 
@@ -255,6 +257,7 @@ def describe(system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None, 
     p.seed = seed
     p.box_rmin = box_rmin
     p.no_normalize = 0 if normalize else 1
+    p.kspace_engine = int(kspace_engine)
     return t, p, keep
 
 
@@ -266,7 +269,7 @@ class ForcePath:
                  shake_maxit=1000, cells_per_cutoff=0, aspc_k=2, scf_iter=1, scf_omega=0.6,
                  minqq=1.0, skin=0.0, nl_every=50, kspace_ctas_per_sm=0, pair_variant=0,
                  thermostat=0, T=298.0, tau_T=0.1, thermo_f=0.0, seed=0, box_rmin=0.0,
-                 normalize=True):
+                 normalize=True, kspace_engine=0):
         lib = library()
         self.system = system
         self.ns = system.ns
@@ -279,7 +282,8 @@ class ForcePath:
                                     kspace_ctas_per_sm=kspace_ctas_per_sm,
                                     pair_variant=pair_variant, thermostat=thermostat, T=T,
                                     tau_T=tau_T, thermo_f=thermo_f, seed=seed,
-                                    box_rmin=box_rmin, normalize=normalize)
+                                    box_rmin=box_rmin, normalize=normalize,
+                                    kspace_engine=kspace_engine)
         self.polar = getattr(system, "polar", False)
         Lb = np.broadcast_to(np.asarray(L, dtype=np.float64), (3,))
         st = C.c_int(0)

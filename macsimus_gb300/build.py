@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libmacgpu.so")
-SOURCES = ["mg_tables.cpp", "mg_kernels.cu", "mg_kspace.cu", "mg_api.cu", "mg_noalloc.cu", "mg_drude.cu", "mg_nlist.cu", "mg_widom.cu", "mg_adjoint.cu", "mg_thermo.cu", "mg_sites.cu"]
+SOURCES = ["mg_tables.cpp", "mg_kernels.cu", "mg_kspace.cu", "mg_api.cu", "mg_noalloc.cu", "mg_drude.cu", "mg_nlist.cu", "mg_widom.cu", "mg_adjoint.cu", "mg_thermo.cu", "mg_sites.cu", "mg_tc.cu", "mg_kspace_tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -66,6 +66,10 @@ struct mg_ctx {
   KTile* d_tiles = nullptr;
   int2* d_p1job = nullptr;
   int ntile = 0, np1job = 0;
+  // pass 2 on the tensor cores (FP32 path): operand tiles
+  int nkrows = 0;
+  bool kspace_tc = false;
+  float *d_za = nullptr, *d_vb = nullptr;
   // SHAKE
   int* d_mol_first = nullptr;
   int* d_mol_cfirst = nullptr;
@@ -583,6 +587,26 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   CK(upload(&ctx->d_col, cols.data(), cols.size()));
   CK(upload(&ctx->d_kvec, kvec.data(), kvec.size()));
   CK(upload(&ctx->d_krows, krows.data(), krows.size()));
+  ctx->nkrows = (int)krows.size();
+  if (p->kspace_engine < 0 || p->kspace_engine > 2)
+    return fail(ctx, MG_ERR_ARG, "kspace_engine: 0 auto, 1 FP32 cores, 2 tensor cores");
+  if (ctx->precision == MG_MIXED && p->kspace_engine != 1) {
+    KArgs kd;
+    kd.Kx = ctx->Kx;
+    kd.Ky = ctx->Ky;
+    kd.Kz = ctx->Kz;
+    kd.nq = ctx->nq;
+    const bool fits = kf_tc_fits(kd, ctx->nkrows);
+    if (!fits && p->kspace_engine == 2)
+      return fail(ctx, MG_ERR_SIZE, "the k set is too large for the tensor-core tiles");
+    ctx->kspace_tc = fits && ctx->nq > 0;
+    if (ctx->kspace_tc) {
+      const size_t KP = (size_t)kf_tc_kp(kd), ntm = (ctx->nq + 127) / 128,
+                   ntn = (4 * (size_t)ctx->nkrows + 127) / 128;
+      CK(dalloc(&ctx->d_za, ntm * 256 * KP));
+      CK(dalloc(&ctx->d_vb, ntn * 256 * KP));
+    }
+  }
   CK(upload(&ctx->d_tiles, tiles.data(), tiles.size()));
   CK(upload(&ctx->d_p1job, p1job.data(), p1job.size()));
   CK(upload(&ctx->d_ekk, ekk.data(), ekk.size()));
@@ -750,6 +774,14 @@ int build_lists(mg_ctx* ctx, const double* r_dev) {
   return fail(ctx, MG_ERR_SIZE, "neighbour list capacity");
 }
 
+// Ewald pass 2 of the FP32 path: tensor cores or FP32 cores
+cudaError_t kf_mixed(mg_ctx* ctx, const Launch& L, const KArgs& a) {
+  if (!ctx->kspace_tc) return k_kf_gemm_mixed(L, a, (const float2*)ctx->d_tab);
+  cudaError_t e = k_kf_tc_za(L, a, (const float2*)ctx->d_tab, ctx->d_za);
+  if (e != cudaSuccess) return e;
+  return k_kf_tc(L, a, ctx->nkrows, (const float2*)ctx->d_tab, ctx->d_za, ctx->d_vb);
+}
+
 ExclArgs excl_args(mg_ctx* ctx, const double* r_dev, double* f) {
   ExclArgs a;
   a.nmol = ctx->nmol;
@@ -847,6 +879,7 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
   ka.np1job = ctx->np1job;
   ka.qdrude = ctx->d_qdrude;
   ka.ns = ctx->ns;
+  ka.status = ctx->d_status;
   ListArgs la = list_args(ctx);
   int nerows = ctx->ncell;
   if (ctx->precision == MG_MIXED) {
@@ -864,7 +897,7 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
       PROFS("phase_tables", ks, k_phase_tables_mixed(LK, kk, r_dev, (float2*)ctx->d_tab, ctx->d_qfix));
       PROFS("ewald_sk", ks, k_sk_gemm_mixed(LK, kk, (const float2*)ctx->d_tab, (float2*)ctx->d_part));
       PROFS("ewald_sk_reduce", ks, k_sk_reduce_mixed(LK, kk, (const float2*)ctx->d_part, measure));
-      PROFS("ewald_kforce", ks, k_kf_gemm_mixed(LK, kk, (const float2*)ctx->d_tab));
+      PROFS("ewald_kforce", ks, kf_mixed(ctx, LK, kk));
       CK(cudaEventRecord(ctx->ev_join, ks));
     }
     PROF("gather", k_gather_mixed(L, ns, r_dev, ctx->d_order, ctx->d_kind, ctx->d_mol, ctx->L[0],
@@ -895,7 +928,7 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
       PROF("phase_tables", k_phase_tables_mixed(L, ka, r_dev, (float2*)ctx->d_tab, ctx->d_qfix));
       PROF("ewald_sk", k_sk_gemm_mixed(L, ka, (const float2*)ctx->d_tab, (float2*)ctx->d_part));
       PROF("ewald_sk_reduce", k_sk_reduce_mixed(L, ka, (const float2*)ctx->d_part, measure));
-      PROF("ewald_kforce", k_kf_gemm_mixed(L, ka, (const float2*)ctx->d_tab));
+      PROF("ewald_kforce", kf_mixed(ctx, L, ka));
     }
   } else {
     PROF("gather", k_gather_fp64(L, ns, r_dev, ctx->d_order, ctx->d_kind, ctx->d_mol, ctx->L[0],
@@ -1072,6 +1105,8 @@ int check_status(mg_ctx* ctx) {
   CK(cudaStreamSynchronize(ctx->stream));
   if (st & 2) return fail(ctx, MG_ERR_NONFINITE, "non-finite site position");
   if (st & 4) return fail(ctx, MG_ERR_SCF, "Drude displacement beyond el.minqq");
+  if (st & 16)
+    return fail(ctx, MG_ERR_CUDA, "a tensor-core Ewald pass gave up waiting for its operands");
   if (st & 8)
     return fail(ctx, MG_ERR_LIST,
                 "a site moved more than skin/2 between neighbour-list builds (larger skin or "
@@ -1115,7 +1150,7 @@ int mg_destroy(mg_ctx* ctx) {
                   ctx->d_adLq, ctx->d_ags, ctx->d_atpart, ctx->d_aT, ctx->d_fk,
                   ctx->d_chi, ctx->d_zth, ctx->d_step, ctx->d_dep_site, ctx->d_dep_first,
                   ctx->d_dep_parent, ctx->d_dep_w, ctx->d_plb, ctx->d_xfirst, ctx->d_xpair,
-                  ctx->d_xq};
+                  ctx->d_xq, ctx->d_za, ctx->d_vb};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ctx->h_sums) cudaFreeHost(ctx->h_sums);
@@ -1223,12 +1258,13 @@ int mg_ewald(mg_ctx* ctx, const double* r, double* f, double* energy) {
   ka.np1job = ctx->np1job;
   ka.qdrude = ctx->d_qdrude;
   ka.ns = ctx->ns;
+  ka.status = ctx->d_status;
   if (ctx->nq > 0) {
     if (ctx->precision == MG_MIXED) {
       CK(k_phase_tables_mixed(L, ka, ctx->d_rs, (float2*)ctx->d_tab, ctx->d_qfix));
       CK(k_sk_gemm_mixed(L, ka, (const float2*)ctx->d_tab, (float2*)ctx->d_part));
       CK(k_sk_reduce_mixed(L, ka, (const float2*)ctx->d_part, true));
-      CK(k_kf_gemm_mixed(L, ka, (const float2*)ctx->d_tab));
+      CK(kf_mixed(ctx, L, ka));
     } else {
       CK(k_phase_tables_fp64(L, ka, ctx->d_rs, (double2*)ctx->d_tab));
       CK(k_sk_gemm_fp64(L, ka, (const double2*)ctx->d_tab, (double2*)ctx->d_part));
@@ -1241,7 +1277,11 @@ int mg_ewald(mg_ctx* ctx, const double* r, double* f, double* energy) {
   CK(cudaMemcpyAsync(fk.data(), ctx->d_fs, nb, cudaMemcpyDeviceToHost, ctx->stream));
   int rc = fetch_sums(ctx);
   if (rc) return rc;
+  rc = fetch_status(ctx);
+  if (rc) return rc;
   CK(cudaStreamSynchronize(ctx->stream));
+  rc = check_status(ctx);
+  if (rc) return rc;
   for (size_t i = 0; i < fk.size(); i++) f[i] += fk[i];
   if (energy) *energy = (ctx->nq > 0 ? ctx->h_sums[10] / (4 * M_PI) : 0) + ctx->eself;
   return MG_OK;
@@ -1602,6 +1642,7 @@ KArgs kspace_args(mg_ctx* ctx) {
   ka.ekk = ctx->d_ekk;
   ka.S = ctx->d_S;
   ka.ns = ctx->ns;
+  ka.status = ctx->d_status;
   return ka;
 }
 

@@ -145,6 +145,7 @@ struct KArgs {
   int np1job;
   const int* qdrude;        // [nq] 1 if the charge is a Drude charge (or NULL)
   int ns;
+  int* status;              // device status word (tensor-core waits that give up: 16)
 };
 cudaError_t k_add_forces(const Launch& L, size_t n, const double* fk, double* f);
 // qf: [nq] scratch for the charges' fixed-point coordinates
@@ -162,6 +163,13 @@ cudaError_t k_sk_gemm_fp64(const Launch& L, const KArgs& a, const double2* tab, 
 cudaError_t k_kf_gemm_mixed(const Launch& L, const KArgs& a, const float2* tab);
 cudaError_t k_kf_gemm_fp64(const Launch& L, const KArgs& a, const double2* tab);
 cudaError_t k_reduce_sum(const Launch& L, const double* part, int nrows, int width, double* out);
+// pass 2 on the tensor cores (mg_kspace_tc.cu): za [ceil(nq/128) * 256 * KP],
+// vb [ceil(4 nrows/128) * 256 * KP] floats, KP = 2 Kz + 1 rounded up to 8
+int kf_tc_kp(const KArgs& a);
+bool kf_tc_fits(const KArgs& a, int nrows);
+cudaError_t k_kf_tc_za(const Launch& L, const KArgs& a, const float2* tab, float* za);
+cudaError_t k_kf_tc(const Launch& L, const KArgs& a, int nrows, const float2* tab,
+                    const float* za, float* vb);
 
 struct ShakeArgs {
   int nmol;
