@@ -70,6 +70,7 @@ struct mg_ctx {
   int nkrows = 0;
   bool kspace_tc = false;
   float *d_za = nullptr, *d_vb = nullptr;
+  TcRow* d_tcrows = nullptr;
   // SHAKE
   int* d_mol_first = nullptr;
   int* d_mol_cfirst = nullptr;
@@ -601,10 +602,11 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
       return fail(ctx, MG_ERR_SIZE, "the k set is too large for the tensor-core tiles");
     ctx->kspace_tc = fits && ctx->nq > 0;
     if (ctx->kspace_tc) {
-      const size_t KP = (size_t)kf_tc_kp(kd), ntm = (ctx->nq + 127) / 128,
-                   ntn = (4 * (size_t)ctx->nkrows + 127) / 128;
-      CK(dalloc(&ctx->d_za, ntm * 256 * KP));
-      CK(dalloc(&ctx->d_vb, ntn * 256 * KP));
+      CK(dalloc(&ctx->d_za, kf_tc_za_floats(kd)));
+      CK(dalloc(&ctx->d_vb, kf_tc_vb_floats(kd, ctx->nkrows)));
+      std::vector<TcRow> tr;
+      kf_tc_rows(kd, krows, &tr);
+      CK(upload(&ctx->d_tcrows, tr.data(), tr.size()));
     }
   }
   CK(upload(&ctx->d_tiles, tiles.data(), tiles.size()));
@@ -779,7 +781,7 @@ cudaError_t kf_mixed(mg_ctx* ctx, const Launch& L, const KArgs& a) {
   if (!ctx->kspace_tc) return k_kf_gemm_mixed(L, a, (const float2*)ctx->d_tab);
   cudaError_t e = k_kf_tc_za(L, a, (const float2*)ctx->d_tab, ctx->d_za);
   if (e != cudaSuccess) return e;
-  return k_kf_tc(L, a, ctx->nkrows, (const float2*)ctx->d_tab, ctx->d_za, ctx->d_vb);
+  return k_kf_tc(L, a, ctx->nkrows, ctx->d_tcrows, ctx->d_za, ctx->d_vb);
 }
 
 ExclArgs excl_args(mg_ctx* ctx, const double* r_dev, double* f) {
@@ -1150,7 +1152,7 @@ int mg_destroy(mg_ctx* ctx) {
                   ctx->d_adLq, ctx->d_ags, ctx->d_atpart, ctx->d_aT, ctx->d_fk,
                   ctx->d_chi, ctx->d_zth, ctx->d_step, ctx->d_dep_site, ctx->d_dep_first,
                   ctx->d_dep_parent, ctx->d_dep_w, ctx->d_plb, ctx->d_xfirst, ctx->d_xpair,
-                  ctx->d_xq, ctx->d_za, ctx->d_vb};
+                  ctx->d_xq, ctx->d_za, ctx->d_vb, ctx->d_tcrows};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ctx->h_sums) cudaFreeHost(ctx->h_sums);

@@ -163,12 +163,20 @@ cudaError_t k_sk_gemm_fp64(const Launch& L, const KArgs& a, const double2* tab, 
 cudaError_t k_kf_gemm_mixed(const Launch& L, const KArgs& a, const float2* tab);
 cudaError_t k_kf_gemm_fp64(const Launch& L, const KArgs& a, const double2* tab);
 cudaError_t k_reduce_sum(const Launch& L, const double* part, int nrows, int width, double* out);
-// pass 2 on the tensor cores (mg_kspace_tc.cu): za [ceil(nq/128) * 256 * KP],
-// vb [ceil(4 nrows/128) * 256 * KP] floats, KP = 2 Kz + 1 rounded up to 8
+// pass 2 on the tensor cores (mg_kspace_tc.cu); KP = 2 Kz + 1 rounded up
+// to 8; per k row (kx, ky) as floats and the offsets of X(kx), Y(ky) in the
+// kernel's phase block
+struct TcRow {
+  float kx, ky;
+  int ox, oy;
+};
 int kf_tc_kp(const KArgs& a);
 bool kf_tc_fits(const KArgs& a, int nrows);
+size_t kf_tc_za_floats(const KArgs& a);
+size_t kf_tc_vb_floats(const KArgs& a, int nrows);
+void kf_tc_rows(const KArgs& a, const std::vector<KRow>& krows, std::vector<TcRow>* out);
 cudaError_t k_kf_tc_za(const Launch& L, const KArgs& a, const float2* tab, float* za);
-cudaError_t k_kf_tc(const Launch& L, const KArgs& a, int nrows, const float2* tab,
+cudaError_t k_kf_tc(const Launch& L, const KArgs& a, int nrows, const TcRow* rows,
                     const float* za, float* vb);
 
 struct ShakeArgs {

@@ -13,13 +13,15 @@
 // kf_tc_vb_kernel).  The product runs on the tcgen05 tensor cores in TF32
 // with each operand split as hi + lo (hi TF32-rounded, lo the FP32 rest) and
 // three products hi*hi + hi*lo + lo*hi accumulated in FP32 in TMEM: the
-// result carries FP32 accuracy.  The epilogue (four warps, one TMEM lane per
-// charge) forms A from the phase rows and accumulates the force.
+// result carries FP32 accuracy.  The epilogue forms A from the phase rows
+// and accumulates the force.
 //
-// One CTA per 128 charges: warp 4 streams the V tiles into shared memory
-// with bulk copies (two stages) and issues the MMAs into two TMEM buffers
-// of 128 columns; warps 0-3 drain the other buffer meanwhile.  Every wait is
-// bounded; a wait that gives up sets bit 16 of the status word.
+// One CTA per 128 charges, 9 warps.  Warp 8 bulk-copies the charges' tile
+// (Z and their phase rows) and streams the V tiles into shared memory (two
+// stages), and one of its threads issues the MMAs into two TMEM buffers of
+// 128 columns.  Warps 0-7 drain the other buffer meanwhile: two warps per
+// TMEM lane quarter (32 charges), each taking 16 of the tile's 32 rows.
+// Every wait is bounded; a wait that gives up sets bit 16 of the status word.
 #include "mg_device.cuh"
 #include "mg_internal.h"
 #include "mg_tc.cuh"
@@ -30,25 +32,39 @@ constexpr int TC_M = 128;             // charges per tile
 constexpr int TC_N = 128;             // D columns per tile
 constexpr int TC_ROWS = TC_N / 4;     // k rows per tile
 constexpr long TC_WAIT = 1L << 24;    // polls before a wait gives up
+constexpr int TC_EPI_WARPS = 8;       // two per TMEM lane quarter
+constexpr int TC_THREADS = 32 * (TC_EPI_WARPS + 1);
 
-// A operand: z_j of every charge, tile by tile (hi then lo, K-major layout)
-__global__ void kf_tc_za_kernel(int nq, int ntm, int row, int oz, int Kz, int KP,
-                                const float2* __restrict__ tab, float* __restrict__ za) {
+// A tiles, one per 128 charges: z_j (hi, then lo, K-major layout), then the
+// charges' phase values X(0..Kx) | Y(-Ky..Ky) transposed ([e][128] float2)
+// for the epilogue; tile stride 256 (KP + nxy) floats
+__global__ void kf_tc_prep_kernel(int nq, int ntm, int row, int oz, int Kz, int KP, int nxy,
+                                  const float2* __restrict__ tab, float* __restrict__ za) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long)ntm * TC_M * KP) return;
-  const int j = (int)(t / KP), kk = (int)(t % KP);
-  float v = 0.f;
-  if (j < nq) {
-    const float2* zr = tab + (long)j * row + oz;   // Z(0..Kz)
-    if (kk <= Kz) v = zr[kk].x;
-    else if (kk <= 2 * Kz) v = zr[kk - Kz].y;
+  const long nz = (long)ntm * TC_M * KP;
+  const size_t tile_f = (size_t)2 * TC_M * (KP + nxy);
+  if (t < nz) {
+    const int j = (int)(t / KP), kk = (int)(t % KP);
+    float v = 0.f;
+    if (j < nq) {
+      const float2* zr = tab + (long)j * row + oz;   // Z(0..Kz)
+      if (kk <= Kz) v = zr[kk].x;
+      else if (kk <= 2 * Kz) v = zr[kk - Kz].y;
+    }
+    float hi, lo;
+    tc::tf32_split(v, hi, lo);
+    float* base = za + (size_t)(j / TC_M) * tile_f;
+    const uint32_t o = tc::kmajor_offset(j % TC_M, kk, KP) >> 2;
+    base[o] = hi;
+    base[(size_t)TC_M * KP + o] = lo;
+    return;
   }
-  float hi, lo;
-  tc::tf32_split(v, hi, lo);
-  float* base = za + (size_t)(j / TC_M) * 2 * TC_M * KP;
-  const uint32_t o = tc::kmajor_offset(j % TC_M, kk, KP) >> 2;
-  base[o] = hi;
-  base[(size_t)TC_M * KP + o] = lo;
+  const long u = t - nz;
+  if (u >= (long)ntm * nxy * TC_M) return;
+  const int tm = (int)(u / ((long)nxy * TC_M)), e = (int)(u / TC_M % nxy), m = (int)(u % TC_M);
+  const int j = tm * TC_M + m;
+  float2* xy = reinterpret_cast<float2*>(za + (size_t)tm * tile_f + (size_t)2 * TC_M * KP);
+  xy[(size_t)e * TC_M + m] = j < nq ? tab[(long)j * row + e] : make_float2(0.f, 0.f);
 }
 
 // B operand: per row r the columns 4r .. 4r+3 = coefficients of H.x, H.y,
@@ -88,11 +104,10 @@ __global__ void kf_tc_vb_kernel(int nrows, int ntn, int Kz, int KP, const KRow* 
 }
 
 struct KfTc {
-  int nq, ns, KP, ntm, ntn, nrows, nxy, oyl, row;
+  int nq, ns, KP, ntm, ntn, nrows, nxy;
   const float* za;
   const float* vb;
-  const float2* tab;
-  const KRow* krows;
+  const TcRow* rows;
   const int* qsite;
   const int* qdrude;
   double Lx, Ly, Lz;
@@ -100,25 +115,19 @@ struct KfTc {
   int* status;
 };
 
-// per k row: (kx, ky) as floats and the offsets of X(kx), Y(ky) in the
-// shared phase block
-struct TcRow {
-  float kx, ky;
-  int ox, oy;
-};
-
+// A tile (Z hi | lo, phase block), two V stages, the row table, barriers
 size_t kf_tc_smem(int KP, int nxy, int nrows) {
-  const size_t ab = (size_t)2 * TC_M * KP * 4;   // one operand tile, hi + lo
-  return 3 * ab + (size_t)nxy * TC_M * sizeof(float2) + (size_t)nrows * sizeof(TcRow) + 128;
+  return (size_t)1024 * (3 * KP + nxy) + (size_t)nrows * sizeof(TcRow) + 128;
 }
 
-__global__ void __launch_bounds__(160, 1) kf_tc_kernel(KfTc a) {
+__global__ void __launch_bounds__(TC_THREADS, 1) kf_tc_kernel(KfTc a) {
   extern __shared__ __align__(1024) unsigned char smem_tc[];
-  const uint32_t ab = (uint32_t)(2 * TC_M * a.KP * 4);
-  unsigned char* As = smem_tc;                 // Z tile (hi | lo)
-  unsigned char* Bs = smem_tc + ab;            // two V stages
-  float2* XY = reinterpret_cast<float2*>(smem_tc + 3 * (size_t)ab);   // [nxy][128]
-  TcRow* rk = reinterpret_cast<TcRow*>(XY + (size_t)a.nxy * TC_M);
+  const uint32_t zb = 1024u * a.KP;              // Z tile bytes (hi | lo); also a V tile
+  const uint32_t ab = zb + 1024u * a.nxy;        // A tile with the phase block
+  unsigned char* As = smem_tc;
+  const float2* XY = reinterpret_cast<const float2*>(smem_tc + zb);   // [nxy][128]
+  unsigned char* Bs = smem_tc + ab;              // two V stages of zb bytes
+  TcRow* rk = reinterpret_cast<TcRow*>(Bs + 2 * (size_t)zb);
   uint64_t* bars = reinterpret_cast<uint64_t*>(rk + a.nrows);
   uint64_t* bar_a = bars;
   uint64_t* full = bars + 1;    // [2] V stage loaded
@@ -128,42 +137,35 @@ __global__ void __launch_bounds__(160, 1) kf_tc_kernel(KfTc a) {
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 9);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int mt = blockIdx.x;
+  constexpr int PW = TC_EPI_WARPS;               // producer warp
 
-  if (warp < 4) {
-    for (int t = tid; t < a.nxy * TC_M; t += 128) {
-      const int e = t / TC_M, m = t % TC_M, j = mt * TC_M + m;
-      XY[t] = j < a.nq ? a.tab[(long)j * a.row + e] : make_float2(0.f, 0.f);
-    }
-    for (int r = tid; r < a.nrows; r += 128) {
-      const KRow rw = a.krows[r];
-      rk[r] = TcRow{(float)rw.kx, (float)rw.ky, rw.kx * TC_M, (a.oyl + rw.ky) * TC_M};
-    }
-  }
   if (tid == 0) {
     tc::mbar_init(bar_a, 1);
     for (int s = 0; s < 2; s++) {
       tc::mbar_init(full + s, 1);
       tc::mbar_init(bfree + s, 1);
       tc::mbar_init(tfull + s, 1);
-      tc::mbar_init(tfree + s, 4);
+      tc::mbar_init(tfree + s, TC_EPI_WARPS);
     }
   }
-  if (warp == 4) tc::tmem_alloc(tslot, 2 * TC_N);
+  if (warp == PW) tc::tmem_alloc(tslot, 2 * TC_N);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tbase = *tslot;
 
-  if (warp == 4) {
+  if (warp == PW) {
     if (lane == 0) {
-      const uint32_t half = (uint32_t)(TC_M * a.KP * 4), sbo = (uint32_t)(a.KP / 4) * 128;
+      const uint32_t half = zb / 2, sbo = (uint32_t)(a.KP / 4) * 128;
       const uint32_t idesc = tc::idesc_tf32(TC_M, TC_N);
-      const size_t tile_f = (size_t)2 * TC_M * a.KP;   // floats per operand tile
-      tc::mbar_expect_tx(bar_a, ab);
-      tc::bulk_g2s(As, a.za + (size_t)mt * tile_f, ab, bar_a);
+      const size_t atile_f = (size_t)2 * TC_M * (a.KP + a.nxy), vtile_f = (size_t)2 * TC_N * a.KP;
+      const uint32_t rbytes = (uint32_t)(a.nrows * sizeof(TcRow));
+      tc::mbar_expect_tx(bar_a, ab + rbytes);
+      tc::bulk_g2s(As, a.za + (size_t)mt * atile_f, ab, bar_a);
+      tc::bulk_g2s(rk, a.rows, rbytes, bar_a);
       for (int t = 0; t < 2 && t < a.ntn; t++) {
-        tc::mbar_expect_tx(full + t, ab);
-        tc::bulk_g2s(Bs + (size_t)t * ab, a.vb + (size_t)t * tile_f, ab, full + t);
+        tc::mbar_expect_tx(full + t, zb);
+        tc::bulk_g2s(Bs + (size_t)t * zb, a.vb + (size_t)t * vtile_f, zb, full + t);
       }
       bool ok = tc::mbar_wait(bar_a, 0, TC_WAIT);
       const uint32_t a_hi = tc::smem_u32(As), a_lo = a_hi + half;
@@ -174,7 +176,7 @@ __global__ void __launch_bounds__(160, 1) kf_tc_kernel(KfTc a) {
         if (!ok) break;
         tc::fence_after_sync();
         const uint32_t d = tbase + (uint32_t)(s * TC_N);
-        const uint32_t b_hi = tc::smem_u32(Bs + (size_t)s * ab), b_lo = b_hi + half;
+        const uint32_t b_hi = tc::smem_u32(Bs + (size_t)s * zb), b_lo = b_hi + half;
         for (int ks = 0; ks < a.KP / 8; ks++) {
           const uint32_t o = 256u * ks;
           tc::mma_tf32(d, tc::smem_desc(a_hi + o, 128, sbo), tc::smem_desc(b_hi + o, 128, sbo),
@@ -191,82 +193,127 @@ __global__ void __launch_bounds__(160, 1) kf_tc_kernel(KfTc a) {
           const int s1 = (t + 1) & 1;
           ok = tc::mbar_wait(bfree + s1, ((t - 1) >> 1) & 1, TC_WAIT);
           if (!ok) break;
-          tc::mbar_expect_tx(full + s1, ab);
-          tc::bulk_g2s(Bs + (size_t)s1 * ab, a.vb + (size_t)(t + 1) * tile_f, ab, full + s1);
+          tc::mbar_expect_tx(full + s1, zb);
+          tc::bulk_g2s(Bs + (size_t)s1 * zb, a.vb + (size_t)(t + 1) * vtile_f, zb, full + s1);
         }
       }
       if (!ok) atomicOr(a.status, 16);
     }
     __syncwarp();
   } else {
-    const int m = 32 * warp + lane;
+    // warp w: TMEM lanes 32 (w % 4) .. (its charges), columns 64 (w / 4) ..
+    // (rows 16 (w / 4) .. 16 (w / 4) + 15 of each tile)
+    const int qd = warp & 3, hf = warp >> 2;
+    const int m = 32 * qd + lane;
+    bool ok = tc::mbar_wait(bar_a, 0, TC_WAIT);
+    ok = __all_sync(0xffffffffu, ok);
     CSum Fx, Fy, Fz;
-    bool ok = true;
-    for (int t = 0; t < a.ntn; t++) {
+    for (int t = 0; ok && t < a.ntn; t++) {
       const int s = t & 1;
       ok = tc::mbar_wait(tfull + s, (t >> 1) & 1, TC_WAIT);
       ok = __all_sync(0xffffffffu, ok);
       if (!ok) break;
       tc::fence_after_sync();
-      float gx = 0.f, gy = 0.f, gz = 0.f;
-#pragma unroll 1
-      for (int c = 0; c < TC_N / 16; c++) {
-        float v[16];
-        tc::tmem_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)(s * TC_N + 16 * c), v);
+      uint32_t v[4][16];
+      const uint32_t ta = tbase + ((uint32_t)(32 * qd) << 16) + (uint32_t)(s * TC_N + 64 * hf);
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-          const int r = t * TC_ROWS + 4 * c + q;
-          if (r < a.nrows) {
-            const TcRow kr = rk[r];
-            const float2 X = XY[kr.ox + m], Y = XY[kr.oy + m];
-            const float Ax = X.x * Y.x - X.y * Y.y, Ay = X.x * Y.y + X.y * Y.x;
-            const float g = Ax * v[4 * q + 1] + Ay * v[4 * q];
-            gx = fmaf(kr.kx, g, gx);
-            gy = fmaf(kr.ky, g, gy);
-            gz += Ax * v[4 * q + 3] + Ay * v[4 * q + 2];
-          }
+      for (int c = 0; c < 4; c++) tc::tmem_ld16_async(ta + 16 * c, v[c]);
+      tc::tmem_wait(v[0]);
+      tc::tmem_regs_after_wait(v[1]);
+      tc::tmem_regs_after_wait(v[2]);
+      tc::tmem_regs_after_wait(v[3]);
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(tfree + s);   // the buffer may take tile t+2
+      float gx = 0.f, gy = 0.f, gz = 0.f;
+#pragma unroll
+      for (int i = 0; i < 16; i++) {
+        const int r = t * TC_ROWS + 16 * hf + i;
+        if (r < a.nrows) {
+          const uint32_t* w = &v[i >> 2][4 * (i & 3)];
+          const float hx = __uint_as_float(w[0]), hy = __uint_as_float(w[1]),
+                      zx = __uint_as_float(w[2]), zy = __uint_as_float(w[3]);
+          const TcRow kr = rk[r];
+          const float2 X = XY[kr.ox + m], Y = XY[kr.oy + m];
+          const float Ax = X.x * Y.x - X.y * Y.y, Ay = X.x * Y.y + X.y * Y.x;
+          const float g = Ax * hy + Ay * hx;
+          gx = fmaf(kr.kx, g, gx);
+          gy = fmaf(kr.ky, g, gy);
+          gz += Ax * zy + Ay * zx;
         }
       }
       Fx.add(gx);
       Fy.add(gy);
       Fz.add(gz);
-      tc::fence_before_sync();
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(tfree + s);
     }
     if (!ok && lane == 0) atomicOr(a.status, 16);
+    // the two warps of a lane quarter: the second hands its sums to the first
+    // through the first V stage (the last products read it long before the
+    // epilogue drained their TMEM buffer)
+    float* part = reinterpret_cast<float*>(Bs);
+    tc::named_sync(1, 32 * TC_EPI_WARPS);
+    if (hf == 1) {
+      part[6 * m + 0] = Fx.s;
+      part[6 * m + 1] = Fx.c;
+      part[6 * m + 2] = Fy.s;
+      part[6 * m + 3] = Fy.c;
+      part[6 * m + 4] = Fz.s;
+      part[6 * m + 5] = Fz.c;
+    }
+    tc::named_sync(1, 32 * TC_EPI_WARPS);
     const int j = mt * TC_M + m;
-    if (ok && j < a.nq) {
+    if (hf == 0 && ok && j < a.nq) {
+      const double sx = Fx.value() + ((double)part[6 * m] + (double)part[6 * m + 1]);
+      const double sy = Fy.value() + ((double)part[6 * m + 2] + (double)part[6 * m + 3]);
+      const double sz = Fz.value() + ((double)part[6 * m + 4] + (double)part[6 * m + 5]);
       const int site = a.qsite[j];
       double* fo = a.f + 3 * (long)site + (a.qdrude && a.qdrude[j] ? 3 * (long)a.ns : 0);
-      fo[0] += __dmul_rn(Fx.value(), 1.0 / a.Lx);
-      fo[1] += __dmul_rn(Fy.value(), 1.0 / a.Ly);
-      fo[2] += __dmul_rn(Fz.value(), 1.0 / a.Lz);
+      fo[0] += __dmul_rn(sx, 1.0 / a.Lx);
+      fo[1] += __dmul_rn(sy, 1.0 / a.Ly);
+      fo[2] += __dmul_rn(sz, 1.0 / a.Lz);
     }
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if (warp == 4) tc::tmem_dealloc(tbase, 2 * TC_N);
-}
-
-bool kf_tc_fits(const KArgs& a, int nrows) {
-  const int KP = ((2 * a.Kz + 1) + 7) / 8 * 8;
-  return kf_tc_smem(KP, (a.Kx + 1) + (2 * a.Ky + 1), nrows) <= 227 * 1024;
+  if (warp == PW) tc::tmem_dealloc(tbase, 2 * TC_N);
 }
 
 int kf_tc_kp(const KArgs& a) { return ((2 * a.Kz + 1) + 7) / 8 * 8; }
 
+bool kf_tc_fits(const KArgs& a, int nrows) {
+  return kf_tc_smem(kf_tc_kp(a), (a.Kx + 1) + (2 * a.Ky + 1), nrows) <= 227 * 1024;
+}
+
+size_t kf_tc_za_floats(const KArgs& a) {
+  const int ntm = (a.nq + TC_M - 1) / TC_M;
+  return (size_t)ntm * 2 * TC_M * (kf_tc_kp(a) + (a.Kx + 1) + (2 * a.Ky + 1));
+}
+
+size_t kf_tc_vb_floats(const KArgs& a, int nrows) {
+  const int ntn = (4 * nrows + TC_N - 1) / TC_N;
+  return (size_t)ntn * 2 * TC_N * kf_tc_kp(a);
+}
+
+void kf_tc_rows(const KArgs& a, const std::vector<KRow>& krows, std::vector<TcRow>* out) {
+  const int oyl = a.Kx + 1 + a.Ky;
+  out->clear();
+  for (const KRow& r : krows)
+    out->push_back(TcRow{(float)r.kx, (float)r.ky, r.kx * TC_M, (oyl + r.ky) * TC_M});
+}
+
 cudaError_t k_kf_tc_za(const Launch& L, const KArgs& a, const float2* tab, float* za) {
   const int KP = kf_tc_kp(a), ntm = (a.nq + TC_M - 1) / TC_M;
-  const long n = (long)ntm * TC_M * KP;
-  kf_tc_za_kernel<<<(int)((n + 255) / 256), 256, 0, L.s>>>(a.nq, ntm, a.row,
-                                                          a.Kx + 2 * a.Ky + 2, a.Kz, KP, tab, za);
+  const int nxy = (a.Kx + 1) + (2 * a.Ky + 1);
+  const long n = (long)ntm * TC_M * (KP + nxy);
+  kf_tc_prep_kernel<<<(int)((n + 255) / 256), 256, 0, L.s>>>(a.nq, ntm, a.row,
+                                                            a.Kx + 2 * a.Ky + 2, a.Kz, KP, nxy,
+                                                            tab, za);
   ++*L.counter;
   return cudaGetLastError();
 }
 
-cudaError_t k_kf_tc(const Launch& L, const KArgs& a, int nrows, const float2* tab,
+cudaError_t k_kf_tc(const Launch& L, const KArgs& a, int nrows, const TcRow* rows,
                     const float* za, float* vb) {
   const int KP = kf_tc_kp(a), ntm = (a.nq + TC_M - 1) / TC_M;
   const int ntn = (4 * nrows + TC_N - 1) / TC_N;
@@ -284,12 +331,9 @@ cudaError_t k_kf_tc(const Launch& L, const KArgs& a, int nrows, const float2* ta
   k.ntn = ntn;
   k.nrows = nrows;
   k.nxy = (a.Kx + 1) + (2 * a.Ky + 1);
-  k.oyl = a.Kx + 1 + a.Ky;
-  k.row = a.row;
   k.za = za;
   k.vb = vb;
-  k.tab = tab;
-  k.krows = a.krows;
+  k.rows = rows;
   k.qsite = a.qsite;
   k.qdrude = a.qdrude;
   k.Lx = a.Lx;
@@ -300,7 +344,7 @@ cudaError_t k_kf_tc(const Launch& L, const KArgs& a, int nrows, const float2* ta
   const size_t smem = kf_tc_smem(KP, k.nxy, nrows);
   e = cudaFuncSetAttribute(kf_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  kf_tc_kernel<<<ntm, 160, smem, L.s>>>(k);
+  kf_tc_kernel<<<ntm, TC_THREADS, smem, L.s>>>(k);
   ++*L.counter;
   return cudaGetLastError();
 }

@@ -140,6 +140,35 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// the same without waiting: several loads in flight, then tmem_wait()
+__device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+#define MG_R16(r)                                                                           \
+  "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]),       \
+      "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), \
+      "+r"(r[14]), "+r"(r[15])
+// wait for this thread's TMEM loads; r (16 registers of one load) counts as
+// written here, so no use of it is scheduled before the wait
+__device__ __forceinline__ void tmem_wait(uint32_t* r) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" : MG_R16(r)::"memory");
+}
+// the same ordering for the registers of a further load after tmem_wait()
+__device__ __forceinline__ void tmem_regs_after_wait(uint32_t* r) {
+  asm volatile("" : MG_R16(r));
+}
+
+// named barrier for a subset of the CTA's warps
+__device__ __forceinline__ void named_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
 // x rounded to TF32 (round to nearest, ties away) and the exact FP32 rest:
 // x = hi + lo, for the three-product split hi*hi + hi*lo + lo*hi
 __device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
