@@ -71,6 +71,10 @@ struct mg_ctx {
   bool kspace_tc = false;
   float *d_za = nullptr, *d_vb = nullptr;
   TcRow* d_tcrows = nullptr;
+  // pass 1 on the tensor cores
+  bool sk_tc = false;
+  float* d_zb = nullptr;
+  int sk_nch = 1, sk_gpc = 1;
   // SHAKE
   int* d_mol_first = nullptr;
   int* d_mol_cfirst = nullptr;
@@ -589,16 +593,18 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   CK(upload(&ctx->d_kvec, kvec.data(), kvec.size()));
   CK(upload(&ctx->d_krows, krows.data(), krows.size()));
   ctx->nkrows = (int)krows.size();
-  if (p->kspace_engine < 0 || p->kspace_engine > 2)
-    return fail(ctx, MG_ERR_ARG, "kspace_engine: 0 auto, 1 FP32 cores, 2 tensor cores");
+  if (p->kspace_engine < 0 || p->kspace_engine > 3)
+    return fail(ctx, MG_ERR_ARG,
+                "kspace_engine: 0 auto, 1 FP32 cores, 2 tensor-core pass 2, 3 tensor cores");
   if (ctx->precision == MG_MIXED && p->kspace_engine != 1) {
     KArgs kd;
     kd.Kx = ctx->Kx;
     kd.Ky = ctx->Ky;
     kd.Kz = ctx->Kz;
     kd.nq = ctx->nq;
+    kd.row = ctx->row;
     const bool fits = kf_tc_fits(kd, ctx->nkrows);
-    if (!fits && p->kspace_engine == 2)
+    if (!fits && p->kspace_engine >= 2)
       return fail(ctx, MG_ERR_SIZE, "the k set is too large for the tensor-core tiles");
     ctx->kspace_tc = fits && ctx->nq > 0;
     if (ctx->kspace_tc) {
@@ -607,6 +613,18 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
       std::vector<TcRow> tr;
       kf_tc_rows(kd, krows, &tr);
       CK(upload(&ctx->d_tcrows, tr.data(), tr.size()));
+      ctx->sk_tc = p->kspace_engine == 3;
+      if (ctx->sk_tc && !sk_tc_fits(kd))
+        return fail(ctx, MG_ERR_SIZE, "the k set is too large for the tensor-core pass 1");
+      if (ctx->sk_tc) {
+        const size_t nzb = sk_tc_zb_floats(kd);
+        CK(dalloc(&ctx->d_zb, nzb));
+        CK(cudaMemset(ctx->d_zb, 0, nzb * sizeof(float)));
+        int dev = 0, nsm = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        sk_tc_split(kd, ctx->nkrows, nsm, &ctx->sk_nch, &ctx->sk_gpc);
+      }
     }
   }
   CK(upload(&ctx->d_tiles, tiles.data(), tiles.size()));
@@ -624,10 +642,15 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
     }
     CK(upload(&ctx->d_erd, erd.data(), ntab));
     CK(upload(&ctx->d_eru, eru.data(), ntab));
-    CK(dalloc((float2**)&ctx->d_tab, (size_t)ctx->nq * ctx->row));
+    {
+      // phase rows zero-padded to whole groups of 32 charges (tensor-core pass 1)
+      const size_t ntab = (size_t)((ctx->nq + 31) / 32 * 32) * ctx->row;
+      CK(dalloc((float2**)&ctx->d_tab, ntab));
+      CK(cudaMemset(ctx->d_tab, 0, ntab * sizeof(float2)));
+    }
     CK(dalloc(&ctx->d_qfix, std::max(1, ctx->nq)));
     CK(dalloc(&ctx->d_fk, 3 * (size_t)ns * (ctx->polar ? 2 : 1)));
-    CK(dalloc((float2**)&ctx->d_part, (size_t)ctx->nchunk * nk));
+    CK(dalloc((float2**)&ctx->d_part, (size_t)std::max(ctx->nchunk, ctx->sk_nch) * nk));
     CK(dalloc(&ctx->d_Wf, nk));
   } else {
     CK(dalloc(&ctx->d_pd, ns));
@@ -776,11 +799,31 @@ int build_lists(mg_ctx* ctx, const double* r_dev) {
   return fail(ctx, MG_ERR_SIZE, "neighbour list capacity");
 }
 
+// Ewald pass 1 of the FP32 path (structure factor partials, then their FP64
+// sum): tensor cores or FP32 cores; the tensor-core operand tiles of both
+// passes are built here from the phase rows
+cudaError_t sk_mixed(mg_ctx* ctx, const Launch& L, const KArgs& a, bool measure) {
+  const float2* tab = (const float2*)ctx->d_tab;
+  float2* part = (float2*)ctx->d_part;
+  if (ctx->kspace_tc) {
+    cudaError_t e = k_kf_tc_za(L, a, tab, ctx->d_za, ctx->sk_tc ? ctx->d_zb : nullptr);
+    if (e != cudaSuccess) return e;
+  }
+  if (!ctx->sk_tc) {
+    cudaError_t e = k_sk_gemm_mixed(L, a, tab, part);
+    if (e != cudaSuccess) return e;
+    return k_sk_reduce_mixed(L, a, part, measure);
+  }
+  cudaError_t e = k_sk_tc(L, a, ctx->nkrows, ctx->sk_nch, ctx->sk_gpc, tab, ctx->d_zb, part);
+  if (e != cudaSuccess) return e;
+  KArgs b = a;
+  b.nchunk = ctx->sk_nch;
+  return k_sk_reduce_mixed(L, b, part, measure);
+}
+
 // Ewald pass 2 of the FP32 path: tensor cores or FP32 cores
 cudaError_t kf_mixed(mg_ctx* ctx, const Launch& L, const KArgs& a) {
   if (!ctx->kspace_tc) return k_kf_gemm_mixed(L, a, (const float2*)ctx->d_tab);
-  cudaError_t e = k_kf_tc_za(L, a, (const float2*)ctx->d_tab, ctx->d_za);
-  if (e != cudaSuccess) return e;
   return k_kf_tc(L, a, ctx->nkrows, ctx->d_tcrows, ctx->d_za, ctx->d_vb);
 }
 
@@ -897,8 +940,7 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
       CK(cudaStreamWaitEvent(ks, ctx->ev_fork, 0));
       CK(cudaMemsetAsync(ctx->d_fk, 0, nf * sizeof(double), ks));
       PROFS("phase_tables", ks, k_phase_tables_mixed(LK, kk, r_dev, (float2*)ctx->d_tab, ctx->d_qfix));
-      PROFS("ewald_sk", ks, k_sk_gemm_mixed(LK, kk, (const float2*)ctx->d_tab, (float2*)ctx->d_part));
-      PROFS("ewald_sk_reduce", ks, k_sk_reduce_mixed(LK, kk, (const float2*)ctx->d_part, measure));
+      PROFS("ewald_sk", ks, sk_mixed(ctx, LK, kk, measure));
       PROFS("ewald_kforce", ks, kf_mixed(ctx, LK, kk));
       CK(cudaEventRecord(ctx->ev_join, ks));
     }
@@ -928,8 +970,7 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
       PROF("ewald_kforce", k_add_forces(L, nf, ctx->d_fk, f_dev));
     } else if (ctx->nq > 0) {
       PROF("phase_tables", k_phase_tables_mixed(L, ka, r_dev, (float2*)ctx->d_tab, ctx->d_qfix));
-      PROF("ewald_sk", k_sk_gemm_mixed(L, ka, (const float2*)ctx->d_tab, (float2*)ctx->d_part));
-      PROF("ewald_sk_reduce", k_sk_reduce_mixed(L, ka, (const float2*)ctx->d_part, measure));
+      PROF("ewald_sk", sk_mixed(ctx, L, ka, measure));
       PROF("ewald_kforce", kf_mixed(ctx, L, ka));
     }
   } else {
@@ -1152,7 +1193,7 @@ int mg_destroy(mg_ctx* ctx) {
                   ctx->d_adLq, ctx->d_ags, ctx->d_atpart, ctx->d_aT, ctx->d_fk,
                   ctx->d_chi, ctx->d_zth, ctx->d_step, ctx->d_dep_site, ctx->d_dep_first,
                   ctx->d_dep_parent, ctx->d_dep_w, ctx->d_plb, ctx->d_xfirst, ctx->d_xpair,
-                  ctx->d_xq, ctx->d_za, ctx->d_vb, ctx->d_tcrows};
+                  ctx->d_xq, ctx->d_za, ctx->d_vb, ctx->d_tcrows, ctx->d_zb};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ctx->h_sums) cudaFreeHost(ctx->h_sums);
@@ -1264,8 +1305,7 @@ int mg_ewald(mg_ctx* ctx, const double* r, double* f, double* energy) {
   if (ctx->nq > 0) {
     if (ctx->precision == MG_MIXED) {
       CK(k_phase_tables_mixed(L, ka, ctx->d_rs, (float2*)ctx->d_tab, ctx->d_qfix));
-      CK(k_sk_gemm_mixed(L, ka, (const float2*)ctx->d_tab, (float2*)ctx->d_part));
-      CK(k_sk_reduce_mixed(L, ka, (const float2*)ctx->d_part, true));
+      CK(sk_mixed(ctx, L, ka, true));
       CK(kf_mixed(ctx, L, ka));
     } else {
       CK(k_phase_tables_fp64(L, ka, ctx->d_rs, (double2*)ctx->d_tab));

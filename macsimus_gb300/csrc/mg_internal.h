@@ -175,7 +175,16 @@ bool kf_tc_fits(const KArgs& a, int nrows);
 size_t kf_tc_za_floats(const KArgs& a);
 size_t kf_tc_vb_floats(const KArgs& a, int nrows);
 void kf_tc_rows(const KArgs& a, const std::vector<KRow>& krows, std::vector<TcRow>* out);
-cudaError_t k_kf_tc_za(const Launch& L, const KArgs& a, const float2* tab, float* za);
+// the operand tiles of both passes from the phase rows (zb may be NULL)
+cudaError_t k_kf_tc_za(const Launch& L, const KArgs& a, const float2* tab, float* za, float* zb);
+// pass 1 on the tensor cores: KN = 2 Kz + 1 rounded up to 16 (at most 64);
+// the phase rows must be zero-padded to whole groups of 32 charges
+int sk_tc_kn(const KArgs& a);
+bool sk_tc_fits(const KArgs& a);
+size_t sk_tc_zb_floats(const KArgs& a);
+void sk_tc_split(const KArgs& a, int nrows, int nsm, int* nch, int* gpc);
+cudaError_t k_sk_tc(const Launch& L, const KArgs& a, int nrows, int nch, int gpc,
+                    const float2* tab, const float* zb, float2* part);
 cudaError_t k_kf_tc(const Launch& L, const KArgs& a, int nrows, const TcRow* rows,
                     const float* za, float* vb);
 

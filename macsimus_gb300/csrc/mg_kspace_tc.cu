@@ -26,6 +26,8 @@
 #include "mg_internal.h"
 #include "mg_tc.cuh"
 
+#include <algorithm>
+
 namespace mg {
 
 constexpr int TC_M = 128;             // charges per tile
@@ -34,12 +36,17 @@ constexpr int TC_ROWS = TC_N / 4;     // k rows per tile
 constexpr long TC_WAIT = 1L << 24;    // polls before a wait gives up
 constexpr int TC_EPI_WARPS = 8;       // two per TMEM lane quarter
 constexpr int TC_THREADS = 32 * (TC_EPI_WARPS + 1);
+constexpr int SK_G = 32;              // pass 1: charges per pipeline stage
+constexpr int SK_PW = 8;              // pass 1: producer warps
+constexpr int SK_THREADS = 32 * (SK_PW + 1);
+constexpr int SK_R = 64;              // pass 1: k rows per tile (re and im: 128 lanes)
 
 // A tiles, one per 128 charges: z_j (hi, then lo, K-major layout), then the
 // charges' phase values X(0..Kx) | Y(-Ky..Ky) transposed ([e][128] float2)
 // for the epilogue; tile stride 256 (KP + nxy) floats
 __global__ void kf_tc_prep_kernel(int nq, int ntm, int row, int oz, int Kz, int KP, int nxy,
-                                  const float2* __restrict__ tab, float* __restrict__ za) {
+                                  int KN, const float2* __restrict__ tab, float* __restrict__ za,
+                                  float* __restrict__ zb) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long nz = (long)ntm * TC_M * KP;
   const size_t tile_f = (size_t)2 * TC_M * (KP + nxy);
@@ -57,6 +64,13 @@ __global__ void kf_tc_prep_kernel(int nq, int ntm, int row, int oz, int Kz, int 
     const uint32_t o = tc::kmajor_offset(j % TC_M, kk, KP) >> 2;
     base[o] = hi;
     base[(size_t)TC_M * KP + o] = lo;
+    if (zb) {
+      // pass 1: Z^T per 32 charges, rows kk (KN of them), K = the charges
+      float* zt = zb + (size_t)(j / SK_G) * 2 * SK_G * KN;
+      const uint32_t oz2 = tc::kmajor_offset(kk, j % SK_G, SK_G) >> 2;
+      zt[oz2] = hi;
+      zt[(size_t)SK_G * KN + oz2] = lo;
+    }
     return;
   }
   const long u = t - nz;
@@ -279,6 +293,263 @@ __global__ void __launch_bounds__(TC_THREADS, 1) kf_tc_kernel(KfTc a) {
   if (warp == PW) tc::tmem_dealloc(tbase, 2 * TC_N);
 }
 
+// ------------------------------------------------------------- pass 1 --
+//
+// S(row, +-kz) = sum_j a_j(row) Z_kz(j) with a_j(row) = q_j X_j(kx) Y_j(ky):
+// for 64 rows at a time, D[128 x KN] = A[128 x 32] Z^T[KN x 32]^T summed
+// over groups of 32 charges, A's lanes 2r and 2r+1 holding Re and Im of
+// a_j(row r) and Z^T's rows [c(0..Kz), s(1..Kz)].  Per row
+//   P = (sum Re a c, sum Re a s),  Q = (sum Im a s, sum Im a c),
+//   S(+kz) = (P.x - Q.x, P.y + Q.y),  S(-kz) = (P.x + Q.x, Q.y - P.y),
+// the +-kz symmetry of the FP32-core kernel.  A is formed in shared memory
+// by eight warps from the charges' phase rows (bulk-copied per group with the
+// Z^T tile), split hi + lo like the operands of pass 2, and multiplied in
+// TF32 as three products.  CTA (row tile, charge chunk); the chunk's partial
+// S go to part[chunk][k], summed in FP64 by the reduce kernel.
+
+struct SkTc {
+  int KP, KN, Kz, nrows, nrt, ngroups, gpc, row, oyl, nk;
+  const float2* tab;   // phase rows, zero-padded to whole groups of 32 charges
+  const float* zb;     // Z^T tiles
+  const KRow* krows;
+  float2* part;
+  int* status;
+};
+
+__host__ __device__ size_t sk_tc_stage(int KN, int row) {
+  const size_t b = (size_t)2 * 128 * SK_G * 4 + (size_t)256 * KN + (size_t)256 * row;
+  return (b + 1023) / 1024 * 1024;
+}
+size_t sk_tc_smem(int KN, int row) {
+  return 2 * sk_tc_stage(KN, row) + SK_R * sizeof(KRow) + 128;
+}
+
+__global__ void __launch_bounds__(SK_THREADS, 1) sk_tc_kernel(SkTc a) {
+  extern __shared__ __align__(1024) unsigned char smem_sk[];
+  const size_t stb = sk_tc_stage(a.KN, a.row);
+  const uint32_t abytes = 2 * 128 * SK_G * 4;             // A tile, hi | lo
+  const uint32_t zbytes = 256u * a.KN, tbytes = 256u * a.row;
+  KRow* rows = reinterpret_cast<KRow*>(smem_sk + 2 * stb);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(rows + SK_R);
+  uint64_t* load = bars;        // [2] Z^T + phase rows of a group loaded
+  uint64_t* afull = bars + 2;   // [2] A tile written
+  uint64_t* freeb = bars + 4;   // [2] stage consumed by the products
+  uint64_t* tfull = bars + 6;   // [2] a group's sums in TMEM buffer b
+  uint64_t* tfree = bars + 8;   // [2] TMEM buffer b drained
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 10);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int rt = blockIdx.x % a.nrt, ch = blockIdx.x / a.nrt;
+  const int g0 = ch * a.gpc, ng = min(a.gpc, a.ngroups - g0), r0 = rt * SK_R;
+  auto stage = [&](int s) { return smem_sk + (size_t)s * stb; };
+
+  if (tid < SK_R)
+    rows[tid] = r0 + tid < a.nrows ? a.krows[r0 + tid] : KRow{0, 0, 1, 0, 0, {0, 0, 0}};
+  if (tid == 0) {
+    for (int s = 0; s < 2; s++) {
+      tc::mbar_init(load + s, 1);
+      tc::mbar_init(afull + s, SK_PW);
+      tc::mbar_init(freeb + s, 1);
+      tc::mbar_init(tfull + s, 1);
+      tc::mbar_init(tfree + s, SK_PW);
+    }
+  }
+  if (warp == SK_PW) tc::tmem_alloc(tslot, 128);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tbase = *tslot;
+
+  if (warp == SK_PW) {
+    if (lane == 0) {
+      auto issue_load = [&](int i) {
+        const int s = i & 1, g = g0 + i;
+        unsigned char* st = stage(s);
+        tc::mbar_expect_tx(load + s, zbytes + tbytes);
+        tc::bulk_g2s(st + abytes, a.zb + (size_t)g * 2 * SK_G * a.KN, zbytes, load + s);
+        tc::bulk_g2s(st + abytes + zbytes, a.tab + (size_t)g * SK_G * a.row, tbytes, load + s);
+      };
+      for (int i = 0; i < 2 && i < ng; i++) issue_load(i);
+      const uint32_t idesc = tc::idesc_tf32(128, a.KN);
+      bool ok = true;
+      for (int i = 0; i < ng; i++) {
+        const int s = i & 1;
+        ok = tc::mbar_wait(afull + s, (i >> 1) & 1, TC_WAIT);
+        if (ok && i >= 2) ok = tc::mbar_wait(tfree + s, ((i - 2) >> 1) & 1, TC_WAIT);
+        if (!ok) break;
+        tc::fence_after_sync();
+        const uint32_t d = tbase + 64u * s;
+        const uint32_t a_hi = tc::smem_u32(stage(s)), a_lo = a_hi + abytes / 2;
+        const uint32_t b_hi = a_hi + abytes, b_lo = b_hi + zbytes / 2;
+#pragma unroll
+        for (int ks = 0; ks < SK_G / 8; ks++) {
+          const uint32_t o = 256u * ks;
+          // every group starts a fresh accumulator: the tensor core's FP32
+          // sums round toward zero, long sums would drift
+          tc::mma_tf32(d, tc::smem_desc(a_hi + o, 128, 1024), tc::smem_desc(b_hi + o, 128, 1024),
+                       idesc, ks > 0 ? 1u : 0u);
+          tc::mma_tf32(d, tc::smem_desc(a_hi + o, 128, 1024), tc::smem_desc(b_lo + o, 128, 1024),
+                       idesc, 1u);
+          tc::mma_tf32(d, tc::smem_desc(a_lo + o, 128, 1024), tc::smem_desc(b_hi + o, 128, 1024),
+                       idesc, 1u);
+        }
+        tc::mma_commit(freeb + s);
+        tc::mma_commit(tfull + s);
+        if (i >= 1 && i + 1 < ng) {
+          const int s1 = (i + 1) & 1;
+          ok = tc::mbar_wait(freeb + s1, ((i - 1) >> 1) & 1, TC_WAIT);
+          if (!ok) break;
+          issue_load(i + 1);
+        }
+      }
+      if (!ok) atomicOr(a.status, 16);
+    }
+    __syncwarp();
+  } else {
+    // producers: thread = (row r, 8 charges of the group); the same warps
+    // drain the group sums from TMEM one group behind: warp w reads lanes
+    // 32 (w % 4) .., columns hc = KN/2 from (w / 4) hc
+    const int r = tid & (SK_R - 1), c0 = (tid >> 6) * 8;
+    const KRow rw = rows[r];
+    const bool valid = r0 + r < a.nrows;
+    const int ox = rw.kx, oy = a.oyl + rw.ky;
+    const uint32_t oR = tc::kmajor_offset(2 * r, 0, SK_G), oI = tc::kmajor_offset(2 * r + 1, 0, SK_G);
+    const int qd = warp & 3, hf = warp >> 2, hc = a.KN / 2;
+    CSum acc[32];
+    bool ok = true;
+    auto drain = [&](int i) {
+      const int b = i & 1;
+      bool w = tc::mbar_wait(tfull + b, (i >> 1) & 1, TC_WAIT);
+      w = __all_sync(0xffffffffu, w);
+      if (!w) return false;
+      tc::fence_after_sync();
+      uint32_t v[4][8];
+      const uint32_t ta = tbase + ((uint32_t)(32 * qd) << 16) + 64u * b + (uint32_t)(hf * hc);
+#pragma unroll
+      for (int c = 0; c < 4; c++)
+        if (8 * c < hc) tc::tmem_ld8_async(ta + 8 * c, v[c]);
+      tc::tmem_wait8(v[0]);
+      tc::tmem_regs_after_wait8(v[1]);
+      tc::tmem_regs_after_wait8(v[2]);
+      tc::tmem_regs_after_wait8(v[3]);
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(tfree + b);
+#pragma unroll
+      for (int c = 0; c < 32; c++)
+        if (c < hc) acc[c].add(__uint_as_float(v[c >> 3][c & 7]));
+      return true;
+    };
+    for (int i = 0; ok && i < ng; i++) {
+      const int s = i & 1;
+      ok = tc::mbar_wait(load + s, (i >> 1) & 1, TC_WAIT);
+      if (ok && i >= 2) ok = tc::mbar_wait(freeb + s, ((i - 2) >> 1) & 1, TC_WAIT);
+      ok = __all_sync(0xffffffffu, ok);
+      if (!ok) break;
+      unsigned char* st = stage(s);
+      const float2* tb = reinterpret_cast<const float2*>(st + abytes + zbytes);
+#pragma unroll
+      for (int c = 0; c < 8; c++) {
+        const int jj = c0 + c;
+        float re = 0.f, im = 0.f;
+        if (valid) {
+          const float2 X = tb[jj * a.row + ox], Y = tb[jj * a.row + oy];
+          re = X.x * Y.x - X.y * Y.y;
+          im = X.x * Y.y + X.y * Y.x;
+        }
+        float rh, rl, ih, il;
+        tc::tf32_split(re, rh, rl);
+        tc::tf32_split(im, ih, il);
+        // column jj of the K-major tile: chunk jj/4, element jj%4
+        const uint32_t ko = ((uint32_t)(jj >> 2) << 7) + ((uint32_t)(jj & 3) << 2);
+        *reinterpret_cast<float*>(st + oR + ko) = rh;
+        *reinterpret_cast<float*>(st + abytes / 2 + oR + ko) = rl;
+        *reinterpret_cast<float*>(st + oI + ko) = ih;
+        *reinterpret_cast<float*>(st + abytes / 2 + oI + ko) = il;
+      }
+      tc::fence_async_smem();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(afull + s);
+      if (i >= 1) ok = drain(i - 1);
+    }
+    if (ok && ng > 0) ok = drain(ng - 1);
+    if (!ok && lane == 0) atomicOr(a.status, 16);
+    // the row sums, in FP64, through the first stage (no product or copy is
+    // pending any more): D row m = 2r + (Re | Im)
+    double* Dsm = reinterpret_cast<double*>(stage(0));
+    const int m = 32 * qd + lane;
+    tc::named_sync(1, 32 * SK_PW);
+#pragma unroll
+    for (int c = 0; c < 32; c++)
+      if (c < hc) Dsm[m * 64 + hf * hc + c] = acc[c].value();
+    tc::named_sync(1, 32 * SK_PW);
+    if (warp < 4 && ok && !(m & 1) && ng > 0) {
+      const int rl = m >> 1;
+      const KRow w = rows[rl];
+      const double* re = Dsm + m * 64;
+      const double* im = Dsm + (m + 1) * 64;
+      float2* out = a.part + (size_t)ch * a.nk;
+      for (int kz = 0; kz <= a.Kz; kz++) {
+        const double Px = re[kz], Qy = im[kz];
+        const double Py = kz ? re[a.Kz + kz] : 0.0, Qx = kz ? im[a.Kz + kz] : 0.0;
+        if (kz >= w.kzlo && kz <= w.kzhi)
+          out[w.kstart + kz - w.kzlo] = make_float2((float)(Px - Qx), (float)(Py + Qy));
+        if (kz > 0 && -kz >= w.kzlo && -kz <= w.kzhi)
+          out[w.kstart - kz - w.kzlo] = make_float2((float)(Px + Qx), (float)(Qy - Py));
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == SK_PW) tc::tmem_dealloc(tbase, 128);
+}
+
+int sk_tc_kn(const KArgs& a) { return ((2 * a.Kz + 1) + 15) / 16 * 16; }
+
+bool sk_tc_fits(const KArgs& a) {
+  return sk_tc_kn(a) <= 64 && sk_tc_smem(sk_tc_kn(a), a.row) <= 227 * 1024;
+}
+
+size_t sk_tc_zb_floats(const KArgs& a) {
+  const int ntm = (a.nq + TC_M - 1) / TC_M;
+  return (size_t)ntm * (TC_M / SK_G) * 2 * SK_G * sk_tc_kn(a);
+}
+
+// charge chunks of the grid: about one CTA per SM over all row tiles
+void sk_tc_split(const KArgs& a, int nrows, int nsm, int* nch, int* gpc) {
+  const int nrt = (nrows + SK_R - 1) / SK_R, ngroups = (a.nq + SK_G - 1) / SK_G;
+  int c = std::max(1, std::min(ngroups, nsm / nrt));
+  *gpc = (ngroups + c - 1) / c;
+  *nch = (ngroups + *gpc - 1) / *gpc;
+}
+
+cudaError_t k_sk_tc(const Launch& L, const KArgs& a, int nrows, int nch, int gpc,
+                    const float2* tab, const float* zb, float2* part) {
+  SkTc k;
+  k.KP = kf_tc_kp(a);
+  k.KN = sk_tc_kn(a);
+  k.Kz = a.Kz;
+  k.nrows = nrows;
+  k.nrt = (nrows + SK_R - 1) / SK_R;
+  k.ngroups = (a.nq + SK_G - 1) / SK_G;
+  k.gpc = gpc;
+  k.row = a.row;
+  k.oyl = a.Kx + 1 + a.Ky;
+  k.nk = a.nk;
+  k.tab = tab;
+  k.zb = zb;
+  k.krows = a.krows;
+  k.part = part;
+  k.status = a.status;
+  const size_t smem = sk_tc_smem(k.KN, a.row);
+  cudaError_t e =
+      cudaFuncSetAttribute(sk_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  sk_tc_kernel<<<k.nrt * nch, SK_THREADS, smem, L.s>>>(k);
+  ++*L.counter;
+  return cudaGetLastError();
+}
+
 int kf_tc_kp(const KArgs& a) { return ((2 * a.Kz + 1) + 7) / 8 * 8; }
 
 bool kf_tc_fits(const KArgs& a, int nrows) {
@@ -302,13 +573,13 @@ void kf_tc_rows(const KArgs& a, const std::vector<KRow>& krows, std::vector<TcRo
     out->push_back(TcRow{(float)r.kx, (float)r.ky, r.kx * TC_M, (oyl + r.ky) * TC_M});
 }
 
-cudaError_t k_kf_tc_za(const Launch& L, const KArgs& a, const float2* tab, float* za) {
+cudaError_t k_kf_tc_za(const Launch& L, const KArgs& a, const float2* tab, float* za, float* zb) {
   const int KP = kf_tc_kp(a), ntm = (a.nq + TC_M - 1) / TC_M;
   const int nxy = (a.Kx + 1) + (2 * a.Ky + 1);
   const long n = (long)ntm * TC_M * (KP + nxy);
   kf_tc_prep_kernel<<<(int)((n + 255) / 256), 256, 0, L.s>>>(a.nq, ntm, a.row,
                                                             a.Kx + 2 * a.Ky + 2, a.Kz, KP, nxy,
-                                                            tab, za);
+                                                            sk_tc_kn(a), tab, za, zb);
   ++*L.counter;
   return cudaGetLastError();
 }

@@ -164,18 +164,36 @@ __device__ __forceinline__ void tmem_regs_after_wait(uint32_t* r) {
   asm volatile("" : MG_R16(r));
 }
 
+// 8 consecutive 32-bit columns, without waiting
+__device__ __forceinline__ void tmem_ld8_async(uint32_t taddr, uint32_t* r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                 "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+}
+#define MG_R8(r)                                                                           \
+  "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), \
+      "+r"(r[7])
+__device__ __forceinline__ void tmem_wait8(uint32_t* r) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" : MG_R8(r)::"memory");
+}
+__device__ __forceinline__ void tmem_regs_after_wait8(uint32_t* r) { asm volatile("" : MG_R8(r)); }
+
 // named barrier for a subset of the CTA's warps
 __device__ __forceinline__ void named_sync(int id, int nthreads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
-// x rounded to TF32 (round to nearest, ties away) and the exact FP32 rest:
-// x = hi + lo, for the three-product split hi*hi + hi*lo + lo*hi
+// x rounded to TF32 (round to nearest, ties away) and the rest, itself
+// rounded to TF32: x = hi + lo + O(2^-22 x), for the three-product split
+// hi*hi + hi*lo + lo*hi.  Rounding lo (instead of letting the tensor core
+// drop its low bits) keeps the products unbiased.
 __device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
-  uint32_t h;
+  uint32_t h, l;
   asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
   hi = __uint_as_float(h);
-  lo = x - hi;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(x - hi));
+  lo = __uint_as_float(l);
 }
 
 }  // namespace tc
