@@ -71,6 +71,7 @@ struct mg_ctx {
   bool kspace_tc = false;
   float *d_za = nullptr, *d_vb = nullptr;
   TcRow* d_tcrows = nullptr;
+  KRow* d_tckrows = nullptr;   // the k rows in (kx, ky) order
   // pass 1 on the tensor cores
   bool sk_tc = false;
   float* d_zb = nullptr;
@@ -611,8 +612,13 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
       CK(dalloc(&ctx->d_za, kf_tc_za_floats(kd)));
       CK(dalloc(&ctx->d_vb, kf_tc_vb_floats(kd, ctx->nkrows)));
       std::vector<TcRow> tr;
-      kf_tc_rows(kd, krows, &tr);
+      std::vector<KRow> tck = krows;
+      std::sort(tck.begin(), tck.end(), [](const KRow& x, const KRow& y) {
+        return x.kx != y.kx ? x.kx < y.kx : x.ky < y.ky;
+      });
+      kf_tc_rows(kd, tck, &tr);
       CK(upload(&ctx->d_tcrows, tr.data(), tr.size()));
+      CK(upload(&ctx->d_tckrows, tck.data(), tck.size()));
       ctx->sk_tc = p->kspace_engine == 3;
       if (ctx->sk_tc && !sk_tc_fits(kd))
         return fail(ctx, MG_ERR_SIZE, "the k set is too large for the tensor-core pass 1");
@@ -824,7 +830,7 @@ cudaError_t sk_mixed(mg_ctx* ctx, const Launch& L, const KArgs& a, bool measure)
 // Ewald pass 2 of the FP32 path: tensor cores or FP32 cores
 cudaError_t kf_mixed(mg_ctx* ctx, const Launch& L, const KArgs& a) {
   if (!ctx->kspace_tc) return k_kf_gemm_mixed(L, a, (const float2*)ctx->d_tab);
-  return k_kf_tc(L, a, ctx->nkrows, ctx->d_tcrows, ctx->d_za, ctx->d_vb);
+  return k_kf_tc(L, a, ctx->nkrows, ctx->d_tckrows, ctx->d_tcrows, ctx->d_za, ctx->d_vb);
 }
 
 ExclArgs excl_args(mg_ctx* ctx, const double* r_dev, double* f) {
@@ -1193,7 +1199,7 @@ int mg_destroy(mg_ctx* ctx) {
                   ctx->d_adLq, ctx->d_ags, ctx->d_atpart, ctx->d_aT, ctx->d_fk,
                   ctx->d_chi, ctx->d_zth, ctx->d_step, ctx->d_dep_site, ctx->d_dep_first,
                   ctx->d_dep_parent, ctx->d_dep_w, ctx->d_plb, ctx->d_xfirst, ctx->d_xpair,
-                  ctx->d_xq, ctx->d_za, ctx->d_vb, ctx->d_tcrows, ctx->d_zb};
+                  ctx->d_xq, ctx->d_za, ctx->d_vb, ctx->d_tcrows, ctx->d_zb, ctx->d_tckrows};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ctx->h_sums) cudaFreeHost(ctx->h_sums);

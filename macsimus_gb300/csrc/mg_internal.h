@@ -185,8 +185,9 @@ size_t sk_tc_zb_floats(const KArgs& a);
 void sk_tc_split(const KArgs& a, int nrows, int nsm, int* nch, int* gpc);
 cudaError_t k_sk_tc(const Launch& L, const KArgs& a, int nrows, int nch, int gpc,
                     const float2* tab, const float* zb, float2* part);
-cudaError_t k_kf_tc(const Launch& L, const KArgs& a, int nrows, const TcRow* rows,
-                    const float* za, float* vb);
+// tckrows: the k rows in the order of the tensor-core tiles ((kx, ky) order)
+cudaError_t k_kf_tc(const Launch& L, const KArgs& a, int nrows, const KRow* tckrows,
+                    const TcRow* rows, const float* za, float* vb);
 
 struct ShakeArgs {
   int nmol;

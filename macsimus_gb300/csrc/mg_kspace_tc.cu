@@ -16,11 +16,12 @@
 // result carries FP32 accuracy.  The epilogue forms A from the phase rows
 // and accumulates the force.
 //
-// One CTA per 128 charges, 9 warps.  Warp 8 bulk-copies the charges' tile
+// One CTA per 128 charges, 17 warps.  Warp 16 bulk-copies the charges' tile
 // (Z and their phase rows) and streams the V tiles into shared memory (two
 // stages), and one of its threads issues the MMAs into two TMEM buffers of
-// 128 columns.  Warps 0-7 drain the other buffer meanwhile: two warps per
-// TMEM lane quarter (32 charges), each taking 16 of the tile's 32 rows.
+// 128 columns.  Warps 0-15 drain the other buffer meanwhile: four warps per
+// TMEM lane quarter (32 charges), each taking 8 of the tile's 32 rows.  The
+// rows run in (kx, ky) order, so X(kx) changes rarely along a warp's rows.
 // Every wait is bounded; a wait that gives up sets bit 16 of the status word.
 #include "mg_device.cuh"
 #include "mg_internal.h"
@@ -34,7 +35,8 @@ constexpr int TC_M = 128;             // charges per tile
 constexpr int TC_N = 128;             // D columns per tile
 constexpr int TC_ROWS = TC_N / 4;     // k rows per tile
 constexpr long TC_WAIT = 1L << 24;    // polls before a wait gives up
-constexpr int TC_EPI_WARPS = 8;       // two per TMEM lane quarter
+constexpr int TC_EPI_WARPS = 16;      // four per TMEM lane quarter
+constexpr int TC_EPI_ROWS = TC_ROWS / (TC_EPI_WARPS / 4);   // rows per warp and tile
 constexpr int TC_THREADS = 32 * (TC_EPI_WARPS + 1);
 constexpr int SK_G = 32;              // pass 1: charges per pipeline stage
 constexpr int SK_PW = 8;              // pass 1: producer warps
@@ -215,40 +217,45 @@ __global__ void __launch_bounds__(TC_THREADS, 1) kf_tc_kernel(KfTc a) {
     }
     __syncwarp();
   } else {
-    // warp w: TMEM lanes 32 (w % 4) .. (its charges), columns 64 (w / 4) ..
-    // (rows 16 (w / 4) .. 16 (w / 4) + 15 of each tile)
+    // warp w: TMEM lanes 32 (w % 4) .. (its charges), columns 32 (w / 4) ..
+    // (rows 8 (w / 4) .. 8 (w / 4) + 7 of each tile)
     const int qd = warp & 3, hf = warp >> 2;
     const int m = 32 * qd + lane;
     bool ok = tc::mbar_wait(bar_a, 0, TC_WAIT);
     ok = __all_sync(0xffffffffu, ok);
     CSum Fx, Fy, Fz;
+    int cur_ox = -1;
+    float2 X = make_float2(0.f, 0.f);
     for (int t = 0; ok && t < a.ntn; t++) {
       const int s = t & 1;
       ok = tc::mbar_wait(tfull + s, (t >> 1) & 1, TC_WAIT);
       ok = __all_sync(0xffffffffu, ok);
       if (!ok) break;
       tc::fence_after_sync();
-      uint32_t v[4][16];
-      const uint32_t ta = tbase + ((uint32_t)(32 * qd) << 16) + (uint32_t)(s * TC_N + 64 * hf);
-#pragma unroll
-      for (int c = 0; c < 4; c++) tc::tmem_ld16_async(ta + 16 * c, v[c]);
+      uint32_t v[2][16];
+      const uint32_t ta = tbase + ((uint32_t)(32 * qd) << 16) +
+                          (uint32_t)(s * TC_N + 4 * TC_EPI_ROWS * hf);
+      tc::tmem_ld16_async(ta, v[0]);
+      tc::tmem_ld16_async(ta + 16, v[1]);
       tc::tmem_wait(v[0]);
       tc::tmem_regs_after_wait(v[1]);
-      tc::tmem_regs_after_wait(v[2]);
-      tc::tmem_regs_after_wait(v[3]);
       tc::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(tfree + s);   // the buffer may take tile t+2
       float gx = 0.f, gy = 0.f, gz = 0.f;
 #pragma unroll
-      for (int i = 0; i < 16; i++) {
-        const int r = t * TC_ROWS + 16 * hf + i;
+      for (int i = 0; i < TC_EPI_ROWS; i++) {
+        const int r = t * TC_ROWS + TC_EPI_ROWS * hf + i;
         if (r < a.nrows) {
           const uint32_t* w = &v[i >> 2][4 * (i & 3)];
           const float hx = __uint_as_float(w[0]), hy = __uint_as_float(w[1]),
                       zx = __uint_as_float(w[2]), zy = __uint_as_float(w[3]);
           const TcRow kr = rk[r];
-          const float2 X = XY[kr.ox + m], Y = XY[kr.oy + m];
+          if (kr.ox != cur_ox) {
+            cur_ox = kr.ox;
+            X = XY[kr.ox + m];
+          }
+          const float2 Y = XY[kr.oy + m];
           const float Ax = X.x * Y.x - X.y * Y.y, Ay = X.x * Y.y + X.y * Y.x;
           const float g = Ax * hy + Ay * hx;
           gx = fmaf(kr.kx, g, gx);
@@ -261,25 +268,30 @@ __global__ void __launch_bounds__(TC_THREADS, 1) kf_tc_kernel(KfTc a) {
       Fz.add(gz);
     }
     if (!ok && lane == 0) atomicOr(a.status, 16);
-    // the two warps of a lane quarter: the second hands its sums to the first
-    // through the first V stage (the last products read it long before the
-    // epilogue drained their TMEM buffer)
+    // the four warps of a lane quarter: the others hand their sums to the
+    // first through the first V stage (the last products read it long before
+    // the epilogue drained their TMEM buffer)
     float* part = reinterpret_cast<float*>(Bs);
     tc::named_sync(1, 32 * TC_EPI_WARPS);
-    if (hf == 1) {
-      part[6 * m + 0] = Fx.s;
-      part[6 * m + 1] = Fx.c;
-      part[6 * m + 2] = Fy.s;
-      part[6 * m + 3] = Fy.c;
-      part[6 * m + 4] = Fz.s;
-      part[6 * m + 5] = Fz.c;
+    if (hf > 0) {
+      float* p = part + (size_t)(hf - 1) * 6 * TC_M;
+      p[0 * TC_M + m] = Fx.s;
+      p[1 * TC_M + m] = Fx.c;
+      p[2 * TC_M + m] = Fy.s;
+      p[3 * TC_M + m] = Fy.c;
+      p[4 * TC_M + m] = Fz.s;
+      p[5 * TC_M + m] = Fz.c;
     }
     tc::named_sync(1, 32 * TC_EPI_WARPS);
     const int j = mt * TC_M + m;
     if (hf == 0 && ok && j < a.nq) {
-      const double sx = Fx.value() + ((double)part[6 * m] + (double)part[6 * m + 1]);
-      const double sy = Fy.value() + ((double)part[6 * m + 2] + (double)part[6 * m + 3]);
-      const double sz = Fz.value() + ((double)part[6 * m + 4] + (double)part[6 * m + 5]);
+      double sx = Fx.value(), sy = Fy.value(), sz = Fz.value();
+      for (int h = 0; h < TC_EPI_WARPS / 4 - 1; h++) {
+        const float* p = part + (size_t)h * 6 * TC_M;
+        sx += (double)p[0 * TC_M + m] + (double)p[1 * TC_M + m];
+        sy += (double)p[2 * TC_M + m] + (double)p[3 * TC_M + m];
+        sz += (double)p[4 * TC_M + m] + (double)p[5 * TC_M + m];
+      }
       const int site = a.qsite[j];
       double* fo = a.f + 3 * (long)site + (a.qdrude && a.qdrude[j] ? 3 * (long)a.ns : 0);
       fo[0] += __dmul_rn(sx, 1.0 / a.Lx);
@@ -584,12 +596,12 @@ cudaError_t k_kf_tc_za(const Launch& L, const KArgs& a, const float2* tab, float
   return cudaGetLastError();
 }
 
-cudaError_t k_kf_tc(const Launch& L, const KArgs& a, int nrows, const TcRow* rows,
-                    const float* za, float* vb) {
+cudaError_t k_kf_tc(const Launch& L, const KArgs& a, int nrows, const KRow* tckrows,
+                    const TcRow* rows, const float* za, float* vb) {
   const int KP = kf_tc_kp(a), ntm = (a.nq + TC_M - 1) / TC_M;
   const int ntn = (4 * nrows + TC_N - 1) / TC_N;
   const long nv = (long)ntn * TC_N * KP;
-  kf_tc_vb_kernel<<<(int)((nv + 255) / 256), 256, 0, L.s>>>(nrows, ntn, a.Kz, KP, a.krows, a.Wf,
+  kf_tc_vb_kernel<<<(int)((nv + 255) / 256), 256, 0, L.s>>>(nrows, ntn, a.Kz, KP, tckrows, a.Wf,
                                                            vb);
   ++*L.counter;
   cudaError_t e = cudaGetLastError();
