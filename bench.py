@@ -150,7 +150,8 @@ def run_ours(args, rank, world, local):
             dist.barrier()
         torch.cuda.synchronize()
 
-    kw = dict(h=w["h"], epsc=1e-7, aspc_k=w["aspc_k"], scf_iter=w["scf_iter"], skin=args.skin)
+    kw = dict(h=w["h"], epsc=1e-7, aspc_k=w["aspc_k"], scf_iter=w["scf_iter"], skin=args.skin,
+              kspace_engine=args.kspace_engine)
     # the autotuner picks the cell subdivision and the Ewald pass-1 split on
     # this configuration (untimed)
     tuned = {}
@@ -299,7 +300,12 @@ def run_ours(args, rank, world, local):
                        "l2": "flushed between timed steps (256 MB write)",
                        "autotuned": tuned or "off",
                        "pair_search": ("Verlet lists, skin %.2f A" % args.skin) if args.skin > 0
-                       else "cells re-binned every step"},
+                       else "cells re-binned every step",
+                       "ewald_kspace": {0: "both passes tensor cores (tcgen05 TF32x3)",
+                                        1: "both passes FP32 cores",
+                                        2: "pass 1 FP32 cores, pass 2 tensor cores (tcgen05 TF32x3)",
+                                        3: "both passes tensor cores (tcgen05 TF32x3)"}[
+                                            args.kspace_engine]},
             "atom_steps_per_s": round(atom_steps, 1),
             "fp64_path": {"value": round(value64, 4), "unit": "ns/day", "steps": k64},
             "mixed_over_fp64": round(value / value64, 3),
@@ -526,6 +532,9 @@ def main():
     ap.add_argument("--ref-budget", type=float, default=150.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--kspace-engine", type=int, default=0,
+                    help="Ewald engine of the FP32 path: 0 tensor cores where they fit, 1 FP32 "
+                         "cores, 2 tensor-core pass 2 only, 3 tensor cores for both passes")
     ap.add_argument("--skin", type=float, default=0.0,
                     help="> 0: Verlet lists of cutoff+skin instead of cells re-binned every step")
     ap.add_argument("--equilibrate", type=int, default=400,

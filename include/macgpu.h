@@ -134,11 +134,11 @@ typedef struct {
      no_normalize != 0 leaves the positions unwrapped. */
   double box_rmin;
   int no_normalize;
-  /* Ewald k-space engine of the FP32 path: 0 = pass 2 on the tensor cores
-     when their shared-memory tiles fit (else the FP32 cores), pass 1 on the
-     FP32 cores; 1 = both passes on the FP32 cores; 2 = pass 2 on the tensor
-     cores; 3 = both passes on the tensor cores.  The tensor-core passes run
-     TF32 split into three products with FP32 accuracy. */
+  /* Ewald k-space engine of the FP32 path: 0 = each pass on the tensor
+     cores when its shared-memory tiles fit (else on the FP32 cores); 1 =
+     both passes on the FP32 cores; 2 = pass 2 on the tensor cores, pass 1 on
+     the FP32 cores; 3 = both passes on the tensor cores.  The tensor-core
+     passes run TF32 split into three products with FP32 accuracy. */
   int kspace_engine;
 } mg_params;
 

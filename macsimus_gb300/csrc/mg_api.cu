@@ -619,9 +619,9 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
       kf_tc_rows(kd, tck, &tr);
       CK(upload(&ctx->d_tcrows, tr.data(), tr.size()));
       CK(upload(&ctx->d_tckrows, tck.data(), tck.size()));
-      ctx->sk_tc = p->kspace_engine == 3;
-      if (ctx->sk_tc && !sk_tc_fits(kd))
+      if (p->kspace_engine == 3 && !sk_tc_fits(kd))
         return fail(ctx, MG_ERR_SIZE, "the k set is too large for the tensor-core pass 1");
+      ctx->sk_tc = p->kspace_engine == 3 || (p->kspace_engine == 0 && sk_tc_fits(kd));
       if (ctx->sk_tc) {
         const size_t nzb = sk_tc_zb_floats(kd);
         CK(dalloc(&ctx->d_zb, nzb));

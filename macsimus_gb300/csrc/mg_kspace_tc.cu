@@ -42,6 +42,7 @@ constexpr int SK_G = 32;              // pass 1: charges per pipeline stage
 constexpr int SK_PW = 8;              // pass 1: producer warps
 constexpr int SK_THREADS = 32 * (SK_PW + 1);
 constexpr int SK_R = 64;              // pass 1: k rows per tile (re and im: 128 lanes)
+constexpr int SK_NS = 3;              // pass 1: pipeline stages
 
 // A tiles, one per 128 charges: z_j (hi, then lo, K-major layout), then the
 // charges' phase values X(0..Kx) | Y(-Ky..Ky) transposed ([e][128] float2)
@@ -333,7 +334,7 @@ __host__ __device__ size_t sk_tc_stage(int KN, int row) {
   return (b + 1023) / 1024 * 1024;
 }
 size_t sk_tc_smem(int KN, int row) {
-  return 2 * sk_tc_stage(KN, row) + SK_R * sizeof(KRow) + 128;
+  return SK_NS * sk_tc_stage(KN, row) + SK_R * sizeof(KRow) + 128;
 }
 
 __global__ void __launch_bounds__(SK_THREADS, 1) sk_tc_kernel(SkTc a) {
@@ -341,14 +342,14 @@ __global__ void __launch_bounds__(SK_THREADS, 1) sk_tc_kernel(SkTc a) {
   const size_t stb = sk_tc_stage(a.KN, a.row);
   const uint32_t abytes = 2 * 128 * SK_G * 4;             // A tile, hi | lo
   const uint32_t zbytes = 256u * a.KN, tbytes = 256u * a.row;
-  KRow* rows = reinterpret_cast<KRow*>(smem_sk + 2 * stb);
+  KRow* rows = reinterpret_cast<KRow*>(smem_sk + SK_NS * stb);
   uint64_t* bars = reinterpret_cast<uint64_t*>(rows + SK_R);
-  uint64_t* load = bars;        // [2] Z^T + phase rows of a group loaded
-  uint64_t* afull = bars + 2;   // [2] A tile written
-  uint64_t* freeb = bars + 4;   // [2] stage consumed by the products
-  uint64_t* tfull = bars + 6;   // [2] a group's sums in TMEM buffer b
-  uint64_t* tfree = bars + 8;   // [2] TMEM buffer b drained
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 10);
+  uint64_t* load = bars;                 // [NS] Z^T + phase rows of a group loaded
+  uint64_t* afull = bars + SK_NS;        // [NS] A tile written
+  uint64_t* freeb = bars + 2 * SK_NS;    // [NS] stage consumed by the products
+  uint64_t* tfull = bars + 3 * SK_NS;    // [2] a group's sums in TMEM buffer b
+  uint64_t* tfree = tfull + 2;           // [2] TMEM buffer b drained
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(tfree + 2);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int rt = blockIdx.x % a.nrt, ch = blockIdx.x / a.nrt;
   const int g0 = ch * a.gpc, ng = min(a.gpc, a.ngroups - g0), r0 = rt * SK_R;
@@ -357,12 +358,14 @@ __global__ void __launch_bounds__(SK_THREADS, 1) sk_tc_kernel(SkTc a) {
   if (tid < SK_R)
     rows[tid] = r0 + tid < a.nrows ? a.krows[r0 + tid] : KRow{0, 0, 1, 0, 0, {0, 0, 0}};
   if (tid == 0) {
-    for (int s = 0; s < 2; s++) {
+    for (int s = 0; s < SK_NS; s++) {
       tc::mbar_init(load + s, 1);
       tc::mbar_init(afull + s, SK_PW);
       tc::mbar_init(freeb + s, 1);
-      tc::mbar_init(tfull + s, 1);
-      tc::mbar_init(tfree + s, SK_PW);
+    }
+    for (int b = 0; b < 2; b++) {
+      tc::mbar_init(tfull + b, 1);
+      tc::mbar_init(tfree + b, SK_PW);
     }
   }
   if (warp == SK_PW) tc::tmem_alloc(tslot, 128);
@@ -374,22 +377,22 @@ __global__ void __launch_bounds__(SK_THREADS, 1) sk_tc_kernel(SkTc a) {
   if (warp == SK_PW) {
     if (lane == 0) {
       auto issue_load = [&](int i) {
-        const int s = i & 1, g = g0 + i;
+        const int s = i % SK_NS, g = g0 + i;
         unsigned char* st = stage(s);
         tc::mbar_expect_tx(load + s, zbytes + tbytes);
         tc::bulk_g2s(st + abytes, a.zb + (size_t)g * 2 * SK_G * a.KN, zbytes, load + s);
         tc::bulk_g2s(st + abytes + zbytes, a.tab + (size_t)g * SK_G * a.row, tbytes, load + s);
       };
-      for (int i = 0; i < 2 && i < ng; i++) issue_load(i);
+      for (int i = 0; i < SK_NS && i < ng; i++) issue_load(i);
       const uint32_t idesc = tc::idesc_tf32(128, a.KN);
       bool ok = true;
       for (int i = 0; i < ng; i++) {
-        const int s = i & 1;
-        ok = tc::mbar_wait(afull + s, (i >> 1) & 1, TC_WAIT);
-        if (ok && i >= 2) ok = tc::mbar_wait(tfree + s, ((i - 2) >> 1) & 1, TC_WAIT);
+        const int s = i % SK_NS, b = i & 1;
+        ok = tc::mbar_wait(afull + s, (i / SK_NS) & 1, TC_WAIT);
+        if (ok && i >= 2) ok = tc::mbar_wait(tfree + b, ((i - 2) >> 1) & 1, TC_WAIT);
         if (!ok) break;
         tc::fence_after_sync();
-        const uint32_t d = tbase + 64u * s;
+        const uint32_t d = tbase + 64u * b;
         const uint32_t a_hi = tc::smem_u32(stage(s)), a_lo = a_hi + abytes / 2;
         const uint32_t b_hi = a_hi + abytes, b_lo = b_hi + zbytes / 2;
 #pragma unroll
@@ -405,12 +408,15 @@ __global__ void __launch_bounds__(SK_THREADS, 1) sk_tc_kernel(SkTc a) {
                        idesc, 1u);
         }
         tc::mma_commit(freeb + s);
-        tc::mma_commit(tfull + s);
-        if (i >= 1 && i + 1 < ng) {
-          const int s1 = (i + 1) & 1;
-          ok = tc::mbar_wait(freeb + s1, ((i - 1) >> 1) & 1, TC_WAIT);
+        tc::mma_commit(tfull + b);
+        // refill the stage of group i-1 with group i-1+NS once its products
+        // are done (the producers saw that stage's copy complete, so they
+        // are done reading it too)
+        if (i >= 1 && i - 1 + SK_NS < ng) {
+          const int s1 = (i - 1) % SK_NS;
+          ok = tc::mbar_wait(freeb + s1, ((i - 1) / SK_NS) & 1, TC_WAIT);
           if (!ok) break;
-          issue_load(i + 1);
+          issue_load(i - 1 + SK_NS);
         }
       }
       if (!ok) atomicOr(a.status, 16);
@@ -452,9 +458,10 @@ __global__ void __launch_bounds__(SK_THREADS, 1) sk_tc_kernel(SkTc a) {
       return true;
     };
     for (int i = 0; ok && i < ng; i++) {
-      const int s = i & 1;
-      ok = tc::mbar_wait(load + s, (i >> 1) & 1, TC_WAIT);
-      if (ok && i >= 2) ok = tc::mbar_wait(freeb + s, ((i - 2) >> 1) & 1, TC_WAIT);
+      const int s = i % SK_NS;
+      // the copy into stage s was issued after the products of group i-NS
+      // (the last readers of its A tile) completed
+      ok = tc::mbar_wait(load + s, (i / SK_NS) & 1, TC_WAIT);
       ok = __all_sync(0xffffffffu, ok);
       if (!ok) break;
       unsigned char* st = stage(s);
