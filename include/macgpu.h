@@ -304,6 +304,17 @@ typedef struct {
 int mg_widom(mg_ctx *ctx, const mg_probe *probe, long long ninsert, unsigned long long seed,
              double T, mg_widom_result *out, double *U);
 
+/* Identity change, cook's XWidom (sim/simmeas.c:1961-2003, with Eidchange
+   of cook/widom.c:16-170): the r-space energy change dU (smoothed LJ and
+   the erfc spline) of giving the sites of each listed molecule the types
+   vtype[] and charges vcharge[] (program units), against the other
+   molecules in the cell list of the last force evaluation.  The listed
+   molecules share one structure (1..8 sites, the same site kinds).  out:
+   sum of exp(-dU/T), raw = sum / nlist (cook's "XWidom"), mu = -T ln raw;
+   no cutoff correction (cook applies none).  dU (optional) per molecule. */
+int mg_xwidom(mg_ctx *ctx, int nlist, const int *mols, const int *vtype, const double *vcharge,
+              double T, mg_widom_result *out, double *dU);
+
 /* ---- autotuner ----
    No reference counterpart.  Times the force evaluation of the configuration
    r for every cell subdivision (cells_per_cutoff 1..3) and Ewald pass-1

@@ -115,6 +115,8 @@ def library():
         L.mg_playback_frame.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_float)]
         _fp = C.POINTER(C.c_float)
         L.mg_tc_selftest.argtypes = [_fp, _fp, _fp, C.c_int, C.c_int]
+        L.mg_xwidom.argtypes = [vp, C.c_int, _ip, _ip, _dp, C.c_double,
+                                C.POINTER(WidomResult), _dp]
         L.mg_md_steps.argtypes = [vp, C.c_int, C.POINTER(Energy)]
         L.mg_selffield.argtypes = [vp, _dp, _dp, C.c_double, C.c_int, C.POINTER(Energy)]
         L.mg_set_stream.argtypes = [vp, vp]
@@ -388,6 +390,23 @@ class ForcePath:
         self._check(library().mg_md_get_state(self._ctx, r.ctypes.data_as(_dp),
                                               r1.ctypes.data_as(_dp)))
         return r.reshape(-1, 3), r1.reshape(-1, 3)
+
+    def xwidom(self, mols, vtype, vcharge, T, energies=False):
+        """cook's XWidom identity change of the listed molecules into sites of
+        types vtype and charges vcharge (program units) in the configuration
+        of the last force evaluation: dict(sum, raw, mu) (+ dU per molecule)"""
+        mols = np.ascontiguousarray(mols, np.int32)
+        vt = np.ascontiguousarray(vtype, np.int32)
+        vq = np.ascontiguousarray(vcharge, np.float64)
+        res = WidomResult()
+        dU = np.zeros(len(mols)) if energies else None
+        self._check(library().mg_xwidom(self._ctx, len(mols), mols.ctypes.data_as(_ip),
+                                        vt.ctypes.data_as(_ip), vq.ctypes.data_as(_dp), float(T),
+                                        C.byref(res), dU.ctypes.data_as(_dp) if energies else None))
+        out = dict(sum=res.sum, raw=res.raw, mu=res.mu)
+        if energies:
+            out["dU"] = dU
+        return out
 
     def playback_frame(self, what="plb", flags=0):
         """(L[3], float32 [ns, 3]) of the MD state as cook writes it into

@@ -30,7 +30,7 @@ struct mg_ctx {
   int Kx = 0, Ky = 0, Kz = 0, row = 0, ntask = 0, ncol = 0, nchunk = 1;
   cudaStream_t stream = nullptr;
   // host copies
-  std::vector<int> h_kind, h_mol;
+  std::vector<int> h_kind, h_mol, h_mol_first;
   // device buffers
   double *d_r = nullptr, *d_f = nullptr, *d_r1 = nullptr, *d_p = nullptr;
   double *d_rs = nullptr, *d_fs = nullptr;  // staging of the host-array calls
@@ -127,6 +127,7 @@ struct mg_ctx {
   std::vector<double> kind_q;
   std::vector<long> type_count;
   bool have_cells = false;
+  const double* last_r = nullptr;   // positions of the last force evaluation (device)
   PairF* d_wtabf = nullptr;
   PairD* d_wtabd = nullptr;
   double *d_wgeom = nullptr, *d_wpart = nullptr;
@@ -667,6 +668,7 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
     CK(dalloc(&ctx->d_Wd, nk));
   }
   CK(upload(&ctx->d_mol_first, t->mol_first, t->nmol + 1));
+  ctx->h_mol_first.assign(t->mol_first, t->mol_first + t->nmol + 1);
   {
     // every pair of sites of one molecule with a charge product is an Ewald
     // exclusion (the r-space term of a rigid molecule is not counted)
@@ -858,6 +860,7 @@ ExclArgs excl_args(mg_ctx* ctx, const double* r_dev, double* f) {
 int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) {
   Launch L = launch(ctx);
   const int ns = ctx->ns;
+  ctx->last_r = r_dev;
   // fork point of the concurrent k-space chain (FP32 path): everything
   // queued before, nothing of this evaluation's r-space work
   if (ctx->precision == MG_MIXED && ctx->overlap && ctx->nq > 0)
@@ -1637,6 +1640,124 @@ int mg_widom(mg_ctx* ctx, const mg_probe* probe, long long ninsert, unsigned lon
   CK(cudaStreamSynchronize(ctx->stream));
   if (d_U) CK(cudaFree(d_U));
   widom_result(ctx, part.data(), nblk, ninsert, T, corr, out);
+  return MG_OK;
+}
+
+int mg_xwidom(mg_ctx* ctx, int nlist, const int* mols, const int* vtype, const double* vcharge,
+              double T, mg_widom_result* out, double* dU) {
+  if (!ctx || !mols || !vtype || !vcharge || !out) return fail(ctx, MG_ERR_ARG, "null argument");
+  if (nlist < 1 || !(T > 0)) return fail(ctx, MG_ERR_ARG, "nlist >= 1 and T > 0 required");
+  if (ctx->polar) return fail(ctx, MG_ERR_ARG, "identity change in a Drude system is not supported");
+  if (!ctx->have_cells || !ctx->last_r)
+    return fail(ctx, MG_ERR_ARG, "no cell list yet: evaluate forces first");
+  if (ctx->use_list)
+    return fail(ctx, MG_ERR_ARG, "identity change needs the cell path (skin <= 0)");
+  // every listed molecule has the sites and site kinds of the first
+  const std::vector<int>& mf = ctx->h_mol_first;
+  for (int l = 0; l < nlist; l++)
+    if (mols[l] < 0 || mols[l] >= ctx->nmol) return fail(ctx, MG_ERR_ARG, "molecule out of range");
+  const int i0 = mf[mols[0]], nps = mf[mols[0] + 1] - i0;
+  if (nps < 1 || nps > MAX_WPROBE) return fail(ctx, MG_ERR_ARG, "molecules of 1..8 sites");
+  for (int l = 1; l < nlist; l++) {
+    const int j0 = mf[mols[l]];
+    if (mf[mols[l] + 1] - j0 != nps) return fail(ctx, MG_ERR_ARG, "molecules differ in sites");
+    for (int s = 0; s < nps; s++)
+      if (ctx->h_kind[j0 + s] != ctx->h_kind[i0 + s])
+        return fail(ctx, MG_ERR_ARG, "molecules differ in site kinds");
+  }
+  for (int s = 0; s < nps; s++)
+    if (vtype[s] < 0 || vtype[s] >= ctx->ntypes) return fail(ctx, MG_ERR_ARG, "type out of range");
+  // constants of the real (h = 0) and the virtual (h = 1) sites with every kind
+  std::vector<PairF> tf(2 * MAX_WPROBE * MAX_KINDS, PairF{});
+  std::vector<PairD> td(2 * MAX_WPROBE * MAX_KINDS, PairD{});
+  for (int h = 0; h < 2; h++)
+    for (int s = 0; s < nps; s++) {
+      const int k = ctx->h_kind[i0 + s];
+      const int ta = h ? vtype[s] : ctx->kind_type[k];
+      const double qs = h ? vcharge[s] : ctx->kind_q[k];
+      for (int b = 0; b < ctx->nkind; b++) {
+        const int tb = ctx->kind_type[b];
+        double eps, sig;
+        PairLJ P;
+        combining_rule(ctx->h_tE[ta], ctx->h_tR[ta], ctx->h_tA[ta], ctx->h_tE[tb], ctx->h_tR[tb],
+                       ctx->h_tA[tb], ctx->comb_rule, &eps, &sig);
+        if (smooth_lj(eps, sig, ctx->C2, &P))
+          return fail(ctx, MG_ERR_SETUP, "smooth LJ cutoff cannot be determined");
+        const double qq = qs * ctx->kind_q[b];
+        const size_t o = ((size_t)h * MAX_WPROBE + s) * MAX_KINDS + b;
+        td[o] = PairD{P.C1q, P.C2q, P.A4, P.E24, P.Sq, qq, P.A, P.E4, 0, 0, 0, 0};
+        tf[o] = PairF{(float)P.C1q, (float)P.C2q, (float)P.A4, (float)P.E24,
+                      (float)P.Sq,  (float)qq,    (float)P.A,  (float)P.E4,
+                      0.f, 0.f, 0.f, 0.f, qq, 0, 0, 0};
+      }
+    }
+  const int nblk = widom_blocks(nlist);
+  int* d_list = nullptr;
+  double *d_U = nullptr, *d_part = nullptr;
+  PairF* d_tf = nullptr;
+  PairD* d_td = nullptr;
+  auto release = [&]() {
+    cudaFree(d_list);
+    cudaFree(d_U);
+    cudaFree(d_part);
+    cudaFree(d_tf);
+    cudaFree(d_td);
+  };
+  cudaError_t e = cudaMalloc((void**)&d_list, sizeof(int) * nlist);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&d_part, sizeof(double) * nblk);
+  if (e == cudaSuccess && dU) e = cudaMalloc((void**)&d_U, sizeof(double) * nlist);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&d_tf, sizeof(PairF) * tf.size());
+  if (e == cudaSuccess) e = cudaMalloc((void**)&d_td, sizeof(PairD) * td.size());
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_list, mols, sizeof(int) * nlist, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_tf, tf.data(), sizeof(PairF) * tf.size(), cudaMemcpyHostToDevice,
+                        ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_td, td.data(), sizeof(PairD) * td.size(), cudaMemcpyHostToDevice,
+                        ctx->stream);
+  XWidomArgs a;
+  a.nlist = nlist;
+  a.nps = nps;
+  a.nkind = ctx->nkind;
+  a.ncx = ctx->ncx;
+  a.ncy = ctx->ncy;
+  a.ncz = ctx->ncz;
+  a.nstencil = ctx->nstencil;
+  a.lanes_sites = ctx->nstencil < 16 ? 1 : 0;
+  a.ntab = ctx->ntab;
+  a.list = d_list;
+  a.mol_first = ctx->d_mol_first;
+  a.r = ctx->last_r;
+  a.cell_start = ctx->d_cell_start;
+  a.stencil = ctx->d_stencil;
+  a.Lx = ctx->L[0];
+  a.Ly = ctx->L[1];
+  a.Lz = ctx->L[2];
+  a.cutoff_sq = ctx->cutoff * ctx->cutoff;
+  a.sgrid = ctx->sgrid;
+  a.T = T;
+  a.U = d_U;
+  a.part = d_part;
+  a.pj = ctx->d_pj;
+  a.pd = ctx->d_pd;
+  a.tabf = d_tf;
+  a.tabd = d_td;
+  a.eru = ctx->d_eru;
+  a.ert = ctx->d_ert;
+  Launch L = launch(ctx);
+  if (e == cudaSuccess) e = k_xwidom(L, a, ctx->precision != MG_MIXED);
+  std::vector<double> part(nblk);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(part.data(), d_part, sizeof(double) * nblk, cudaMemcpyDeviceToHost,
+                        ctx->stream);
+  if (e == cudaSuccess && dU)
+    e = cudaMemcpyAsync(dU, d_U, sizeof(double) * nlist, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  release();
+  if (e != cudaSuccess) return fail(ctx, MG_ERR_CUDA, std::string("xwidom: ") + cudaGetErrorString(e));
+  // no cutoff correction: cook's XWidom applies none
+  widom_result(ctx, part.data(), nblk, nlist, T, 0.0, out);
   return MG_OK;
 }
 

@@ -331,6 +331,27 @@ struct WidomBox {
   const double* ert;    // erfc splines (FP64)
 };
 int widom_blocks(long long n);
+// identity change of whole molecules (cook's XWidom): per listed molecule the
+// r-space energy of its sites with the real and with the virtual constants,
+// against the other molecules in the cell list of the last force evaluation
+struct XWidomArgs {
+  int nlist, nps, nkind, ncx, ncy, ncz, nstencil, lanes_sites, ntab;
+  const int* list;        // [nlist] molecules
+  const int* mol_first;
+  const double* r;        // positions of the last force evaluation (site order)
+  const int* cell_start;
+  const int4* stencil;
+  double Lx, Ly, Lz, cutoff_sq, sgrid, T;
+  double* U;              // [nlist] energy changes, or null
+  double* part;           // [nblocks] sums of exp(-dU/T)
+  const int4* pj;
+  const double4* pd;
+  const PairF* tabf;      // [2][MAX_WPROBE][MAX_KINDS]: real site constants, then virtual
+  const PairD* tabd;
+  const float4* eru;
+  const double* ert;
+};
+cudaError_t k_xwidom(const Launch& L, const XWidomArgs& a, bool fp64);
 cudaError_t k_widom(const Launch& L, const WidomBox* boxes, int nbox, long long n, bool fp64);
 
 cudaError_t k_drude_take(const Launch& L, const DrudeArgs& a, const double* r, double* out);

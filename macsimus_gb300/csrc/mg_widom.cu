@@ -214,6 +214,135 @@ __global__ void __launch_bounds__(WD_THREADS) widom_fp64_kernel(const WidomBox* 
   wd_block_sum(wacc, a.part);
 }
 
+// ------------------------------------------------- identity change --
+//
+// cook/widom.c:16-170 (Eidchange), sim/simmeas.c:1961-2003 (XWidom): a warp
+// per listed molecule; each of its sites against every site of the other
+// molecules within the cutoff, with the virtual minus the real constants
+// (smoothed LJ, erfc spline times the charge change); lane 0 adds
+// exp(-dU/T) (skipped for -dU/T <= -700).
+
+__device__ __forceinline__ float xw_lj(const PairF& P, float rr) {
+  if (rr >= P.C2q) return 0.f;
+  if (rr < P.C1q) {
+    const float x = P.Sq / rr, y = x * x * x;
+    return P.E4 * fmaf(y, y, -y);
+  }
+  const float x = rr - P.C2q;
+  return P.A * x * x;
+}
+__device__ __forceinline__ double xw_lj(const PairD& P, double rr) {
+  if (rr >= P.C2q) return 0.0;
+  if (rr < P.C1q) {
+    const double x = P.Sq / rr, y = x * x * x;
+    return P.E4 * (y * y - y);
+  }
+  const double x = rr - P.C2q;
+  return P.A * x * x;
+}
+
+__device__ __forceinline__ int xw_cell(double x, double L, int n) {
+  const double s = x / L - floor(x / L);
+  const int c = (int)(s * n);
+  return c < 0 ? 0 : (c >= n ? n - 1 : c);
+}
+
+template <bool FP64>
+__global__ void __launch_bounds__(WD_THREADS) xwidom_kernel(XWidomArgs a) {
+  __shared__ PairF tf[FP64 ? 1 : 2 * MAX_WPROBE * MAX_KINDS];
+  __shared__ PairD td[FP64 ? 2 * MAX_WPROBE * MAX_KINDS : 1];
+  for (int t = threadIdx.x; t < 2 * MAX_WPROBE * MAX_KINDS; t += WD_THREADS) {
+    if (FP64) td[t] = a.tabd[t];
+    else tf[t] = a.tabf[t];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int nw = gridDim.x * WD_WARPS;
+  const float sx = (float)(a.Lx * 2.3283064365386963e-10), sy = (float)(a.Ly * 2.3283064365386963e-10),
+              sz = (float)(a.Lz * 2.3283064365386963e-10);
+  const float cqf = (float)a.cutoff_sq, sgf = (float)a.sgrid;
+  double wacc = 0;
+  for (int l = blockIdx.x * WD_WARPS + (threadIdx.x >> 5); l < a.nlist; l += nw) {
+    const int n = a.list[l], i0 = a.mol_first[n];
+    double U = 0;
+    for (int s = 0; s < a.nps; s++) {
+      const double* ri = a.r + 3 * (long)(i0 + s);
+      const double x = ri[0], y = ri[1], z = ri[2];
+      const int cx = xw_cell(x, a.Lx, a.ncx), cy = xw_cell(y, a.Ly, a.ncy),
+                cz = xw_cell(z, a.Lz, a.ncz);
+      // the site as the cell list stores it: 32-bit box fraction (mixed) or
+      // the position wrapped into the box (FP64)
+      const unsigned ux = (unsigned)llrint((x / a.Lx - floor(x / a.Lx)) * 4294967296.0),
+                     uy = (unsigned)llrint((y / a.Ly - floor(y / a.Ly)) * 4294967296.0),
+                     uz = (unsigned)llrint((z / a.Lz - floor(z / a.Lz)) * 4294967296.0);
+      const double wx = x - a.Lx * floor(x / a.Lx), wy = y - a.Ly * floor(y / a.Ly),
+                   wz = z - a.Lz * floor(z / a.Lz);
+      const int s0 = a.lanes_sites ? 0 : lane, ds = a.lanes_sites ? 1 : 32;
+      for (int st = s0; st < a.nstencil; st += ds) {
+        const int4 o = a.stencil[st];
+        const int c2 = (wd_wrap(cx + o.x, a.ncx) * a.ncy + wd_wrap(cy + o.y, a.ncy)) * a.ncz +
+                       wd_wrap(cz + o.z, a.ncz);
+        const int j0 = a.cell_start[c2], j1 = a.cell_start[c2 + 1];
+        double u = 0;
+        for (int j = j0 + (a.lanes_sites ? lane : 0); j < j1; j += a.lanes_sites ? 32 : 1) {
+          if (FP64) {
+            const double4 q = a.pd[j];
+            const long long w = __double_as_longlong(q.w);
+            if ((int)(w >> 8) == n) continue;
+            double dx = wx - q.x, dy = wy - q.y, dz = wz - q.z;
+            dx -= a.Lx * rint(dx / a.Lx);
+            dy -= a.Ly * rint(dy / a.Ly);
+            dz -= a.Lz * rint(dz / a.Lz);
+            const double rr = dx * dx + dy * dy + dz * dz;
+            if (rr >= a.cutoff_sq) continue;
+            const PairD& PR = td[s * MAX_KINDS + (int)(w & 255)];
+            const PairD& PV = td[(MAX_WPROBE + s) * MAX_KINDS + (int)(w & 255)];
+            u += xw_lj(PV, rr) - xw_lj(PR, rr);
+            const double dq = PV.qq - PR.qq;
+            if (dq != 0) {
+              const double* e = a.ert + 6 * min((int)(rr * a.sgrid), a.ntab - 1);
+              u += (e[1] / (e[2] + rr) + e[0]) * dq;
+            }
+          } else {
+            const int4 q = a.pj[j];
+            if ((q.w >> 8) == n) continue;
+            const float dx = (float)(int)(ux - (unsigned)q.x) * sx;
+            const float dy = (float)(int)(uy - (unsigned)q.y) * sy;
+            const float dz = (float)(int)(uz - (unsigned)q.z) * sz;
+            const float rr = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            if (rr >= cqf) continue;
+            const PairF& PR = tf[s * MAX_KINDS + (q.w & 255)];
+            const PairF& PV = tf[(MAX_WPROBE + s) * MAX_KINDS + (q.w & 255)];
+            float du = xw_lj(PV, rr) - xw_lj(PR, rr);
+            const float dq = PV.qq - PR.qq;
+            if (dq != 0.f) {
+              const float4 e = __ldg(a.eru + min((int)(rr * sgf), a.ntab - 1));
+              du += (__fdividef(e.y, e.z + rr) + e.x) * dq;
+            }
+            u += du;
+          }
+        }
+        U += u;
+      }
+    }
+    U = warp_sum(U);
+    if (lane == 0) {
+      if (a.U) a.U[l] = U;
+      const double e = -U / a.T;
+      if (e > -700) wacc += exp(e);
+    }
+  }
+  wd_block_sum(wacc, a.part);
+}
+
+cudaError_t k_xwidom(const Launch& L, const XWidomArgs& a, bool fp64) {
+  const int nb = widom_blocks(a.nlist);
+  if (fp64) xwidom_kernel<true><<<nb, WD_THREADS, 0, L.s>>>(a);
+  else xwidom_kernel<false><<<nb, WD_THREADS, 0, L.s>>>(a);
+  ++*L.counter;
+  return cudaGetLastError();
+}
+
 int widom_blocks(long long n) {
   long long b = (n + WD_WARPS - 1) / WD_WARPS;
   return (int)(b < 152 * 8 ? (b > 0 ? b : 1) : 152 * 8);

@@ -47,11 +47,14 @@ SITE_TYPES = {
     "AP": (22.9898, 0.5, 3.3),
     "AM": (35.453, 0.7, 4.1),
     "PRB": (39.948, 0.65, 3.2),
+    # the cation with changed size, well depth and charge: the target of an
+    # identity change (XWidom) of AP
+    "APV": (22.9898, 0.55, 3.4),
     # TIP4P/2005: the LJ oxygen and the massless charge site M
     "OT": (15.9994, 0.774908, 3.1589),
     "MW": (0.0, 0.0, 0.0),
 }
-TYPE_ORDER = ["H", "O", "NA", "CL", "OD", "AP", "AM", "PRB", "OT", "MW"]
+TYPE_ORDER = ["H", "O", "NA", "CL", "OD", "AP", "AM", "PRB", "OT", "MW", "APV"]
 
 # Drude parameters of a site type: (alphapol A^3, chargepol e).  The Drude
 # water has the shell charge -1.8 e on a spring of 4184 kJ/mol/A^2
@@ -147,7 +150,7 @@ def spce_drude():
 
 SPECIES = {"WAT": spce, "NA": lambda: ion("NA"), "CL": lambda: ion("CL"), "WATD": spce_drude,
            "AP": lambda: ion("AP", 1.0), "AM": lambda: ion("AM", -1.0),
-           "PRB": lambda: ion("PRB", 0.0), "T4P": tip4p2005}
+           "PRB": lambda: ion("PRB", 0.0), "T4P": tip4p2005, "APV": lambda: ion("APV", 0.8)}
 
 
 @dataclass

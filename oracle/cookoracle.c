@@ -983,6 +983,66 @@ double orc_einsert(const orc_sys_t *s, const double *r, int nps, const int *ptyp
   return U + El;
 }
 
+/* cook/widom.c:16-170 (Eidchange) and sim/simmeas.c:1961-2003 (XWidom):
+   for each listed molecule, the r-space energy change (smoothed LJ + erfc
+   spline) of giving its sites the types vtype[] and charges vq[], summed
+   over every site of the other molecules within the cutoff (the molecule
+   itself is taken out of the cell list first); returns the sum of
+   exp(-dU/T) (a term with -dU/T <= -700 counts 0); dU[] per molecule */
+double orc_xwidom(const orc_sys_t *s, const double *r, int nlist, const int *mols,
+                  const int *mol_first, const int *vtype, const double *vq, double T,
+                  double *dU)
+{
+  const double cq = SQ(s->cutoff);
+  double sum = 0;
+  int l, i, j;
+  for (l = 0; l < nlist; l++) {
+    const int n = mols[l], i0 = mol_first[n], i1 = mol_first[n + 1];
+    double Ur = 0, Uv = 0, El = 0, e;
+    for (i = i0; i < i1; i++) {
+      const int k = i - i0;
+      for (j = 0; j < s->ns; j++) {
+        double dr[3], rr, x, y;
+        const orc_ss_t *sr, *sv;
+        if (s->mol[j] == s->mol[i]) continue;
+        nearest(s->L, r + 3 * i, r + 3 * j, dr);
+        rr = SQ(dr[0]) + SQ(dr[1]) + SQ(dr[2]);
+        if (rr >= cq) continue;
+        sr = s->ss + s->type[i] * s->ntypes + s->type[j];
+        sv = s->ss + vtype[k] * s->ntypes + s->type[j];
+        if (rr < sr->C2q) {
+          if (rr < sr->C1q) {
+            x = sr->Sq / rr;
+            y = x * x * x;
+            Ur += sr->E4 * (y * y - y);
+          } else {
+            x = rr - sr->C2q;
+            Ur += x * x * sr->A;
+          }
+        }
+        if (rr < sv->C2q) {
+          if (rr < sv->C1q) {
+            x = sv->Sq / rr;
+            y = x * x * x;
+            Uv += sv->E4 * (y * y - y);
+          } else {
+            x = rr - sv->C2q;
+            Uv += x * x * sv->A;
+          }
+        }
+        if (s->q[j] != 0 && vq[k] != s->q[i]) {
+          const double *p = s->ertab + 6 * (int)(rr * s->sgrid);
+          El += (p[1] / (p[2] + rr) + p[0]) * (vq[k] - s->q[i]) * s->q[j];
+        }
+      }
+    }
+    if (dU) dU[l] = Uv - Ur + El;
+    e = -(Uv - Ur + El) / T;
+    if (e > -700) sum += exp(e);
+  }
+  return sum;
+}
+
 typedef struct {
   const orc_sys_t *s;
   const double *r, *geom, *pq;

@@ -128,6 +128,9 @@ double orc_widom(const orc_sys_t *s, const double *r, int nps, const int *ptype,
                  const double *pq, const double *geom, long long n, unsigned long long seed,
                  double T, double *U, int nthreads);
 double orc_widom_corr(const orc_sys_t *s, int nps, const int *ptype);
+double orc_xwidom(const orc_sys_t *s, const double *r, int nlist, const int *mols,
+                  const int *mol_first, const int *vtype, const double *vq, double T,
+                  double *dU);
 
 /* Adjoint: gradients of E, W = LJ sum r.f + E_el and (g = dLoss/dF) of a
    force loss with respect to the LJ (epsilon, sigma) of every type pair a<=b

@@ -75,6 +75,8 @@ def lib():
         L.orc_widom_word.restype = u64
         L.orc_widom_sites.argtypes = [u64, C.c_longlong, dp, C.c_int, dp, dp]
         L.orc_einsert.argtypes = [C.POINTER(SYS), dp, C.c_int, ip, dp, dp]
+        L.orc_xwidom.argtypes = [C.POINTER(SYS), dp, C.c_int, ip, ip, ip, dp, C.c_double, dp]
+        L.orc_xwidom.restype = C.c_double
         L.orc_einsert.restype = C.c_double
         L.orc_widom.argtypes = [C.POINTER(SYS), dp, C.c_int, ip, dp, dp, C.c_longlong, u64,
                                 C.c_double, dp, C.c_int]
@@ -277,6 +279,20 @@ class Oracle:
         pq = np.ascontiguousarray(probe_q, np.float64)
         pp = np.ascontiguousarray(positions, np.float64).reshape(-1)
         return lib().orc_einsert(C.byref(self.sys), _dp(r), len(pt), _ip(pt), _dp(pq), _dp(pp))
+
+    def xwidom(self, r, mols, vtype, vq, T):
+        """identity change of the listed molecules to site types vtype and
+        charges vq (cook's XWidom): (sum of exp(-dU/T), dU per molecule)"""
+        s = self.system
+        r = np.ascontiguousarray(r, dtype=np.float64).reshape(-1)
+        mols = np.ascontiguousarray(mols, np.int32)
+        vtype = np.ascontiguousarray(vtype, np.int32)
+        vq = np.ascontiguousarray(vq, np.float64)
+        mf = np.ascontiguousarray(s.mol_first, np.int32)
+        dU = np.zeros(len(mols))
+        tot = lib().orc_xwidom(C.byref(self.sys), _dp(r), len(mols), _ip(mols), _ip(mf),
+                               _ip(vtype), _dp(vq), T, _dp(dU))
+        return tot, dU
 
     def widom(self, r, probe_types, probe_q, geometry, n, seed, T, energies=False, nthreads=8):
         """(sum of exp(-U/T), corr, U or None) over n insertions"""

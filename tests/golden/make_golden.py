@@ -61,6 +61,12 @@ CASES = {
     "widom500": dict(binary="cookwidom", species=["AP", "AM", "PRB"], N=[250, 250, 0],
                      L=37.0, cutoff=10.0, alpha=0.31, kn=8, steps=1, h=0.002, epsc=1e-10,
                      extra_def=["corr=1"], extra_get=["widom.sp=2", "widom.n=10000000"]),
+    # identity change AP -> APV (sigma 3.3 -> 3.4 A, epsilon 0.5 -> 0.55
+    # kJ/mol, charge +1 -> +0.8 e) of every cation of the same box
+    # (sim/simmeas.c XWidom, cook/widom.c Eidchange)
+    "xwidom500": dict(binary="cookwidom", species=["AP", "AM", "APV"], N=[250, 250, 0],
+                      L=37.0, cutoff=10.0, alpha=0.31, kn=8, steps=1, h=0.002, epsc=1e-10,
+                      extra_get=["widom.spreal=0", "widom.sp=2"]),
 }
 
 
@@ -135,7 +141,11 @@ def run_case(name, c, keep=None):
                 omegac=float(m3.group(1)) if m3 else None,
                 species=c["species"], N=c["N"])
     mw = re.search(r"mu = (\S+) \+- \S+ K \(raw value without cutoff correction\)", prt)
-    if mw:
+    if mw and "widom.spreal" in get_text(c):
+        # identity change: cook prints mu = -T ln <exp(-dU/T)> over the molecules
+        mc = re.search(r"corr = (\S+)/V = (\S+)", prt)
+        meta["xwidom"] = dict(mu_raw_K=float(mw.group(1)), corr=float(mc.group(1)))
+    elif mw:
         mc = re.search(r"corr = (\S+)/V = (\S+)", prt)
         mk = re.search(r"mu = (\S+) \+- \S+ kT \(corrected\)", prt)
         meta["widom"] = dict(mu_raw_K=float(mw.group(1)), corr=float(mc.group(1)),

@@ -99,3 +99,26 @@ def test_errors_are_reported():
     fd.forces(np.vstack([gd["r"][0], gd["rD"][0]]))
     with pytest.raises(M.MGError):
         fd.widom([0], n=10)          # Drude systems are not supported
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_identity_change_vs_oracle_and_reference(precision):
+    """cook's XWidom on the device: every AP cation of the last configuration
+    changed into APV; energy changes per molecule against the oracle and the
+    chemical potential against cook's printed value (6 digits)"""
+    g, meta, system, ew = load("xwidom500")
+    T = 298.0
+    fp = M.ForcePath(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"],
+                     precision=precision)
+    orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
+    r = g["r"][-1]
+    fp.forces(r)
+    ap = list(range(system.counts[0]))
+    vt, vq = [ff.TYPE_ORDER.index("APV")], [0.8 * ff.ELECTRON]
+    res = fp.xwidom(ap, vt, vq, T, energies=True)
+    s, dU = orc.xwidom(r, ap, vt, vq, T)
+    tol = 1e-7 if precision == "fp64" else 2e-3          # K
+    assert np.abs(res["dU"] - dU).max() < tol * max(1.0, np.abs(dU).max())
+    assert abs(res["sum"] / s - 1) < (1e-9 if precision == "fp64" else 1e-5)
+    mu = meta["xwidom"]["mu_raw_K"]
+    assert abs(res["mu"] - mu) <= 6e-6 * abs(mu) + (0 if precision == "fp64" else 0.01)

@@ -86,3 +86,21 @@ def test_einsert_is_a_pair_sum():
     y = x ** 3
     u = ss.E4 * (y * y - y) if rr < ss.C1q else ss.A * (rr - ss.C2q) ** 2
     assert abs((e_full - e_rest) - u) < 1e-9 * abs(u)
+
+
+def test_identity_change_matches_cook():
+    """cook's XWidom (sim/simmeas.c:1961, cook/widom.c Eidchange): every AP
+    cation of the last configuration turned into APV (sigma 3.3 -> 3.4 A,
+    epsilon 0.5 -> 0.55 kJ/mol, charge +1 -> +0.8 e); cook prints
+    mu = -T ln <exp(-dU/T)> to 6 significant digits"""
+    g, meta, system, ew = load("xwidom500")
+    orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
+    T = 298.0
+    ap = list(range(system.counts[0]))   # molecules run species by species
+    assert system.species[0] == "AP" and len(ap) == 250
+    vt = [ff.TYPE_ORDER.index("APV")]
+    vq = [0.8 * ff.ELECTRON]
+    s, dU = orc.xwidom(g["r"][-1], ap, vt, vq, T)
+    mu = -T * np.log(s / len(ap))
+    assert abs(mu - meta["xwidom"]["mu_raw_K"]) <= 6e-6 * abs(meta["xwidom"]["mu_raw_K"])
+    assert np.isclose(s, np.exp(-dU / T).sum(), rtol=1e-12)
