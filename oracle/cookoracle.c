@@ -775,10 +775,28 @@ int orc_forces(const orc_sys_t *s, const double *r, double *f, orc_en_t *en, int
 
 /* sim/constrd.c:767-839 (SHAKE=1 sweeps) with sim/verlet.c:101-104 (no
    thermostat) and the VERLET=3 kinetic energy of sim/shakev3.c */
+int orc_shake_step_dp(int ns, double *r, double *r1, const double *f, const double *mass,
+                      int nmol, const int *mol_first, const int *mol_nc, const int *cfirst,
+                      const int *ci, const int *cj, const double *bondq,
+                      double h, double eps, double omega, int maxit, const double *dp,
+                      double *ekin);
+
 int orc_shake_step(int ns, double *r, double *r1, const double *f, const double *mass,
                    int nmol, const int *mol_first, const int *mol_nc, const int *cfirst,
                    const int *ci, const int *cj, const double *bondq,
                    double h, double eps, double omega, int maxit, double *ekin)
+{
+  return orc_shake_step_dp(ns, r, r1, f, mass, nmol, mol_first, mol_nc, cfirst, ci, cj, bondq,
+                           h, eps, omega, maxit, NULL, ekin);
+}
+
+/* the same step with dp[] added to the unconstrained positions: the
+   Nose-Hoover friction term -Vfactor v_pred of sim/verlet.c:22-37 */
+int orc_shake_step_dp(int ns, double *r, double *r1, const double *f, const double *mass,
+                      int nmol, const int *mol_first, const int *mol_nc, const int *cfirst,
+                      const int *ci, const int *cj, const double *bondq,
+                      double h, double eps, double omega, int maxit, const double *dp,
+                      double *ekin)
 {
   double hh = h * h, kin = 0;
   int n, worst = 0;
@@ -791,7 +809,7 @@ int orc_shake_step(int ns, double *r, double *r1, const double *f, const double 
       for (k = 0; k < 3; k++)
         /* a massless site is a dependant, placed by depend_r after the step */
         p[3 * i + k] = f[3 * i + k] * (mass[i] > 0 ? hh / mass[i] : 0) + r[3 * i + k] +
-                       r1[3 * i + k];
+                       r1[3 * i + k] + (dp ? dp[3 * i + k] : 0);
     if (nc > 0) {
       do {
         it++;

@@ -108,6 +108,12 @@ int orc_shake_step(int ns, double *r, double *r1, const double *f, const double 
                    int nmol, const int *mol_first, const int *mol_nc, const int *cfirst,
                    const int *ci, const int *cj, const double *bondq,
                    double h, double eps, double omega, int maxit, double *ekin);
+/* orc_shake_step with dp[] added to the unconstrained positions (NULL: none) */
+int orc_shake_step_dp(int ns, double *r, double *r1, const double *f, const double *mass,
+                      int nmol, const int *mol_first, const int *mol_nc, const int *cfirst,
+                      const int *ci, const int *cj, const double *bondq,
+                      double h, double eps, double omega, int maxit, const double *dp,
+                      double *ekin);
 
 /* one Drude relaxation iteration (sim/scf.c selffield): r and f hold 2*ns
    vectors (sites, then Drude displacements / Drude forces); energies added

@@ -67,6 +67,8 @@ def lib():
         L.orc_forces.argtypes = [C.POINTER(SYS), dp, dp, C.POINTER(EN), C.c_int]
         L.orc_shake_step.argtypes = [C.c_int, dp, dp, dp, dp, C.c_int, ip, ip, ip, ip, ip, dp,
                                      C.c_double, C.c_double, C.c_double, C.c_int, dp]
+        L.orc_shake_step_dp.argtypes = [C.c_int, dp, dp, dp, dp, C.c_int, ip, ip, ip, ip, ip, dp,
+                                        C.c_double, C.c_double, C.c_double, C.c_int, dp, dp]
         L.orc_selffield.argtypes = [C.POINTER(SYS), dp, dp, C.POINTER(EN), C.c_double]
         L.orc_selffield.restype = C.c_double
         L.orc_aspc_coef.argtypes = [C.c_int, dp, dp]
@@ -226,7 +228,8 @@ class Oracle:
             en["Pvir"] = list(e.Pvir)
         return r2, f2, en, d
 
-    def shake_step(self, r, r1, f, h, eps=1e-10, omega=0.6, maxit=1000):
+    def shake_step(self, r, r1, f, h, eps=1e-10, omega=0.6, maxit=1000, dp=None):
+        """leap-frog + SHAKE (dp: added to the unconstrained positions)"""
         s = self.system
         r = np.ascontiguousarray(r, dtype=np.float64).copy().reshape(-1)
         r1 = np.ascontiguousarray(r1, dtype=np.float64).copy().reshape(-1)
@@ -239,9 +242,11 @@ class Oracle:
         cj = np.ascontiguousarray(s.cons[:, 1], np.int32)
         bq = np.ascontiguousarray(s.cons_len ** 2, np.float64)
         ek = C.c_double()
-        it = lib().orc_shake_step(s.ns, _dp(r), _dp(r1), _dp(f), _dp(mass), s.nmol, _ip(mfirst),
-                                  _ip(nc), _ip(cfirst), _ip(ci), _ip(cj), _dp(bq), h, eps,
-                                  omega, maxit, C.byref(ek))
+        dpa = None if dp is None else np.ascontiguousarray(dp, np.float64).reshape(-1)
+        it = lib().orc_shake_step_dp(s.ns, _dp(r), _dp(r1), _dp(f), _dp(mass), s.nmol,
+                                     _ip(mfirst), _ip(nc), _ip(cfirst), _ip(ci), _ip(cj), _dp(bq),
+                                     h, eps, omega, maxit,
+                                     _dp(dpa) if dpa is not None else None, C.byref(ek))
         return r.reshape(-1, 3), r1.reshape(-1, 3), it, ek.value
 
 
@@ -342,6 +347,50 @@ def normalize(system, r, L, r0=0.15):
         lo = r[a:b][heavy].min(axis=0)
         r[a:b] += np.where(lo < r0, L, np.where(lo >= r0 + L, -L, 0.0))
     return r
+
+
+def trvp_coef(k):
+    """time-reversible velocity predictor of length k (sim/trvpscale.c:31-35;
+    J. Chem. Theory Comput. 7, 3596 (2011)): h v(t) ~ sum_j b_j X_j"""
+    b = [(2 * k + 1) / (k + 1)]
+    for j in range(k):
+        b.append(-b[j] * (k - j) / (k + j + 2))
+    return b
+
+
+class NoseHoover:
+    """cook's Nose-Hoover thermostat for Verlet + SHAKE (thermostat=2):
+    sim/trvpscale.c (predicted velocities of all degrees of freedom from the
+    last k <= pred displacements, k growing from 0), sim/verlet.c:22-37
+    (p = h^2 f/m + r + r1 - Vfactor v_pred, Vfactor the predicted h dlogs/dt)
+    and sim/thermo.c:180-212 (leap-frog of logs with the step's temperature,
+    the extended energy of VERLET=3)."""
+
+    def __init__(self, T, tau, nf, h, pred=2):
+        self.T, self.tau, self.nf, self.h, self.pred = T, tau, nf, h, pred
+        self.k, self.hist, self.lhist = 0, [], []
+        self.logs = self.logsv = 0.0
+        self.ext = 0.0
+
+    def step(self, orc, r, r1, f, eps=1e-10, omega=0.6):
+        h, k = self.h, self.k
+        b = trvp_coef(k)
+        X = [np.asarray(r1, np.float64)] + self.hist[:k]
+        Lx = [self.logsv] + self.lhist[:k]
+        vpred = sum(bj * xj for bj, xj in zip(b, X))
+        vfactor = sum(bj * lj for bj, lj in zip(b, Lx))
+        knew = min(self.pred, k + 1)
+        self.hist = [np.array(r1, np.float64)] + self.hist[:knew - 1]
+        self.lhist = [self.logsv] + self.lhist[:knew - 1]
+        self.k = knew
+        rn, r1n, it, ek = orc.shake_step(r, r1, f, h, eps=eps, omega=omega, dp=-vfactor * vpred)
+        # En.T of cook: twice the kinetic energy over No.f
+        Tk = 2 * ek / self.nf
+        ld, lo = self.logsv, self.logs
+        self.logsv += h * h * (Tk / self.T - 1) / self.tau ** 2
+        self.logs += self.logsv
+        self.ext = self.nf * self.T * (lo + (self.tau / h) ** 2 * (ld ** 2 + self.logsv ** 2) / 4)
+        return rn, r1n, it, ek
 
 
 def aspc_coef(k):

@@ -36,6 +36,14 @@ CASES = {
     # 216 SPC/E waters, cutoff 9 A, alpha 0.35/A, |n|<=6
     "spce216": dict(binary="cookew", species=["WAT"], N=[216], L=18.6206,
                     cutoff=9.0, alpha=0.35, kn=6, steps=3, h=0.002, epsc=1e-10),
+    # 216 SPC/E under cook's Nose-Hoover thermostat (tau.T 0.05 ps, the
+    # Verlet+SHAKE form with the time-reversible velocity predictor, k <= 2
+    # by the default -p229); playback (-y) and velocity playback (-n1) frames
+    # after every step give the initial r1 the dumps lack
+    "nose216": dict(binary="cookew", species=["WAT"], N=[216], L=18.6206,
+                    cutoff=9.0, alpha=0.35, kn=6, steps=5, h=0.002, epsc=1e-10,
+                    options=["-y99999", "-n1"], extra_def=["thermostat=2", "tau.T=0.05"],
+                    extra_get=["dt.plb=0.002"]),
     # the 864 SPC/E configuration: L=29.65 A, cutoff 12, alpha 0.26, |n|<=8
     "spce864": dict(binary="cookew", species=["WAT"], N=[864], L=29.65,
                     cutoff=12.0, alpha=0.26, kn=8, steps=2, h=0.002, epsc=1e-10),

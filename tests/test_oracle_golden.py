@@ -178,3 +178,28 @@ def test_reference_states_are_normalized():
         g, meta, system, ew = load(case)
         for d in range(g["r"].shape[0]):
             assert np.array_equal(O.normalize(system, g["r"][d], ew["L"]), g["r"][d])
+
+
+def test_nose_hoover_trajectory_matches_reference():
+    """cook's Nose-Hoover Verlet+SHAKE (thermostat=2, tau.T 0.05 ps, TRVP
+    k -> 2): five steps from r(t0) and the initial r1 of cook's velocity
+    playback (float32) reproduce cook's positions; cook's printed En.kin of
+    the last step (the thermostat changes it from the NVE value)"""
+    g, meta, system, ew = load("nose216")
+    p = meta["params"]
+    orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
+    h = p["h"]
+    nh = O.NoseHoover(298.0, 0.05, 3 * system.ns - len(system.cons) - 3, h)
+    r = g["r"][1].copy()
+    r1 = g["vlb_r"][0].astype(np.float64) * h
+    for step in range(5):
+        f, _ = orc.forces(r, measure=False, nthreads=4)
+        r, r1, it, ek = nh.step(orc, r, r1, f, omega=meta["omegac"] / 2)
+        ref = g["r"][step + 2] if step + 2 < g["r"].shape[0] else g["plb_r"][5]
+        # dumps print 12 decimals, the playback frame is float32
+        tol = 5e-8 if step + 2 < g["r"].shape[0] else 3e-6
+        assert np.abs(r - ref).max() < tol, step
+    assert nh.k == 2 and nh.logsv != 0
+    # the last step's kinetic energy (9 digits printed); the initial r1 is
+    # known to float precision only
+    assert abs(ek / meta["Ekin_last"] - 1) < 1e-8
