@@ -119,10 +119,14 @@ typedef struct {
      the erfc force spline in shared memory (else read through L1).
      mg_autotune picks it. */
   int pair_variant;
-  /* thermostat after every SHAKE step (sim/thermo.c): 0 none, 1 Berendsen,
-     2 Bussi (stochastic velocity rescaling); temperature T (K), time
-     constant tau_T (ps), degrees of freedom thermo_f (<=0: cook's No.f,
-     3 (ns - ndep) - nc - 3), seed of the Bussi stream */
+  /* thermostat (sim/thermo.c): 0 none, 1 Berendsen, 2 Bussi (stochastic
+     velocity rescaling), both applied after every SHAKE step; 3 Nose-Hoover
+     in cook's Verlet+SHAKE form (cook's thermostat=2, T_NOSE: friction
+     -Vfactor vpred inside the step with the time-reversible velocity
+     predictor of nose_pred steps, sim/trvpscale.c, sim/verlet.c:22-37,
+     sim/thermo.c:180-212); temperature T (K), time constant tau_T (ps),
+     degrees of freedom thermo_f (<=0: cook's No.f, 3 (ns - ndep) - nc - 3),
+     seed of the Bussi stream */
   int thermostat;
   double T, tau_T, thermo_f;
   unsigned long long seed;
@@ -140,6 +144,9 @@ typedef struct {
      the FP32 cores; 3 = both passes on the tensor cores.  The tensor-core
      passes run TF32 split into three products with FP32 accuracy. */
   int kspace_engine;
+  /* Nose-Hoover predictor length k (cook's No.pred = option -p % 10,
+     sim/main.c:404-405), 1..8; <=0 selects 2 */
+  int nose_pred;
 } mg_params;
 
 /* Energies of one force evaluation (program units, K).
@@ -226,6 +233,13 @@ int mg_last_launches(const mg_ctx *ctx);
 /* factor by which the last thermostat call scaled the velocities (1 if
    none); a synchronising read */
 double mg_thermostat_factor(mg_ctx *ctx);
+
+/* Nose-Hoover state after the last step (thermostat 3): state[0] = logs,
+   state[1] = h dlogs/dt (cook's cfg[0]->logs and cfg[1]->logs), state[2] =
+   the thermostat's part of the conserved energy of that step (cook's Eext
+   of VERLET=3, sim/thermo.c:205-212), in K; a synchronising read.
+   mg_md_set_state starts the thermostat from logs = 0 with no history. */
+int mg_nose_state(mg_ctx *ctx, double state[3]);
 
 /* FP32 path: run the Ewald k-space chain on a second stream beside the
    r-space chain (on by default; off serialises them, e.g. to time kernels

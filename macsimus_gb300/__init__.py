@@ -56,7 +56,8 @@ class Params(C.Structure):
                 ("nl_every", C.c_int), ("kspace_ctas_per_sm", C.c_int), ("pair_variant", C.c_int),
                 ("thermostat", C.c_int), ("T", C.c_double), ("tau_T", C.c_double),
                 ("thermo_f", C.c_double), ("seed", C.c_ulonglong), ("box_rmin", C.c_double),
-                ("no_normalize", C.c_int), ("kspace_engine", C.c_int)]
+                ("no_normalize", C.c_int), ("kspace_engine", C.c_int),
+                ("nose_pred", C.c_int)]
 
 
 class Energy(C.Structure):
@@ -123,6 +124,7 @@ def library():
         L.mg_set_overlap.argtypes = [vp, C.c_int]
         L.mg_thermostat_factor.argtypes = [vp]
         L.mg_thermostat_factor.restype = C.c_double
+        L.mg_nose_state.argtypes = [vp, _dp]
         L.mg_profile_enable.argtypes = [vp, C.c_int]
         L.mg_profile_reset.argtypes = [vp]
         L.mg_profile_entry.argtypes = [vp, C.c_int, C.POINTER(C.c_char_p), _dp,
@@ -182,7 +184,8 @@ def describe(system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None, 
              rshift=3, rplus=2.5, epsinf=3e33, h=0.002, epsc=1e-7, omegac=1.2, shake_maxit=1000,
              cells_per_cutoff=0, aspc_k=2, scf_iter=1, scf_omega=0.6, minqq=1.0, skin=0.0,
              nl_every=50, kspace_ctas_per_sm=0, pair_variant=0, thermostat=0, T=298.0,
-             tau_T=0.1, thermo_f=0.0, seed=0, box_rmin=0.0, normalize=True, kspace_engine=0):
+             tau_T=0.1, thermo_f=0.0, seed=0, box_rmin=0.0, normalize=True, kspace_engine=0,
+             nose_pred=2):
     """(mg_topology, mg_params, arrays to keep alive) of one box"""
     keep = []
 
@@ -252,7 +255,8 @@ def describe(system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None, 
     p.nl_every = nl_every
     p.kspace_ctas_per_sm = kspace_ctas_per_sm
     p.pair_variant = pair_variant
-    p.thermostat = {"none": 0, "berendsen": 1, "bussi": 2}.get(thermostat, thermostat) or 0
+    p.thermostat = {"none": 0, "berendsen": 1, "bussi": 2,
+                    "nose": 3}.get(thermostat, thermostat) or 0
     p.T = T
     p.tau_T = tau_T
     p.thermo_f = thermo_f
@@ -260,6 +264,7 @@ def describe(system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None, 
     p.box_rmin = box_rmin
     p.no_normalize = 0 if normalize else 1
     p.kspace_engine = int(kspace_engine)
+    p.nose_pred = int(nose_pred)
     return t, p, keep
 
 
@@ -271,7 +276,7 @@ class ForcePath:
                  shake_maxit=1000, cells_per_cutoff=0, aspc_k=2, scf_iter=1, scf_omega=0.6,
                  minqq=1.0, skin=0.0, nl_every=50, kspace_ctas_per_sm=0, pair_variant=0,
                  thermostat=0, T=298.0, tau_T=0.1, thermo_f=0.0, seed=0, box_rmin=0.0,
-                 normalize=True, kspace_engine=0):
+                 normalize=True, kspace_engine=0, nose_pred=2):
         lib = library()
         self.system = system
         self.ns = system.ns
@@ -285,7 +290,7 @@ class ForcePath:
                                     pair_variant=pair_variant, thermostat=thermostat, T=T,
                                     tau_T=tau_T, thermo_f=thermo_f, seed=seed,
                                     box_rmin=box_rmin, normalize=normalize,
-                                    kspace_engine=kspace_engine)
+                                    kspace_engine=kspace_engine, nose_pred=nose_pred)
         self.polar = getattr(system, "polar", False)
         Lb = np.broadcast_to(np.asarray(L, dtype=np.float64), (3,))
         st = C.c_int(0)
@@ -422,6 +427,13 @@ class ForcePath:
     def thermostat_factor(self):
         """velocity factor of the last thermostat call"""
         return library().mg_thermostat_factor(self._ctx)
+
+    def nose_state(self):
+        """Nose-Hoover (thermostat="nose"): (logs, h dlogs/dt, the thermostat's
+        part of the conserved energy of the last step, K)"""
+        st = (C.c_double * 3)()
+        self._check(library().mg_nose_state(self._ctx, st))
+        return tuple(st)
 
     def set_overlap(self, on):
         """FP32 path: k-space chain concurrent with the r-space chain (default on)"""

@@ -118,6 +118,9 @@ struct mg_ctx {
   unsigned long long seed = 0;
   long long* d_step = nullptr;
   double *d_chi = nullptr, *d_zth = nullptr;
+  // Nose-Hoover: state (NoseSlot) and the r1 history [nose_pred][3 ns]
+  int nose_pred = 0;
+  double *d_nh = nullptr, *d_vhist = nullptr;
   // Widom: the type table, the site kinds, sites per type; cell data of the
   // last force evaluation (cook's lastlist)
   int ntypes = 0, comb_rule = 1;
@@ -280,8 +283,11 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   ctx->use_list = p->skin > 0;
   ctx->pair_variant = p->pair_variant;
   ctx->thermostat = p->thermostat;
-  if (ctx->thermostat < 0 || ctx->thermostat > 2)
-    return fail(ctx, MG_ERR_ARG, "thermostat: 0 none, 1 Berendsen, 2 Bussi");
+  if (ctx->thermostat < 0 || ctx->thermostat > 3)
+    return fail(ctx, MG_ERR_ARG, "thermostat: 0 none, 1 Berendsen, 2 Bussi, 3 Nose-Hoover");
+  ctx->nose_pred = p->nose_pred > 0 ? p->nose_pred : 2;
+  if (ctx->nose_pred > MG_NOSE_MAXPRED)
+    return fail(ctx, MG_ERR_ARG, "nose_pred must be at most 8");
   if (ctx->thermostat && !(p->T > 0 && p->tau_T > 0))
     return fail(ctx, MG_ERR_ARG, "thermostat needs T > 0 and tau_T > 0");
   ctx->T = p->T;
@@ -739,6 +745,12 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   CK(dalloc(&ctx->d_zth, 1));
   CK(dalloc(&ctx->d_step, 1));
   CK(cudaMemset(ctx->d_step, 0, sizeof(long long)));
+  if (ctx->thermostat == 3) {
+    CK(dalloc(&ctx->d_nh, NH_HIST + MG_NOSE_MAXPRED));
+    CK(cudaMemset(ctx->d_nh, 0, sizeof(double) * (NH_HIST + MG_NOSE_MAXPRED)));
+    CK(dalloc(&ctx->d_vhist, (size_t)ctx->nose_pred * 3 * ns));
+    CK(cudaMemset(ctx->d_vhist, 0, sizeof(double) * ctx->nose_pred * 3 * (size_t)ns));
+  }
   {
     const double one = 1;
     CK(cudaMemcpy(ctx->d_zth, &one, sizeof(double), cudaMemcpyHostToDevice));
@@ -1090,6 +1102,10 @@ ShakeArgs shake_args(mg_ctx* ctx) {
   sa.normalize = ctx->normalize;
   sa.r0 = ctx->box_r0;
   for (int d = 0; d < 3; d++) sa.Lb[d] = ctx->L[d];
+  sa.nh = ctx->d_nh;
+  sa.vhist = ctx->thermostat == 3 ? ctx->d_vhist : nullptr;
+  sa.nh_pred = ctx->nose_pred;
+  sa.nstride = 3LL * ctx->ns;
   return sa;
 }
 
@@ -1117,6 +1133,8 @@ ThermoArgs thermo_args(mg_ctx* ctx) {
   t.seed = ctx->seed;
   t.step = ctx->d_step;
   t.zout = ctx->d_zth;
+  t.nh = ctx->d_nh;
+  t.pred = ctx->nose_pred;
   return t;
 }
 
@@ -1200,7 +1218,7 @@ int mg_destroy(mg_ctx* ctx) {
                   ctx->d_wtabf, ctx->d_wtabd, ctx->d_wgeom, ctx->d_wpart, ctx->d_wbox,
                   ctx->d_qfix, ctx->d_adjtab, ctx->d_ag, ctx->d_aq, ctx->d_apart, ctx->d_adEq,
                   ctx->d_adLq, ctx->d_ags, ctx->d_atpart, ctx->d_aT, ctx->d_fk,
-                  ctx->d_chi, ctx->d_zth, ctx->d_step, ctx->d_dep_site, ctx->d_dep_first,
+                  ctx->d_chi, ctx->d_zth, ctx->d_step, ctx->d_nh, ctx->d_vhist, ctx->d_dep_site, ctx->d_dep_first,
                   ctx->d_dep_parent, ctx->d_dep_w, ctx->d_plb, ctx->d_xfirst, ctx->d_xpair,
                   ctx->d_xq, ctx->d_za, ctx->d_vb, ctx->d_tcrows, ctx->d_zb, ctx->d_tckrows};
   for (void* b : bufs)
@@ -1362,6 +1380,12 @@ int mg_md_set_state(mg_ctx* ctx, const double* r, const double* r1) {
     ctx->hist_h = 0;
     ctx->aspc_kk = 0;
     ctx->cur_omega = ctx->scf_omega;
+  }
+  if (ctx->thermostat == 3) {
+    // Nose-Hoover from logs = 0 and h dlogs/dt = 0 with no predictor
+    // history (cook's k = 0 at the first step, sim/trvpscale.c:28)
+    CK(cudaMemsetAsync(ctx->d_nh, 0, sizeof(double) * (NH_HIST + MG_NOSE_MAXPRED),
+                       ctx->stream));
   }
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->have_state = true;
@@ -1945,6 +1969,18 @@ double mg_thermostat_factor(mg_ctx* ctx) {
   cudaMemcpyAsync(&z, ctx->d_zth, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
   cudaStreamSynchronize(ctx->stream);
   return z;
+}
+
+int mg_nose_state(mg_ctx* ctx, double state[3]) {
+  if (!ctx || !state) return fail(ctx, MG_ERR_ARG, "null argument");
+  if (ctx->thermostat != 3) return fail(ctx, MG_ERR_ARG, "no Nose-Hoover thermostat");
+  double h[NH_HIST];
+  CK(cudaMemcpyAsync(h, ctx->d_nh, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  state[0] = h[NH_LOGS];
+  state[1] = h[NH_LOGSV];
+  state[2] = h[NH_EXT];
+  return MG_OK;
 }
 
 int mg_set_overlap(mg_ctx* ctx, int on) {

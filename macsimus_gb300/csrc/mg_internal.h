@@ -209,8 +209,22 @@ struct ShakeArgs {
   // lowest massive-site coordinate is outside [r0, r0 + L) moves by L
   int normalize;
   double r0, Lb[3];
+  // Nose-Hoover (vhist != null): the friction displacement -Vfactor vpred
+  // joins the unconstrained positions; vpred and Vfactor come from the
+  // thermostat state nh (NoseSlot) and the history of r1 (nh_pred slots of
+  // nstride doubles), which the kernel shifts by one step
+  const double* nh;
+  double* vhist;
+  int nh_pred;
+  long long nstride;
 };
 cudaError_t k_shake(const Launch& L, const ShakeArgs& a);
+
+// Nose-Hoover thermostat state on the device: logs, h dlogs/dt, the
+// predictor length k reached so far, the extended energy of the last step,
+// then the history of h dlogs/dt (newest first)
+enum NoseSlot { NH_LOGS = 0, NH_LOGSV = 1, NH_K = 2, NH_EXT = 3, NH_HIST = 4 };
+constexpr int MG_NOSE_MAXPRED = 8;
 
 // Ewald exclusion corrections of the intramolecular pairs, one thread per
 // molecule (mixed cell path: the pair kernel skips these pairs)
@@ -296,13 +310,15 @@ struct WidomArgs {
 };
 // thermostat after SHAKE (mg_thermo.cu)
 struct ThermoArgs {
-  int kind;              // 1 Berendsen, 2 Bussi
+  int kind;              // 1 Berendsen, 2 Bussi, 3 Nose-Hoover
   int ns, nkin, nchi;    // sites, SHAKE kinetic partials, Bussi chi^2 partials
   double nf;             // degrees of freedom
   double T, tau, h;
   unsigned long long seed;
   long long* step;       // device step counter (Bussi stream), advanced per call
   double* zout;          // the factor of the step, or null
+  double* nh;            // Nose-Hoover state (NoseSlot), kind 3
+  int pred;              // Nose-Hoover predictor length
 };
 cudaError_t k_thermostat(const Launch& L, const ThermoArgs& a, const double* kin_part,
                          double* chi_part, double* r1);

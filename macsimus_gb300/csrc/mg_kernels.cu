@@ -1021,7 +1021,8 @@ cudaError_t k_reduce_sum(const Launch& L, const double* part, int nrows, int wid
 // -------------------------------------------------------------- SHAKE --
 
 // sim/constrd.c:767-839 + sim/verlet.c:101-104 + sim/shakev3.c (SHAKE=1,
-// VERLET=3, no thermostat), one thread per molecule, FP64.  The new
+// VERLET=3; Nose-Hoover's friction term of sim/verlet.c:22-37 when the
+// thermostat state is given), one thread per molecule, FP64.  The new
 // positions are then wrapped as cook's normalize(-1) does after the step
 // (sim/norm.c:415-444): the molecule's lowest coordinate over its massive
 // sites decides a shift of +L (below r0), -L (at or above r0 + L) or none.
@@ -1047,10 +1048,50 @@ __device__ __forceinline__ void sh_add(int k, double3& a, double3& b, double3& c
   else { c.x += s * x; c.y += s * y; c.z += s * z; }
 }
 
+// Nose-Hoover with Verlet + SHAKE (cook's T_NOSE): the time-reversible
+// velocity predictor of length k (sim/trvpscale.c:31-57; J. Chem. Theory
+// Comput. 7, 3596 (2011)), b_0 = (2k+1)/(k+1), b_{j+1} = -b_j (k-j)/(k+j+2),
+// predicts h v(t) = sum_j b_j r1(t - j h) for every degree of freedom and
+// Vfactor = h dlogs/dt from the history of logs; the step then adds
+// -Vfactor vpred to h^2 f/m (sim/verlet.c:22-37).  k grows by one per step
+// up to the predictor length.
+struct NoseStep {
+  double b[MG_NOSE_MAXPRED + 1];
+  double vf;
+  int k, knew;
+};
+
+__device__ __forceinline__ NoseStep nose_begin(const ShakeArgs& a) {
+  NoseStep q;
+  q.k = (int)a.nh[NH_K];
+  q.knew = min(a.nh_pred, q.k + 1);
+  q.b[0] = (double)(2 * q.k + 1) / (q.k + 1);
+  for (int j = 0; j < q.k; j++) q.b[j + 1] = -q.b[j] * (double)(q.k - j) / (q.k + j + 2);
+  q.vf = 0;
+  q.vf += q.b[0] * a.nh[NH_LOGSV];
+  for (int j = 1; j <= q.k; j++) q.vf += q.b[j] * a.nh[NH_HIST + j - 1];
+  return q;
+}
+
+// the friction displacement of degree of freedom t (r1 = its r1(t)); the
+// history moves one slot back and takes r1
+__device__ __forceinline__ double nose_dof(const ShakeArgs& a, const NoseStep& q, long long t,
+                                           double r1) {
+  double v = 0;
+  v += q.b[0] * r1;
+  for (int j = 1; j <= q.k; j++) v += q.b[j] * a.vhist[(j - 1) * a.nstride + t];
+  for (int j = q.knew - 1; j >= 1; j--) a.vhist[j * a.nstride + t] = a.vhist[(j - 1) * a.nstride + t];
+  if (q.knew > 0) a.vhist[t] = r1;
+  return -q.vf * v;
+}
+
+template <bool NOSE>
 __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
   __shared__ double red[SH_THREADS];
   const int n = blockIdx.x * SH_THREADS + threadIdx.x;
   double kin = 0;
+  [[maybe_unused]] NoseStep nose;
+  if constexpr (NOSE) nose = nose_begin(a);
   if (n < a.nmol) {
     const int i0 = a.mol_first[n], i1 = a.mol_first[n + 1];
     const int c0 = a.mol_cfirst[n], c1 = a.mol_cfirst[n + 1];
@@ -1062,9 +1103,18 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
         const int i = i0 + s;
         R[s] = make_double3(a.r[3 * i], a.r[3 * i + 1], a.r[3 * i + 2]);
         im[s] = a.imass[i];
-        P[s] = make_double3(a.f[3 * i] * (a.hh * im[s]) + R[s].x + a.r1[3 * i],
-                            a.f[3 * i + 1] * (a.hh * im[s]) + R[s].y + a.r1[3 * i + 1],
-                            a.f[3 * i + 2] * (a.hh * im[s]) + R[s].z + a.r1[3 * i + 2]);
+        if constexpr (NOSE) {
+          const double dx = nose_dof(a, nose, 3 * i, a.r1[3 * i]);
+          const double dy = nose_dof(a, nose, 3 * i + 1, a.r1[3 * i + 1]);
+          const double dz = nose_dof(a, nose, 3 * i + 2, a.r1[3 * i + 2]);
+          P[s] = make_double3(a.f[3 * i] * (a.hh * im[s]) + dx + R[s].x + a.r1[3 * i],
+                              a.f[3 * i + 1] * (a.hh * im[s]) + dy + R[s].y + a.r1[3 * i + 1],
+                              a.f[3 * i + 2] * (a.hh * im[s]) + dz + R[s].z + a.r1[3 * i + 2]);
+        } else {
+          P[s] = make_double3(a.f[3 * i] * (a.hh * im[s]) + R[s].x + a.r1[3 * i],
+                              a.f[3 * i + 1] * (a.hh * im[s]) + R[s].y + a.r1[3 * i + 1],
+                              a.f[3 * i + 2] * (a.hh * im[s]) + R[s].z + a.r1[3 * i + 2]);
+        }
       }
       int ci[3], cj[3];
       double bq[3], ibq[3], wq[3], rx[3], ry[3], rz[3], mi[3], mj[3];
@@ -1139,7 +1189,12 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
     double* p = a.p;
     for (int i = i0; i < i1; i++)
       for (int k = 0; k < 3; k++)
-        p[3 * i + k] = a.f[3 * i + k] * (a.hh * a.imass[i]) + a.r[3 * i + k] + a.r1[3 * i + k];
+        if constexpr (NOSE)
+          p[3 * i + k] = a.f[3 * i + k] * (a.hh * a.imass[i]) +
+                         nose_dof(a, nose, 3 * i + k, a.r1[3 * i + k]) + a.r[3 * i + k] +
+                         a.r1[3 * i + k];
+        else
+          p[3 * i + k] = a.f[3 * i + k] * (a.hh * a.imass[i]) + a.r[3 * i + k] + a.r1[3 * i + k];
     if (c1 > c0) {
       int it = 0;
       double maxsq;
@@ -1200,7 +1255,10 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
 }
 
 cudaError_t k_shake(const Launch& L, const ShakeArgs& a) {
-  shake_kernel<<<cdiv(a.nmol, SH_THREADS), SH_THREADS, 0, L.s>>>(a);
+  if (a.vhist)
+    shake_kernel<true><<<cdiv(a.nmol, SH_THREADS), SH_THREADS, 0, L.s>>>(a);
+  else
+    shake_kernel<false><<<cdiv(a.nmol, SH_THREADS), SH_THREADS, 0, L.s>>>(a);
   LAUNCHED(L);
   return cudaGetLastError();
 }

@@ -8,6 +8,13 @@
 //   Bussi      z = sqrt(e + c(1-e)(u1^2 + sum_{i<f} u_i^2) + 2 e sqrt(c(1-e)) u1),
 //              e = exp(-h/tau), c = T/(f En.T)     (sim/thermo.c:165-179)
 //
+//   Nose-Hoover (kind 3; cook's T_NOSE with Verlet + SHAKE): the friction
+//              term is in the SHAKE kernel; after the step
+//              h dlogs/dt += h^2 (En.T/T - 1)/tau^2, logs += h dlogs/dt and
+//              Eext = f T (logs_old + (tau/h)^2 (v_old^2 + v_new^2)/4)
+//              (sim/thermo.c:180-212, VERLET=3); the old h dlogs/dt enters
+//              the predictor history (sim/trvpscale.c)
+//
 // The Gaussian numbers of the Bussi thermostat come from a counter-based
 // stream (SplitMix64 output function of seed + (step * 2^40 + i + 1) * gamma,
 // Box-Muller on pairs), so that the draws of a step do not depend on the
@@ -90,12 +97,38 @@ __global__ void thermostat_scale_kernel(ThermoArgs a, const double* __restrict__
     r1[t] *= z;
 }
 
+// Nose-Hoover: one thread advances the thermostat state (NoseSlot) with the
+// kinetic energy of the step, summed in the order of thermostat_scale_kernel
+__global__ void nose_update_kernel(ThermoArgs a, const double* __restrict__ kin_part) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double k = 0;
+  for (int b = 0; b < a.nkin; b++) k += kin_part[b];
+  const double ET = k / (2 * a.h * a.h) / a.nf;
+  double* s = a.nh;
+  const int kk = (int)s[NH_K], knew = min(a.pred, kk + 1);
+  const double lo = s[NH_LOGS], ld = s[NH_LOGSV];
+  for (int j = knew - 1; j >= 1; j--) s[NH_HIST + j] = s[NH_HIST + j - 1];
+  if (knew > 0) s[NH_HIST] = ld;
+  const double lv = ld + a.h * a.h * (ET / a.T - 1) / (a.tau * a.tau);
+  const double th = a.tau / a.h;
+  s[NH_LOGSV] = lv;
+  s[NH_LOGS] = lo + lv;
+  s[NH_K] = knew;
+  s[NH_EXT] = a.nf * a.T * (lo + th * th * (ld * ld + lv * lv) / 4);
+  if (a.zout) *a.zout = 1;
+}
+
 // the step counter of the Bussi stream lives on the device (so that a
 // captured step replays with fresh draws)
 __global__ void step_increment_kernel(long long* step) { ++*step; }
 
 cudaError_t k_thermostat(const Launch& L, const ThermoArgs& a, const double* kin_part,
                          double* chi_part, double* r1) {
+  if (a.kind == 3) {
+    nose_update_kernel<<<1, 32, 0, L.s>>>(a, kin_part);
+    ++*L.counter;
+    return cudaGetLastError();
+  }
   if (a.kind == 2) {
     bussi_chi2_kernel<<<a.nchi, TH_THREADS, 0, L.s>>>((long long)a.nf, a.seed, a.step, chi_part);
     ++*L.counter;

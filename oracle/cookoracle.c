@@ -807,9 +807,11 @@ int orc_shake_step_dp(int ns, double *r, double *r1, const double *f, const doub
     double maxsq;
     for (i = i0; i < i1; i++)
       for (k = 0; k < 3; k++)
-        /* a massless site is a dependant, placed by depend_r after the step */
-        p[3 * i + k] = f[3 * i + k] * (mass[i] > 0 ? hh / mass[i] : 0) + r[3 * i + k] +
-                       r1[3 * i + k] + (dp ? dp[3 * i + k] : 0);
+        /* a massless site is a dependant, placed by depend_r after the step;
+           the friction term joins h^2 f/m before r and r1 are added, as in
+           sim/verlet.c:35-36 */
+        p[3 * i + k] = f[3 * i + k] * (mass[i] > 0 ? hh / mass[i] : 0) +
+                       (dp ? dp[3 * i + k] : 0) + r[3 * i + k] + r1[3 * i + k];
     if (nc > 0) {
       do {
         it++;

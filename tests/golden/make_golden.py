@@ -175,6 +175,61 @@ def run_case(name, c, keep=None):
     return dumps, meta
 
 
+# Energy-conservation runs: per-step Etot of cook's own integrator, read from
+# the table that cook prints every measurement cycle (noint=1: every step;
+# sim/maincps.c, columns t/ps Tkin/K Epot/K Etot/K).  The 864-water box of
+# the SPC/E configuration equilibrates from cook's crystal start under the
+# Berendsen thermostat (tau.T 0.1 ps, 1500 steps), then runs 5000 NVE steps.
+ENERGY_CASES = {
+    "nve864": dict(binary="cookewP1", species=["WAT"], N=[864], L=29.65, cutoff=12.0,
+                   alpha=0.26, kn=8, h=0.002, epsc=1e-10,
+                   sweeps=[dict(thermostat="Berendsen", tau_T=0.1, steps=1500),
+                           dict(thermostat="none", steps=5000)]),
+}
+
+
+def run_energy_case(name, c):
+    binary = os.path.join(REFBIN, c["binary"])
+    if not os.path.exists(binary):
+        raise SystemExit("missing %s: run oracle/build_ref.sh first" % binary)
+    wd = tempfile.mkdtemp(prefix="golden_")
+    with open(os.path.join(wd, "ff.ble"), "w") as f:
+        f.write(ble_text(c["species"]))
+    with open(os.path.join(wd, "sim.def"), "w") as f:
+        f.write(def_text(dict(c, steps=0)))
+    sw = []
+    for i, w in enumerate(c["sweeps"]):
+        lines = ['init="crystal"'] if i == 0 else []
+        lines.append('thermostat="%s"' % w["thermostat"])
+        if "tau_T" in w:
+            lines.append("tau.T=%g" % w["tau_T"])
+        lines += ["no=%d" % w["steps"], ";"]
+        sw.append("\n".join(lines))
+    with open(os.path.join(wd, "sim.get"), "w") as f:
+        f.write("\n".join(sw) + "\n")
+    env = dict(os.environ, NSLOTS=str(min(os.cpu_count() or 1, 16)))
+    p = subprocess.run([binary, "ff.ble", "sim"], cwd=wd, stdin=subprocess.DEVNULL, env=env,
+                       capture_output=True, text=True, timeout=3600)
+    if p.returncode != 0:
+        raise SystemExit("%s failed:\n%s" % (name, p.stdout[-3000:]))
+    rows = []
+    for line in open(os.path.join(wd, "sim.prt")):
+        m = re.match(r"\s+(\d+\.\d{3})\s+(\S+)\s+(-?\d+)\s+(-?\d+\.\d+)\s", line)
+        if m:
+            rows.append([float(m.group(k)) for k in (1, 2, 3, 4)])
+    a = np.array(rows)
+    nsteps = sum(w["steps"] for w in c["sweeps"])
+    assert a.shape[0] == nsteps, (a.shape, nsteps)
+    shutil.rmtree(wd)
+    n0 = c["sweeps"][0]["steps"]
+    # t of the first NVE step, then per step the printed Tkin (K) and Etot (K)
+    meta = dict(case=name, params=c, t0=a[n0, 0], Tkin=a[n0:, 1].tolist(),
+                Etot=a[n0:, 3].tolist())
+    with open(os.path.join(HERE, name + ".json"), "w") as f:
+        json.dump(meta, f, sort_keys=True)
+    print("wrote %s: %d NVE steps" % (name, len(meta["Etot"])))
+
+
 def save_case(name, dumps, meta):
     arrays = {}
     d0 = dumps[0]
@@ -198,8 +253,11 @@ def save_case(name, dumps, meta):
 
 
 def main(argv):
-    names = argv or list(CASES)
+    names = argv or list(CASES) + list(ENERGY_CASES)
     for n in names:
+        if n in ENERGY_CASES:
+            run_energy_case(n, ENERGY_CASES[n])
+            continue
         dumps, meta = run_case(n, CASES[n])
         save_case(n, dumps, meta)
 

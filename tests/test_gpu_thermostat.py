@@ -1,5 +1,6 @@
-"""Device thermostats (cook's Berendsen and Bussi, sim/thermo.c) against the
-oracle's step + factor, and their long-run temperatures."""
+"""Device thermostats (cook's Berendsen, Bussi and Nose-Hoover, sim/thermo.c)
+against the oracle's step + factor and cook's Nose-Hoover trajectory, and
+their long-run temperatures."""
 import numpy as np
 import pytest
 
@@ -64,3 +65,57 @@ def test_bussi_stream_is_reproducible():
         fp.md_steps(20, measure=False)
         out.append(fp.md_get_state()[1])
     assert np.array_equal(out[0], out[1])
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 5e-8), ("mixed", 2e-5)])
+def test_nose_hoover_matches_reference_trajectory(precision, tol):
+    """cook's Nose-Hoover Verlet+SHAKE (thermostat=2 in cook, tau.T 0.05 ps,
+    TRVP k -> 2) on the device: five steps from the state of cook's second
+    dump reproduce cook's dumped positions (FP64: the dumps' 12 printed
+    decimals; mixed: the force error times h^2/m) and the oracle's
+    thermostat variables"""
+    g, meta, system, ew = load("nose216")
+    h = meta["params"]["h"]
+    nf = 3 * system.ns - len(system.cons_len) - 3
+    r = g["r"][1].copy()
+    r1 = g["vlb_r"][0].astype(np.float64) * h
+    fp = fp_for(meta, system, ew, precision, thermostat="nose", T=298.0, tau_T=0.05)
+    fp.md_set_state(r, r1)
+    orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
+    nh = O.NoseHoover(298.0, 0.05, nf, h)
+    ro, r1o = r, r1
+    for step in range(5):
+        en = fp.md_steps(1)
+        f, _ = orc.forces(ro, measure=False, nthreads=4)
+        ro, r1o, it, ek = nh.step(orc, ro, r1o, f, omega=meta["omegac"] / 2)
+        rg, r1g = fp.md_get_state()
+        if step + 2 < g["r"].shape[0]:
+            assert np.abs(rg - g["r"][step + 2]).max() < tol, step
+        assert np.abs(rg - ro).max() < tol, step
+        logs, logsv, ext = fp.nose_state()
+        assert abs(logsv - nh.logsv) < 1e-6 * abs(nh.logsv) + (1e-12 if precision == "fp64"
+                                                               else 1e-9), step
+        assert abs(logs - nh.logs) < 1e-6 * abs(nh.logs) + 1e-9, step
+    assert abs(en["ekin"] / meta["Ekin_last"] - 1) < (1e-8 if precision == "fp64" else 1e-5)
+    assert abs(ext - nh.ext) < 1e-5 * abs(nh.ext) + 1e-3
+
+
+def test_nose_hoover_holds_the_temperature_and_conserves_its_energy():
+    """Nose-Hoover NVT from the 864-water lattice start: the temperature
+    relaxes to 298 K, and the extended energy Etot + Eext of cook's VERLET=3
+    form fluctuates far less than Etot itself while the thermostat moves
+    energy in and out"""
+    g, meta, system, ew = load("spce864")
+    nf = 3 * system.ns - len(system.cons_len) - 3
+    fp = fp_for(meta, system, ew, "mixed", thermostat="nose", T=298.0, tau_T=0.1)
+    fp.md_set_state(g["r"][1], g["r"][1] - g["r"][0])
+    fp.md_steps(1500, measure=False)
+    temps, ham, cons = [], [], []
+    for _ in range(100):
+        en = fp.md_steps(10)
+        ext = fp.nose_state()[2]
+        temps.append(2 * en["ekin"] / nf)
+        ham.append(en["el"] + en["lj"] + en["ekin"])
+        cons.append(ham[-1] + ext)
+    assert abs(np.mean(temps) / 298.0 - 1) < 0.03, temps[:5]
+    assert np.std(cons) < 0.2 * np.std(ham), (np.std(cons), np.std(ham))
