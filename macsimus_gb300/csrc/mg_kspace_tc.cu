@@ -310,7 +310,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) kf_tc_kernel(KfTc a) {
 //
 // S(row, +-kz) = sum_j a_j(row) Z_kz(j) with a_j(row) = q_j X_j(kx) Y_j(ky):
 // for 64 rows at a time, D[128 x KN] = A[128 x 32] Z^T[KN x 32]^T summed
-// over groups of 32 charges, A's lanes 2r and 2r+1 holding Re and Im of
+// over groups of 32 charges, A's lanes r and 64 + r holding Re and Im of
 // a_j(row r) and Z^T's rows [c(0..Kz), s(1..Kz)].  Per row
 //   P = (sum Re a c, sum Re a s),  Q = (sum Im a s, sum Im a c),
 //   S(+kz) = (P.x - Q.x, P.y + Q.y),  S(-kz) = (P.x + Q.x, Q.y - P.y),
@@ -423,14 +423,17 @@ __global__ void __launch_bounds__(SK_THREADS, 1) sk_tc_kernel(SkTc a) {
     }
     __syncwarp();
   } else {
-    // producers: thread = (row r, 8 charges of the group); the same warps
-    // drain the group sums from TMEM one group behind: warp w reads lanes
-    // 32 (w % 4) .., columns hc = KN/2 from (w / 4) hc
+    // producers: thread = (row r, 8 charges of the group), writing four
+    // charges per 16-byte store; a warp's 32 rows fall on 8 different
+    // 16-byte columns of the 8-row core matrices, so each store takes the
+    // minimum of four shared-memory wavefronts.  The same warps drain the
+    // group sums from TMEM one group behind: warp w reads lanes 32 (w % 4)
+    // .., columns hc = KN/2 from (w / 4) hc
     const int r = tid & (SK_R - 1), c0 = (tid >> 6) * 8;
     const KRow rw = rows[r];
     const bool valid = r0 + r < a.nrows;
     const int ox = rw.kx, oy = a.oyl + rw.ky;
-    const uint32_t oR = tc::kmajor_offset(2 * r, 0, SK_G), oI = tc::kmajor_offset(2 * r + 1, 0, SK_G);
+    const uint32_t oR = tc::kmajor_offset(r, 0, SK_G), oI = tc::kmajor_offset(SK_R + r, 0, SK_G);
     const int qd = warp & 3, hf = warp >> 2, hc = a.KN / 2;
     CSum acc[32];
     bool ok = true;
@@ -467,23 +470,28 @@ __global__ void __launch_bounds__(SK_THREADS, 1) sk_tc_kernel(SkTc a) {
       unsigned char* st = stage(s);
       const float2* tb = reinterpret_cast<const float2*>(st + abytes + zbytes);
 #pragma unroll
-      for (int c = 0; c < 8; c++) {
-        const int jj = c0 + c;
-        float re = 0.f, im = 0.f;
-        if (valid) {
-          const float2 X = tb[jj * a.row + ox], Y = tb[jj * a.row + oy];
-          re = X.x * Y.x - X.y * Y.y;
-          im = X.x * Y.y + X.y * Y.x;
+      for (int h = 0; h < 2; h++) {
+        float rh[4], rl[4], ih[4], il[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const int jj = c0 + 4 * h + c;
+          float re = 0.f, im = 0.f;
+          if (valid) {
+            const float2 X = tb[jj * a.row + ox], Y = tb[jj * a.row + oy];
+            re = X.x * Y.x - X.y * Y.y;
+            im = X.x * Y.y + X.y * Y.x;
+          }
+          tc::tf32_split(re, rh[c], rl[c]);
+          tc::tf32_split(im, ih[c], il[c]);
         }
-        float rh, rl, ih, il;
-        tc::tf32_split(re, rh, rl);
-        tc::tf32_split(im, ih, il);
-        // column jj of the K-major tile: chunk jj/4, element jj%4
-        const uint32_t ko = ((uint32_t)(jj >> 2) << 7) + ((uint32_t)(jj & 3) << 2);
-        *reinterpret_cast<float*>(st + oR + ko) = rh;
-        *reinterpret_cast<float*>(st + abytes / 2 + oR + ko) = rl;
-        *reinterpret_cast<float*>(st + oI + ko) = ih;
-        *reinterpret_cast<float*>(st + abytes / 2 + oI + ko) = il;
+        // columns c0+4h .. c0+4h+3 of the K-major tile: one 16-byte chunk
+        const uint32_t ko = (uint32_t)((c0 + 4 * h) >> 2) << 7;
+        *reinterpret_cast<float4*>(st + oR + ko) = make_float4(rh[0], rh[1], rh[2], rh[3]);
+        *reinterpret_cast<float4*>(st + abytes / 2 + oR + ko) =
+            make_float4(rl[0], rl[1], rl[2], rl[3]);
+        *reinterpret_cast<float4*>(st + oI + ko) = make_float4(ih[0], ih[1], ih[2], ih[3]);
+        *reinterpret_cast<float4*>(st + abytes / 2 + oI + ko) =
+            make_float4(il[0], il[1], il[2], il[3]);
       }
       tc::fence_async_smem();
       __syncwarp();
@@ -493,7 +501,7 @@ __global__ void __launch_bounds__(SK_THREADS, 1) sk_tc_kernel(SkTc a) {
     if (ok && ng > 0) ok = drain(ng - 1);
     if (!ok && lane == 0) atomicOr(a.status, 16);
     // the row sums, in FP64, through the first stage (no product or copy is
-    // pending any more): D row m = 2r + (Re | Im)
+    // pending any more): D row m = r (Re) or 64 + r (Im)
     double* Dsm = reinterpret_cast<double*>(stage(0));
     const int m = 32 * qd + lane;
     tc::named_sync(1, 32 * SK_PW);
@@ -501,11 +509,10 @@ __global__ void __launch_bounds__(SK_THREADS, 1) sk_tc_kernel(SkTc a) {
     for (int c = 0; c < 32; c++)
       if (c < hc) Dsm[m * 64 + hf * hc + c] = acc[c].value();
     tc::named_sync(1, 32 * SK_PW);
-    if (warp < 4 && ok && !(m & 1) && ng > 0) {
-      const int rl = m >> 1;
-      const KRow w = rows[rl];
+    if (warp < 2 && ok && ng > 0) {
+      const KRow w = rows[m];
       const double* re = Dsm + m * 64;
-      const double* im = Dsm + (m + 1) * 64;
+      const double* im = Dsm + (m + SK_R) * 64;
       float2* out = a.part + (size_t)ch * a.nk;
       for (int kz = 0; kz <= a.Kz; kz++) {
         const double Px = re[kz], Qy = im[kz];
