@@ -39,10 +39,13 @@ constexpr int TC_EPI_WARPS = 16;      // four per TMEM lane quarter
 constexpr int TC_EPI_ROWS = TC_ROWS / (TC_EPI_WARPS / 4);   // rows per warp and tile
 constexpr int TC_THREADS = 32 * (TC_EPI_WARPS + 1);
 constexpr int SK_G = 32;              // pass 1: charges per pipeline stage
-constexpr int SK_PW = 8;              // pass 1: producer warps
+constexpr int SK_PW = 16;             // pass 1: producer warps
 constexpr int SK_THREADS = 32 * (SK_PW + 1);
 constexpr int SK_R = 64;              // pass 1: k rows per tile (re and im: 128 lanes)
 constexpr int SK_NS = 3;              // pass 1: pipeline stages
+static_assert(SK_PW == 16, "pass-1 drain: four warps per TMEM lane quarter");
+constexpr int SK_CPT = SK_G * SK_R / (32 * SK_PW);   // pass 1: charges per producer thread
+static_assert(SK_CPT % 4 == 0, "pass-1 producers store whole 16-byte chunks");
 
 // A tiles, one per 128 charges: z_j (hi, then lo, K-major layout), then the
 // charges' phase values X(0..Kx) | Y(-Ky..Ky) transposed ([e][128] float2)
@@ -315,7 +318,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) kf_tc_kernel(KfTc a) {
 //   P = (sum Re a c, sum Re a s),  Q = (sum Im a s, sum Im a c),
 //   S(+kz) = (P.x - Q.x, P.y + Q.y),  S(-kz) = (P.x + Q.x, Q.y - P.y),
 // the +-kz symmetry of the FP32-core kernel.  A is formed in shared memory
-// by eight warps from the charges' phase rows (bulk-copied per group with the
+// by sixteen warps from the charges' phase rows (bulk-copied per group with the
 // Z^T tile), split hi + lo like the operands of pass 2, and multiplied in
 // TF32 as three products.  CTA (row tile, charge chunk); the chunk's partial
 // S go to part[chunk][k], summed in FP64 by the reduce kernel.
@@ -423,19 +426,20 @@ __global__ void __launch_bounds__(SK_THREADS, 1) sk_tc_kernel(SkTc a) {
     }
     __syncwarp();
   } else {
-    // producers: thread = (row r, 8 charges of the group), writing four
+    // producers: thread = (row r, 4 charges of the group), writing four
     // charges per 16-byte store; a warp's 32 rows fall on 8 different
     // 16-byte columns of the 8-row core matrices, so each store takes the
     // minimum of four shared-memory wavefronts.  The same warps drain the
     // group sums from TMEM one group behind: warp w reads lanes 32 (w % 4)
-    // .., columns hc = KN/2 from (w / 4) hc
-    const int r = tid & (SK_R - 1), c0 = (tid >> 6) * 8;
+    // .. and the 8-column chunks w / 4 and w / 4 + 4 of the KN columns
+    const int r = tid & (SK_R - 1), c0 = (tid >> 6) * SK_CPT;
     const KRow rw = rows[r];
     const bool valid = r0 + r < a.nrows;
     const int ox = rw.kx, oy = a.oyl + rw.ky;
     const uint32_t oR = tc::kmajor_offset(r, 0, SK_G), oI = tc::kmajor_offset(SK_R + r, 0, SK_G);
-    const int qd = warp & 3, hf = warp >> 2, hc = a.KN / 2;
-    CSum acc[32];
+    const int qd = warp & 3, hf = warp >> 2;
+    const bool ch1 = 8 * (hf + 4) < a.KN;   // second chunk present (KN > 32)
+    CSum acc[16];
     bool ok = true;
     auto drain = [&](int i) {
       const int b = i & 1;
@@ -443,21 +447,20 @@ __global__ void __launch_bounds__(SK_THREADS, 1) sk_tc_kernel(SkTc a) {
       w = __all_sync(0xffffffffu, w);
       if (!w) return false;
       tc::fence_after_sync();
-      uint32_t v[4][8];
-      const uint32_t ta = tbase + ((uint32_t)(32 * qd) << 16) + 64u * b + (uint32_t)(hf * hc);
-#pragma unroll
-      for (int c = 0; c < 4; c++)
-        if (8 * c < hc) tc::tmem_ld8_async(ta + 8 * c, v[c]);
+      uint32_t v[2][8];
+      const uint32_t ta = tbase + ((uint32_t)(32 * qd) << 16) + 64u * b + (uint32_t)(8 * hf);
+      tc::tmem_ld8_async(ta, v[0]);
+      if (ch1) tc::tmem_ld8_async(ta + 32, v[1]);
       tc::tmem_wait8(v[0]);
       tc::tmem_regs_after_wait8(v[1]);
-      tc::tmem_regs_after_wait8(v[2]);
-      tc::tmem_regs_after_wait8(v[3]);
       tc::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(tfree + b);
 #pragma unroll
-      for (int c = 0; c < 32; c++)
-        if (c < hc) acc[c].add(__uint_as_float(v[c >> 3][c & 7]));
+      for (int c = 0; c < 8; c++) acc[c].add(__uint_as_float(v[0][c]));
+      if (ch1)
+#pragma unroll
+        for (int c = 0; c < 8; c++) acc[8 + c].add(__uint_as_float(v[1][c]));
       return true;
     };
     for (int i = 0; ok && i < ng; i++) {
@@ -470,7 +473,7 @@ __global__ void __launch_bounds__(SK_THREADS, 1) sk_tc_kernel(SkTc a) {
       unsigned char* st = stage(s);
       const float2* tb = reinterpret_cast<const float2*>(st + abytes + zbytes);
 #pragma unroll
-      for (int h = 0; h < 2; h++) {
+      for (int h = 0; h < SK_CPT / 4; h++) {
         float rh[4], rl[4], ih[4], il[4];
 #pragma unroll
         for (int c = 0; c < 4; c++) {
@@ -506,8 +509,10 @@ __global__ void __launch_bounds__(SK_THREADS, 1) sk_tc_kernel(SkTc a) {
     const int m = 32 * qd + lane;
     tc::named_sync(1, 32 * SK_PW);
 #pragma unroll
-    for (int c = 0; c < 32; c++)
-      if (c < hc) Dsm[m * 64 + hf * hc + c] = acc[c].value();
+    for (int c = 0; c < 8; c++) {
+      Dsm[m * 64 + 8 * hf + c] = acc[c].value();
+      if (ch1) Dsm[m * 64 + 8 * (hf + 4) + c] = acc[8 + c].value();
+    }
     tc::named_sync(1, 32 * SK_PW);
     if (warp < 2 && ok && ng > 0) {
       const KRow w = rows[m];
