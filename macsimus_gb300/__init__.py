@@ -155,9 +155,9 @@ def library():
 def autotune(system, L, cutoff, alpha, kappa, r, nrep=3, **kw):
     """the fastest (cells_per_cutoff, kspace_ctas_per_sm, pair_variant) for
     this box and configuration (mg_autotune), with the timings (3x3 grid x
-    split, then the 4 pair variants)"""
+    split, then the 8 pair variants)"""
     t, p, keep = describe(system, L, cutoff, alpha, kappa, **kw)
-    ms = np.zeros(13)
+    ms = np.zeros(17)
     rr = _arr(r, np.float64).reshape(-1)
     rc = library().mg_autotune(C.byref(t), C.byref(p), rr.ctypes.data_as(_dp), int(nrep),
                                ms.ctypes.data_as(_dp))

@@ -911,7 +911,7 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
   pa.ntab = ctx->ntab;
   pa.pdj = ctx->d_pdj;
   pa.pdd = ctx->d_pdd;
-  pa.pair_warps = (ctx->pair_variant & 1) ? 8 : 4;
+  pa.pair_warps = (ctx->pair_variant & 4) ? 16 : ((ctx->pair_variant & 1) ? 8 : 4);
   pa.spline_smem = (ctx->pair_variant & 2) && ctx->ntab * 16 <= 200 * 1024 ? 1 : 0;
   KArgs ka;
   ka.nq = ctx->nq;
@@ -2325,7 +2325,7 @@ int mg_autotune(const mg_topology* top, mg_params* par, const double* r, int nre
   int bv = par->pair_variant;
   if (!rc && bc) {
     double bestv = 1e300;
-    for (int v = 0; v < 4 && rc == MG_OK; v++) {
+    for (int v = 0; v < 8 && rc == MG_OK; v++) {
       mg_params p2 = *par;
       p2.cells_per_cutoff = bc;
       p2.kspace_ctas_per_sm = bk;

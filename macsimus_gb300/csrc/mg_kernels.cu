@@ -149,7 +149,9 @@ constexpr int FOLD = 8;   // stencil cells per FP32 force batch before the FP64 
 // box of the home-cell centre, so the image taken is the nearest one for
 // every pair inside the cutoff.  Without REL (one cell: all pairs) each pair
 // takes its nearest image from its own fixed-point difference.
-// NW warps per CTA (the autotuner picks 4 or 8); STAB: the force spline in
+// NW warps per CTA (the autotuner picks 4, 8 or 16: more warps per home
+// cell finish a cell sooner, which shortens the tail of the grid); STAB: the
+// force spline in
 // shared memory (dynamic, ntab float4) instead of read through L1.
 // Intramolecular pairs are skipped: their Ewald exclusion terms come from
 // excl_mixed_kernel, once per pair.  Forces are summed in FP32 per batch of
@@ -372,7 +374,7 @@ cudaError_t k_pair_mixed(const Launch& L, const PairArgs& a, const int4* pj, con
         sz = (float)(a.Lz / 4294967296.0);
   const float cq = (float)a.cutoff_sq, sg = (float)a.sgrid, al = (float)a.alpha;
   const bool rel = !a.allpairs;
-  const int nw = a.pair_warps == 8 ? 8 : 4;
+  const int nw = a.pair_warps == 16 ? 16 : (a.pair_warps == 8 ? 8 : 4);
   const bool stab = a.spline_smem && !measure;
   const size_t dsm = sizeof(PairFS) * (size_t)a.nkind * a.nkind +
                      (stab ? sizeof(float4) * (size_t)a.ntab : 0);
@@ -388,7 +390,10 @@ cudaError_t k_pair_mixed(const Launch& L, const PairArgs& a, const int4* pj, con
   } while (0)
 #define PAIR_MIXED_W(M, P, R)                              \
   do {                                                     \
-    if (nw == 8) {                                         \
+    if (nw == 16) {                                        \
+      if (stab) PAIR_MIXED(M, P, R, 16, true);             \
+      else PAIR_MIXED(M, P, R, 16, false);                 \
+    } else if (nw == 8) {                                  \
       if (stab) PAIR_MIXED(M, P, R, 8, true);              \
       else PAIR_MIXED(M, P, R, 8, false);                  \
     } else {                                               \

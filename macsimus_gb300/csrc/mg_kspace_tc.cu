@@ -44,6 +44,7 @@ constexpr int SK_THREADS = 32 * (SK_PW + 1);
 constexpr int SK_R = 64;              // pass 1: k rows per tile (re and im: 128 lanes)
 constexpr int SK_NS = 3;              // pass 1: pipeline stages
 static_assert(SK_PW == 16, "pass-1 drain: four warps per TMEM lane quarter");
+constexpr int SK_FOLD = 8;            // pass 1: group sums per compensated add
 constexpr int SK_CPT = SK_G * SK_R / (32 * SK_PW);   // pass 1: charges per producer thread
 static_assert(SK_CPT % 4 == 0, "pass-1 producers store whole 16-byte chunks");
 
@@ -439,7 +440,12 @@ __global__ void __launch_bounds__(SK_THREADS, 1) sk_tc_kernel(SkTc a) {
     const uint32_t oR = tc::kmajor_offset(r, 0, SK_G), oI = tc::kmajor_offset(SK_R + r, 0, SK_G);
     const int qd = warp & 3, hf = warp >> 2;
     const bool ch1 = 8 * (hf + 4) < a.KN;   // second chunk present (KN > 32)
+    // group sums: plain FP32 over SK_FOLD groups (rounded to nearest, so
+    // unbiased), then into compensated sums
     CSum acc[16];
+    float pend[16];
+#pragma unroll
+    for (int c = 0; c < 16; c++) pend[c] = 0.f;
     bool ok = true;
     auto drain = [&](int i) {
       const int b = i & 1;
@@ -457,10 +463,17 @@ __global__ void __launch_bounds__(SK_THREADS, 1) sk_tc_kernel(SkTc a) {
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(tfree + b);
 #pragma unroll
-      for (int c = 0; c < 8; c++) acc[c].add(__uint_as_float(v[0][c]));
+      for (int c = 0; c < 8; c++) pend[c] += __uint_as_float(v[0][c]);
       if (ch1)
 #pragma unroll
-        for (int c = 0; c < 8; c++) acc[8 + c].add(__uint_as_float(v[1][c]));
+        for (int c = 0; c < 8; c++) pend[8 + c] += __uint_as_float(v[1][c]);
+      if ((i & (SK_FOLD - 1)) == SK_FOLD - 1 || i == ng - 1) {
+#pragma unroll
+        for (int c = 0; c < 16; c++) {
+          acc[c].add(pend[c]);
+          pend[c] = 0.f;
+        }
+      }
       return true;
     };
     for (int i = 0; ok && i < ng; i++) {
