@@ -299,6 +299,7 @@ class ForcePath:
             raise MGError(st.value, "mg_create failed")
         self._owned = True
         self.precision = precision
+        self.thermostat = p.thermostat
         self.L = np.array(Lb)
         self.kappa = lib.mg_kappa(self._ctx)
         self.nkvec = lib.mg_nkvec(self._ctx)
@@ -395,6 +396,28 @@ class ForcePath:
         self._check(library().mg_md_get_state(self._ctx, r.ctypes.data_as(_dp),
                                               r1.ctypes.data_as(_dp)))
         return r.reshape(-1, 3), r1.reshape(-1, 3)
+
+    def md_load_cfg(self, path):
+        """MD state from cook's SIMNAME.cfg (loadcfg, sim/simils.c:1150):
+        cfg[0] = r(t), cfg[1] = r(t) - r(t-h); returns the parsed file"""
+        from . import cfgfile
+        c = cfgfile.read_cfg(path)
+        if c["polar"] != self.polar:
+            raise cfgfile.CfgError("POLAR file for a non-polar box or the reverse")
+        r, r1 = cfgfile.state_from_cfg(c, self.ns)
+        self.md_set_state(r, r1)
+        return c
+
+    def md_save_cfg(self, path, template, t=None, Etot=None):
+        """the device MD state as cook's SIMNAME.cfg (savecfg,
+        sim/simils.c:1445); the other records (options, species, box,
+        thermostat) come from template, a parsed .cfg of the same system;
+        a Nose-Hoover context also writes logs and h dlogs/dt"""
+        from . import cfgfile
+        r, r1 = self.md_get_state()
+        nose = self.nose_state()[:2] if getattr(self, "thermostat", 0) == 3 else None
+        cfgfile.write_cfg(path, cfgfile.cfg_with_state(template, r, r1, t=t, Etot=Etot,
+                                                       nose=nose))
 
     def xwidom(self, mols, vtype, vcharge, T, energies=False):
         """cook's XWidom identity change of the listed molecules into sites of

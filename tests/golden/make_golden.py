@@ -230,6 +230,62 @@ def run_energy_case(name, c):
     print("wrote %s: %d NVE steps" % (name, len(meta["Etot"])))
 
 
+# Resume parity through cook's .cfg files (sim/simils.c savecfg/loadcfg):
+# run A from cook's crystal start writes sim.cfg; run B continues from that
+# file (init="cont"); run C continues from a file that
+# macsimus_gb300.cfgfile writes: A's state with r1 = r(t) - r(t-h) scaled by
+# c["r1_scale"].  Stored: A's file as it is, the final cfg[0] / cfg[1] of B
+# and C, and the SHA-256 of the file written for C.
+RESUME_CASES = {
+    "resume216": dict(binary="cookew", species=["WAT"], N=[216], L=18.6206, cutoff=9.0,
+                      alpha=0.35, kn=6, h=0.002, epsc=1e-10, steps_a=4, steps_b=3,
+                      r1_scale=0.5),
+}
+
+
+def run_resume_case(name, c):
+    import hashlib
+    from macsimus_gb300 import cfgfile
+    binary = os.path.join(REFBIN, c["binary"])
+    if not os.path.exists(binary):
+        raise SystemExit("missing %s: run oracle/build_ref.sh first" % binary)
+    wd = tempfile.mkdtemp(prefix="golden_")
+    with open(os.path.join(wd, "ff.ble"), "w") as f:
+        f.write(ble_text(c["species"]))
+    with open(os.path.join(wd, "sim.def"), "w") as f:
+        f.write(def_text(dict(c, steps=0)))
+
+    def run(init, steps):
+        with open(os.path.join(wd, "sim.get"), "w") as f:
+            f.write('init="%s"\nno=%d\n;\n' % (init, steps))
+        p = subprocess.run([binary, "ff.ble", "sim"], cwd=wd, stdin=subprocess.DEVNULL,
+                           capture_output=True, text=True, timeout=600)
+        if p.returncode != 0:
+            raise SystemExit("%s failed:\n%s" % (name, p.stdout[-3000:]))
+        return cfgfile.read_cfg(os.path.join(wd, "sim.cfg"))
+
+    run("crystal", c["steps_a"])
+    a_bytes = open(os.path.join(wd, "sim.cfg"), "rb").read()
+    with open(os.path.join(HERE, name + "_a.cfg"), "wb") as f:
+        f.write(a_bytes)
+    b = run("cont", c["steps_b"])
+    a = cfgfile.read_cfg(os.path.join(HERE, name + "_a.cfg"))
+    r, r1 = a["cfg"][0]["rp"], a["cfg"][1]["rp"]
+    w = cfgfile.cfg_with_state(a, r, r1 * c["r1_scale"])
+    cfgfile.write_cfg(os.path.join(wd, "sim.cfg"), w)
+    sha = hashlib.sha256(open(os.path.join(wd, "sim.cfg"), "rb").read()).hexdigest()
+    cc = run("cont", c["steps_b"])
+    shutil.rmtree(wd)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"),
+                        rB=b["cfg"][0]["rp"], r1B=b["cfg"][1]["rp"],
+                        rC=cc["cfg"][0]["rp"], r1C=cc["cfg"][1]["rp"])
+    meta = dict(case=name, params=c, sha256_written=sha, tB=b["t"], tC=cc["t"],
+                omegac=None)
+    with open(os.path.join(HERE, name + ".json"), "w") as f:
+        json.dump(meta, f, indent=1, sort_keys=True)
+    print("wrote %s" % name)
+
+
 def save_case(name, dumps, meta):
     arrays = {}
     d0 = dumps[0]
@@ -253,10 +309,13 @@ def save_case(name, dumps, meta):
 
 
 def main(argv):
-    names = argv or list(CASES) + list(ENERGY_CASES)
+    names = argv or list(CASES) + list(ENERGY_CASES) + list(RESUME_CASES)
     for n in names:
         if n in ENERGY_CASES:
             run_energy_case(n, ENERGY_CASES[n])
+            continue
+        if n in RESUME_CASES:
+            run_resume_case(n, RESUME_CASES[n])
             continue
         dumps, meta = run_case(n, CASES[n])
         save_case(n, dumps, meta)
