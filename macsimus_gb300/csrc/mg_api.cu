@@ -383,8 +383,17 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   erfc_table(grid, p->cutoff + rplus, p->cutoff, p->alpha, p->rshift, &ert, &ctx->sgrid);
   int ntab = (int)(ert.size() / 6);
 
-  // ---- cells: size >= cutoff/cdiv and at least 2*cdiv+1 cells per edge
-  int cdivv = p->cells_per_cutoff > 0 ? p->cells_per_cutoff : 2;
+  // ---- cells: size >= cutoff/cdiv and at least 2*cdiv+1 cells per edge.
+  // Automatic cdiv: about 24 sites per cell (a warp's lanes own the sites of
+  // a home cell), i.e. cdiv = cutoff (rho/24)^(1/3): 2 for water at a 10-12 A
+  // cutoff, 1 for dilute ionic fluids
+  int cdivv = p->cells_per_cutoff;
+  if (cdivv <= 0) {
+    const double rho = ns / (p->L[0] * p->L[1] * p->L[2]);
+    cdivv = (int)std::lround((ctx->use_list ? p->cutoff + ctx->skin : p->cutoff) *
+                             std::cbrt(rho / 24.0));
+    cdivv = std::max(1, std::min(cdivv, 3));
+  }
   // cells cover the list radius cutoff+skin (or the cutoff without lists)
   const double rgrid = ctx->use_list ? p->cutoff + ctx->skin : p->cutoff;
   int nc3[3] = {1, 1, 1};
