@@ -151,7 +151,7 @@ def run_ours(args, rank, world, local):
         torch.cuda.synchronize()
 
     kw = dict(h=w["h"], epsc=1e-7, aspc_k=w["aspc_k"], scf_iter=w["scf_iter"], skin=args.skin,
-              kspace_engine=args.kspace_engine)
+              kspace_engine=args.kspace_engine or 0)
     # the autotuner picks the cell subdivision and the Ewald pass-1 split on
     # this configuration (untimed)
     tuned = {}
@@ -306,7 +306,7 @@ def run_ours(args, rank, world, local):
                                         1: "both passes FP32 cores",
                                         2: "pass 1 FP32 cores, pass 2 tensor cores (tcgen05 TF32x3)",
                                         3: "both passes tensor cores (tcgen05 TF32x3)"}[
-                                            args.kspace_engine]},
+                                            args.kspace_engine or 0]},
             "atom_steps_per_s": round(atom_steps, 1),
             "fp64_path": {"value": round(value64, 4), "unit": "ns/day", "steps": k64},
             "mixed_over_fp64": round(value / value64, 3),
@@ -366,9 +366,12 @@ def run_batch(args, rank, world, local):
             dist.barrier()
         torch.cuda.synchronize()
 
+    engine = 1 if args.kspace_engine is None else args.kspace_engine
+
     def make(precision):
         return M.Batch([dict(system=b["system"], L=b["L"], cutoff=b["cutoff"], alpha=b["alpha"],
-                             kappa=b["kappa"], h=b["h"]) for b in boxes], precision=precision)
+                             kappa=b["kappa"], h=b["h"], kspace_engine=engine) for b in boxes],
+                       precision=precision)
 
     bm = make("mixed")
     # relax the lattice starts: velocity rescaling to 298 K every 10 steps
@@ -465,6 +468,8 @@ def run_batch(args, rank, world, local):
                                    "all), per-box Ewald, leap-frog dt 2 fs; Widom 1e5 "
                                    "insertions per box" % (nbox, sum(b["system"].ns for b in allb)),
                        "boxes_on_rank0": len(boxes),
+                       "ewald_kspace": {0: "tensor cores where the tiles fit", 1: "FP32 cores",
+                                        2: "pass 2 on tensor cores", 3: "tensor cores"}[engine],
                        "l2": "inputs larger than L2 (per-step working set > 129 MB)"},
             "atom_steps_per_s": round(world * nsite * args.steps / (ms * 1e-3), 1),
             "fp64_path": {"value": round(value64, 4), "unit": "ns/day", "steps": k64},
@@ -534,9 +539,11 @@ def main():
     ap.add_argument("--ref-budget", type=float, default=150.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--kspace-engine", type=int, default=0,
+    ap.add_argument("--kspace-engine", type=int, default=None,
                     help="Ewald engine of the FP32 path: 0 tensor cores where they fit, 1 FP32 "
-                         "cores, 2 tensor-core pass 2 only, 3 tensor cores for both passes")
+                         "cores, 2 tensor-core pass 2 only, 3 tensor cores for both passes "
+                         "(default: 0 for one box; 1 for batches of small boxes, measured "
+                         "faster when many boxes share the GPU)")
     ap.add_argument("--skin", type=float, default=0.0,
                     help="> 0: Verlet lists of cutoff+skin instead of cells re-binned every step")
     ap.add_argument("--equilibrate", type=int, default=400,
