@@ -285,10 +285,15 @@ def run_ours(args, rank, world, local):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "fp32+fp64acc", "data": "synthetic (seeded fcc lattice, random orientations, %d relaxation steps of "
                     "rigid SPC/E at 1 fs with velocity rescaling to 298 K)" % args.equilibrate,
-            "config": {"workload": "%d %s waters (%d sites%s), L=%.3f A, cutoff %.0f A, "
+            "config": {"workload": "%s (%d sites%s), L=%.3f A, cutoff %.0f A, "
                                    "alpha %.2f/A, |n|<=%d (%d k-vectors), leap-frog+SHAKE "
                                    "dt %.0f fs%s" % (
-                                       system.nmol, "Drude" if system.polar else "SPC/E", ns,
+                                       " + ".join("%d %s" % (n, {"WAT": "SPC/E waters",
+                                                                 "WATD": "Drude waters",
+                                                                 "NA": "Na+", "CL": "Cl-"}
+                                                             .get(sp, sp))
+                                                  for sp, n in zip(system.species,
+                                                                   system.counts)), ns,
                                        " + %d Drude shells" % int((system.qpol != 0).sum())
                                        if system.polar else "", w["L"], w["cutoff"], w["alpha"],
                                        w["kn"], fp.nkvec, w["h"] * 1000,
