@@ -50,42 +50,57 @@ static_assert(SK_CPT % 4 == 0, "pass-1 producers store whole 16-byte chunks");
 
 // A tiles, one per 128 charges: z_j (hi, then lo, K-major layout), then the
 // charges' phase values X(0..Kx) | Y(-Ky..Ky) transposed ([e][128] float2)
-// for the epilogue; tile stride 256 (KP + nxy) floats
-__global__ void kf_tc_prep_kernel(int nq, int ntm, int row, int oz, int Kz, int KP, int nxy,
-                                  int KN, const float2* __restrict__ tab, float* __restrict__ za,
-                                  float* __restrict__ zb) {
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long nz = (long)ntm * TC_M * KP;
+// for the epilogue; tile stride 256 (KP + nxy) floats.  With zb, also the
+// pass-1 Z^T tiles (per 32 charges, rows kk of z_j, K = the charges).  One
+// CTA per group of 32 charges: the group's phase rows are read once,
+// coalesced, into shared memory; every warp store then writes a whole
+// 128-byte core matrix (8 rows x 4 values) or 256 contiguous bytes of the
+// phase block.  Charges at or beyond nq and rows beyond 2 Kz are zero.
+__global__ void __launch_bounds__(256) kf_tc_prep_kernel(int nq, int row, int oz, int Kz, int KP,
+                                                         int nxy, int KN,
+                                                         const float2* __restrict__ tab,
+                                                         float* __restrict__ za,
+                                                         float* __restrict__ zb) {
+  extern __shared__ float2 st_prep[];   // [32][row]
+  const int g = blockIdx.x, j0 = g * SK_G;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nvalid = min(SK_G, max(0, nq - j0));
+  for (int t = tid; t < SK_G * row; t += 256)
+    st_prep[t] = t / row < nvalid ? tab[(long)j0 * row + t] : make_float2(0.f, 0.f);
+  __syncthreads();
+  // component kk of z_j = [c(0..Kz), s(1..Kz)] of charge c of the group
+  auto zval = [&](int c, int kk) -> float {
+    const float2* zr = st_prep + c * row + oz;
+    return kk <= Kz ? zr[kk].x : (kk <= 2 * Kz ? zr[kk - Kz].y : 0.f);
+  };
+  const int r = lane & 7, cc = lane >> 3;   // row and 4-byte column inside a core matrix
+  const int m0 = SK_G * (g % (TC_M / SK_G));  // first row of the group in its 128-charge tile
   const size_t tile_f = (size_t)2 * TC_M * (KP + nxy);
-  if (t < nz) {
-    const int j = (int)(t / KP), kk = (int)(t % KP);
-    float v = 0.f;
-    if (j < nq) {
-      const float2* zr = tab + (long)j * row + oz;   // Z(0..Kz)
-      if (kk <= Kz) v = zr[kk].x;
-      else if (kk <= 2 * Kz) v = zr[kk - Kz].y;
-    }
+  float* base = za + (size_t)(g / (TC_M / SK_G)) * tile_f;
+  for (int q = warp; q < (SK_G / 8) * (KP / 4); q += 8) {
+    const int c = 8 * (q / (KP / 4)) + r, kk = 4 * (q % (KP / 4)) + cc;
     float hi, lo;
-    tc::tf32_split(v, hi, lo);
-    float* base = za + (size_t)(j / TC_M) * tile_f;
-    const uint32_t o = tc::kmajor_offset(j % TC_M, kk, KP) >> 2;
+    tc::tf32_split(zval(c, kk), hi, lo);
+    const uint32_t o = tc::kmajor_offset(m0 + c, kk, KP) >> 2;
     base[o] = hi;
     base[(size_t)TC_M * KP + o] = lo;
-    if (zb) {
-      // pass 1: Z^T per 32 charges, rows kk (KN of them), K = the charges
-      float* zt = zb + (size_t)(j / SK_G) * 2 * SK_G * KN;
-      const uint32_t oz2 = tc::kmajor_offset(kk, j % SK_G, SK_G) >> 2;
-      zt[oz2] = hi;
-      zt[(size_t)SK_G * KN + oz2] = lo;
-    }
-    return;
   }
-  const long u = t - nz;
-  if (u >= (long)ntm * nxy * TC_M) return;
-  const int tm = (int)(u / ((long)nxy * TC_M)), e = (int)(u / TC_M % nxy), m = (int)(u % TC_M);
-  const int j = tm * TC_M + m;
-  float2* xy = reinterpret_cast<float2*>(za + (size_t)tm * tile_f + (size_t)2 * TC_M * KP);
-  xy[(size_t)e * TC_M + m] = j < nq ? tab[(long)j * row + e] : make_float2(0.f, 0.f);
+  if (zb) {
+    float* zt = zb + (size_t)g * 2 * SK_G * KN;
+    for (int q = warp; q < (KN / 8) * (SK_G / 4); q += 8) {
+      const int kk = 8 * (q / (SK_G / 4)) + r, c = 4 * (q % (SK_G / 4)) + cc;
+      float hi, lo;
+      tc::tf32_split(zval(c, kk), hi, lo);
+      const uint32_t o = tc::kmajor_offset(kk, c, SK_G) >> 2;
+      zt[o] = hi;
+      zt[(size_t)SK_G * KN + o] = lo;
+    }
+  }
+  float2* xy = reinterpret_cast<float2*>(base + (size_t)2 * TC_M * KP);
+  for (int t = tid; t < nxy * SK_G; t += 256) {
+    const int e = t / SK_G, c = t % SK_G;
+    xy[(size_t)e * TC_M + m0 + c] = st_prep[c * row + e];
+  }
 }
 
 // B operand: per row r the columns 4r .. 4r+3 = coefficients of H.x, H.y,
@@ -231,22 +246,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1) kf_tc_kernel(KfTc a) {
     CSum Fx, Fy, Fz;
     int cur_ox = -1;
     float2 X = make_float2(0.f, 0.f);
-    for (int t = 0; ok && t < a.ntn; t++) {
-      const int s = t & 1;
-      ok = tc::mbar_wait(tfull + s, (t >> 1) & 1, TC_WAIT);
-      ok = __all_sync(0xffffffffu, ok);
-      if (!ok) break;
-      tc::fence_after_sync();
-      uint32_t v[2][16];
+    // the TMEM loads of tile t+1 are issued before tile t is worked on, so
+    // their latency hides behind the arithmetic (two register sets; the loop
+    // is unrolled by two so that both stay in registers)
+    auto wait_full = [&](int t) {
+      bool w = tc::mbar_wait(tfull + (t & 1), (t >> 1) & 1, TC_WAIT);
+      w = __all_sync(0xffffffffu, w);
+      if (w) tc::fence_after_sync();
+      return w;
+    };
+    auto issue = [&](int t, uint32_t (&v)[2][16]) {
       const uint32_t ta = tbase + ((uint32_t)(32 * qd) << 16) +
-                          (uint32_t)(s * TC_N + 4 * TC_EPI_ROWS * hf);
+                          (uint32_t)((t & 1) * TC_N + 4 * TC_EPI_ROWS * hf);
       tc::tmem_ld16_async(ta, v[0]);
       tc::tmem_ld16_async(ta + 16, v[1]);
+    };
+    auto finish = [&](int t, uint32_t (&v)[2][16]) {
       tc::tmem_wait(v[0]);
       tc::tmem_regs_after_wait(v[1]);
       tc::fence_before_sync();
       __syncwarp();
-      if (lane == 0) tc::mbar_arrive(tfree + s);   // the buffer may take tile t+2
+      if (lane == 0) tc::mbar_arrive(tfree + (t & 1));   // the buffer may take tile t+2
+    };
+    auto work = [&](int t, const uint32_t (&v)[2][16]) {
       float gx = 0.f, gy = 0.f, gz = 0.f;
 #pragma unroll
       for (int i = 0; i < TC_EPI_ROWS; i++) {
@@ -271,6 +293,33 @@ __global__ void __launch_bounds__(TC_THREADS, 1) kf_tc_kernel(KfTc a) {
       Fx.add(gx);
       Fy.add(gy);
       Fz.add(gz);
+    };
+    uint32_t va[2][16], vb[2][16];
+    if (ok && a.ntn > 0) {
+      ok = wait_full(0);
+      if (ok) {
+        issue(0, va);
+        finish(0, va);
+      }
+    }
+    for (int t = 0; ok && t < a.ntn; t += 2) {
+      // va holds tile t
+      const bool n1 = t + 1 < a.ntn, n2 = t + 2 < a.ntn;
+      if (n1) {
+        ok = wait_full(t + 1);
+        if (!ok) break;
+        issue(t + 1, vb);
+      }
+      work(t, va);
+      if (!n1) break;
+      finish(t + 1, vb);
+      if (n2) {
+        ok = wait_full(t + 2);
+        if (!ok) break;
+        issue(t + 2, va);
+      }
+      work(t + 1, vb);
+      if (n2) finish(t + 2, va);
     }
     if (!ok && lane == 0) atomicOr(a.status, 16);
     // the four warps of a lane quarter: the others hand their sums to the
@@ -620,10 +669,14 @@ void kf_tc_rows(const KArgs& a, const std::vector<KRow>& krows, std::vector<TcRo
 cudaError_t k_kf_tc_za(const Launch& L, const KArgs& a, const float2* tab, float* za, float* zb) {
   const int KP = kf_tc_kp(a), ntm = (a.nq + TC_M - 1) / TC_M;
   const int nxy = (a.Kx + 1) + (2 * a.Ky + 1);
-  const long n = (long)ntm * TC_M * (KP + nxy);
-  kf_tc_prep_kernel<<<(int)((n + 255) / 256), 256, 0, L.s>>>(a.nq, ntm, a.row,
-                                                            a.Kx + 2 * a.Ky + 2, a.Kz, KP, nxy,
-                                                            sk_tc_kn(a), tab, za, zb);
+  const size_t smem = sizeof(float2) * SK_G * (size_t)a.row;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kf_tc_prep_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  kf_tc_prep_kernel<<<ntm * (TC_M / SK_G), 256, smem, L.s>>>(
+      a.nq, a.row, a.Kx + 2 * a.Ky + 2, a.Kz, KP, nxy, sk_tc_kn(a), tab, za, zb);
   ++*L.counter;
   return cudaGetLastError();
 }
