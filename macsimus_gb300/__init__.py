@@ -389,10 +389,17 @@ class ForcePath:
         self._check(library().mg_md_set_state(self._ctx, r.ctypes.data_as(_dp),
                                               r1.ctypes.data_as(_dp)))
 
-    def md_get_state(self):
+    def md_get_state(self, out=None):
+        """(r, r1) of the device MD state; out = (r, r1): contiguous float64
+        arrays (e.g. pinned host buffers) to copy into instead of new ones"""
         nv = 3 * self.ns * (2 if self.polar else 1)
-        r = np.empty(nv)
-        r1 = np.empty(nv)
+        if out is None:
+            r, r1 = np.empty(nv), np.empty(nv)
+        else:
+            r, r1 = out
+            for a in (r, r1):
+                if a.dtype != np.float64 or a.size != nv or not a.flags.c_contiguous:
+                    raise ValueError("out arrays must be contiguous float64 of %d values" % nv)
         self._check(library().mg_md_get_state(self._ctx, r.ctypes.data_as(_dp),
                                               r1.ctypes.data_as(_dp)))
         return r.reshape(-1, 3), r1.reshape(-1, 3)

@@ -45,6 +45,12 @@ def test_saved_state_reads_back_and_resumes(tmp_path):
     path = str(tmp_path / "saved.cfg")
     fp.md_save_cfg(path, c, t=c["t"] + 2 * c["h"])
     r, r1 = fp.md_get_state()
+    # the same state copied into caller-owned buffers
+    bufs = (np.empty(r.size), np.empty(r1.size))
+    fp.md_get_state(out=bufs)
+    assert np.array_equal(bufs[0].reshape(-1, 3), r) and np.array_equal(bufs[1].reshape(-1, 3), r1)
+    with pytest.raises(ValueError):
+        fp.md_get_state(out=(np.empty(5), np.empty(5)))
     back = cf.read_cfg(path)
     rb, r1b = cf.state_from_cfg(back, system.ns)
     assert np.array_equal(rb, r) and np.array_equal(r1b, r1)
