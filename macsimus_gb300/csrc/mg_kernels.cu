@@ -189,9 +189,9 @@ __global__ void __launch_bounds__(NW * 32)
   const unsigned refx = (unsigned)((((unsigned long long)(2 * cx + 1)) << 31) / a.ncx),
                  refy = (unsigned)((((unsigned long long)(2 * cy + 1)) << 31) / a.ncy),
                  refz = (unsigned)((((unsigned long long)(2 * cz + 1)) << 31) / a.ncz);
-  double en[NEN];
-#pragma unroll
-  for (int k = 0; k < NEN; k++) en[k] = 0;
+  // per-lane energy sums: FP32 per neighbour cell, folded into compensated
+  // FP32 sums (the FP64 pipe of this GPU is narrow); FP64 from the CTA sum on
+  CSum es[9];
 
   for (int ib = 0; ib < ni; ib += 32) {
     const bool vi = ib + lane < ni;
@@ -305,11 +305,12 @@ __global__ void __launch_bounds__(NW * 32)
         }
         __syncwarp();
       }
-      // energies fold into FP64 after every neighbour cell, forces every FOLD
+      // energies fold into the compensated sums after every neighbour cell,
+      // forces every FOLD cells
       if (MEASURE) {
-        en[0] += e_el; en[1] += e_lj; en[2] += e_vir;
-        en[3] += pv.p0; en[4] += pv.p1; en[5] += pv.p2;
-        en[6] += pv.p3; en[7] += pv.p4; en[8] += pv.p5;
+        es[0].add(e_el); es[1].add(e_lj); es[2].add(e_vir);
+        es[3].add(pv.p0); es[4].add(pv.p1); es[5].add(pv.p2);
+        es[6].add(pv.p3); es[7].add(pv.p4); es[8].add(pv.p5);
         e_el = e_lj = e_vir = 0;
         pv.zero();
       }
@@ -355,7 +356,7 @@ __global__ void __launch_bounds__(NW * 32)
   if (MEASURE) {
     // each unordered pair was visited from both ends
     for (int k = 0; k < 9; k++) {
-      ered[threadIdx.x] = 0.5 * en[k];
+      ered[threadIdx.x] = 0.5 * es[k].value();
       __syncthreads();
       for (int w = NT / 2; w > 0; w >>= 1) {
         if (threadIdx.x < w) ered[threadIdx.x] += ered[threadIdx.x + w];
