@@ -828,16 +828,20 @@ int build_lists(mg_ctx* ctx, const double* r_dev) {
   return fail(ctx, MG_ERR_SIZE, "neighbour list capacity");
 }
 
+// phase rows of the FP32 path; with the tensor-core passes the same kernel
+// builds their operand tiles
+cudaError_t phase_mixed(mg_ctx* ctx, const Launch& L, const KArgs& a, const double* r) {
+  if (ctx->kspace_tc)
+    return k_kf_tc_phase(L, a, r, (float2*)ctx->d_tab, ctx->d_za,
+                         ctx->sk_tc ? ctx->d_zb : nullptr);
+  return k_phase_tables_mixed(L, a, r, (float2*)ctx->d_tab, ctx->d_qfix);
+}
+
 // Ewald pass 1 of the FP32 path (structure factor partials, then their FP64
-// sum): tensor cores or FP32 cores; the tensor-core operand tiles of both
-// passes are built here from the phase rows
+// sum): tensor cores or FP32 cores
 cudaError_t sk_mixed(mg_ctx* ctx, const Launch& L, const KArgs& a, bool measure) {
   const float2* tab = (const float2*)ctx->d_tab;
   float2* part = (float2*)ctx->d_part;
-  if (ctx->kspace_tc) {
-    cudaError_t e = k_kf_tc_za(L, a, tab, ctx->d_za, ctx->sk_tc ? ctx->d_zb : nullptr);
-    if (e != cudaSuccess) return e;
-  }
   if (!ctx->sk_tc) {
     cudaError_t e = k_sk_gemm_mixed(L, a, tab, part);
     if (e != cudaSuccess) return e;
@@ -969,7 +973,7 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
       kk.f = ctx->d_fk;
       CK(cudaStreamWaitEvent(ks, ctx->ev_fork, 0));
       CK(cudaMemsetAsync(ctx->d_fk, 0, nf * sizeof(double), ks));
-      PROFS("phase_tables", ks, k_phase_tables_mixed(LK, kk, r_dev, (float2*)ctx->d_tab, ctx->d_qfix));
+      PROFS("phase_tables", ks, phase_mixed(ctx, LK, kk, r_dev));
       PROFS("ewald_sk", ks, sk_mixed(ctx, LK, kk, measure));
       PROFS("ewald_kforce", ks, kf_mixed(ctx, LK, kk));
       CK(cudaEventRecord(ctx->ev_join, ks));
@@ -999,7 +1003,7 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
       CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
       PROF("ewald_kforce", k_add_forces(L, nf, ctx->d_fk, f_dev));
     } else if (ctx->nq > 0) {
-      PROF("phase_tables", k_phase_tables_mixed(L, ka, r_dev, (float2*)ctx->d_tab, ctx->d_qfix));
+      PROF("phase_tables", phase_mixed(ctx, L, ka, r_dev));
       PROF("ewald_sk", sk_mixed(ctx, L, ka, measure));
       PROF("ewald_kforce", kf_mixed(ctx, L, ka));
     }
@@ -1340,7 +1344,7 @@ int mg_ewald(mg_ctx* ctx, const double* r, double* f, double* energy) {
   ka.status = ctx->d_status;
   if (ctx->nq > 0) {
     if (ctx->precision == MG_MIXED) {
-      CK(k_phase_tables_mixed(L, ka, ctx->d_rs, (float2*)ctx->d_tab, ctx->d_qfix));
+      CK(phase_mixed(ctx, L, ka, ctx->d_rs));
       CK(sk_mixed(ctx, L, ka, true));
       CK(kf_mixed(ctx, L, ka));
     } else {

@@ -7,6 +7,17 @@ namespace mg {
 
 constexpr int NEN = 10;   // er, lj, vir, Pvir[6], (spare)
 
+__device__ __forceinline__ double wrap01(double s) { return s - floor(s); }
+
+// a coordinate as a 32-bit fixed-point fraction of the box edge Lb (the
+// difference of two such numbers, as 32-bit integers, is the nearest-image
+// separation)
+__device__ __forceinline__ int fixed32(double x, double Lb) {
+  double s = wrap01(x / Lb);
+  long long v = llrint(s * 4294967296.0);
+  return (int)(unsigned int)(v & 0xffffffffLL);
+}
+
 // Ewald exclusion term -erf(alpha r)/r and its f/r (cook's exacterud_sqrt);
 // with minus_const the constant 2 alpha/sqrt(pi) is taken off the energy
 // (exacterud_sqrt_1, the centre-Drude pair of one site)

@@ -177,6 +177,9 @@ size_t kf_tc_vb_floats(const KArgs& a, int nrows);
 void kf_tc_rows(const KArgs& a, const std::vector<KRow>& krows, std::vector<TcRow>* out);
 // the operand tiles of both passes from the phase rows (zb may be NULL)
 cudaError_t k_kf_tc_za(const Launch& L, const KArgs& a, const float2* tab, float* za, float* zb);
+// the phase rows and the operand tiles in one kernel, from the positions
+cudaError_t k_kf_tc_phase(const Launch& L, const KArgs& a, const double* r, float2* tab,
+                          float* za, float* zb);
 // pass 1 on the tensor cores: KN = 2 Kz + 1 rounded up to 16 (at most 64);
 // the phase rows must be zero-padded to whole groups of 32 charges
 int sk_tc_kn(const KArgs& a);

@@ -30,7 +30,6 @@ static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 
 // ------------------------------------------------------------- cell list --
 
-__device__ __forceinline__ double wrap01(double s) { return s - floor(s); }
 
 __device__ __forceinline__ int cell_coord(double s, int n) {
   int c = (int)(s * n);
@@ -83,11 +82,6 @@ cudaError_t k_cell_bounds(const Launch& L, int ns, int ncell, const int* key_sor
   return cudaGetLastError();
 }
 
-__device__ __forceinline__ int fixed32(double x, double Lb) {
-  double s = wrap01(x / Lb);
-  long long v = llrint(s * 4294967296.0);
-  return (int)(unsigned int)(v & 0xffffffffLL);
-}
 
 __global__ void gather_mixed_kernel(int ns, const double* __restrict__ r,
                                     const int* __restrict__ order, const int* __restrict__ kind,

@@ -103,6 +103,99 @@ __global__ void __launch_bounds__(256) kf_tc_prep_kernel(int nq, int row, int oz
   }
 }
 
+// The same tiles computed straight from the positions (tensor-core path):
+// per group of 32 charges the fixed-point coordinates and the phase rows
+// (the arithmetic of charge_fixed_kernel and phase_tables_mixed_kernel, so
+// the values are the same bit for bit), written to the phase table for
+// pass 1 and, through shared memory, to the operand tiles.
+__global__ void __launch_bounds__(256) kf_tc_phase_kernel(KArgs a, const double* __restrict__ r,
+                                                          int KP, int nxy, int KN,
+                                                          float2* __restrict__ tab,
+                                                          float* __restrict__ za,
+                                                          float* __restrict__ zb) {
+  extern __shared__ float2 st_ph[];   // [32][row]
+  __shared__ uint4 sfix[SK_G];
+  __shared__ float sq[SK_G];
+  const int g = blockIdx.x, j0 = g * SK_G, row = a.row, Kz = a.Kz;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nvalid = min(SK_G, max(0, a.nq - j0));
+  if (tid < SK_G) {
+    uint4 f = make_uint4(0u, 0u, 0u, 0u);
+    float q = 0.f;
+    if (tid < nvalid) {
+      const int j = j0 + tid, site = a.qsite[j];
+      double x = r[3 * site], y = r[3 * site + 1], z = r[3 * site + 2];
+      if (a.qdrude && a.qdrude[j]) {
+        x += r[3 * (long)a.ns + 3 * site];
+        y += r[3 * (long)a.ns + 3 * site + 1];
+        z += r[3 * (long)a.ns + 3 * site + 2];
+      }
+      f = make_uint4((unsigned)fixed32(x, a.Lx), (unsigned)fixed32(y, a.Ly),
+                     (unsigned)fixed32(z, a.Lz), 0u);
+      q = (float)a.qval[j];
+    }
+    sfix[tid] = f;
+    sq[tid] = q;
+  }
+  __syncthreads();
+  for (int t = tid; t < SK_G * row; t += 256) {
+    const int c = t / row, e = t % row;
+    float2 v = make_float2(0.f, 0.f);
+    if (c < nvalid) {
+      int d, n;
+      if (e <= a.Kx) { d = 0; n = e; }
+      else if (e <= a.Kx + 2 * a.Ky + 1) { d = 1; n = e - (a.Kx + 1) - a.Ky; }
+      else { d = 2; n = e - (a.Kx + 2 * a.Ky + 2); }
+      const uint4 S4 = sfix[c];
+      const unsigned S = d == 0 ? S4.x : (d == 1 ? S4.y : S4.z);
+      const int ph = (int)(S * (unsigned int)n);
+      const float tt = (float)ph * 2.3283064365386963e-10f;
+      float sn, cs;
+      sincospif(2.f * tt, &sn, &cs);
+      if (d == 0) {
+        cs *= sq[c];
+        sn *= sq[c];
+      }
+      v = make_float2(cs, sn);
+      tab[(long)j0 * row + t] = v;
+    }
+    st_ph[t] = v;
+  }
+  __syncthreads();
+  auto zval = [&](int c, int kk) -> float {
+    const float2* zr = st_ph + c * row + (a.Kx + 2 * a.Ky + 2);
+    return kk <= Kz ? zr[kk].x : (kk <= 2 * Kz ? zr[kk - Kz].y : 0.f);
+  };
+  const int rr = lane & 7, cc = lane >> 3;
+  const int m0 = SK_G * (g % (TC_M / SK_G));
+  const size_t tile_f = (size_t)2 * TC_M * (KP + nxy);
+  float* base = za + (size_t)(g / (TC_M / SK_G)) * tile_f;
+  for (int q = warp; q < (SK_G / 8) * (KP / 4); q += 8) {
+    const int c = 8 * (q / (KP / 4)) + rr, kk = 4 * (q % (KP / 4)) + cc;
+    float hi, lo;
+    tc::tf32_split(zval(c, kk), hi, lo);
+    const uint32_t o = tc::kmajor_offset(m0 + c, kk, KP) >> 2;
+    base[o] = hi;
+    base[(size_t)TC_M * KP + o] = lo;
+  }
+  if (zb) {
+    float* zt = zb + (size_t)g * 2 * SK_G * KN;
+    for (int q = warp; q < (KN / 8) * (SK_G / 4); q += 8) {
+      const int kk = 8 * (q / (SK_G / 4)) + rr, c = 4 * (q % (SK_G / 4)) + cc;
+      float hi, lo;
+      tc::tf32_split(zval(c, kk), hi, lo);
+      const uint32_t o = tc::kmajor_offset(kk, c, SK_G) >> 2;
+      zt[o] = hi;
+      zt[(size_t)SK_G * KN + o] = lo;
+    }
+  }
+  float2* xy = reinterpret_cast<float2*>(base + (size_t)2 * TC_M * KP);
+  for (int t = tid; t < nxy * SK_G; t += 256) {
+    const int e = t / SK_G, c = t % SK_G;
+    xy[(size_t)e * TC_M + m0 + c] = st_ph[c * row + e];
+  }
+}
+
 // B operand: per row r the columns 4r .. 4r+3 = coefficients of H.x, H.y,
 // Hz.x, Hz.y over z_j (hi then lo per tile of 32 rows)
 __global__ void kf_tc_vb_kernel(int nrows, int ntn, int Kz, int KP, const KRow* __restrict__ krows,
@@ -664,6 +757,22 @@ void kf_tc_rows(const KArgs& a, const std::vector<KRow>& krows, std::vector<TcRo
   out->clear();
   for (const KRow& r : krows)
     out->push_back(TcRow{(float)r.kx, (float)r.ky, r.kx * TC_M, (oyl + r.ky) * TC_M});
+}
+
+cudaError_t k_kf_tc_phase(const Launch& L, const KArgs& a, const double* r, float2* tab,
+                          float* za, float* zb) {
+  const int KP = kf_tc_kp(a), ntm = (a.nq + TC_M - 1) / TC_M;
+  const int nxy = (a.Kx + 1) + (2 * a.Ky + 1);
+  const size_t smem = sizeof(float2) * SK_G * (size_t)a.row;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kf_tc_phase_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  kf_tc_phase_kernel<<<ntm * (TC_M / SK_G), 256, smem, L.s>>>(a, r, KP, nxy, sk_tc_kn(a), tab,
+                                                              za, zb);
+  ++*L.counter;
+  return cudaGetLastError();
 }
 
 cudaError_t k_kf_tc_za(const Launch& L, const KArgs& a, const float2* tab, float* za, float* zb) {
