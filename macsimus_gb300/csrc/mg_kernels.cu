@@ -15,8 +15,8 @@
 // Mixed precision: positions enter the pair kernel as 32-bit fixed-point
 // fractions of the box, so the nearest-image difference is an exact integer
 // subtraction; pair arithmetic is FP32; per-site sums are carried in FP32
-// within a neighbour-cell batch and folded into FP64; all global reductions
-// are FP64 in a fixed order.
+// within a neighbour-cell batch and folded into compensated FP32 sums; all
+// global reductions are FP64 in a fixed order.
 #include "mg_internal.h"
 #include "mg_device.cuh"
 
