@@ -369,7 +369,11 @@ cudaError_t k_pair_mixed(const Launch& L, const PairArgs& a, const int4* pj, con
         sz = (float)(a.Lz / 4294967296.0);
   const float cq = (float)a.cutoff_sq, sg = (float)a.sgrid, al = (float)a.alpha;
   const bool rel = !a.allpairs;
-  const int nw = a.pair_warps == 16 ? 16 : (a.pair_warps == 8 ? 8 : 4);
+  // the measuring kernel (energies, virial) always runs with 4 warps and the
+  // spline through L1: with more registers per thread it keeps more CTAs
+  // resident that way (1.0 ms on 32768 waters; 16 warps + shared-memory
+  // spline, the fastest force-only choice there, 1.8 ms)
+  const int nw = measure ? 4 : (a.pair_warps == 16 ? 16 : (a.pair_warps == 8 ? 8 : 4));
   const bool stab = a.spline_smem && !measure;
   const size_t dsm = sizeof(PairFS) * (size_t)a.nkind * a.nkind +
                      (stab ? sizeof(float4) * (size_t)a.ntab : 0);
