@@ -1037,10 +1037,11 @@ __device__ __forceinline__ double wrap_shift(double lo, double r0, double L) {
 }
 
 // three-site, three-constraint molecules (rigid water) with the positions in
-// registers: the same sweeps, in the same order and with the same roundings,
-// as the general path below (which works on the global array p).  The
-// per-constraint factors omega/(m_i^-1 + m_j^-1)/d^2 and 1/d^2 are formed
-// once per call: FP64 divisions are slow on this GPU.
+// registers: the same sweeps in the same order as the general path below
+// (which works on the global array p), 15 FP64 operations per constraint
+// and sweep: the per-constraint factors m^-1 omega/(m_i^-1 + m_j^-1)/d^2 and
+// the tolerance eps d^2 are formed once per call (FP64 divisions and
+// multiplications are slow on this GPU's narrow FP64 pipe).
 __device__ __forceinline__ double3 sh_get(int k, const double3& a, const double3& b,
                                           const double3& c) {
   return k == 0 ? a : (k == 1 ? b : c);
@@ -1120,41 +1121,43 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
                               a.f[3 * i + 2] * (a.hh * im[s]) + R[s].z + a.r1[3 * i + 2]);
         }
       }
+      // per constraint: the tolerance as a bound on |d| (eps bq, so no
+      // product per sweep) and the factors m_i^-1 wq, m_j^-1 wq that turn d
+      // into the two displacements along r_ij
       int ci[3], cj[3];
-      double bq[3], ibq[3], wq[3], rx[3], ry[3], rz[3], mi[3], mj[3];
+      double bq[3], tol[3], awi[3], awj[3], rx[3], ry[3], rz[3];
 #pragma unroll
       for (int q = 0; q < 3; q++) {
         const int2 ij = a.cons[c0 + q];
         ci[q] = ij.x - i0;
         cj[q] = ij.y - i0;
         bq[q] = a.bondq[c0 + q];
-        mi[q] = a.imass[ij.x];
-        mj[q] = a.imass[ij.y];
-        ibq[q] = 1.0 / bq[q];
-        wq[q] = a.omega / (mi[q] + mj[q]) * ibq[q];
+        const double mi = a.imass[ij.x], mj = a.imass[ij.y];
+        const double wq = a.omega / (mi + mj) * (1.0 / bq[q]);
+        tol[q] = a.eps * bq[q];
+        awi[q] = mi * wq;
+        awj[q] = -(mj * wq);
         const double3 ri = sh_get(ci[q], R[0], R[1], R[2]), rj = sh_get(cj[q], R[0], R[1], R[2]);
         rx[q] = ri.x - rj.x;
         ry[q] = ri.y - rj.y;
         rz[q] = ri.z - rj.z;
       }
       int it = 0;
-      double maxsq;
+      bool over;
       do {
         it++;
-        maxsq = 0;
+        over = false;
 #pragma unroll
         for (int q = 0; q < 3; q++) {
           const double3 pi = sh_get(ci[q], P[0], P[1], P[2]), pj = sh_get(cj[q], P[0], P[1], P[2]);
           const double px = pi.x - pj.x, py = pi.y - pj.y, pz = pi.z - pj.z;
           const double d = bq[q] - (px * px + py * py + pz * pz);
-          maxsq = fmax(maxsq, fabs(d) * ibq[q]);
-          const double sq = d * wq[q];
-          const double sx = rx[q] * sq, sy = ry[q] * sq, sz = rz[q] * sq;
-          sh_add(ci[q], P[0], P[1], P[2], mi[q], sx, sy, sz);
-          sh_add(cj[q], P[0], P[1], P[2], -mj[q], sx, sy, sz);
+          over |= fabs(d) > tol[q];
+          sh_add(ci[q], P[0], P[1], P[2], d * awi[q], rx[q], ry[q], rz[q]);
+          sh_add(cj[q], P[0], P[1], P[2], d * awj[q], rx[q], ry[q], rz[q]);
         }
-      } while (maxsq > a.eps && it < a.maxit);
-      if (maxsq > a.eps) atomicOr(a.status, 1);
+      } while (over && it < a.maxit);
+      if (over) atomicOr(a.status, 1);
       double sx = 0, sy = 0, sz = 0;
       if (a.normalize) {
         double lx = 9e9, ly = 9e9, lz = 9e9;
