@@ -240,6 +240,13 @@ RESUME_CASES = {
     "resume216": dict(binary="cookew", species=["WAT"], N=[216], L=18.6206, cutoff=9.0,
                       alpha=0.35, kn=6, h=0.002, epsc=1e-10, steps_a=4, steps_b=3,
                       r1_scale=0.5),
+    # the same with 216 Drude waters (POLAR build, ASPC k=2 + one SCF
+    # iteration): cfg[0] and cfg[1] hold 2 ns vectors, the Drude
+    # displacements after the sites
+    "resume_drude216": dict(binary="cookpol", species=["WATD"], N=[216], L=18.6206,
+                            cutoff=9.0, alpha=0.35, kn=6, h=0.001, epsc=1e-10, steps_a=4,
+                            steps_b=3, r1_scale=0.5, options=["-p220"],
+                            extra_def=["scf.eps=-1"]),
 }
 
 
@@ -258,8 +265,8 @@ def run_resume_case(name, c):
     def run(init, steps):
         with open(os.path.join(wd, "sim.get"), "w") as f:
             f.write('init="%s"\nno=%d\n;\n' % (init, steps))
-        p = subprocess.run([binary, "ff.ble", "sim"], cwd=wd, stdin=subprocess.DEVNULL,
-                           capture_output=True, text=True, timeout=600)
+        p = subprocess.run([binary, "ff.ble", "sim"] + c.get("options", []), cwd=wd,
+                           stdin=subprocess.DEVNULL, capture_output=True, text=True, timeout=600)
         if p.returncode != 0:
             raise SystemExit("%s failed:\n%s" % (name, p.stdout[-3000:]))
         return cfgfile.read_cfg(os.path.join(wd, "sim.cfg"))

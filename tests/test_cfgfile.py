@@ -112,3 +112,23 @@ def test_damaged_files_are_refused(tmp_path):
     # a state of the wrong shape
     with pytest.raises(cf.CfgError):
         cf.cfg_with_state(cf.read_cfg(A), np.zeros((10, 3)), np.zeros((10, 3)))
+
+
+def test_polar_cfg_holds_the_drude_half():
+    """cook's Drude build (POLAR, cfgkey 3) saves 2 ns vectors per
+    configuration, the Drude displacements after the sites, and tau.dip as
+    key 17 (sim/simils.c:1505-1509); the file round-trips byte for byte"""
+    path = os.path.join(GOLDEN, "resume_drude216_a.cfg")
+    c = cf.read_cfg(path)
+    assert c["cfgkey"] == 3 and c["polar"] and 17 in c["keys"]
+    r, r1 = cf.state_from_cfg(c, 648)
+    assert r.shape == (1296, 3) and r1.shape == (1296, 3)
+    # Drude displacements: a few hundredths of an angstrom
+    assert 1e-3 < np.abs(r[648:]).max() < 0.2
+    out = os.path.join(os.environ.get("TMPDIR", "/tmp"), "mg_cfg_polar_%d.cfg" % os.getpid())
+    try:
+        cf.write_cfg(out, c)
+        assert open(out, "rb").read() == open(path, "rb").read()
+    finally:
+        if os.path.exists(out):
+            os.remove(out)

@@ -60,3 +60,27 @@ def test_saved_state_reads_back_and_resumes(tmp_path):
     fp2.md_load_cfg(path)
     fp2.md_steps(2, measure=False)
     assert np.array_equal(fp2.md_get_state()[0], fp.md_get_state()[0])
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-8), ("mixed", 1e-5)])
+def test_drude_device_resumes_from_cook_cfg(precision, tol):
+    """a Drude context loaded from cook's POLAR .cfg (sites and Drude
+    displacements; the ASPC history restarted from cfg[0] and cfg[1] as cook
+    restarts it) continues as cook continued the same file"""
+    import json
+    from golden_cases import GOLDEN
+    from macsimus_gb300 import forcefield as ff
+    meta = json.load(open(os.path.join(GOLDEN, "resume_drude216.json")))
+    g = np.load(os.path.join(GOLDEN, "resume_drude216.npz"))
+    p = meta["params"]
+    system = ff.build_system(p["species"], p["N"])
+    omegac = json.load(open(os.path.join(GOLDEN, "drude216.json")))["omegac"]
+    fp = M.ForcePath(system, np.array([p["L"]] * 3), p["cutoff"], p["alpha"],
+                     (p["kn"] + 1e-6) / p["L"], precision=precision, h=p["h"], epsc=p["epsc"],
+                     omegac=omegac, aspc_k=2, scf_iter=1)
+    fp.md_load_cfg(os.path.join(GOLDEN, "resume_drude216_a.cfg"))
+    fp.md_steps(p["steps_b"], measure=False)
+    r, _ = fp.md_get_state()
+    ns = system.ns
+    assert np.abs(r[:ns] - g["rB"][:ns]).max() < tol
+    assert np.abs(r[ns:] - g["rB"][ns:]).max() < tol
