@@ -147,6 +147,22 @@ typedef struct {
   /* Nose-Hoover predictor length k (cook's No.pred = option -p % 10,
      sim/main.c:404-405), 1..8; <=0 selects 2 */
   int nose_pred;
+  /* dipole term of Ewald(2) (sim/ewald.c:865-887), cook's el.corr
+     (sim/simglob.h:828): 0 = the isotropic term of epsinf (none for
+     epsinf >= 1e20, tin foil); bits 1, 2, 4 = the Yeh-Berkowitz slab term
+     along x, y, z instead; + 8 = its energy and virial without the force */
+  int dipole_corr;
+  /* cook's drmax (sim/main.c:140) for its bounddr step limiter
+     (sim/norm.c:1513-1560): 0 = off; otherwise, after every MD step and its
+     thermostat, the displacement r1 of a site longer than |drmax| (A) is
+     scaled to that length (cook applies a positive drmax only to thermostatted
+     runs that start with init > 2; the caller decides) */
+  double drmax;
+  /* drift_step != 0: the momentum drift is removed after every step (after
+     bounddr), cook's removedrifts with its momentum bits and DRIFT_STEP
+     (sim/norm.c:677-705, sim/main.c:1626); cook's default removes it once
+     per cycle, which a host loop does with mg_remove_drift */
+  int drift_step;
 } mg_params;
 
 /* Energies of one force evaluation (program units, K).
@@ -159,9 +175,17 @@ typedef struct {
   double ek;        /* k-space part */
   double er;        /* r-space part incl. Ewald exclusion corrections */
   double eself;     /* -alpha/sqrt(pi) sum q^2 */
-  double edip;      /* dipole term */
+  double edip;      /* dipole term (finite epsinf or Yeh-Berkowitz; part of el) */
   double self;      /* Drude spring energy (En.self) */
   double ekin;      /* kinetic energy (mg_md_steps only) */
+  /* pressure of the last step of mg_md_steps (zero after mg_forces), as
+     cook's measurePconstraints assembles it (sim/constrd.c:115-265) with
+     No.Pkinq = 1; tensors xx yy zz yz zx xy in K/A^3 (times 13806490 =
+     cook's Punit gives Pa) */
+  double virc;      /* constraint virial En.virc: sum of the SHAKE factors / h^2 (sim/virc.c) */
+  double Pkin[6];   /* kinetic tensor sum m v v / V, leap-frog v of sim/shakev3.c */
+  double Ptens[6];  /* (Pvir + constraint virial tensor PTvirc) / V + Pkin */
+  double P;         /* cook's Pevir: (2 ekin + vir + virc + el - 2 self) / (3 V) */
 } mg_energy;
 
 /* Create a context on the current CUDA device.  Builds the smooth-cutoff LJ
@@ -223,6 +247,15 @@ int mg_tc_selftest(const float *A, const float *B, float *C, int n, int k);
 int mg_playback_frame(mg_ctx *ctx, int what, int flags, float *frame);
 /* advance nsteps; energies of the last step in *en when en != NULL */
 int mg_md_steps(mg_ctx *ctx, int nsteps, mg_energy *en);
+/* what the drmax limiter did since the last report (cook prints "dr in 1
+   step reduced for N site(s), min Q x"): sites reduced (summed over steps)
+   and the smallest factor (1 if none); resets both (a synchronising call) */
+int mg_bounddr_report(mg_ctx *ctx, long long *nreduced, double *minfactor);
+/* cook's removedrifts for the linear momentum (sim/norm.c:677-705, called
+   once per cycle at sim/maincps.c:65): the mass-weighted mean of r1 is
+   subtracted from every site of the MD state; vdrift (or NULL) gets the
+   removed drift velocity, A/ps */
+int mg_remove_drift(mg_ctx *ctx, double vdrift[3]);
 
 /* number of kernels launched by the last call (diagnostics) */
 int mg_last_launches(const mg_ctx *ctx);
@@ -273,11 +306,12 @@ int mg_probe_fp32_tflops(double *tflops);
    L, alpha, kappa as in mg_params; stream is a cudaStream_t (NULL: default
    stream); the call returns after the work is done.  Limits: at most
    MG_NOALLOC_MAX_CHARGES charges, MG_NOALLOC_MAX_KVEC k-vectors, phase rows
-   of at most MG_NOALLOC_MAX_ROW entries ((Kx+1)+(2Ky+1)+(2Kz+1)); larger
-   inputs return MG_ERR_SIZE.  The first call on a device looks up the
-   array's device address (make it before any stream capture).  All calls
-   share the array and keep the last call's data in it: calls that overlap on
-   the GPU (or run concurrently from several host threads) race. */
+   of at most MG_NOALLOC_MAX_ROW entries ((Kx+1)+(2Ky+1)+(Kz+1), Kx, Ky, Kz
+   the largest |kx|, |ky|, |kz| of the k set); larger inputs return
+   MG_ERR_SIZE.  Every call looks up the array's address on the current
+   device.  All calls share the array and keep the last call's data in it:
+   calls that overlap on the GPU (or run concurrently from several host
+   threads) race. */
 #define MG_NOALLOC_MAX_CHARGES 4096
 #define MG_NOALLOC_MAX_KVEC 4096
 #define MG_NOALLOC_MAX_ROW 96

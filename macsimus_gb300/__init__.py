@@ -57,18 +57,22 @@ class Params(C.Structure):
                 ("thermostat", C.c_int), ("T", C.c_double), ("tau_T", C.c_double),
                 ("thermo_f", C.c_double), ("seed", C.c_ulonglong), ("box_rmin", C.c_double),
                 ("no_normalize", C.c_int), ("kspace_engine", C.c_int),
-                ("nose_pred", C.c_int)]
+                ("nose_pred", C.c_int), ("dipole_corr", C.c_int), ("drmax", C.c_double),
+                ("drift_step", C.c_int)]
 
 
 class Energy(C.Structure):
     _fields_ = [("el", C.c_double), ("lj", C.c_double), ("vir", C.c_double),
                 ("Pvir", C.c_double * 6), ("ek", C.c_double), ("er", C.c_double),
                 ("eself", C.c_double), ("edip", C.c_double), ("self", C.c_double),
-                ("ekin", C.c_double)]
+                ("ekin", C.c_double), ("virc", C.c_double), ("Pkin", C.c_double * 6),
+                ("Ptens", C.c_double * 6), ("P", C.c_double)]
+    _tensors = ("Pvir", "Pkin", "Ptens")
 
     def asdict(self):
-        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "Pvir"}
-        d["Pvir"] = list(self.Pvir)
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in self._tensors}
+        for k in self._tensors:
+            d[k] = list(getattr(self, k))
         return d
 
 
@@ -125,6 +129,8 @@ def library():
         L.mg_thermostat_factor.argtypes = [vp]
         L.mg_thermostat_factor.restype = C.c_double
         L.mg_nose_state.argtypes = [vp, _dp]
+        L.mg_bounddr_report.argtypes = [vp, C.POINTER(C.c_longlong), _dp]
+        L.mg_remove_drift.argtypes = [vp, _dp]
         L.mg_profile_enable.argtypes = [vp, C.c_int]
         L.mg_profile_reset.argtypes = [vp]
         L.mg_profile_entry.argtypes = [vp, C.c_int, C.POINTER(C.c_char_p), _dp,
@@ -185,7 +191,7 @@ def describe(system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None, 
              cells_per_cutoff=0, aspc_k=2, scf_iter=1, scf_omega=0.6, minqq=1.0, skin=0.0,
              nl_every=50, kspace_ctas_per_sm=0, pair_variant=0, thermostat=0, T=298.0,
              tau_T=0.1, thermo_f=0.0, seed=0, box_rmin=0.0, normalize=True, kspace_engine=0,
-             nose_pred=2):
+             nose_pred=2, dipole_corr=0, drmax=0.0, drift_step=False):
     """(mg_topology, mg_params, arrays to keep alive) of one box"""
     keep = []
 
@@ -265,6 +271,9 @@ def describe(system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None, 
     p.no_normalize = 0 if normalize else 1
     p.kspace_engine = int(kspace_engine)
     p.nose_pred = int(nose_pred)
+    p.dipole_corr = int(dipole_corr)
+    p.drmax = float(drmax)
+    p.drift_step = 1 if drift_step else 0
     return t, p, keep
 
 
@@ -276,7 +285,8 @@ class ForcePath:
                  shake_maxit=1000, cells_per_cutoff=0, aspc_k=2, scf_iter=1, scf_omega=0.6,
                  minqq=1.0, skin=0.0, nl_every=50, kspace_ctas_per_sm=0, pair_variant=0,
                  thermostat=0, T=298.0, tau_T=0.1, thermo_f=0.0, seed=0, box_rmin=0.0,
-                 normalize=True, kspace_engine=0, nose_pred=2):
+                 normalize=True, kspace_engine=0, nose_pred=2, dipole_corr=0, drmax=0.0,
+                 drift_step=False):
         lib = library()
         self.system = system
         self.ns = system.ns
@@ -290,7 +300,9 @@ class ForcePath:
                                     pair_variant=pair_variant, thermostat=thermostat, T=T,
                                     tau_T=tau_T, thermo_f=thermo_f, seed=seed,
                                     box_rmin=box_rmin, normalize=normalize,
-                                    kspace_engine=kspace_engine, nose_pred=nose_pred)
+                                    kspace_engine=kspace_engine, nose_pred=nose_pred,
+                                    dipole_corr=dipole_corr, drmax=drmax,
+                                    drift_step=drift_step)
         self.polar = getattr(system, "polar", False)
         Lb = np.broadcast_to(np.asarray(L, dtype=np.float64), (3,))
         st = C.c_int(0)
@@ -373,9 +385,9 @@ class ForcePath:
         e = Energy()
         if en is not None:
             for k, v in en.items():
-                if k == "Pvir":
+                if k in Energy._tensors:
                     for m in range(6):
-                        e.Pvir[m] = v[m]
+                        getattr(e, k)[m] = v[m]
                 else:
                     setattr(e, k, v)
         self._check(library().mg_selffield(self._ctx, r.ctypes.data_as(_dp),
@@ -457,6 +469,20 @@ class ForcePath:
     def thermostat_factor(self):
         """velocity factor of the last thermostat call"""
         return library().mg_thermostat_factor(self._ctx)
+
+    def remove_drift(self):
+        """cook's removedrifts (momentum) on the MD state; returns the removed
+        drift velocity, A/ps"""
+        v = np.zeros(3)
+        self._check(library().mg_remove_drift(self._ctx, v.ctypes.data_as(_dp)))
+        return v
+
+    def bounddr_report(self):
+        """(sites whose step was reduced, smallest factor) since the last
+        report: cook's bounddr with drmax"""
+        n, q = C.c_longlong(), C.c_double()
+        self._check(library().mg_bounddr_report(self._ctx, C.byref(n), C.byref(q)))
+        return n.value, q.value
 
     def nose_state(self):
         """Nose-Hoover (thermostat="nose"): (logs, h dlogs/dt, the thermostat's

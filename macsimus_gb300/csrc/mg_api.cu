@@ -12,9 +12,11 @@
 #include <string>
 #include <vector>
 
-#include <cub/device/device_radix_sort.cuh>
 
 using namespace mg;
+
+// length of the reduction-output block d_sums / h_sums (doubles)
+constexpr int NSUMS = 48;
 
 struct mg_ctx {
   std::string err;
@@ -22,9 +24,24 @@ struct mg_ctx {
   int ns = 0, nmol = 0, nc = 0, nq = 0, nk = 0, nkind = 0, launches = 0;
   double L[3] = {0, 0, 0};
   double cutoff = 0, alpha = 0, kappa = 0, sgrid = 0, eself = 0, epsinf = 3e33;
+  // dipole term of Ewald(2) (finite epsinf or Yeh-Berkowitz): force factors
+  // c_d (force q (-c_d M_d)), energy factors e_d (E = sum e_d M_d^2)
+  bool dipole = false;
+  int elcorr = 0;
+  double dipc[3] = {0, 0, 0}, dipe[3] = {0, 0, 0};
+  double* d_dippart = nullptr;
+  // cook's bounddr after every MD step (drmax != 0): sites reduced, float
+  // bits of the smallest factor
+  double drmax = 0;
+  unsigned int* d_bdrep = nullptr;
+  // momentum drift removal (cook's removedrifts, momentum bits): after every
+  // step with drift_step, else on request; total mass of the sites
+  bool drift_step = false;
+  double total_mass = 0;
+  double *d_driftpart = nullptr, *d_drift = nullptr;  // [blocks*3], [6]: P, removed drift
   double h = 0.002, epsc = 1e-7, omega = 0.6;
   int shake_maxit = 1000;
-  int ncx = 0, ncy = 0, ncz = 0, ncell = 0, nstencil = 0, sort_bits = 1;
+  int ncx = 0, ncy = 0, ncz = 0, ncell = 0, nstencil = 0;
   bool allpairs = false;
   int ntab = 0;
   int Kx = 0, Ky = 0, Kz = 0, row = 0, ntask = 0, ncol = 0, nchunk = 1;
@@ -37,8 +54,7 @@ struct mg_ctx {
   int *d_kind = nullptr, *d_mol = nullptr;
   int *d_key = nullptr, *d_idx = nullptr, *d_key_s = nullptr, *d_order = nullptr;
   int* d_cell_start = nullptr;
-  void* d_sort_tmp = nullptr;
-  size_t sort_tmp_bytes = 0;
+  int *d_ccount = nullptr, *d_ccursor = nullptr;  // cell counts (kept zero), cursors
   int4* d_pj = nullptr;
   double4* d_pd = nullptr;
   int4* d_stencil = nullptr;
@@ -82,6 +98,7 @@ struct mg_ctx {
   int2* d_cons = nullptr;
   double *d_bondq = nullptr, *d_imass = nullptr, *d_mass = nullptr;
   double* d_kinpart = nullptr;
+  double* d_meas = nullptr;  // [nblocks * 13] constraint virial and kinetic tensor sums
   int* d_status = nullptr;
   // linear dependant sites
   int ndep = 0;
@@ -94,7 +111,9 @@ struct mg_ctx {
   int nxblocks = 0;
   float* d_plb = nullptr;  // playback frame staging
   // reduction outputs
-  double* d_sums = nullptr;  // [0..9] pair, [10..16] k-space, [17] kinetic
+  // [0..9] pair, [10..16] k-space, [17] kinetic, [20..27] Drude,
+  // [31] status word (host copy), [32..44] SHAKE measurement
+  double* d_sums = nullptr;
   double* h_sums = nullptr;  // pinned
   bool have_state = false;
   // neighbour lists
@@ -259,8 +278,8 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   for (int d = 0; d < 3; d++)
     if (!(p->L[d] > 2 * p->cutoff))
       return fail(ctx, MG_ERR_ARG, "the cutoff must be shorter than half the box");
-  if (p->epsinf < 1e20)
-    return fail(ctx, MG_ERR_ARG, "only conducting (tin-foil) boundary conditions, epsinf>=1e20");
+  if (!(p->epsinf >= 1) || p->dipole_corr < 0 || p->dipole_corr > 15)
+    return fail(ctx, MG_ERR_ARG, "epsinf must be >= 1, dipole_corr 0..15");
   if (t->nmol >= (1 << 23)) return fail(ctx, MG_ERR_SIZE, "too many molecules (limit 2^23-1)");
 
   ctx->precision = p->precision;
@@ -270,6 +289,26 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   ctx->cutoff = p->cutoff;
   ctx->alpha = p->alpha;
   ctx->epsinf = p->epsinf;
+  ctx->elcorr = p->dipole_corr;
+  {
+    // sim/ewald.c:869-887; the tin-foil term (epsinf >= 1e20) is below 1e-30 K
+    const double V = p->L[0] * p->L[1] * p->L[2];
+    if (ctx->elcorr & 7) {
+      for (int d = 0; d < 3; d++)
+        if (ctx->elcorr & (1 << d)) {
+          ctx->dipe[d] = 2 * M_PI / V;
+          ctx->dipc[d] = (ctx->elcorr & 8) ? 0 : 4 * M_PI / V;
+        }
+      ctx->dipole = true;
+    } else if (p->epsinf < 1e20) {
+      const double c = 4 * M_PI / (2 * p->epsinf + 1) / V;
+      for (int d = 0; d < 3; d++) {
+        ctx->dipc[d] = c;
+        ctx->dipe[d] = c / 2;
+      }
+      ctx->dipole = true;
+    }
+  }
   ctx->h = p->h > 0 ? p->h : 0.002;
   ctx->epsc = p->epsc > 0 ? p->epsc : 1e-7;
   ctx->omega = 0.5 * (p->omegac > 0 ? p->omegac : 1.2);
@@ -294,6 +333,8 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   ctx->tau_T = p->tau_T;
   ctx->seed = p->seed;
   ctx->skin = p->skin > 0 ? p->skin : 0;
+  ctx->drmax = std::fabs(p->drmax);
+  ctx->drift_step = p->drift_step != 0;
   ctx->normalize = p->no_normalize ? 0 : 1;
   ctx->box_r0 = p->box_rmin > 0 ? p->box_rmin : (p->box_rmin < 0 ? 0.0 : 0.15);
   ctx->nl_every = p->nl_every > 0 ? p->nl_every : 50;
@@ -419,7 +460,6 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   ctx->ncy = nc3[1];
   ctx->ncz = nc3[2];
   ctx->ncell = nc3[0] * nc3[1] * nc3[2];
-  while ((1 << ctx->sort_bits) < ctx->ncell) ctx->sort_bits++;
   std::vector<int4> st;
   if (allpairs) {
     st.push_back(make_int4(0, 0, 0, 0));
@@ -578,9 +618,12 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   CK(dalloc(&ctx->d_key_s, ns));
   CK(dalloc(&ctx->d_order, ns));
   CK(dalloc(&ctx->d_cell_start, ctx->ncell + 1));
-  CK(cub::DeviceRadixSort::SortPairs(nullptr, ctx->sort_tmp_bytes, ctx->d_key, ctx->d_key_s,
-                                     ctx->d_idx, ctx->d_order, ns, 0, ctx->sort_bits));
-  CK(cudaMalloc(&ctx->d_sort_tmp, ctx->sort_tmp_bytes));
+  {
+    const size_t nc4 = ((size_t)ctx->ncell + 3) / 4 * 4;
+    CK(dalloc(&ctx->d_ccount, nc4));
+    CK(cudaMemset(ctx->d_ccount, 0, nc4 * sizeof(int)));
+    CK(dalloc(&ctx->d_ccursor, ctx->ncell));
+  }
   CK(upload(&ctx->d_stencil, st.data(), st.size()));
   ctx->nxblocks = (t->nmol + EXCL_THREADS - 1) / EXCL_THREADS;
   ctx->nepart = std::max(ctx->ncell + ctx->nxblocks,
@@ -605,6 +648,7 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   }
   CK(upload(&ctx->d_qsite, qsite.data(), qsite.size()));
   CK(upload(&ctx->d_qval, qval.data(), qval.size()));
+  if (ctx->dipole) CK(dalloc(&ctx->d_dippart, 3 * (size_t)dipole_blocks(std::max(ctx->nq, 1))));
   CK(upload(&ctx->d_task, tasks.data(), tasks.size()));
   CK(upload(&ctx->d_col, cols.data(), cols.size()));
   CK(upload(&ctx->d_kvec, kvec.data(), kvec.size()));
@@ -710,6 +754,7 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   CK(upload(&ctx->d_imass, imass.data(), ns));
   CK(upload(&ctx->d_mass, mass.data(), ns));
   CK(dalloc(&ctx->d_kinpart, (size_t)(t->nmol + 127) / 128 + 1));
+  CK(dalloc(&ctx->d_meas, 13 * ((size_t)(t->nmol + 127) / 128 + 1)));
   // dependants: parents and dependants of one molecule, consecutive per
   // molecule, no dependant a parent, weights summing to 1 (cook fixes
   // other sums with a warning, cook/simdef.c:390)
@@ -766,8 +811,17 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   }
   CK(dalloc(&ctx->d_status, 1));
   CK(cudaMemset(ctx->d_status, 0, sizeof(int)));
-  CK(dalloc(&ctx->d_sums, 32));
-  CK(cudaMallocHost((void**)&ctx->h_sums, 32 * sizeof(double)));
+  if (ctx->drmax > 0) {
+    const unsigned int rep0[2] = {0u, 0x3f800000u};  // no site, factor 1.0f
+    CK(upload(&ctx->d_bdrep, rep0, 2));
+  }
+  ctx->total_mass = 0;
+  for (int i = 0; i < ns; i++) ctx->total_mass += t->mass[i];
+  CK(dalloc(&ctx->d_driftpart, 3 * (size_t)drift_blocks(ns)));
+  CK(dalloc(&ctx->d_drift, 6));
+  CK(dalloc(&ctx->d_sums, NSUMS));
+  CK(cudaMemset(ctx->d_sums, 0, NSUMS * sizeof(double)));
+  CK(cudaMallocHost((void**)&ctx->h_sums, NSUMS * sizeof(double)));
   return MG_OK;
 }
 
@@ -893,14 +947,10 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
   const bool rebuild = !ctx->use_list || ctx->need_build || ctx->since_build >= ctx->nl_every;
   if (rebuild) {
     // linked cells
-    PROF("cell_list", k_prep_cells(L, ns, r_dev, ctx->d_status, ctx->L[0], ctx->L[1], ctx->L[2],
-                                   ctx->ncx, ctx->ncy, ctx->ncz, ctx->d_key, ctx->d_idx));
-    PROF("cell_list", cub::DeviceRadixSort::SortPairs(ctx->d_sort_tmp, ctx->sort_tmp_bytes,
-                                                      ctx->d_key, ctx->d_key_s, ctx->d_idx,
-                                                      ctx->d_order, ns, 0, ctx->sort_bits,
-                                                      ctx->stream));
-    ctx->launches += 2;
-    PROF("cell_list", k_cell_bounds(L, ns, ctx->ncell, ctx->d_key_s, ctx->d_cell_start));
+    PROF("cell_list", k_cell_list(L, ns, r_dev, ctx->d_status, ctx->L[0], ctx->L[1], ctx->L[2],
+                                  ctx->ncx, ctx->ncy, ctx->ncz, ctx->d_key, ctx->d_ccount,
+                                  ctx->d_ccursor, ctx->d_idx, ctx->d_order, ctx->d_key_s,
+                                  ctx->d_cell_start));
   }
   PairArgs pa;
   pa.ns = ns;
@@ -1033,6 +1083,10 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
       PROF("ewald_kforce", k_kf_gemm_fp64(L, ka, (const double2*)ctx->d_tab));
     }
   }
+  // the dipole term (finite epsinf or Yeh-Berkowitz), after the k-space forces
+  if (ctx->dipole && ctx->nq > 0)
+    PROF("ewald_dipole", k_dipole(L, ka, r_dev, ctx->d_dippart, ctx->d_sums + 45, ctx->dipc,
+                                  f_dev));
   ctx->have_cells = true;
   if (measure) {
     PROF("reduce", k_reduce_sum(L, ctx->d_epart, nerows, 10, ctx->d_sums));
@@ -1074,6 +1128,27 @@ void add_drude_energy(mg_ctx* ctx, mg_energy* en) {
   for (int m = 0; m < 6; m++) en->Pvir[m] += s[22 + m];
 }
 
+// the dipole term's energy from the reduced moment M (h_sums[45..47]) and,
+// with Pv != NULL, its virial tensor added to Pv (sim/ewald.c:888-890: Edip on
+// the diagonal; the ADDFORCES terms q ek R of sim/ewaldf.c summed over the
+// charges give ek_a M_b)
+double dipole_energy(mg_ctx* ctx, double* Pv) {
+  if (!ctx->dipole) return 0;
+  const double* M = ctx->h_sums + 45;
+  double E = 0, ek[3];
+  for (int d = 0; d < 3; d++) {
+    E += ctx->dipe[d] * M[d] * M[d];
+    ek[d] = -ctx->dipc[d] * M[d];
+  }
+  if (Pv) {
+    for (int d = 0; d < 3; d++) Pv[d] += E + ek[d] * M[d];
+    Pv[3] += ek[1] * M[2];
+    Pv[4] += ek[2] * M[0];
+    Pv[5] += ek[0] * M[1];
+  }
+  return E;
+}
+
 // energies from the reduced sums (host, after the stream has been synchronized)
 void fill_energy(mg_ctx* ctx, mg_energy* en) {
   const double* s = ctx->h_sums;
@@ -1090,11 +1165,34 @@ void fill_energy(mg_ctx* ctx, mg_energy* en) {
   if (ctx->nq > 0) {
     for (int m = 0; m < 3; m++) en->Pvir[m] += Ek;
     for (int m = 0; m < 6; m++) en->Pvir[m] -= 2 / (4 * M_PI) * s[11 + m];
+    en->edip = dipole_energy(ctx, en->Pvir);
+    en->el += en->edip;
   }
 }
 
-ShakeArgs shake_args(mg_ctx* ctx) {
+// after a measured SHAKE step (energies and ekin already filled): cook's
+// measurePconstraints (sim/constrd.c:115-265) with the constraint virial of
+// the sweeps divided by h^2 (sim/constrd.c:1038-1040), the VERLET=3 kinetic
+// tensor scaled by 1/(2 h^2) (sim/constrd.c:1012-1017), No.Pkinq = 1 (cook's
+// corr without bit 4): Pvir = (force virial + constraint virial)/V,
+// Pkin = kinetic tensor/V, Ptens = Pvir + Pkin, and the pressure from the
+// scalar virial En.vir + En.virc + En.el (- 2 En.self with Drude charges),
+// cook's Pevir
+void fill_pressure(mg_ctx* ctx, mg_energy* en) {
+  const double* s = ctx->h_sums + 32;
+  const double hh = ctx->h * ctx->h, V = ctx->L[0] * ctx->L[1] * ctx->L[2];
+  en->virc = s[0] / hh;
+  for (int m = 0; m < 6; m++) {
+    en->Pkin[m] = s[7 + m] * (0.5 / hh) / V;
+    en->Ptens[m] = (en->Pvir[m] + s[1 + m] / hh) / V + en->Pkin[m];
+  }
+  const double vir = en->vir + en->virc + en->el - 2 * en->self;
+  en->P = (2 * en->ekin + vir) / (3 * V);
+}
+
+ShakeArgs shake_args(mg_ctx* ctx, bool measure) {
   ShakeArgs sa;
+  sa.meas_part = measure ? ctx->d_meas : nullptr;
   sa.nmol = ctx->nmol;
   sa.mol_first = ctx->d_mol_first;
   sa.mol_cfirst = ctx->d_mol_cfirst;
@@ -1158,16 +1256,23 @@ int md_step_enqueue(mg_ctx* ctx, bool measure) {
   int rc = forces_async(ctx, ctx->d_r, ctx->d_f, measure);
   if (rc) return rc;
   CK(k_depend_f(L, depend_args(ctx), ctx->d_f));
-  CK(k_shake(L, shake_args(ctx)));
+  CK(k_shake(L, shake_args(ctx, measure)));
   CK(k_depend_r(L, depend_args(ctx), ctx->d_r));
-  if (measure) CK(k_reduce_sum(L, ctx->d_kinpart, (ctx->nmol + 127) / 128, 1, ctx->d_sums + 17));
+  if (measure) {
+    CK(k_reduce_sum(L, ctx->d_kinpart, (ctx->nmol + 127) / 128, 1, ctx->d_sums + 17));
+    CK(k_reduce_sum(L, ctx->d_meas, (ctx->nmol + 127) / 128, 13, ctx->d_sums + 32));
+  }
   if (ctx->thermostat)
     CK(k_thermostat(L, thermo_args(ctx), ctx->d_kinpart, ctx->d_chi, ctx->d_r1));
+  if (ctx->drmax > 0) CK(k_bounddr(L, ctx->ns, ctx->drmax, ctx->d_r1, ctx->d_bdrep));
+  if (ctx->drift_step)
+    CK(k_remove_drift(L, ctx->ns, ctx->d_mass, ctx->total_mass, ctx->d_r1, ctx->d_driftpart,
+                      ctx->d_drift, nullptr));
   return MG_OK;
 }
 
 int fetch_sums(mg_ctx* ctx) {
-  CK(cudaMemcpyAsync(ctx->h_sums, ctx->d_sums, 32 * sizeof(double), cudaMemcpyDeviceToHost,
+  CK(cudaMemcpyAsync(ctx->h_sums, ctx->d_sums, NSUMS * sizeof(double), cudaMemcpyDeviceToHost,
                      ctx->stream));
   return MG_OK;
 }
@@ -1218,13 +1323,14 @@ int mg_destroy(mg_ctx* ctx) {
   if (!ctx) return MG_OK;
   void* bufs[] = {ctx->d_rs, ctx->d_fs, ctx->d_r,      ctx->d_f,       ctx->d_r1,    ctx->d_p,      ctx->d_kind,
                   ctx->d_mol,    ctx->d_key,     ctx->d_idx,   ctx->d_key_s,  ctx->d_order,
-                  ctx->d_cell_start, ctx->d_sort_tmp, ctx->d_pj, ctx->d_pd,  ctx->d_stencil,
+                  ctx->d_cell_start, ctx->d_ccount, ctx->d_ccursor, ctx->d_pj, ctx->d_pd,  ctx->d_stencil,
                   ctx->d_ptabf,  ctx->d_ptabd,   ctx->d_erd,   ctx->d_eru,    ctx->d_ert,
                   ctx->d_epart,  ctx->d_qsite,   ctx->d_qval,  ctx->d_task,   ctx->d_col,
                   ctx->d_kvec,   ctx->d_ekk,     ctx->d_S,     ctx->d_Wf,     ctx->d_Wd,
                   ctx->d_tab,    ctx->d_part,    ctx->d_ekpart, ctx->d_mol_first,
                   ctx->d_mol_cfirst, ctx->d_cons, ctx->d_bondq, ctx->d_imass, ctx->d_mass,
-                  ctx->d_kinpart, ctx->d_status, ctx->d_sums, ctx->d_krows,
+                  ctx->d_kinpart, ctx->d_meas, ctx->d_dippart, ctx->d_bdrep, ctx->d_driftpart,
+                  ctx->d_drift, ctx->d_status, ctx->d_sums, ctx->d_krows,
                   ctx->d_tiles, ctx->d_p1job, ctx->d_dsite, ctx->d_qdrude, ctx->d_qc,
                   ctx->d_qp, ctx->d_aqq, ctx->d_hist, ctx->d_drpart, ctx->d_pdj, ctx->d_pdd,
                   ctx->d_nlist, ctx->d_ncount, ctx->d_rbuild, ctx->d_dmax,
@@ -1354,8 +1460,10 @@ int mg_ewald(mg_ctx* ctx, const double* r, double* f, double* energy) {
       CK(k_kf_gemm_fp64(L, ka, (const double2*)ctx->d_tab));
     }
     CK(k_reduce_sum(L, ctx->d_ekpart, ctx->nkblocks, 7, ctx->d_sums + 10));
+    if (ctx->dipole)
+      CK(k_dipole(L, ka, ctx->d_rs, ctx->d_dippart, ctx->d_sums + 45, ctx->dipc, ctx->d_fs));
   }
-  std::vector<double> fk(3 * (size_t)ctx->ns);
+  std::vector<double> fk(nb / sizeof(double));
   CK(cudaMemcpyAsync(fk.data(), ctx->d_fs, nb, cudaMemcpyDeviceToHost, ctx->stream));
   int rc = fetch_sums(ctx);
   if (rc) return rc;
@@ -1365,7 +1473,9 @@ int mg_ewald(mg_ctx* ctx, const double* r, double* f, double* energy) {
   rc = check_status(ctx);
   if (rc) return rc;
   for (size_t i = 0; i < fk.size(); i++) f[i] += fk[i];
-  if (energy) *energy = (ctx->nq > 0 ? ctx->h_sums[10] / (4 * M_PI) : 0) + ctx->eself;
+  if (energy)
+    *energy = (ctx->nq > 0 ? ctx->h_sums[10] / (4 * M_PI) + dipole_energy(ctx, nullptr) : 0) +
+              ctx->eself;
   return MG_OK;
 }
 
@@ -1424,6 +1534,36 @@ int mg_md_get_state(mg_ctx* ctx, double* r, double* r1) {
   return MG_OK;
 }
 
+int mg_remove_drift(mg_ctx* ctx, double vdrift[3]) {
+  if (!ctx || !ctx->have_state) return fail(ctx, MG_ERR_ARG, "no MD state");
+  Launch L = launch(ctx);
+  CK(k_remove_drift(L, ctx->ns, ctx->d_mass, ctx->total_mass, ctx->d_r1, ctx->d_driftpart,
+                    ctx->d_drift, ctx->d_drift + 3));
+  double v[3];
+  CK(cudaMemcpyAsync(v, ctx->d_drift + 3, sizeof(v), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (vdrift)
+    for (int d = 0; d < 3; d++) vdrift[d] = v[d] / ctx->h;
+  return MG_OK;
+}
+
+int mg_bounddr_report(mg_ctx* ctx, long long* nreduced, double* minfactor) {
+  if (!ctx) return MG_ERR_ARG;
+  unsigned int rep[2] = {0u, 0x3f800000u};
+  if (ctx->d_bdrep) {
+    CK(cudaMemcpyAsync(rep, ctx->d_bdrep, sizeof(rep), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const unsigned int rep0[2] = {0u, 0x3f800000u};
+    CK(cudaMemcpyAsync(ctx->d_bdrep, rep0, sizeof(rep0), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  float q;
+  std::memcpy(&q, rep + 1, sizeof(q));
+  if (nreduced) *nreduced = rep[0];
+  if (minfactor) *minfactor = q;
+  return MG_OK;
+}
+
 int mg_playback_frame(mg_ctx* ctx, int what, int flags, float* frame) {
   if (!ctx || !frame) return fail(ctx, MG_ERR_ARG, "null argument");
   if (!ctx->have_state) return fail(ctx, MG_ERR_ARG, "no MD state");
@@ -1446,7 +1586,6 @@ int mg_md_steps(mg_ctx* ctx, int nsteps, mg_energy* en) {
   if (!ctx || !ctx->have_state || nsteps < 0) return fail(ctx, MG_ERR_ARG, "no MD state");
   ctx->launches = 0;
   Launch L = launch(ctx);
-  const ShakeArgs sa = shake_args(ctx);
   const int nkin = (ctx->nmol + 127) / 128;
   for (int s = 0; s < nsteps; s++) {
     const bool last = s == nsteps - 1;
@@ -1495,7 +1634,7 @@ int mg_md_steps(mg_ctx* ctx, int nsteps, mg_energy* en) {
     // and dependant positions for the next force evaluation: the same
     // positions cook's depend_r makes at the start of its next step
     if (ctx->ndep > 0) PROF("depend", k_depend_f(L, depend_args(ctx), ctx->d_f));
-    PROF("shake", k_shake(L, sa));
+    PROF("shake", k_shake(L, shake_args(ctx, measure)));
     if (ctx->ndep > 0) PROF("depend", k_depend_r(L, depend_args(ctx), ctx->d_r));
     if (ctx->use_list) {
       ctx->since_build++;
@@ -1507,9 +1646,21 @@ int mg_md_steps(mg_ctx* ctx, int nsteps, mg_energy* en) {
       CK(cudaEventRecord(ctx->ev_dmax, ctx->stream));
       ctx->dmax_pending = true;
     }
-    if (measure) PROF("reduce", k_reduce_sum(L, ctx->d_kinpart, nkin, 1, ctx->d_sums + 17));
+    if (measure) {
+      PROF("reduce", k_reduce_sum(L, ctx->d_kinpart, nkin, 1, ctx->d_sums + 17));
+      PROF("reduce", k_reduce_sum(L, ctx->d_meas, nkin, 13, ctx->d_sums + 32));
+    }
     if (ctx->thermostat)
       PROF("thermostat", k_thermostat(L, thermo_args(ctx), ctx->d_kinpart, ctx->d_chi, ctx->d_r1));
+    // cook calls bounddr after Shake (and its thermostat) and normalize
+    // (sim/main.c:1607-1623)
+    if (ctx->drmax > 0)
+      PROF("bounddr", k_bounddr(L, ctx->ns, ctx->drmax, ctx->d_r1, ctx->d_bdrep));
+    // then the momentum drift (cook's removedrifts with DRIFT_STEP,
+    // sim/main.c:1626)
+    if (ctx->drift_step)
+      PROF("drift", k_remove_drift(L, ctx->ns, ctx->d_mass, ctx->total_mass, ctx->d_r1,
+                                   ctx->d_driftpart, ctx->d_drift, nullptr));
   }
   if (en) {
     int rc = fetch_sums(ctx);
@@ -1525,6 +1676,7 @@ int mg_md_steps(mg_ctx* ctx, int nsteps, mg_energy* en) {
     fill_energy(ctx, en);
     if (ctx->polar && ctx->nd > 0) add_drude_energy(ctx, en);
     en->ekin = ctx->h_sums[17] / (ctx->h * ctx->h) / 4;
+    fill_pressure(ctx, en);
   }
   return MG_OK;
 }
@@ -1856,9 +2008,10 @@ KArgs kspace_args(mg_ctx* ctx) {
 
 int mg_adjoint(mg_ctx* ctx, const double* r, const double* g, mg_adjoint_out* out) {
   if (!ctx || !r || !out) return fail(ctx, MG_ERR_ARG, "null argument");
-  if (ctx->precision != MG_FP64 || ctx->polar || ctx->use_list)
+  if (ctx->precision != MG_FP64 || ctx->polar || ctx->use_list || ctx->dipole)
     return fail(ctx, MG_ERR_ARG,
-                "the adjoint needs an FP64, non-polar context with cells re-binned (skin <= 0)");
+                "the adjoint needs an FP64, non-polar, tin-foil context with cells re-binned "
+                "(skin <= 0)");
   const int ns = ctx->ns, nk2 = ctx->nkind * ctx->nkind, nt = ctx->ntypes;
   if (!ctx->d_adjtab) {
     // per pair of kinds: the smoothed-LJ constants, their sigma derivatives
@@ -2241,6 +2394,7 @@ int mg_batch_md_steps(mg_batch* b, int nsteps, mg_energy* en) {
     if (en) {
       fill_energy(c, &en[i]);
       en[i].ekin = c->h_sums[17] / (c->h * c->h) / 4;
+      fill_pressure(c, &en[i]);
     }
   }
   return MG_OK;

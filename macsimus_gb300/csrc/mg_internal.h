@@ -83,11 +83,13 @@ struct Launch {
 };
 
 // kernels (mg_kernels.cu); each returns cudaGetLastError()
-cudaError_t k_prep_cells(const Launch& L, int ns, const double* r, int* status,
-                         double Lx, double Ly, double Lz, int ncx, int ncy, int ncz,
-                         int* cellkey, int* idx);
-cudaError_t k_cell_bounds(const Launch& L, int ns, int ncell, const int* key_sorted,
-                          int* cell_start);
+// the linked-cell list as a counting sort (four kernels): key [ns] cell of
+// every site; count [ncell rounded up to 4] zero on entry and on return;
+// cursor [ncell], slot_site [ns] scratch; out: order [ns] sorted -> site
+// (site order within a cell), key_s [ns] the sorted cells, start [ncell+1]
+cudaError_t k_cell_list(const Launch& L, int ns, const double* r, int* status, double Lx,
+                        double Ly, double Lz, int ncx, int ncy, int ncz, int* key, int* count,
+                        int* cursor, int* slot_site, int* order, int* key_s, int* start);
 cudaError_t k_gather_mixed(const Launch& L, int ns, const double* r, const int* order,
                            const int* kind, const int* mol, double Lx, double Ly, double Lz,
                            int4* pj);
@@ -163,6 +165,11 @@ cudaError_t k_sk_gemm_fp64(const Launch& L, const KArgs& a, const double2* tab, 
 cudaError_t k_kf_gemm_mixed(const Launch& L, const KArgs& a, const float2* tab);
 cudaError_t k_kf_gemm_fp64(const Launch& L, const KArgs& a, const double2* tab);
 cudaError_t k_reduce_sum(const Launch& L, const double* part, int nrows, int width, double* out);
+// the dipole term of Ewald(2): M = sum q r into M[0..2] (part: [dipole_blocks(nq) * 3]
+// scratch), then forces q (-c_d M_d) added to f (none when c is zero)
+int dipole_blocks(int nq);
+cudaError_t k_dipole(const Launch& L, const KArgs& a, const double* r, double* part, double* M,
+                     const double c[3], double* f);
 // pass 2 on the tensor cores (mg_kspace_tc.cu); KP = 2 Kz + 1 rounded up
 // to 8; per k row (kx, ky) as floats and the offsets of X(kx), Y(ky) in the
 // kernel's phase block
@@ -207,6 +214,9 @@ struct ShakeArgs {
   const double* f;
   double* p;           // scratch [3*ns]
   double* kin_part;    // [nblocks]
+  // measured step (or null): per CTA [nblocks * 13] the constraint virial
+  // sum, its tensor (xx yy zz yz zx xy) and the kinetic tensor sum
+  double* meas_part;
   int* status;         // set to 1 on non-convergence
   // molecule wrapping after the step (cook's normalize): a molecule whose
   // lowest massive-site coordinate is outside [r0, r0 + L) moves by L
@@ -323,6 +333,14 @@ struct ThermoArgs {
   double* nh;            // Nose-Hoover state (NoseSlot), kind 3
   int pred;              // Nose-Hoover predictor length
 };
+// cook's bounddr: r1 of every site limited to length drmax; rep[0] counts
+// the sites reduced, rep[1] keeps the float bits of the smallest factor
+cudaError_t k_bounddr(const Launch& L, int ns, double drmax, double* r1, unsigned int* rep);
+// momentum drift removal: part [drift_blocks(ns) * 3] scratch, P [3] the
+// summed momentum, vout [3] (or null) the drift per step that was removed
+int drift_blocks(int ns);
+cudaError_t k_remove_drift(const Launch& L, int ns, const double* mass, double total_mass,
+                           double* r1, double* part, double* P, double* vout);
 cudaError_t k_thermostat(const Launch& L, const ThermoArgs& a, const double* kin_part,
                          double* chi_part, double* r1);
 

@@ -20,8 +20,6 @@
 #include "mg_internal.h"
 #include "mg_device.cuh"
 
-#include <cub/device/device_radix_sort.cuh>
-
 namespace mg {
 
 #define LAUNCHED(L) (++*(L).counter)
@@ -36,11 +34,26 @@ __device__ __forceinline__ int cell_coord(double s, int n) {
   return c < 0 ? 0 : (c >= n ? n - 1 : c);
 }
 
+// ------------------------------------------------------ the cell list --
+//
+// cook threads the sites of every cell into a linked list
+// (cook/linklist.c:38-269).  Here the cells are runs of one array: the sites
+// sorted by cell, in increasing site order within a cell (a stable sort, so
+// the order and every sum over it are the same run to run), cell c holding
+// order[start[c] .. start[c+1]).  A counting sort in four kernels:
+//   cell_count    key of every site, sites per cell (atomic increments)
+//   cell_scan     one CTA: start = exclusive scan of the counts, cursor =
+//                 start, the counts zeroed again for the next list
+//   cell_scatter  every site into a free slot of its cell (atomic cursor)
+//   cell_order    a warp per cell ranks its sites by site index and writes
+//                 order[] and the sorted keys (the slots of cell_scatter
+//                 depend on the timing of the atomics; the ranks do not)
+
 // cell key of every site; a non-finite coordinate sets bit 1 of *status and
 // the site is binned into cell 0 so that every later index stays in range
-__global__ void prep_cells_kernel(int ns, const double* __restrict__ r, double Lx, double Ly,
+__global__ void cell_count_kernel(int ns, const double* __restrict__ r, double Lx, double Ly,
                                   double Lz, int ncx, int ncy, int ncz, int* __restrict__ key,
-                                  int* __restrict__ idx, int* __restrict__ status) {
+                                  int* __restrict__ count, int* __restrict__ status) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ns) return;
   const double x = r[3 * i], y = r[3 * i + 1], z = r[3 * i + 2];
@@ -53,35 +66,117 @@ __global__ void prep_cells_kernel(int ns, const double* __restrict__ r, double L
     atomicOr(status, 2);
   }
   key[i] = k;
-  idx[i] = i;
+  atomicAdd(count + k, 1);
 }
 
-cudaError_t k_prep_cells(const Launch& L, int ns, const double* r, int* status, double Lx,
-                         double Ly, double Lz, int ncx, int ncy, int ncz, int* cellkey, int* idx) {
-  prep_cells_kernel<<<cdiv(ns, 256), 256, 0, L.s>>>(ns, r, Lx, Ly, Lz, ncx, ncy, ncz, cellkey, idx,
+// exclusive scan of count[0..ncell) into start[0..ncell] and cursor[], in
+// tiles of 4 x 1024 counts (int4 loads; count is padded with zeros to a
+// multiple of 4 entries); the counts are cleared for the next list
+constexpr int SCAN_THREADS = 1024;
+__global__ void __launch_bounds__(SCAN_THREADS)
+cell_scan_kernel(int ncell, int* __restrict__ count, int* __restrict__ start,
+                 int* __restrict__ cursor) {
+  __shared__ int wsum[SCAN_THREADS / 32];
+  __shared__ int carry_s;
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  if (t == 0) carry_s = 0;
+  __syncthreads();
+  const int n4 = (ncell + 3) / 4;
+  for (int base = 0; base < n4; base += SCAN_THREADS) {
+    const int q = base + t;
+    int4 v = make_int4(0, 0, 0, 0);
+    if (q < n4) {
+      v = reinterpret_cast<int4*>(count)[q];
+      reinterpret_cast<int4*>(count)[q] = make_int4(0, 0, 0, 0);
+    }
+    const int tot = v.x + v.y + v.z + v.w;
+    int incl = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[w] = incl;
+    const int carry = carry_s;
+    __syncthreads();
+    if (w == 0) {
+      int x = wsum[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      wsum[lane] = x;   // inclusive sums of the warps
+    }
+    __syncthreads();
+    const int ex = carry + (w ? wsum[w - 1] : 0) + incl - tot;
+    if (q < n4) {
+      const int e[4] = {ex, ex + v.x, ex + v.x + v.y, ex + v.x + v.y + v.z};
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+        if (4 * q + k < ncell) {
+          start[4 * q + k] = e[k];
+          cursor[4 * q + k] = e[k];
+        }
+    }
+    __syncthreads();
+    if (t == SCAN_THREADS - 1) carry_s = carry + wsum[31];
+    __syncthreads();
+  }
+  if (t == 0) start[ncell] = carry_s;
+}
+
+__global__ void cell_scatter_kernel(int ns, const int* __restrict__ key, int* __restrict__ cursor,
+                                    int* __restrict__ slot_site) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ns) return;
+  slot_site[atomicAdd(cursor + key[i], 1)] = i;
+}
+
+constexpr int ORDER_THREADS = 256;
+__global__ void __launch_bounds__(ORDER_THREADS)
+cell_order_kernel(int ncell, const int* __restrict__ start, const int* __restrict__ slot_site,
+                  int* __restrict__ order, int* __restrict__ key_s) {
+  const int c = blockIdx.x * (ORDER_THREADS / 32) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (c >= ncell) return;
+  const int s0 = start[c], n = start[c + 1] - s0;
+  if (n <= 32) {
+    // one site per lane, ranks by shuffles
+    const int mine = lane < n ? slot_site[s0 + lane] : 0x7fffffff;
+    int rank = 0;
+    for (int j = 0; j < n; j++) rank += __shfl_sync(0xffffffffu, mine, j) < mine;
+    if (lane < n) {
+      order[s0 + rank] = mine;
+      key_s[s0 + rank] = c;
+    }
+  } else {
+    for (int e = lane; e < n; e += 32) {
+      const int mine = slot_site[s0 + e];
+      int rank = 0;
+      for (int j = 0; j < n; j++) rank += slot_site[s0 + j] < mine;
+      order[s0 + rank] = mine;
+      key_s[s0 + rank] = c;
+    }
+  }
+}
+
+cudaError_t k_cell_list(const Launch& L, int ns, const double* r, int* status, double Lx,
+                        double Ly, double Lz, int ncx, int ncy, int ncz, int* key, int* count,
+                        int* cursor, int* slot_site, int* order, int* key_s, int* start) {
+  const int ncell = ncx * ncy * ncz;
+  cell_count_kernel<<<cdiv(ns, 256), 256, 0, L.s>>>(ns, r, Lx, Ly, Lz, ncx, ncy, ncz, key, count,
                                                     status);
   LAUNCHED(L);
-  return cudaGetLastError();
-}
-
-__global__ void cell_bounds_kernel(int ns, int ncell, const int* __restrict__ key,
-                                   int* __restrict__ start) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ns) return;
-  int k = key[t];
-  int prev = t ? key[t - 1] : -1;
-  for (int c = prev + 1; c <= k; c++) start[c] = t;
-  if (t == ns - 1)
-    for (int c = k + 1; c <= ncell; c++) start[c] = ns;
-}
-
-cudaError_t k_cell_bounds(const Launch& L, int ns, int ncell, const int* key_sorted,
-                          int* cell_start) {
-  cell_bounds_kernel<<<cdiv(ns, 256), 256, 0, L.s>>>(ns, ncell, key_sorted, cell_start);
+  cell_scan_kernel<<<1, SCAN_THREADS, 0, L.s>>>(ncell, count, start, cursor);
+  LAUNCHED(L);
+  cell_scatter_kernel<<<cdiv(ns, 256), 256, 0, L.s>>>(ns, key, cursor, slot_site);
+  LAUNCHED(L);
+  cell_order_kernel<<<cdiv(ncell, ORDER_THREADS / 32), ORDER_THREADS, 0, L.s>>>(
+      ncell, start, slot_site, order, key_s);
   LAUNCHED(L);
   return cudaGetLastError();
 }
-
 
 __global__ void gather_mixed_kernel(int ns, const double* __restrict__ r,
                                     const int* __restrict__ order, const int* __restrict__ kind,
@@ -1090,11 +1185,47 @@ __device__ __forceinline__ double nose_dof(const ShakeArgs& a, const NoseStep& q
   return -q.vf * v;
 }
 
-template <bool NOSE>
+// the measured quantities of a SHAKE step (MEAS): cook's En.virc and
+// PTvirc (sim/virc.c, summed over the sweeps before the division by h^2 of
+// sim/constrd.c:1038-1040) and the VERLET=3 kinetic tensor sum
+// m (V1 V1 + V2 V2) of sim/shakev3.c:20-32 (before hscale), per molecule
+struct ShakeMeas {
+  double virc, pt[6], pk[6];
+};
+__device__ __forceinline__ void meas_zero(ShakeMeas& m) {
+  m.virc = 0;
+#pragma unroll
+  for (int k = 0; k < 6; k++) m.pt[k] = m.pk[k] = 0;
+}
+// constraint virial of one constraint: virc += sq, PTvirc += (sq/bondq) rij rij
+// (xx yy zz yz zx xy); sq = the sweep sum of (bondq - |pij|^2) omega/(mi+mj)
+__device__ __forceinline__ void meas_cons(ShakeMeas& m, double sq, double sqb, double x, double y,
+                                          double z) {
+  m.virc += sq;
+  m.pt[0] += sqb * (x * x);
+  m.pt[1] += sqb * (y * y);
+  m.pt[2] += sqb * (z * z);
+  m.pt[3] += sqb * (y * z);
+  m.pt[4] += sqb * (z * x);
+  m.pt[5] += sqb * (x * y);
+}
+__device__ __forceinline__ void meas_kin(ShakeMeas& m, double mi, double v1x, double v1y,
+                                         double v1z, double v2x, double v2y, double v2z) {
+  m.pk[0] += (v1x * v1x + v2x * v2x) * mi;
+  m.pk[1] += (v1y * v1y + v2y * v2y) * mi;
+  m.pk[2] += (v1z * v1z + v2z * v2z) * mi;
+  m.pk[3] += (v1y * v1z + v2y * v2z) * mi;
+  m.pk[4] += (v1z * v1x + v2z * v2x) * mi;
+  m.pk[5] += (v1x * v1y + v2x * v2y) * mi;
+}
+
+template <bool NOSE, bool MEAS>
 __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
   __shared__ double red[SH_THREADS];
   const int n = blockIdx.x * SH_THREADS + threadIdx.x;
   double kin = 0;
+  [[maybe_unused]] ShakeMeas ms;
+  if constexpr (MEAS) meas_zero(ms);
   [[maybe_unused]] NoseStep nose;
   if constexpr (NOSE) nose = nose_begin(a);
   if (n < a.nmol) {
@@ -1126,6 +1257,7 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
       // into the two displacements along r_ij
       int ci[3], cj[3];
       double bq[3], tol[3], awi[3], awj[3], rx[3], ry[3], rz[3];
+      [[maybe_unused]] double dsum[3] = {0, 0, 0};
 #pragma unroll
       for (int q = 0; q < 3; q++) {
         const int2 ij = a.cons[c0 + q];
@@ -1153,11 +1285,20 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
           const double px = pi.x - pj.x, py = pi.y - pj.y, pz = pi.z - pj.z;
           const double d = bq[q] - (px * px + py * py + pz * pz);
           over |= fabs(d) > tol[q];
+          if constexpr (MEAS) dsum[q] += d;
           sh_add(ci[q], P[0], P[1], P[2], d * awi[q], rx[q], ry[q], rz[q]);
           sh_add(cj[q], P[0], P[1], P[2], d * awj[q], rx[q], ry[q], rz[q]);
         }
       } while (over && it < a.maxit);
       if (over) atomicOr(a.status, 1);
+      if constexpr (MEAS) {
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+          const int2 ij = a.cons[c0 + q];
+          const double wb = a.omega / (a.imass[ij.x] + a.imass[ij.y]);
+          meas_cons(ms, dsum[q] * wb, dsum[q] * wb / bq[q], rx[q], ry[q], rz[q]);
+        }
+      }
       double sx = 0, sy = 0, sz = 0;
       if (a.normalize) {
         double lx = 9e9, ly = 9e9, lz = 9e9;
@@ -1185,6 +1326,7 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
         v1s += v1z * v1z;
         v2s += v2z * v2z;
         kin += (v1s + v2s) * a.mass[i];
+        if constexpr (MEAS) meas_kin(ms, a.mass[i], v1x, v1y, v1z, v2x, v2y, v2z);
         a.r1[3 * i] = v2x;
         a.r1[3 * i + 1] = v2y;
         a.r1[3 * i + 2] = v2z;
@@ -1218,6 +1360,9 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
           const double d = bq - (px * px + py * py + pz * pz);
           maxsq = fmax(maxsq, fabs(d) * ibq);
           const double sq = d * wq;
+          if constexpr (MEAS)
+            meas_cons(ms, d * (a.omega / (mi + mj)), sq, a.r[3 * ij.x] - a.r[3 * ij.y],
+                      a.r[3 * ij.x + 1] - a.r[3 * ij.y + 1], a.r[3 * ij.x + 2] - a.r[3 * ij.y + 2]);
           const double rx = (a.r[3 * ij.x] - a.r[3 * ij.y]) * sq,
                        ry = (a.r[3 * ij.x + 1] - a.r[3 * ij.y + 1]) * sq,
                        rz = (a.r[3 * ij.x + 2] - a.r[3 * ij.y + 2]) * sq;
@@ -1240,15 +1385,17 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
         sh[k] = wrap_shift(lo, a.r0, a.Lb[k]);
       }
     for (int i = i0; i < i1; i++) {
-      double v1s = 0, v2s = 0;
+      double v1s = 0, v2s = 0, v1[3], v2[3];
       for (int k = 0; k < 3; k++) {
-        const double v1 = a.r1[3 * i + k], v2 = p[3 * i + k] - a.r[3 * i + k];
-        v1s += v1 * v1;
-        v2s += v2 * v2;
-        a.r1[3 * i + k] = v2;
+        v1[k] = a.r1[3 * i + k];
+        v2[k] = p[3 * i + k] - a.r[3 * i + k];
+        v1s += v1[k] * v1[k];
+        v2s += v2[k] * v2[k];
+        a.r1[3 * i + k] = v2[k];
         a.r[3 * i + k] = p[3 * i + k] + sh[k];
       }
       kin += (v1s + v2s) * a.mass[i];
+      if constexpr (MEAS) meas_kin(ms, a.mass[i], v1[0], v1[1], v1[2], v2[0], v2[1], v2[2]);
     }
     }
   }
@@ -1259,13 +1406,47 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
     __syncthreads();
   }
   if (threadIdx.x == 0) a.kin_part[blockIdx.x] = red[0];
+  if constexpr (MEAS) {
+    // the 13 measured sums of the CTA in a fixed order: a shuffle tree per
+    // warp, then the warps' sums in warp order (red[] is free again)
+    __syncthreads();
+    double v[13];
+    v[0] = ms.virc;
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+      v[1 + k] = ms.pt[k];
+      v[7 + k] = ms.pk[k];
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 13; k++) {
+      double x = v[k];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      if (lane == 0) red[wid * 13 + k] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < 13) {
+      double x = 0;
+      for (int w = 0; w < SH_THREADS / 32; w++) x += red[w * 13 + threadIdx.x];
+      a.meas_part[(long)blockIdx.x * 13 + threadIdx.x] = x;
+    }
+  }
 }
 
 cudaError_t k_shake(const Launch& L, const ShakeArgs& a) {
-  if (a.vhist)
-    shake_kernel<true><<<cdiv(a.nmol, SH_THREADS), SH_THREADS, 0, L.s>>>(a);
-  else
-    shake_kernel<false><<<cdiv(a.nmol, SH_THREADS), SH_THREADS, 0, L.s>>>(a);
+  const int nb = cdiv(a.nmol, SH_THREADS);
+  if (a.vhist) {
+    if (a.meas_part)
+      shake_kernel<true, true><<<nb, SH_THREADS, 0, L.s>>>(a);
+    else
+      shake_kernel<true, false><<<nb, SH_THREADS, 0, L.s>>>(a);
+  } else {
+    if (a.meas_part)
+      shake_kernel<false, true><<<nb, SH_THREADS, 0, L.s>>>(a);
+    else
+      shake_kernel<false, false><<<nb, SH_THREADS, 0, L.s>>>(a);
+  }
   LAUNCHED(L);
   return cudaGetLastError();
 }

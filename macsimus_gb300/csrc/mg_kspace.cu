@@ -620,4 +620,76 @@ cudaError_t k_kf_gemm_fp64(const Launch& L, const KArgs& a, const double2* tab) 
   return launch_kf_gemm<double2>(L, a, tab, a.Wd);
 }
 
+// ----------------------------------------------------- the dipole term --
+//
+// Ewald(2)'s dipole term (sim/ewald.c:865-887, forces through the ADDFORCES
+// of sim/ewaldf.c): with M = sum_i q_i r_i over the charges (Drude charges
+// at r + rpol), every charge gets the force q_i ek, ek = -c M (isotropic:
+// c = 4 pi / ((2 epsinf + 1) V); Yeh-Berkowitz: c = 4 pi / V on the selected
+// axes, no force with bit 8).  FP64 throughout, M summed in a fixed order.
+
+__device__ __forceinline__ void charge_position(const KArgs& a, const double* __restrict__ r,
+                                                int j, double p[3]) {
+  const int site = a.qsite[j];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    p[d] = r[3 * (long)site + d];
+    if (a.qdrude && a.qdrude[j]) p[d] += r[3 * (long)a.ns + 3 * (long)site + d];
+  }
+}
+
+constexpr int DIP_THREADS = 256;
+__global__ void __launch_bounds__(DIP_THREADS)
+dipole_moment_kernel(KArgs a, const double* __restrict__ r, double* __restrict__ part) {
+  __shared__ double red[3][DIP_THREADS];
+  const int j = blockIdx.x * DIP_THREADS + threadIdx.x;
+  double m[3] = {0, 0, 0};
+  if (j < a.nq) {
+    double p[3];
+    charge_position(a, r, j, p);
+    const double q = a.qval[j];
+#pragma unroll
+    for (int d = 0; d < 3; d++) m[d] = q * p[d];
+  }
+#pragma unroll
+  for (int d = 0; d < 3; d++) red[d][threadIdx.x] = m[d];
+  __syncthreads();
+  for (int w = DIP_THREADS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+#pragma unroll
+      for (int d = 0; d < 3; d++) red[d][threadIdx.x] += red[d][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < 3) part[3 * (long)blockIdx.x + threadIdx.x] = red[threadIdx.x][0];
+}
+
+// forces q_i ek; ek from the reduced moment M (device) and the factors
+__global__ void dipole_force_kernel(KArgs a, const double* __restrict__ M, double c0, double c1,
+                                    double c2, double* __restrict__ f) {
+  const int j = blockIdx.x * DIP_THREADS + threadIdx.x;
+  if (j >= a.nq) return;
+  const double q = a.qval[j];
+  const int site = a.qsite[j];
+  double* fo = f + 3 * (long)site + (a.qdrude && a.qdrude[j] ? 3 * (long)a.ns : 0);
+  fo[0] += q * (-c0 * M[0]);
+  fo[1] += q * (-c1 * M[1]);
+  fo[2] += q * (-c2 * M[2]);
+}
+
+int dipole_blocks(int nq) { return (nq + DIP_THREADS - 1) / DIP_THREADS; }
+
+cudaError_t k_dipole(const Launch& L, const KArgs& a, const double* r, double* part, double* M,
+                     const double c[3], double* f) {
+  const int nb = dipole_blocks(a.nq);
+  dipole_moment_kernel<<<nb, DIP_THREADS, 0, L.s>>>(a, r, part);
+  ++*L.counter;
+  cudaError_t e = k_reduce_sum(L, part, nb, 3, M);
+  if (e != cudaSuccess) return e;
+  if (c[0] != 0 || c[1] != 0 || c[2] != 0) {
+    dipole_force_kernel<<<nb, DIP_THREADS, 0, L.s>>>(a, M, c[0], c[1], c[2], f);
+    ++*L.counter;
+  }
+  return cudaGetLastError();
+}
+
 }  // namespace mg

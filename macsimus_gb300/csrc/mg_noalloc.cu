@@ -10,10 +10,11 @@
 // keeps it resident until the process exits.  Host-side k tables are built in
 // static host buffers, so no call allocates on the host either.
 //
-// The host cannot use the array's name as a device address: on the first
-// call on a device the code below asks the runtime for that device's address
-// of the array (cudaGetSymbolAddress, with the device current) and keeps it
-// for later calls on the same device.
+// The host cannot use the array's name as a device address: every call asks
+// the runtime for the current device's address of the array
+// (cudaGetSymbolAddress, with that device current; the lookup is cheap and
+// stays right when the device's context is reset and the module reloaded),
+// together with the device's SM count, which sizes the pass-1 split.
 #include "../../include/macgpu.h"
 #include "mg_internal.h"
 
@@ -58,8 +59,6 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[SCRATCH_BYTES];
 
 namespace {
 
-constexpr int MAXDEV = 64;
-unsigned char* g_dev_ptr[MAXDEV];  // device address of g_noalloc_scratch per device
 // errors are returned as status codes and described on stderr
 int fail_na(int code, const char* msg) {
   fprintf(stderr, "%s\n", msg);
@@ -125,6 +124,21 @@ __global__ void iota_kernel(int n, int* __restrict__ out) {
   if (i < n) out[i] = i;
 }
 
+// sum of q^2 over the charges in a fixed order (one CTA; the self term)
+constexpr int SQ_THREADS = 256;
+__global__ void sumq2_kernel(int n, const double* __restrict__ q, double* __restrict__ out) {
+  __shared__ double red[SQ_THREADS];
+  double s = 0;
+  for (int i = threadIdx.x; i < n; i += SQ_THREADS) s += q[i] * q[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = SQ_THREADS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+
 }  // namespace
 
 extern "C" int mg_ewald_kspace_noalloc(const double* r_dev, const double* q_dev, int nq,
@@ -135,18 +149,16 @@ extern "C" int mg_ewald_kspace_noalloc(const double* r_dev, const double* q_dev,
   if (nq > MAXQ)
     return fail_na(MG_ERR_SIZE, "mg_ewald_kspace_noalloc: more charges than MG_NOALLOC_MAX_CHARGES");
   cudaStream_t s = (cudaStream_t)stream;
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAXDEV)
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm < 1)
     return fail_na(MG_ERR_CUDA, "mg_ewald_kspace_noalloc: no usable current device");
-  if (!g_dev_ptr[dev]) {
-    // set-up, once per device, with that device current
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-      return fail_na(MG_ERR_CUDA, "mg_ewald_kspace_noalloc: cudaGetSymbolAddress failed");
-    g_dev_ptr[dev] = (unsigned char*)p;
-  }
-  unsigned char* base = g_dev_ptr[dev];
+  // the current device's address of the scratch array (the current device
+  // is the one the kernels below run on)
+  void* sym = nullptr;
+  if (cudaGetSymbolAddress(&sym, g_noalloc_scratch) != cudaSuccess || !sym)
+    return fail_na(MG_ERR_CUDA, "mg_ewald_kspace_noalloc: cudaGetSymbolAddress failed");
+  unsigned char* base = (unsigned char*)sym;
 
   // ---- k tables on the host (static buffers)
   double kap = kappa;
@@ -192,8 +204,20 @@ extern "C" int mg_ewald_kspace_noalloc(const double* r_dev, const double* q_dev,
     i = j;
   }
   auto ext = [](const KRow& r) { return std::max(std::abs(r.kzlo), std::abs(r.kzhi)); };
-  std::stable_sort(h_rows, h_rows + nrows,
-                   [&](const KRow& x, const KRow& y) { return ext(x) > ext(y); });
+  // rows by decreasing kz extent, stable: a counting sort over the extents
+  // (std::stable_sort may take a temporary buffer from the heap)
+  {
+    static KRow tmp[MAXK];
+    static int cnt[MAXK + 2];
+    int emax = 0;
+    for (int i = 0; i < nrows; i++) emax = std::max(emax, ext(h_rows[i]));
+    if (emax > MAXK) return fail_na(MG_ERR_SIZE, "mg_ewald_kspace_noalloc: k set too long in z");
+    std::fill(cnt, cnt + emax + 2, 0);
+    for (int i = 0; i < nrows; i++) cnt[emax - ext(h_rows[i]) + 1]++;
+    for (int e = 1; e <= emax + 1; e++) cnt[e] += cnt[e - 1];
+    for (int i = 0; i < nrows; i++) tmp[cnt[emax - ext(h_rows[i])]++] = h_rows[i];
+    std::copy(tmp, tmp + nrows, h_rows);
+  }
   int ntile = 0, njob = 0;
   for (int r0 = 0; r0 < nrows; r0 += KTR) {
     const int n = std::min(KTR, nrows - r0);
@@ -206,7 +230,7 @@ extern "C" int mg_ewald_kspace_noalloc(const double* r_dev, const double* q_dev,
     h_tiles[ntile++] = KTile{r0, n, R, 0};
   }
   const int nchunk = std::max(1, std::min(std::min(MAXCHUNK, std::max(1, nq / 64)),
-                                          (8 * 152 + njob - 1) / njob));
+                                          (8 * nsm + njob - 1) / njob));
 
   // ---- pointers into the scratch
   float2* tab = (float2*)(base + OFF_TAB);
@@ -274,18 +298,15 @@ extern "C" int mg_ewald_kspace_noalloc(const double* r_dev, const double* q_dev,
   NA_CK(k_sk_reduce_mixed(Lc, ka, part, true));
   NA_CK(k_kf_gemm_mixed(Lc, ka, tab));
   NA_CK(k_reduce_sum(Lc, ekpart, (nk + 255) / 256, 7, sums));
-  double e = 0;
-  NA_CK(cudaMemcpyAsync(&e, sums, sizeof(double), cudaMemcpyDeviceToHost, s));
+  // sums[0] = sum_k ekk |S|^2, sums[8] = sum q^2; both read in one copy
+  // on the caller's stream
+  sumq2_kernel<<<1, SQ_THREADS, 0, s>>>(nq, q_dev, sums + 8);
+  NA_CK(cudaGetLastError());
+  double e[9];
+  NA_CK(cudaMemcpyAsync(e, sums, sizeof(e), cudaMemcpyDeviceToHost, s));
   NA_CK(cudaStreamSynchronize(s));
 #undef NA_CK
-  if (energy) {
-    // k-space energy sum_k ekk |S|^2 / (4 pi) plus the self term
-    double sumq2 = 0;
-    static double hq[MAXQ];
-    if (cudaMemcpy(hq, q_dev, sizeof(double) * nq, cudaMemcpyDeviceToHost) != cudaSuccess)
-      return fail_na(MG_ERR_CUDA, "mg_ewald_kspace_noalloc: reading the charges");
-    for (int i = 0; i < nq; i++) sumq2 += hq[i] * hq[i];
-    *energy = e / (4 * M_PI) - alpha / 1.772453850905516 * sumq2;
-  }
+  // k-space energy sum_k ekk |S|^2 / (4 pi) plus the self term
+  if (energy) *energy = e[0] / (4 * M_PI) - alpha / 1.772453850905516 * e[8];
   return MG_OK;
 }

@@ -143,4 +143,81 @@ cudaError_t k_thermostat(const Launch& L, const ThermoArgs& a, const double* kin
   return cudaGetLastError();
 }
 
+// cook's bounddr (sim/norm.c:1513-1560), after the step and its thermostat:
+// a site whose displacement in the step r1 is longer than drmax has r1
+// scaled to that length; the number of such sites and the smallest factor
+// are accumulated in rep[0] (count) and rep[1] (float bits of the factor,
+// atomicMin on the bits of a positive float keeps the order)
+__global__ void bounddr_kernel(int ns, double vvmax, double* __restrict__ r1,
+                               unsigned int* __restrict__ rep) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ns) return;
+  double* p = r1 + 3 * (long)i;
+  const double vv = p[0] * p[0] + p[1] * p[1] + p[2] * p[2];
+  if (vv > vvmax) {
+    const double q = sqrt(vvmax / vv);
+    p[0] *= q;
+    p[1] *= q;
+    p[2] *= q;
+    atomicAdd(rep, 1u);
+    atomicMin(rep + 1, __float_as_uint((float)q));
+  }
+}
+
+// cook's removedrifts for the momentum (sim/norm.c:677-705): the mass
+// weighted sum of r1 (per CTA, then one fixed-order reduction), divided by
+// the total mass of the free sites and subtracted from every site's r1
+__global__ void __launch_bounds__(TH_THREADS)
+momentum_part_kernel(int ns, const double* __restrict__ mass, const double* __restrict__ r1,
+                     double* __restrict__ part) {
+  __shared__ double red[3][TH_THREADS];
+  const int i = blockIdx.x * TH_THREADS + threadIdx.x;
+#pragma unroll
+  for (int d = 0; d < 3; d++) red[d][threadIdx.x] = i < ns ? mass[i] * r1[3 * (long)i + d] : 0.0;
+  __syncthreads();
+  for (int w = TH_THREADS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+#pragma unroll
+      for (int d = 0; d < 3; d++) red[d][threadIdx.x] += red[d][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < 3) part[3 * (long)blockIdx.x + threadIdx.x] = red[threadIdx.x][0];
+}
+
+__global__ void momentum_remove_kernel(int ns, const double* __restrict__ P, double imass,
+                                       double* __restrict__ r1, double* __restrict__ vout) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const double v0 = P[0] * imass, v1 = P[1] * imass, v2 = P[2] * imass;
+  if (i == 0 && vout) {
+    vout[0] = v0;
+    vout[1] = v1;
+    vout[2] = v2;
+  }
+  if (i >= ns) return;
+  r1[3 * (long)i] -= v0;
+  r1[3 * (long)i + 1] -= v1;
+  r1[3 * (long)i + 2] -= v2;
+}
+
+int drift_blocks(int ns) { return (ns + TH_THREADS - 1) / TH_THREADS; }
+
+cudaError_t k_remove_drift(const Launch& L, int ns, const double* mass, double total_mass,
+                           double* r1, double* part, double* P, double* vout) {
+  const int nb = drift_blocks(ns);
+  momentum_part_kernel<<<nb, TH_THREADS, 0, L.s>>>(ns, mass, r1, part);
+  ++*L.counter;
+  cudaError_t e = k_reduce_sum(L, part, nb, 3, P);
+  if (e != cudaSuccess) return e;
+  momentum_remove_kernel<<<nb, TH_THREADS, 0, L.s>>>(ns, P, 1.0 / total_mass, r1, vout);
+  ++*L.counter;
+  return cudaGetLastError();
+}
+
+cudaError_t k_bounddr(const Launch& L, int ns, double drmax, double* r1, unsigned int* rep) {
+  bounddr_kernel<<<(ns + TH_THREADS - 1) / TH_THREADS, TH_THREADS, 0, L.s>>>(ns, drmax * drmax,
+                                                                              r1, rep);
+  ++*L.counter;
+  return cudaGetLastError();
+}
+
 }  // namespace mg

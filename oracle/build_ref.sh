@@ -5,9 +5,12 @@
 # written here) and the module list that cook/configure.sh emits for the
 # Ewald + linked-cell build.  Outputs go only to oracle/_ref/ (git-ignored).
 #
-# usage: oracle/build_ref.sh [REFERENCE_DIR]   (default /root/reference)
+# usage: oracle/build_ref.sh [REFERENCE_DIR]
+# The reference tree is the argument, else $MACSIMUS_REF, else the read-only
+# checkout this recipe was written against (/root/reference); without a
+# reference tree the script does nothing and exits 0.
 set -euo pipefail
-REF=${1:-/root/reference}
+REF=${1:-${MACSIMUS_REF:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT=$HERE/_ref
 if [ ! -d "$REF/cook" ]; then
@@ -64,3 +67,7 @@ variant cookewP1 "-lpthread" "#define PARALLEL 1" "#define BARRIER"
 variant cookpol "" "#define POLAR 0"
 # Widom insertion build (WIDOM without SLAB)
 variant cookwidom "" "#define WIDOM"
+# full pressure tensor (PRESSURETENSOR = PT_VIR|PT_KIN|PT_OFF: virial and
+# kinetic parts with the off-diagonal terms), plain and Drude builds
+variant cookewpt "" "#define PRESSURETENSOR 7"
+variant cookpolpt "" "#define POLAR 0" "#define PRESSURETENSOR 7"

@@ -726,9 +726,22 @@ int orc_forces(const orc_sys_t *s, const double *r, double *f, orc_en_t *en, int
       charge_pos(s, r, g_qlist + i, p);
       for (m = 0; m < 3; m++) M[m] += g_qlist[i].q * p[m];
     }
-    c = 4 * M_PI / (2 * s->epsinf + 1) / V;
-    for (m = 0; m < 3; m++) ek[m] = -c * M[m];
-    Edip = c / 2 * (SQ(M[0]) + SQ(M[1]) + SQ(M[2]));
+    if (s->elcorr) {
+      /* Yeh-Berkowitz: the selected axes only (sim/ewald.c:869-882) */
+      c = 4 * M_PI / V;
+      Edip = 0;
+      for (m = 0; m < 3; m++) {
+        ek[m] = 0;
+        if (s->elcorr & 1 << m) {
+          if (!(s->elcorr & 8)) ek[m] = -c * M[m];
+          Edip += c / 2 * SQ(M[m]);
+        }
+      }
+    } else {
+      c = 4 * M_PI / (2 * s->epsinf + 1) / V;
+      for (m = 0; m < 3; m++) ek[m] = -c * M[m];
+      Edip = c / 2 * (SQ(M[0]) + SQ(M[1]) + SQ(M[2]));
+    }
     for (i = 0; i < g_nq; i++) {
       const qitem_t *it = g_qlist + i;
       double *fo = f + (it->drude ? 3 * ns : 0) + 3 * it->site, p[3];
@@ -798,7 +811,23 @@ int orc_shake_step_dp(int ns, double *r, double *r1, const double *f, const doub
                       double h, double eps, double omega, int maxit, const double *dp,
                       double *ekin)
 {
-  double hh = h * h, kin = 0;
+  return orc_shake_step_meas(ns, r, r1, f, mass, nmol, mol_first, mol_nc, cfirst, ci, cj,
+                             bondq, h, eps, omega, maxit, dp, ekin, NULL);
+}
+
+/* the step of a measured cycle: with meas != NULL also cook's constraint
+   virial (sim/virc.c, accumulated in the sweep at sim/constrd.c:833 and
+   divided by h^2 at sim/constrd.c:1038-1040) and the VERLET=3 kinetic
+   tensor (sim/shakev3.c:20-32 scaled by hscale = 0.5/h^2,
+   sim/constrd.c:1012-1017): meas[0] = En.virc, meas[1..6] = PTvirc,
+   meas[7..12] = En.Pkin before the division by V (xx yy zz yz zx xy) */
+int orc_shake_step_meas(int ns, double *r, double *r1, const double *f, const double *mass,
+                        int nmol, const int *mol_first, const int *mol_nc, const int *cfirst,
+                        const int *ci, const int *cj, const double *bondq,
+                        double h, double eps, double omega, int maxit, const double *dp,
+                        double *ekin, double *meas)
+{
+  double hh = h * h, kin = 0, virc = 0, PT[6] = {0, 0, 0, 0, 0, 0}, PK[6] = {0, 0, 0, 0, 0, 0};
   int n, worst = 0;
   double *p = malloc(sizeof(double) * 3 * ns);
   for (n = 0; n < nmol; n++) {
@@ -824,6 +853,16 @@ int orc_shake_step_dp(int ns, double *r, double *r1, const double *f, const doub
           if (fabs(sq / bondq[al]) > maxsq) maxsq = fabs(sq / bondq[al]);
           for (k = 0; k < 3; k++) rij[k] = r[3 * a + k] - r[3 * b + k];
           sq *= omega / (mi + mj);
+          if (meas) {
+            double sb = sq / bondq[al];
+            PT[0] += sb * (rij[0] * rij[0]);
+            PT[1] += sb * (rij[1] * rij[1]);
+            PT[2] += sb * (rij[2] * rij[2]);
+            PT[3] += sb * (rij[1] * rij[2]);
+            PT[4] += sb * (rij[2] * rij[0]);
+            PT[5] += sb * (rij[0] * rij[1]);
+            virc += sq;
+          }
           sq /= bondq[al];
           for (k = 0; k < 3; k++) {
             rij[k] *= sq;
@@ -842,11 +881,24 @@ int orc_shake_step_dp(int ns, double *r, double *r1, const double *f, const doub
         V2[k] = p[3 * i + k] - r[3 * i + k];
       }
       kin += (SQ(V1[0]) + SQ(V1[1]) + SQ(V1[2]) + SQ(V2[0]) + SQ(V2[1]) + SQ(V2[2])) * mass[i];
+      PK[0] += (V1[0] * V1[0] + V2[0] * V2[0]) * mass[i];
+      PK[1] += (V1[1] * V1[1] + V2[1] * V2[1]) * mass[i];
+      PK[2] += (V1[2] * V1[2] + V2[2] * V2[2]) * mass[i];
+      PK[3] += (V1[1] * V1[2] + V2[1] * V2[2]) * mass[i];
+      PK[4] += (V1[2] * V1[0] + V2[2] * V2[0]) * mass[i];
+      PK[5] += (V1[0] * V1[1] + V2[0] * V2[1]) * mass[i];
       for (k = 0; k < 3; k++) { r1[3 * i + k] = V2[k]; r[3 * i + k] = p[3 * i + k]; }
     }
   }
   free(p);
   if (ekin) *ekin = kin / hh / 4;
+  if (meas) {
+    meas[0] = virc / hh;
+    for (n = 0; n < 6; n++) {
+      meas[1 + n] = PT[n] / hh;
+      meas[7 + n] = PK[n] * (0.5 / hh);
+    }
+  }
   return worst;
 }
 

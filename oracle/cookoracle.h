@@ -92,6 +92,10 @@ typedef struct {
   /* Drude (POLAR); NULL if non-polar */
   const double *qpol;   /* [ns] Drude charge */
   const double *alphaqq;/* [ns] 1/(Drude spring constant) = alphapol/qpol^2 in p.u. */
+  /* cook's el.corr (sim/simglob.h:828): bits 1, 2, 4 select the
+     Yeh-Berkowitz dipole term along x, y, z in place of the isotropic
+     epsinf term; bit 8 keeps its energy and virial but applies no force */
+  int elcorr;
 } orc_sys_t;
 
 /* forces(B,A) of cook: f (3*ns, or 6*ns with Drude) is overwritten; energies
@@ -114,6 +118,15 @@ int orc_shake_step_dp(int ns, double *r, double *r1, const double *f, const doub
                       const int *ci, const int *cj, const double *bondq,
                       double h, double eps, double omega, int maxit, const double *dp,
                       double *ekin);
+
+/* orc_shake_step_dp of a measured cycle: meas[13] gets cook's En.virc,
+   PTvirc[6] (sim/virc.c / h^2) and En.Pkin[6] (m (V1 V1 + V2 V2) / (2 h^2),
+   before the division by V) of the step */
+int orc_shake_step_meas(int ns, double *r, double *r1, const double *f, const double *mass,
+                        int nmol, const int *mol_first, const int *mol_nc, const int *cfirst,
+                        const int *ci, const int *cj, const double *bondq,
+                        double h, double eps, double omega, int maxit, const double *dp,
+                        double *ekin, double *meas);
 
 /* one Drude relaxation iteration (sim/scf.c selffield): r and f hold 2*ns
    vectors (sites, then Drude displacements / Drude forces); energies added

@@ -34,7 +34,7 @@ class SYS(C.Structure):
                 ("L", C.c_double * 3), ("cutoff", C.c_double), ("alpha", C.c_double),
                 ("kappa", C.c_double), ("epsinf", C.c_double), ("ertab", C.POINTER(C.c_double)),
                 ("ntab", C.c_int), ("sgrid", C.c_double), ("qpol", C.POINTER(C.c_double)),
-                ("alphaqq", C.POINTER(C.c_double))]
+                ("alphaqq", C.POINTER(C.c_double)), ("elcorr", C.c_int)]
 
 
 _lib = None
@@ -69,6 +69,9 @@ def lib():
                                      C.c_double, C.c_double, C.c_double, C.c_int, dp]
         L.orc_shake_step_dp.argtypes = [C.c_int, dp, dp, dp, dp, C.c_int, ip, ip, ip, ip, ip, dp,
                                         C.c_double, C.c_double, C.c_double, C.c_int, dp, dp]
+        L.orc_shake_step_meas.argtypes = [C.c_int, dp, dp, dp, dp, C.c_int, ip, ip, ip, ip, ip,
+                                          dp, C.c_double, C.c_double, C.c_double, C.c_int, dp,
+                                          dp, dp]
         L.orc_selffield.argtypes = [C.POINTER(SYS), dp, dp, C.POINTER(EN), C.c_double]
         L.orc_selffield.restype = C.c_double
         L.orc_aspc_coef.argtypes = [C.c_int, dp, dp]
@@ -159,7 +162,7 @@ class Oracle:
     """The oracle's view of one system + Ewald parameters."""
 
     def __init__(self, system, Lbox, cutoff, alpha, kappa, LJcutoff=None, grid=256,
-                 rshift=3, rplus=2.5, epsinf=3e33):
+                 rshift=3, rplus=2.5, epsinf=3e33, elcorr=0):
         L = lib()
         self.system = system
         self.L = np.array(Lbox, dtype=np.float64)
@@ -185,6 +188,7 @@ class Oracle:
         s.alpha = alpha
         s.kappa = self.kappa
         s.epsinf = epsinf
+        s.elcorr = elcorr
         s.ertab = _dp(self.tab)
         s.ntab = ntab
         s.sgrid = sg.value
@@ -228,8 +232,10 @@ class Oracle:
             en["Pvir"] = list(e.Pvir)
         return r2, f2, en, d
 
-    def shake_step(self, r, r1, f, h, eps=1e-10, omega=0.6, maxit=1000, dp=None):
-        """leap-frog + SHAKE (dp: added to the unconstrained positions)"""
+    def shake_step(self, r, r1, f, h, eps=1e-10, omega=0.6, maxit=1000, dp=None, meas=None):
+        """leap-frog + SHAKE (dp: added to the unconstrained positions); meas
+        (a float64 array of 13) receives En.virc, PTvirc[6] and the kinetic
+        tensor En.Pkin[6] before the division by V"""
         s = self.system
         r = np.ascontiguousarray(r, dtype=np.float64).copy().reshape(-1)
         r1 = np.ascontiguousarray(r1, dtype=np.float64).copy().reshape(-1)
@@ -243,10 +249,11 @@ class Oracle:
         bq = np.ascontiguousarray(s.cons_len ** 2, np.float64)
         ek = C.c_double()
         dpa = None if dp is None else np.ascontiguousarray(dp, np.float64).reshape(-1)
-        it = lib().orc_shake_step_dp(s.ns, _dp(r), _dp(r1), _dp(f), _dp(mass), s.nmol,
-                                     _ip(mfirst), _ip(nc), _ip(cfirst), _ip(ci), _ip(cj), _dp(bq),
-                                     h, eps, omega, maxit,
-                                     _dp(dpa) if dpa is not None else None, C.byref(ek))
+        it = lib().orc_shake_step_meas(s.ns, _dp(r), _dp(r1), _dp(f), _dp(mass), s.nmol,
+                                       _ip(mfirst), _ip(nc), _ip(cfirst), _ip(ci), _ip(cj),
+                                       _dp(bq), h, eps, omega, maxit,
+                                       _dp(dpa) if dpa is not None else None, C.byref(ek),
+                                       _dp(meas) if meas is not None else None)
         return r.reshape(-1, 3), r1.reshape(-1, 3), it, ek.value
 
 
@@ -349,6 +356,28 @@ def normalize(system, r, L, r0=0.15):
     return r
 
 
+def bounddr(r1, drmax):
+    """cook's bounddr (sim/norm.c:1513-1560): every site's displacement in
+    one step longer than drmax scaled to drmax; returns (r1, sites reduced,
+    smallest factor)"""
+    r1 = np.array(r1, np.float64).reshape(-1, 3)
+    vv = (r1 * r1).sum(1)
+    big = vv > drmax * drmax
+    q = np.sqrt(drmax * drmax / vv[big])
+    r1[big] *= q[:, None]
+    return r1, int(big.sum()), float(q.min()) if big.any() else 1.0
+
+
+def remove_drift(system, r1):
+    """cook's removedrifts for the momentum bits (sim/norm.c:677-705): the
+    mass-weighted mean of r1 subtracted from every site; returns (r1, the
+    drift in A per step)"""
+    r1 = np.array(r1, np.float64).reshape(-1, 3)
+    m = np.asarray(system.mass, np.float64)[:, None]
+    v = (m * r1).sum(0) / m.sum()
+    return r1 - v, v
+
+
 def trvp_coef(k):
     """time-reversible velocity predictor of length k (sim/trvpscale.c:31-35;
     J. Chem. Theory Comput. 7, 3596 (2011)): h v(t) ~ sum_j b_j X_j"""
@@ -403,3 +432,62 @@ def aspc_coef(k):
 def thermostat_factor(kind, kin2, h, nf, T, tau, seed=0, step=0):
     """velocity factor of cook's Berendsen (1) / Bussi (2) thermostat"""
     return lib().orc_thermostat(kind, kin2, h, nf, T, tau, seed, step)
+
+
+def drude_md(orc, system, r, r1, h, k, niter, nsteps, epsc, omegac, measure=False):
+    """ASPC + SCF + SHAKE steps of a Drude box (sim/constrd.c:726-736 with
+    sim/pred2.c:26-100 and sim/scf.c): the predictor history restarted from
+    r (displacements of cfg[0]) and r1 (of cfg[1]) as cook restarts it, k the
+    ASPC length, niter force evaluations + SCF iterations per step.  Returns
+    (r, r1, pressure of the last step or None)."""
+    ns = system.ns
+    hist = [np.zeros((ns, 3)) for _ in range(k + 2)]
+    hist[0] = r[ns:].copy()
+    hist[k + 1] = r1[ns:].copy()
+    hp, kk = 0, 0
+    om = 0.6
+    r, r1 = r.copy(), r1.copy()
+    K2 = k + 2
+    press = None
+    for step in range(nsteps):
+        meas_step = measure and step == nsteps - 1
+        B, _ = aspc_coef(kk)
+        pred = sum(B[i] * hist[(hp - i) % K2] for i in range(kk + 2))
+        if kk < k:
+            kk += 1
+            om = aspc_coef(kk)[1]
+        r2 = np.vstack([r[:ns], pred])
+        for it in range(niter):
+            last = meas_step and it == niter - 1
+            f2, en = orc.forces(r2, measure=last, nthreads=4)
+            r2, f2, en, _ = orc.selffield(r2, f2, om, en if last else None)
+        hp = (hp + 1) % K2
+        hist[hp] = r2[ns:].copy()
+        meas = np.zeros(13) if meas_step else None
+        rs, r1s, it, ek = orc.shake_step(r2[:ns], r1[:ns], f2[:ns], h, eps=epsc,
+                                         omega=omegac / 2, meas=meas)
+        if meas_step:
+            press = measure_pressure(en, meas, ek, orc.L)
+            press["ekin"] = ek
+        r = np.vstack([rs, r2[ns:]])
+        r1 = np.vstack([r1s, r1[ns:]])
+    return r, r1, press
+
+
+PUNIT = 13806490.0   # Pa per K/A^3 (sim/units.h:103)
+
+
+def measure_pressure(en, meas, ekin, L):
+    """cook's measurePconstraints (sim/constrd.c:115-265) with No.Pkinq = 1:
+    en = energies of the step's force evaluation (+ the SCF iteration for
+    Drude builds: el, self, vir, Pvir), meas = the 13 sums of shake_step,
+    ekin = the kinetic energy.  Returns K/A^3 values: Pvir (+ constraint
+    part), Pkin, Ptens = Pvir + Pkin (xx yy zz yz zx xy), P = cook's Pevir,
+    and virc, vir (= En.vir after the constraint and electrostatic parts)."""
+    V = float(np.prod(L))
+    virc = float(meas[0])
+    Pvir = (np.asarray(en["Pvir"], float) + np.asarray(meas[1:7])) / V
+    Pkin = np.asarray(meas[7:13]) / V
+    vir = en["vir"] + virc + en["el"] - 2 * en.get("self", 0.0)
+    return dict(virc=virc, vir=vir, Pvir=Pvir, Pkin=Pkin, Ptens=Pvir + Pkin,
+                P=(2 * ekin + vir) / (3 * V))

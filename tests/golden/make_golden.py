@@ -62,6 +62,24 @@ CASES = {
     "tip4p216": dict(binary="cookew", species=["T4P"], N=[216], L=18.6206,
                      cutoff=9.0, alpha=0.35, kn=6, steps=3, h=0.002, epsc=1e-10,
                      options=["-y99999", "-n1"], extra_get=["dt.plb=0.002"]),
+    # the dipole term of Ewald(2) (sim/ewald.c:865-887) on the 216 SPC/E box:
+    # isotropic surroundings of dielectric constant 1 (el.epsinf), the
+    # Yeh-Berkowitz slab term along z (el.corr=4), and its energy-only
+    # form (el.corr=12)
+    "dip216eps": dict(binary="cookew", species=["WAT"], N=[216], L=18.6206,
+                      cutoff=9.0, alpha=0.35, kn=6, steps=2, h=0.002, epsc=1e-10,
+                      extra_def=["el.epsinf=1"], epsinf=1.0, elcorr=0),
+    "dip216yb": dict(binary="cookew", species=["WAT"], N=[216], L=18.6206,
+                     cutoff=9.0, alpha=0.35, kn=6, steps=2, h=0.002, epsc=1e-10,
+                     extra_def=["el.corr=4"], epsinf=3e33, elcorr=4),
+    "dip216yb8": dict(binary="cookew", species=["WAT"], N=[216], L=18.6206,
+                      cutoff=9.0, alpha=0.35, kn=6, steps=2, h=0.002, epsc=1e-10,
+                      extra_def=["el.corr=12"], epsinf=3e33, elcorr=12),
+    # cook's step limiter bounddr (sim/norm.c:1513): drmax=-0.02 A (negative:
+    # on for any start) reduces the step of the fast sites after every step
+    "bounddr216": dict(binary="cookew", species=["WAT"], N=[216], L=18.6206,
+                       cutoff=9.0, alpha=0.35, kn=6, steps=4, h=0.002, epsc=1e-10,
+                       extra_get=["drmax=-0.02"], drmax=0.02),
     # Widom insertions of a neutral LJ probe (sigma 3.2 A, epsilon 0.65
     # kJ/mol) into 250 + 250 LJ ions of charge +-1 e, L = 37 A (reduced
     # density 0.5 at sigma 3.7 A), cutoff 10, alpha 0.31, |n|<=8; 1e7
@@ -230,6 +248,66 @@ def run_energy_case(name, c):
     print("wrote %s: %d NVE steps" % (name, len(meta["Etot"])))
 
 
+# NVE drift with error bars that resolve a factor of two: four runs of the
+# 864-water box from independent crystal starts (cook option -z: the seed of
+# its random velocities), each 1500 Berendsen steps then 25000 NVE steps.
+# Stored per run: block means of the printed per-step Etot over 50 steps,
+# the mean Tkin and cook's own linear regression of Etot(t) over the NVE
+# sweep (LRAdd("Etot"), sim/maincps.c:277; printed by LRPrint).
+NVE_ENSEMBLES = {
+    "nve864x4": dict(binary="cookewP1", species=["WAT"], N=[864], L=29.65, cutoff=12.0,
+                     alpha=0.26, kn=8, h=0.002, epsc=1e-10, seeds=[11, 12, 13, 14],
+                     equil=1500, steps=25000, block=50, threads=2),
+}
+
+
+def run_nve_ensemble(name, c):
+    binary = os.path.join(REFBIN, c["binary"])
+    if not os.path.exists(binary):
+        raise SystemExit("missing %s: run oracle/build_ref.sh first" % binary)
+    procs = []
+    for seed in c["seeds"]:
+        wd = tempfile.mkdtemp(prefix="golden_")
+        with open(os.path.join(wd, "ff.ble"), "w") as f:
+            f.write(ble_text(c["species"]))
+        with open(os.path.join(wd, "sim.def"), "w") as f:
+            f.write(def_text(dict(c, steps=0)))
+        with open(os.path.join(wd, "sim.get"), "w") as f:
+            f.write('init="crystal"\nthermostat="Berendsen"\ntau.T=0.1\nno=%d\n;\n'
+                    'thermostat="none"\nno=%d\n;\n' % (c["equil"], c["steps"]))
+        env = dict(os.environ, NSLOTS=str(c["threads"]))
+        procs.append((seed, wd, subprocess.Popen([binary, "ff.ble", "sim", "-z%d" % seed],
+                                                 cwd=wd, stdin=subprocess.DEVNULL, env=env,
+                                                 stdout=subprocess.DEVNULL,
+                                                 stderr=subprocess.DEVNULL)))
+    runs = []
+    for seed, wd, p in procs:
+        if p.wait() != 0:
+            raise SystemExit("%s seed %d failed" % (name, seed))
+        rows = []
+        prt = open(os.path.join(wd, "sim.prt")).read()
+        for line in prt.splitlines():
+            m = re.match(r"\s+(\d+\.\d{3})\s+(\S+)\s+(-?\d+)\s+(-?\d+\.\d+)\s", line)
+            if m:
+                rows.append([float(m.group(k)) for k in (1, 2, 3, 4)])
+        a = np.array(rows)
+        assert a.shape[0] == c["equil"] + c["steps"], a.shape
+        nve = a[c["equil"]:]
+        b = c["block"]
+        nb = len(nve) // b
+        lr = re.findall(r'LINEAR REGRESSION "Etot" (\d+) points.*?\n.*?\n(\S+) (\S+) # A stderr\n'
+                        r'(\S+) (\S+) # B stderr', prt)
+        n_lr, _, _, B, sB = lr[-1]
+        runs.append(dict(seed=seed, t0=nve[0, 0], Tkin_mean=float(nve[:, 1].mean()),
+                         Etot_block=nve[:nb * b, 3].reshape(nb, b).mean(1).tolist(),
+                         lr_points=int(n_lr), lr_slope=float(B), lr_slope_se=float(sB)))
+        shutil.rmtree(wd)
+    meta = dict(case=name, params=c, runs=runs)
+    with open(os.path.join(HERE, name + ".json"), "w") as f:
+        json.dump(meta, f, sort_keys=True)
+    print("wrote %s: %d runs" % (name, len(runs)))
+
+
 # Resume parity through cook's .cfg files (sim/simils.c savecfg/loadcfg):
 # run A from cook's crystal start writes sim.cfg; run B continues from that
 # file (init="cont"); run C continues from a file that
@@ -293,6 +371,67 @@ def run_resume_case(name, c):
     print("wrote %s" % name)
 
 
+# Pressure of one measured step (cook's measurePconstraints, sim/constrd.c:
+# 115-265, with the constraint virial of sim/virc.c): builds with
+# PRESSURETENSOR 7 (full tensor).  Run A from cook's crystal start writes
+# sim.cfg after steps_a steps; run B appends one step from that file
+# (init="append": no earlier statistics loaded) with -v134: -v128 dumps the
+# forces, -v2|-v4 print every statistic of the step (its only sample) with
+# 9 significant digits.  Stored: A's file and B's printed values.
+PRESSURE_CASES = {
+    "press_spce216": dict(binary="cookewpt", species=["WAT"], N=[216], L=18.6206, cutoff=9.0,
+                          alpha=0.35, kn=6, h=0.002, epsc=1e-10, steps_a=4),
+    "press_tip4p216": dict(binary="cookewpt", species=["T4P"], N=[216], L=18.6206,
+                           cutoff=9.0, alpha=0.35, kn=6, h=0.002, epsc=1e-10, steps_a=4),
+    "press_drude216": dict(binary="cookpolpt", species=["WATD"], N=[216], L=18.6206,
+                           cutoff=9.0, alpha=0.35, kn=6, h=0.001, epsc=1e-10, steps_a=4,
+                           options=["-p220"], extra_def=["scf.eps=-1"]),
+}
+
+
+def run_pressure_case(name, c):
+    binary = os.path.join(REFBIN, c["binary"])
+    if not os.path.exists(binary):
+        raise SystemExit("missing %s: run oracle/build_ref.sh first" % binary)
+    wd = tempfile.mkdtemp(prefix="golden_")
+    with open(os.path.join(wd, "ff.ble"), "w") as f:
+        f.write(ble_text(c["species"]))
+    with open(os.path.join(wd, "sim.def"), "w") as f:
+        f.write(def_text(dict(c, steps=0)))
+
+    def run(init, steps, opts):
+        with open(os.path.join(wd, "sim.get"), "w") as f:
+            f.write('init="%s"\nno=%d\n;\n' % (init, steps))
+        p = subprocess.run([binary, "ff.ble", "sim"] + c.get("options", []) + opts, cwd=wd,
+                           stdin=subprocess.DEVNULL, capture_output=True, text=True, timeout=600)
+        if p.returncode != 0:
+            raise SystemExit("%s failed:\n%s" % (name, p.stdout[-3000:]))
+
+    run("crystal", c["steps_a"], [])
+    with open(os.path.join(wd, "sim.cfg"), "rb") as f:
+        a_bytes = f.read()
+    with open(os.path.join(HERE, name + "_a.cfg"), "wb") as f:
+        f.write(a_bytes)
+    os.remove(os.path.join(wd, "sim.sta"))
+    run("append", 1, ["-v134"])
+    stats = {}
+    for line in open(os.path.join(wd, "sim.prt")):
+        m = re.match(r"#\s*(\S+)\s+-\s+-\s+1 =(.+)=$", line.rstrip())
+        if m:
+            stats[m.group(2)] = float(m.group(1))
+    d0 = parse_dump(os.path.join(wd, "sim.0.dump"))
+    m3 = re.search(r"omegac=(\S+) \(optimized\)", open(os.path.join(wd, "sim.prt")).read())
+    shutil.rmtree(wd)
+    arrays = dict(r=d0["r"], f=d0["f"])
+    if "rD" in d0:
+        arrays.update(rD=d0["rD"], fD=d0["fD"])
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+    meta = dict(case=name, params=c, stats=stats, omegac=float(m3.group(1)) if m3 else None)
+    with open(os.path.join(HERE, name + ".json"), "w") as f:
+        json.dump(meta, f, indent=1, sort_keys=True)
+    print("wrote %s: %d printed statistics" % (name, len(stats)))
+
+
 def save_case(name, dumps, meta):
     arrays = {}
     d0 = dumps[0]
@@ -316,8 +455,15 @@ def save_case(name, dumps, meta):
 
 
 def main(argv):
-    names = argv or list(CASES) + list(ENERGY_CASES) + list(RESUME_CASES)
+    names = argv or (list(CASES) + list(ENERGY_CASES) + list(RESUME_CASES) +
+                     list(PRESSURE_CASES) + list(NVE_ENSEMBLES))
     for n in names:
+        if n in NVE_ENSEMBLES:
+            run_nve_ensemble(n, NVE_ENSEMBLES[n])
+            continue
+        if n in PRESSURE_CASES:
+            run_pressure_case(n, PRESSURE_CASES[n])
+            continue
         if n in ENERGY_CASES:
             run_energy_case(n, ENERGY_CASES[n])
             continue

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 import macsimus_gb300 as M
-from golden_cases import CASES, load
+from golden_cases import CASES, DIPOLE_CASES, load
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -54,11 +54,55 @@ def test_forces_vs_oracle_and_reference(case, precision):
     assert abs(en["el"] + en["lj"] - meta["Epot_last"]) < etot_tol + 1e-3
 
 
+@pytest.mark.parametrize("case", DIPOLE_CASES)
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_dipole_term(case, precision):
+    """Ewald(2)'s dipole term on the device: epsinf = 1, Yeh-Berkowitz along
+    z (el.corr=4) and energy only (el.corr=12): forces against cook's dumps
+    and the oracle, the term's energy and virial against the oracle"""
+    g, meta, system, ew = load(case)
+    fp = M.ForcePath(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"],
+                     precision=precision, epsinf=ew["epsinf"], dipole_corr=ew["elcorr"])
+    orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"], epsinf=ew["epsinf"],
+                   elcorr=ew["elcorr"])
+    tol = 1e-10 if precision == "fp64" else MIXED_TOL
+    for d in (0, g["r"].shape[0] - 1):
+        f, en = fp.forces(g["r"][d], measure=True)
+        fo, eo = orc.forces(g["r"][d], nthreads=4)
+        assert rel_rms(f, fo) < tol
+        assert rel_rms(f, g["f"][d]) < max(tol, 2e-10)
+        assert abs(en["edip"] - eo["edip"]) < 1e-9 * eo["edip"]
+        etol = 1e-10 if precision == "fp64" else 2e-6
+        assert abs(en["el"] - eo["el"]) <= etol * abs(eo["eself"])
+        for m in range(6):
+            assert abs(en["Pvir"][m] - eo["Pvir"][m]) <= 10 * etol * abs(eo["Pvir"][0]), m
+    # the k-space entry point carries the same term
+    fk, e = fp.ewald(g["r"][0])
+    _, eo = orc.forces(g["r"][0])
+    assert abs(e - (eo["ek"] + eo["eself"] + eo["edip"])) < (1e-9 if precision == "fp64" else 2e-6) * abs(eo["eself"])
+
+
 @pytest.mark.parametrize("cells", [1, 2, 3])
 def test_cell_subdivision_does_not_change_forces(cells):
     g, meta, system, ew, fp = make("spce864", "fp64", cells_per_cutoff=cells)
     f, _ = fp.forces(g["r"][0])
     assert rel_rms(f, g["f"][0]) < 2e-10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cell_list_is_deterministic(precision):
+    """the counting-sort cell list (atomic slots, then every cell's sites
+    ranked by site index) gives the same order at every evaluation: forces
+    and energies bit-identical over repeated evaluations, also after the
+    configuration changed in between"""
+    g, meta, system, ew, fp = make("brine532", precision)
+    f0, e0 = fp.forces(g["r"][0], measure=True)
+    for k in range(12):
+        if k % 3 == 2:
+            fp.forces(g["r"][1])
+        f, e = fp.forces(g["r"][0], measure=True)
+        assert np.array_equal(f, f0)
+        assert e["el"] == e0["el"] and e["lj"] == e0["lj"]
 
 
 def test_ewald_kspace_part():

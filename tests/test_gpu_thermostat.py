@@ -119,3 +119,45 @@ def test_nose_hoover_holds_the_temperature_and_conserves_its_energy():
         cons.append(ham[-1] + ext)
     assert abs(np.mean(temps) / 298.0 - 1) < 0.03, temps[:5]
     assert np.std(cons) < 0.2 * np.std(ham), (np.std(cons), np.std(ham))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_bounddr_and_drift_removal_match_reference_trajectory(precision):
+    """the device steps with drmax = 0.02 A and the momentum drift removed
+    after every step reproduce cook's run with drmax = -0.02 (tests/golden/
+    bounddr216); the limiter reports the sites it reduced"""
+    from golden_cases import load
+    g, meta, system, ew = load("bounddr216")
+    p = meta["params"]
+    fp = M.ForcePath(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"],
+                     precision=precision, h=p["h"], epsc=p["epsc"], omegac=meta["omegac"],
+                     drmax=p["drmax"], drift_step=True)
+    R = g["r"]
+    r1, _, _ = O.bounddr(R[2] - R[1], p["drmax"])
+    r1, _ = O.remove_drift(system, r1)
+    fp.md_set_state(R[2], r1)
+    tol = 1e-9 if precision == "fp64" else 1e-6
+    nred = 0
+    for k in range(2):
+        fp.md_steps(1, measure=False)
+        r, r1d = fp.md_get_state()
+        assert np.abs(r - R[3 + k]).max() < tol
+        n, q = fp.bounddr_report()
+        _, no, qo = O.bounddr(r - R[2 + k], p["drmax"])
+        assert n == no and abs(q - qo) < 1e-6
+        nred += n
+        assert np.abs((system.mass[:, None] * r1d).sum(0)).max() < 1e-9 * system.mass.sum()
+    assert nred > 100
+
+
+def test_remove_drift_matches_oracle():
+    from golden_cases import load
+    g, meta, system, ew = load("spce216")
+    fp = M.ForcePath(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"], precision="fp64")
+    r1 = (g["r"][2] - g["r"][1]) + np.array([1e-3, -2e-3, 5e-4])
+    fp.md_set_state(g["r"][2], r1)
+    v = fp.remove_drift()
+    _, r1d = fp.md_get_state()
+    r1o, vo = O.remove_drift(system, r1)
+    assert np.abs(r1d - r1o).max() < 1e-15
+    assert np.abs(v - vo / meta["params"]["h"]).max() < 1e-12

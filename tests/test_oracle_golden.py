@@ -9,7 +9,7 @@ sim/constrd.c (SHAKE).
 import numpy as np
 import pytest
 
-from golden_cases import CASES, load
+from golden_cases import CASES, DIPOLE_CASES, load
 from oracle import oracle as O
 
 
@@ -28,6 +28,21 @@ def test_forces_match_reference_dumps(case):
         # dumps print 12 decimals of r and 9 of f: 1e-10 relative is the floor
         assert rel_rms(f, g["f"][d]) < 1e-10
     # En.pot of the last step (cook prints 9 significant digits)
+    assert abs((en["el"] + en["lj"]) / meta["Epot_last"] - 1) < 5e-9
+
+
+@pytest.mark.parametrize("case", DIPOLE_CASES)
+def test_dipole_term_matches_reference_dumps(case):
+    """Ewald(2)'s dipole term (sim/ewald.c:865-887): surroundings of
+    dielectric constant 1, the Yeh-Berkowitz slab term along z (el.corr=4)
+    and its energy-only form (el.corr=12, no force)"""
+    g, meta, system, ew = load(case)
+    orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"], epsinf=ew["epsinf"],
+                   elcorr=ew["elcorr"])
+    for d in range(g["r"].shape[0]):
+        f, en = orc.forces(g["r"][d], nthreads=4)
+        assert rel_rms(f, g["f"][d]) < 1e-10
+    assert en["edip"] > 1.0          # a real term, not the tin-foil 1e-31 K
     assert abs((en["el"] + en["lj"]) / meta["Epot_last"] - 1) < 5e-9
 
 
@@ -203,3 +218,24 @@ def test_nose_hoover_trajectory_matches_reference():
     # the last step's kinetic energy (9 digits printed); the initial r1 is
     # known to float precision only
     assert abs(ek / meta["Ekin_last"] - 1) < 1e-8
+
+
+def test_bounddr_and_drift_removal_match_reference_trajectory():
+    """cook with drmax = -0.02 A: after every step bounddr scales the step of
+    every faster site down to 0.02 A (sim/norm.c:1513-1560), then the
+    momentum drift that this creates is removed (removedrifts, momentum bits,
+    once per cycle = every step here, sim/maincps.c:65)"""
+    g, meta, system, ew = load("bounddr216")
+    p = meta["params"]
+    orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
+    R = g["r"]
+    r1, n, q = O.bounddr(R[2] - R[1], p["drmax"])
+    assert n > 100 and q < 0.5
+    r1, _ = O.remove_drift(system, r1)
+    r = R[2]
+    for k in range(2):
+        f, _ = orc.forces(r, measure=False, nthreads=4)
+        r, r1, it, ek = orc.shake_step(r, r1, f, p["h"], eps=p["epsc"], omega=meta["omegac"] / 2)
+        assert np.abs(r - R[3 + k]).max() < 1e-9
+        r1, n, q = O.bounddr(r1, p["drmax"])
+        r1, _ = O.remove_drift(system, r1)

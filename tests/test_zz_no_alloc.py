@@ -49,6 +49,35 @@ def test_noalloc_matches_context_entry_point_twice():
         assert abs(e.value - ek) < 2e-6 * eself
 
 
+def test_noalloc_calls_leave_free_device_memory_unchanged():
+    """The defining property: after a first call, further calls (also with
+    another number of charges and another box) change the free device memory
+    by nothing (cudaMemGetInfo, through torch)."""
+    import torch
+    lib = M.library()
+    g, meta, system, ew = load("spce216")
+    q = torch.tensor(system.q, dtype=torch.float64, device="cuda")
+    r = torch.tensor(g["r"][0].reshape(-1), dtype=torch.float64, device="cuda")
+    f = torch.zeros_like(r)
+    e = C.c_double()
+    L1 = np.ascontiguousarray(ew["L"], dtype=np.float64)
+    L2 = L1 * 1.05
+
+    def call(n, L):
+        rc = lib.mg_ewald_kspace_noalloc(r.data_ptr(), q.data_ptr(), n,
+                                         L.ctypes.data_as(C.POINTER(C.c_double)), ew["alpha"],
+                                         ew["kappa"], f.data_ptr(), C.byref(e), None)
+        assert rc == 0
+
+    call(system.ns, L1)                       # warm-up: the module and its array are loaded
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for n, L in ((system.ns, L1), (system.ns - 90, L2), (300, L1), (system.ns, L2)):
+        call(n, L)
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] == free0
+
+
 def test_noalloc_rejects_sizes_beyond_its_maximum():
     import torch
     lib = M.library()
