@@ -169,6 +169,10 @@ def run_ours(args, rank, world, local):
         tuned = dict(cells_per_cutoff=best["cells_per_cutoff"],
                      kspace_ctas_per_sm=best["kspace_ctas_per_sm"],
                      pair_variant=best["pair_variant"])
+    if args.pair_variant is not None:
+        tuned["pair_variant"] = args.pair_variant
+    if args.cells is not None:
+        tuned["cells_per_cutoff"] = args.cells
     fp = M.ForcePath(system, [w["L"]] * 3, w["cutoff"], w["alpha"], w["kappa"], precision="mixed",
                      **kw, **tuned)
     fp.set_stream(stream.cuda_stream)
@@ -176,9 +180,15 @@ def run_ours(args, rank, world, local):
     f64 = M.ForcePath(system, [w["L"]] * 3, w["cutoff"], w["alpha"], w["kappa"],
                       precision="fp64", **kw)
     f64.set_stream(stream.cuda_stream)
-    fm, _ = fp.forces(w["r"])
-    fd, _ = f64.forces(w["r"])
+    fm, em = fp.forces(w["r"], measure=True)
+    fd, ed = f64.forces(w["r"], measure=True)
     force_err = float(np.sqrt(((fm - fd) ** 2).sum() / (fd ** 2).sum()))
+    # the energies beside the forces: the k-space energy relative to itself
+    # (the tensor-core passes accumulate in FP32 rounded toward zero), the
+    # total potential energy relative to the Ewald energy scale |E_self|
+    energy_err = {"ek_rel": (em["ek"] - ed["ek"]) / abs(ed["ek"]),
+                  "epot_rel_eself": (em["el"] + em["lj"] - ed["el"] - ed["lj"]) / abs(ed["eself"]),
+                  "lj_rel": (em["lj"] - ed["lj"]) / abs(ed["lj"])}
 
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 
@@ -324,6 +334,7 @@ def run_ours(args, rank, world, local):
             "fp64_path": {"value": round(value64, 4), "unit": "ns/day", "steps": k64},
             "mixed_over_fp64": round(value / value64, 3),
             "force_rel_rms_vs_fp64": force_err,
+            "energy_err_vs_fp64": {k: float("%.3g" % v) for k, v in energy_err.items()},
             "e2e": {"value": round(e2e, 4), "unit": "ns/day",
                     "h2d_bytes_per_step": rh.nbytes + r1h.nbytes,
                     "d2h_bytes_per_step": rh.nbytes + r1h.nbytes, "steps": ke2e},
@@ -401,12 +412,17 @@ def run_batch(args, rank, world, local):
     # accuracy against the FP64 path on the relaxed states
     b64 = make("fp64")
     num = den = 0.0
+    ek_err, ep_err = [], []
     for i in range(len(boxes)):
-        fm, _ = bm.box[i].forces(states[i][0])
-        fd, _ = b64.box[i].forces(states[i][0])
+        fm, em = bm.box[i].forces(states[i][0], measure=True)
+        fd, ed = b64.box[i].forces(states[i][0], measure=True)
         num += ((fm - fd) ** 2).sum()
         den += (fd ** 2).sum()
+        ek_err.append((em["ek"] - ed["ek"]) / abs(ed["ek"]))
+        ep_err.append((em["el"] + em["lj"] - ed["el"] - ed["lj"]) / abs(ed["eself"]))
     force_err = float(np.sqrt(num / den))
+    # the largest per-box energy errors
+    energy_err = {"ek_rel": max(ek_err, key=abs), "epot_rel_eself": max(ep_err, key=abs)}
 
     def timed(batch, k, warm):
         for i in range(len(boxes)):
@@ -486,6 +502,7 @@ def run_batch(args, rank, world, local):
             "fp64_path": {"value": round(value64, 4), "unit": "ns/day", "steps": k64},
             "mixed_over_fp64": round(value / value64, 3),
             "force_rel_rms_vs_fp64": force_err,
+            "energy_err_vs_fp64": {k: float("%.3g" % v) for k, v in energy_err.items()},
             "widom": {"insertions_per_s": round(len(boxes) * nins / (wms * 1e-3), 1),
                       "ms": round(wms, 3), "mu_K_box0": res[0]["mu"]},
             "e2e": {"value": round(ns_per_day(h, ke, e2e_s), 4), "unit": "ns/day",
@@ -559,6 +576,11 @@ def main():
                     help="> 0: Verlet lists of cutoff+skin instead of cells re-binned every step")
     ap.add_argument("--equilibrate", type=int, default=400,
                     help="relax the lattice start (rigid molecules, velocity rescaling)")
+    ap.add_argument("--pair-variant", type=int, default=None,
+                    help="FP32 pair kernel (mg_params.pair_variant; 8 = the group kernel), "
+                         "instead of the autotuner's choice")
+    ap.add_argument("--cells", type=int, default=None,
+                    help="cells per cutoff instead of the autotuner's choice")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -115,9 +115,12 @@ typedef struct {
   /* Ewald pass 1 work split: charge chunks sized for this many CTAs per SM;
      <=0 selects 10 (FP32) / 8 (FP64).  mg_autotune picks it. */
   int kspace_ctas_per_sm;
-  /* FP32 cell pair kernel: bit 0 = 8 warps per home cell (else 4), bit 2 =
-     16 warps per home cell (over bit 0), bit 1 = the erfc force spline in
-     shared memory (else read through L1).  mg_autotune picks it. */
+  /* FP32 pair kernel: 8 = the group kernel (a warp per group of 8 home
+     sites; neighbours pruned against the group's bounding box; needs a grid
+     of at least 2 cdiv + 1 cells per edge, else the cell kernel runs);
+     otherwise the cell kernel with bit 0 = 8 warps per home cell (else 4),
+     bit 2 = 16 warps per home cell (over bit 0), bit 1 = the erfc force
+     spline in shared memory (else read through L1).  mg_autotune picks it. */
   int pair_variant;
   /* thermostat (sim/thermo.c): 0 none, 1 Berendsen, 2 Bussi (stochastic
      velocity rescaling), both applied after every SHAKE step; 3 Nose-Hoover
@@ -367,10 +370,11 @@ int mg_xwidom(mg_ctx *ctx, int nlist, const int *mols, const int *vtype, const d
    No reference counterpart.  Times the force evaluation of the configuration
    r for every cell subdivision (cells_per_cutoff 1..3) and Ewald pass-1
    split (kspace_ctas_per_sm 6, 10, 16) and writes the fastest pair into
-   *par, then the fastest of the 8 pair_variant values at that choice.
-   Builds and frees its own trial contexts; ms[17] (optional) gets the time
-   per evaluation of each trial (cdiv-major, then the pair variants; -1 if
-   that grid is not possible). */
+   *par, then the fastest of the 8 cell-kernel pair_variant values at that
+   choice and of the group kernel (pair_variant 8) at every subdivision.
+   Builds and frees its own trial contexts; ms[20] (optional) gets the time
+   per evaluation of each trial (cdiv-major, then the 8 cell-kernel variants,
+   then the group kernel at cdiv 1..3; -1 if that grid is not possible). */
 int mg_autotune(const mg_topology *top, mg_params *par, const double *r, int nrep, double *ms);
 
 /* ---- adjoint ----

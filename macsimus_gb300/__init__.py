@@ -161,16 +161,17 @@ def library():
 def autotune(system, L, cutoff, alpha, kappa, r, nrep=3, **kw):
     """the fastest (cells_per_cutoff, kspace_ctas_per_sm, pair_variant) for
     this box and configuration (mg_autotune), with the timings (3x3 grid x
-    split, then the 8 pair variants)"""
+    split, the 8 cell-kernel pair variants, the group kernel at cdiv 1..3)"""
     t, p, keep = describe(system, L, cutoff, alpha, kappa, **kw)
-    ms = np.zeros(17)
+    ms = np.zeros(20)
     rr = _arr(r, np.float64).reshape(-1)
     rc = library().mg_autotune(C.byref(t), C.byref(p), rr.ctypes.data_as(_dp), int(nrep),
                                ms.ctypes.data_as(_dp))
     if rc:
         raise MGError(rc, "mg_autotune failed")
     return dict(cells_per_cutoff=p.cells_per_cutoff, kspace_ctas_per_sm=p.kspace_ctas_per_sm,
-                pair_variant=p.pair_variant, ms=ms[:9].reshape(3, 3), ms_pair=ms[9:])
+                pair_variant=p.pair_variant, ms=ms[:9].reshape(3, 3), ms_pair=ms[9:17],
+                ms_group=ms[17:])
 
 
 def fp32_peak_tflops():

@@ -53,11 +53,17 @@ struct mg_ctx {
   double *d_rs = nullptr, *d_fs = nullptr;  // staging of the host-array calls
   int *d_kind = nullptr, *d_mol = nullptr;
   int *d_key = nullptr, *d_idx = nullptr, *d_key_s = nullptr, *d_order = nullptr;
+  int4* d_pfix = nullptr;  // fixed-point site records in site order (cell list scratch)
   int* d_cell_start = nullptr;
   int *d_ccount = nullptr, *d_ccursor = nullptr;  // cell counts (kept zero), cursors
   int4* d_pj = nullptr;
   double4* d_pd = nullptr;
   int4* d_stencil = nullptr;
+  // group pair kernel: the stencil as z-runs, first group and cell of every
+  // group, its grid; nprows = energy rows of the pair kernel (cell or group)
+  int4* d_spans = nullptr;
+  int nspans = 0, ngroup_grid = 0, nprows = 0;
+  int *d_gstart = nullptr, *d_gcell = nullptr;
   PairF* d_ptabf = nullptr;
   PairD* d_ptabd = nullptr;
   float4 *d_erd = nullptr, *d_eru = nullptr;
@@ -182,6 +188,9 @@ struct mg_ctx {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   double* d_fk = nullptr;
   bool prof_on = false;
+  // one MD step (force-only / measured) captured as a CUDA graph
+  cudaGraphExec_t g_step = nullptr, g_meas = nullptr;
+  int graph_launches = 0, graph_launches_meas = 0;
   struct Rec { int id; cudaEvent_t a, b; };
   std::vector<std::string> pnames;
   std::vector<double> pms;
@@ -471,10 +480,25 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
                          (double)std::max(std::abs(dy) - 1, 0) * p->L[1] / nc3[1],
                          (double)std::max(std::abs(dz) - 1, 0) * p->L[2] / nc3[2]};
           double dmin2 = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
-          if (dmin2 < rgrid * rgrid * (1 + 1e-9)) st.push_back(make_int4(dx, dy, dz, 0));
+          // margin: a site's cell comes from its 32-bit fixed-point
+          // coordinate, within 2^-32 L of the cell's bounds
+          if (dmin2 < rgrid * rgrid * (1 + 1e-6)) st.push_back(make_int4(dx, dy, dz, 0));
         }
   }
   ctx->nstencil = (int)st.size();
+  // z-runs of the stencil: its entries come (dx, dy)-major with dz running
+  std::vector<int4> spans;
+  for (size_t k = 0; k < st.size();) {
+    size_t e = k + 1;
+    while (e < st.size() && st[e].x == st[k].x && st[e].y == st[k].y && st[e].z == st[e - 1].z + 1)
+      e++;
+    spans.push_back(make_int4(st[k].x, st[k].y, st[k].z, st[e - 1].z));
+    k = e;
+  }
+  ctx->nspans = (int)spans.size();
+  // work items of the group kernel: at most ns / GROUP_SITES + ncell
+  ctx->ngroup_grid = (int)(((long)ns / GROUP_SITES + ctx->ncell + GROUP_WARPS) / GROUP_WARPS);
+  ctx->nprows = std::max(ctx->ncell, ctx->ngroup_grid);
 
   // ---- k-vectors (cook's set), sorted into (kx,ky) columns of consecutive kz
   double kappa = p->kappa;
@@ -614,6 +638,7 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   CK(upload(&ctx->d_kind, ctx->h_kind.data(), ns));
   CK(upload(&ctx->d_mol, ctx->h_mol.data(), ns));
   CK(dalloc(&ctx->d_key, ns));
+  CK(dalloc(&ctx->d_pfix, ns));
   CK(dalloc(&ctx->d_idx, ns));
   CK(dalloc(&ctx->d_key_s, ns));
   CK(dalloc(&ctx->d_order, ns));
@@ -625,10 +650,15 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
     CK(dalloc(&ctx->d_ccursor, ctx->ncell));
   }
   CK(upload(&ctx->d_stencil, st.data(), st.size()));
+  CK(upload(&ctx->d_spans, spans.data(), spans.size()));
+  CK(dalloc(&ctx->d_gstart, (size_t)ctx->ncell + 1));
+  CK(dalloc(&ctx->d_gcell, (size_t)ns / GROUP_SITES + ctx->ncell + 1));
   ctx->nxblocks = (t->nmol + EXCL_THREADS - 1) / EXCL_THREADS;
-  ctx->nepart = std::max(ctx->ncell + ctx->nxblocks,
+  ctx->nepart = std::max(ctx->nprows + ctx->nxblocks,
                          std::max(list_blocks(ns, true), list_blocks(ns, false)));
   CK(dalloc(&ctx->d_epart, (size_t)ctx->nepart * 10));
+  // rows a pair kernel does not write stay zero
+  CK(cudaMemset(ctx->d_epart, 0, (size_t)ctx->nepart * 10 * sizeof(double)));
   if (ctx->use_list) {
     // capacity: the largest expected count in a sphere of the list radius at
     // 1.5 times the mean site density, in multiples of 32 (grown on overflow)
@@ -931,8 +961,8 @@ ExclArgs excl_args(mg_ctx* ctx, const double* r_dev, double* f) {
   a.alpha = (float)ctx->alpha;
   a.r = r_dev;
   a.f = f;
-  // energy rows after the cell kernel's
-  a.epart = ctx->d_epart + (size_t)ctx->ncell * 10;
+  // energy rows after the pair kernel's
+  a.epart = ctx->d_epart + (size_t)ctx->nprows * 10;
   return a;
 }
 
@@ -945,14 +975,16 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
   if (ctx->precision == MG_MIXED && ctx->overlap && ctx->nq > 0)
     CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
   const bool rebuild = !ctx->use_list || ctx->need_build || ctx->since_build >= ctx->nl_every;
+  const double iL[3] = {1.0 / ctx->L[0], 1.0 / ctx->L[1], 1.0 / ctx->L[2]};
   if (rebuild) {
-    // linked cells
-    PROF("cell_list", k_cell_list(L, ns, r_dev, ctx->d_status, ctx->L[0], ctx->L[1], ctx->L[2],
-                                  ctx->ncx, ctx->ncy, ctx->ncz, ctx->d_key, ctx->d_ccount,
+    // linked cells, with the fixed-point records of the sorted sites (d_pj,
+    // when the context has them) and the work items of the group kernel
+    PROF("cell_list", k_cell_list(L, ns, r_dev, ctx->d_status, iL, ctx->ncx, ctx->ncy, ctx->ncz,
+                                  ctx->d_kind, ctx->d_mol, ctx->d_pfix, ctx->d_key, ctx->d_ccount,
                                   ctx->d_ccursor, ctx->d_idx, ctx->d_order, ctx->d_key_s,
-                                  ctx->d_cell_start));
+                                  ctx->d_cell_start, ctx->d_gstart, ctx->d_pj, ctx->d_gcell));
   }
-  PairArgs pa;
+  PairArgs pa{};
   pa.ns = ns;
   pa.ncx = ctx->ncx;
   pa.ncy = ctx->ncy;
@@ -976,6 +1008,12 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
   pa.pdd = ctx->d_pdd;
   pa.pair_warps = (ctx->pair_variant & 4) ? 16 : ((ctx->pair_variant & 1) ? 8 : 4);
   pa.spline_smem = (ctx->pair_variant & 2) && ctx->ntab * 16 <= 200 * 1024 ? 1 : 0;
+  pa.group = (ctx->pair_variant & 8) ? 1 : 0;
+  pa.gstart = ctx->d_gstart;
+  pa.gcell = ctx->d_gcell;
+  pa.spans = ctx->d_spans;
+  pa.nspans = ctx->nspans;
+  pa.ngrid = ctx->ngroup_grid;
   KArgs ka;
   ka.nq = ctx->nq;
   ka.nk = ctx->nk;
@@ -986,9 +1024,7 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
   ka.Ky = ctx->Ky;
   ka.Kz = ctx->Kz;
   ka.row = ctx->row;
-  ka.Lx = ctx->L[0];
-  ka.Ly = ctx->L[1];
-  ka.Lz = ctx->L[2];
+  set_box(ka, ctx->L);
   ka.alpha = ctx->alpha;
   ka.qsite = ctx->d_qsite;
   ka.qval = ctx->d_qval;
@@ -1010,7 +1046,7 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
   ka.ns = ctx->ns;
   ka.status = ctx->d_status;
   ListArgs la = list_args(ctx);
-  int nerows = ctx->ncell;
+  int nerows = ctx->nprows;
   if (ctx->precision == MG_MIXED) {
     // the k-space chain on kstream, concurrent with the r-space chain below;
     // its forces go to d_fk and are added at the join
@@ -1028,8 +1064,10 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
       PROFS("ewald_kforce", ks, kf_mixed(ctx, LK, kk));
       CK(cudaEventRecord(ctx->ev_join, ks));
     }
-    PROF("gather", k_gather_mixed(L, ns, r_dev, ctx->d_order, ctx->d_kind, ctx->d_mol, ctx->L[0],
-                                  ctx->L[1], ctx->L[2], ctx->d_pj));
+    // new positions with the order of an earlier build (lists kept)
+    if (!rebuild)
+      PROF("gather", k_gather_mixed(L, ns, r_dev, ctx->d_order, ctx->d_kind, ctx->d_mol, iL,
+                                    ctx->d_pj));
     if (ctx->polar) PROF("gather", k_gather_drude(L, ns, r_dev, ctx->d_order, ctx->d_pdj, nullptr));
     if (ctx->use_list) {
       if (rebuild) {
@@ -1047,7 +1085,7 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
       // summation order with and without the concurrent k-space chain
       ExclArgs xa = excl_args(ctx, r_dev, f_dev);
       PROF("exclusions", k_excl_mixed(L, xa, measure, ctx->polar));
-      nerows = ctx->ncell + ctx->nxblocks;
+      nerows = ctx->nprows + ctx->nxblocks;
     }
     if (fork) {
       CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
@@ -1063,8 +1101,7 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
     if (ctx->polar) PROF("gather", k_gather_drude(L, ns, r_dev, ctx->d_order, nullptr, ctx->d_pdd));
     if (ctx->use_list) {
       if (rebuild) {
-        PROF("gather", k_gather_mixed(L, ns, r_dev, ctx->d_order, ctx->d_kind, ctx->d_mol,
-                                      ctx->L[0], ctx->L[1], ctx->L[2], ctx->d_pj));
+        // the fixed-point records came with the cell list
         int rc = build_lists(ctx, r_dev);
         if (rc) return rc;
         la = list_args(ctx);
@@ -1302,6 +1339,131 @@ int check_status(mg_ctx* ctx) {
   return fail(ctx, MG_ERR_SHAKE, "SHAKE: too many iterations");
 }
 
+// the steps kernel by kernel (Drude boxes, neighbour lists, profiling)
+int md_steps_launched(mg_ctx* ctx, int nsteps, mg_energy* en) {
+  Launch L = launch(ctx);
+  const int nkin = (ctx->nmol + 127) / 128;
+  for (int s = 0; s < nsteps; s++) {
+    const bool last = s == nsteps - 1;
+    const bool measure = last && en != nullptr;
+    if (ctx->use_list && ctx->dmax_pending) {
+      // the previous step's largest displacement since the build: rebuild
+      // once half of the skin/2 budget is used (one more step cannot spend
+      // the other half at any physical speed)
+      CK(cudaEventSynchronize(ctx->ev_dmax));
+      ctx->dmax_pending = false;
+      float d2;
+      std::memcpy(&d2, ctx->h_dmax, sizeof(float));
+      if (d2 > 0.0625 * ctx->skin * ctx->skin) ctx->need_build = true;
+    }
+    if (ctx->polar && ctx->nd > 0) {
+      // ASPC predictor, then scf_iter force evaluations each followed by one
+      // SCF iteration (sim/constrd.c:726-736, sim/pred2.c:56-97)
+      const int K2 = ctx->aspc_k + 2;
+      const size_t slot = 3 * (size_t)ctx->nd;
+      AspcCoef B;
+      double om;
+      aspc_coefficients(ctx->aspc_kk, B.b, &om);
+      B.n = ctx->aspc_kk + 2;
+      DrudeArgs d = drude_args(ctx);
+      PROF("drude_aspc", k_aspc_predict(L, d, ctx->d_hist, K2, ctx->hist_h, B, ctx->d_r));
+      if (ctx->aspc_kk < ctx->aspc_k) {
+        ctx->aspc_kk++;
+        aspc_coefficients(ctx->aspc_kk, B.b, &om);
+        ctx->cur_omega = om;
+      }
+      const int hn = (ctx->hist_h + 1) % K2;
+      for (int it = 0; it < ctx->scf_iter; it++) {
+        const bool lastit = it == ctx->scf_iter - 1;
+        int rc = forces_async(ctx, ctx->d_r, ctx->d_f, measure && lastit);
+        if (rc) return rc;
+        rc = selffield_async(ctx, ctx->d_r, ctx->d_f, ctx->cur_omega, measure && lastit,
+                             lastit ? ctx->d_hist + slot * hn : nullptr);
+        if (rc) return rc;
+      }
+      ctx->hist_h = hn;
+    } else {
+      int rc = forces_async(ctx, ctx->d_r, ctx->d_f, measure);
+      if (rc) return rc;
+    }
+    // forces on dependants to their parents (sim/constrd.c:747), the step,
+    // and dependant positions for the next force evaluation: the same
+    // positions cook's depend_r makes at the start of its next step
+    if (ctx->ndep > 0) PROF("depend", k_depend_f(L, depend_args(ctx), ctx->d_f));
+    PROF("shake", k_shake(L, shake_args(ctx, measure)));
+    if (ctx->ndep > 0) PROF("depend", k_depend_r(L, depend_args(ctx), ctx->d_r));
+    if (ctx->use_list) {
+      ctx->since_build++;
+      PROF("neighbour_list", k_check_skin(L, ctx->ns, ctx->d_r, ctx->d_rbuild,
+                                          0.25 * ctx->skin * ctx->skin, ctx->L, ctx->d_status,
+                                          ctx->d_dmax));
+      CK(cudaMemcpyAsync(ctx->h_dmax, ctx->d_dmax, sizeof(int), cudaMemcpyDeviceToHost,
+                         ctx->stream));
+      CK(cudaEventRecord(ctx->ev_dmax, ctx->stream));
+      ctx->dmax_pending = true;
+    }
+    if (measure) {
+      PROF("reduce", k_reduce_sum(L, ctx->d_kinpart, nkin, 1, ctx->d_sums + 17));
+      PROF("reduce", k_reduce_sum(L, ctx->d_meas, nkin, 13, ctx->d_sums + 32));
+    }
+    if (ctx->thermostat)
+      PROF("thermostat", k_thermostat(L, thermo_args(ctx), ctx->d_kinpart, ctx->d_chi, ctx->d_r1));
+    // cook calls bounddr after Shake (and its thermostat) and normalize
+    // (sim/main.c:1607-1623)
+    if (ctx->drmax > 0)
+      PROF("bounddr", k_bounddr(L, ctx->ns, ctx->drmax, ctx->d_r1, ctx->d_bdrep));
+    // then the momentum drift (cook's removedrifts with DRIFT_STEP,
+    // sim/main.c:1626)
+    if (ctx->drift_step)
+      PROF("drift", k_remove_drift(L, ctx->ns, ctx->d_mass, ctx->total_mass, ctx->d_r1,
+                                   ctx->d_driftpart, ctx->d_drift, nullptr));
+  }
+  return MG_OK;
+}
+
+void drop_graphs(mg_ctx* ctx) {
+  if (ctx->g_step) cudaGraphExecDestroy(ctx->g_step);
+  if (ctx->g_meas) cudaGraphExecDestroy(ctx->g_meas);
+  ctx->g_step = ctx->g_meas = nullptr;
+}
+
+// steps that md_step_enqueue covers (no Drude SCF, cells re-binned every
+// step) and that nothing times kernel by kernel run as a captured graph
+bool graph_step_ok(const mg_ctx* ctx) {
+  return !ctx->polar && !ctx->use_list && !ctx->prof_on;
+}
+
+// capture one step on the context's own stream (a caller's stream may be
+// the legacy default stream, which cannot capture); the graph is launched
+// on whatever stream the context runs on
+int capture_md_step(mg_ctx* ctx, bool measure, cudaGraphExec_t* out) {
+  cudaStream_t keep = ctx->stream;
+  CK(cudaStreamSynchronize(keep));
+  ctx->stream = ctx->own_stream;
+  const int l0 = ctx->launches;
+  cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) {
+    ctx->stream = keep;
+    return fail(ctx, MG_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+  }
+  int rc = md_step_enqueue(ctx, measure);
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(ctx->stream, &g);
+  ctx->stream = keep;
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return fail(ctx, MG_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess)
+    return fail(ctx, MG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  (measure ? ctx->graph_launches_meas : ctx->graph_launches) = ctx->launches - l0;
+  ctx->launches = l0;
+  return MG_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1322,8 +1484,9 @@ mg_ctx* mg_create(const mg_topology* top, const mg_params* par, int* status) {
 int mg_destroy(mg_ctx* ctx) {
   if (!ctx) return MG_OK;
   void* bufs[] = {ctx->d_rs, ctx->d_fs, ctx->d_r,      ctx->d_f,       ctx->d_r1,    ctx->d_p,      ctx->d_kind,
-                  ctx->d_mol,    ctx->d_key,     ctx->d_idx,   ctx->d_key_s,  ctx->d_order,
-                  ctx->d_cell_start, ctx->d_ccount, ctx->d_ccursor, ctx->d_pj, ctx->d_pd,  ctx->d_stencil,
+                  ctx->d_mol,    ctx->d_key,     ctx->d_pfix,   ctx->d_idx,   ctx->d_key_s,  ctx->d_order,
+                  ctx->d_cell_start, ctx->d_ccount, ctx->d_ccursor, ctx->d_spans, ctx->d_gstart,
+                  ctx->d_gcell, ctx->d_pj, ctx->d_pd,  ctx->d_stencil,
                   ctx->d_ptabf,  ctx->d_ptabd,   ctx->d_erd,   ctx->d_eru,    ctx->d_ert,
                   ctx->d_epart,  ctx->d_qsite,   ctx->d_qval,  ctx->d_task,   ctx->d_col,
                   ctx->d_kvec,   ctx->d_ekk,     ctx->d_S,     ctx->d_Wf,     ctx->d_Wd,
@@ -1346,6 +1509,8 @@ int mg_destroy(mg_ctx* ctx) {
   if (ctx->h_dmax) cudaFreeHost(ctx->h_dmax);
   if (ctx->ev_dmax) cudaEventDestroy(ctx->ev_dmax);
   for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
+  if (ctx->g_step) cudaGraphExecDestroy(ctx->g_step);
+  if (ctx->g_meas) cudaGraphExecDestroy(ctx->g_meas);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   if (ctx->kstream) cudaStreamDestroy(ctx->kstream);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
@@ -1425,9 +1590,7 @@ int mg_ewald(mg_ctx* ctx, const double* r, double* f, double* energy) {
   ka.Ky = ctx->Ky;
   ka.Kz = ctx->Kz;
   ka.row = ctx->row;
-  ka.Lx = ctx->L[0];
-  ka.Ly = ctx->L[1];
-  ka.Lz = ctx->L[2];
+  set_box(ka, ctx->L);
   ka.alpha = ctx->alpha;
   ka.qsite = ctx->d_qsite;
   ka.qval = ctx->d_qval;
@@ -1585,82 +1748,26 @@ int mg_playback_frame(mg_ctx* ctx, int what, int flags, float* frame) {
 int mg_md_steps(mg_ctx* ctx, int nsteps, mg_energy* en) {
   if (!ctx || !ctx->have_state || nsteps < 0) return fail(ctx, MG_ERR_ARG, "no MD state");
   ctx->launches = 0;
-  Launch L = launch(ctx);
-  const int nkin = (ctx->nmol + 127) / 128;
-  for (int s = 0; s < nsteps; s++) {
-    const bool last = s == nsteps - 1;
-    const bool measure = last && en != nullptr;
-    if (ctx->use_list && ctx->dmax_pending) {
-      // the previous step's largest displacement since the build: rebuild
-      // once half of the skin/2 budget is used (one more step cannot spend
-      // the other half at any physical speed)
-      CK(cudaEventSynchronize(ctx->ev_dmax));
-      ctx->dmax_pending = false;
-      float d2;
-      std::memcpy(&d2, ctx->h_dmax, sizeof(float));
-      if (d2 > 0.0625 * ctx->skin * ctx->skin) ctx->need_build = true;
-    }
-    if (ctx->polar && ctx->nd > 0) {
-      // ASPC predictor, then scf_iter force evaluations each followed by one
-      // SCF iteration (sim/constrd.c:726-736, sim/pred2.c:56-97)
-      const int K2 = ctx->aspc_k + 2;
-      const size_t slot = 3 * (size_t)ctx->nd;
-      AspcCoef B;
-      double om;
-      aspc_coefficients(ctx->aspc_kk, B.b, &om);
-      B.n = ctx->aspc_kk + 2;
-      DrudeArgs d = drude_args(ctx);
-      PROF("drude_aspc", k_aspc_predict(L, d, ctx->d_hist, K2, ctx->hist_h, B, ctx->d_r));
-      if (ctx->aspc_kk < ctx->aspc_k) {
-        ctx->aspc_kk++;
-        aspc_coefficients(ctx->aspc_kk, B.b, &om);
-        ctx->cur_omega = om;
-      }
-      const int hn = (ctx->hist_h + 1) % K2;
-      for (int it = 0; it < ctx->scf_iter; it++) {
-        const bool lastit = it == ctx->scf_iter - 1;
-        int rc = forces_async(ctx, ctx->d_r, ctx->d_f, measure && lastit);
-        if (rc) return rc;
-        rc = selffield_async(ctx, ctx->d_r, ctx->d_f, ctx->cur_omega, measure && lastit,
-                             lastit ? ctx->d_hist + slot * hn : nullptr);
+  if (graph_step_ok(ctx)) {
+    // the step as one captured graph per kind (force-only, measured)
+    for (int s = 0; s < nsteps; s++) {
+      const bool measure = s == nsteps - 1 && en != nullptr;
+      cudaGraphExec_t& g = measure ? ctx->g_meas : ctx->g_step;
+      if (!g) {
+        int rc = capture_md_step(ctx, measure, &g);
         if (rc) return rc;
       }
-      ctx->hist_h = hn;
-    } else {
-      int rc = forces_async(ctx, ctx->d_r, ctx->d_f, measure);
-      if (rc) return rc;
+      CK(cudaGraphLaunch(g, ctx->stream));
+      ctx->launches += measure ? ctx->graph_launches_meas : ctx->graph_launches;
     }
-    // forces on dependants to their parents (sim/constrd.c:747), the step,
-    // and dependant positions for the next force evaluation: the same
-    // positions cook's depend_r makes at the start of its next step
-    if (ctx->ndep > 0) PROF("depend", k_depend_f(L, depend_args(ctx), ctx->d_f));
-    PROF("shake", k_shake(L, shake_args(ctx, measure)));
-    if (ctx->ndep > 0) PROF("depend", k_depend_r(L, depend_args(ctx), ctx->d_r));
-    if (ctx->use_list) {
-      ctx->since_build++;
-      PROF("neighbour_list", k_check_skin(L, ctx->ns, ctx->d_r, ctx->d_rbuild,
-                                          0.25 * ctx->skin * ctx->skin, ctx->L, ctx->d_status,
-                                          ctx->d_dmax));
-      CK(cudaMemcpyAsync(ctx->h_dmax, ctx->d_dmax, sizeof(int), cudaMemcpyDeviceToHost,
-                         ctx->stream));
-      CK(cudaEventRecord(ctx->ev_dmax, ctx->stream));
-      ctx->dmax_pending = true;
+    if (nsteps > 0) {
+      // what the captured force evaluation leaves behind, as a launched one
+      ctx->last_r = ctx->d_r;
+      ctx->have_cells = true;
     }
-    if (measure) {
-      PROF("reduce", k_reduce_sum(L, ctx->d_kinpart, nkin, 1, ctx->d_sums + 17));
-      PROF("reduce", k_reduce_sum(L, ctx->d_meas, nkin, 13, ctx->d_sums + 32));
-    }
-    if (ctx->thermostat)
-      PROF("thermostat", k_thermostat(L, thermo_args(ctx), ctx->d_kinpart, ctx->d_chi, ctx->d_r1));
-    // cook calls bounddr after Shake (and its thermostat) and normalize
-    // (sim/main.c:1607-1623)
-    if (ctx->drmax > 0)
-      PROF("bounddr", k_bounddr(L, ctx->ns, ctx->drmax, ctx->d_r1, ctx->d_bdrep));
-    // then the momentum drift (cook's removedrifts with DRIFT_STEP,
-    // sim/main.c:1626)
-    if (ctx->drift_step)
-      PROF("drift", k_remove_drift(L, ctx->ns, ctx->d_mass, ctx->total_mass, ctx->d_r1,
-                                   ctx->d_driftpart, ctx->d_drift, nullptr));
+  } else {
+    int rc = md_steps_launched(ctx, nsteps, en);
+    if (rc) return rc;
   }
   if (en) {
     int rc = fetch_sums(ctx);
@@ -1953,7 +2060,7 @@ int mg_xwidom(mg_ctx* ctx, int nlist, const int* mols, const int* vtype, const d
 namespace {
 
 PairArgs pair_args(mg_ctx* ctx) {
-  PairArgs pa;
+  PairArgs pa{};
   pa.ns = ctx->ns;
   pa.ncx = ctx->ncx;
   pa.ncy = ctx->ncy;
@@ -1990,9 +2097,7 @@ KArgs kspace_args(mg_ctx* ctx) {
   ka.Ky = ctx->Ky;
   ka.Kz = ctx->Kz;
   ka.row = ctx->row;
-  ka.Lx = ctx->L[0];
-  ka.Ly = ctx->L[1];
-  ka.Lz = ctx->L[2];
+  set_box(ka, ctx->L);
   ka.alpha = ctx->alpha;
   ka.qsite = ctx->d_qsite;
   ka.qval = ctx->d_qval;
@@ -2151,6 +2256,7 @@ int mg_nose_state(mg_ctx* ctx, double state[3]) {
 
 int mg_set_overlap(mg_ctx* ctx, int on) {
   if (!ctx) return MG_ERR_ARG;
+  if (ctx->overlap != (on != 0)) drop_graphs(ctx);
   ctx->overlap = on != 0;
   return MG_OK;
 }
@@ -2518,6 +2624,37 @@ int mg_autotune(const mg_topology* top, mg_params* par, const double* r, int nre
       if (t > 0 && t < bestv) {
         bestv = t;
         bv = v;
+      }
+    }
+    // the group pair kernel (variant 8) at every cell subdivision: its
+    // pruning favours other cells than the cell kernel does
+    for (int a = 0; a < 3 && rc == MG_OK; a++) {
+      mg_params p2 = *par;
+      p2.cells_per_cutoff = cd[a];
+      p2.kspace_ctas_per_sm = bk;
+      p2.pair_variant = 8;
+      int st = 0;
+      mg_ctx* c = mg_create(top, &p2, &st);
+      double t = -1;
+      if (c) {
+        int e = mg_forces_device(c, r_dev, f_dev, 0, nullptr);
+        if (!e) {
+          cudaEventRecord(e0, c->stream);
+          for (int k = 0; k < nrep && !e; k++) e = mg_forces_device(c, r_dev, f_dev, 0, nullptr);
+          cudaEventRecord(e1, c->stream);
+          cudaEventSynchronize(e1);
+          float f = 0;
+          cudaEventElapsedTime(&f, e0, e1);
+          if (!e) t = f / nrep;
+        }
+        if (e) rc = e;
+        mg_destroy(c);
+      }
+      if (ms) ms[17 + a] = t;
+      if (t > 0 && t < bestv) {
+        bestv = t;
+        bv = 8;
+        bc = cd[a];
       }
     }
   }

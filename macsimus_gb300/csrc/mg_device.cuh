@@ -9,13 +9,18 @@ constexpr int NEN = 10;   // er, lj, vir, Pvir[6], (spare)
 
 __device__ __forceinline__ double wrap01(double s) { return s - floor(s); }
 
-// a coordinate as a 32-bit fixed-point fraction of the box edge Lb (the
+// a coordinate as a 32-bit fixed-point fraction of the box edge (the
 // difference of two such numbers, as 32-bit integers, is the nearest-image
-// separation)
-__device__ __forceinline__ int fixed32(double x, double Lb) {
-  double s = wrap01(x / Lb);
+// separation); iLb = 1 / box edge, formed once on the host (an FP64 division
+// costs tens of operations on this GPU's narrow FP64 pipe)
+__device__ __forceinline__ int fixed32(double x, double iLb) {
+  double s = wrap01(x * iLb);
   long long v = llrint(s * 4294967296.0);
   return (int)(unsigned int)(v & 0xffffffffLL);
+}
+// the cell of a fixed-point coordinate among n cells along the edge
+__device__ __forceinline__ int fixed_cell(int fx, int n) {
+  return (int)(((unsigned long long)(unsigned)fx * (unsigned)n) >> 32);
 }
 
 // Ewald exclusion term -erf(alpha r)/r and its f/r (cook's exacterud_sqrt);

@@ -87,12 +87,23 @@ struct Launch {
 // every site; count [ncell rounded up to 4] zero on entry and on return;
 // cursor [ncell], slot_site [ns] scratch; out: order [ns] sorted -> site
 // (site order within a cell), key_s [ns] the sorted cells, start [ncell+1]
-cudaError_t k_cell_list(const Launch& L, int ns, const double* r, int* status, double Lx,
-                        double Ly, double Lz, int ncx, int ncy, int ncz, int* key, int* count,
-                        int* cursor, int* slot_site, int* order, int* key_s, int* start);
+// pfix [ns] scratch: the fixed-point site records in site order; pj (or
+// null) gets them in cell order: {x, y, z as 32-bit fractions of the box,
+// (molecule << 8) | kind} (kind, mol: [ns] site tables).  gstart
+// [ncell+1]: first group of each cell (groups: its sites in runs of
+// GROUP_SITES, in cell order); gcell [ns / GROUP_SITES + ncell] (or null):
+// the cell of every group
+cudaError_t k_cell_list(const Launch& L, int ns, const double* r, int* status, const double iL[3],
+                        int ncx, int ncy, int ncz, const int* kind, const int* mol, int4* pfix,
+                        int* key, int* count, int* cursor, int* slot_site, int* order,
+                        int* key_s, int* start, int* gstart, int4* pj, int* gcell);
+// sites per work item (group) of the group pair kernel, its warps per CTA
+constexpr int GROUP_SITES = 8;
+constexpr int GROUP_WARPS = 4;
+// the fixed-point records of the sorted sites for new positions and an
+// unchanged order (neighbour lists kept from an earlier build)
 cudaError_t k_gather_mixed(const Launch& L, int ns, const double* r, const int* order,
-                           const int* kind, const int* mol, double Lx, double Ly, double Lz,
-                           int4* pj);
+                           const int* kind, const int* mol, const double iL[3], int4* pj);
 cudaError_t k_gather_fp64(const Launch& L, int ns, const double* r, const int* order,
                           const int* kind, const int* mol, double Lx, double Ly, double Lz,
                           double4* pd);
@@ -117,6 +128,15 @@ struct PairArgs {
   int pair_warps;           // mixed cell kernel: warps per CTA (4 or 8)
   int spline_smem;          // mixed cell kernel: force spline in shared memory
   const double4* pdd;       // FP64, Drude builds: sorted Drude displacements
+  // group pair kernel (FP32 path, grids with the nearest image per cell):
+  // work items = groups of GROUP_SITES sites of a home cell (gstart, gcell),
+  // the stencil as z-runs (dx, dy, dzlo, dzhi) of consecutive cells
+  int group;
+  const int* gstart;
+  const int* gcell;
+  const int4* spans;
+  int nspans;
+  int ngrid;                // CTAs of the group kernel (its energy rows)
 };
 cudaError_t k_pair_mixed(const Launch& L, const PairArgs& a, const int4* pj,
                          const PairF* ptab, const float4* erd, const float4* eru,
@@ -128,6 +148,7 @@ struct KArgs {
   int nq, nk, ntask, ncol, nchunk;
   int Kx, Ky, Kz, row;      // table extents; row = (Kx+1)+(2Ky+1)+(2Kz+1)
   double Lx, Ly, Lz;
+  double iLx, iLy, iLz;     // 1 / box edges (set_box)
   double alpha;
   const int* qsite;         // [nq] site of each charge
   const double* qval;       // [nq]
@@ -149,6 +170,14 @@ struct KArgs {
   int ns;
   int* status;              // device status word (tensor-core waits that give up: 16)
 };
+inline void set_box(KArgs& a, const double L[3]) {
+  a.Lx = L[0];
+  a.Ly = L[1];
+  a.Lz = L[2];
+  a.iLx = 1.0 / L[0];
+  a.iLy = 1.0 / L[1];
+  a.iLz = 1.0 / L[2];
+}
 cudaError_t k_add_forces(const Launch& L, size_t n, const double* fk, double* f);
 // qf: [nq] scratch for the charges' fixed-point coordinates
 cudaError_t k_phase_tables_mixed(const Launch& L, const KArgs& a, const double* r, float2* tab,

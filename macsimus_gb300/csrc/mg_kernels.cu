@@ -1,6 +1,8 @@
 // sm_103a kernels of the cook force path.
 //
-//   cell list      k_prep_cells + (CUB radix sort) + k_cell_bounds + k_gather_*
+//   cell list      k_cell_list: a counting sort of the sites by cell (count,
+//                  scan, scatter, per-cell rank) with the fixed-point site
+//                  records of the FP32 path; k_gather_* for the FP64 path
 //   r-space sum    k_pair_mixed / k_pair_fp64: one CTA per home cell, its warps
 //                  split the neighbour-cell stencil; neighbour cells are staged
 //                  per warp in shared memory (16-byte loads) and every lane owns
@@ -29,10 +31,6 @@ static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 // ------------------------------------------------------------- cell list --
 
 
-__device__ __forceinline__ int cell_coord(double s, int n) {
-  int c = (int)(s * n);
-  return c < 0 ? 0 : (c >= n ? n - 1 : c);
-}
 
 // ------------------------------------------------------ the cell list --
 //
@@ -49,37 +47,51 @@ __device__ __forceinline__ int cell_coord(double s, int n) {
 //                 order[] and the sorted keys (the slots of cell_scatter
 //                 depend on the timing of the atomics; the ranks do not)
 
-// cell key of every site; a non-finite coordinate sets bit 1 of *status and
-// the site is binned into cell 0 so that every later index stays in range
-__global__ void cell_count_kernel(int ns, const double* __restrict__ r, double Lx, double Ly,
-                                  double Lz, int ncx, int ncy, int ncz, int* __restrict__ key,
+// the fixed-point record of every site (site order) and its cell, from the
+// fixed-point coordinates (so that the cell and the coordinates the pair
+// kernels use agree to the last bit); a non-finite coordinate sets bit 1 of
+// *status and the site is binned into cell 0 so that every later index
+// stays in range
+__global__ void cell_count_kernel(int ns, const double* __restrict__ r, double iLx, double iLy,
+                                  double iLz, int ncx, int ncy, int ncz,
+                                  const int* __restrict__ kind, const int* __restrict__ mol,
+                                  int4* __restrict__ pfix, int* __restrict__ key,
                                   int* __restrict__ count, int* __restrict__ status) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ns) return;
   const double x = r[3 * i], y = r[3 * i + 1], z = r[3 * i + 2];
   int k = 0;
+  const int4 q = make_int4(fixed32(x, iLx), fixed32(y, iLy), fixed32(z, iLz),
+                           (mol[i] << 8) | kind[i]);
   if (isfinite(x) && isfinite(y) && isfinite(z)) {
-    const int cx = cell_coord(wrap01(x / Lx), ncx), cy = cell_coord(wrap01(y / Ly), ncy),
-              cz = cell_coord(wrap01(z / Lz), ncz);
-    k = (cx * ncy + cy) * ncz + cz;
+    k = (fixed_cell(q.x, ncx) * ncy + fixed_cell(q.y, ncy)) * ncz + fixed_cell(q.z, ncz);
   } else {
     atomicOr(status, 2);
   }
+  pfix[i] = q;
   key[i] = k;
   atomicAdd(count + k, 1);
 }
 
 // exclusive scan of count[0..ncell) into start[0..ncell] and cursor[], in
 // tiles of 4 x 1024 counts (int4 loads; count is padded with zeros to a
-// multiple of 4 entries); the counts are cleared for the next list
+// multiple of 4 entries); the counts are cleared for the next list.  With
+// gstart the same scan of the group counts ceil(count / GROUP_SITES) (the
+// work items of the group pair kernel) goes to gstart[0..ncell].
 constexpr int SCAN_THREADS = 1024;
+__device__ __forceinline__ int2 add2(int2 a, int2 b) { return make_int2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ int2 shfl_up2(int2 v, int o) {
+  return make_int2(__shfl_up_sync(0xffffffffu, v.x, o), __shfl_up_sync(0xffffffffu, v.y, o));
+}
+__device__ __forceinline__ int ngroups(int n) { return (n + GROUP_SITES - 1) / GROUP_SITES; }
+
 __global__ void __launch_bounds__(SCAN_THREADS)
 cell_scan_kernel(int ncell, int* __restrict__ count, int* __restrict__ start,
-                 int* __restrict__ cursor) {
-  __shared__ int wsum[SCAN_THREADS / 32];
-  __shared__ int carry_s;
+                 int* __restrict__ cursor, int* __restrict__ gstart) {
+  __shared__ int2 wsum[SCAN_THREADS / 32];
+  __shared__ int2 carry_s;
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-  if (t == 0) carry_s = 0;
+  if (t == 0) carry_s = make_int2(0, 0);
   __syncthreads();
   const int n4 = (ncell + 3) / 4;
   for (int base = 0; base < n4; base += SCAN_THREADS) {
@@ -89,41 +101,51 @@ cell_scan_kernel(int ncell, int* __restrict__ count, int* __restrict__ start,
       v = reinterpret_cast<int4*>(count)[q];
       reinterpret_cast<int4*>(count)[q] = make_int4(0, 0, 0, 0);
     }
-    const int tot = v.x + v.y + v.z + v.w;
-    int incl = tot;
+    // (sites, groups) of the four cells
+    const int2 tot = make_int2(v.x + v.y + v.z + v.w,
+                               ngroups(v.x) + ngroups(v.y) + ngroups(v.z) + ngroups(v.w));
+    int2 incl = tot;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
+      const int2 y = shfl_up2(incl, o);
+      if (lane >= o) incl = add2(incl, y);
     }
     if (lane == 31) wsum[w] = incl;
-    const int carry = carry_s;
+    const int2 carry = carry_s;
     __syncthreads();
     if (w == 0) {
-      int x = wsum[lane];
+      int2 x = wsum[lane];
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
+        const int2 y = shfl_up2(x, o);
+        if (lane >= o) x = add2(x, y);
       }
       wsum[lane] = x;   // inclusive sums of the warps
     }
     __syncthreads();
-    const int ex = carry + (w ? wsum[w - 1] : 0) + incl - tot;
+    const int2 wprev = w ? wsum[w - 1] : make_int2(0, 0);
+    const int ex = carry.x + wprev.x + incl.x - tot.x;
+    const int gx = carry.y + wprev.y + incl.y - tot.y;
     if (q < n4) {
       const int e[4] = {ex, ex + v.x, ex + v.x + v.y, ex + v.x + v.y + v.z};
+      const int g[4] = {gx, gx + ngroups(v.x), gx + ngroups(v.x) + ngroups(v.y),
+                        gx + ngroups(v.x) + ngroups(v.y) + ngroups(v.z)};
 #pragma unroll
       for (int k = 0; k < 4; k++)
         if (4 * q + k < ncell) {
           start[4 * q + k] = e[k];
           cursor[4 * q + k] = e[k];
+          if (gstart) gstart[4 * q + k] = g[k];
         }
     }
     __syncthreads();
-    if (t == SCAN_THREADS - 1) carry_s = carry + wsum[31];
+    if (t == SCAN_THREADS - 1) carry_s = add2(carry, wsum[31]);
     __syncthreads();
   }
-  if (t == 0) start[ncell] = carry_s;
+  if (t == 0) {
+    start[ncell] = carry_s.x;
+    if (gstart) gstart[ncell] = carry_s.y;
+  }
 }
 
 __global__ void cell_scatter_kernel(int ns, const int* __restrict__ key, int* __restrict__ cursor,
@@ -136,11 +158,16 @@ __global__ void cell_scatter_kernel(int ns, const int* __restrict__ key, int* __
 constexpr int ORDER_THREADS = 256;
 __global__ void __launch_bounds__(ORDER_THREADS)
 cell_order_kernel(int ncell, const int* __restrict__ start, const int* __restrict__ slot_site,
-                  int* __restrict__ order, int* __restrict__ key_s) {
+                  const int4* __restrict__ pfix, int* __restrict__ order, int* __restrict__ key_s,
+                  int4* __restrict__ pj, const int* __restrict__ gstart,
+                  int* __restrict__ gcell) {
   const int c = blockIdx.x * (ORDER_THREADS / 32) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (c >= ncell) return;
   const int s0 = start[c], n = start[c + 1] - s0;
+  // the cell of each of its groups (work items of the group pair kernel)
+  if (gcell)
+    for (int g = gstart[c] + lane; g < gstart[c + 1]; g += 32) gcell[g] = c;
   if (n <= 32) {
     // one site per lane, ranks by shuffles
     const int mine = lane < n ? slot_site[s0 + lane] : 0x7fffffff;
@@ -149,6 +176,7 @@ cell_order_kernel(int ncell, const int* __restrict__ start, const int* __restric
     if (lane < n) {
       order[s0 + rank] = mine;
       key_s[s0 + rank] = c;
+      if (pj) pj[s0 + rank] = pfix[mine];
     }
   } else {
     for (int e = lane; e < n; e += 32) {
@@ -157,42 +185,44 @@ cell_order_kernel(int ncell, const int* __restrict__ start, const int* __restric
       for (int j = 0; j < n; j++) rank += slot_site[s0 + j] < mine;
       order[s0 + rank] = mine;
       key_s[s0 + rank] = c;
+      if (pj) pj[s0 + rank] = pfix[mine];
     }
   }
 }
 
-cudaError_t k_cell_list(const Launch& L, int ns, const double* r, int* status, double Lx,
-                        double Ly, double Lz, int ncx, int ncy, int ncz, int* key, int* count,
-                        int* cursor, int* slot_site, int* order, int* key_s, int* start) {
+cudaError_t k_cell_list(const Launch& L, int ns, const double* r, int* status, const double iL[3],
+                        int ncx, int ncy, int ncz, const int* kind, const int* mol, int4* pfix,
+                        int* key, int* count, int* cursor, int* slot_site, int* order,
+                        int* key_s, int* start, int* gstart, int4* pj, int* gcell) {
   const int ncell = ncx * ncy * ncz;
-  cell_count_kernel<<<cdiv(ns, 256), 256, 0, L.s>>>(ns, r, Lx, Ly, Lz, ncx, ncy, ncz, key, count,
-                                                    status);
+  cell_count_kernel<<<cdiv(ns, 256), 256, 0, L.s>>>(ns, r, iL[0], iL[1], iL[2], ncx, ncy, ncz,
+                                                    kind, mol, pfix, key, count, status);
   LAUNCHED(L);
-  cell_scan_kernel<<<1, SCAN_THREADS, 0, L.s>>>(ncell, count, start, cursor);
+  cell_scan_kernel<<<1, SCAN_THREADS, 0, L.s>>>(ncell, count, start, cursor, gstart);
   LAUNCHED(L);
   cell_scatter_kernel<<<cdiv(ns, 256), 256, 0, L.s>>>(ns, key, cursor, slot_site);
   LAUNCHED(L);
   cell_order_kernel<<<cdiv(ncell, ORDER_THREADS / 32), ORDER_THREADS, 0, L.s>>>(
-      ncell, start, slot_site, order, key_s);
+      ncell, start, slot_site, pfix, order, key_s, pj, gstart, gcell);
   LAUNCHED(L);
   return cudaGetLastError();
 }
 
 __global__ void gather_mixed_kernel(int ns, const double* __restrict__ r,
                                     const int* __restrict__ order, const int* __restrict__ kind,
-                                    const int* __restrict__ mol, double Lx, double Ly, double Lz,
-                                    int4* __restrict__ pj) {
+                                    const int* __restrict__ mol, double iLx, double iLy,
+                                    double iLz, int4* __restrict__ pj) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ns) return;
   int i = order[t];
-  pj[t] = make_int4(fixed32(r[3 * i], Lx), fixed32(r[3 * i + 1], Ly), fixed32(r[3 * i + 2], Lz),
-                    (mol[i] << 8) | kind[i]);
+  pj[t] = make_int4(fixed32(r[3 * i], iLx), fixed32(r[3 * i + 1], iLy),
+                    fixed32(r[3 * i + 2], iLz), (mol[i] << 8) | kind[i]);
 }
 
 cudaError_t k_gather_mixed(const Launch& L, int ns, const double* r, const int* order,
-                           const int* kind, const int* mol, double Lx, double Ly, double Lz,
-                           int4* pj) {
-  gather_mixed_kernel<<<cdiv(ns, 256), 256, 0, L.s>>>(ns, r, order, kind, mol, Lx, Ly, Lz, pj);
+                           const int* kind, const int* mol, const double iL[3], int4* pj) {
+  gather_mixed_kernel<<<cdiv(ns, 256), 256, 0, L.s>>>(ns, r, order, kind, mol, iL[0], iL[1],
+                                                      iL[2], pj);
   LAUNCHED(L);
   return cudaGetLastError();
 }
@@ -457,6 +487,228 @@ __global__ void __launch_bounds__(NW * 32)
   }
 }
 
+// ------------------------------------------------- group pair kernel --
+//
+// The same pair terms as pair_mixed_kernel with the work cut by pruning.
+// One warp per group of up to GROUP_SITES = 8 sites of a home cell (the
+// group's sites are consecutive in the cell's site order); lane = (i = lane
+// & 7, s = lane >> 3).  The neighbour sites come from the stencil's z-runs
+// (cells consecutive along z are consecutive in the sorted array, so a run
+// is one or, across the periodic edge, two contiguous ranges) in batches of
+// 32: every neighbour is tested once against the cutoff sphere around the
+// group's bounding box, the kept ones are compacted into shared memory
+// (warp ballot, fixed order) and taken four at a time, one per s, each
+// against the lane's own site i.  The test keeps every pair within the
+// cutoff (the box distance is a lower bound of every pair distance, with the
+// same FP32 operations), so the pair set is the cell kernel's.  The pair
+// terms are predicated rather than branched (the lanes of a warp hold
+// different kinds of pairs, and a branch per kind would run every path one
+// after the other).  Forces: FP32 per z-run, folded into compensated sums;
+// at the end the four s-lanes of a site are summed in a fixed order.  No
+// atomics: results are reproducible.
+template <bool MEASURE, bool POLAR, int NW>
+__global__ void __launch_bounds__(NW * 32)
+    pair_group_mixed_kernel(PairArgs a, const int4* __restrict__ pj,
+                            const PairF* __restrict__ ptab_g, const float4* __restrict__ erd,
+                            const float4* __restrict__ eru, float sx, float sy, float sz, float cq,
+                            float sgrid) {
+  constexpr int NT = NW * 32;
+  extern __shared__ float4 dyn_smem[];   // the nk x nk FP32 pair table
+  __shared__ float4 sj[NW][32];
+  __shared__ float4 sjd[POLAR ? NW : 1][32];
+  __shared__ double ered[NT];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int il = lane & 7, sl = lane >> 3;
+  const int nk = a.nkind, ntab = a.ntab;
+  PairFS* ptab = reinterpret_cast<PairFS*>(dyn_smem);
+  for (int t = threadIdx.x; t < 3 * nk * nk; t += NT)
+    dyn_smem[t] = reinterpret_cast<const float4*>(ptab_g + t / 3)[t % 3];
+  __syncthreads();
+  const int ncell = a.ncx * a.ncy * a.ncz;
+  const int nitems = a.gstart[ncell];
+  CSum es[9];
+
+  for (int item = blockIdx.x * NW + warp; item < nitems; item += gridDim.x * NW) {
+    const int c = a.gcell[item];
+    const int cz = c % a.ncz, cy = (c / a.ncz) % a.ncy, cx = c / (a.ncy * a.ncz);
+    const int i0 = a.cell_start[c] + GROUP_SITES * (item - a.gstart[c]);
+    const int ni = min(GROUP_SITES, a.cell_start[c + 1] - i0);
+    const unsigned refx = (unsigned)((((unsigned long long)(2 * cx + 1)) << 31) / a.ncx),
+                   refy = (unsigned)((((unsigned long long)(2 * cy + 1)) << 31) / a.ncy),
+                   refz = (unsigned)((((unsigned long long)(2 * cz + 1)) << 31) / a.ncz);
+    const bool vi = il < ni;
+    const int ti = i0 + il;
+    const int4 me = vi ? pj[ti] : make_int4(0, 0, 0, 0);
+    const float4 md = (POLAR && vi) ? a.pdj[ti] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int kind_i = me.w & 255, mol_i = me.w >> 8;
+    const float xi = (float)(int)((unsigned)me.x - refx) * sx,
+                yi = (float)(int)((unsigned)me.y - refy) * sy,
+                zi = (float)(int)((unsigned)me.z - refz) * sz;
+    // bounding box of the group's sites (the same in all four s-copies)
+    float blx = vi ? xi : 3e38f, bly = vi ? yi : 3e38f, blz = vi ? zi : 3e38f;
+    float bhx = vi ? xi : -3e38f, bhy = vi ? yi : -3e38f, bhz = vi ? zi : -3e38f;
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+      blx = fminf(blx, __shfl_xor_sync(0xffffffffu, blx, o));
+      bly = fminf(bly, __shfl_xor_sync(0xffffffffu, bly, o));
+      blz = fminf(blz, __shfl_xor_sync(0xffffffffu, blz, o));
+      bhx = fmaxf(bhx, __shfl_xor_sync(0xffffffffu, bhx, o));
+      bhy = fmaxf(bhy, __shfl_xor_sync(0xffffffffu, bhy, o));
+      bhz = fmaxf(bhz, __shfl_xor_sync(0xffffffffu, bhz, o));
+    }
+    CSum fx, fy, fz, gx, gy, gz;
+    for (int sp = 0; sp < a.nspans; sp++) {
+      const int4 o = a.spans[sp];
+      int x2 = cx + o.x, y2 = cy + o.y;
+      x2 += (x2 < 0) ? a.ncx : (x2 >= a.ncx ? -a.ncx : 0);
+      y2 += (y2 < 0) ? a.ncy : (y2 >= a.ncy ? -a.ncy : 0);
+      const int col = (x2 * a.ncy + y2) * a.ncz;
+      int za = cz + o.z, zb = cz + o.w;
+      if (zb < 0) { za += a.ncz; zb += a.ncz; }
+      if (za >= a.ncz) { za -= a.ncz; zb -= a.ncz; }
+      // the z-run (at most ncz cells) as one or two contiguous ranges
+      int ra0, ra1, rb0 = 0, rb1 = -1;
+      if (za < 0) { ra0 = za + a.ncz; ra1 = a.ncz - 1; rb0 = 0; rb1 = zb; }
+      else if (zb >= a.ncz) { ra0 = za; ra1 = a.ncz - 1; rb0 = 0; rb1 = zb - a.ncz; }
+      else { ra0 = za; ra1 = zb; }
+      float ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;
+      float e_el = 0, e_lj = 0, e_vir = 0;
+      PvF pv;
+      pv.zero();
+      for (int part = 0; part < 2; part++) {
+        const int z0 = part ? rb0 : ra0, z1 = part ? rb1 : ra1;
+        if (z1 < z0) continue;
+        const int j0 = a.cell_start[col + z0], j1 = a.cell_start[col + z1 + 1];
+        for (int jb = j0; jb < j1; jb += 32) {
+          const int j = jb + lane;
+          bool keep = false;
+          float4 f4 = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (j < j1) {
+            const int4 q = pj[j];
+            f4 = make_float4((float)(int)((unsigned)q.x - refx) * sx,
+                             (float)(int)((unsigned)q.y - refy) * sy,
+                             (float)(int)((unsigned)q.z - refz) * sz, __int_as_float(q.w));
+            const float ddx = fmaxf(fmaxf(blx - f4.x, f4.x - bhx), 0.f),
+                        ddy = fmaxf(fmaxf(bly - f4.y, f4.y - bhy), 0.f),
+                        ddz = fmaxf(fmaxf(blz - f4.z, f4.z - bhz), 0.f);
+            keep = fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz)) < cq;
+          }
+          const unsigned M = __ballot_sync(0xffffffffu, keep);
+          if (keep) {
+            const int slot = __popc(M & ((1u << lane) - 1u));
+            sj[warp][slot] = f4;
+            if (POLAR) sjd[warp][slot] = a.pdj[j];
+          }
+          __syncwarp();
+          const int n = __popc(M);
+          for (int t = sl; t < n; t += 4) {
+            const float4 q = sj[warp][t];
+            const float dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
+            const float rr = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const int qw = __float_as_int(q.w);
+            const bool ok = vi && rr < cq && (qw >> 8) != mol_i;
+            const PairFS P = ptab[kind_i * nk + (qw & 255)];
+            const float x = __fdividef(P.Sq, rr), y = x * x * x, xt = rr - P.C2q;
+            const bool core = rr < P.C1q, tail = rr < P.C2q;
+            const float flj = core ? P.E24 * fmaf(2.f * y, y, -y) * x : (tail ? P.A4 * xt : 0.f);
+            float e_el_p = 0.f;
+            float f = flj + spline_any<MEASURE, true>(erd, eru, rr, sgrid, ntab, P.qq, e_el_p);
+            f = ok ? f : 0.f;
+            ax = fmaf(f, dx, ax);
+            ay = fmaf(f, dy, ay);
+            az = fmaf(f, dz, az);
+            if (MEASURE && ok) {
+              e_lj += core ? P.E4 * fmaf(y, y, -y) : (tail ? P.A * xt * xt : 0.f);
+              e_vir += rr * flj;
+              e_el += e_el_p;
+              pv.add(dx, dy, dz, f);
+            }
+            if (POLAR) {
+              // Drude(i) - centre(j), centre(i) - Drude(j), Drude(i) -
+              // Drude(j): zero charge products give zero terms
+              const float4 qd = sjd[warp][t];
+              float e_p = 0.f;
+              const float ex = dx + md.x, ey = dy + md.y, ez = dz + md.z;
+              float fp = spline_any<MEASURE, true>(
+                  erd, eru, fmaf(ex, ex, fmaf(ey, ey, ez * ez)), sgrid, ntab, P.qpc, e_p);
+              fp = ok ? fp : 0.f;
+              bx = fmaf(fp, ex, bx);
+              by = fmaf(fp, ey, by);
+              bz = fmaf(fp, ez, bz);
+              const float cx2 = dx - qd.x, cy2 = dy - qd.y, cz2 = dz - qd.z;
+              float fc = spline_any<MEASURE, true>(
+                  erd, eru, fmaf(cx2, cx2, fmaf(cy2, cy2, cz2 * cz2)), sgrid, ntab, P.qcp, e_p);
+              fc = ok ? fc : 0.f;
+              ax = fmaf(fc, cx2, ax);
+              ay = fmaf(fc, cy2, ay);
+              az = fmaf(fc, cz2, az);
+              const float px = ex - qd.x, py = ey - qd.y, pz = ez - qd.z;
+              float fd = spline_any<MEASURE, true>(
+                  erd, eru, fmaf(px, px, fmaf(py, py, pz * pz)), sgrid, ntab, P.qpp, e_p);
+              fd = ok ? fd : 0.f;
+              bx = fmaf(fd, px, bx);
+              by = fmaf(fd, py, by);
+              bz = fmaf(fd, pz, bz);
+              if (MEASURE && ok) {
+                pv.add(ex, ey, ez, fp);
+                pv.add(cx2, cy2, cz2, fc);
+                pv.add(px, py, pz, fd);
+                e_el += e_p;
+              }
+            }
+          }
+          __syncwarp();
+        }
+      }
+      // the z-run's FP32 sums into the compensated sums
+      fx.add(ax); fy.add(ay); fz.add(az);
+      if (POLAR) { gx.add(bx); gy.add(by); gz.add(bz); }
+      if (MEASURE) {
+        es[0].add(e_el); es[1].add(e_lj); es[2].add(e_vir);
+        es[3].add(pv.p0); es[4].add(pv.p1); es[5].add(pv.p2);
+        es[6].add(pv.p3); es[7].add(pv.p4); es[8].add(pv.p5);
+      }
+    }
+    // the four s-lanes of a site, summed in a fixed order (xor 8, then 16:
+    // every lane holds (s0 + s1) + (s2 + s3))
+    double g[6] = {fx.value(), fy.value(), fz.value(), 0, 0, 0};
+    if (POLAR) {
+      g[3] = gx.value();
+      g[4] = gy.value();
+      g[5] = gz.value();
+    }
+#pragma unroll
+    for (int k = 0; k < (POLAR ? 6 : 3); k++) {
+      g[k] += __shfl_xor_sync(0xffffffffu, g[k], 8);
+      g[k] += __shfl_xor_sync(0xffffffffu, g[k], 16);
+    }
+    if (sl == 0 && vi) {
+      const int site = a.order[ti];
+      a.f[3 * site] = g[0];
+      a.f[3 * site + 1] = g[1];
+      a.f[3 * site + 2] = g[2];
+      if (POLAR) {
+        a.f[3 * (long)a.ns + 3 * site] = g[3];
+        a.f[3 * (long)a.ns + 3 * site + 1] = g[4];
+        a.f[3 * (long)a.ns + 3 * site + 2] = g[5];
+      }
+    }
+  }
+  if (MEASURE) {
+    // each unordered pair was visited from both ends; one row per CTA
+    for (int k = 0; k < 9; k++) {
+      ered[threadIdx.x] = 0.5 * es[k].value();
+      __syncthreads();
+      for (int w = NT / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) ered[threadIdx.x] += ered[threadIdx.x + w];
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) a.epart[blockIdx.x * NEN + k] = ered[0];
+      __syncthreads();
+    }
+  }
+}
+
 cudaError_t k_pair_mixed(const Launch& L, const PairArgs& a, const int4* pj, const PairF* ptab,
                          const float4* erd, const float4* eru, bool measure, bool polar) {
   int ncell = a.ncx * a.ncy * a.ncz;
@@ -464,6 +716,25 @@ cudaError_t k_pair_mixed(const Launch& L, const PairArgs& a, const int4* pj, con
         sz = (float)(a.Lz / 4294967296.0);
   const float cq = (float)a.cutoff_sq, sg = (float)a.sgrid, al = (float)a.alpha;
   const bool rel = !a.allpairs;
+  if (a.group && rel) {
+    const size_t gsm = sizeof(PairFS) * (size_t)a.nkind * a.nkind;
+    cudaError_t ge = cudaSuccess;
+#define PAIR_GROUP(M, P)                                                                        \
+  do {                                                                                          \
+    if (gsm > 48 * 1024)                                                                        \
+      ge = cudaFuncSetAttribute(pair_group_mixed_kernel<M, P, GROUP_WARPS>,                    \
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm);         \
+    if (ge == cudaSuccess)                                                                      \
+      pair_group_mixed_kernel<M, P, GROUP_WARPS><<<a.ngrid, GROUP_WARPS * 32, gsm, L.s>>>(     \
+          a, pj, ptab, erd, eru, sx, sy, sz, cq, sg);                                           \
+  } while (0)
+    if (polar) { if (measure) PAIR_GROUP(true, true); else PAIR_GROUP(false, true); }
+    else { if (measure) PAIR_GROUP(true, false); else PAIR_GROUP(false, false); }
+#undef PAIR_GROUP
+    if (ge != cudaSuccess) return ge;
+    LAUNCHED(L);
+    return cudaGetLastError();
+  }
   // the measuring kernel (energies, virial) always runs with 4 warps and the
   // spline through L1: with more registers per thread it keeps more CTAs
   // resident that way (1.0 ms on 32768 waters; 16 warps + shared-memory
@@ -817,8 +1088,8 @@ __global__ void charge_fixed_kernel(KArgs a, const double* __restrict__ r, uint4
     y += r[3 * (long)a.ns + 3 * site + 1];
     z += r[3 * (long)a.ns + 3 * site + 2];
   }
-  qf[j] = make_uint4((unsigned)fixed32(x, a.Lx), (unsigned)fixed32(y, a.Ly),
-                     (unsigned)fixed32(z, a.Lz), 0u);
+  qf[j] = make_uint4((unsigned)fixed32(x, a.iLx), (unsigned)fixed32(y, a.iLy),
+                     (unsigned)fixed32(z, a.iLz), 0u);
 }
 
 __global__ void phase_tables_mixed_kernel(KArgs a, const uint4* __restrict__ qf,

@@ -130,8 +130,8 @@ __global__ void __launch_bounds__(256) kf_tc_phase_kernel(KArgs a, const double*
         y += r[3 * (long)a.ns + 3 * site + 1];
         z += r[3 * (long)a.ns + 3 * site + 2];
       }
-      f = make_uint4((unsigned)fixed32(x, a.Lx), (unsigned)fixed32(y, a.Ly),
-                     (unsigned)fixed32(z, a.Lz), 0u);
+      f = make_uint4((unsigned)fixed32(x, a.iLx), (unsigned)fixed32(y, a.iLy),
+                     (unsigned)fixed32(z, a.iLz), 0u);
       q = (float)a.qval[j];
     }
     sfix[tid] = f;

@@ -273,9 +273,7 @@ extern "C" int mg_ewald_kspace_noalloc(const double* r_dev, const double* q_dev,
   ka.Ky = Ky;
   ka.Kz = Kz;
   ka.row = rowlen;
-  ka.Lx = L[0];
-  ka.Ly = L[1];
-  ka.Lz = L[2];
+  set_box(ka, L);
   ka.alpha = alpha;
   ka.qsite = qsite;
   ka.qval = q_dev;

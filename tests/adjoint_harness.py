@@ -63,12 +63,24 @@ def observables(orc_factory, system, r, target=None):
 
 # ------------------------------------------------- torch.autograd wrapper --
 
+def charge_groups_grad(dq, system, q_groups):
+    """the gradient of charge parameters from per-site dX/dq_i: parameter k
+    sets q = w * theta_k on the sites of every (type, w) of q_groups[k], so
+    dX/dtheta_k = sum over those (type, w) of w * sum of dX/dq_i"""
+    return np.array([sum(w * dq[system.type == t].sum() for t, w in grp) for grp in q_groups])
+
+
 def make_force_match(M, frames, targets, system, ew, lj_types, q_types):
     """A torch.autograd.Function of theta = (eps_t, sigma_t for t in lj_types,
-    q_t for t in q_types) -> force-matching loss mean |F(theta) - target|^2
-    over the frames, with the gradient from the GPU adjoint (mg_adjoint).
-    Charges of q_types are shared by all sites of the type."""
+    then one charge parameter per entry of q_types) -> force-matching loss
+    mean |F(theta) - target|^2 over the frames, with the gradient from the GPU
+    adjoint (mg_adjoint).  An entry of q_types is a type (every site of it
+    takes the parameter as its charge) or a list of (type, weight): the sites
+    of each type take weight * parameter, which keeps a neutral molecule or
+    an ion pair neutral (e.g. [(H, 1), (O, -2)])."""
     import torch
+
+    groups = [[(t, 1.0)] if np.isscalar(t) else list(t) for t in q_types]
 
     def unpack(theta):
         th = theta.detach().cpu().numpy().astype(np.float64)
@@ -77,8 +89,9 @@ def make_force_match(M, frames, targets, system, ew, lj_types, q_types):
         n = len(lj_types)
         for k, t in enumerate(lj_types):
             eps[t], sig[t] = th[k], th[n + k]
-        for k, t in enumerate(q_types):
-            q[system.type == t] = th[2 * n + k]
+        for k, grp in enumerate(groups):
+            for t, w in grp:
+                q[system.type == t] = w * th[2 * n + k]
         return with_params(system, eps=eps, sig=sig, q=q)
 
     class ForceMatch(torch.autograd.Function):
@@ -98,8 +111,8 @@ def make_force_match(M, frames, targets, system, ew, lj_types, q_types):
                 for k, t in enumerate(lj_types):
                     grad[k] += de[t]
                     grad[n + k] += ds[t]
-                for k, t in enumerate(q_types):
-                    grad[2 * n + k] += adj["dLq"][s.type == t].sum()
+                if groups:
+                    grad[2 * n:] += charge_groups_grad(adj["dLq"], s, groups)
             fp.close()
             ctx.save_for_backward(torch.tensor(grad, dtype=theta.dtype))
             return theta.new_tensor(loss)

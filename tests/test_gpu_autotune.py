@@ -18,10 +18,16 @@ def test_autotune_choice_and_forces(precision):
     assert best["kspace_ctas_per_sm"] in (6, 10, 16)
     ms = best["ms"]
     assert (ms[ms > 0] > 0).any()
-    assert ms[best["cells_per_cutoff"] - 1, [6, 10, 16].index(best["kspace_ctas_per_sm"])] == \
-        ms[ms > 0].min()
+    if best["pair_variant"] != 8:
+        # the cell kernel's grid: the fastest of the grid x split trials
+        assert ms[best["cells_per_cutoff"] - 1,
+                  [6, 10, 16].index(best["kspace_ctas_per_sm"])] == ms[ms > 0].min()
+    else:
+        # the group kernel: its fastest subdivision
+        mg = best["ms_group"]
+        assert mg[best["cells_per_cutoff"] - 1] == mg[mg > 0].min()
     f0, _ = M.ForcePath(*args, precision=precision).forces(g["r"][0])
-    assert best["pair_variant"] in range(8)
+    assert best["pair_variant"] in range(9)
     f1, _ = M.ForcePath(*args, precision=precision, cells_per_cutoff=best["cells_per_cutoff"],
                         kspace_ctas_per_sm=best["kspace_ctas_per_sm"],
                         pair_variant=best["pair_variant"]).forces(g["r"][0])

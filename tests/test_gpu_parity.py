@@ -105,6 +105,52 @@ def test_cell_list_is_deterministic(precision):
         assert e["el"] == e0["el"] and e["lj"] == e0["lj"]
 
 
+@pytest.mark.parametrize("case", ["spce864", "brine532"])
+def test_group_pair_kernel_matches_oracle(case):
+    """the group pair kernel (pair_variant 8: warps over groups of 8 home
+    sites, neighbours pruned against the group's bounding box) gives the
+    oracle's forces and energies as the cell kernel does"""
+    g, meta, system, ew, fc = make(case, "mixed")
+    _, _, _, _, fg = make(case, "mixed", pair_variant=8)
+    orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
+    for d in (0, g["r"].shape[0] - 1):
+        f, en = fg.forces(g["r"][d], measure=True)
+        f0, e0 = fc.forces(g["r"][d], measure=True)
+        fo, eo = orc.forces(g["r"][d], nthreads=4)
+        assert rel_rms(f, fo) < MIXED_TOL
+        assert rel_rms(f, f0) < 2e-6
+        for k in ("el", "er", "ek"):
+            assert abs(en[k] - eo[k]) <= 2e-6 * abs(eo["eself"]), k
+        assert abs(en["lj"] - eo["lj"]) <= 1e-5 * abs(eo["lj"])
+        for m in range(6):
+            assert abs(en["Pvir"][m] - eo["Pvir"][m]) <= 2e-5 * abs(eo["Pvir"][0]), m
+        # bit-reproducible like the cell kernel
+        f2, _ = fg.forces(g["r"][d], measure=True)
+        assert np.array_equal(f2, f)
+
+
+@pytest.mark.parametrize("cells", [2, 3])
+@pytest.mark.parametrize("polar", [False, True])
+def test_group_pair_kernel_full_size(cells, polar):
+    """32768 waters (SPC/E, or with Drude shells displaced at random): the
+    group kernel equals the cell kernel within the mixed rounding, for cells
+    of a half and of a third of the cutoff"""
+    from macsimus_gb300 import configs
+    w = configs.workload("drude32768" if polar else "spce32768", seed=3)
+    r = w["r"].copy()
+    if polar:
+        rng = np.random.default_rng(4)
+        r[w["system"].ns:] = rng.normal(0, 0.05, (w["system"].ns, 3)) * \
+            (w["system"].qpol != 0)[:, None]
+    args = (w["system"], [w["L"]] * 3, w["cutoff"], w["alpha"], w["kappa"])
+    f0, e0 = M.ForcePath(*args, precision="mixed", cells_per_cutoff=cells).forces(r, measure=True)
+    f1, e1 = M.ForcePath(*args, precision="mixed", cells_per_cutoff=cells,
+                         pair_variant=8).forces(r, measure=True)
+    assert rel_rms(f1, f0) < 2e-6
+    assert abs(e1["er"] - e0["er"]) < 2e-6 * abs(e0["eself"])
+    assert abs(e1["lj"] - e0["lj"]) < 1e-5 * abs(e0["lj"])
+
+
 def test_ewald_kspace_part():
     g, meta, system, ew, fp = make("spce216", "fp64")
     fk, e = fp.ewald(g["r"][0])
