@@ -168,7 +168,7 @@ def run_ours(args, rank, world, local):
                           precision="mixed", **kw)
         tuned = dict(cells_per_cutoff=best["cells_per_cutoff"],
                      kspace_ctas_per_sm=best["kspace_ctas_per_sm"],
-                     pair_variant=best["pair_variant"])
+                     pair_variant=best["pair_variant"], kspace_serial=best["kspace_serial"])
     if args.pair_variant is not None:
         tuned["pair_variant"] = args.pair_variant
     if args.cells is not None:
@@ -231,7 +231,7 @@ def run_ours(args, rank, world, local):
     # k-space and r-space chains serialised, so that no kernel shares the GPU
     fp.set_overlap(False)
     _, _, prof = timed_steps(fp, min(args.steps, 20), 2, profile=True)
-    fp.set_overlap(True)
+    fp.set_overlap(not tuned.get("kspace_serial", 0))
     t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -348,8 +348,9 @@ def run_ours(args, rank, world, local):
                          "avg_launch_ms": round(kavg, 5)},
             "kernel_share": shares,
             "kernel_share_note": "per-kernel CUDA-event times of a separate pass with the k-space "
-                                 "and r-space chains serialised; the timed steps run them "
-                                 "concurrently on two streams",
+                                 "and r-space chains serialised; the timed steps run them %s" % (
+                                     "one after the other (autotuned)" if tuned.get("kspace_serial")
+                                     else "concurrently on two streams"),
             "clocks": clk,
             "cpu_baseline": cpu,
         }

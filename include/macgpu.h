@@ -166,6 +166,10 @@ typedef struct {
      (sim/norm.c:677-705, sim/main.c:1626); cook's default removes it once
      per cycle, which a host loop does with mg_remove_drift */
   int drift_step;
+  /* FP32 path: 0 runs the Ewald k-space chain on a second stream beside the
+     r-space chain, 1 after it on one stream (mg_set_overlap changes it
+     later); mg_autotune picks it.  No reference counterpart. */
+  int kspace_serial;
 } mg_params;
 
 /* Energies of one force evaluation (program units, K).
@@ -281,6 +285,10 @@ int mg_nose_state(mg_ctx *ctx, double state[3]);
    r-space chain (on by default; off serialises them, e.g. to time kernels
    one by one).  No reference counterpart. */
 int mg_set_overlap(mg_ctx *ctx, int on);
+/* mg_md_steps of a non-polar box with cells re-binned: replay one captured
+   CUDA graph per step (on, the default) or launch the kernels one by one.
+   No reference counterpart. */
+int mg_set_graph(mg_ctx *ctx, int on);
 int mg_set_stream(mg_ctx *ctx, void *stream);
 
 /* Per-kernel timing with CUDA events recorded on the context stream around
@@ -372,9 +380,11 @@ int mg_xwidom(mg_ctx *ctx, int nlist, const int *mols, const int *vtype, const d
    split (kspace_ctas_per_sm 6, 10, 16) and writes the fastest pair into
    *par, then the fastest of the 8 cell-kernel pair_variant values at that
    choice and of the group kernel (pair_variant 8) at every subdivision.
-   Builds and frees its own trial contexts; ms[20] (optional) gets the time
-   per evaluation of each trial (cdiv-major, then the 8 cell-kernel variants,
-   then the group kernel at cdiv 1..3; -1 if that grid is not possible). */
+   Last, for the FP32 path, kspace_serial 0 or 1 at that choice.  Builds
+   and frees its own trial contexts; ms[22] (optional) gets the time per
+   evaluation of each trial (cdiv-major, then the 8 cell-kernel variants,
+   the group kernel at cdiv 1..3, kspace_serial 0 and 1; -1 if that grid is
+   not possible or the trial did not run). */
 int mg_autotune(const mg_topology *top, mg_params *par, const double *r, int nrep, double *ms);
 
 /* ---- adjoint ----
@@ -415,8 +425,16 @@ int mg_batch_size(const mg_batch *b);
 mg_ctx *mg_batch_box(mg_batch *b, int i);
 /* kernels launched by the last batch call (graph nodes counted per step) */
 int mg_batch_last_launches(const mg_batch *b);
-/* en: NULL or [nbox] energies of the last step */
+/* en: NULL or [nbox] energies of the last step.  When every box runs the
+   FP32 path with the Ewald passes on the FP32 cores (kspace_engine 1), the
+   cell pair kernel with 4 warps (pair_variant 0), cells re-binned every step
+   and no Drude charges, dependants, thermostat, drmax, drift removal or
+   dipole term, a step is one launch per kernel over all boxes (blockIdx.y =
+   box, each box with its single-launch arguments, so its results are those
+   of the box run alone); otherwise one graph node per box kernel. */
 int mg_batch_md_steps(mg_batch *b, int nsteps, mg_energy *en);
+/* 1 once mg_batch_md_steps has chosen the one-launch-per-kernel form */
+int mg_batch_fused(const mg_batch *b);
 /* probes: one ghost for all boxes (probe_per_box = 0) or [nbox];
    out: [nbox] */
 int mg_batch_widom(mg_batch *b, const mg_probe *probes, int probe_per_box, long long ninsert,

@@ -58,7 +58,8 @@ class Params(C.Structure):
                 ("thermo_f", C.c_double), ("seed", C.c_ulonglong), ("box_rmin", C.c_double),
                 ("no_normalize", C.c_int), ("kspace_engine", C.c_int),
                 ("nose_pred", C.c_int), ("dipole_corr", C.c_int), ("drmax", C.c_double),
-                ("drift_step", C.c_int)]
+                ("drift_step", C.c_int),
+                ("kspace_serial", C.c_int)]
 
 
 class Energy(C.Structure):
@@ -129,6 +130,8 @@ def library():
         L.mg_thermostat_factor.argtypes = [vp]
         L.mg_thermostat_factor.restype = C.c_double
         L.mg_nose_state.argtypes = [vp, _dp]
+        L.mg_set_graph.argtypes = [vp, C.c_int]
+        L.mg_batch_fused.argtypes = [vp]
         L.mg_bounddr_report.argtypes = [vp, C.POINTER(C.c_longlong), _dp]
         L.mg_remove_drift.argtypes = [vp, _dp]
         L.mg_profile_enable.argtypes = [vp, C.c_int]
@@ -163,15 +166,16 @@ def autotune(system, L, cutoff, alpha, kappa, r, nrep=3, **kw):
     this box and configuration (mg_autotune), with the timings (3x3 grid x
     split, the 8 cell-kernel pair variants, the group kernel at cdiv 1..3)"""
     t, p, keep = describe(system, L, cutoff, alpha, kappa, **kw)
-    ms = np.zeros(20)
+    ms = np.full(22, -1.0)
     rr = _arr(r, np.float64).reshape(-1)
     rc = library().mg_autotune(C.byref(t), C.byref(p), rr.ctypes.data_as(_dp), int(nrep),
                                ms.ctypes.data_as(_dp))
     if rc:
         raise MGError(rc, "mg_autotune failed")
     return dict(cells_per_cutoff=p.cells_per_cutoff, kspace_ctas_per_sm=p.kspace_ctas_per_sm,
-                pair_variant=p.pair_variant, ms=ms[:9].reshape(3, 3), ms_pair=ms[9:17],
-                ms_group=ms[17:])
+                pair_variant=p.pair_variant, kspace_serial=p.kspace_serial,
+                ms=ms[:9].reshape(3, 3), ms_pair=ms[9:17], ms_group=ms[17:20],
+                ms_serial=ms[20:22])
 
 
 def fp32_peak_tflops():
@@ -192,7 +196,7 @@ def describe(system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None, 
              cells_per_cutoff=0, aspc_k=2, scf_iter=1, scf_omega=0.6, minqq=1.0, skin=0.0,
              nl_every=50, kspace_ctas_per_sm=0, pair_variant=0, thermostat=0, T=298.0,
              tau_T=0.1, thermo_f=0.0, seed=0, box_rmin=0.0, normalize=True, kspace_engine=0,
-             nose_pred=2, dipole_corr=0, drmax=0.0, drift_step=False):
+             nose_pred=2, dipole_corr=0, drmax=0.0, drift_step=False, kspace_serial=0):
     """(mg_topology, mg_params, arrays to keep alive) of one box"""
     keep = []
 
@@ -275,6 +279,7 @@ def describe(system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None, 
     p.dipole_corr = int(dipole_corr)
     p.drmax = float(drmax)
     p.drift_step = 1 if drift_step else 0
+    p.kspace_serial = int(kspace_serial)
     return t, p, keep
 
 
@@ -287,7 +292,7 @@ class ForcePath:
                  minqq=1.0, skin=0.0, nl_every=50, kspace_ctas_per_sm=0, pair_variant=0,
                  thermostat=0, T=298.0, tau_T=0.1, thermo_f=0.0, seed=0, box_rmin=0.0,
                  normalize=True, kspace_engine=0, nose_pred=2, dipole_corr=0, drmax=0.0,
-                 drift_step=False):
+                 drift_step=False, kspace_serial=0):
         lib = library()
         self.system = system
         self.ns = system.ns
@@ -303,7 +308,7 @@ class ForcePath:
                                     box_rmin=box_rmin, normalize=normalize,
                                     kspace_engine=kspace_engine, nose_pred=nose_pred,
                                     dipole_corr=dipole_corr, drmax=drmax,
-                                    drift_step=drift_step)
+                                    drift_step=drift_step, kspace_serial=kspace_serial)
         self.polar = getattr(system, "polar", False)
         Lb = np.broadcast_to(np.asarray(L, dtype=np.float64), (3,))
         st = C.c_int(0)
@@ -496,6 +501,10 @@ class ForcePath:
         """FP32 path: k-space chain concurrent with the r-space chain (default on)"""
         self._check(library().mg_set_overlap(self._ctx, 1 if on else 0))
 
+    def set_graph(self, on):
+        """MD steps as one replayed CUDA graph each (default) or kernel by kernel"""
+        self._check(library().mg_set_graph(self._ctx, 1 if on else 0))
+
     def set_stream(self, stream_handle):
         """run on a caller's CUDA stream (e.g. torch.cuda.current_stream().cuda_stream)"""
         self._check(library().mg_set_stream(self._ctx, C.c_void_p(stream_handle or None)))
@@ -602,6 +611,11 @@ class Batch:
     @property
     def launches(self):
         return library().mg_batch_last_launches(self._b)
+
+    @property
+    def fused(self):
+        """True once MD steps run as one launch per kernel over all boxes"""
+        return bool(library().mg_batch_fused(self._b))
 
     def md_steps(self, n, measure=True):
         en = (Energy * self.nbox)()

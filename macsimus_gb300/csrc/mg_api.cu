@@ -191,6 +191,7 @@ struct mg_ctx {
   // one MD step (force-only / measured) captured as a CUDA graph
   cudaGraphExec_t g_step = nullptr, g_meas = nullptr;
   int graph_launches = 0, graph_launches_meas = 0;
+  bool use_graph = true;
   struct Rec { int id; cudaEvent_t a, b; };
   std::vector<std::string> pnames;
   std::vector<double> pms;
@@ -344,6 +345,7 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   ctx->skin = p->skin > 0 ? p->skin : 0;
   ctx->drmax = std::fabs(p->drmax);
   ctx->drift_step = p->drift_step != 0;
+  ctx->overlap = p->kspace_serial == 0;
   ctx->normalize = p->no_normalize ? 0 : 1;
   ctx->box_r0 = p->box_rmin > 0 ? p->box_rmin : (p->box_rmin < 0 ? 0.0 : 0.15);
   ctx->nl_every = p->nl_every > 0 ? p->nl_every : 50;
@@ -966,26 +968,11 @@ ExclArgs excl_args(mg_ctx* ctx, const double* r_dev, double* f) {
   return a;
 }
 
-int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) {
-  Launch L = launch(ctx);
-  const int ns = ctx->ns;
-  ctx->last_r = r_dev;
-  // fork point of the concurrent k-space chain (FP32 path): everything
-  // queued before, nothing of this evaluation's r-space work
-  if (ctx->precision == MG_MIXED && ctx->overlap && ctx->nq > 0)
-    CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
-  const bool rebuild = !ctx->use_list || ctx->need_build || ctx->since_build >= ctx->nl_every;
-  const double iL[3] = {1.0 / ctx->L[0], 1.0 / ctx->L[1], 1.0 / ctx->L[2]};
-  if (rebuild) {
-    // linked cells, with the fixed-point records of the sorted sites (d_pj,
-    // when the context has them) and the work items of the group kernel
-    PROF("cell_list", k_cell_list(L, ns, r_dev, ctx->d_status, iL, ctx->ncx, ctx->ncy, ctx->ncz,
-                                  ctx->d_kind, ctx->d_mol, ctx->d_pfix, ctx->d_key, ctx->d_ccount,
-                                  ctx->d_ccursor, ctx->d_idx, ctx->d_order, ctx->d_key_s,
-                                  ctx->d_cell_start, ctx->d_gstart, ctx->d_pj, ctx->d_gcell));
-  }
+// the arguments of the pair kernels and of the Ewald passes of a force
+// evaluation into f_dev
+PairArgs make_pair_args(mg_ctx* ctx, double* f_dev) {
   PairArgs pa{};
-  pa.ns = ns;
+  pa.ns = ctx->ns;
   pa.ncx = ctx->ncx;
   pa.ncy = ctx->ncy;
   pa.ncz = ctx->ncz;
@@ -1014,7 +1001,11 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
   pa.spans = ctx->d_spans;
   pa.nspans = ctx->nspans;
   pa.ngrid = ctx->ngroup_grid;
-  KArgs ka;
+  return pa;
+}
+
+KArgs make_kargs(mg_ctx* ctx, double* f_dev) {
+  KArgs ka{};
   ka.nq = ctx->nq;
   ka.nk = ctx->nk;
   ka.ntask = ctx->ntask;
@@ -1045,6 +1036,29 @@ int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) 
   ka.qdrude = ctx->d_qdrude;
   ka.ns = ctx->ns;
   ka.status = ctx->d_status;
+  return ka;
+}
+
+int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) {
+  Launch L = launch(ctx);
+  const int ns = ctx->ns;
+  ctx->last_r = r_dev;
+  // fork point of the concurrent k-space chain (FP32 path): everything
+  // queued before, nothing of this evaluation's r-space work
+  if (ctx->precision == MG_MIXED && ctx->overlap && ctx->nq > 0)
+    CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
+  const bool rebuild = !ctx->use_list || ctx->need_build || ctx->since_build >= ctx->nl_every;
+  const double iL[3] = {1.0 / ctx->L[0], 1.0 / ctx->L[1], 1.0 / ctx->L[2]};
+  if (rebuild) {
+    // linked cells, with the fixed-point records of the sorted sites (d_pj,
+    // when the context has them) and the work items of the group kernel
+    PROF("cell_list", k_cell_list(L, ns, r_dev, ctx->d_status, iL, ctx->ncx, ctx->ncy, ctx->ncz,
+                                  ctx->d_kind, ctx->d_mol, ctx->d_pfix, ctx->d_key, ctx->d_ccount,
+                                  ctx->d_ccursor, ctx->d_idx, ctx->d_order, ctx->d_key_s,
+                                  ctx->d_cell_start, ctx->d_gstart, ctx->d_pj, ctx->d_gcell));
+  }
+  PairArgs pa = make_pair_args(ctx, f_dev);
+  KArgs ka = make_kargs(ctx, f_dev);
   ListArgs la = list_args(ctx);
   int nerows = ctx->nprows;
   if (ctx->precision == MG_MIXED) {
@@ -1430,7 +1444,7 @@ void drop_graphs(mg_ctx* ctx) {
 // steps that md_step_enqueue covers (no Drude SCF, cells re-binned every
 // step) and that nothing times kernel by kernel run as a captured graph
 bool graph_step_ok(const mg_ctx* ctx) {
-  return !ctx->polar && !ctx->use_list && !ctx->prof_on;
+  return ctx->use_graph && !ctx->polar && !ctx->use_list && !ctx->prof_on;
 }
 
 // capture one step on the context's own stream (a caller's stream may be
@@ -2261,6 +2275,12 @@ int mg_set_overlap(mg_ctx* ctx, int on) {
   return MG_OK;
 }
 
+int mg_set_graph(mg_ctx* ctx, int on) {
+  if (!ctx) return MG_ERR_ARG;
+  ctx->use_graph = on != 0;
+  return MG_OK;
+}
+
 int mg_set_stream(mg_ctx* ctx, void* stream) {
   if (!ctx) return MG_ERR_ARG;
   CK(cudaStreamSynchronize(ctx->stream));
@@ -2341,6 +2361,14 @@ struct mg_batch {
   int launches_step = 0, launches = 0;
   WidomBox* d_wbox = nullptr;
   int wcap = 0;
+  // one launch per kernel over all boxes, when every box qualifies
+  // (fused_ok): the boxes' kernel arguments on the device, the largest
+  // grids, one captured graph per kind of step
+  int fused_ok = -1;
+  BoxStep* d_steps = nullptr;
+  BatchGrid grid{};
+  cudaGraphExec_t gf_step = nullptr, gf_meas = nullptr;
+  int launches_fused = 0;
 };
 
 namespace {
@@ -2445,6 +2473,9 @@ int mg_batch_destroy(mg_batch* b) {
   }
   if (b->g_step) cudaGraphExecDestroy(b->g_step);
   if (b->g_meas) cudaGraphExecDestroy(b->g_meas);
+  if (b->gf_step) cudaGraphExecDestroy(b->gf_step);
+  if (b->gf_meas) cudaGraphExecDestroy(b->gf_meas);
+  if (b->d_steps) cudaFree(b->d_steps);
   if (b->d_wbox) cudaFree(b->d_wbox);
   for (cudaEvent_t e : b->ev_join)
     if (e) cudaEventDestroy(e);
@@ -2463,6 +2494,150 @@ mg_ctx* mg_batch_box(mg_batch* b, int i) {
 }
 int mg_batch_last_launches(const mg_batch* b) { return b ? b->launches : 0; }
 
+namespace {
+
+// a box the batched kernels take: the FP32 path without Drude charges,
+// dependants, thermostat, step limiter or drift removal, cells re-binned
+// at every step on a grid of at least 3 cells per edge, the cell pair kernel
+// with 4 warps, Ewald passes on the FP32 cores, no dipole term
+bool fusable(const mg_ctx* c) {
+  return c->precision == MG_MIXED && !c->polar && !c->use_list && !c->allpairs &&
+         c->pair_variant == 0 && !c->kspace_tc && !c->sk_tc && c->thermostat == 0 &&
+         c->ndep == 0 && !c->dipole && c->drmax == 0 && !c->drift_step && c->nq > 0 &&
+         !c->prof_on;
+}
+
+// the boxes' arguments for the batched kernels, exactly those of their
+// single launches in forces_async / md_step_enqueue
+int build_fused(mg_batch* b) {
+  const int nbox = (int)b->box.size();
+  std::vector<BoxStep> h(nbox);
+  BatchGrid& g = b->grid;
+  g = BatchGrid{};
+  for (int i = 0; i < nbox; i++) {
+    mg_ctx* c = b->box[i];
+    BoxStep& e = h[i];
+    std::memset(&e, 0, sizeof(e));
+    e.ns = c->ns;
+    e.ncx = c->ncx;
+    e.ncy = c->ncy;
+    e.ncz = c->ncz;
+    for (int d = 0; d < 3; d++) e.iL[d] = 1.0 / c->L[d];
+    e.r = c->d_r;
+    e.status = c->d_status;
+    e.kind = c->d_kind;
+    e.mol = c->d_mol;
+    e.pfix = c->d_pfix;
+    e.key = c->d_key;
+    e.count = c->d_ccount;
+    e.cursor = c->d_ccursor;
+    e.slot_site = c->d_idx;
+    e.order = c->d_order;
+    e.key_s = c->d_key_s;
+    e.start = c->d_cell_start;
+    e.gstart = c->d_gstart;
+    e.pj = c->d_pj;
+    e.gcell = c->d_gcell;
+    e.pa = make_pair_args(c, c->d_f);
+    e.ptab = c->d_ptabf;
+    e.erd = c->d_erd;
+    e.eru = c->d_eru;
+    e.sx = (float)(c->L[0] / 4294967296.0);
+    e.sy = (float)(c->L[1] / 4294967296.0);
+    e.sz = (float)(c->L[2] / 4294967296.0);
+    e.cq = (float)(c->cutoff * c->cutoff);
+    e.sg = (float)c->sgrid;
+    e.al = (float)c->alpha;
+    e.xa = excl_args(c, c->d_r, c->d_f);
+    e.ka = make_kargs(c, c->d_f);
+    e.tab = (float2*)c->d_tab;
+    e.qf = c->d_qfix;
+    e.part = (float2*)c->d_part;
+    e.sa = shake_args(c, true);
+    const int nkin = (c->nmol + 127) / 128;
+    e.rpart[0] = c->d_epart;
+    e.rrows[0] = c->nprows + c->nxblocks;
+    e.rwidth[0] = 10;
+    e.rout[0] = c->d_sums;
+    e.rpart[1] = c->d_ekpart;
+    e.rrows[1] = c->nkblocks;
+    e.rwidth[1] = 7;
+    e.rout[1] = c->d_sums + 10;
+    e.rpart[2] = c->d_kinpart;
+    e.rrows[2] = nkin;
+    e.rwidth[2] = 1;
+    e.rout[2] = c->d_sums + 17;
+    e.rpart[3] = c->d_meas;
+    e.rrows[3] = nkin;
+    e.rwidth[3] = 13;
+    e.rout[3] = c->d_sums + 32;
+    e.g_site = cell_site_blocks(c->ns);
+    e.g_order = cell_order_blocks(c->ncell);
+    e.g_pair = c->ncell;
+    e.g_excl = c->nmol > 0 ? (c->nmol + EXCL_THREADS - 1) / EXCL_THREADS : 0;
+    e.g_charge = (c->nq + 255) / 256;
+    e.g_phase = (int)(((long)c->nq * c->row + 255) / 256);
+    e.g_p1x = c->np1job;
+    e.g_p1y = c->nchunk;
+    e.g_skr = (c->nk + 255) / 256;
+    e.g_kf = kf_mixed_blocks(c->nq);
+    e.g_shake = (c->nmol + 127) / 128;
+    g.site = std::max(g.site, e.g_site);
+    g.order = std::max(g.order, e.g_order);
+    g.pair = std::max(g.pair, e.g_pair);
+    g.excl = std::max(g.excl, e.g_excl);
+    g.charge = std::max(g.charge, e.g_charge);
+    g.phase = std::max(g.phase, e.g_phase);
+    g.p1x = std::max(g.p1x, e.g_p1x);
+    g.p1y = std::max(g.p1y, e.g_p1y);
+    g.skr = std::max(g.skr, e.g_skr);
+    g.kf = std::max(g.kf, e.g_kf);
+    g.shake = std::max(g.shake, e.g_shake);
+    g.pair_smem = std::max(g.pair_smem, sizeof(PairFS) * (size_t)c->nkind * c->nkind);
+    g.kf_smem = std::max(g.kf_smem, kf_mixed_smem(e.ka));
+  }
+  if (cudaMalloc(&b->d_steps, sizeof(BoxStep) * (size_t)nbox) != cudaSuccess ||
+      cudaMemcpy(b->d_steps, h.data(), sizeof(BoxStep) * (size_t)nbox, cudaMemcpyHostToDevice) !=
+          cudaSuccess)
+    return bfail(b, MG_ERR_CUDA, "batch: uploading the boxes' kernel arguments");
+  return MG_OK;
+}
+
+// one MD step of every box with the batched kernels, on the batch stream
+int fused_step_enqueue(mg_batch* b, bool measure) {
+  const int nbox = (int)b->box.size();
+  Launch L{b->main, &b->launches_fused};
+  BCK(k_batch_rspace(L, b->d_steps, nbox, b->grid, measure));
+  BCK(k_batch_pass1(L, b->d_steps, nbox, b->grid));
+  BCK(k_batch_sk_reduce(L, b->d_steps, nbox, b->grid, measure));
+  BCK(k_batch_pass2(L, b->d_steps, nbox, b->grid));
+  BCK(k_batch_step(L, b->d_steps, nbox, b->grid, measure));
+  return MG_OK;
+}
+
+int capture_fused(mg_batch* b, bool measure, cudaGraphExec_t* out) {
+  BCK(cudaStreamBeginCapture(b->main, cudaStreamCaptureModeRelaxed));
+  b->launches_fused = 0;
+  int rc = fused_step_enqueue(b, measure);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(b->main, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return bfail(b, MG_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess)
+    return bfail(b, MG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  b->launches_step = b->launches_fused;
+  return MG_OK;
+}
+
+}  // namespace
+
+int mg_batch_fused(const mg_batch* b) { return b && b->fused_ok == 1 ? 1 : 0; }
+
 int mg_batch_md_steps(mg_batch* b, int nsteps, mg_energy* en) {
   if (!b || nsteps < 0) return bfail(b, MG_ERR_ARG, "bad arguments");
   for (size_t i = 0; i < b->box.size(); i++) {
@@ -2475,9 +2650,28 @@ int mg_batch_md_steps(mg_batch* b, int nsteps, mg_energy* en) {
   }
   // the lanes must have finished what the per-box calls queued on them
   for (cudaStream_t s : b->lanes) BCK(cudaStreamSynchronize(s));
+  if (b->fused_ok < 0) {
+    bool ok = true;
+    for (const mg_ctx* c : b->box) ok = ok && fusable(c);
+    b->fused_ok = ok ? 1 : 0;
+    if (ok) {
+      int rc = build_fused(b);
+      if (rc) return rc;
+    }
+  }
   b->launches = 0;
   for (int s = 0; s < nsteps; s++) {
     const bool meas = en && s == nsteps - 1;
+    if (b->fused_ok == 1) {
+      cudaGraphExec_t& g = meas ? b->gf_meas : b->gf_step;
+      if (!g) {
+        int rc = capture_fused(b, meas, &g);
+        if (rc) return rc;
+      }
+      BCK(cudaGraphLaunch(g, b->main));
+      b->launches += b->launches_step;
+      continue;
+    }
     cudaGraphExec_t& g = meas ? b->g_meas : b->g_step;
     if (!g) {
       int rc = capture_step(b, meas, &g);
@@ -2486,6 +2680,12 @@ int mg_batch_md_steps(mg_batch* b, int nsteps, mg_energy* en) {
     BCK(cudaGraphLaunch(g, b->main));
     b->launches += b->launches_step;
   }
+  if (b->fused_ok == 1 && nsteps > 0)
+    for (mg_ctx* c : b->box) {
+      // what a launched force evaluation leaves behind (Widom's cell list)
+      c->last_r = c->d_r;
+      c->have_cells = true;
+    }
   BCK(cudaStreamSynchronize(b->main));
   for (size_t i = 0; i < b->box.size(); i++) {
     mg_ctx* c = b->box[i];
@@ -2658,6 +2858,41 @@ int mg_autotune(const mg_topology* top, mg_params* par, const double* r, int nre
       }
     }
   }
+  // the Ewald chain beside the r-space chain or after it: which is faster
+  // depends on how the two kernels share the SMs
+  int bser = par->kspace_serial;
+  if (!rc && bc && par->precision == MG_MIXED) {
+    double bests = 1e300;
+    for (int ser = 0; ser < 2 && rc == MG_OK; ser++) {
+      mg_params p2 = *par;
+      p2.cells_per_cutoff = bc;
+      p2.kspace_ctas_per_sm = bk;
+      p2.pair_variant = bv;
+      p2.kspace_serial = ser;
+      int st = 0;
+      mg_ctx* c = mg_create(top, &p2, &st);
+      double t = -1;
+      if (c) {
+        int e = mg_forces_device(c, r_dev, f_dev, 0, nullptr);
+        if (!e) {
+          cudaEventRecord(e0, c->stream);
+          for (int k = 0; k < nrep && !e; k++) e = mg_forces_device(c, r_dev, f_dev, 0, nullptr);
+          cudaEventRecord(e1, c->stream);
+          cudaEventSynchronize(e1);
+          float f = 0;
+          cudaEventElapsedTime(&f, e0, e1);
+          if (!e) t = f / nrep;
+        }
+        if (e) rc = e;
+        mg_destroy(c);
+      }
+      if (ms) ms[20 + ser] = t;
+      if (t > 0 && t < bests) {
+        bests = t;
+        bser = ser;
+      }
+    }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(r_dev);
@@ -2667,5 +2902,6 @@ int mg_autotune(const mg_topology* top, mg_params* par, const double* r, int nre
   par->cells_per_cutoff = bc;
   par->kspace_ctas_per_sm = bk;
   par->pair_variant = bv;
+  par->kspace_serial = bser;
   return MG_OK;
 }

@@ -86,7 +86,7 @@ struct Launch {
 // the linked-cell list as a counting sort (four kernels): key [ns] cell of
 // every site; count [ncell rounded up to 4] zero on entry and on return;
 // cursor [ncell], slot_site [ns] scratch; out: order [ns] sorted -> site
-// (site order within a cell), key_s [ns] the sorted cells, start [ncell+1]
+// (by z, then site index, within a cell), key_s [ns] the sorted cells, start [ncell+1]
 // pfix [ns] scratch: the fixed-point site records in site order; pj (or
 // null) gets them in cell order: {x, y, z as 32-bit fractions of the box,
 // (molecule << 8) | kind} (kind, mol: [ns] site tables).  gstart
@@ -284,6 +284,74 @@ struct ExclArgs {
 };
 constexpr int EXCL_THREADS = 128;
 cudaError_t k_excl_mixed(const Launch& L, const ExclArgs& a, bool measure, bool polar);
+
+// ---- batches: one launch per kernel over all boxes ----
+// One box of a batched MD step (non-polar boxes on the FP32 path whose
+// Ewald passes run on the FP32 cores, cells re-binned at every step): the
+// arguments of every kernel of its step and the CTAs each would be launched
+// with.  The batched kernels take blockIdx.y (pass 1: blockIdx.z) as the
+// box; CTAs beyond a box's own grid return at once.
+struct BoxStep {
+  // cell list
+  int ns, ncx, ncy, ncz;
+  double iL[3];
+  const double* r;
+  int* status;
+  const int* kind;
+  const int* mol;
+  int4* pfix;
+  int* key;
+  int* count;
+  int* cursor;
+  int* slot_site;
+  int* order;
+  int* key_s;
+  int* start;
+  int* gstart;
+  int4* pj;
+  int* gcell;
+  // r-space (the cell pair kernel, 4 warps per home cell)
+  PairArgs pa;
+  const PairF* ptab;
+  const float4* erd;
+  const float4* eru;
+  float sx, sy, sz, cq, sg, al;
+  ExclArgs xa;
+  // k-space on the FP32 cores
+  KArgs ka;
+  float2* tab;
+  uint4* qf;
+  float2* part;
+  // integrator
+  ShakeArgs sa;
+  // sums of a measured step: rows of part -> out, four of them
+  const double* rpart[4];
+  int rrows[4], rwidth[4];
+  double* rout[4];
+  // CTAs of each kernel
+  int g_site, g_order, g_pair, g_excl, g_charge, g_phase, g_p1x, g_p1y, g_skr, g_kf, g_shake;
+};
+// the largest grid and shared memory of each kernel over the boxes
+struct BatchGrid {
+  int site, order, pair, excl, charge, phase, p1x, p1y, skr, kf, shake;
+  size_t pair_smem, kf_smem;
+};
+// the force evaluation up to Ewald pass 1 (cell list, pair and exclusion
+// kernels, phase rows), then pass 1 (mg_kspace.cu), then the S(k) sums and
+// pass 2; then the step (SHAKE and, measured, the sums)
+cudaError_t k_batch_rspace(const Launch& L, const BoxStep* d, int nbox, const BatchGrid& g,
+                           bool measure);
+cudaError_t k_batch_pass1(const Launch& L, const BoxStep* d, int nbox, const BatchGrid& g);
+cudaError_t k_batch_sk_reduce(const Launch& L, const BoxStep* d, int nbox, const BatchGrid& g,
+                              bool measure);
+cudaError_t k_batch_pass2(const Launch& L, const BoxStep* d, int nbox, const BatchGrid& g);
+cudaError_t k_batch_step(const Launch& L, const BoxStep* d, int nbox, const BatchGrid& g,
+                         bool measure);
+size_t kf_mixed_smem(const KArgs& a);
+int kf_mixed_blocks(int nq);
+int cell_site_blocks(int ns);
+int cell_order_blocks(int ncell);
+
 
 // neighbour lists (mg_nlist.cu)
 struct ListArgs {

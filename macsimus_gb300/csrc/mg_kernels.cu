@@ -36,16 +36,17 @@ static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 //
 // cook threads the sites of every cell into a linked list
 // (cook/linklist.c:38-269).  Here the cells are runs of one array: the sites
-// sorted by cell, in increasing site order within a cell (a stable sort, so
+// sorted by cell and within a cell by z, then site index (a fixed order, so
 // the order and every sum over it are the same run to run), cell c holding
 // order[start[c] .. start[c+1]).  A counting sort in four kernels:
 //   cell_count    key of every site, sites per cell (atomic increments)
 //   cell_scan     one CTA: start = exclusive scan of the counts, cursor =
 //                 start, the counts zeroed again for the next list
 //   cell_scatter  every site into a free slot of its cell (atomic cursor)
-//   cell_order    a warp per cell ranks its sites by site index and writes
-//                 order[] and the sorted keys (the slots of cell_scatter
-//                 depend on the timing of the atomics; the ranks do not)
+//   cell_order    a warp per cell ranks its sites by z (then site index)
+//                 and writes order[] and the sorted keys (the slots of
+//                 cell_scatter depend on the timing of the atomics; the ranks
+//                 do not)
 
 // the fixed-point record of every site (site order) and its cell, from the
 // fixed-point coordinates (so that the cell and the coordinates the pair
@@ -85,9 +86,13 @@ __device__ __forceinline__ int2 shfl_up2(int2 v, int o) {
 }
 __device__ __forceinline__ int ngroups(int n) { return (n + GROUP_SITES - 1) / GROUP_SITES; }
 
-__global__ void __launch_bounds__(SCAN_THREADS)
-cell_scan_kernel(int ncell, int* __restrict__ count, int* __restrict__ start,
-                 int* __restrict__ cursor, int* __restrict__ gstart) {
+__device__ __forceinline__ void cell_scan_kernel_body(int ncell,
+    int* __restrict__ count,
+    int* __restrict__ start,
+    int* __restrict__ cursor,
+    int* __restrict__ gstart,
+    const int bx_,
+    const int by_) {
   __shared__ int2 wsum[SCAN_THREADS / 32];
   __shared__ int2 carry_s;
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
@@ -148,6 +153,11 @@ cell_scan_kernel(int ncell, int* __restrict__ count, int* __restrict__ start,
   }
 }
 
+__global__ void __launch_bounds__(SCAN_THREADS)
+cell_scan_kernel(int ncell, int* __restrict__ count, int* __restrict__ start, int* __restrict__ cursor, int* __restrict__ gstart) {
+  cell_scan_kernel_body(ncell, count, start, cursor, gstart, blockIdx.x, 0);
+}
+
 __global__ void cell_scatter_kernel(int ns, const int* __restrict__ key, int* __restrict__ cursor,
                                     int* __restrict__ slot_site) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -156,23 +166,37 @@ __global__ void cell_scatter_kernel(int ns, const int* __restrict__ key, int* __
 }
 
 constexpr int ORDER_THREADS = 256;
-__global__ void __launch_bounds__(ORDER_THREADS)
-cell_order_kernel(int ncell, const int* __restrict__ start, const int* __restrict__ slot_site,
-                  const int4* __restrict__ pfix, int* __restrict__ order, int* __restrict__ key_s,
-                  int4* __restrict__ pj, const int* __restrict__ gstart,
-                  int* __restrict__ gcell) {
-  const int c = blockIdx.x * (ORDER_THREADS / 32) + (threadIdx.x >> 5);
+__device__ __forceinline__ void cell_order_kernel_body(int ncell,
+    const int* __restrict__ start,
+    const int* __restrict__ slot_site,
+    const int4* __restrict__ pfix,
+    int* __restrict__ order,
+    int* __restrict__ key_s,
+    int4* __restrict__ pj,
+    const int* __restrict__ gstart,
+    int* __restrict__ gcell,
+    const int bx_,
+    const int by_) {
+  const int c = bx_ * (ORDER_THREADS / 32) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (c >= ncell) return;
   const int s0 = start[c], n = start[c + 1] - s0;
   // the cell of each of its groups (work items of the group pair kernel)
   if (gcell)
     for (int g = gstart[c] + lane; g < gstart[c + 1]; g += 32) gcell[g] = c;
+  // the sites of a cell in increasing z (ties by site index): runs of
+  // consecutive sites are then thin slabs, which the group kernel's
+  // bounding boxes prune well
   if (n <= 32) {
     // one site per lane, ranks by shuffles
     const int mine = lane < n ? slot_site[s0 + lane] : 0x7fffffff;
+    const unsigned mz = lane < n ? (unsigned)pfix[mine].z : 0xffffffffu;
     int rank = 0;
-    for (int j = 0; j < n; j++) rank += __shfl_sync(0xffffffffu, mine, j) < mine;
+    for (int j = 0; j < n; j++) {
+      const int os = __shfl_sync(0xffffffffu, mine, j);
+      const unsigned oz = __shfl_sync(0xffffffffu, mz, j);
+      rank += oz < mz || (oz == mz && os < mine);
+    }
     if (lane < n) {
       order[s0 + rank] = mine;
       key_s[s0 + rank] = c;
@@ -181,13 +205,23 @@ cell_order_kernel(int ncell, const int* __restrict__ start, const int* __restric
   } else {
     for (int e = lane; e < n; e += 32) {
       const int mine = slot_site[s0 + e];
+      const unsigned mz = (unsigned)pfix[mine].z;
       int rank = 0;
-      for (int j = 0; j < n; j++) rank += slot_site[s0 + j] < mine;
+      for (int j = 0; j < n; j++) {
+        const int os = slot_site[s0 + j];
+        const unsigned oz = (unsigned)pfix[os].z;
+        rank += oz < mz || (oz == mz && os < mine);
+      }
       order[s0 + rank] = mine;
       key_s[s0 + rank] = c;
       if (pj) pj[s0 + rank] = pfix[mine];
     }
   }
+}
+
+__global__ void __launch_bounds__(ORDER_THREADS)
+cell_order_kernel(int ncell, const int* __restrict__ start, const int* __restrict__ slot_site, const int4* __restrict__ pfix, int* __restrict__ order, int* __restrict__ key_s, int4* __restrict__ pj, const int* __restrict__ gstart, int* __restrict__ gcell) {
+  cell_order_kernel_body(ncell, start, slot_site, pfix, order, key_s, pj, gstart, gcell, blockIdx.x, 0);
 }
 
 cudaError_t k_cell_list(const Launch& L, int ns, const double* r, int* status, const double iL[3],
@@ -278,10 +312,19 @@ constexpr int FOLD = 8;   // stencil cells per FP32 force batch before the FP64 
 // (Knuth's TwoSum): no FP64 instruction in the loop (the FP64 pipe of this
 // GPU is narrow and also serves the float/double conversions).
 template <bool MEASURE, bool POLAR, bool REL, int NW, bool STAB>
-__global__ void __launch_bounds__(NW * 32)
-    pair_mixed_kernel(PairArgs a, const int4* __restrict__ pj, const PairF* __restrict__ ptab_g,
-                      const float4* __restrict__ erd_g, const float4* __restrict__ eru, float sx,
-                      float sy, float sz, float cq, float sgrid, float alpha) {
+__device__ __forceinline__ void pair_mixed_kernel_body(const PairArgs& a,
+    const int4* __restrict__ pj,
+    const PairF* __restrict__ ptab_g,
+    const float4* __restrict__ erd_g,
+    const float4* __restrict__ eru,
+    float sx,
+    float sy,
+    float sz,
+    float cq,
+    float sgrid,
+    float alpha,
+    const int bx_,
+    const int by_) {
   constexpr int NT = NW * 32;
   // dynamic shared memory: the nk x nk FP32 pair table, then (STAB) the
   // force spline
@@ -301,7 +344,7 @@ __global__ void __launch_bounds__(NW * 32)
   const float4* erd = STAB ? s_erd : erd_g;
   __syncthreads();
 
-  const int c = blockIdx.x;
+  const int c = bx_;
   const int cz = c % a.ncz, cy = (c / a.ncz) % a.ncy, cx = c / (a.ncy * a.ncz);
   const int i0 = a.cell_start[c], ni = a.cell_start[c + 1] - i0;
   // fixed-point centre of the home cell
@@ -481,10 +524,16 @@ __global__ void __launch_bounds__(NW * 32)
         if (threadIdx.x < w) ered[threadIdx.x] += ered[threadIdx.x + w];
         __syncthreads();
       }
-      if (threadIdx.x == 0) a.epart[blockIdx.x * NEN + k] = ered[0];
+      if (threadIdx.x == 0) a.epart[bx_ * NEN + k] = ered[0];
       __syncthreads();
     }
   }
+}
+
+template <bool MEASURE, bool POLAR, bool REL, int NW, bool STAB>
+__global__ void __launch_bounds__(NW * 32)
+    pair_mixed_kernel(const __grid_constant__ PairArgs a, const int4* __restrict__ pj, const PairF* __restrict__ ptab_g, const float4* __restrict__ erd_g, const float4* __restrict__ eru, float sx, float sy, float sz, float cq, float sgrid, float alpha) {
+  pair_mixed_kernel_body<MEASURE, POLAR, REL, NW, STAB>(a, pj, ptab_g, erd_g, eru, sx, sy, sz, cq, sgrid, alpha, blockIdx.x, 0);
 }
 
 // ------------------------------------------------- group pair kernel --
@@ -958,9 +1007,11 @@ __device__ __forceinline__ double near_img(double d, double L, double iL) {
 }
 
 template <bool MEASURE, bool POLAR>
-__global__ void __launch_bounds__(EXCL_THREADS) excl_mixed_kernel(ExclArgs a) {
+__device__ __forceinline__ void excl_mixed_kernel_body(const ExclArgs& a,
+    const int bx_,
+    const int by_) {
   __shared__ double red[EXCL_THREADS];
-  const int n = blockIdx.x * EXCL_THREADS + threadIdx.x;
+  const int n = bx_ * EXCL_THREADS + threadIdx.x;
   double en[7] = {0, 0, 0, 0, 0, 0, 0};
   if (n < a.nmol) {
     const long ns3 = 3 * (long)a.ns;
@@ -1005,10 +1056,15 @@ __global__ void __launch_bounds__(EXCL_THREADS) excl_mixed_kernel(ExclArgs a) {
         if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
         __syncthreads();
       }
-      if (threadIdx.x == 0) a.epart[blockIdx.x * NEN + k] = red[0];
+      if (threadIdx.x == 0) a.epart[bx_ * NEN + k] = red[0];
       __syncthreads();
     }
   }
+}
+
+template <bool MEASURE, bool POLAR>
+__global__ void __launch_bounds__(EXCL_THREADS) excl_mixed_kernel(const __grid_constant__ ExclArgs a) {
+  excl_mixed_kernel_body<MEASURE, POLAR>(a, blockIdx.x, 0);
 }
 
 cudaError_t k_excl_mixed(const Launch& L, const ExclArgs& a, bool measure, bool polar) {
@@ -1078,8 +1134,12 @@ cudaError_t k_add_forces(const Launch& L, size_t n, const double* fk, double* f)
 }
 
 // fixed-point coordinates of every charge (Drude charges at r + rpol)
-__global__ void charge_fixed_kernel(KArgs a, const double* __restrict__ r, uint4* __restrict__ qf) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void charge_fixed_kernel_body(const KArgs& a,
+    const double* __restrict__ r,
+    uint4* __restrict__ qf,
+    const int bx_,
+    const int by_) {
+  const int j = bx_ * blockDim.x + threadIdx.x;
   if (j >= a.nq) return;
   const int site = a.qsite[j];
   double x = r[3 * site], y = r[3 * site + 1], z = r[3 * site + 2];
@@ -1092,9 +1152,16 @@ __global__ void charge_fixed_kernel(KArgs a, const double* __restrict__ r, uint4
                      (unsigned)fixed32(z, a.iLz), 0u);
 }
 
-__global__ void phase_tables_mixed_kernel(KArgs a, const uint4* __restrict__ qf,
-                                          float2* __restrict__ tab) {
-  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void charge_fixed_kernel(const __grid_constant__ KArgs a, const double* __restrict__ r, uint4* __restrict__ qf) {
+  charge_fixed_kernel_body(a, r, qf, blockIdx.x, 0);
+}
+
+__device__ __forceinline__ void phase_tables_mixed_kernel_body(const KArgs& a,
+    const uint4* __restrict__ qf,
+    float2* __restrict__ tab,
+    const int bx_,
+    const int by_) {
+  long t = (long)bx_ * blockDim.x + threadIdx.x;
   if (t >= (long)a.nq * a.row) return;
   int j = (int)(t / a.row), e = (int)(t % a.row);
   int d, n;
@@ -1114,6 +1181,10 @@ __global__ void phase_tables_mixed_kernel(KArgs a, const uint4* __restrict__ qf,
     sn *= q;
   }
   tab[t] = make_float2(cs, sn);
+}
+
+__global__ void phase_tables_mixed_kernel(const __grid_constant__ KArgs a, const uint4* __restrict__ qf, float2* __restrict__ tab) {
+  phase_tables_mixed_kernel_body(a, qf, tab, blockIdx.x, 0);
 }
 
 __global__ void phase_tables_fp64_kernel(KArgs a, const double* __restrict__ r,
@@ -1247,10 +1318,14 @@ cudaError_t k_sk_fp64(const Launch& L, const KArgs& a, const double2* tab, doubl
 // S(k) = sum over chunks (FP64, fixed order); energy and virial per k
 // (sim/ewpass2m.c: E1 = |S|^2 ekk, ptf = 1/kk + (pi/alpha)^2) reduced per block
 template <typename T2>
-__global__ void sk_reduce_kernel(KArgs a, const T2* __restrict__ part, bool measure,
-                                 double pi2_over_a2) {
+__device__ __forceinline__ void sk_reduce_kernel_body(const KArgs& a,
+    const T2* __restrict__ part,
+    bool measure,
+    double pi2_over_a2,
+    const int bx_,
+    const int by_) {
   __shared__ double red[256][7];
-  const int k = blockIdx.x * 256 + threadIdx.x;
+  const int k = bx_ * 256 + threadIdx.x;
   double e[7] = {0, 0, 0, 0, 0, 0, 0};
   if (k < a.nk) {
     double sr = 0, si = 0;
@@ -1288,7 +1363,12 @@ __global__ void sk_reduce_kernel(KArgs a, const T2* __restrict__ part, bool meas
     __syncthreads();
   }
   if (threadIdx.x == 0)
-    for (int m = 0; m < 7; m++) a.ek_part[blockIdx.x * 7 + m] = red[0][m];
+    for (int m = 0; m < 7; m++) a.ek_part[bx_ * 7 + m] = red[0][m];
+}
+
+template <typename T2>
+__global__ void sk_reduce_kernel(const __grid_constant__ KArgs a, const T2* __restrict__ part, bool measure, double pi2_over_a2) {
+  sk_reduce_kernel_body<T2>(a, part, measure, pi2_over_a2, blockIdx.x, 0);
 }
 
 cudaError_t k_sk_reduce_mixed(const Launch& L, const KArgs& a, const float2* part, bool measure) {
@@ -1365,8 +1445,12 @@ cudaError_t k_kforce_fp64(const Launch& L, const KArgs& a, const double2* tab) {
 }
 
 // out[k] = sum over rows of part[row*width+k], fixed order (one CTA)
-__global__ void reduce_rows_kernel(const double* __restrict__ part, int nrows, int width,
-                                   double* __restrict__ out) {
+__device__ __forceinline__ void reduce_rows_kernel_body(const double* __restrict__ part,
+    int nrows,
+    int width,
+    double* __restrict__ out,
+    const int bx_,
+    const int by_) {
   __shared__ double red[256];
   for (int k = 0; k < width; k++) {
     double s = 0;
@@ -1380,6 +1464,10 @@ __global__ void reduce_rows_kernel(const double* __restrict__ part, int nrows, i
     if (threadIdx.x == 0) out[k] = red[0];
     __syncthreads();
   }
+}
+
+__global__ void reduce_rows_kernel(const double* __restrict__ part, int nrows, int width, double* __restrict__ out) {
+  reduce_rows_kernel_body(part, nrows, width, out, blockIdx.x, 0);
 }
 
 cudaError_t k_reduce_sum(const Launch& L, const double* part, int nrows, int width, double* out) {
@@ -1491,9 +1579,11 @@ __device__ __forceinline__ void meas_kin(ShakeMeas& m, double mi, double v1x, do
 }
 
 template <bool NOSE, bool MEAS>
-__global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
+__device__ __forceinline__ void shake_kernel_body(const ShakeArgs& a,
+    const int bx_,
+    const int by_) {
   __shared__ double red[SH_THREADS];
-  const int n = blockIdx.x * SH_THREADS + threadIdx.x;
+  const int n = bx_ * SH_THREADS + threadIdx.x;
   double kin = 0;
   [[maybe_unused]] ShakeMeas ms;
   if constexpr (MEAS) meas_zero(ms);
@@ -1676,7 +1766,7 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
     if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
     __syncthreads();
   }
-  if (threadIdx.x == 0) a.kin_part[blockIdx.x] = red[0];
+  if (threadIdx.x == 0) a.kin_part[bx_] = red[0];
   if constexpr (MEAS) {
     // the 13 measured sums of the CTA in a fixed order: a shuffle tree per
     // warp, then the warps' sums in warp order (red[] is free again)
@@ -1700,9 +1790,14 @@ __global__ void __launch_bounds__(SH_THREADS) shake_kernel(ShakeArgs a) {
     if (threadIdx.x < 13) {
       double x = 0;
       for (int w = 0; w < SH_THREADS / 32; w++) x += red[w * 13 + threadIdx.x];
-      a.meas_part[(long)blockIdx.x * 13 + threadIdx.x] = x;
+      a.meas_part[(long)bx_ * 13 + threadIdx.x] = x;
     }
   }
+}
+
+template <bool NOSE, bool MEAS>
+__global__ void __launch_bounds__(SH_THREADS) shake_kernel(const __grid_constant__ ShakeArgs a) {
+  shake_kernel_body<NOSE, MEAS>(a, blockIdx.x, 0);
 }
 
 cudaError_t k_shake(const Launch& L, const ShakeArgs& a) {
@@ -1742,6 +1837,159 @@ __global__ void fma_probe_kernel(int iters, float* __restrict__ out) {
 
 cudaError_t k_fma_probe(cudaStream_t s, int blocks, int threads, int iters, float* out) {
   fma_probe_kernel<<<blocks, threads, 0, s>>>(iters, out);
+  return cudaGetLastError();
+}
+
+}  // namespace mg
+
+namespace mg {
+
+// ------------------------------------------------------------ batches --
+//
+// The kernels of one MD step over every box of a batch, one launch each:
+// blockIdx.y is the box, blockIdx.x the CTA of that box's own grid (the
+// same CTAs, threads and arguments as the box's single launch, so every box
+// gets its single-launch results bit for bit); CTAs beyond a box's grid
+// return at once.
+
+int cell_site_blocks(int ns) { return cdiv(ns, 256); }
+int cell_order_blocks(int ncell) { return cdiv(ncell, ORDER_THREADS / 32); }
+
+__global__ void batch_cell_count_kernel(const BoxStep* __restrict__ B) {
+  const BoxStep& e = B[blockIdx.y];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= e.ns) return;
+  const double x = e.r[3 * i], y = e.r[3 * i + 1], z = e.r[3 * i + 2];
+  int k = 0;
+  const int4 q = make_int4(fixed32(x, e.iL[0]), fixed32(y, e.iL[1]), fixed32(z, e.iL[2]),
+                           (e.mol[i] << 8) | e.kind[i]);
+  if (isfinite(x) && isfinite(y) && isfinite(z)) {
+    k = (fixed_cell(q.x, e.ncx) * e.ncy + fixed_cell(q.y, e.ncy)) * e.ncz +
+        fixed_cell(q.z, e.ncz);
+  } else {
+    atomicOr(e.status, 2);
+  }
+  e.pfix[i] = q;
+  e.key[i] = k;
+  atomicAdd(e.count + k, 1);
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) batch_cell_scan_kernel(const BoxStep* __restrict__ B) {
+  const BoxStep& e = B[blockIdx.y];
+  cell_scan_kernel_body(e.ncx * e.ncy * e.ncz, e.count, e.start, e.cursor, e.gstart, 0, 0);
+}
+
+__global__ void batch_cell_scatter_kernel(const BoxStep* __restrict__ B) {
+  const BoxStep& e = B[blockIdx.y];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= e.ns) return;
+  e.slot_site[atomicAdd(e.cursor + e.key[i], 1)] = i;
+}
+
+__global__ void __launch_bounds__(ORDER_THREADS) batch_cell_order_kernel(const BoxStep* __restrict__ B) {
+  const BoxStep& e = B[blockIdx.y];
+  if ((int)blockIdx.x >= e.g_order) return;
+  cell_order_kernel_body(e.ncx * e.ncy * e.ncz, e.start, e.slot_site, e.pfix, e.order, e.key_s,
+                         e.pj, e.gstart, e.gcell, blockIdx.x, 0);
+}
+
+template <bool MEASURE>
+__global__ void __launch_bounds__(4 * 32) batch_pair_kernel(const BoxStep* __restrict__ B) {
+  const BoxStep& e = B[blockIdx.y];
+  if ((int)blockIdx.x >= e.g_pair) return;
+  pair_mixed_kernel_body<MEASURE, false, true, 4, false>(e.pa, e.pj, e.ptab, e.erd, e.eru, e.sx,
+                                                         e.sy, e.sz, e.cq, e.sg, e.al,
+                                                         blockIdx.x, 0);
+}
+
+template <bool MEASURE>
+__global__ void __launch_bounds__(EXCL_THREADS) batch_excl_kernel(const BoxStep* __restrict__ B) {
+  const BoxStep& e = B[blockIdx.y];
+  if ((int)blockIdx.x >= e.g_excl) return;
+  excl_mixed_kernel_body<MEASURE, false>(e.xa, blockIdx.x, 0);
+}
+
+__global__ void batch_charge_fixed_kernel(const BoxStep* __restrict__ B) {
+  const BoxStep& e = B[blockIdx.y];
+  if ((int)blockIdx.x >= e.g_charge) return;
+  charge_fixed_kernel_body(e.ka, e.r, e.qf, blockIdx.x, 0);
+}
+
+__global__ void batch_phase_kernel(const BoxStep* __restrict__ B) {
+  const BoxStep& e = B[blockIdx.y];
+  if ((int)blockIdx.x >= e.g_phase) return;
+  phase_tables_mixed_kernel_body(e.ka, e.qf, e.tab, blockIdx.x, 0);
+}
+
+__global__ void batch_sk_reduce_kernel(const BoxStep* __restrict__ B, bool measure) {
+  const BoxStep& e = B[blockIdx.y];
+  if ((int)blockIdx.x >= e.g_skr) return;
+  const double pa = 9.869604401089358 / (e.ka.alpha * e.ka.alpha);
+  sk_reduce_kernel_body<float2>(e.ka, e.part, measure, pa, blockIdx.x, 0);
+}
+
+template <bool MEAS>
+__global__ void __launch_bounds__(SH_THREADS) batch_shake_kernel(const BoxStep* __restrict__ B) {
+  const BoxStep& e = B[blockIdx.y];
+  if ((int)blockIdx.x >= e.g_shake) return;
+  shake_kernel_body<false, MEAS>(e.sa, blockIdx.x, 0);
+}
+
+// sums k0..k1-1 of every box (one CTA each)
+__global__ void batch_reduce_kernel(const BoxStep* __restrict__ B, int k0, int k1) {
+  const BoxStep& e = B[blockIdx.y];
+  for (int k = k0; k < k1; k++)
+    reduce_rows_kernel_body(e.rpart[k], e.rrows[k], e.rwidth[k], e.rout[k], 0, 0);
+}
+
+cudaError_t k_batch_rspace(const Launch& L, const BoxStep* d, int nbox, const BatchGrid& g,
+                           bool measure) {
+  batch_cell_count_kernel<<<dim3(g.site, nbox), 256, 0, L.s>>>(d);
+  batch_cell_scan_kernel<<<dim3(1, nbox), SCAN_THREADS, 0, L.s>>>(d);
+  batch_cell_scatter_kernel<<<dim3(g.site, nbox), 256, 0, L.s>>>(d);
+  batch_cell_order_kernel<<<dim3(g.order, nbox), ORDER_THREADS, 0, L.s>>>(d);
+  cudaError_t e = cudaSuccess;
+  if (measure) {
+    if (g.pair_smem > 48 * 1024)
+      e = cudaFuncSetAttribute(batch_pair_kernel<true>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.pair_smem);
+    if (e == cudaSuccess)
+      batch_pair_kernel<true><<<dim3(g.pair, nbox), 128, g.pair_smem, L.s>>>(d);
+    if (g.excl > 0) batch_excl_kernel<true><<<dim3(g.excl, nbox), EXCL_THREADS, 0, L.s>>>(d);
+  } else {
+    if (g.pair_smem > 48 * 1024)
+      e = cudaFuncSetAttribute(batch_pair_kernel<false>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.pair_smem);
+    if (e == cudaSuccess)
+      batch_pair_kernel<false><<<dim3(g.pair, nbox), 128, g.pair_smem, L.s>>>(d);
+    if (g.excl > 0) batch_excl_kernel<false><<<dim3(g.excl, nbox), EXCL_THREADS, 0, L.s>>>(d);
+  }
+  if (e != cudaSuccess) return e;
+  batch_charge_fixed_kernel<<<dim3(g.charge, nbox), 256, 0, L.s>>>(d);
+  batch_phase_kernel<<<dim3(g.phase, nbox), 256, 0, L.s>>>(d);
+  *L.counter += 7 + (g.excl > 0 ? 1 : 0);
+  return cudaGetLastError();
+}
+
+cudaError_t k_batch_sk_reduce(const Launch& L, const BoxStep* d, int nbox, const BatchGrid& g,
+                              bool measure) {
+  batch_sk_reduce_kernel<<<dim3(g.skr, nbox), 256, 0, L.s>>>(d, measure);
+  LAUNCHED(L);
+  return cudaGetLastError();
+}
+
+cudaError_t k_batch_step(const Launch& L, const BoxStep* d, int nbox, const BatchGrid& g,
+                         bool measure) {
+  if (measure) {
+    // the energies of the force evaluation (rows 0, 1), the step, its sums (2, 3)
+    batch_reduce_kernel<<<dim3(1, nbox), 256, 0, L.s>>>(d, 0, 2);
+    batch_shake_kernel<true><<<dim3(g.shake, nbox), SH_THREADS, 0, L.s>>>(d);
+    batch_reduce_kernel<<<dim3(1, nbox), 256, 0, L.s>>>(d, 2, 4);
+    *L.counter += 3;
+  } else {
+    batch_shake_kernel<false><<<dim3(g.shake, nbox), SH_THREADS, 0, L.s>>>(d);
+    LAUNCHED(L);
+  }
   return cudaGetLastError();
 }
 

@@ -213,11 +213,10 @@ __device__ __forceinline__ void sk_stage_mac(const float2 (*X)[KTR], const float
 template <int MZ>
 __device__ __forceinline__ void sk_gemm_mixed_body(const KArgs& a, const float2* __restrict__ tab,
                                                    float2* __restrict__ part, const KTile& tile,
-                                                   int kz0, int nz, SkSmem& sm) {
+                                                   int kz0, int nz, SkSmem& sm, const int ch) {
   auto& Xs = sm.X;
   auto& Ys = sm.Y;
   auto& Zs = sm.Z;
-  const int ch = blockIdx.y;
   const int j0 = (int)((long)a.nq * ch / a.nchunk), j1 = (int)((long)a.nq * (ch + 1) / a.nchunk);
   const int tid = threadIdx.x, tr = tid >> 3, tz = tid & 7;
   const int oy = a.Kx + 1 + a.Ky, oz = a.Kx + 2 * a.Ky + 2;
@@ -291,19 +290,27 @@ __device__ __forceinline__ void sk_gemm_mixed_body(const KArgs& a, const float2*
   }
 }
 
-__global__ void __launch_bounds__(Q1_THREADS)
-    sk_gemm_mixed_kernel(KArgs a, const float2* __restrict__ tab, float2* __restrict__ part) {
+__device__ __forceinline__ void sk_gemm_mixed_kernel_body(const KArgs& a,
+    const float2* __restrict__ tab,
+    float2* __restrict__ part,
+    const int bx_,
+    const int by_) {
   __shared__ __align__(16) SkSmem sm;
-  const int2 job = a.p1job[blockIdx.x];
+  const int2 job = a.p1job[bx_];
   const KTile tile = a.tiles[job.x];
   const int kz0 = job.y;
   const int nz = min(Q1_NZ, tile.R - kz0 + 1);
   switch ((nz + 7) >> 3) {
-    case 1: sk_gemm_mixed_body<1>(a, tab, part, tile, kz0, nz, sm); break;
-    case 2: sk_gemm_mixed_body<2>(a, tab, part, tile, kz0, nz, sm); break;
-    case 3: sk_gemm_mixed_body<3>(a, tab, part, tile, kz0, nz, sm); break;
-    default: sk_gemm_mixed_body<4>(a, tab, part, tile, kz0, nz, sm); break;
+    case 1: sk_gemm_mixed_body<1>(a, tab, part, tile, kz0, nz, sm, by_); break;
+    case 2: sk_gemm_mixed_body<2>(a, tab, part, tile, kz0, nz, sm, by_); break;
+    case 3: sk_gemm_mixed_body<3>(a, tab, part, tile, kz0, nz, sm, by_); break;
+    default: sk_gemm_mixed_body<4>(a, tab, part, tile, kz0, nz, sm, by_); break;
   }
+}
+
+__global__ void __launch_bounds__(Q1_THREADS)
+    sk_gemm_mixed_kernel(const __grid_constant__ KArgs a, const float2* __restrict__ tab, float2* __restrict__ part) {
+  sk_gemm_mixed_kernel_body(a, tab, part, blockIdx.x, blockIdx.y);
 }
 
 cudaError_t k_sk_gemm_mixed(const Launch& L, const KArgs& a, const float2* tab, float2* part) {
@@ -468,20 +475,25 @@ static cudaError_t launch_kf_gemm(const Launch& L, const KArgs& a, const T2* tab
 constexpr int Q2_THREADS = 256;
 constexpr int Q2_NJ = 32;
 
+int kf_mixed_blocks(int nq) { return (nq + Q2_NJ - 1) / Q2_NJ; }
+
 size_t kf_mixed_smem(const KArgs& a) {
   const int nz = a.Kz + 1, nw = 2 * a.Kz + 1, nxy = a.Kx + 1 + 2 * a.Ky + 1;
   return sizeof(float2) * ((size_t)nz * Q2_NJ + (size_t)Q2_NJ * nxy + 2 * (size_t)nw * KTR);
 }
 
-__global__ void __launch_bounds__(Q2_THREADS, 2)
-    kf_gemm_mixed_kernel(KArgs a, const float2* __restrict__ tab, const float2* __restrict__ W) {
+__device__ __forceinline__ void kf_gemm_mixed_kernel_body(const KArgs& a,
+    const float2* __restrict__ tab,
+    const float2* __restrict__ W,
+    const int bx_,
+    const int by_) {
   extern __shared__ __align__(16) unsigned char smem_kf[];
   const int nz = a.Kz + 1, nw = 2 * a.Kz + 1, nxy = a.Kx + 1 + 2 * a.Ky + 1;
   float2* Zs = reinterpret_cast<float2*>(smem_kf);  // [nz][Q2_NJ]: Z(0..Kz)
   float2* XYs = Zs + (size_t)nz * Q2_NJ;            // [Q2_NJ][nxy]
   float2* Ws = XYs + (size_t)Q2_NJ * nxy;           // [2][nw][KTR]: W(kz = z - R)
   const int tid = threadIdx.x, tw = tid & 31, tj = tid >> 5;
-  const int jbase = blockIdx.x * Q2_NJ;
+  const int jbase = bx_ * Q2_NJ;
   const int oz = a.Kx + 2 * a.Ky + 2, oyl = a.Kx + 1 + a.Ky;
   for (int t = tid; t < nz * Q2_NJ; t += Q2_THREADS) {
     const int z = t / Q2_NJ, c = t % Q2_NJ, j = jbase + c;
@@ -607,6 +619,11 @@ __global__ void __launch_bounds__(Q2_THREADS, 2)
   }
 }
 
+__global__ void __launch_bounds__(Q2_THREADS, 2)
+    kf_gemm_mixed_kernel(const __grid_constant__ KArgs a, const float2* __restrict__ tab, const float2* __restrict__ W) {
+  kf_gemm_mixed_kernel_body(a, tab, W, blockIdx.x, 0);
+}
+
 cudaError_t k_kf_gemm_mixed(const Launch& L, const KArgs& a, const float2* tab) {
   const size_t smem = kf_mixed_smem(a);
   cudaError_t e = cudaFuncSetAttribute(kf_gemm_mixed_kernel,
@@ -689,6 +706,40 @@ cudaError_t k_dipole(const Launch& L, const KArgs& a, const double* r, double* p
     dipole_force_kernel<<<nb, DIP_THREADS, 0, L.s>>>(a, M, c[0], c[1], c[2], f);
     ++*L.counter;
   }
+  return cudaGetLastError();
+}
+
+}  // namespace mg
+
+namespace mg {
+
+// Ewald passes 1 and 2 of every box of a batch, one launch each (blockIdx.z
+// / blockIdx.y the box; CTAs beyond a box's own grid return at once)
+__global__ void __launch_bounds__(Q1_THREADS) batch_sk_gemm_kernel(const BoxStep* __restrict__ B) {
+  const BoxStep& e = B[blockIdx.z];
+  if ((int)blockIdx.x >= e.g_p1x || (int)blockIdx.y >= e.g_p1y) return;
+  sk_gemm_mixed_kernel_body(e.ka, e.tab, e.part, blockIdx.x, blockIdx.y);
+}
+
+__global__ void __launch_bounds__(Q2_THREADS) batch_kf_gemm_kernel(const BoxStep* __restrict__ B) {
+  const BoxStep& e = B[blockIdx.y];
+  if ((int)blockIdx.x >= e.g_kf) return;
+  kf_gemm_mixed_kernel_body(e.ka, e.tab, e.ka.Wf, blockIdx.x, 0);
+}
+
+cudaError_t k_batch_pass1(const Launch& L, const BoxStep* d, int nbox, const BatchGrid& g) {
+  batch_sk_gemm_kernel<<<dim3(g.p1x, g.p1y, nbox), Q1_THREADS, 0, L.s>>>(d);
+  ++*L.counter;
+  return cudaGetLastError();
+}
+
+cudaError_t k_batch_pass2(const Launch& L, const BoxStep* d, int nbox, const BatchGrid& g) {
+  cudaError_t e = cudaFuncSetAttribute(batch_kf_gemm_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)g.kf_smem);
+  if (e != cudaSuccess) return e;
+  batch_kf_gemm_kernel<<<dim3(g.kf, nbox), Q2_THREADS, g.kf_smem, L.s>>>(d);
+  ++*L.counter;
   return cudaGetLastError();
 }
 

@@ -43,6 +43,41 @@ def test_batch_md_equals_single_boxes(precision):
     batch.close()
 
 
+def test_fused_batch_md_equals_single_boxes():
+    """boxes on the FP32 path with the Ewald passes on the FP32 cores: one
+    launch per kernel over all boxes (blockIdx.y = box); every box gets the
+    positions, velocities and energies it gets alone, bit for bit, and the
+    launches per step do not grow with the number of boxes"""
+    launches = {}
+    for n in (3, 7):
+        bs = boxes(n, seed=13)
+        batch = M.Batch([dict(args(b), kspace_engine=1) for b in bs], precision="mixed", lanes=3)
+        for i, b in enumerate(bs):
+            batch.box[i].md_set_state(b["r"], b["r1"])
+        en = batch.md_steps(6)
+        assert batch.fused
+        batch.md_steps(2, measure=False)
+        launches[n] = batch.launches
+        for i, b in enumerate(bs):
+            a = dict(args(b), kspace_engine=1)
+            fp = M.ForcePath(a.pop("system"), a.pop("L"), a.pop("cutoff"), a.pop("alpha"),
+                             a.pop("kappa"), precision="mixed", **a)
+            fp.md_set_state(b["r"], b["r1"])
+            e1 = fp.md_steps(6)
+            fp.md_steps(2, measure=False)
+            rb, r1b = batch.box[i].md_get_state()
+            rs, r1s = fp.md_get_state()
+            assert np.array_equal(rb, rs) and np.array_equal(r1b, r1s)
+            for k in ("el", "lj", "ekin", "virc"):
+                assert en[i][k] == e1[k], k
+            assert en[i]["Ptens"] == e1["Ptens"]
+        # Widom into the configurations the batched step left
+        w = batch.widom([2], n=20000, seed=3, T=298.0)
+        assert all(np.isfinite(x["mu"]) for x in w)
+        batch.close()
+    assert launches[3] == launches[7]
+
+
 def test_batch_forces_match_oracle():
     bs = boxes(3, seed=5)
     batch = M.Batch([args(b) for b in bs], precision="fp64")
