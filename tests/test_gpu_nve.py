@@ -84,3 +84,65 @@ def test_nve_drift_no_worse_than_reference(precision):
     # fluctuation and step-to-step changes of Etot: cook's size
     assert fg < 1.3 * fc, (fg, fc)
     assert dg < 1.3 * dc, (dg, dc)
+
+
+def ensemble_drifts(runs_E, h_block):
+    """per run the drift (K/ps) of block means, then their mean and the
+    standard error of that mean over the runs"""
+    s = []
+    for E in runs_E:
+        E = np.asarray(E)
+        t = (np.arange(len(E)) + 0.5) * h_block
+        x = t - t.mean()
+        s.append(float((x * (E - E.mean())).sum() / (x * x).sum()))
+    s = np.array(s)
+    return s, s.mean(), s.std(ddof=1) / np.sqrt(len(s))
+
+
+def device_ensemble(precision, ref):
+    """the same protocol as cook's four runs: 864 SPC/E from lattice starts
+    with independent seeds, Berendsen 0.1 ps for the equilibration steps,
+    then NVE; Etot of every step in block means"""
+    from macsimus_gb300 import configs
+    p = ref["params"]
+    g, meta, system, ew = load("spce864")
+    out = []
+    for seed in p["seeds"]:
+        w = configs.workload("spce864", seed=seed)
+        kw = dict(precision=precision, h=p["h"], epsc=p["epsc"], omegac=meta["omegac"])
+        eq = M.ForcePath(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"],
+                         thermostat="berendsen", T=298.0, tau_T=0.1, **kw)
+        eq.md_set_state(w["r"], w["r1"])
+        eq.md_steps(p["equil"], measure=False)
+        r, r1 = eq.md_get_state()
+        eq.close()
+        fp = M.ForcePath(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"], **kw)
+        fp.md_set_state(r, r1)
+        E = np.empty(p["steps"])
+        for k in range(p["steps"]):
+            en = fp.md_steps(1)
+            E[k] = en["el"] + en["lj"] + en["ekin"]
+        fp.close()
+        nb = p["steps"] // p["block"]
+        out.append(E[:nb * p["block"]].reshape(nb, p["block"]).mean(1))
+    return out
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_nve_drift_ensemble_against_reference(precision):
+    """four independent 50 ps NVE runs on each side (tests/golden/nve864x4:
+    cook's own runs from crystal starts with seeds 11..14, 1500 Berendsen
+    steps then 25000 NVE steps): the mean drift of the device is at most
+    1.2 x the magnitude of cook's plus two combined standard errors (the
+    standard errors from the spread of the four runs)"""
+    ref = json.load(open(os.path.join(GOLDEN, "nve864x4.json")))
+    p = ref["params"]
+    hb = p["h"] * p["block"]
+    sc, mc, ec = ensemble_drifts([r["Etot_block"] for r in ref["runs"]], hb)
+    runs = device_ensemble(precision, ref)
+    sg, mg, eg = ensemble_drifts(runs, hb)
+    print("NVE drift over 4 x %d steps, K/ps: cook %s -> %.2f +- %.2f; %s %s -> %.2f +- %.2f"
+          % (p["steps"], np.round(sc, 2), mc, ec, precision, np.round(sg, 2), mg, eg))
+    # the same equilibrium temperature
+    assert abs(np.mean([r["Tkin_mean"] for r in ref["runs"]]) / 298.0 - 1) < 0.03
+    assert abs(mg) <= 1.2 * abs(mc) + 2 * np.hypot(ec, eg), (mg, eg, mc, ec)
