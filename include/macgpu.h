@@ -379,12 +379,14 @@ int mg_xwidom(mg_ctx *ctx, int nlist, const int *mols, const int *vtype, const d
    r for every cell subdivision (cells_per_cutoff 1..3) and Ewald pass-1
    split (kspace_ctas_per_sm 6, 10, 16) and writes the fastest pair into
    *par, then the fastest of the 8 cell-kernel pair_variant values at that
-   choice and of the group kernel (pair_variant 8) at every subdivision.
-   Last, for the FP32 path, kspace_serial 0 or 1 at that choice.  Builds
-   and frees its own trial contexts; ms[22] (optional) gets the time per
-   evaluation of each trial (cdiv-major, then the 8 cell-kernel variants,
-   the group kernel at cdiv 1..3, kspace_serial 0 and 1; -1 if that grid is
-   not possible or the trial did not run). */
+   choice and of the group kernel (pair_variant 8) at every subdivision,
+   each timed (FP32 path) with kspace_serial 0 and 1, the pair chosen
+   together.  Builds and frees its own trial contexts; ms[22] (optional)
+   gets the time per evaluation of each trial (cdiv-major, then the 8
+   cell-kernel variants and the group kernel at cdiv 1..3, the faster of
+   the two kspace_serial settings each, then the chosen variant with
+   kspace_serial 0 and 1; -1 if that grid is not possible or the trial did
+   not run). */
 int mg_autotune(const mg_topology *top, mg_params *par, const double *r, int nrep, double *ms);
 
 /* ---- adjoint ----

@@ -162,9 +162,11 @@ def library():
 
 
 def autotune(system, L, cutoff, alpha, kappa, r, nrep=3, **kw):
-    """the fastest (cells_per_cutoff, kspace_ctas_per_sm, pair_variant) for
-    this box and configuration (mg_autotune), with the timings (3x3 grid x
-    split, the 8 cell-kernel pair variants, the group kernel at cdiv 1..3)"""
+    """the fastest (cells_per_cutoff, kspace_ctas_per_sm, pair_variant,
+    kspace_serial) for this box and configuration (mg_autotune), with the
+    timings (3x3 grid x split, the 8 cell-kernel pair variants, the group
+    kernel at cdiv 1..3, the chosen variant with the Ewald chain concurrent
+    and serial)"""
     t, p, keep = describe(system, L, cutoff, alpha, kappa, **kw)
     ms = np.full(22, -1.0)
     rr = _arr(r, np.float64).reshape(-1)

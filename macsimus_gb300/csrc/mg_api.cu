@@ -2763,30 +2763,35 @@ int mg_autotune(const mg_topology* top, mg_params* par, const double* r, int nre
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
+  int rc = MG_OK;
+  // time per force evaluation of one trial context (-1: not possible)
+  auto trial = [&](const mg_params& p2) -> double {
+    int st = 0;
+    mg_ctx* c = mg_create(top, &p2, &st);
+    if (!c) return -1;
+    double t = -1;
+    int e = mg_forces_device(c, r_dev, f_dev, 0, nullptr);  // warm-up
+    if (!e) {
+      cudaEventRecord(e0, c->stream);
+      for (int k = 0; k < nrep && !e; k++) e = mg_forces_device(c, r_dev, f_dev, 0, nullptr);
+      cudaEventRecord(e1, c->stream);
+      cudaEventSynchronize(e1);
+      float f = 0;
+      cudaEventElapsedTime(&f, e0, e1);
+      if (!e) t = f / nrep;
+    }
+    if (e) rc = e;
+    mg_destroy(c);
+    return t;
+  };
   double best = 1e300;
-  int bc = 0, bk = 0, rc = MG_OK;
+  int bc = 0, bk = 0;
   for (int a = 0; a < 3 && rc == MG_OK; a++)
-    for (int b = 0; b < 3; b++) {
+    for (int b = 0; b < 3 && rc == MG_OK; b++) {
       mg_params p2 = *par;
       p2.cells_per_cutoff = cd[a];
       p2.kspace_ctas_per_sm = kc[b];
-      int st = 0;
-      mg_ctx* c = mg_create(top, &p2, &st);
-      double t = -1;
-      if (c) {
-        int e = mg_forces_device(c, r_dev, f_dev, 0, nullptr);  // warm-up
-        if (!e) {
-          cudaEventRecord(e0, c->stream);
-          for (int k = 0; k < nrep && !e; k++) e = mg_forces_device(c, r_dev, f_dev, 0, nullptr);
-          cudaEventRecord(e1, c->stream);
-          cudaEventSynchronize(e1);
-          float f = 0;
-          cudaEventElapsedTime(&f, e0, e1);
-          if (!e) t = f / nrep;
-        }
-        if (e) rc = e;
-        mg_destroy(c);
-      }
+      const double t = trial(p2);
       if (ms) ms[3 * a + b] = t;
       if (t > 0 && t < best) {
         best = t;
@@ -2794,104 +2799,44 @@ int mg_autotune(const mg_topology* top, mg_params* par, const double* r, int nre
         bk = kc[b];
       }
     }
-  // the pair-kernel variants at the best grid and split
-  int bv = par->pair_variant;
+  // the pair-kernel variants at the best split, each with the Ewald chain
+  // beside the r-space chain and after it (FP32 path): which is faster
+  // depends on how the kernels share the SMs, so the two are chosen together
+  int bv = par->pair_variant, bser = par->kspace_serial;
+  const int nser = par->precision == MG_MIXED ? 2 : 1;
+  double tser[2] = {-1, -1};
   if (!rc && bc) {
     double bestv = 1e300;
-    for (int v = 0; v < 8 && rc == MG_OK; v++) {
-      mg_params p2 = *par;
-      p2.cells_per_cutoff = bc;
-      p2.kspace_ctas_per_sm = bk;
-      p2.pair_variant = v;
-      int st = 0;
-      mg_ctx* c = mg_create(top, &p2, &st);
-      double t = -1;
-      if (c) {
-        int e = mg_forces_device(c, r_dev, f_dev, 0, nullptr);
-        if (!e) {
-          cudaEventRecord(e0, c->stream);
-          for (int k = 0; k < nrep && !e; k++) e = mg_forces_device(c, r_dev, f_dev, 0, nullptr);
-          cudaEventRecord(e1, c->stream);
-          cudaEventSynchronize(e1);
-          float f = 0;
-          cudaEventElapsedTime(&f, e0, e1);
-          if (!e) t = f / nrep;
+    auto consider = [&](int v, int cdv, double* slot) {
+      double tv = -1, ts[2] = {-1, -1};
+      for (int ser = 0; ser < nser && rc == MG_OK; ser++) {
+        mg_params p2 = *par;
+        p2.cells_per_cutoff = cdv;
+        p2.kspace_ctas_per_sm = bk;
+        p2.pair_variant = v;
+        p2.kspace_serial = nser == 2 ? ser : par->kspace_serial;
+        ts[ser] = trial(p2);
+        if (ts[ser] > 0 && (tv < 0 || ts[ser] < tv)) tv = ts[ser];
+        if (ts[ser] > 0 && ts[ser] < bestv) {
+          bestv = ts[ser];
+          bv = v;
+          bc = cdv;
+          bser = p2.kspace_serial;
+          tser[0] = ts[0];
+          tser[1] = ts[1];
         }
-        if (e) rc = e;
-        mg_destroy(c);
       }
-      if (ms) ms[9 + v] = t;
-      if (t > 0 && t < bestv) {
-        bestv = t;
-        bv = v;
-      }
-    }
+      if (slot) *slot = tv;
+    };
+    const int cbest = bc;
+    for (int v = 0; v < 8 && rc == MG_OK; v++) consider(v, cbest, ms ? ms + 9 + v : nullptr);
     // the group pair kernel (variant 8) at every cell subdivision: its
     // pruning favours other cells than the cell kernel does
-    for (int a = 0; a < 3 && rc == MG_OK; a++) {
-      mg_params p2 = *par;
-      p2.cells_per_cutoff = cd[a];
-      p2.kspace_ctas_per_sm = bk;
-      p2.pair_variant = 8;
-      int st = 0;
-      mg_ctx* c = mg_create(top, &p2, &st);
-      double t = -1;
-      if (c) {
-        int e = mg_forces_device(c, r_dev, f_dev, 0, nullptr);
-        if (!e) {
-          cudaEventRecord(e0, c->stream);
-          for (int k = 0; k < nrep && !e; k++) e = mg_forces_device(c, r_dev, f_dev, 0, nullptr);
-          cudaEventRecord(e1, c->stream);
-          cudaEventSynchronize(e1);
-          float f = 0;
-          cudaEventElapsedTime(&f, e0, e1);
-          if (!e) t = f / nrep;
-        }
-        if (e) rc = e;
-        mg_destroy(c);
-      }
-      if (ms) ms[17 + a] = t;
-      if (t > 0 && t < bestv) {
-        bestv = t;
-        bv = 8;
-        bc = cd[a];
-      }
-    }
+    for (int a = 0; a < 3 && rc == MG_OK; a++) consider(8, cd[a], ms ? ms + 17 + a : nullptr);
   }
-  // the Ewald chain beside the r-space chain or after it: which is faster
-  // depends on how the two kernels share the SMs
-  int bser = par->kspace_serial;
-  if (!rc && bc && par->precision == MG_MIXED) {
-    double bests = 1e300;
-    for (int ser = 0; ser < 2 && rc == MG_OK; ser++) {
-      mg_params p2 = *par;
-      p2.cells_per_cutoff = bc;
-      p2.kspace_ctas_per_sm = bk;
-      p2.pair_variant = bv;
-      p2.kspace_serial = ser;
-      int st = 0;
-      mg_ctx* c = mg_create(top, &p2, &st);
-      double t = -1;
-      if (c) {
-        int e = mg_forces_device(c, r_dev, f_dev, 0, nullptr);
-        if (!e) {
-          cudaEventRecord(e0, c->stream);
-          for (int k = 0; k < nrep && !e; k++) e = mg_forces_device(c, r_dev, f_dev, 0, nullptr);
-          cudaEventRecord(e1, c->stream);
-          cudaEventSynchronize(e1);
-          float f = 0;
-          cudaEventElapsedTime(&f, e0, e1);
-          if (!e) t = f / nrep;
-        }
-        if (e) rc = e;
-        mg_destroy(c);
-      }
-      if (ms) ms[20 + ser] = t;
-      if (t > 0 && t < bests) {
-        bests = t;
-        bser = ser;
-      }
-    }
+  if (ms) {
+    ms[20] = tser[0];
+    ms[21] = tser[1];
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

@@ -73,6 +73,16 @@ constexpr int KTR = 64;         // rows per k-space tile
 constexpr int KZC_MIXED = 32;
 inline int phase_row_mixed(int Kx, int Ky, int Kz) { return (Kx + 1) + (2 * Ky + 1) + (Kz + 1); }
 
+// The body of a kernel that has a single-box launch and a batched launch
+// (blockIdx.y = box): compiled once, not inlined, so that both launches run
+// the same machine code.  Inlined into two kernels, the compiler may fuse a
+// multiply and an add into an FMA in one and not in the other, and a box of
+// a batch would no longer get its single-launch results bit for bit.  It
+// runs once per CTA, so the call costs nothing measurable.
+#ifdef __CUDACC__
+#define MG_BODY __device__ __noinline__
+#endif
+
 constexpr int KZT = 4;          // kz per pass-1 thread
 constexpr int PAIR_THREADS = 128;
 constexpr int MAX_KINDS = 16;

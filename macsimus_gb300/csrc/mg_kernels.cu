@@ -53,16 +53,16 @@ static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 // kernels use agree to the last bit); a non-finite coordinate sets bit 1 of
 // *status and the site is binned into cell 0 so that every later index
 // stays in range
-__global__ void cell_count_kernel(int ns, const double* __restrict__ r, double iLx, double iLy,
-                                  double iLz, int ncx, int ncy, int ncz,
-                                  const int* __restrict__ kind, const int* __restrict__ mol,
-                                  int4* __restrict__ pfix, int* __restrict__ key,
-                                  int* __restrict__ count, int* __restrict__ status) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+MG_BODY void cell_count_kernel_body(int ns, const double* __restrict__ r, const double* iL,
+                                   int ncx, int ncy, int ncz, const int* __restrict__ kind,
+                                   const int* __restrict__ mol, int4* __restrict__ pfix,
+                                   int* __restrict__ key, int* __restrict__ count,
+                                   int* __restrict__ status, const int bx_) {
+  const int i = bx_ * blockDim.x + threadIdx.x;
   if (i >= ns) return;
   const double x = r[3 * i], y = r[3 * i + 1], z = r[3 * i + 2];
   int k = 0;
-  const int4 q = make_int4(fixed32(x, iLx), fixed32(y, iLy), fixed32(z, iLz),
+  const int4 q = make_int4(fixed32(x, iL[0]), fixed32(y, iL[1]), fixed32(z, iL[2]),
                            (mol[i] << 8) | kind[i]);
   if (isfinite(x) && isfinite(y) && isfinite(z)) {
     k = (fixed_cell(q.x, ncx) * ncy + fixed_cell(q.y, ncy)) * ncz + fixed_cell(q.z, ncz);
@@ -72,6 +72,19 @@ __global__ void cell_count_kernel(int ns, const double* __restrict__ r, double i
   pfix[i] = q;
   key[i] = k;
   atomicAdd(count + k, 1);
+}
+
+struct Inv3 {
+  double v[3];
+};
+
+__global__ void cell_count_kernel(int ns, const double* __restrict__ r, const __grid_constant__ Inv3 iL, int ncx,
+                                  int ncy, int ncz, const int* __restrict__ kind,
+                                  const int* __restrict__ mol, int4* __restrict__ pfix,
+                                  int* __restrict__ key, int* __restrict__ count,
+                                  int* __restrict__ status) {
+  cell_count_kernel_body(ns, r, iL.v, ncx, ncy, ncz, kind, mol, pfix, key, count, status,
+                         blockIdx.x);
 }
 
 // exclusive scan of count[0..ncell) into start[0..ncell] and cursor[], in
@@ -86,7 +99,7 @@ __device__ __forceinline__ int2 shfl_up2(int2 v, int o) {
 }
 __device__ __forceinline__ int ngroups(int n) { return (n + GROUP_SITES - 1) / GROUP_SITES; }
 
-__device__ __forceinline__ void cell_scan_kernel_body(int ncell,
+MG_BODY void cell_scan_kernel_body(int ncell,
     int* __restrict__ count,
     int* __restrict__ start,
     int* __restrict__ cursor,
@@ -166,7 +179,7 @@ __global__ void cell_scatter_kernel(int ns, const int* __restrict__ key, int* __
 }
 
 constexpr int ORDER_THREADS = 256;
-__device__ __forceinline__ void cell_order_kernel_body(int ncell,
+MG_BODY void cell_order_kernel_body(int ncell,
     const int* __restrict__ start,
     const int* __restrict__ slot_site,
     const int4* __restrict__ pfix,
@@ -229,8 +242,9 @@ cudaError_t k_cell_list(const Launch& L, int ns, const double* r, int* status, c
                         int* key, int* count, int* cursor, int* slot_site, int* order,
                         int* key_s, int* start, int* gstart, int4* pj, int* gcell) {
   const int ncell = ncx * ncy * ncz;
-  cell_count_kernel<<<cdiv(ns, 256), 256, 0, L.s>>>(ns, r, iL[0], iL[1], iL[2], ncx, ncy, ncz,
-                                                    kind, mol, pfix, key, count, status);
+  const Inv3 il{{iL[0], iL[1], iL[2]}};
+  cell_count_kernel<<<cdiv(ns, 256), 256, 0, L.s>>>(ns, r, il, ncx, ncy, ncz, kind, mol, pfix, key,
+                                                    count, status);
   LAUNCHED(L);
   cell_scan_kernel<<<1, SCAN_THREADS, 0, L.s>>>(ncell, count, start, cursor, gstart);
   LAUNCHED(L);
@@ -312,7 +326,7 @@ constexpr int FOLD = 8;   // stencil cells per FP32 force batch before the FP64 
 // (Knuth's TwoSum): no FP64 instruction in the loop (the FP64 pipe of this
 // GPU is narrow and also serves the float/double conversions).
 template <bool MEASURE, bool POLAR, bool REL, int NW, bool STAB>
-__device__ __forceinline__ void pair_mixed_kernel_body(const PairArgs& a,
+MG_BODY void pair_mixed_kernel_body(const PairArgs& a,
     const int4* __restrict__ pj,
     const PairF* __restrict__ ptab_g,
     const float4* __restrict__ erd_g,
@@ -1007,7 +1021,7 @@ __device__ __forceinline__ double near_img(double d, double L, double iL) {
 }
 
 template <bool MEASURE, bool POLAR>
-__device__ __forceinline__ void excl_mixed_kernel_body(const ExclArgs& a,
+MG_BODY void excl_mixed_kernel_body(const ExclArgs& a,
     const int bx_,
     const int by_) {
   __shared__ double red[EXCL_THREADS];
@@ -1134,7 +1148,7 @@ cudaError_t k_add_forces(const Launch& L, size_t n, const double* fk, double* f)
 }
 
 // fixed-point coordinates of every charge (Drude charges at r + rpol)
-__device__ __forceinline__ void charge_fixed_kernel_body(const KArgs& a,
+MG_BODY void charge_fixed_kernel_body(const KArgs& a,
     const double* __restrict__ r,
     uint4* __restrict__ qf,
     const int bx_,
@@ -1156,7 +1170,7 @@ __global__ void charge_fixed_kernel(const __grid_constant__ KArgs a, const doubl
   charge_fixed_kernel_body(a, r, qf, blockIdx.x, 0);
 }
 
-__device__ __forceinline__ void phase_tables_mixed_kernel_body(const KArgs& a,
+MG_BODY void phase_tables_mixed_kernel_body(const KArgs& a,
     const uint4* __restrict__ qf,
     float2* __restrict__ tab,
     const int bx_,
@@ -1318,7 +1332,7 @@ cudaError_t k_sk_fp64(const Launch& L, const KArgs& a, const double2* tab, doubl
 // S(k) = sum over chunks (FP64, fixed order); energy and virial per k
 // (sim/ewpass2m.c: E1 = |S|^2 ekk, ptf = 1/kk + (pi/alpha)^2) reduced per block
 template <typename T2>
-__device__ __forceinline__ void sk_reduce_kernel_body(const KArgs& a,
+MG_BODY void sk_reduce_kernel_body(const KArgs& a,
     const T2* __restrict__ part,
     bool measure,
     double pi2_over_a2,
@@ -1445,7 +1459,7 @@ cudaError_t k_kforce_fp64(const Launch& L, const KArgs& a, const double2* tab) {
 }
 
 // out[k] = sum over rows of part[row*width+k], fixed order (one CTA)
-__device__ __forceinline__ void reduce_rows_kernel_body(const double* __restrict__ part,
+MG_BODY void reduce_rows_kernel_body(const double* __restrict__ part,
     int nrows,
     int width,
     double* __restrict__ out,
@@ -1579,7 +1593,7 @@ __device__ __forceinline__ void meas_kin(ShakeMeas& m, double mi, double v1x, do
 }
 
 template <bool NOSE, bool MEAS>
-__device__ __forceinline__ void shake_kernel_body(const ShakeArgs& a,
+MG_BODY void shake_kernel_body(const ShakeArgs& a,
     const int bx_,
     const int by_) {
   __shared__ double red[SH_THREADS];
@@ -1857,21 +1871,8 @@ int cell_order_blocks(int ncell) { return cdiv(ncell, ORDER_THREADS / 32); }
 
 __global__ void batch_cell_count_kernel(const BoxStep* __restrict__ B) {
   const BoxStep& e = B[blockIdx.y];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= e.ns) return;
-  const double x = e.r[3 * i], y = e.r[3 * i + 1], z = e.r[3 * i + 2];
-  int k = 0;
-  const int4 q = make_int4(fixed32(x, e.iL[0]), fixed32(y, e.iL[1]), fixed32(z, e.iL[2]),
-                           (e.mol[i] << 8) | e.kind[i]);
-  if (isfinite(x) && isfinite(y) && isfinite(z)) {
-    k = (fixed_cell(q.x, e.ncx) * e.ncy + fixed_cell(q.y, e.ncy)) * e.ncz +
-        fixed_cell(q.z, e.ncz);
-  } else {
-    atomicOr(e.status, 2);
-  }
-  e.pfix[i] = q;
-  e.key[i] = k;
-  atomicAdd(e.count + k, 1);
+  cell_count_kernel_body(e.ns, e.r, e.iL, e.ncx, e.ncy, e.ncz, e.kind, e.mol, e.pfix, e.key,
+                         e.count, e.status, blockIdx.x);
 }
 
 __global__ void __launch_bounds__(SCAN_THREADS) batch_cell_scan_kernel(const BoxStep* __restrict__ B) {

@@ -290,7 +290,7 @@ __device__ __forceinline__ void sk_gemm_mixed_body(const KArgs& a, const float2*
   }
 }
 
-__device__ __forceinline__ void sk_gemm_mixed_kernel_body(const KArgs& a,
+MG_BODY void sk_gemm_mixed_kernel_body(const KArgs& a,
     const float2* __restrict__ tab,
     float2* __restrict__ part,
     const int bx_,
@@ -482,7 +482,7 @@ size_t kf_mixed_smem(const KArgs& a) {
   return sizeof(float2) * ((size_t)nz * Q2_NJ + (size_t)Q2_NJ * nxy + 2 * (size_t)nw * KTR);
 }
 
-__device__ __forceinline__ void kf_gemm_mixed_kernel_body(const KArgs& a,
+MG_BODY void kf_gemm_mixed_kernel_body(const KArgs& a,
     const float2* __restrict__ tab,
     const float2* __restrict__ W,
     const int bx_,

@@ -26,6 +26,11 @@ def test_autotune_choice_and_forces(precision):
         # the group kernel: its fastest subdivision
         mg = best["ms_group"]
         assert mg[best["cells_per_cutoff"] - 1] == mg[mg > 0].min()
+    if precision == "mixed":
+        # the Ewald chain beside or after the r-space chain, chosen with the variant
+        assert best["kspace_serial"] in (0, 1)
+        s = best["ms_serial"]
+        assert s[best["kspace_serial"]] == s[s > 0].min()
     f0, _ = M.ForcePath(*args, precision=precision).forces(g["r"][0])
     assert best["pair_variant"] in range(9)
     f1, _ = M.ForcePath(*args, precision=precision, cells_per_cutoff=best["cells_per_cutoff"],
