@@ -281,9 +281,10 @@ def run_ours(args, rank, world, local):
     name, (kms, kcnt) = top
     kavg = kms / max(kcnt, 1)
     achieved = algo.get(name, 0) / (kavg * 1e-3) / 1e12 if kavg > 0 else 0.0
-    # the pair step's kernel: the group kernel (pair_variant 8) or the cell kernel
-    if name == "pair_mixed" and tuned.get("pair_variant", 0) == 8:
-        name = "pair_group"
+    # the pair step's kernel: the group kernel (pair_variant 8), its half-shell
+    # form (9) or the cell kernel
+    if name == "pair_mixed" and tuned.get("pair_variant", 0) in (8, 9):
+        name = "pair_group" if tuned["pair_variant"] == 8 else "pair_half"
         algo[name] = algo["pair_mixed"]
         achieved = algo[name] / (kavg * 1e-3) / 1e12 if kavg > 0 else 0.0
     traffic = None

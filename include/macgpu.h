@@ -118,6 +118,10 @@ typedef struct {
   /* FP32 pair kernel: 8 = the group kernel (a warp per group of 8 home
      sites; neighbours pruned against the group's bounding box; needs a grid
      of at least 2 cdiv + 1 cells per edge, else the cell kernel runs);
+     9 = the group kernel with Newton's third law (every pair once, over a
+     half-shell stencil; forces summed in 64-bit fixed point, 2^-32 K/A,
+     by integer atomics, so still reproducible bit for bit; Drude builds run
+     variant 8 instead);
      otherwise the cell kernel with bit 0 = 8 warps per home cell (else 4),
      bit 2 = 16 warps per home cell (over bit 0), bit 1 = the erfc force
      spline in shared memory (else read through L1).  mg_autotune picks it. */
@@ -379,14 +383,16 @@ int mg_xwidom(mg_ctx *ctx, int nlist, const int *mols, const int *vtype, const d
    r for every cell subdivision (cells_per_cutoff 1..3) and Ewald pass-1
    split (kspace_ctas_per_sm 6, 10, 16) and writes the fastest pair into
    *par, then the fastest of the 8 cell-kernel pair_variant values at that
-   choice and of the group kernel (pair_variant 8) at every subdivision,
-   each timed (FP32 path) with kspace_serial 0 and 1, the pair chosen
-   together.  Builds and frees its own trial contexts; ms[22] (optional)
-   gets the time per evaluation of each trial (cdiv-major, then the 8
-   cell-kernel variants and the group kernel at cdiv 1..3, the faster of
-   the two kspace_serial settings each, then the chosen variant with
-   kspace_serial 0 and 1; -1 if that grid is not possible or the trial did
-   not run). */
+   choice, of the group kernel (pair_variant 8) at every subdivision and,
+   on the FP32 path without Drude shells, of its half-shell form
+   (pair_variant 9) at every subdivision, each timed (FP32 path) with
+   kspace_serial 0 and 1, the pair chosen together.  Builds and frees its
+   own trial contexts; ms[25] (optional) gets the time per evaluation of
+   each trial (cdiv-major, then the 8 cell-kernel variants, the group
+   kernel at cdiv 1..3 and the half-shell group kernel at cdiv 1..3, the
+   faster of the two kspace_serial settings each, then the chosen variant
+   with kspace_serial 0 and 1; -1 if that grid is not possible or the trial
+   did not run). */
 int mg_autotune(const mg_topology *top, mg_params *par, const double *r, int nrep, double *ms);
 
 /* ---- adjoint ----

@@ -63,6 +63,11 @@ struct mg_ctx {
   // group, its grid; nprows = energy rows of the pair kernel (cell or group)
   int4* d_spans = nullptr;
   int nspans = 0, ngroup_grid = 0, nprows = 0;
+  // its half-shell form (pair_variant 9): the half stencil as z-runs and the
+  // 64-bit fixed-point force sums (sorted order, zero between evaluations)
+  int4* d_hspans = nullptr;
+  int nhspans = 0;
+  long long* d_facc = nullptr;
   int *d_gstart = nullptr, *d_gcell = nullptr;
   PairF* d_ptabf = nullptr;
   PairD* d_ptabd = nullptr;
@@ -331,6 +336,8 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   ctx->minqq = p->minqq > 0 ? p->minqq : 1.0;
   ctx->use_list = p->skin > 0;
   ctx->pair_variant = p->pair_variant;
+  if (ctx->pair_variant < 0 || ctx->pair_variant > 9)
+    return fail(ctx, MG_ERR_ARG, "pair_variant must be 0..9");
   ctx->thermostat = p->thermostat;
   if (ctx->thermostat < 0 || ctx->thermostat > 3)
     return fail(ctx, MG_ERR_ARG, "thermostat: 0 none, 1 Berendsen, 2 Bussi, 3 Nose-Hoover");
@@ -498,6 +505,17 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
     k = e;
   }
   ctx->nspans = (int)spans.size();
+  // the half shell: columns with dx > 0, or dx = 0 and dy > 0, whole; the
+  // column (0, 0) from the home cell up (dz >= 0)
+  std::vector<int4> hspans;
+  for (const int4& sp : spans) {
+    if (sp.x > 0 || (sp.x == 0 && sp.y > 0)) {
+      hspans.push_back(sp);
+    } else if (sp.x == 0 && sp.y == 0 && sp.w >= 0) {
+      hspans.push_back(make_int4(0, 0, std::max(sp.z, 0), sp.w));
+    }
+  }
+  ctx->nhspans = (int)hspans.size();
   // work items of the group kernel: at most ns / GROUP_SITES + ncell
   ctx->ngroup_grid = (int)(((long)ns / GROUP_SITES + ctx->ncell + GROUP_WARPS) / GROUP_WARPS);
   ctx->nprows = std::max(ctx->ncell, ctx->ngroup_grid);
@@ -653,6 +671,11 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   }
   CK(upload(&ctx->d_stencil, st.data(), st.size()));
   CK(upload(&ctx->d_spans, spans.data(), spans.size()));
+  CK(upload(&ctx->d_hspans, hspans.data(), hspans.size()));
+  if (ctx->pair_variant == 9) {
+    CK(dalloc(&ctx->d_facc, 3 * (size_t)ns));
+    CK(cudaMemset(ctx->d_facc, 0, 3 * (size_t)ns * sizeof(long long)));
+  }
   CK(dalloc(&ctx->d_gstart, (size_t)ctx->ncell + 1));
   CK(dalloc(&ctx->d_gcell, (size_t)ns / GROUP_SITES + ctx->ncell + 1));
   ctx->nxblocks = (t->nmol + EXCL_THREADS - 1) / EXCL_THREADS;
@@ -996,6 +1019,10 @@ PairArgs make_pair_args(mg_ctx* ctx, double* f_dev) {
   pa.pair_warps = (ctx->pair_variant & 4) ? 16 : ((ctx->pair_variant & 1) ? 8 : 4);
   pa.spline_smem = (ctx->pair_variant & 2) && ctx->ntab * 16 <= 200 * 1024 ? 1 : 0;
   pa.group = (ctx->pair_variant & 8) ? 1 : 0;
+  pa.newton = ctx->pair_variant == 9 ? 1 : 0;
+  pa.hspans = ctx->d_hspans;
+  pa.nhspans = ctx->nhspans;
+  pa.facc = ctx->d_facc;
   pa.gstart = ctx->d_gstart;
   pa.gcell = ctx->d_gcell;
   pa.spans = ctx->d_spans;
@@ -1500,6 +1527,7 @@ int mg_destroy(mg_ctx* ctx) {
   void* bufs[] = {ctx->d_rs, ctx->d_fs, ctx->d_r,      ctx->d_f,       ctx->d_r1,    ctx->d_p,      ctx->d_kind,
                   ctx->d_mol,    ctx->d_key,     ctx->d_pfix,   ctx->d_idx,   ctx->d_key_s,  ctx->d_order,
                   ctx->d_cell_start, ctx->d_ccount, ctx->d_ccursor, ctx->d_spans, ctx->d_gstart,
+                  ctx->d_hspans, ctx->d_facc,
                   ctx->d_gcell, ctx->d_pj, ctx->d_pd,  ctx->d_stencil,
                   ctx->d_ptabf,  ctx->d_ptabd,   ctx->d_erd,   ctx->d_eru,    ctx->d_ert,
                   ctx->d_epart,  ctx->d_qsite,   ctx->d_qval,  ctx->d_task,   ctx->d_col,
@@ -2833,10 +2861,13 @@ int mg_autotune(const mg_topology* top, mg_params* par, const double* r, int nre
     // the group pair kernel (variant 8) at every cell subdivision: its
     // pruning favours other cells than the cell kernel does
     for (int a = 0; a < 3 && rc == MG_OK; a++) consider(8, cd[a], ms ? ms + 17 + a : nullptr);
+    // and its half-shell form (Newton's third law; FP32 path without Drude shells)
+    if (par->precision == MG_MIXED && !polar)
+      for (int a = 0; a < 3 && rc == MG_OK; a++) consider(9, cd[a], ms ? ms + 20 + a : nullptr);
   }
   if (ms) {
-    ms[20] = tser[0];
-    ms[21] = tser[1];
+    ms[23] = tser[0];
+    ms[24] = tser[1];
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

@@ -147,6 +147,13 @@ struct PairArgs {
   const int4* spans;
   int nspans;
   int ngrid;                // CTAs of the group kernel (its energy rows)
+  // the group kernel with Newton's third law (pair_variant 9, no Drude
+  // shells): the half-shell z-runs, and the 64-bit fixed-point force sums
+  // (2^-32 K/A units, sorted order, kept zero between evaluations)
+  int newton;
+  const int4* hspans;
+  int nhspans;
+  long long* facc;
 };
 cudaError_t k_pair_mixed(const Launch& L, const PairArgs& a, const int4* pj,
                          const PairF* ptab, const float4* erd, const float4* eru,

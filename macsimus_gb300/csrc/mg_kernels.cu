@@ -772,6 +772,221 @@ __global__ void __launch_bounds__(NW * 32)
   }
 }
 
+// ------------------------------------------- group kernel, half shell --
+//
+// Newton's third law in the group kernel (pair_variant 9, no Drude shells):
+// every unordered pair once.  The stencil is the half shell: the z-runs of
+// the columns with dx > 0, or dx = 0 and dy > 0, whole, and the column
+// (0, 0) from the home cell up; inside the home cell a pair is taken from
+// its site with the lower sorted index (the grid has at least 2 cdiv + 1
+// cells per edge, so no cell reaches another by two stencil offsets and no
+// pair is found twice).  The pair terms are the group kernel's.  Forces go
+// into 64-bit fixed-point sums (FIX_SCALE units per K/A) in sorted order by
+// integer atomics; integer addition does not depend on the order, so the
+// forces come out the same bit for bit on every run.  The neighbour's force
+// of an iteration is summed over the 8 home lanes by a reduce-scatter (three
+// shuffle levels: lanes i = 0, 2, 4 end with x, y, z), scaled by 2^32 in
+// FP32 (exact) and added with one atomic per component; the home sites' own
+// compensated sums once per group.
+// finish_forces_kernel turns the sums into the FP64 forces (site order) and
+// clears them for the next evaluation.
+constexpr double FIX_SCALE = 4294967296.0;  // 2^32: |F| < 2^31 K/A, steps of 2.3e-10 K/A
+
+template <bool MEASURE, int NW>
+__global__ void __launch_bounds__(NW * 32)
+    pair_half_mixed_kernel(PairArgs a, const int4* __restrict__ pj,
+                           const PairF* __restrict__ ptab_g, const float4* __restrict__ erd,
+                           const float4* __restrict__ eru, float sx, float sy, float sz, float cq,
+                           float sgrid) {
+  constexpr int NT = NW * 32;
+  extern __shared__ float4 dyn_smem[];   // the nk x nk FP32 pair table
+  __shared__ float4 sj[NW][32];
+  __shared__ int sjt[NW][32];
+  __shared__ double ered[NT];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int il = lane & 7, sl = lane >> 3;
+  const int nk = a.nkind, ntab = a.ntab;
+  PairFS* ptab = reinterpret_cast<PairFS*>(dyn_smem);
+  for (int t = threadIdx.x; t < 3 * nk * nk; t += NT)
+    dyn_smem[t] = reinterpret_cast<const float4*>(ptab_g + t / 3)[t % 3];
+  __syncthreads();
+  const int ncell = a.ncx * a.ncy * a.ncz;
+  const int nitems = a.gstart[ncell];
+  unsigned long long* facc = reinterpret_cast<unsigned long long*>(a.facc);
+  // reduce-scatter roles: after the three levels lane i holds component
+  // i >> 1 (0 x, 1 y, 2 z, 3 nothing); lanes i = 0, 2, 4 write it
+  const bool b2 = (il & 4) != 0, b1 = (il & 2) != 0;
+  const int comp = il >> 1;
+  const bool jw = !(il & 1) && comp < 3;
+  CSum es[9];
+
+  for (int item = blockIdx.x * NW + warp; item < nitems; item += gridDim.x * NW) {
+    const int c = a.gcell[item];
+    const int cz = c % a.ncz, cy = (c / a.ncz) % a.ncy, cx = c / (a.ncy * a.ncz);
+    const int hs = a.cell_start[c], he = a.cell_start[c + 1];
+    const int i0 = hs + GROUP_SITES * (item - a.gstart[c]);
+    const int ni = min(GROUP_SITES, he - i0);
+    const unsigned refx = (unsigned)((((unsigned long long)(2 * cx + 1)) << 31) / a.ncx),
+                   refy = (unsigned)((((unsigned long long)(2 * cy + 1)) << 31) / a.ncy),
+                   refz = (unsigned)((((unsigned long long)(2 * cz + 1)) << 31) / a.ncz);
+    const bool vi = il < ni;
+    const int ti = i0 + il;
+    const int4 me = vi ? pj[ti] : make_int4(0, 0, 0, 0);
+    const int kind_i = me.w & 255, mol_i = me.w >> 8;
+    const float xi = (float)(int)((unsigned)me.x - refx) * sx,
+                yi = (float)(int)((unsigned)me.y - refy) * sy,
+                zi = (float)(int)((unsigned)me.z - refz) * sz;
+    float blx = vi ? xi : 3e38f, bly = vi ? yi : 3e38f, blz = vi ? zi : 3e38f;
+    float bhx = vi ? xi : -3e38f, bhy = vi ? yi : -3e38f, bhz = vi ? zi : -3e38f;
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+      blx = fminf(blx, __shfl_xor_sync(0xffffffffu, blx, o));
+      bly = fminf(bly, __shfl_xor_sync(0xffffffffu, bly, o));
+      blz = fminf(blz, __shfl_xor_sync(0xffffffffu, blz, o));
+      bhx = fmaxf(bhx, __shfl_xor_sync(0xffffffffu, bhx, o));
+      bhy = fmaxf(bhy, __shfl_xor_sync(0xffffffffu, bhy, o));
+      bhz = fmaxf(bhz, __shfl_xor_sync(0xffffffffu, bhz, o));
+    }
+    CSum fx, fy, fz;
+    for (int sp = 0; sp < a.nhspans; sp++) {
+      const int4 o = a.hspans[sp];
+      int x2 = cx + o.x, y2 = cy + o.y;
+      x2 += (x2 < 0) ? a.ncx : (x2 >= a.ncx ? -a.ncx : 0);
+      y2 += (y2 < 0) ? a.ncy : (y2 >= a.ncy ? -a.ncy : 0);
+      const int col = (x2 * a.ncy + y2) * a.ncz;
+      int za = cz + o.z, zb = cz + o.w;
+      if (zb < 0) { za += a.ncz; zb += a.ncz; }
+      if (za >= a.ncz) { za -= a.ncz; zb -= a.ncz; }
+      int ra0, ra1, rb0 = 0, rb1 = -1;
+      if (za < 0) { ra0 = za + a.ncz; ra1 = a.ncz - 1; rb0 = 0; rb1 = zb; }
+      else if (zb >= a.ncz) { ra0 = za; ra1 = a.ncz - 1; rb0 = 0; rb1 = zb - a.ncz; }
+      else { ra0 = za; ra1 = zb; }
+      float ax = 0, ay = 0, az = 0;
+      float e_el = 0, e_lj = 0, e_vir = 0;
+      PvF pv;
+      pv.zero();
+      for (int part = 0; part < 2; part++) {
+        const int z0 = part ? rb0 : ra0, z1 = part ? rb1 : ra1;
+        if (z1 < z0) continue;
+        // home-cell sites before the group pair with it from their own group
+        const int j0 = max(a.cell_start[col + z0], col + z0 == c ? i0 : 0),
+                  j1 = a.cell_start[col + z1 + 1];
+        for (int jb = j0; jb < j1; jb += 32) {
+          const int j = jb + lane;
+          bool keep = false;
+          float4 f4 = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (j < j1) {
+            const int4 q = pj[j];
+            f4 = make_float4((float)(int)((unsigned)q.x - refx) * sx,
+                             (float)(int)((unsigned)q.y - refy) * sy,
+                             (float)(int)((unsigned)q.z - refz) * sz, __int_as_float(q.w));
+            const float ddx = fmaxf(fmaxf(blx - f4.x, f4.x - bhx), 0.f),
+                        ddy = fmaxf(fmaxf(bly - f4.y, f4.y - bhy), 0.f),
+                        ddz = fmaxf(fmaxf(blz - f4.z, f4.z - bhz), 0.f);
+            keep = fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz)) < cq;
+          }
+          const unsigned M = __ballot_sync(0xffffffffu, keep);
+          if (keep) {
+            const int slot = __popc(M & ((1u << lane) - 1u));
+            sj[warp][slot] = f4;
+            sjt[warp][slot] = j;
+          }
+          __syncwarp();
+          const int n = __popc(M);
+          // the whole warp iterates: the reduce-scatter needs every lane
+          for (int t0 = 0; t0 < n; t0 += 4) {
+            const int t = t0 + sl;
+            const bool vt = t < n;
+            const float4 q = sj[warp][vt ? t : 0];
+            const int tj = sjt[warp][vt ? t : 0];
+            const float dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
+            const float rr = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const int qw = __float_as_int(q.w);
+            const bool ok = vt && vi && rr < cq && (qw >> 8) != mol_i &&
+                            (tj > ti || tj >= he || tj < hs);
+            const PairFS P = ptab[kind_i * nk + (qw & 255)];
+            const float x = __fdividef(P.Sq, rr), y = x * x * x, xt = rr - P.C2q;
+            const bool core = rr < P.C1q, tail = rr < P.C2q;
+            const float flj = core ? P.E24 * fmaf(2.f * y, y, -y) * x : (tail ? P.A4 * xt : 0.f);
+            float e_el_p = 0.f;
+            float f = flj + spline_any<MEASURE, true>(erd, eru, rr, sgrid, ntab, P.qq, e_el_p);
+            f = ok ? f : 0.f;
+            // the products rounded once and used for both sites (no
+            // contraction into an FMA on one side only)
+            const float px = __fmul_rn(f, dx), py = __fmul_rn(f, dy), pz = __fmul_rn(f, dz);
+            ax = __fadd_rn(ax, px);
+            ay = __fadd_rn(ay, py);
+            az = __fadd_rn(az, pz);
+            if (MEASURE && ok) {
+              e_lj += core ? P.E4 * fmaf(y, y, -y) : (tail ? P.A * xt * xt : 0.f);
+              e_vir += rr * flj;
+              e_el += e_el_p;
+              pv.add(dx, dy, dz, f);
+            }
+            // the neighbour's force, minus the sum over the 8 home lanes
+            float k0 = b2 ? pz : px, k1 = b2 ? 0.f : py;
+            const float s0 = b2 ? px : pz, s1 = b2 ? py : 0.f;
+            k0 += __shfl_xor_sync(0xffffffffu, s0, 4);
+            k1 += __shfl_xor_sync(0xffffffffu, s1, 4);
+            float k = b1 ? k1 : k0;
+            k += __shfl_xor_sync(0xffffffffu, b1 ? k0 : k1, 2);
+            k += __shfl_xor_sync(0xffffffffu, k, 1);
+            if (jw && vt)
+              atomicAdd(facc + 3 * (long)tj + comp,
+                        (unsigned long long)__float2ll_rn(k * -(float)FIX_SCALE));
+          }
+          __syncwarp();
+        }
+      }
+      fx.add(ax); fy.add(ay); fz.add(az);
+      if (MEASURE) {
+        es[0].add(e_el); es[1].add(e_lj); es[2].add(e_vir);
+        es[3].add(pv.p0); es[4].add(pv.p1); es[5].add(pv.p2);
+        es[6].add(pv.p3); es[7].add(pv.p4); es[8].add(pv.p5);
+      }
+    }
+    // the home sites' sums: the four s-lanes in a fixed order, then lane
+    // s = 0, 1, 2 adds component x, y, z
+    double g[3] = {fx.value(), fy.value(), fz.value()};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      g[k] += __shfl_xor_sync(0xffffffffu, g[k], 8);
+      g[k] += __shfl_xor_sync(0xffffffffu, g[k], 16);
+    }
+    if (vi && sl < 3)
+      atomicAdd(facc + 3 * (long)ti + sl,
+                (unsigned long long)__double2ll_rn((sl == 0 ? g[0] : (sl == 1 ? g[1] : g[2])) *
+                                                   FIX_SCALE));
+  }
+  if (MEASURE) {
+    // every unordered pair once; one row per CTA
+    for (int k = 0; k < 9; k++) {
+      ered[threadIdx.x] = es[k].value();
+      __syncthreads();
+      for (int w = NT / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) ered[threadIdx.x] += ered[threadIdx.x + w];
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) a.epart[blockIdx.x * NEN + k] = ered[0];
+      __syncthreads();
+    }
+  }
+}
+
+// the fixed-point sums (sorted order) into the FP64 forces (site order);
+// the sums are cleared for the next evaluation
+__global__ void finish_forces_kernel(int ns, const int* __restrict__ order,
+                                     long long* __restrict__ facc, double* __restrict__ f) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ns) return;
+  const int site = order[t];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    f[3 * (long)site + d] = (double)facc[3 * (long)t + d] * (1.0 / FIX_SCALE);
+    facc[3 * (long)t + d] = 0;
+  }
+}
+
 cudaError_t k_pair_mixed(const Launch& L, const PairArgs& a, const int4* pj, const PairF* ptab,
                          const float4* erd, const float4* eru, bool measure, bool polar) {
   int ncell = a.ncx * a.ncy * a.ncz;
@@ -779,6 +994,26 @@ cudaError_t k_pair_mixed(const Launch& L, const PairArgs& a, const int4* pj, con
         sz = (float)(a.Lz / 4294967296.0);
   const float cq = (float)a.cutoff_sq, sg = (float)a.sgrid, al = (float)a.alpha;
   const bool rel = !a.allpairs;
+  if (a.group && a.newton && rel && !polar) {
+    const size_t gsm = sizeof(PairFS) * (size_t)a.nkind * a.nkind;
+    cudaError_t ge = cudaSuccess;
+#define PAIR_HALF(M)                                                                            \
+  do {                                                                                          \
+    if (gsm > 48 * 1024)                                                                        \
+      ge = cudaFuncSetAttribute(pair_half_mixed_kernel<M, GROUP_WARPS>,                        \
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm);         \
+    if (ge == cudaSuccess)                                                                      \
+      pair_half_mixed_kernel<M, GROUP_WARPS><<<a.ngrid, GROUP_WARPS * 32, gsm, L.s>>>(         \
+          a, pj, ptab, erd, eru, sx, sy, sz, cq, sg);                                           \
+  } while (0)
+    if (measure) PAIR_HALF(true); else PAIR_HALF(false);
+#undef PAIR_HALF
+    if (ge != cudaSuccess) return ge;
+    LAUNCHED(L);
+    finish_forces_kernel<<<cdiv(a.ns, 256), 256, 0, L.s>>>(a.ns, a.order, a.facc, a.f);
+    LAUNCHED(L);
+    return cudaGetLastError();
+  }
   if (a.group && rel) {
     const size_t gsm = sizeof(PairFS) * (size_t)a.nkind * a.nkind;
     cudaError_t ge = cudaSuccess;

@@ -18,21 +18,23 @@ def test_autotune_choice_and_forces(precision):
     assert best["kspace_ctas_per_sm"] in (6, 10, 16)
     ms = best["ms"]
     assert (ms[ms > 0] > 0).any()
-    if best["pair_variant"] != 8:
+    if best["pair_variant"] < 8:
         # the cell kernel's grid: the fastest of the grid x split trials
         assert ms[best["cells_per_cutoff"] - 1,
                   [6, 10, 16].index(best["kspace_ctas_per_sm"])] == ms[ms > 0].min()
     else:
-        # the group kernel: its fastest subdivision
-        mg = best["ms_group"]
+        # the group kernel or its half-shell form: its fastest subdivision
+        mg = best["ms_group"] if best["pair_variant"] == 8 else best["ms_half"]
         assert mg[best["cells_per_cutoff"] - 1] == mg[mg > 0].min()
+    if precision == "fp64":
+        assert (best["ms_half"] < 0).all()
     if precision == "mixed":
         # the Ewald chain beside or after the r-space chain, chosen with the variant
         assert best["kspace_serial"] in (0, 1)
         s = best["ms_serial"]
         assert s[best["kspace_serial"]] == s[s > 0].min()
     f0, _ = M.ForcePath(*args, precision=precision).forces(g["r"][0])
-    assert best["pair_variant"] in range(9)
+    assert best["pair_variant"] in range(10)
     f1, _ = M.ForcePath(*args, precision=precision, cells_per_cutoff=best["cells_per_cutoff"],
                         kspace_ctas_per_sm=best["kspace_ctas_per_sm"],
                         pair_variant=best["pair_variant"]).forces(g["r"][0])

@@ -106,12 +106,14 @@ def test_cell_list_is_deterministic(precision):
 
 
 @pytest.mark.parametrize("case", ["spce864", "brine532"])
-def test_group_pair_kernel_matches_oracle(case):
+@pytest.mark.parametrize("variant", [8, 9])
+def test_group_pair_kernel_matches_oracle(case, variant):
     """the group pair kernel (pair_variant 8: warps over groups of 8 home
-    sites, neighbours pruned against the group's bounding box) gives the
+    sites, neighbours pruned against the group's bounding box) and its
+    half-shell form (9: every pair once, forces in fixed point) give the
     oracle's forces and energies as the cell kernel does"""
     g, meta, system, ew, fc = make(case, "mixed")
-    _, _, _, _, fg = make(case, "mixed", pair_variant=8)
+    _, _, _, _, fg = make(case, "mixed", pair_variant=variant)
     orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
     for d in (0, g["r"].shape[0] - 1):
         f, en = fg.forces(g["r"][d], measure=True)
@@ -131,10 +133,12 @@ def test_group_pair_kernel_matches_oracle(case):
 
 @pytest.mark.parametrize("cells", [2, 3])
 @pytest.mark.parametrize("polar", [False, True])
-def test_group_pair_kernel_full_size(cells, polar):
+@pytest.mark.parametrize("variant", [8, 9])
+def test_group_pair_kernel_full_size(cells, polar, variant):
     """32768 waters (SPC/E, or with Drude shells displaced at random): the
-    group kernel equals the cell kernel within the mixed rounding, for cells
-    of a half and of a third of the cutoff"""
+    group kernel and its half-shell form (Drude builds run the group kernel
+    for it) equal the cell kernel within the mixed rounding, for cells of a
+    half and of a third of the cutoff"""
     from macsimus_gb300 import configs
     w = configs.workload("drude32768" if polar else "spce32768", seed=3)
     r = w["r"].copy()
@@ -145,10 +149,44 @@ def test_group_pair_kernel_full_size(cells, polar):
     args = (w["system"], [w["L"]] * 3, w["cutoff"], w["alpha"], w["kappa"])
     f0, e0 = M.ForcePath(*args, precision="mixed", cells_per_cutoff=cells).forces(r, measure=True)
     f1, e1 = M.ForcePath(*args, precision="mixed", cells_per_cutoff=cells,
-                         pair_variant=8).forces(r, measure=True)
+                         pair_variant=variant).forces(r, measure=True)
     assert rel_rms(f1, f0) < 2e-6
     assert abs(e1["er"] - e0["er"]) < 2e-6 * abs(e0["eself"])
     assert abs(e1["lj"] - e0["lj"]) < 1e-5 * abs(e0["lj"])
+
+
+@pytest.mark.parametrize("cells", [1, 2, 3])
+def test_half_shell_kernel_every_pair_once(cells):
+    """the half-shell group kernel at every cell subdivision (the column
+    (0, 0) from the home cell up, pairs inside a cell from the lower sorted
+    index): the oracle's forces, LJ energy and virial, so no pair is missing
+    or taken twice"""
+    g, meta, system, ew, fh = make("spce864", "mixed", pair_variant=9, cells_per_cutoff=cells)
+    orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
+    f, en = fh.forces(g["r"][0], measure=True)
+    fo, eo = orc.forces(g["r"][0], nthreads=4)
+    assert rel_rms(f, fo) < MIXED_TOL
+    assert abs(en["lj"] - eo["lj"]) <= 1e-5 * abs(eo["lj"])
+    assert abs(en["er"] - eo["er"]) <= 2e-6 * abs(eo["eself"])
+    assert abs(en["vir"] - eo["vir"]) <= 2e-5 * abs(eo["vir"])
+
+
+def test_half_shell_md_is_reproducible():
+    """MD with the half-shell kernel: the fixed-point force sums make the
+    trajectory the same bit for bit on every run, with and without
+    measurement, although the atomics land in any order"""
+    g, meta, system, ew, _ = make("spce864", "mixed")
+
+    def run(measure):
+        _, _, _, _, fp = make("spce864", "mixed", pair_variant=9)
+        fp.md_set_state(g["r"][2], g["r"][2] - g["r"][1])
+        for _ in range(4):
+            fp.md_steps(5, measure=measure)
+        return fp.md_get_state()
+
+    a, b, c = run(True), run(True), run(False)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert np.array_equal(a[0], c[0]) and np.array_equal(a[1], c[1])
 
 
 def test_ewald_kspace_part():
