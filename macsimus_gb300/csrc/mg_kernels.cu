@@ -785,15 +785,46 @@ __global__ void __launch_bounds__(NW * 32)
 // integer atomics; integer addition does not depend on the order, so the
 // forces come out the same bit for bit on every run.  The neighbour's force
 // of an iteration is summed over the 8 home lanes by a reduce-scatter (three
-// shuffle levels: lanes i = 0, 2, 4 end with x, y, z), scaled by 2^32 in
-// FP32 (exact) and added with one atomic per component; the home sites' own
-// compensated sums once per group.
-// finish_forces_kernel turns the sums into the FP64 forces (site order) and
-// clears them for the next evaluation.
-constexpr double FIX_SCALE = 4294967296.0;  // 2^32: |F| < 2^31 K/A, steps of 2.3e-10 K/A
+// shuffle levels: lanes i = 0, 2, 4 end with x, y, z) and added with one
+// atomic per component; the home sites' own compensated sums once per
+// group.  Every rounding of the force arithmetic is explicit (the `_rn`
+// intrinsics and explicit FMAs), so that the measuring and the plain
+// instantiation run the same arithmetic: nvcc and ptxas may otherwise fuse
+// a product into a following add in one kernel and not in the other, and a
+// measured step would move the sites differently.  finish_forces_kernel
+// turns the sums into the FP64 forces (site order) and clears them for the
+// next evaluation.  Measured on 32768 waters (cells of cutoff/2): 0.37 ms
+// against 0.45 ms for the group kernel.  Pairing two iterations on one
+// conversion and one atomic, and a float-to-integer conversion in FP32
+// arithmetic instead of the one on the FP64 pipe, both measured slower.
+constexpr double FIX_SCALE = 4294967296.0;  // 2^32: steps of 2.3e-10 K/A, |F| < 2^31 K/A
 
+
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// the half-shell kernel's pair force factor f (force on i = f (r_i - r_j))
+// with every rounding explicit; flj: the LJ part.  The same terms as
+// spline_any and the group kernel: smoothed LJ (core below C1q, quadratic
+// tail up to C2q) and the hyperbolic erfc spline d.x + d.y / (d.z + r^2)
+__device__ __forceinline__ float pair_force_rn(const PairFS& P, float rr,
+                                               const float4* __restrict__ erd, float sgrid,
+                                               int ntab, float& flj) {
+  const float x = __fmul_rn(P.Sq, rcp_approx(rr)), y = __fmul_rn(__fmul_rn(x, x), x);
+  flj = rr < P.C1q ? __fmul_rn(__fmul_rn(P.E24, __fmaf_rn(__fmul_rn(2.f, y), y, -y)), x)
+                   : (rr < P.C2q ? __fmul_rn(P.A4, __fadd_rn(rr, -P.C2q)) : 0.f);
+  const int ix = min(__float_as_int(__fmaf_rn(rr, sgrid, 12582911.5f)) - 0x4B400000, ntab - 1);
+  const float4 d = __ldg(erd + ix);
+  return __fmaf_rn(__fmaf_rn(d.y, rcp_approx(__fadd_rn(d.z, rr)), d.x), P.qq, flj);
+}
+
+// 7 CTAs per SM (72 registers, no spills): measured faster than 8 (64) and
+// than no bound (95)
 template <bool MEASURE, int NW>
-__global__ void __launch_bounds__(NW * 32)
+__global__ void __launch_bounds__(NW * 32, MEASURE ? 1 : 7)
     pair_half_mixed_kernel(PairArgs a, const int4* __restrict__ pj,
                            const PairF* __restrict__ ptab_g, const float4* __restrict__ erd,
                            const float4* __restrict__ eru, float sx, float sy, float sz, float cq,
@@ -833,9 +864,9 @@ __global__ void __launch_bounds__(NW * 32)
     const int ti = i0 + il;
     const int4 me = vi ? pj[ti] : make_int4(0, 0, 0, 0);
     const int kind_i = me.w & 255, mol_i = me.w >> 8;
-    const float xi = (float)(int)((unsigned)me.x - refx) * sx,
-                yi = (float)(int)((unsigned)me.y - refy) * sy,
-                zi = (float)(int)((unsigned)me.z - refz) * sz;
+    const float xi = __fmul_rn((float)(int)((unsigned)me.x - refx), sx),
+                yi = __fmul_rn((float)(int)((unsigned)me.y - refy), sy),
+                zi = __fmul_rn((float)(int)((unsigned)me.z - refz), sz);
     float blx = vi ? xi : 3e38f, bly = vi ? yi : 3e38f, blz = vi ? zi : 3e38f;
     float bhx = vi ? xi : -3e38f, bhy = vi ? yi : -3e38f, bhz = vi ? zi : -3e38f;
 #pragma unroll
@@ -877,9 +908,10 @@ __global__ void __launch_bounds__(NW * 32)
           float4 f4 = make_float4(0.f, 0.f, 0.f, 0.f);
           if (j < j1) {
             const int4 q = pj[j];
-            f4 = make_float4((float)(int)((unsigned)q.x - refx) * sx,
-                             (float)(int)((unsigned)q.y - refy) * sy,
-                             (float)(int)((unsigned)q.z - refz) * sz, __int_as_float(q.w));
+            f4 = make_float4(__fmul_rn((float)(int)((unsigned)q.x - refx), sx),
+                             __fmul_rn((float)(int)((unsigned)q.y - refy), sy),
+                             __fmul_rn((float)(int)((unsigned)q.z - refz), sz),
+                             __int_as_float(q.w));
             const float ddx = fmaxf(fmaxf(blx - f4.x, f4.x - bhx), 0.f),
                         ddy = fmaxf(fmaxf(bly - f4.y, f4.y - bhy), 0.f),
                         ddz = fmaxf(fmaxf(blz - f4.z, f4.z - bhz), 0.f);
@@ -899,41 +931,41 @@ __global__ void __launch_bounds__(NW * 32)
             const bool vt = t < n;
             const float4 q = sj[warp][vt ? t : 0];
             const int tj = sjt[warp][vt ? t : 0];
-            const float dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
-            const float rr = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const float dx = __fadd_rn(xi, -q.x), dy = __fadd_rn(yi, -q.y),
+                        dz = __fadd_rn(zi, -q.z);
+            const float rr = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
             const int qw = __float_as_int(q.w);
             const bool ok = vt && vi && rr < cq && (qw >> 8) != mol_i &&
                             (tj > ti || tj >= he || tj < hs);
             const PairFS P = ptab[kind_i * nk + (qw & 255)];
-            const float x = __fdividef(P.Sq, rr), y = x * x * x, xt = rr - P.C2q;
-            const bool core = rr < P.C1q, tail = rr < P.C2q;
-            const float flj = core ? P.E24 * fmaf(2.f * y, y, -y) * x : (tail ? P.A4 * xt : 0.f);
-            float e_el_p = 0.f;
-            float f = flj + spline_any<MEASURE, true>(erd, eru, rr, sgrid, ntab, P.qq, e_el_p);
+            float flj;
+            float f = pair_force_rn(P, rr, erd, sgrid, ntab, flj);
             f = ok ? f : 0.f;
-            // the products rounded once and used for both sites (no
-            // contraction into an FMA on one side only)
+            ax = __fmaf_rn(f, dx, ax);
+            ay = __fmaf_rn(f, dy, ay);
+            az = __fmaf_rn(f, dz, az);
             const float px = __fmul_rn(f, dx), py = __fmul_rn(f, dy), pz = __fmul_rn(f, dz);
-            ax = __fadd_rn(ax, px);
-            ay = __fadd_rn(ay, py);
-            az = __fadd_rn(az, pz);
             if (MEASURE && ok) {
-              e_lj += core ? P.E4 * fmaf(y, y, -y) : (tail ? P.A * xt * xt : 0.f);
+              // energies and virial: no effect on the forces
+              const float x = __fdividef(P.Sq, rr), y = x * x * x, xt = rr - P.C2q;
+              e_lj += rr < P.C1q ? P.E4 * fmaf(y, y, -y) : (rr < P.C2q ? P.A * xt * xt : 0.f);
               e_vir += rr * flj;
+              float e_el_p = 0.f;
+              spline_any<true, true>(erd, eru, rr, sgrid, ntab, P.qq, e_el_p);
               e_el += e_el_p;
               pv.add(dx, dy, dz, f);
             }
             // the neighbour's force, minus the sum over the 8 home lanes
             float k0 = b2 ? pz : px, k1 = b2 ? 0.f : py;
             const float s0 = b2 ? px : pz, s1 = b2 ? py : 0.f;
-            k0 += __shfl_xor_sync(0xffffffffu, s0, 4);
-            k1 += __shfl_xor_sync(0xffffffffu, s1, 4);
+            k0 = __fadd_rn(k0, __shfl_xor_sync(0xffffffffu, s0, 4));
+            k1 = __fadd_rn(k1, __shfl_xor_sync(0xffffffffu, s1, 4));
             float k = b1 ? k1 : k0;
-            k += __shfl_xor_sync(0xffffffffu, b1 ? k0 : k1, 2);
-            k += __shfl_xor_sync(0xffffffffu, k, 1);
+            k = __fadd_rn(k, __shfl_xor_sync(0xffffffffu, b1 ? k0 : k1, 2));
+            k = __fadd_rn(k, __shfl_xor_sync(0xffffffffu, k, 1));
             if (jw && vt)
               atomicAdd(facc + 3 * (long)tj + comp,
-                        (unsigned long long)__float2ll_rn(k * -(float)FIX_SCALE));
+                        (unsigned long long)__float2ll_rn(__fmul_rn(k, -(float)FIX_SCALE)));
           }
           __syncwarp();
         }

@@ -171,14 +171,16 @@ def test_half_shell_kernel_every_pair_once(cells):
     assert abs(en["vir"] - eo["vir"]) <= 2e-5 * abs(eo["vir"])
 
 
-def test_half_shell_md_is_reproducible():
-    """MD with the half-shell kernel: the fixed-point force sums make the
-    trajectory the same bit for bit on every run, with and without
-    measurement, although the atomics land in any order"""
+@pytest.mark.parametrize("variant", [8, 9])
+def test_group_kernel_md_is_reproducible(variant):
+    """MD with the group kernel and its half-shell form: the same trajectory
+    bit for bit on every run, with and without measurement (the half-shell
+    kernel's fixed-point force sums do not depend on the order in which the
+    atomics land)"""
     g, meta, system, ew, _ = make("spce864", "mixed")
 
     def run(measure):
-        _, _, _, _, fp = make("spce864", "mixed", pair_variant=9)
+        _, _, _, _, fp = make("spce864", "mixed", pair_variant=variant)
         fp.md_set_state(g["r"][2], g["r"][2] - g["r"][1])
         for _ in range(4):
             fp.md_steps(5, measure=measure)
