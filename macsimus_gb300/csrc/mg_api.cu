@@ -608,11 +608,16 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   ctx->nq = (int)qsite.size();
   ctx->nd = (int)dsite.size();
   ctx->ndblocks = (ctx->nd + 127) / 128;
-  // charge chunks of pass 1: about 8 (FP64 kernel) or 6 (FP32 kernel) CTAs
-  // per SM, at least 64 charges each
+  // charge chunks of pass 1: about 8 (FP64 kernel) or 10 (FP32 kernel) CTAs
+  // per SM of a GB300, at least 512 charges each.  Smaller chunks fill the
+  // GPU with one small box but multiply the partial sums the reduction
+  // reads (nk x nchunk): a batch of 256 boxes of 500-4000 ions spent more
+  // time reducing 64-charge chunks than in pass 1 itself.  The split is
+  // fixed by the box, not by the device, so results do not depend on it.
   const int p1ctas = (p->kspace_ctas_per_sm > 0 ? p->kspace_ctas_per_sm
-                                                : (ctx->precision == MG_MIXED ? 10 : 8)) * 152;
-  ctx->nchunk = std::max(1, std::min(std::max(1, ctx->nq / 64),
+                                                : (ctx->precision == MG_MIXED ? 10 : 8)) *
+                     PARTITION_SMS;
+  ctx->nchunk = std::max(1, std::min(std::max(1, ctx->nq / 512),
                                      (p1ctas + ctx->np1job - 1) / ctx->np1job));
   ctx->nkblocks = (nk + 255) / 256;
 
@@ -849,7 +854,7 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   // cook's No.f: 3 per site less constraints, dependants and the conserved
   // momentum (sim/siminit.c:518-530)
   ctx->thermo_f = p->thermo_f > 0 ? p->thermo_f : 3.0 * (ns - t->ndep) - t->nc - 3;
-  ctx->nchi = 2 * 152;
+  ctx->nchi = 2 * PARTITION_SMS;
   CK(dalloc(&ctx->d_chi, (size_t)ctx->nchi));
   CK(dalloc(&ctx->d_zth, 1));
   CK(dalloc(&ctx->d_step, 1));
@@ -1890,7 +1895,7 @@ int widom_prepare(mg_ctx* ctx, const mg_probe* probe, long long ninsert, unsigne
   }
   if (!ctx->d_wgeom) {
     CK(dalloc(&ctx->d_wgeom, 3 * MAX_WPROBE));
-    CK(dalloc(&ctx->d_wpart, 152 * 8));
+    CK(dalloc(&ctx->d_wpart, PARTITION_SMS * 8));
     CK(dalloc(&ctx->d_wtabf, MAX_WPROBE * MAX_KINDS));
     CK(dalloc(&ctx->d_wtabd, MAX_WPROBE * MAX_KINDS));
     CK(dalloc(&ctx->d_wbox, 1));

@@ -83,6 +83,12 @@ inline int phase_row_mixed(int Kx, int Ky, int Kz) { return (Kx + 1) + (2 * Ky +
 #define MG_BODY __device__ __noinline__
 #endif
 
+// the SM count of a GB300, used to size fixed partitions of sums (pass-1
+// charge chunks, Widom and Bussi partials): fixed rather than queried, so
+// that the summation order, and with it the last bits, do not depend on the
+// device
+constexpr int PARTITION_SMS = 152;
+
 constexpr int KZT = 4;          // kz per pass-1 thread
 constexpr int PAIR_THREADS = 128;
 constexpr int MAX_KINDS = 16;

@@ -133,7 +133,7 @@ cudaError_t k_thermostat(const Launch& L, const ThermoArgs& a, const double* kin
     bussi_chi2_kernel<<<a.nchi, TH_THREADS, 0, L.s>>>((long long)a.nf, a.seed, a.step, chi_part);
     ++*L.counter;
   }
-  const int grid = (int)std::min<long long>((3LL * a.ns + TH_THREADS - 1) / TH_THREADS, 4 * 152);
+  const int grid = (int)std::min<long long>((3LL * a.ns + TH_THREADS - 1) / TH_THREADS, 4 * PARTITION_SMS);
   thermostat_scale_kernel<<<grid, TH_THREADS, 0, L.s>>>(a, kin_part, chi_part, r1);
   ++*L.counter;
   if (a.kind == 2) {

@@ -345,7 +345,7 @@ cudaError_t k_xwidom(const Launch& L, const XWidomArgs& a, bool fp64) {
 
 int widom_blocks(long long n) {
   long long b = (n + WD_WARPS - 1) / WD_WARPS;
-  return (int)(b < 152 * 8 ? (b > 0 ? b : 1) : 152 * 8);
+  return (int)(b < PARTITION_SMS * 8 ? (b > 0 ? b : 1) : PARTITION_SMS * 8);
 }
 
 cudaError_t k_widom(const Launch& L, const WidomBox* boxes, int nbox, long long n, bool fp64) {
