@@ -399,7 +399,7 @@ def run_batch(args, rank, world, local):
             dist.barrier()
         torch.cuda.synchronize()
 
-    engine = 1 if args.kspace_engine is None else args.kspace_engine
+    engine = 0 if args.kspace_engine is None else args.kspace_engine
 
     def make(precision):
         return M.Batch([dict(system=b["system"], L=b["L"], cutoff=b["cutoff"], alpha=b["alpha"],
@@ -579,8 +579,8 @@ def main():
     ap.add_argument("--kspace-engine", type=int, default=None,
                     help="Ewald engine of the FP32 path: 0 tensor cores where they fit, 1 FP32 "
                          "cores, 2 tensor-core pass 2 only, 3 tensor cores for both passes "
-                         "(default: 0 for one box; 1 for batches of small boxes, measured "
-                         "faster when many boxes share the GPU)")
+                         "(default 0: one launch per pass over all boxes of a batch, the "
+                         "boxes whose tiles do not fit on the FP32 cores)")
     ap.add_argument("--skin", type=float, default=0.0,
                     help="> 0: Verlet lists of cutoff+skin instead of cells re-binned every step")
     ap.add_argument("--equilibrate", type=int, default=400,

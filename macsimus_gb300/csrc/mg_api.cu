@@ -192,6 +192,11 @@ struct mg_ctx {
   cudaStream_t kstream = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   double* d_fk = nullptr;
+  // the tensor-core passes' arguments (TcBox) for the position and force
+  // buffers of the context's own calls: slot 3 ri + fi for r = (d_r, d_rs)[ri],
+  // f = (d_f, d_fs, d_fk)[fi]; slot 6 for a caller's buffers
+  TcBox* d_tcb = nullptr;
+  TcBox h_tcb[7];
   bool prof_on = false;
   // one MD step (force-only / measured) captured as a CUDA graph
   cudaGraphExec_t g_step = nullptr, g_meas = nullptr;
@@ -746,10 +751,7 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
         const size_t nzb = sk_tc_zb_floats(kd);
         CK(dalloc(&ctx->d_zb, nzb));
         CK(cudaMemset(ctx->d_zb, 0, nzb * sizeof(float)));
-        int dev = 0, nsm = 0;
-        CK(cudaGetDevice(&dev));
-        CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-        sk_tc_split(kd, ctx->nkrows, nsm, &ctx->sk_nch, &ctx->sk_gpc);
+        sk_tc_split(kd, ctx->nkrows, &ctx->sk_nch, &ctx->sk_gpc);
       }
     }
   }
@@ -942,12 +944,58 @@ int build_lists(mg_ctx* ctx, const double* r_dev) {
   return fail(ctx, MG_ERR_SIZE, "neighbour list capacity");
 }
 
+// the arguments of the context's tensor-core Ewald passes (r: the positions,
+// needed by the phase kernel only)
+TcBox tc_args(mg_ctx* ctx, const KArgs& a, const double* r) {
+  TcBox b;
+  tc_box(a, ctx->nkrows, ctx->sk_nch, ctx->sk_gpc, ctx->d_tckrows, ctx->d_tcrows, r,
+         (float2*)ctx->d_tab, ctx->d_za, ctx->sk_tc ? ctx->d_zb : nullptr, ctx->d_vb,
+         (float2*)ctx->d_part, &b);
+  return b;
+}
+
+// the device copy of the tensor-core arguments for positions r (NULL: any;
+// only the phase kernel reads them) and the forces of a; *h gets the host
+// copy.  Buffers other than the context's own go to the last slot, uploaded
+// before the launch (not while the stream is being captured).
+const TcBox* tc_slot(mg_ctx* ctx, const Launch& L, const KArgs& a, const double* r,
+                     const TcBox** h) {
+  const double* rs[2] = {ctx->d_r, ctx->d_rs};
+  const double* fs[3] = {ctx->d_f, ctx->d_fs, ctx->d_fk};
+  int ri = -1, fi = -1;
+  for (int i = 0; i < 2; i++)
+    if (!r || r == rs[i]) {
+      ri = i;
+      break;
+    }
+  for (int i = 0; i < 3; i++)
+    if (a.f == fs[i]) fi = i;
+  if (ri >= 0 && fi >= 0) {
+    *h = &ctx->h_tcb[3 * ri + fi];
+    return ctx->d_tcb + 3 * ri + fi;
+  }
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(L.s, &cs) != cudaSuccess ||
+      cs != cudaStreamCaptureStatusNone)
+    return nullptr;
+  ctx->h_tcb[6] = tc_args(ctx, a, r);
+  if (cudaMemcpyAsync(ctx->d_tcb + 6, &ctx->h_tcb[6], sizeof(TcBox), cudaMemcpyHostToDevice,
+                      L.s) != cudaSuccess ||
+      cudaStreamSynchronize(L.s) != cudaSuccess)
+    return nullptr;
+  *h = &ctx->h_tcb[6];
+  return ctx->d_tcb + 6;
+}
+
 // phase rows of the FP32 path; with the tensor-core passes the same kernel
 // builds their operand tiles
 cudaError_t phase_mixed(mg_ctx* ctx, const Launch& L, const KArgs& a, const double* r) {
-  if (ctx->kspace_tc)
-    return k_kf_tc_phase(L, a, r, (float2*)ctx->d_tab, ctx->d_za,
-                         ctx->sk_tc ? ctx->d_zb : nullptr);
+  if (ctx->kspace_tc) {
+    const TcBox* h = nullptr;
+    const TcBox* d = tc_slot(ctx, L, a, r, &h);
+    if (!d) return cudaErrorInvalidValue;
+    return k_batch_tc_phase(L, d, 1, h->g_phase, h->smem_phase);
+  }
   return k_phase_tables_mixed(L, a, r, (float2*)ctx->d_tab, ctx->d_qfix);
 }
 
@@ -961,7 +1009,10 @@ cudaError_t sk_mixed(mg_ctx* ctx, const Launch& L, const KArgs& a, bool measure)
     if (e != cudaSuccess) return e;
     return k_sk_reduce_mixed(L, a, part, measure);
   }
-  cudaError_t e = k_sk_tc(L, a, ctx->nkrows, ctx->sk_nch, ctx->sk_gpc, tab, ctx->d_zb, part);
+  const TcBox* h = nullptr;
+  const TcBox* d = tc_slot(ctx, L, a, nullptr, &h);
+  if (!d) return cudaErrorInvalidValue;
+  cudaError_t e = k_batch_sk_tc(L, d, 1, h->g_sk, h->smem_sk);
   if (e != cudaSuccess) return e;
   KArgs b = a;
   b.nchunk = ctx->sk_nch;
@@ -971,7 +1022,10 @@ cudaError_t sk_mixed(mg_ctx* ctx, const Launch& L, const KArgs& a, bool measure)
 // Ewald pass 2 of the FP32 path: tensor cores or FP32 cores
 cudaError_t kf_mixed(mg_ctx* ctx, const Launch& L, const KArgs& a) {
   if (!ctx->kspace_tc) return k_kf_gemm_mixed(L, a, (const float2*)ctx->d_tab);
-  return k_kf_tc(L, a, ctx->nkrows, ctx->d_tckrows, ctx->d_tcrows, ctx->d_za, ctx->d_vb);
+  const TcBox* h = nullptr;
+  const TcBox* d = tc_slot(ctx, L, a, nullptr, &h);
+  if (!d) return cudaErrorInvalidValue;
+  return k_batch_kf_tc(L, d, 1, h->g_vb, h->g_kf, h->smem_kf);
 }
 
 ExclArgs excl_args(mg_ctx* ctx, const double* r_dev, double* f) {
@@ -1069,6 +1123,23 @@ KArgs make_kargs(mg_ctx* ctx, double* f_dev) {
   ka.ns = ctx->ns;
   ka.status = ctx->d_status;
   return ka;
+}
+
+// the tensor-core arguments for the context's own buffer pairs, on the
+// device once (a context with the Ewald passes on the tensor cores)
+int tc_upload_slots(mg_ctx* ctx) {
+  if (!ctx->kspace_tc) return MG_OK;
+  double* rs[2] = {ctx->d_r, ctx->d_rs};
+  double* fs[3] = {ctx->d_f, ctx->d_fs, ctx->d_fk};
+  for (int ri = 0; ri < 2; ri++)
+    for (int fi = 0; fi < 3; fi++) {
+      const KArgs ka = make_kargs(ctx, fs[fi]);
+      ctx->h_tcb[3 * ri + fi] = tc_args(ctx, ka, rs[ri]);
+    }
+  ctx->h_tcb[6] = ctx->h_tcb[0];
+  CK(dalloc(&ctx->d_tcb, 7));
+  CK(cudaMemcpy(ctx->d_tcb, ctx->h_tcb, 7 * sizeof(TcBox), cudaMemcpyHostToDevice));
+  return MG_OK;
 }
 
 int forces_async(mg_ctx* ctx, const double* r_dev, double* f_dev, bool measure) {
@@ -1517,6 +1588,7 @@ extern "C" {
 mg_ctx* mg_create(const mg_topology* top, const mg_params* par, int* status) {
   mg_ctx* ctx = new mg_ctx();
   int rc = setup(ctx, top, par);
+  if (rc == MG_OK) rc = tc_upload_slots(ctx);
   if (rc != MG_OK) {
     fprintf(stderr, "mg_create: %s\n", ctx->err.c_str());
     mg_destroy(ctx);
@@ -1532,7 +1604,7 @@ int mg_destroy(mg_ctx* ctx) {
   void* bufs[] = {ctx->d_rs, ctx->d_fs, ctx->d_r,      ctx->d_f,       ctx->d_r1,    ctx->d_p,      ctx->d_kind,
                   ctx->d_mol,    ctx->d_key,     ctx->d_pfix,   ctx->d_idx,   ctx->d_key_s,  ctx->d_order,
                   ctx->d_cell_start, ctx->d_ccount, ctx->d_ccursor, ctx->d_spans, ctx->d_gstart,
-                  ctx->d_hspans, ctx->d_facc,
+                  ctx->d_hspans, ctx->d_facc, ctx->d_tcb,
                   ctx->d_gcell, ctx->d_pj, ctx->d_pd,  ctx->d_stencil,
                   ctx->d_ptabf,  ctx->d_ptabd,   ctx->d_erd,   ctx->d_eru,    ctx->d_ert,
                   ctx->d_epart,  ctx->d_qsite,   ctx->d_qval,  ctx->d_task,   ctx->d_col,
@@ -2399,6 +2471,7 @@ struct mg_batch {
   // grids, one captured graph per kind of step
   int fused_ok = -1;
   BoxStep* d_steps = nullptr;
+  TcBox* d_tc = nullptr;
   BatchGrid grid{};
   cudaGraphExec_t gf_step = nullptr, gf_meas = nullptr;
   int launches_fused = 0;
@@ -2509,6 +2582,7 @@ int mg_batch_destroy(mg_batch* b) {
   if (b->gf_step) cudaGraphExecDestroy(b->gf_step);
   if (b->gf_meas) cudaGraphExecDestroy(b->gf_meas);
   if (b->d_steps) cudaFree(b->d_steps);
+  if (b->d_tc) cudaFree(b->d_tc);
   if (b->d_wbox) cudaFree(b->d_wbox);
   for (cudaEvent_t e : b->ev_join)
     if (e) cudaEventDestroy(e);
@@ -2532,10 +2606,11 @@ namespace {
 // a box the batched kernels take: the FP32 path without Drude charges,
 // dependants, thermostat, step limiter or drift removal, cells re-binned
 // at every step on a grid of at least 3 cells per edge, the cell pair kernel
-// with 4 warps, Ewald passes on the FP32 cores, no dipole term
+// with 4 warps, both Ewald passes on the FP32 cores or both on the tensor
+// cores, no dipole term
 bool fusable(const mg_ctx* c) {
   return c->precision == MG_MIXED && !c->polar && !c->use_list && !c->allpairs &&
-         c->pair_variant == 0 && !c->kspace_tc && !c->sk_tc && c->thermostat == 0 &&
+         c->pair_variant == 0 && c->kspace_tc == c->sk_tc && c->thermostat == 0 &&
          c->ndep == 0 && !c->dipole && c->drmax == 0 && !c->drift_step && c->nq > 0 &&
          !c->prof_on;
 }
@@ -2545,6 +2620,7 @@ bool fusable(const mg_ctx* c) {
 int build_fused(mg_batch* b) {
   const int nbox = (int)b->box.size();
   std::vector<BoxStep> h(nbox);
+  std::vector<TcBox> tc(nbox);
   BatchGrid& g = b->grid;
   g = BatchGrid{};
   for (int i = 0; i < nbox; i++) {
@@ -2615,6 +2691,25 @@ int build_fused(mg_batch* b) {
     e.g_skr = (c->nk + 255) / 256;
     e.g_kf = kf_mixed_blocks(c->nq);
     e.g_shake = (c->nmol + 127) / 128;
+    TcBox& t = tc[i];
+    if (c->kspace_tc) {
+      // the tensor-core passes, with the arguments of the box's single
+      // launches (tc_args); its pass 1 reduces sk_nch chunks
+      t = tc_args(c, e.ka, c->d_r);
+      e.ka.nchunk = c->sk_nch;
+      e.g_charge = e.g_phase = e.g_p1x = e.g_p1y = e.g_kf = 0;
+      g.any_tc = true;
+    } else {
+      t = TcBox{};
+      g.any_fp32 = true;
+    }
+    g.tc_phase = std::max(g.tc_phase, t.g_phase);
+    g.tc_sk = std::max(g.tc_sk, t.g_sk);
+    g.tc_vb = std::max(g.tc_vb, t.g_vb);
+    g.tc_kf = std::max(g.tc_kf, t.g_kf);
+    g.tc_phase_smem = std::max(g.tc_phase_smem, t.smem_phase);
+    g.tc_sk_smem = std::max(g.tc_sk_smem, t.smem_sk);
+    g.tc_kf_smem = std::max(g.tc_kf_smem, t.smem_kf);
     g.site = std::max(g.site, e.g_site);
     g.order = std::max(g.order, e.g_order);
     g.pair = std::max(g.pair, e.g_pair);
@@ -2627,10 +2722,13 @@ int build_fused(mg_batch* b) {
     g.kf = std::max(g.kf, e.g_kf);
     g.shake = std::max(g.shake, e.g_shake);
     g.pair_smem = std::max(g.pair_smem, sizeof(PairFS) * (size_t)c->nkind * c->nkind);
-    g.kf_smem = std::max(g.kf_smem, kf_mixed_smem(e.ka));
+    if (!c->kspace_tc) g.kf_smem = std::max(g.kf_smem, kf_mixed_smem(e.ka));
   }
   if (cudaMalloc(&b->d_steps, sizeof(BoxStep) * (size_t)nbox) != cudaSuccess ||
       cudaMemcpy(b->d_steps, h.data(), sizeof(BoxStep) * (size_t)nbox, cudaMemcpyHostToDevice) !=
+          cudaSuccess ||
+      cudaMalloc(&b->d_tc, sizeof(TcBox) * (size_t)nbox) != cudaSuccess ||
+      cudaMemcpy(b->d_tc, tc.data(), sizeof(TcBox) * (size_t)nbox, cudaMemcpyHostToDevice) !=
           cudaSuccess)
     return bfail(b, MG_ERR_CUDA, "batch: uploading the boxes' kernel arguments");
   return MG_OK;
@@ -2640,11 +2738,18 @@ int build_fused(mg_batch* b) {
 int fused_step_enqueue(mg_batch* b, bool measure) {
   const int nbox = (int)b->box.size();
   Launch L{b->main, &b->launches_fused};
-  BCK(k_batch_rspace(L, b->d_steps, nbox, b->grid, measure));
-  BCK(k_batch_pass1(L, b->d_steps, nbox, b->grid));
-  BCK(k_batch_sk_reduce(L, b->d_steps, nbox, b->grid, measure));
-  BCK(k_batch_pass2(L, b->d_steps, nbox, b->grid));
-  BCK(k_batch_step(L, b->d_steps, nbox, b->grid, measure));
+  const BatchGrid& g = b->grid;
+  // the order of a single box's serial chain: cell list, pair and
+  // exclusion terms, phase rows (with the operand tiles), pass 1, its sum,
+  // pass 2, the step
+  BCK(k_batch_rspace(L, b->d_steps, nbox, g, measure));
+  if (g.any_tc) BCK(k_batch_tc_phase(L, b->d_tc, nbox, g.tc_phase, g.tc_phase_smem));
+  if (g.any_fp32) BCK(k_batch_pass1(L, b->d_steps, nbox, g));
+  if (g.any_tc) BCK(k_batch_sk_tc(L, b->d_tc, nbox, g.tc_sk, g.tc_sk_smem));
+  BCK(k_batch_sk_reduce(L, b->d_steps, nbox, g, measure));
+  if (g.any_fp32) BCK(k_batch_pass2(L, b->d_steps, nbox, g));
+  if (g.any_tc) BCK(k_batch_kf_tc(L, b->d_tc, nbox, g.tc_vb, g.tc_kf, g.tc_kf_smem));
+  BCK(k_batch_step(L, b->d_steps, nbox, g, measure));
   return MG_OK;
 }
 

@@ -229,6 +229,49 @@ struct TcRow {
   float kx, ky;
   int ox, oy;
 };
+static_assert(sizeof(TcRow) == 16, "pass 2 reads a TcRow as one int4");
+// the arguments of the tensor-core pass 2 (one CTA per 128 charges) and
+// pass 1 (nrt row tiles x charge chunks) kernels
+struct KfTc {
+  int nq, ns, KP, ntm, ntn, nrows, nxy;
+  const float* za;
+  const float* vb;
+  const TcRow* rows;
+  const int* qsite;
+  const int* qdrude;
+  double Lx, Ly, Lz;
+  double* f;
+  int* status;
+};
+struct SkTc {
+  int KP, KN, Kz, nrows, nrt, ngroups, gpc, row, oyl, nk;
+  const float2* tab;   // phase rows, zero-padded to whole groups of 32 charges
+  const float* zb;     // Z^T tiles
+  const KRow* krows;
+  float2* part;
+  int* status;
+};
+// every argument of one box's tensor-core Ewald passes, as its single
+// launches (k_kf_tc_phase, k_sk_tc, k_kf_tc) take them, with their grids
+// and shared-memory sizes; the batched launches take an array of these
+struct TcBox {
+  KArgs ka;
+  const double* r;
+  float2* tab;
+  float* za;
+  float* zb;
+  int KP, nxy, KN;
+  SkTc sk;
+  KfTc kf;
+  const KRow* tckrows;   // the V-tile builder's rows and output
+  float* vb;
+  int g_phase, g_sk, g_vb, g_kf;
+  size_t smem_phase, smem_sk, smem_kf;
+};
+// zb (and with it pass 1) may be NULL; part: pass 1's partial sums
+void tc_box(const KArgs& a, int nrows, int nch, int gpc, const KRow* tckrows, const TcRow* rows,
+            const double* r, float2* tab, float* za, float* zb, float* vb, float2* part,
+            TcBox* out);
 int kf_tc_kp(const KArgs& a);
 bool kf_tc_fits(const KArgs& a, int nrows);
 size_t kf_tc_za_floats(const KArgs& a);
@@ -236,20 +279,26 @@ size_t kf_tc_vb_floats(const KArgs& a, int nrows);
 void kf_tc_rows(const KArgs& a, const std::vector<KRow>& krows, std::vector<TcRow>* out);
 // the operand tiles of both passes from the phase rows (zb may be NULL)
 cudaError_t k_kf_tc_za(const Launch& L, const KArgs& a, const float2* tab, float* za, float* zb);
-// the phase rows and the operand tiles in one kernel, from the positions
-cudaError_t k_kf_tc_phase(const Launch& L, const KArgs& a, const double* r, float2* tab,
-                          float* za, float* zb);
+
 // pass 1 on the tensor cores: KN = 2 Kz + 1 rounded up to 16 (at most 64);
 // the phase rows must be zero-padded to whole groups of 32 charges
 int sk_tc_kn(const KArgs& a);
 bool sk_tc_fits(const KArgs& a);
 size_t sk_tc_zb_floats(const KArgs& a);
-void sk_tc_split(const KArgs& a, int nrows, int nsm, int* nch, int* gpc);
-cudaError_t k_sk_tc(const Launch& L, const KArgs& a, int nrows, int nch, int gpc,
-                    const float2* tab, const float* zb, float2* part);
-// tckrows: the k rows in the order of the tensor-core tiles ((kx, ky) order)
-cudaError_t k_kf_tc(const Launch& L, const KArgs& a, int nrows, const KRow* tckrows,
-                    const TcRow* rows, const float* za, float* vb);
+// charge chunks of pass 1 (of PARTITION_SMS CTAs over the row tiles, at
+// least 64 groups of 32 charges each: a CTA's set-up and pipeline drain
+// cost about as much as 15 groups): a split fixed by the box
+void sk_tc_split(const KArgs& a, int nrows, int* nch, int* gpc);
+
+// the tensor-core passes of nbox boxes (d: device array of their TcBox;
+// grid: the largest box grid; smem: the largest box's shared memory); a
+// single box is a list of one.  Phase rows and operand tiles; pass 1;
+// the V tiles from W (in the order of the tensor-core tiles, (kx, ky)
+// order) and pass 2
+cudaError_t k_batch_tc_phase(const Launch& L, const TcBox* d, int nbox, int grid, size_t smem);
+cudaError_t k_batch_sk_tc(const Launch& L, const TcBox* d, int nbox, int grid, size_t smem);
+cudaError_t k_batch_kf_tc(const Launch& L, const TcBox* d, int nbox, int gvb, int gkf,
+                          size_t smem);
 
 struct ShakeArgs {
   int nmol;
@@ -340,7 +389,8 @@ struct BoxStep {
   const float4* eru;
   float sx, sy, sz, cq, sg, al;
   ExclArgs xa;
-  // k-space on the FP32 cores
+  // k-space on the FP32 cores (the tensor-core passes take a TcBox; ka
+  // serves both, its nchunk the chunk count of the box's pass 1)
   KArgs ka;
   float2* tab;
   uint4* qf;
@@ -354,10 +404,15 @@ struct BoxStep {
   // CTAs of each kernel
   int g_site, g_order, g_pair, g_excl, g_charge, g_phase, g_p1x, g_p1y, g_skr, g_kf, g_shake;
 };
-// the largest grid and shared memory of each kernel over the boxes
+// the largest grid and shared memory of each kernel over the boxes (the
+// FP32-core k-space kernels have zero grids for boxes on the tensor cores
+// and the other way round; tc: the TcBox grids and shared memory)
 struct BatchGrid {
   int site, order, pair, excl, charge, phase, p1x, p1y, skr, kf, shake;
   size_t pair_smem, kf_smem;
+  int tc_phase, tc_sk, tc_vb, tc_kf;
+  size_t tc_phase_smem, tc_sk_smem, tc_kf_smem;
+  bool any_fp32, any_tc;
 };
 // the force evaluation up to Ewald pass 1 (cell list, pair and exclusion
 // kernels, phase rows), then pass 1 (mg_kspace.cu), then the S(k) sums and

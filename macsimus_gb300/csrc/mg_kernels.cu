@@ -2233,9 +2233,16 @@ cudaError_t k_batch_rspace(const Launch& L, const BoxStep* d, int nbox, const Ba
     if (g.excl > 0) batch_excl_kernel<false><<<dim3(g.excl, nbox), EXCL_THREADS, 0, L.s>>>(d);
   }
   if (e != cudaSuccess) return e;
-  batch_charge_fixed_kernel<<<dim3(g.charge, nbox), 256, 0, L.s>>>(d);
-  batch_phase_kernel<<<dim3(g.phase, nbox), 256, 0, L.s>>>(d);
-  *L.counter += 7 + (g.excl > 0 ? 1 : 0);
+  *L.counter += 5 + (g.excl > 0 ? 1 : 0);
+  // the FP32-core phase rows (none when every box is on the tensor cores)
+  if (g.charge > 0) {
+    batch_charge_fixed_kernel<<<dim3(g.charge, nbox), 256, 0, L.s>>>(d);
+    ++*L.counter;
+  }
+  if (g.phase > 0) {
+    batch_phase_kernel<<<dim3(g.phase, nbox), 256, 0, L.s>>>(d);
+    ++*L.counter;
+  }
   return cudaGetLastError();
 }
 

@@ -108,15 +108,14 @@ __global__ void __launch_bounds__(256) kf_tc_prep_kernel(int nq, int row, int oz
 // (the arithmetic of charge_fixed_kernel and phase_tables_mixed_kernel, so
 // the values are the same bit for bit), written to the phase table for
 // pass 1 and, through shared memory, to the operand tiles.
-__global__ void __launch_bounds__(256) kf_tc_phase_kernel(KArgs a, const double* __restrict__ r,
-                                                          int KP, int nxy, int KN,
-                                                          float2* __restrict__ tab,
-                                                          float* __restrict__ za,
-                                                          float* __restrict__ zb) {
+__device__ __forceinline__ void kf_tc_phase_body(const KArgs& a_in, const double* __restrict__ r, int KP, int nxy,
+                              int KN, float2* __restrict__ tab, float* __restrict__ za,
+                              float* __restrict__ zb, const int bx_) {
+  const KArgs a = a_in;   // a local copy (see kf_tc_body)
   extern __shared__ float2 st_ph[];   // [32][row]
   __shared__ uint4 sfix[SK_G];
   __shared__ float sq[SK_G];
-  const int g = blockIdx.x, j0 = g * SK_G, row = a.row, Kz = a.Kz;
+  const int g = bx_, j0 = g * SK_G, row = a.row, Kz = a.Kz;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nvalid = min(SK_G, max(0, a.nq - j0));
   if (tid < SK_G) {
@@ -198,9 +197,9 @@ __global__ void __launch_bounds__(256) kf_tc_phase_kernel(KArgs a, const double*
 
 // B operand: per row r the columns 4r .. 4r+3 = coefficients of H.x, H.y,
 // Hz.x, Hz.y over z_j (hi then lo per tile of 32 rows)
-__global__ void kf_tc_vb_kernel(int nrows, int ntn, int Kz, int KP, const KRow* __restrict__ krows,
-                                const float2* __restrict__ W, float* __restrict__ vb) {
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void kf_tc_vb_body(int nrows, int ntn, int Kz, int KP, const KRow* __restrict__ krows,
+                           const float2* __restrict__ W, float* __restrict__ vb, const int bx_) {
+  const long t = (long)bx_ * blockDim.x + threadIdx.x;
   if (t >= (long)ntn * TC_N * KP) return;
   const int n = (int)(t / KP), kk = (int)(t % KP);
   const int r = n / 4, comp = n % 4;
@@ -232,32 +231,27 @@ __global__ void kf_tc_vb_kernel(int nrows, int ntn, int Kz, int KP, const KRow* 
   base[(size_t)TC_N * KP + o] = lo;
 }
 
-struct KfTc {
-  int nq, ns, KP, ntm, ntn, nrows, nxy;
-  const float* za;
-  const float* vb;
-  const TcRow* rows;
-  const int* qsite;
-  const int* qdrude;
-  double Lx, Ly, Lz;
-  double* f;
-  int* status;
-};
-
-// A tile (Z hi | lo, phase block), two V stages, the row table, barriers
+// A tile (Z hi | lo, phase block), two V stages, barriers (nrows: kept for
+// the callers; the row table is read from global memory)
 size_t kf_tc_smem(int KP, int nxy, int nrows) {
-  return (size_t)1024 * (3 * KP + nxy) + (size_t)nrows * sizeof(TcRow) + 128;
+  (void)nrows;
+  return (size_t)1024 * (3 * KP + nxy) + 128;
 }
 
-__global__ void __launch_bounds__(TC_THREADS, 1) kf_tc_kernel(KfTc a) {
+__device__ __forceinline__ void kf_tc_body(const KfTc& a_in, const int bx_) {
+  // a local copy: the stores below cannot alias it, so its fields stay in
+  // registers instead of being reloaded through the reference
+  const KfTc a = a_in;
   extern __shared__ __align__(1024) unsigned char smem_tc[];
   const uint32_t zb = 1024u * a.KP;              // Z tile bytes (hi | lo); also a V tile
   const uint32_t ab = zb + 1024u * a.nxy;        // A tile with the phase block
   unsigned char* As = smem_tc;
   const float2* XY = reinterpret_cast<const float2*>(smem_tc + zb);   // [nxy][128]
   unsigned char* Bs = smem_tc + ab;              // two V stages of zb bytes
-  TcRow* rk = reinterpret_cast<TcRow*>(Bs + 2 * (size_t)zb);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(rk + a.nrows);
+  // the row table is read through L1 (every lane of a warp reads the same
+  // row), which keeps nrows x 16 bytes out of shared memory: boxes up to
+  // |n| <= 23 fit
+  uint64_t* bars = reinterpret_cast<uint64_t*>(Bs + 2 * (size_t)zb);
   uint64_t* bar_a = bars;
   uint64_t* full = bars + 1;    // [2] V stage loaded
   uint64_t* bfree = bars + 3;   // [2] V stage consumed
@@ -265,7 +259,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) kf_tc_kernel(KfTc a) {
   uint64_t* tfree = bars + 7;   // [2] TMEM buffer drained
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 9);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int mt = blockIdx.x;
+  const int mt = bx_;
   constexpr int PW = TC_EPI_WARPS;               // producer warp
 
   if (tid == 0) {
@@ -288,10 +282,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) kf_tc_kernel(KfTc a) {
       const uint32_t half = zb / 2, sbo = (uint32_t)(a.KP / 4) * 128;
       const uint32_t idesc = tc::idesc_tf32(TC_M, TC_N);
       const size_t atile_f = (size_t)2 * TC_M * (a.KP + a.nxy), vtile_f = (size_t)2 * TC_N * a.KP;
-      const uint32_t rbytes = (uint32_t)(a.nrows * sizeof(TcRow));
-      tc::mbar_expect_tx(bar_a, ab + rbytes);
+      tc::mbar_expect_tx(bar_a, ab);
       tc::bulk_g2s(As, a.za + (size_t)mt * atile_f, ab, bar_a);
-      tc::bulk_g2s(rk, a.rows, rbytes, bar_a);
       for (int t = 0; t < 2 && t < a.ntn; t++) {
         tc::mbar_expect_tx(full + t, zb);
         tc::bulk_g2s(Bs + (size_t)t * zb, a.vb + (size_t)t * vtile_f, zb, full + t);
@@ -370,7 +362,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) kf_tc_kernel(KfTc a) {
           const uint32_t* w = &v[i >> 2][4 * (i & 3)];
           const float hx = __uint_as_float(w[0]), hy = __uint_as_float(w[1]),
                       zx = __uint_as_float(w[2]), zy = __uint_as_float(w[3]);
-          const TcRow kr = rk[r];
+          const int4 kq = __ldg(reinterpret_cast<const int4*>(a.rows) + r);
+          const TcRow kr{__int_as_float(kq.x), __int_as_float(kq.y), kq.z, kq.w};
           if (kr.ox != cur_ox) {
             cur_ox = kr.ox;
             X = XY[kr.ox + m];
@@ -466,14 +459,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) kf_tc_kernel(KfTc a) {
 // TF32 as three products.  CTA (row tile, charge chunk); the chunk's partial
 // S go to part[chunk][k], summed in FP64 by the reduce kernel.
 
-struct SkTc {
-  int KP, KN, Kz, nrows, nrt, ngroups, gpc, row, oyl, nk;
-  const float2* tab;   // phase rows, zero-padded to whole groups of 32 charges
-  const float* zb;     // Z^T tiles
-  const KRow* krows;
-  float2* part;
-  int* status;
-};
 
 __host__ __device__ size_t sk_tc_stage(int KN, int row) {
   const size_t b = (size_t)2 * 128 * SK_G * 4 + (size_t)256 * KN + (size_t)256 * row;
@@ -483,7 +468,8 @@ size_t sk_tc_smem(int KN, int row) {
   return SK_NS * sk_tc_stage(KN, row) + SK_R * sizeof(KRow) + 128;
 }
 
-__global__ void __launch_bounds__(SK_THREADS, 1) sk_tc_kernel(SkTc a) {
+__device__ __forceinline__ void sk_tc_body(const SkTc& a_in, const int bx_) {
+  const SkTc a = a_in;   // a local copy (see kf_tc_body)
   extern __shared__ __align__(1024) unsigned char smem_sk[];
   const size_t stb = sk_tc_stage(a.KN, a.row);
   const uint32_t abytes = 2 * 128 * SK_G * 4;             // A tile, hi | lo
@@ -497,7 +483,7 @@ __global__ void __launch_bounds__(SK_THREADS, 1) sk_tc_kernel(SkTc a) {
   uint64_t* tfree = tfull + 2;           // [2] TMEM buffer b drained
   uint32_t* tslot = reinterpret_cast<uint32_t*>(tfree + 2);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int rt = blockIdx.x % a.nrt, ch = blockIdx.x / a.nrt;
+  const int rt = bx_ % a.nrt, ch = bx_ / a.nrt;
   const int g0 = ch * a.gpc, ng = min(a.gpc, a.ngroups - g0), r0 = rt * SK_R;
   auto stage = [&](int s) { return smem_sk + (size_t)s * stb; };
 
@@ -701,41 +687,6 @@ size_t sk_tc_zb_floats(const KArgs& a) {
   return (size_t)ntm * (TC_M / SK_G) * 2 * SK_G * sk_tc_kn(a);
 }
 
-// charge chunks of the grid: about one CTA per SM over all row tiles
-void sk_tc_split(const KArgs& a, int nrows, int nsm, int* nch, int* gpc) {
-  const int nrt = (nrows + SK_R - 1) / SK_R, ngroups = (a.nq + SK_G - 1) / SK_G;
-  int c = std::max(1, std::min(ngroups, nsm / nrt));
-  *gpc = (ngroups + c - 1) / c;
-  *nch = (ngroups + *gpc - 1) / *gpc;
-}
-
-cudaError_t k_sk_tc(const Launch& L, const KArgs& a, int nrows, int nch, int gpc,
-                    const float2* tab, const float* zb, float2* part) {
-  SkTc k;
-  k.KP = kf_tc_kp(a);
-  k.KN = sk_tc_kn(a);
-  k.Kz = a.Kz;
-  k.nrows = nrows;
-  k.nrt = (nrows + SK_R - 1) / SK_R;
-  k.ngroups = (a.nq + SK_G - 1) / SK_G;
-  k.gpc = gpc;
-  k.row = a.row;
-  k.oyl = a.Kx + 1 + a.Ky;
-  k.nk = a.nk;
-  k.tab = tab;
-  k.zb = zb;
-  k.krows = a.krows;
-  k.part = part;
-  k.status = a.status;
-  const size_t smem = sk_tc_smem(k.KN, a.row);
-  cudaError_t e =
-      cudaFuncSetAttribute(sk_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  sk_tc_kernel<<<k.nrt * nch, SK_THREADS, smem, L.s>>>(k);
-  ++*L.counter;
-  return cudaGetLastError();
-}
-
 int kf_tc_kp(const KArgs& a) { return ((2 * a.Kz + 1) + 7) / 8 * 8; }
 
 bool kf_tc_fits(const KArgs& a, int nrows) {
@@ -759,22 +710,6 @@ void kf_tc_rows(const KArgs& a, const std::vector<KRow>& krows, std::vector<TcRo
     out->push_back(TcRow{(float)r.kx, (float)r.ky, r.kx * TC_M, (oyl + r.ky) * TC_M});
 }
 
-cudaError_t k_kf_tc_phase(const Launch& L, const KArgs& a, const double* r, float2* tab,
-                          float* za, float* zb) {
-  const int KP = kf_tc_kp(a), ntm = (a.nq + TC_M - 1) / TC_M;
-  const int nxy = (a.Kx + 1) + (2 * a.Ky + 1);
-  const size_t smem = sizeof(float2) * SK_G * (size_t)a.row;
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(kf_tc_phase_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-  }
-  kf_tc_phase_kernel<<<ntm * (TC_M / SK_G), 256, smem, L.s>>>(a, r, KP, nxy, sk_tc_kn(a), tab,
-                                                              za, zb);
-  ++*L.counter;
-  return cudaGetLastError();
-}
-
 cudaError_t k_kf_tc_za(const Launch& L, const KArgs& a, const float2* tab, float* za, float* zb) {
   const int KP = kf_tc_kp(a), ntm = (a.nq + TC_M - 1) / TC_M;
   const int nxy = (a.Kx + 1) + (2 * a.Ky + 1);
@@ -790,24 +725,57 @@ cudaError_t k_kf_tc_za(const Launch& L, const KArgs& a, const float2* tab, float
   return cudaGetLastError();
 }
 
-cudaError_t k_kf_tc(const Launch& L, const KArgs& a, int nrows, const KRow* tckrows,
-                    const TcRow* rows, const float* za, float* vb) {
-  const int KP = kf_tc_kp(a), ntm = (a.nq + TC_M - 1) / TC_M;
-  const int ntn = (4 * nrows + TC_N - 1) / TC_N;
-  const long nv = (long)ntn * TC_N * KP;
-  kf_tc_vb_kernel<<<(int)((nv + 255) / 256), 256, 0, L.s>>>(nrows, ntn, a.Kz, KP, tckrows, a.Wf,
-                                                           vb);
-  ++*L.counter;
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  KfTc k;
+void sk_tc_split(const KArgs& a, int nrows, int* nch, int* gpc) {
+  const int nrt = (nrows + SK_R - 1) / SK_R, ngroups = (a.nq + SK_G - 1) / SK_G;
+  const int c = std::max(1, std::min(ngroups / 64, PARTITION_SMS / nrt));
+  *gpc = (ngroups + c - 1) / c;
+  *nch = (ngroups + *gpc - 1) / *gpc;
+}
+
+void tc_box(const KArgs& a, int nrows, int nch, int gpc, const KRow* tckrows, const TcRow* rows,
+            const double* r, float2* tab, float* za, float* zb, float* vb, float2* part,
+            TcBox* out) {
+  TcBox& b = *out;
+  b = TcBox{};
+  b.ka = a;
+  b.r = r;
+  b.tab = tab;
+  b.za = za;
+  b.zb = zb;
+  b.KP = kf_tc_kp(a);
+  b.nxy = (a.Kx + 1) + (2 * a.Ky + 1);
+  b.KN = sk_tc_kn(a);
+  const int ntm = (a.nq + TC_M - 1) / TC_M;
+  b.g_phase = ntm * (TC_M / SK_G);
+  b.smem_phase = sizeof(float2) * SK_G * (size_t)a.row;
+  if (zb) {
+    SkTc& k = b.sk;
+    k.KP = b.KP;
+    k.KN = b.KN;
+    k.Kz = a.Kz;
+    k.nrows = nrows;
+    k.nrt = (nrows + SK_R - 1) / SK_R;
+    k.ngroups = (a.nq + SK_G - 1) / SK_G;
+    k.gpc = gpc;
+    k.row = a.row;
+    k.oyl = a.Kx + 1 + a.Ky;
+    k.nk = a.nk;
+    k.tab = tab;
+    k.zb = zb;
+    k.krows = a.krows;
+    k.part = part;
+    k.status = a.status;
+    b.g_sk = k.nrt * nch;
+    b.smem_sk = sk_tc_smem(k.KN, a.row);
+  }
+  KfTc& k = b.kf;
   k.nq = a.nq;
   k.ns = a.ns;
-  k.KP = KP;
+  k.KP = b.KP;
   k.ntm = ntm;
-  k.ntn = ntn;
+  k.ntn = (4 * nrows + TC_N - 1) / TC_N;
   k.nrows = nrows;
-  k.nxy = (a.Kx + 1) + (2 * a.Ky + 1);
+  k.nxy = b.nxy;
   k.za = za;
   k.vb = vb;
   k.rows = rows;
@@ -818,10 +786,75 @@ cudaError_t k_kf_tc(const Launch& L, const KArgs& a, int nrows, const KRow* tckr
   k.Lz = a.Lz;
   k.f = a.f;
   k.status = a.status;
-  const size_t smem = kf_tc_smem(KP, k.nxy, nrows);
-  e = cudaFuncSetAttribute(kf_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  b.tckrows = tckrows;
+  b.vb = vb;
+  b.g_vb = (int)(((long)k.ntn * TC_N * b.KP + 255) / 256);
+  b.g_kf = ntm;
+  b.smem_kf = kf_tc_smem(b.KP, b.nxy, nrows);
+}
+
+// ---------------------------------------------------------------- launches --
+//
+// The tensor-core passes of a list of boxes, one launch each (blockIdx.y =
+// box; CTAs beyond a box's own grid return before they touch TMEM or a
+// barrier).  A single box is a list of one: a box of a batch runs the same
+// kernel with the same arguments as the box alone, so it gets the same
+// results bit for bit.
+
+__global__ void __launch_bounds__(256) batch_tc_phase_kernel(const TcBox* __restrict__ B) {
+  const TcBox& b = B[blockIdx.y];
+  if ((int)blockIdx.x >= b.g_phase) return;
+  kf_tc_phase_body(b.ka, b.r, b.KP, b.nxy, b.KN, b.tab, b.za, b.zb, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(SK_THREADS, 1) batch_sk_tc_kernel(const TcBox* __restrict__ B) {
+  const TcBox& b = B[blockIdx.y];
+  if ((int)blockIdx.x >= b.g_sk) return;
+  sk_tc_body(b.sk, blockIdx.x);
+}
+
+__global__ void batch_tc_vb_kernel(const TcBox* __restrict__ B) {
+  const TcBox& b = B[blockIdx.y];
+  if ((int)blockIdx.x >= b.g_vb) return;
+  kf_tc_vb_body(b.kf.nrows, b.kf.ntn, b.ka.Kz, b.KP, b.tckrows, b.ka.Wf, b.vb, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1) batch_kf_tc_kernel(const TcBox* __restrict__ B) {
+  const TcBox& b = B[blockIdx.y];
+  if ((int)blockIdx.x >= b.g_kf) return;
+  kf_tc_body(b.kf, blockIdx.x);
+}
+
+cudaError_t k_batch_tc_phase(const Launch& L, const TcBox* d, int nbox, int grid, size_t smem) {
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(batch_tc_phase_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  batch_tc_phase_kernel<<<dim3(grid, nbox), 256, smem, L.s>>>(d);
+  ++*L.counter;
+  return cudaGetLastError();
+}
+
+cudaError_t k_batch_sk_tc(const Launch& L, const TcBox* d, int nbox, int grid, size_t smem) {
+  cudaError_t e = cudaFuncSetAttribute(batch_sk_tc_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  kf_tc_kernel<<<ntm, TC_THREADS, smem, L.s>>>(k);
+  batch_sk_tc_kernel<<<dim3(grid, nbox), SK_THREADS, smem, L.s>>>(d);
+  ++*L.counter;
+  return cudaGetLastError();
+}
+
+cudaError_t k_batch_kf_tc(const Launch& L, const TcBox* d, int nbox, int gvb, int gkf,
+                          size_t smem) {
+  batch_tc_vb_kernel<<<dim3(gvb, nbox), 256, 0, L.s>>>(d);
+  ++*L.counter;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(batch_kf_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem);
+  if (e != cudaSuccess) return e;
+  batch_kf_tc_kernel<<<dim3(gkf, nbox), TC_THREADS, smem, L.s>>>(d);
   ++*L.counter;
   return cudaGetLastError();
 }

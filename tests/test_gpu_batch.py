@@ -43,15 +43,18 @@ def test_batch_md_equals_single_boxes(precision):
     batch.close()
 
 
-def test_fused_batch_md_equals_single_boxes():
-    """boxes on the FP32 path with the Ewald passes on the FP32 cores: one
-    launch per kernel over all boxes (blockIdx.y = box); every box gets the
-    positions, velocities and energies it gets alone, bit for bit, and the
-    launches per step do not grow with the number of boxes"""
+@pytest.mark.parametrize("engine", [1, 0])
+def test_fused_batch_md_equals_single_boxes(engine):
+    """boxes on the FP32 path with the Ewald passes on the FP32 cores (1) or
+    the tensor cores (0): one launch per kernel over all boxes (blockIdx.y =
+    box); every box gets the positions, velocities and energies it gets
+    alone, bit for bit, and the launches per step do not grow with the
+    number of boxes"""
     launches = {}
     for n in (3, 7):
         bs = boxes(n, seed=13)
-        batch = M.Batch([dict(args(b), kspace_engine=1) for b in bs], precision="mixed", lanes=3)
+        batch = M.Batch([dict(args(b), kspace_engine=engine) for b in bs], precision="mixed",
+                        lanes=3)
         for i, b in enumerate(bs):
             batch.box[i].md_set_state(b["r"], b["r1"])
         en = batch.md_steps(6)
@@ -59,7 +62,7 @@ def test_fused_batch_md_equals_single_boxes():
         batch.md_steps(2, measure=False)
         launches[n] = batch.launches
         for i, b in enumerate(bs):
-            a = dict(args(b), kspace_engine=1)
+            a = dict(args(b), kspace_engine=engine)
             fp = M.ForcePath(a.pop("system"), a.pop("L"), a.pop("cutoff"), a.pop("alpha"),
                              a.pop("kappa"), precision="mixed", **a)
             fp.md_set_state(b["r"], b["r1"])
