@@ -491,8 +491,42 @@ def run_batch(args, rank, world, local):
     barrier()
     e2e_s = time.perf_counter() - t0
     nbytes = sum(a.nbytes + b.nbytes for a, b in host)
-    peak = M.fp32_peak_tflops()
-    nkq = sum((b["kn"] ** 3) * 2.1 * b["system"].ns for b in boxes)
+    # per stage of the fused step (CUDA events between the launches), and
+    # the roofline of the stage with the largest share: its algorithmic
+    # work over its time (Ewald passes: 8 flops per (k-vector, charge), on
+    # the tensor cores as TF32 products, three MMAs per product, at half
+    # the bf16 rate; the pair terms: 45 flops per in-cutoff pair, FP32)
+    for i in range(len(boxes)):
+        bm.box[i].md_set_state(*states[i])
+    stages = bm.profile(5) if bm.fused else {}
+    fp32_peak = M.fp32_peak_tflops()
+    nkq = sum(bm.box[i].nkvec * int((b["system"].q != 0).sum()) for i, b in enumerate(boxes))
+    npair = sum(b["system"].ns * (b["system"].ns - 1) / 2 *
+                (4.0 / 3.0 * math.pi * b["cutoff"] ** 3) / np.prod(np.broadcast_to(b["L"], 3))
+                for b in boxes)
+    roof = None
+    if stages:
+        top = max(stages, key=stages.get)
+        t_top = stages[top] * 1e-3
+        if top in ("ewald_sk", "ewald_kforce"):
+            peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json"))) \
+                if os.path.exists(os.path.join(REPO, "MEASURED_PEAKS.json")) else {}
+            bf16 = peaks.get("bf16_tflops", 1900.0)
+            achieved = FLOP_PER_KQ * nkq / t_top / 1e12
+            roof = {"bound": "tensor", "kernel": "batch " + top, "achieved": round(achieved, 3),
+                    "peak": bf16, "unit": "TFLOP/s", "frac": round(achieved / bf16, 4),
+                    "traffic": None, "avg_launch_ms": round(stages[top], 4),
+                    "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst) %s; the passes run "
+                                   "TF32 products (half the bf16 rate), three MMAs each" % (
+                                       "measured" if peaks else "fallback")}
+        else:
+            achieved = (FLOP_PER_PAIR * npair if top == "pair" else 0.0) / t_top / 1e12
+            roof = {"bound": "fp32", "kernel": "batch " + top, "achieved": round(achieved, 3),
+                    "peak": round(fp32_peak, 3), "unit": "TFLOP/s",
+                    "frac": round(achieved / fp32_peak, 4), "traffic": None,
+                    "avg_launch_ms": round(stages[top], 4),
+                    "peak_source": "measured FP32 FMA loop (mg_probe_fp32_tflops)"}
+    shares = {k: round(v / max(sum(stages.values()), 1e-30), 4) for k, v in stages.items()}
     if rank == 0:
         print(json.dumps({
             "metric": METRIC, "value": round(value, 4), "unit": "ns/day", "n_gpus": world,
@@ -517,12 +551,10 @@ def run_batch(args, rank, world, local):
             "e2e": {"value": round(ns_per_day(h, ke, e2e_s), 4), "unit": "ns/day",
                     "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "steps": ke},
             "gpu_launches": launches,
-            "roofline": {"bound": "fp32", "kernel": "whole step (k-space products)",
-                         "achieved": round(2 * FLOP_PER_KQ * nkq / (ms / args.steps * 1e-3) / 1e12, 3),
-                         "peak": round(peak, 3), "unit": "TFLOP/s",
-                         "frac": round(2 * FLOP_PER_KQ * nkq / (ms / args.steps * 1e-3) / 1e12 / peak, 4),
-                         "traffic": None,
-                         "peak_source": "measured FP32 FMA loop (mg_probe_fp32_tflops)"},
+            "roofline": roof,
+            "kernel_share": shares,
+            "kernel_share_note": "stages of the fused step (one launch per kernel over all "
+                                 "boxes), CUDA events between the launches, 5 steps",
             "clocks": clk, "cpu_baseline": None,
         }), flush=True)
     bm.close()

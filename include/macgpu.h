@@ -434,15 +434,24 @@ mg_ctx *mg_batch_box(mg_batch *b, int i);
 /* kernels launched by the last batch call (graph nodes counted per step) */
 int mg_batch_last_launches(const mg_batch *b);
 /* en: NULL or [nbox] energies of the last step.  When every box runs the
-   FP32 path with the Ewald passes on the FP32 cores (kspace_engine 1), the
-   cell pair kernel with 4 warps (pair_variant 0), cells re-binned every step
-   and no Drude charges, dependants, thermostat, drmax, drift removal or
-   dipole term, a step is one launch per kernel over all boxes (blockIdx.y =
-   box, each box with its single-launch arguments, so its results are those
-   of the box run alone); otherwise one graph node per box kernel. */
+   FP32 path with both Ewald passes on the FP32 cores or both on the tensor
+   cores (kspace_engine 1 or 0; under 0 a box whose tiles do not fit runs on
+   the FP32 cores), the cell pair kernel with 4 warps (pair_variant 0),
+   cells re-binned every step and no Drude charges, dependants, thermostat,
+   drmax, drift removal or dipole term, a step is one launch per kernel over
+   all boxes (blockIdx.y = box, each box with its single-launch arguments,
+   so its results are those of the box run alone); otherwise one graph node
+   per box kernel. */
 int mg_batch_md_steps(mg_batch *b, int nsteps, mg_energy *en);
 /* 1 once mg_batch_md_steps has chosen the one-launch-per-kernel form */
 int mg_batch_fused(const mg_batch *b);
+/* No reference counterpart.  nrep further MD steps of a fused batch (no
+   energies), each timed stage by stage with CUDA events; ms[7] gets the
+   mean time per step of: the cell lists; the pair and exclusion terms (with
+   the FP32-core phase rows); the tensor-core phase rows and operand tiles;
+   Ewald pass 1; the S(k) sums; pass 2; the step (SHAKE).  The events sit
+   between launches, so the stages add up to a little more than a step. */
+int mg_batch_profile(mg_batch *b, int nrep, double ms[7]);
 /* probes: one ghost for all boxes (probe_per_box = 0) or [nbox];
    out: [nbox] */
 int mg_batch_widom(mg_batch *b, const mg_probe *probes, int probe_per_box, long long ninsert,

@@ -132,6 +132,7 @@ def library():
         L.mg_nose_state.argtypes = [vp, _dp]
         L.mg_set_graph.argtypes = [vp, C.c_int]
         L.mg_batch_fused.argtypes = [vp]
+        L.mg_batch_profile.argtypes = [vp, C.c_int, _dp]
         L.mg_bounddr_report.argtypes = [vp, C.POINTER(C.c_longlong), _dp]
         L.mg_remove_drift.argtypes = [vp, _dp]
         L.mg_profile_enable.argtypes = [vp, C.c_int]
@@ -618,6 +619,16 @@ class Batch:
     def fused(self):
         """True once MD steps run as one launch per kernel over all boxes"""
         return bool(library().mg_batch_fused(self._b))
+
+    PROFILE_STAGES = ("cell_list", "pair", "phase_tc", "ewald_sk", "ewald_sk_reduce",
+                      "ewald_kforce", "shake")
+
+    def profile(self, nrep=5):
+        """nrep further MD steps of the fused batch timed stage by stage:
+        {stage: ms per step} (mg_batch_profile)"""
+        ms = np.zeros(7)
+        self._check(library().mg_batch_profile(self._b, int(nrep), ms.ctypes.data_as(_dp)))
+        return dict(zip(self.PROFILE_STAGES, ms.tolist()))
 
     def md_steps(self, n, measure=True):
         en = (Energy * self.nbox)()

@@ -2735,21 +2735,34 @@ int build_fused(mg_batch* b) {
 }
 
 // one MD step of every box with the batched kernels, on the batch stream
-int fused_step_enqueue(mg_batch* b, bool measure) {
+// with ev (profiling, not captured): an event recorded after each of the
+// seven stages (cell list; pair terms; phase rows and operand tiles; pass 1;
+// S(k) sums; pass 2; the step) and one before them
+int fused_step_enqueue(mg_batch* b, bool measure, cudaEvent_t* ev = nullptr) {
   const int nbox = (int)b->box.size();
   Launch L{b->main, &b->launches_fused};
   const BatchGrid& g = b->grid;
+  auto mark = [&](int k) { return ev ? cudaEventRecord(ev[k], b->main) : cudaSuccess; };
   // the order of a single box's serial chain: cell list, pair and
   // exclusion terms, phase rows (with the operand tiles), pass 1, its sum,
   // pass 2, the step
-  BCK(k_batch_rspace(L, b->d_steps, nbox, g, measure));
+  BCK(mark(0));
+  BCK(k_batch_cells(L, b->d_steps, nbox, g));
+  BCK(mark(1));
+  BCK(k_batch_pairs(L, b->d_steps, nbox, g, measure));
+  BCK(mark(2));
   if (g.any_tc) BCK(k_batch_tc_phase(L, b->d_tc, nbox, g.tc_phase, g.tc_phase_smem));
+  BCK(mark(3));
   if (g.any_fp32) BCK(k_batch_pass1(L, b->d_steps, nbox, g));
   if (g.any_tc) BCK(k_batch_sk_tc(L, b->d_tc, nbox, g.tc_sk, g.tc_sk_smem));
+  BCK(mark(4));
   BCK(k_batch_sk_reduce(L, b->d_steps, nbox, g, measure));
+  BCK(mark(5));
   if (g.any_fp32) BCK(k_batch_pass2(L, b->d_steps, nbox, g));
   if (g.any_tc) BCK(k_batch_kf_tc(L, b->d_tc, nbox, g.tc_vb, g.tc_kf, g.tc_kf_smem));
+  BCK(mark(6));
   BCK(k_batch_step(L, b->d_steps, nbox, g, measure));
+  BCK(mark(7));
   return MG_OK;
 }
 
@@ -2775,6 +2788,37 @@ int capture_fused(mg_batch* b, bool measure, cudaGraphExec_t* out) {
 }  // namespace
 
 int mg_batch_fused(const mg_batch* b) { return b && b->fused_ok == 1 ? 1 : 0; }
+
+int mg_batch_profile(mg_batch* b, int nrep, double ms[7]) {
+  if (!b || !ms || nrep < 1) return bfail(b, MG_ERR_ARG, "bad arguments");
+  if (b->fused_ok != 1) return bfail(b, MG_ERR_ARG, "the batch does not run the fused step");
+  for (int k = 0; k < 7; k++) ms[k] = 0;
+  cudaEvent_t ev[8] = {};
+  for (int k = 0; k < 8; k++)
+    if (cudaEventCreate(&ev[k]) != cudaSuccess) {
+      for (int j = 0; j < k; j++) cudaEventDestroy(ev[j]);
+      return bfail(b, MG_ERR_CUDA, "profile events");
+    }
+  int rc = MG_OK;
+  for (int r = 0; r < nrep && rc == MG_OK; r++) {
+    rc = fused_step_enqueue(b, false, ev);
+    if (rc == MG_OK && cudaEventSynchronize(ev[7]) != cudaSuccess)
+      rc = bfail(b, MG_ERR_CUDA, "profile step");
+    for (int k = 0; k < 7 && rc == MG_OK; k++) {
+      float t = 0;
+      cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+      ms[k] += t / nrep;
+    }
+  }
+  for (int k = 0; k < 8; k++) cudaEventDestroy(ev[k]);
+  if (rc == MG_OK) {
+    for (mg_ctx* c : b->box) {
+      c->last_r = c->d_r;
+      c->have_cells = true;
+    }
+  }
+  return rc;
+}
 
 int mg_batch_md_steps(mg_batch* b, int nsteps, mg_energy* en) {
   if (!b || nsteps < 0) return bfail(b, MG_ERR_ARG, "bad arguments");

@@ -414,11 +414,13 @@ struct BatchGrid {
   size_t tc_phase_smem, tc_sk_smem, tc_kf_smem;
   bool any_fp32, any_tc;
 };
-// the force evaluation up to Ewald pass 1 (cell list, pair and exclusion
-// kernels, phase rows), then pass 1 (mg_kspace.cu), then the S(k) sums and
-// pass 2; then the step (SHAKE and, measured, the sums)
-cudaError_t k_batch_rspace(const Launch& L, const BoxStep* d, int nbox, const BatchGrid& g,
-                           bool measure);
+// the force evaluation up to Ewald pass 1 (the cell list; the pair and
+// exclusion kernels and the FP32-core phase rows), then pass 1
+// (mg_kspace.cu), then the S(k) sums and pass 2; then the step (SHAKE and,
+// measured, the sums)
+cudaError_t k_batch_cells(const Launch& L, const BoxStep* d, int nbox, const BatchGrid& g);
+cudaError_t k_batch_pairs(const Launch& L, const BoxStep* d, int nbox, const BatchGrid& g,
+                          bool measure);
 cudaError_t k_batch_pass1(const Launch& L, const BoxStep* d, int nbox, const BatchGrid& g);
 cudaError_t k_batch_sk_reduce(const Launch& L, const BoxStep* d, int nbox, const BatchGrid& g,
                               bool measure);

@@ -2210,12 +2210,17 @@ __global__ void batch_reduce_kernel(const BoxStep* __restrict__ B, int k0, int k
     reduce_rows_kernel_body(e.rpart[k], e.rrows[k], e.rwidth[k], e.rout[k], 0, 0);
 }
 
-cudaError_t k_batch_rspace(const Launch& L, const BoxStep* d, int nbox, const BatchGrid& g,
-                           bool measure) {
+cudaError_t k_batch_cells(const Launch& L, const BoxStep* d, int nbox, const BatchGrid& g) {
   batch_cell_count_kernel<<<dim3(g.site, nbox), 256, 0, L.s>>>(d);
   batch_cell_scan_kernel<<<dim3(1, nbox), SCAN_THREADS, 0, L.s>>>(d);
   batch_cell_scatter_kernel<<<dim3(g.site, nbox), 256, 0, L.s>>>(d);
   batch_cell_order_kernel<<<dim3(g.order, nbox), ORDER_THREADS, 0, L.s>>>(d);
+  *L.counter += 4;
+  return cudaGetLastError();
+}
+
+cudaError_t k_batch_pairs(const Launch& L, const BoxStep* d, int nbox, const BatchGrid& g,
+                          bool measure) {
   cudaError_t e = cudaSuccess;
   if (measure) {
     if (g.pair_smem > 48 * 1024)
@@ -2233,7 +2238,7 @@ cudaError_t k_batch_rspace(const Launch& L, const BoxStep* d, int nbox, const Ba
     if (g.excl > 0) batch_excl_kernel<false><<<dim3(g.excl, nbox), EXCL_THREADS, 0, L.s>>>(d);
   }
   if (e != cudaSuccess) return e;
-  *L.counter += 5 + (g.excl > 0 ? 1 : 0);
+  *L.counter += 1 + (g.excl > 0 ? 1 : 0);
   // the FP32-core phase rows (none when every box is on the tensor cores)
   if (g.charge > 0) {
     batch_charge_fixed_kernel<<<dim3(g.charge, nbox), 256, 0, L.s>>>(d);

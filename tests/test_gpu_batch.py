@@ -118,3 +118,28 @@ def test_batch_requires_state():
     with pytest.raises(M.MGError):
         batch.md_steps(1)
     batch.close()
+
+
+def test_batch_profile_stages():
+    """mg_batch_profile: the fused step stage by stage; every stage runs
+    (its time is positive) and the steps it takes are ordinary MD steps"""
+    bs = boxes(4, seed=17)
+    batch = M.Batch([dict(args(b), kspace_engine=0) for b in bs], precision="mixed", lanes=2)
+    for i, b in enumerate(bs):
+        batch.box[i].md_set_state(b["r"], b["r1"])
+    batch.md_steps(2, measure=False)
+    assert batch.fused
+    st = batch.profile(3)
+    assert set(st) == set(M.Batch.PROFILE_STAGES)
+    for k in ("cell_list", "pair", "ewald_sk", "ewald_sk_reduce", "ewald_kforce", "shake"):
+        assert st[k] > 0, k
+    # the profiled steps advanced the boxes like md_steps: the same state as
+    # 2 + 3 plain steps from the start
+    ref = M.Batch([dict(args(b), kspace_engine=0) for b in bs], precision="mixed", lanes=2)
+    for i, b in enumerate(bs):
+        ref.box[i].md_set_state(b["r"], b["r1"])
+    ref.md_steps(5, measure=False)
+    for i in range(len(bs)):
+        assert np.array_equal(batch.box[i].md_get_state()[0], ref.box[i].md_get_state()[0])
+    batch.close()
+    ref.close()
