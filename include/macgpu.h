@@ -119,9 +119,9 @@ typedef struct {
      sites; neighbours pruned against the group's bounding box; needs a grid
      of at least 2 cdiv + 1 cells per edge, else the cell kernel runs);
      9 = the group kernel with Newton's third law (every pair once, over a
-     half-shell stencil; forces summed in 64-bit fixed point, 2^-32 K/A,
-     by integer atomics, so still reproducible bit for bit; Drude builds run
-     variant 8 instead);
+     half-shell stencil; forces, of the shells too, summed in 64-bit fixed
+     point, 2^-32 K/A, by integer atomics, so still reproducible bit for
+     bit);
      otherwise the cell kernel with bit 0 = 8 warps per home cell (else 4),
      bit 2 = 16 warps per home cell (over bit 0), bit 1 = the erfc force
      spline in shared memory (else read through L1).  mg_autotune picks it. */
@@ -384,11 +384,12 @@ int mg_xwidom(mg_ctx *ctx, int nlist, const int *mols, const int *vtype, const d
    split (kspace_ctas_per_sm 6, 10, 16) and writes the fastest pair into
    *par, then the fastest of the 8 cell-kernel pair_variant values at that
    choice, of the group kernel (pair_variant 8) at every subdivision and,
-   on the FP32 path without Drude shells, of its half-shell form
-   (pair_variant 9) at every subdivision, each timed (FP32 path) with
+   on the FP32 path, of its half-shell form (pair_variant 9) at every
+   subdivision, each timed (FP32 path) with
    kspace_serial 0 and 1, the pair chosen together.  Builds and frees its
    own trial contexts; ms[25] (optional) gets the time per evaluation of
-   each trial (cdiv-major, then the 8 cell-kernel variants, the group
+   each trial (the best of three blocks of nrep evaluations; cdiv-major,
+   then the 8 cell-kernel variants, the group
    kernel at cdiv 1..3 and the half-shell group kernel at cdiv 1..3, the
    faster of the two kspace_serial settings each, then the chosen variant
    with kspace_serial 0 and 1; -1 if that grid is not possible or the trial

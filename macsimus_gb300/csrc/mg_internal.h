@@ -418,6 +418,8 @@ struct BatchGrid {
 // exclusion kernels and the FP32-core phase rows), then pass 1
 // (mg_kspace.cu), then the S(k) sums and pass 2; then the step (SHAKE and,
 // measured, the sums)
+// out[i] = *p[i] for the n status words of a batch's boxes
+cudaError_t k_gather_status(cudaStream_t s, const int* const* p, int n, int* out);
 cudaError_t k_batch_cells(const Launch& L, const BoxStep* d, int nbox, const BatchGrid& g);
 cudaError_t k_batch_pairs(const Launch& L, const BoxStep* d, int nbox, const BatchGrid& g,
                           bool measure);

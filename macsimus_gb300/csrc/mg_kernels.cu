@@ -821,10 +821,33 @@ __device__ __forceinline__ float pair_force_rn(const PairFS& P, float rr,
   return __fmaf_rn(__fmaf_rn(d.y, rcp_approx(__fadd_rn(d.z, rr)), d.x), P.qq, flj);
 }
 
+// the Drude terms of a pair in the half-shell kernel, every rounding
+// explicit: (charge product) x (d.x + d.y / (d.z + r^2)) at the separation
+// (ex, ey, ez); e: its energy when measuring
+template <bool MEASURE>
+__device__ __forceinline__ float drude_force_rn(const float4* __restrict__ erd,
+                                                const float4* __restrict__ eru, float ex,
+                                                float ey, float ez, float sgrid, int ntab,
+                                                float q, float& e) {
+  const float r2 = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, __fmul_rn(ez, ez)));
+  const int ix = min(__float_as_int(__fmaf_rn(r2, sgrid, 12582911.5f)) - 0x4B400000, ntab - 1);
+  const float4 d = __ldg(erd + ix);
+  if (MEASURE) {
+    float ee = 0.f;
+    spline_any<true, true>(erd, eru, r2, sgrid, ntab, q, ee);
+    e += ee;
+  }
+  return __fmul_rn(__fmaf_rn(d.y, rcp_approx(__fadd_rn(d.z, r2)), d.x), q);
+}
+
 // 7 CTAs per SM (72 registers, no spills): measured faster than 8 (64) and
-// than no bound (95)
-template <bool MEASURE, int NW>
-__global__ void __launch_bounds__(NW * 32, MEASURE ? 1 : 7)
+// than no bound (95).  POLAR (Drude shells): four charge terms per pair,
+// forces on both centres and both shells; the neighbour's six components
+// (centre x y z, shell x y z) are reduce-scattered over the 8 home lanes
+// in three levels (keeping 4, 2, 1 of 8 padded components), so lane i ends
+// with component i and lanes 0..5 write them
+template <bool MEASURE, bool POLAR, int NW>
+__global__ void __launch_bounds__(NW * 32, MEASURE ? 1 : (POLAR ? 5 : 7))
     pair_half_mixed_kernel(PairArgs a, const int4* __restrict__ pj,
                            const PairF* __restrict__ ptab_g, const float4* __restrict__ erd,
                            const float4* __restrict__ eru, float sx, float sy, float sz, float cq,
@@ -832,6 +855,7 @@ __global__ void __launch_bounds__(NW * 32, MEASURE ? 1 : 7)
   constexpr int NT = NW * 32;
   extern __shared__ float4 dyn_smem[];   // the nk x nk FP32 pair table
   __shared__ float4 sj[NW][32];
+  __shared__ float4 sjd[POLAR ? NW : 1][32];
   __shared__ int sjt[NW][32];
   __shared__ double ered[NT];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -844,11 +868,14 @@ __global__ void __launch_bounds__(NW * 32, MEASURE ? 1 : 7)
   const int ncell = a.ncx * a.ncy * a.ncz;
   const int nitems = a.gstart[ncell];
   unsigned long long* facc = reinterpret_cast<unsigned long long*>(a.facc);
-  // reduce-scatter roles: after the three levels lane i holds component
-  // i >> 1 (0 x, 1 y, 2 z, 3 nothing); lanes i = 0, 2, 4 write it
-  const bool b2 = (il & 4) != 0, b1 = (il & 2) != 0;
-  const int comp = il >> 1;
-  const bool jw = !(il & 1) && comp < 3;
+  const long dhalf = 3 * (long)a.ns;   // the shells' sums after the centres'
+  // reduce-scatter roles: without shells lane i ends with component i >> 1
+  // (0 x, 1 y, 2 z, 3 nothing) and lanes i = 0, 2, 4 write it; with shells
+  // lane i ends with component i (0-2 centre, 3-5 shell, 6-7 nothing)
+  const bool b2 = (il & 4) != 0, b1 = (il & 2) != 0, b0 = (il & 1) != 0;
+  const int comp = POLAR ? il : il >> 1;
+  const bool jw = POLAR ? il < 6 : (!b0 && comp < 3);
+  const long joff = POLAR && il >= 3 ? dhalf - 3 : 0;   // shell components
   CSum es[9];
 
   for (int item = blockIdx.x * NW + warp; item < nitems; item += gridDim.x * NW) {
@@ -863,6 +890,7 @@ __global__ void __launch_bounds__(NW * 32, MEASURE ? 1 : 7)
     const bool vi = il < ni;
     const int ti = i0 + il;
     const int4 me = vi ? pj[ti] : make_int4(0, 0, 0, 0);
+    const float4 md = (POLAR && vi) ? a.pdj[ti] : make_float4(0.f, 0.f, 0.f, 0.f);
     const int kind_i = me.w & 255, mol_i = me.w >> 8;
     const float xi = __fmul_rn((float)(int)((unsigned)me.x - refx), sx),
                 yi = __fmul_rn((float)(int)((unsigned)me.y - refy), sy),
@@ -878,7 +906,7 @@ __global__ void __launch_bounds__(NW * 32, MEASURE ? 1 : 7)
       bhy = fmaxf(bhy, __shfl_xor_sync(0xffffffffu, bhy, o));
       bhz = fmaxf(bhz, __shfl_xor_sync(0xffffffffu, bhz, o));
     }
-    CSum fx, fy, fz;
+    CSum fx, fy, fz, gx, gy, gz;
     for (int sp = 0; sp < a.nhspans; sp++) {
       const int4 o = a.hspans[sp];
       int x2 = cx + o.x, y2 = cy + o.y;
@@ -892,7 +920,7 @@ __global__ void __launch_bounds__(NW * 32, MEASURE ? 1 : 7)
       if (za < 0) { ra0 = za + a.ncz; ra1 = a.ncz - 1; rb0 = 0; rb1 = zb; }
       else if (zb >= a.ncz) { ra0 = za; ra1 = a.ncz - 1; rb0 = 0; rb1 = zb - a.ncz; }
       else { ra0 = za; ra1 = zb; }
-      float ax = 0, ay = 0, az = 0;
+      float ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;
       float e_el = 0, e_lj = 0, e_vir = 0;
       PvF pv;
       pv.zero();
@@ -922,6 +950,7 @@ __global__ void __launch_bounds__(NW * 32, MEASURE ? 1 : 7)
             const int slot = __popc(M & ((1u << lane) - 1u));
             sj[warp][slot] = f4;
             sjt[warp][slot] = j;
+            if (POLAR) sjd[warp][slot] = a.pdj[j];
           }
           __syncwarp();
           const int n = __popc(M);
@@ -944,7 +973,46 @@ __global__ void __launch_bounds__(NW * 32, MEASURE ? 1 : 7)
             ax = __fmaf_rn(f, dx, ax);
             ay = __fmaf_rn(f, dy, ay);
             az = __fmaf_rn(f, dz, az);
-            const float px = __fmul_rn(f, dx), py = __fmul_rn(f, dy), pz = __fmul_rn(f, dz);
+            float px = __fmul_rn(f, dx), py = __fmul_rn(f, dy), pz = __fmul_rn(f, dz);
+            // the neighbour's shell (POLAR)
+            float hx = 0.f, hy = 0.f, hz = 0.f;
+            float e_p = 0.f;
+            if (POLAR) {
+              // shell(i) - centre(j), centre(i) - shell(j), shell(i) - shell(j)
+              const float4 qd = sjd[warp][vt ? t : 0];
+              const float ex = __fadd_rn(dx, md.x), ey = __fadd_rn(dy, md.y),
+                          ez = __fadd_rn(dz, md.z);
+              float fp = drude_force_rn<MEASURE>(erd, eru, ex, ey, ez, sgrid, ntab, P.qpc, e_p);
+              const float cx2 = __fadd_rn(dx, -qd.x), cy2 = __fadd_rn(dy, -qd.y),
+                          cz2 = __fadd_rn(dz, -qd.z);
+              float fc = drude_force_rn<MEASURE>(erd, eru, cx2, cy2, cz2, sgrid, ntab, P.qcp,
+                                                 e_p);
+              const float ux = __fadd_rn(ex, -qd.x), uy = __fadd_rn(ey, -qd.y),
+                          uz = __fadd_rn(ez, -qd.z);
+              float fd = drude_force_rn<MEASURE>(erd, eru, ux, uy, uz, sgrid, ntab, P.qpp, e_p);
+              fp = ok ? fp : 0.f;
+              fc = ok ? fc : 0.f;
+              fd = ok ? fd : 0.f;
+              // home centre: + fc (cx2); home shell: + fp (e) + fd (u)
+              ax = __fmaf_rn(fc, cx2, ax);
+              ay = __fmaf_rn(fc, cy2, ay);
+              az = __fmaf_rn(fc, cz2, az);
+              bx = __fmaf_rn(fp, ex, __fmaf_rn(fd, ux, bx));
+              by = __fmaf_rn(fp, ey, __fmaf_rn(fd, uy, by));
+              bz = __fmaf_rn(fp, ez, __fmaf_rn(fd, uz, bz));
+              // neighbour centre: -(f d + fp e); neighbour shell: -(fc cx2 + fd u)
+              px = __fmaf_rn(fp, ex, px);
+              py = __fmaf_rn(fp, ey, py);
+              pz = __fmaf_rn(fp, ez, pz);
+              hx = __fmaf_rn(fc, cx2, __fmul_rn(fd, ux));
+              hy = __fmaf_rn(fc, cy2, __fmul_rn(fd, uy));
+              hz = __fmaf_rn(fc, cz2, __fmul_rn(fd, uz));
+              if (MEASURE && ok) {
+                pv.add(ex, ey, ez, fp);
+                pv.add(cx2, cy2, cz2, fc);
+                pv.add(ux, uy, uz, fd);
+              }
+            }
             if (MEASURE && ok) {
               // energies and virial: no effect on the forces
               const float x = __fdividef(P.Sq, rr), y = x * x * x, xt = rr - P.C2q;
@@ -952,25 +1020,44 @@ __global__ void __launch_bounds__(NW * 32, MEASURE ? 1 : 7)
               e_vir += rr * flj;
               float e_el_p = 0.f;
               spline_any<true, true>(erd, eru, rr, sgrid, ntab, P.qq, e_el_p);
-              e_el += e_el_p;
+              e_el += e_el_p + e_p;
               pv.add(dx, dy, dz, f);
             }
-            // the neighbour's force, minus the sum over the 8 home lanes
-            float k0 = b2 ? pz : px, k1 = b2 ? 0.f : py;
-            const float s0 = b2 ? px : pz, s1 = b2 ? py : 0.f;
-            k0 = __fadd_rn(k0, __shfl_xor_sync(0xffffffffu, s0, 4));
-            k1 = __fadd_rn(k1, __shfl_xor_sync(0xffffffffu, s1, 4));
-            float k = b1 ? k1 : k0;
-            k = __fadd_rn(k, __shfl_xor_sync(0xffffffffu, b1 ? k0 : k1, 2));
-            k = __fadd_rn(k, __shfl_xor_sync(0xffffffffu, k, 1));
+            float k;
+            if (POLAR) {
+              // components 0-5 = (px, py, pz, hx, hy, hz), 6-7 zero; level 1
+              // keeps 4 (xor 4), level 2 keeps 2 (xor 2), level 3 keeps 1
+              const float v0 = b2 ? hy : px, v1 = b2 ? hz : py, v2 = b2 ? 0.f : pz,
+                          v3 = b2 ? 0.f : hx;
+              const float w0 = b2 ? px : hy, w1 = b2 ? py : hz, w2 = b2 ? pz : 0.f,
+                          w3 = b2 ? hx : 0.f;
+              const float k0 = __fadd_rn(v0, __shfl_xor_sync(0xffffffffu, w0, 4)),
+                          k1 = __fadd_rn(v1, __shfl_xor_sync(0xffffffffu, w1, 4)),
+                          k2 = __fadd_rn(v2, __shfl_xor_sync(0xffffffffu, w2, 4)),
+                          k3 = __fadd_rn(v3, __shfl_xor_sync(0xffffffffu, w3, 4));
+              const float m0 = __fadd_rn(b1 ? k2 : k0,
+                                         __shfl_xor_sync(0xffffffffu, b1 ? k0 : k2, 2)),
+                          m1 = __fadd_rn(b1 ? k3 : k1,
+                                         __shfl_xor_sync(0xffffffffu, b1 ? k1 : k3, 2));
+              k = __fadd_rn(b0 ? m1 : m0, __shfl_xor_sync(0xffffffffu, b0 ? m0 : m1, 1));
+            } else {
+              float k0 = b2 ? pz : px, k1 = b2 ? 0.f : py;
+              const float s0 = b2 ? px : pz, s1 = b2 ? py : 0.f;
+              k0 = __fadd_rn(k0, __shfl_xor_sync(0xffffffffu, s0, 4));
+              k1 = __fadd_rn(k1, __shfl_xor_sync(0xffffffffu, s1, 4));
+              k = b1 ? k1 : k0;
+              k = __fadd_rn(k, __shfl_xor_sync(0xffffffffu, b1 ? k0 : k1, 2));
+              k = __fadd_rn(k, __shfl_xor_sync(0xffffffffu, k, 1));
+            }
             if (jw && vt)
-              atomicAdd(facc + 3 * (long)tj + comp,
+              atomicAdd(facc + 3 * (long)tj + comp + joff,
                         (unsigned long long)__float2ll_rn(__fmul_rn(k, -(float)FIX_SCALE)));
           }
           __syncwarp();
         }
       }
       fx.add(ax); fy.add(ay); fz.add(az);
+      if (POLAR) { gx.add(bx); gy.add(by); gz.add(bz); }
       if (MEASURE) {
         es[0].add(e_el); es[1].add(e_lj); es[2].add(e_vir);
         es[3].add(pv.p0); es[4].add(pv.p1); es[5].add(pv.p2);
@@ -978,17 +1065,27 @@ __global__ void __launch_bounds__(NW * 32, MEASURE ? 1 : 7)
       }
     }
     // the home sites' sums: the four s-lanes in a fixed order, then lane
-    // s = 0, 1, 2 adds component x, y, z
-    double g[3] = {fx.value(), fy.value(), fz.value()};
+    // s = 0, 1, 2 adds component x, y, z (of the centre and the shell)
+    double g[6] = {fx.value(), fy.value(), fz.value(), 0, 0, 0};
+    if (POLAR) {
+      g[3] = gx.value();
+      g[4] = gy.value();
+      g[5] = gz.value();
+    }
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
+    for (int k = 0; k < (POLAR ? 6 : 3); k++) {
       g[k] += __shfl_xor_sync(0xffffffffu, g[k], 8);
       g[k] += __shfl_xor_sync(0xffffffffu, g[k], 16);
     }
-    if (vi && sl < 3)
+    if (vi && sl < 3) {
       atomicAdd(facc + 3 * (long)ti + sl,
                 (unsigned long long)__double2ll_rn((sl == 0 ? g[0] : (sl == 1 ? g[1] : g[2])) *
                                                    FIX_SCALE));
+      if (POLAR)
+        atomicAdd(facc + dhalf + 3 * (long)ti + sl,
+                  (unsigned long long)__double2ll_rn(
+                      (sl == 0 ? g[3] : (sl == 1 ? g[4] : g[5])) * FIX_SCALE));
+    }
   }
   if (MEASURE) {
     // every unordered pair once; one row per CTA
@@ -1005,17 +1102,21 @@ __global__ void __launch_bounds__(NW * 32, MEASURE ? 1 : 7)
   }
 }
 
-// the fixed-point sums (sorted order) into the FP64 forces (site order);
-// the sums are cleared for the next evaluation
-__global__ void finish_forces_kernel(int ns, const int* __restrict__ order,
+// the fixed-point sums (sorted order) into the FP64 forces (site order),
+// with shells the second half of each; the sums are cleared for the next
+// evaluation
+__global__ void finish_forces_kernel(int ns, int halves, const int* __restrict__ order,
                                      long long* __restrict__ facc, double* __restrict__ f) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ns) return;
   const int site = order[t];
+  for (int h = 0; h < halves; h++) {
+    const long o = 3 * (long)ns * h;
 #pragma unroll
-  for (int d = 0; d < 3; d++) {
-    f[3 * (long)site + d] = (double)facc[3 * (long)t + d] * (1.0 / FIX_SCALE);
-    facc[3 * (long)t + d] = 0;
+    for (int d = 0; d < 3; d++) {
+      f[o + 3 * (long)site + d] = (double)facc[o + 3 * (long)t + d] * (1.0 / FIX_SCALE);
+      facc[o + 3 * (long)t + d] = 0;
+    }
   }
 }
 
@@ -1026,23 +1127,25 @@ cudaError_t k_pair_mixed(const Launch& L, const PairArgs& a, const int4* pj, con
         sz = (float)(a.Lz / 4294967296.0);
   const float cq = (float)a.cutoff_sq, sg = (float)a.sgrid, al = (float)a.alpha;
   const bool rel = !a.allpairs;
-  if (a.group && a.newton && rel && !polar) {
+  if (a.group && a.newton && rel) {
     const size_t gsm = sizeof(PairFS) * (size_t)a.nkind * a.nkind;
     cudaError_t ge = cudaSuccess;
-#define PAIR_HALF(M)                                                                            \
+#define PAIR_HALF(M, P)                                                                         \
   do {                                                                                          \
     if (gsm > 48 * 1024)                                                                        \
-      ge = cudaFuncSetAttribute(pair_half_mixed_kernel<M, GROUP_WARPS>,                        \
+      ge = cudaFuncSetAttribute(pair_half_mixed_kernel<M, P, GROUP_WARPS>,                     \
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm);         \
     if (ge == cudaSuccess)                                                                      \
-      pair_half_mixed_kernel<M, GROUP_WARPS><<<a.ngrid, GROUP_WARPS * 32, gsm, L.s>>>(         \
+      pair_half_mixed_kernel<M, P, GROUP_WARPS><<<a.ngrid, GROUP_WARPS * 32, gsm, L.s>>>(      \
           a, pj, ptab, erd, eru, sx, sy, sz, cq, sg);                                           \
   } while (0)
-    if (measure) PAIR_HALF(true); else PAIR_HALF(false);
+    if (polar) { if (measure) PAIR_HALF(true, true); else PAIR_HALF(false, true); }
+    else { if (measure) PAIR_HALF(true, false); else PAIR_HALF(false, false); }
 #undef PAIR_HALF
     if (ge != cudaSuccess) return ge;
     LAUNCHED(L);
-    finish_forces_kernel<<<cdiv(a.ns, 256), 256, 0, L.s>>>(a.ns, a.order, a.facc, a.f);
+    finish_forces_kernel<<<cdiv(a.ns, 256), 256, 0, L.s>>>(a.ns, polar ? 2 : 1, a.order, a.facc,
+                                                           a.f);
     LAUNCHED(L);
     return cudaGetLastError();
   }
@@ -2208,6 +2311,17 @@ __global__ void batch_reduce_kernel(const BoxStep* __restrict__ B, int k0, int k
   const BoxStep& e = B[blockIdx.y];
   for (int k = k0; k < k1; k++)
     reduce_rows_kernel_body(e.rpart[k], e.rrows[k], e.rwidth[k], e.rout[k], 0, 0);
+}
+
+__global__ void gather_status_kernel(const int* const* __restrict__ p, int n,
+                                     int* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = *p[i];
+}
+
+cudaError_t k_gather_status(cudaStream_t s, const int* const* p, int n, int* out) {
+  gather_status_kernel<<<cdiv(n, 256), 256, 0, s>>>(p, n, out);
+  return cudaGetLastError();
 }
 
 cudaError_t k_batch_cells(const Launch& L, const BoxStep* d, int nbox, const BatchGrid& g) {

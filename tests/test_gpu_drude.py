@@ -44,6 +44,29 @@ def test_drude_forces(precision):
         assert abs(en["lj"] - eo["lj"]) <= (1e-10 if precision == "fp64" else 1e-5) * abs(eo["lj"])
 
 
+@pytest.mark.parametrize("variant", [8, 9])
+def test_drude_group_kernels(variant):
+    """the group kernel (8) and its half-shell form (9: every pair once, the
+    neighbour's centre and shell forces in fixed point) with Drude shells:
+    the oracle's centre and shell forces, energies and virial, as the cell
+    kernel gives them; bit-reproducible"""
+    g, meta, system, ew, fp, orc = setup("mixed", pair_variant=variant)
+    for d in (1, g["r"].shape[0] - 1):
+        r2 = np.vstack([g["r"][d], g["rD"][d]])
+        f2, en = fp.forces(r2, measure=True)
+        fo, eo = orc.forces(r2, nthreads=4)
+        ns = system.ns
+        assert rel_rms(f2, fo) < MIXED_TOL
+        assert rel_rms(f2[ns:], fo[ns:]) < MIXED_TOL   # the shells alone
+        for k in ("el", "er", "ek"):
+            assert abs(en[k] - eo[k]) <= 2e-6 * abs(eo["eself"]), k
+        assert abs(en["lj"] - eo["lj"]) <= 1e-5 * abs(eo["lj"])
+        for m in range(6):
+            assert abs(en["Pvir"][m] - eo["Pvir"][m]) <= 2e-5 * abs(eo["Pvir"][0]), m
+        f3, _ = fp.forces(r2, measure=True)
+        assert np.array_equal(f3, f2)
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_selffield_iteration(precision):
     g, meta, system, ew, fp, orc = setup(precision)
