@@ -43,6 +43,15 @@ constexpr int SK_PW = 16;             // pass 1: producer warps
 constexpr int SK_THREADS = 32 * (SK_PW + 1);
 constexpr int SK_R = 64;              // pass 1: k rows per tile (re and im: 128 lanes)
 constexpr int SK_NS = 3;              // pass 1: pipeline stages
+// pass 1: the producer warps drain group i - SK_LAG after forming group i's
+// A tile, from SK_TB = SK_LAG + 1 TMEM buffers of 64 columns: the drain
+// reads a group whose products finished long ago, and the products of a
+// group reuse a buffer drained the iteration before, so neither side waits
+#ifndef SK_LAG
+#define SK_LAG 2
+#endif
+constexpr int SK_TB = SK_LAG + 1;
+constexpr uint32_t SK_TCOLS = SK_TB <= 2 ? 128u : 256u;   // allocated TMEM columns
 static_assert(SK_PW == 16, "pass-1 drain: four warps per TMEM lane quarter");
 constexpr int SK_FOLD = 8;            // pass 1: group sums per compensated add
 constexpr int SK_CPT = SK_G * SK_R / (32 * SK_PW);   // pass 1: charges per producer thread
@@ -479,9 +488,9 @@ __device__ __forceinline__ void sk_tc_body(const SkTc& a_in, const int bx_) {
   uint64_t* load = bars;                 // [NS] Z^T + phase rows of a group loaded
   uint64_t* afull = bars + SK_NS;        // [NS] A tile written
   uint64_t* freeb = bars + 2 * SK_NS;    // [NS] stage consumed by the products
-  uint64_t* tfull = bars + 3 * SK_NS;    // [2] a group's sums in TMEM buffer b
-  uint64_t* tfree = tfull + 2;           // [2] TMEM buffer b drained
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(tfree + 2);
+  uint64_t* tfull = bars + 3 * SK_NS;    // [SK_TB] a group's sums in TMEM buffer b
+  uint64_t* tfree = tfull + SK_TB;       // [SK_TB] TMEM buffer b drained
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(tfree + SK_TB);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int rt = bx_ % a.nrt, ch = bx_ / a.nrt;
   const int g0 = ch * a.gpc, ng = min(a.gpc, a.ngroups - g0), r0 = rt * SK_R;
@@ -495,12 +504,12 @@ __device__ __forceinline__ void sk_tc_body(const SkTc& a_in, const int bx_) {
       tc::mbar_init(afull + s, SK_PW);
       tc::mbar_init(freeb + s, 1);
     }
-    for (int b = 0; b < 2; b++) {
+    for (int b = 0; b < SK_TB; b++) {
       tc::mbar_init(tfull + b, 1);
       tc::mbar_init(tfree + b, SK_PW);
     }
   }
-  if (warp == SK_PW) tc::tmem_alloc(tslot, 128);
+  if (warp == SK_PW) tc::tmem_alloc(tslot, SK_TCOLS);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -519,9 +528,10 @@ __device__ __forceinline__ void sk_tc_body(const SkTc& a_in, const int bx_) {
       const uint32_t idesc = tc::idesc_tf32(128, a.KN);
       bool ok = true;
       for (int i = 0; i < ng; i++) {
-        const int s = i % SK_NS, b = i & 1;
+        const int s = i % SK_NS, b = i % SK_TB;
         ok = tc::mbar_wait(afull + s, (i / SK_NS) & 1, TC_WAIT);
-        if (ok && i >= 2) ok = tc::mbar_wait(tfree + b, ((i - 2) >> 1) & 1, TC_WAIT);
+        // buffer b last held group i - SK_TB, drained SK_LAG groups later
+        if (ok && i >= SK_TB) ok = tc::mbar_wait(tfree + b, (i / SK_TB - 1) & 1, TC_WAIT);
         if (!ok) break;
         tc::fence_after_sync();
         const uint32_t d = tbase + 64u * b;
@@ -576,8 +586,8 @@ __device__ __forceinline__ void sk_tc_body(const SkTc& a_in, const int bx_) {
     for (int c = 0; c < 16; c++) pend[c] = 0.f;
     bool ok = true;
     auto drain = [&](int i) {
-      const int b = i & 1;
-      bool w = tc::mbar_wait(tfull + b, (i >> 1) & 1, TC_WAIT);
+      const int b = i % SK_TB;
+      bool w = tc::mbar_wait(tfull + b, (i / SK_TB) & 1, TC_WAIT);
       w = __all_sync(0xffffffffu, w);
       if (!w) return false;
       tc::fence_after_sync();
@@ -640,9 +650,9 @@ __device__ __forceinline__ void sk_tc_body(const SkTc& a_in, const int bx_) {
       tc::fence_async_smem();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(afull + s);
-      if (i >= 1) ok = drain(i - 1);
+      if (i >= SK_LAG) ok = drain(i - SK_LAG);
     }
-    if (ok && ng > 0) ok = drain(ng - 1);
+    for (int i = max(0, ng - SK_LAG); ok && i < ng; i++) ok = drain(i);
     if (!ok && lane == 0) atomicOr(a.status, 16);
     // the row sums, in FP64, through the first stage (no product or copy is
     // pending any more): D row m = r (Re) or 64 + r (Im)
@@ -673,7 +683,7 @@ __device__ __forceinline__ void sk_tc_body(const SkTc& a_in, const int bx_) {
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if (warp == SK_PW) tc::tmem_dealloc(tbase, 128);
+  if (warp == SK_PW) tc::tmem_dealloc(tbase, SK_TCOLS);
 }
 
 int sk_tc_kn(const KArgs& a) { return ((2 * a.Kz + 1) + 15) / 16 * 16; }
