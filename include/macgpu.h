@@ -82,6 +82,18 @@ typedef struct {
   const int *dep_first;       /* [ndep+1] */
   const int *dep_parent;      /* [dep_first[ndep]] */
   const double *dep_w;        /* [dep_first[ndep]] */
+  /* the kind of each dependant (NULL: all linear): 0 "Middle" (DEP_M),
+     1 "Rowlinson" (DEP_R: at D0 + wz n / |n|, n = (D1 - D0) x (D2 - D0),
+     sim/norm.c:1196-1214, forces sim/norm.c:1304-1336), 2 "Lone" (DEP_L:
+     at sum_p w_p D_p + wz z / |z|, z = (sum x_p D_p) x (sum y_p D_p),
+     sim/norm.c:1216-1231, forces sim/norm.c:1338-1360); Rowlinson and Lone
+     dependants have exactly 3 parents D0, D1, D2 */
+  const int *dep_type;
+  /* [13 ndep] per dependant (NULL when all are linear): wz, x[3], y[3],
+     tx[3], ty[3] (cook's d->wz, d->x, d->y, d->tx, d->ty; zeros where the
+     kind does not use them).  The virial and pressure-tensor terms cook adds
+     in depend_f for these two kinds are not added to mg_energy. */
+  const double *dep_par;
 } mg_topology;
 
 /* Run parameters (cook's box, el, cutoff, h, epsc ... globals). */

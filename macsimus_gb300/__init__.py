@@ -42,7 +42,7 @@ class Topology(C.Structure):
                 ("type_RvdW", _dp), ("type_alpha", _dp), ("comb_rule", C.c_int), ("nc", C.c_int),
                 ("cons", _ip), ("cons_len", _dp), ("mol_cfirst", _ip), ("chargepol", _dp),
                 ("alphapol", _dp), ("ndep", C.c_int), ("dep_site", _ip), ("dep_first", _ip),
-                ("dep_parent", _ip), ("dep_w", _dp)]
+                ("dep_parent", _ip), ("dep_w", _dp), ("dep_type", _ip), ("dep_par", _dp)]
 
 
 class Params(C.Structure):
@@ -235,6 +235,9 @@ def describe(system, L, cutoff, alpha, kappa, precision="mixed", LJcutoff=None, 
         t.dep_first = ip(system.dep_first)
         t.dep_parent = ip(system.dep_parent)
         t.dep_w = dp(system.dep_w)
+        if system.dep_type is not None and (system.dep_type != 0).any():
+            t.dep_type = ip(system.dep_type)
+            t.dep_par = dp(system.dep_par)
     else:
         t.ndep = 0
     if getattr(system, "polar", False):

@@ -115,6 +115,8 @@ struct mg_ctx {
   int ndep = 0;
   int *d_dep_site = nullptr, *d_dep_first = nullptr, *d_dep_parent = nullptr;
   double* d_dep_w = nullptr;
+  int* d_dep_type = nullptr;    // null: all linear
+  double* d_dep_par = nullptr;
   // intramolecular (excluded) charge pairs of the mixed cell path
   int* d_xfirst = nullptr;
   int2* d_xpair = nullptr;
@@ -848,12 +850,24 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
         sw += t->dep_w[q];
       }
       if (std::fabs(sw - 1) > 1e-5) return fail(ctx, MG_ERR_ARG, "dependant weights must sum to 1");
+      if (t->dep_type) {
+        const int ty = t->dep_type[k];
+        if (ty < 0 || ty > 2) return fail(ctx, MG_ERR_ARG, "dependant kind must be 0, 1 or 2");
+        if (ty > 0 && t->dep_first[k + 1] - t->dep_first[k] != 3)
+          return fail(ctx, MG_ERR_ARG, "a Rowlinson or Lone dependant needs 3 parents");
+        if (ty > 0 && !t->dep_par)
+          return fail(ctx, MG_ERR_ARG, "Rowlinson or Lone dependants need dep_par");
+      }
     }
     const int npar = t->dep_first[t->ndep];
     CK(upload(&ctx->d_dep_site, t->dep_site, t->ndep));
     CK(upload(&ctx->d_dep_first, t->dep_first, t->ndep + 1));
     CK(upload(&ctx->d_dep_parent, t->dep_parent, npar));
     CK(upload(&ctx->d_dep_w, t->dep_w, npar));
+    if (t->dep_type) {
+      CK(upload(&ctx->d_dep_type, t->dep_type, t->ndep));
+      CK(upload(&ctx->d_dep_par, t->dep_par, 13 * (size_t)t->ndep));
+    }
   }
   // cook's No.f: 3 per site less constraints, dependants and the conserved
   // momentum (sim/siminit.c:518-530)
@@ -1384,6 +1398,8 @@ DependArgs depend_args(mg_ctx* ctx) {
   a.parent = ctx->d_dep_parent;
   a.w = ctx->d_dep_w;
   a.mol = ctx->d_mol;
+  a.type = ctx->d_dep_type;
+  a.par = ctx->d_dep_par;
   return a;
 }
 
@@ -1411,7 +1427,7 @@ int md_step_enqueue(mg_ctx* ctx, bool measure) {
   Launch L = launch(ctx);
   int rc = forces_async(ctx, ctx->d_r, ctx->d_f, measure);
   if (rc) return rc;
-  CK(k_depend_f(L, depend_args(ctx), ctx->d_f));
+  CK(k_depend_f(L, depend_args(ctx), ctx->d_r, ctx->d_f));
   CK(k_shake(L, shake_args(ctx, measure)));
   CK(k_depend_r(L, depend_args(ctx), ctx->d_r));
   if (measure) {
@@ -1508,7 +1524,7 @@ int md_steps_launched(mg_ctx* ctx, int nsteps, mg_energy* en) {
     // forces on dependants to their parents (sim/constrd.c:747), the step,
     // and dependant positions for the next force evaluation: the same
     // positions cook's depend_r makes at the start of its next step
-    if (ctx->ndep > 0) PROF("depend", k_depend_f(L, depend_args(ctx), ctx->d_f));
+    if (ctx->ndep > 0) PROF("depend", k_depend_f(L, depend_args(ctx), ctx->d_r, ctx->d_f));
     PROF("shake", k_shake(L, shake_args(ctx, measure)));
     if (ctx->ndep > 0) PROF("depend", k_depend_r(L, depend_args(ctx), ctx->d_r));
     if (ctx->use_list) {
@@ -1622,7 +1638,7 @@ int mg_destroy(mg_ctx* ctx) {
                   ctx->d_qfix, ctx->d_adjtab, ctx->d_ag, ctx->d_aq, ctx->d_apart, ctx->d_adEq,
                   ctx->d_adLq, ctx->d_ags, ctx->d_atpart, ctx->d_aT, ctx->d_fk,
                   ctx->d_chi, ctx->d_zth, ctx->d_step, ctx->d_nh, ctx->d_vhist, ctx->d_dep_site, ctx->d_dep_first,
-                  ctx->d_dep_parent, ctx->d_dep_w, ctx->d_plb, ctx->d_xfirst, ctx->d_xpair,
+                  ctx->d_dep_parent, ctx->d_dep_w, ctx->d_dep_type, ctx->d_dep_par, ctx->d_plb, ctx->d_xfirst, ctx->d_xpair,
                   ctx->d_xq, ctx->d_za, ctx->d_vb, ctx->d_tcrows, ctx->d_zb, ctx->d_tckrows};
   for (void* b : bufs)
     if (b) cudaFree(b);

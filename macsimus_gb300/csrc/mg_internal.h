@@ -582,9 +582,12 @@ struct DependArgs {
   const int* parent;  // parent sites
   const double* w;    // parent weights
   const int* mol;     // [ns] molecule of each site
+  const int* type;    // [ndep] 0 Middle, 1 Rowlinson, 2 Lone (or null: all Middle)
+  const double* par;  // [13 ndep] wz, x[3], y[3], tx[3], ty[3]
 };
 cudaError_t k_depend_r(const Launch& L, const DependArgs& a, double* r);
-cudaError_t k_depend_f(const Launch& L, const DependArgs& a, double* f);
+// the dependants' forces onto their parents at positions r
+cudaError_t k_depend_f(const Launch& L, const DependArgs& a, const double* r, double* f);
 // one playback frame (float triples of ns sites) from the MD state
 cudaError_t k_playback_frame(const Launch& L, int ns, int what, int flags, const double* r,
                              const double* r1, double ih, const double Lb[3], float* out);

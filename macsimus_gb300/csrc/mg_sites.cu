@@ -1,12 +1,15 @@
-// Per-site utilities of the MD state: playback frames and linear dependants.
+// Per-site utilities of the MD state: playback frames and dependant sites.
 //
-// Linear ("Middle") dependant sites, cook's depend_t of type DEP_M: a massless
-// site placed at a weighted sum of parent sites of its molecule (the charge
-// site M of TIP4P water), sim/norm.c:1161-1195 (depend_r) and
-// sim/norm.c:1276-1300 (depend_f).  The tables list the dependants of a
-// molecule consecutively; one thread walks the dependants of one molecule in
-// table order, so force redistribution onto shared parents has no races and
-// the summation order is cook's.
+// Dependant sites, cook's depend_t (sim/norm.c:1161-1360): massless sites
+// placed from parent sites of their molecule -- linear ("Middle", DEP_M: a
+// weighted sum, the charge site M of TIP4P water), "Rowlinson" (DEP_R: above
+// parent D0 along the normal of the triangle D0 D1 D2) and "Lone" (DEP_L: an
+// in-plane weighted sum plus wz along the normal of a frame built from the
+// parents) -- and their forces redistributed onto the parents (depend_f).
+// The tables list the dependants of a molecule consecutively, in cook's
+// order; one thread walks the dependants of one molecule in table order, so
+// the redistribution onto shared parents has no races and cook's summation
+// order.  FP64, the reference's operation order.
 #include "mg_internal.h"
 
 namespace mg {
@@ -18,41 +21,137 @@ __device__ __forceinline__ bool dep_owner(const DependArgs& a, int k) {
   return k == 0 || a.mol[a.site[k - 1]] != a.mol[a.site[k]];
 }
 
+__device__ __forceinline__ void vcross(const double* b, const double* c, double* a) {
+  a[0] = b[1] * c[2] - b[2] * c[1];
+  a[1] = b[2] * c[0] - b[0] * c[2];
+  a[2] = b[0] * c[1] - b[1] * c[0];
+}
+__device__ __forceinline__ double vdot(const double* a, const double* b) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
 __global__ void __launch_bounds__(DEP_THREADS)
     depend_r_kernel(DependArgs a, double* __restrict__ r) {
   const int k0 = blockIdx.x * DEP_THREADS + threadIdx.x;
   if (k0 >= a.ndep || !dep_owner(a, k0)) return;
   const int m = a.mol[a.site[k0]];
   for (int k = k0; k < a.ndep && a.mol[a.site[k]] == m; k++) {
-    double x = 0, y = 0, z = 0;
-    for (int p = a.first[k]; p < a.first[k + 1]; p++) {
-      const double w = a.w[p];
-      const double* rp = r + 3 * (long)a.parent[p];
-      x += w * rp[0];
-      y += w * rp[1];
-      z += w * rp[2];
-    }
+    const int typ = a.type ? a.type[k] : 0;
     double* rd = r + 3 * (long)a.site[k];
-    rd[0] = x;
-    rd[1] = y;
-    rd[2] = z;
+    const int p0 = a.first[k];
+    if (typ == 1) {
+      // Rowlinson: D0 + wz l / |l|, l = (D1 - D0) x (D2 - D0) (sim/norm.c:1205-1214)
+      const double* d0 = r + 3 * (long)a.parent[p0];
+      const double* d1 = r + 3 * (long)a.parent[p0 + 1];
+      const double* d2 = r + 3 * (long)a.parent[p0 + 2];
+      const double h1[3] = {d1[0] - d0[0], d1[1] - d0[1], d1[2] - d0[2]};
+      const double h2[3] = {d2[0] - d0[0], d2[1] - d0[1], d2[2] - d0[2]};
+      double l[3];
+      vcross(h1, h2, l);
+      const double nrm = a.par[13 * (long)k] / sqrt(vdot(l, l));
+      rd[0] = d0[0] + nrm * l[0];
+      rd[1] = d0[1] + nrm * l[1];
+      rd[2] = d0[2] + nrm * l[2];
+    } else if (typ == 2) {
+      // Lone: sum w D + wz z / |z|, z = (sum x D) x (sum y D) (sim/norm.c:1216-1231)
+      const double* q = a.par + 13 * (long)k;
+      double d[3] = {0, 0, 0}, xx[3] = {0, 0, 0}, yy[3] = {0, 0, 0}, zz[3];
+      for (int c = 0; c < 3; c++) {
+        const double* rp = r + 3 * (long)a.parent[p0 + c];
+        const double w = a.w[p0 + c];
+        for (int e = 0; e < 3; e++) {
+          d[e] += w * rp[e];
+          xx[e] += q[1 + c] * rp[e];
+          yy[e] += q[4 + c] * rp[e];
+        }
+      }
+      vcross(xx, yy, zz);
+      const double rr = q[0] / sqrt(vdot(zz, zz));
+      rd[0] = d[0] + rr * zz[0];
+      rd[1] = d[1] + rr * zz[1];
+      rd[2] = d[2] + rr * zz[2];
+    } else {
+      double x = 0, y = 0, z = 0;
+      for (int p = p0; p < a.first[k + 1]; p++) {
+        const double w = a.w[p];
+        const double* rp = r + 3 * (long)a.parent[p];
+        x += w * rp[0];
+        y += w * rp[1];
+        z += w * rp[2];
+      }
+      rd[0] = x;
+      rd[1] = y;
+      rd[2] = z;
+    }
   }
 }
 
 __global__ void __launch_bounds__(DEP_THREADS)
-    depend_f_kernel(DependArgs a, double* __restrict__ f) {
+    depend_f_kernel(DependArgs a, const double* __restrict__ r, double* __restrict__ f) {
   const int k0 = blockIdx.x * DEP_THREADS + threadIdx.x;
   if (k0 >= a.ndep || !dep_owner(a, k0)) return;
   const int m = a.mol[a.site[k0]];
   for (int k = k0; k < a.ndep && a.mol[a.site[k]] == m; k++) {
+    const int typ = a.type ? a.type[k] : 0;
     const double* fd = f + 3 * (long)a.site[k];
-    const double fx = fd[0], fy = fd[1], fz = fd[2];
-    for (int p = a.first[k]; p < a.first[k + 1]; p++) {
-      const double w = a.w[p];
-      double* fp = f + 3 * (long)a.parent[p];
-      fp[0] += w * fx;
-      fp[1] += w * fy;
-      fp[2] += w * fz;
+    const double F[3] = {fd[0], fd[1], fd[2]};
+    const int p0 = a.first[k];
+    if (typ == 1) {
+      // Rowlinson (sim/norm.c:1304-1336): the torque of F about D0 through
+      // forces along l on D1 and D2
+      const int i0 = a.parent[p0], i1 = a.parent[p0 + 1], i2 = a.parent[p0 + 2];
+      const double* d0 = r + 3 * (long)i0;
+      const double* d1 = r + 3 * (long)i1;
+      const double* d2 = r + 3 * (long)i2;
+      const double* rl = r + 3 * (long)a.site[k];
+      const double h1[3] = {d1[0] - d0[0], d1[1] - d0[1], d1[2] - d0[2]};
+      const double h2[3] = {d2[0] - d0[0], d2[1] - d0[1], d2[2] - d0[2]};
+      const double l[3] = {rl[0] - d0[0], rl[1] - d0[1], rl[2] - d0[2]};
+      double M[3], Mp[3];
+      vcross(l, F, M);
+      vcross(l, M, Mp);
+      const double h1h1 = vdot(h1, h1), h2h2 = vdot(h2, h2), h1h2 = vdot(h1, h2);
+      const double det = (h1h1 * h2h2 - h1h2 * h1h2) * vdot(l, l);
+      const double a1 = (vdot(Mp, h1) * h2h2 - vdot(Mp, h2) * h1h2) / det;
+      const double a2 = (vdot(Mp, h2) * h1h1 - vdot(Mp, h1) * h1h2) / det;
+      double* f0 = f + 3 * (long)i0;
+      double* f1 = f + 3 * (long)i1;
+      double* f2 = f + 3 * (long)i2;
+      for (int e = 0; e < 3; e++) {
+        f0[e] += F[e] - (a1 + a2) * l[e];
+        f1[e] += a1 * l[e];
+        f2[e] += a2 * l[e];
+      }
+    } else if (typ == 2) {
+      // Lone (sim/norm.c:1338-1360): w F on the parents plus forces along z
+      // that carry the torque of F about the in-plane point
+      const double* q = a.par + 13 * (long)k;
+      double xx[3] = {0, 0, 0}, yy[3] = {0, 0, 0}, zz[3];
+      for (int c = 0; c < 3; c++) {
+        const double* rp = r + 3 * (long)a.parent[p0 + c];
+        for (int e = 0; e < 3; e++) {
+          xx[e] += q[1 + c] * rp[e];
+          yy[e] += q[4 + c] * rp[e];
+        }
+      }
+      vcross(xx, yy, zz);
+      const double rr = vdot(zz, zz);
+      const double fx = vdot(xx, F) / sqrt(vdot(xx, xx) * rr);
+      const double fy = vdot(yy, F) / sqrt(vdot(yy, yy) * rr);
+      for (int c = 0; c < 3; c++) {
+        const double alpha = fx * q[7 + c] + fy * q[10 + c];
+        const double w = a.w[p0 + c];
+        double* fp = f + 3 * (long)a.parent[p0 + c];
+        for (int e = 0; e < 3; e++) fp[e] += w * F[e] + alpha * zz[e];
+      }
+    } else {
+      for (int p = p0; p < a.first[k + 1]; p++) {
+        const double w = a.w[p];
+        double* fp = f + 3 * (long)a.parent[p];
+        fp[0] += w * F[0];
+        fp[1] += w * F[1];
+        fp[2] += w * F[2];
+      }
     }
   }
 }
@@ -94,9 +193,9 @@ cudaError_t k_depend_r(const Launch& L, const DependArgs& a, double* r) {
   return cudaGetLastError();
 }
 
-cudaError_t k_depend_f(const Launch& L, const DependArgs& a, double* f) {
+cudaError_t k_depend_f(const Launch& L, const DependArgs& a, const double* r, double* f) {
   if (a.ndep <= 0) return cudaSuccess;
-  depend_f_kernel<<<(a.ndep + DEP_THREADS - 1) / DEP_THREADS, DEP_THREADS, 0, L.s>>>(a, f);
+  depend_f_kernel<<<(a.ndep + DEP_THREADS - 1) / DEP_THREADS, DEP_THREADS, 0, L.s>>>(a, r, f);
   ++*L.counter;
   return cudaGetLastError();
 }

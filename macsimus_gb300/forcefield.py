@@ -93,8 +93,32 @@ class Species:
     geometry: np.ndarray   # reference geometry [ns,3] (A)
     bonds: list = field(default_factory=list)  # (i, j, length)
     drude: dict = None     # {site index: (alphapol A^3, chargepol e)}
-    # linear ("Middle") dependants: (site, [(parent, weight), ...])
+    # dependants: (site, [(parent, weight), ...]) for a linear ("Middle")
+    # one; (site, [3 parents], "R", {"wz": .}) for a Rowlinson one (above
+    # parent 0 along the normal of the parents' plane); (site, [3 parents],
+    # "L", {"x", "y", "wz", "tx", "ty"}) for a Lone (out-of-plane) one
+    # (cook/simdef.c:322-432; sim/norm.c:1161-1360)
     dependants: list = field(default_factory=list)
+
+
+DEP_KINDS = {"M": 0, "R": 1, "L": 2}
+
+
+def dep_parameters(kind, extra):
+    """the 13 parameters of a Rowlinson or Lone dependant as cook reads them
+    from the .ble (printed with 15 digits, then the coefficient vectors
+    x, y, tx, ty shifted to zero sum, cook/simdef.c:313-320): wz, x[3],
+    y[3], tx[3], ty[3] (zeros where unused)"""
+    par = np.zeros(13)
+    if kind == "M":
+        return par
+    par[0] = float("%.15g" % extra["wz"])
+    if kind == "L":
+        for o, key in ((1, "x"), (4, "y"), (7, "tx"), (10, "ty")):
+            v = [float("%.15g" % c) for c in extra[key]]
+            sm = (v[0] + v[1] + v[2]) / 3
+            par[o:o + 3] = [v[0] - sm, v[1] - sm, v[2] - sm]
+    return par
 
 
 def spce():
@@ -120,6 +144,54 @@ def tip4p2005():
                  np.array([[0.0, 0.0, 0.0], h1, h2, m]),
                  bonds=[(0, 1, doh), (0, 2, doh), (1, 2, dhh)])
     sp.dependants = [(3, [(0, 1 - 2 * w), (1, w), (2, w)])]
+    return sp
+
+
+def water_lone_rowlinson():
+    """A test model for the out-of-plane dependants (no reference example
+    uses them): the rigid TIP4P/2005 geometry with O (LJ), H, H, two "Lone"
+    sites 0.3 A behind O along the bisector and 0.5 A above and below the
+    molecular plane, and a "Rowlinson" site 0.25 A above O along the
+    normal, charged so that the molecule is neutral.  The Lone frame is
+    xx = H1 - H2, yy = (H1 + H2)/2 - O (orthogonal for the symmetric
+    molecule); tx, ty make the normal forces on O, H, H reproduce the torque
+    of the dependant's force about its in-plane point: sum tx = sum ty = 0,
+    sum tx a = sum ty b = -wz, sum tx b = sum ty a = 0 with (a, b) the
+    parents' coordinates in that frame (the conditions of sim/norm.c:1338-1360
+    for a rigid triangle)"""
+    a = math.radians(104.52)
+    doh = 0.9572
+    o = np.zeros(3)
+    h1 = np.array([doh, 0.0, 0.0])
+    h2 = np.array([doh * math.cos(a), doh * math.sin(a), 0.0])
+    bis = 0.5 * (h1 + h2) - o
+    sb = -0.3 / float(np.linalg.norm(bis))
+    w = [1 - sb, 0.5 * sb, 0.5 * sb]
+    x, y = [0.0, 1.0, -1.0], [-1.0, 0.5, 0.5]
+    xx = h1 - h2
+    yy = bis
+    zhat = np.cross(xx, yy) / np.linalg.norm(np.cross(xx, yy))
+    xh, yh = xx / np.linalg.norm(xx), yy / np.linalg.norm(yy)
+    p = w[0] * o + w[1] * h1 + w[2] * h2
+    par = [o, h1, h2]
+    A = np.array([[1.0, 1.0, 1.0],
+                  [float((r - p) @ xh) for r in par],
+                  [float((r - p) @ yh) for r in par]])
+    lones = []
+    geom = [o, h1, h2]
+    for wz in (0.5, -0.5):
+        tx = np.linalg.solve(A, [0.0, -wz, 0.0])
+        ty = np.linalg.solve(A, [0.0, 0.0, -wz])
+        lones.append(dict(x=x, y=y, wz=wz, tx=list(tx), ty=list(ty)))
+        geom.append(p + wz * zhat)
+    geom.append(o + 0.25 * zhat)
+    dhh = float(np.linalg.norm(h1 - h2))
+    sp = Species("T5R", ["OT", "H", "H", "MW", "MW", "MW"],
+                 [0.0, 0.5564, 0.5564, -0.40, -0.40, -0.3128], np.array(geom),
+                 bonds=[(0, 1, doh), (0, 2, doh), (1, 2, dhh)])
+    sp.dependants = [(3, [(0, w[0]), (1, w[1]), (2, w[2])], "L", lones[0]),
+                     (4, [(0, w[0]), (1, w[1]), (2, w[2])], "L", lones[1]),
+                     (5, [(0, 1.0), (1, 0.0), (2, 0.0)], "R", dict(wz=0.25))]
     return sp
 
 
@@ -150,7 +222,8 @@ def spce_drude():
 
 SPECIES = {"WAT": spce, "NA": lambda: ion("NA"), "CL": lambda: ion("CL"), "WATD": spce_drude,
            "AP": lambda: ion("AP", 1.0), "AM": lambda: ion("AM", -1.0),
-           "PRB": lambda: ion("PRB", 0.0), "T4P": tip4p2005, "APV": lambda: ion("APV", 0.8)}
+           "PRB": lambda: ion("PRB", 0.0), "T4P": tip4p2005, "APV": lambda: ion("APV", 0.8),
+           "T5R": water_lone_rowlinson}
 
 
 @dataclass
@@ -173,11 +246,13 @@ class System:
     counts: list = None
     qpol: np.ndarray = None     # [ns] Drude charge (program units) or None
     alphapol: np.ndarray = None # [ns] Drude polarizability volume (A^3) or None
-    # linear dependants (massless sites): site, parents [dep_first[k]:dep_first[k+1]]
+    # dependants (massless sites): site, parents [dep_first[k]:dep_first[k+1]]
     dep_site: np.ndarray = None   # [ndep] int32
     dep_first: np.ndarray = None  # [ndep+1] int32
     dep_parent: np.ndarray = None # [np] int32 (global site indices)
     dep_w: np.ndarray = None      # [np] weights
+    dep_type: np.ndarray = None   # [ndep] int32: 0 Middle, 1 Rowlinson, 2 Lone
+    dep_par: np.ndarray = None    # [ndep, 13]: wz, x[3], y[3], tx[3], ty[3]
 
     @property
     def ndep(self):
@@ -209,7 +284,7 @@ def build_system(species_names, counts):
     tix = {n: i for i, n in enumerate(TYPE_ORDER)}
     typ, q, mass, mol, mfirst, cons, clen, cfirst = [], [], [], [], [0], [], [], [0]
     qpol, apol = [], []
-    dsite, dfirst, dpar, dw = [], [0], [], []
+    dsite, dfirst, dpar, dw, dtype, dprm = [], [0], [], [], [], []
     polar = any(t in TYPE_DRUDE for s in species_names for t in SPECIES[s]().sites)
     imol = 0
     for sname, n in zip(species_names, counts):
@@ -229,12 +304,21 @@ def build_system(species_names, counts):
             for (i, j, d) in sp.bonds:
                 cons.append((base + i, base + j))
                 clen.append(d)
-            for (k, parents) in sp.dependants:
+            for dep in sp.dependants:
+                k, parents = dep[0], dep[1]
+                kind = dep[2] if len(dep) > 2 else "M"
                 dsite.append(base + k)
-                for (pi, w) in parents:
+                # the weights as cook reads and normalizes them (cook/simdef.c:386-390)
+                ws = [float("%.12f" % w) for (_, w) in parents]
+                sw = 0.0
+                for w in ws:
+                    sw += w
+                for (pi, _), w in zip(parents, ws):
                     dpar.append(base + pi)
-                    dw.append(w)
+                    dw.append(w / sw)
                 dfirst.append(len(dpar))
+                dtype.append(DEP_KINDS[kind])
+                dprm.append(dep_parameters(kind, dep[3] if len(dep) > 3 else None))
             imol += 1
             mfirst.append(len(typ))
             cfirst.append(len(cons))
@@ -248,7 +332,9 @@ def build_system(species_names, counts):
                   dep_site=np.array(dsite, np.int32) if dsite else None,
                   dep_first=np.array(dfirst, np.int32) if dsite else None,
                   dep_parent=np.array(dpar, np.int32) if dsite else None,
-                  dep_w=np.array(dw) if dsite else None)
+                  dep_w=np.array(dw) if dsite else None,
+                  dep_type=np.array(dtype, np.int32) if dsite else None,
+                  dep_par=np.array(dprm).reshape(-1, 13) if dsite else None)
 
 
 def ble_text(species_names):
@@ -287,11 +373,23 @@ def ble_text(species_names):
             lines.append("  %d %s   %d %s   450  %.15f" % (i, sp.sites[i], j, sp.sites[j], d))
         lines += ["", "angles", "", "dihedrals", "", "impropers", "", "aromatics", "",
                   "dependants"]
-        # cook/simdef.c readdependants: M site name n (parent name weight)... e
-        for (k, parents) in sp.dependants:
-            lines.append("  M %d %s %d " % (k, sp.sites[k], len(parents)) +
-                         " ".join("%d %s %.12f" % (pi, sp.sites[pi], w) for pi, w in parents) +
-                         " e")
+        # cook/simdef.c readdependants: kind site name n (parent name weight)...
+        # [R: wz | L: x[3] y[3] wz tx[3] ty[3]] e; cook prepends every
+        # dependant to its list, so the file lists them last first and cook
+        # runs them in the order of sp.dependants
+        for dep in reversed(sp.dependants):
+            k, parents = dep[0], dep[1]
+            kind = dep[2] if len(dep) > 2 else "M"
+            line = ("  %s %d %s %d " % (kind, k, sp.sites[k], len(parents)) +
+                    " ".join("%d %s %.12f" % (pi, sp.sites[pi], w) for pi, w in parents))
+            if kind == "R":
+                line += " %.15g" % dep[3]["wz"]
+            elif kind == "L":
+                e = dep[3]
+                line += " " + " ".join("%.15g" % c for c in
+                                       list(e["x"]) + list(e["y"]) + [e["wz"]] +
+                                       list(e["tx"]) + list(e["ty"]))
+            lines.append(line + " e")
         lines += ["", ""]
     return "\n".join(lines) + "\n\n"
 

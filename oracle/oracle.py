@@ -7,6 +7,8 @@ import ctypes as C
 import os
 import subprocess
 
+import math
+
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -319,26 +321,87 @@ class Oracle:
         return s, corr, U
 
 
+def _dep_kind(system, k):
+    t = getattr(system, "dep_type", None)
+    return 0 if t is None else int(t[k])
+
+
 def depend_r(system, r):
-    """positions of the linear ("Middle") dependants from their parents,
-    r_d = sum_p w_p r_p (sim/norm.c:1188-1193, depend_r for d->type<=DEP_M);
+    """positions of the dependants from their parents, in table order
+    (sim/norm.c:1161-1231, depend_r): linear ("Middle") r_d = sum_p w_p r_p;
+    "Rowlinson" r_d = D0 + wz l/|l|, l = (D1 - D0) x (D2 - D0); "Lone"
+    r_d = sum_p w_p D_p + wz z/|z|, z = (sum x_p D_p) x (sum y_p D_p);
     returns a copy"""
     r = np.array(r, dtype=np.float64, copy=True)
     for k in range(system.ndep):
         a, b = system.dep_first[k], system.dep_first[k + 1]
-        r[system.dep_site[k]] = (system.dep_w[a:b, None] * r[system.dep_parent[a:b]]).sum(0)
+        par = system.dep_parent[a:b]
+        kind = _dep_kind(system, k)
+        if kind == 1:
+            wz = system.dep_par[k][0]
+            h1 = r[par[1]] - r[par[0]]
+            h2 = r[par[2]] - r[par[0]]
+            l = np.cross(h1, h2)
+            r[system.dep_site[k]] = r[par[0]] + (wz / math.sqrt(l @ l)) * l
+        elif kind == 2:
+            q = system.dep_par[k]
+            d = np.zeros(3)
+            xx = np.zeros(3)
+            yy = np.zeros(3)
+            for c in range(3):
+                d += system.dep_w[a + c] * r[par[c]]
+                xx += q[1 + c] * r[par[c]]
+                yy += q[4 + c] * r[par[c]]
+            zz = np.cross(xx, yy)
+            r[system.dep_site[k]] = d + (q[0] / math.sqrt(zz @ zz)) * zz
+        else:
+            r[system.dep_site[k]] = (system.dep_w[a:b, None] * r[par]).sum(0)
     return r
 
 
-def depend_f(system, f):
-    """forces on the linear dependants added to their parents, f_p += w_p f_d,
-    in table order (sim/norm.c:1296-1299, depend_f for d->type<=DEP_M); the
-    dependant keeps its force, as in cook; returns a copy"""
+def depend_f(system, f, r=None):
+    """forces on the dependants added to their parents in table order
+    (sim/norm.c:1276-1360, depend_f): linear f_p += w_p f_d; "Rowlinson" the
+    force onto D0 and the torque about D0 through forces along l on D1, D2;
+    "Lone" f_p += w_p f_d + alpha_p z with alpha_p = fx tx_p + fy ty_p (r:
+    the positions, needed by the two out-of-plane kinds); the dependant
+    keeps its force, as in cook; returns a copy"""
     f = np.array(f, dtype=np.float64, copy=True)
     for k in range(system.ndep):
         fd = f[system.dep_site[k]].copy()
-        for q in range(system.dep_first[k], system.dep_first[k + 1]):
-            f[system.dep_parent[q]] += system.dep_w[q] * fd
+        a, b = system.dep_first[k], system.dep_first[k + 1]
+        par = system.dep_parent[a:b]
+        kind = _dep_kind(system, k)
+        if kind == 1:
+            h1 = r[par[1]] - r[par[0]]
+            h2 = r[par[2]] - r[par[0]]
+            l = r[system.dep_site[k]] - r[par[0]]
+            M = np.cross(l, fd)
+            Mp = np.cross(l, M)
+            h1h1, h2h2, h1h2 = h1 @ h1, h2 @ h2, h1 @ h2
+            det = (h1h1 * h2h2 - h1h2 * h1h2) * (l @ l)
+            a1 = ((Mp @ h1) * h2h2 - (Mp @ h2) * h1h2) / det
+            a2 = ((Mp @ h2) * h1h1 - (Mp @ h1) * h1h2) / det
+            f[par[0]] += fd - (a1 + a2) * l
+            f[par[1]] += a1 * l
+            f[par[2]] += a2 * l
+        elif kind == 2:
+            q = system.dep_par[k]
+            xx = np.zeros(3)
+            yy = np.zeros(3)
+            for c in range(3):
+                xx += q[1 + c] * r[par[c]]
+                yy += q[4 + c] * r[par[c]]
+            zz = np.cross(xx, yy)
+            rr = zz @ zz
+            fx = (xx @ fd) / math.sqrt((xx @ xx) * rr)
+            fy = (yy @ fd) / math.sqrt((yy @ yy) * rr)
+            for c in range(3):
+                alpha = fx * q[7 + c] + fy * q[10 + c]
+                f[par[c]] += system.dep_w[a + c] * fd + alpha * zz
+        else:
+            for qi in range(a, b):
+                f[system.dep_parent[qi]] += system.dep_w[qi] * fd
     return f
 
 

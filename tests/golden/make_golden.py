@@ -62,6 +62,11 @@ CASES = {
     "tip4p216": dict(binary="cookew", species=["T4P"], N=[216], L=18.6206,
                      cutoff=9.0, alpha=0.35, kn=6, steps=3, h=0.002, epsc=1e-10,
                      options=["-y99999", "-n1"], extra_get=["dt.plb=0.002"]),
+    # 216 rigid waters with two "Lone" (out-of-plane) dependants and one
+    # "Rowlinson" dependant each (test model T5R: cook's DEP_L and DEP_R,
+    # sim/norm.c:1196-1231, 1304-1360), charged so that they carry force
+    "t5r216": dict(binary="cookew", species=["T5R"], N=[216], L=18.6206,
+                   cutoff=9.0, alpha=0.35, kn=6, steps=3, h=0.002, epsc=1e-10),
     # the dipole term of Ewald(2) (sim/ewald.c:865-887) on the 216 SPC/E box:
     # isotropic surroundings of dielectric constant 1 (el.epsinf), the
     # Yeh-Berkowitz slab term along z (el.corr=4), and its energy-only

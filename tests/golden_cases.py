@@ -7,7 +7,7 @@ import numpy as np
 from macsimus_gb300 import forcefield as ff
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["spce216", "brine532", "spce864", "widom500", "tip4p216"]
+CASES = ["spce216", "brine532", "spce864", "widom500", "tip4p216", "t5r216"]
 POLAR_CASES = ["drude216"]
 
 

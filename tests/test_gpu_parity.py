@@ -326,11 +326,13 @@ def test_concurrent_kspace_chain_gives_identical_forces(case):
     assert e1["el"] == e2["el"] and e1["lj"] == e2["lj"]
 
 
+@pytest.mark.parametrize("case", ["tip4p216", "t5r216"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_dependant_md_chain_matches_oracle(precision):
-    """five TIP4P/2005 steps on the device against the oracle's chain of
-    forces, depend_f, SHAKE and depend_r from the same start"""
-    g, meta, system, ew, fp = make("tip4p216", precision)
+def test_dependant_md_chain_matches_oracle(precision, case):
+    """five steps on the device against the oracle's chain of forces,
+    depend_f, SHAKE and depend_r from the same start: TIP4P/2005 (a linear
+    dependant) and the T5R model (two Lone and one Rowlinson dependant)"""
+    g, meta, system, ew, fp = make(case, precision)
     p = meta["params"]
     orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
     R = g["r"]
@@ -340,10 +342,17 @@ def test_dependant_md_chain_matches_oracle(precision):
     rg, _ = fp.md_get_state()
     for _ in range(5):
         f, _ = orc.forces(r, measure=False, nthreads=4)
-        r, r1, it, _ = orc.shake_step(r, r1, O.depend_f(system, f), p["h"], eps=p["epsc"],
+        r, r1, it, _ = orc.shake_step(r, r1, O.depend_f(system, f, r), p["h"], eps=p["epsc"],
                                       omega=meta["omegac"] / 2)
         r = O.depend_r(system, O.normalize(system, r, ew["L"]))
     assert np.abs(rg - r).max() < (1e-9 if precision == "fp64" else 2e-6)
+    if case == "t5r216":
+        # and one step from cook's state gives cook's next positions
+        g, meta, system, ew, fp = make(case, precision)
+        fp.md_set_state(R[2], R[2] - R[1])
+        fp.md_steps(1)
+        assert np.abs(fp.md_get_state()[0] - R[3]).max() < (1e-9 if precision == "fp64"
+                                                             else 2e-6)
 
 
 @pytest.mark.parametrize("case", ["spce216", "tip4p216"])

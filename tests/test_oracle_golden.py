@@ -185,6 +185,29 @@ def test_dependant_step_matches_reference_trajectory():
     assert abs(ek / meta["Ekin_last"] - 1) < 5e-9
 
 
+def test_out_of_plane_dependants_match_reference():
+    """the test model T5R (two "Lone" and one "Rowlinson" dependant per
+    rigid water, sim/norm.c:1196-1231, 1304-1360): cook's dumped positions
+    of the dependants follow from their parents; its step from the forces
+    moved onto O, H, H keeps the total force and gives cook's next
+    positions"""
+    g, meta, system, ew = load("t5r216")
+    assert system.ndep == 648 and set(system.dep_type.tolist()) == {1, 2}
+    for d in range(g["r"].shape[0]):
+        assert np.abs(O.depend_r(system, g["r"][d]) - g["r"][d]).max() < 1e-10
+    p = meta["params"]
+    orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
+    R, F = g["r"], g["f"]
+    f = O.depend_f(system, F[2], R[2])
+    dep = system.dep_site
+    assert np.allclose(f.sum(0) - f[dep].sum(0), F[2].sum(0), atol=1e-7)
+    rn, _, it, _ = orc.shake_step(R[2], R[2] - R[1], f, p["h"], eps=p["epsc"],
+                                  omega=meta["omegac"] / 2)
+    rn = O.depend_r(system, O.normalize(system, rn, ew["L"]))
+    assert it > 0
+    assert np.abs(rn - R[3]).max() < 1e-9
+
+
 def test_reference_states_are_normalized():
     """cook's dumped positions are normalized: every molecule's lowest
     massive-site coordinate lies in [r0, r0 + L) with r0 = 0.15 (the value
