@@ -91,8 +91,9 @@ typedef struct {
   const int *dep_type;
   /* [13 ndep] per dependant (NULL when all are linear): wz, x[3], y[3],
      tx[3], ty[3] (cook's d->wz, d->x, d->y, d->tx, d->ty; zeros where the
-     kind does not use them).  The virial and pressure-tensor terms cook adds
-     in depend_f for these two kinds are not added to mg_energy. */
+     kind does not use them).  A measured MD step adds the virial and
+     pressure-tensor terms cook's depend_f adds for these two kinds
+     (sim/norm.c:1335-1338, 1363-1368) to mg_energy's vir and Pvir. */
   const double *dep_par;
 } mg_topology;
 

@@ -16,7 +16,7 @@
 using namespace mg;
 
 // length of the reduction-output block d_sums / h_sums (doubles)
-constexpr int NSUMS = 48;
+constexpr int NSUMS = 56;
 
 struct mg_ctx {
   std::string err;
@@ -116,6 +116,9 @@ struct mg_ctx {
   int *d_dep_site = nullptr, *d_dep_first = nullptr, *d_dep_parent = nullptr;
   double* d_dep_w = nullptr;
   int* d_dep_type = nullptr;    // null: all linear
+  // with Rowlinson or Lone dependants: per dependant the virial and virial
+  // tensor rows of a measured depend_f, reduced into d_sums + 48
+  double* d_deppart = nullptr;
   double* d_dep_par = nullptr;
   // intramolecular (excluded) charge pairs of the mixed cell path
   int* d_xfirst = nullptr;
@@ -867,6 +870,7 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
     if (t->dep_type) {
       CK(upload(&ctx->d_dep_type, t->dep_type, t->ndep));
       CK(upload(&ctx->d_dep_par, t->dep_par, 13 * (size_t)t->ndep));
+      CK(dalloc(&ctx->d_deppart, 7 * (size_t)t->ndep));
     }
   }
   // cook's No.f: 3 per site less constraints, dependants and the conserved
@@ -1390,7 +1394,7 @@ ShakeArgs shake_args(mg_ctx* ctx, bool measure) {
   return sa;
 }
 
-DependArgs depend_args(mg_ctx* ctx) {
+DependArgs depend_args(mg_ctx* ctx, bool measure = false) {
   DependArgs a;
   a.ndep = ctx->ndep;
   a.site = ctx->d_dep_site;
@@ -1400,7 +1404,28 @@ DependArgs depend_args(mg_ctx* ctx) {
   a.mol = ctx->d_mol;
   a.type = ctx->d_dep_type;
   a.par = ctx->d_dep_par;
+  a.vpart = measure ? ctx->d_deppart : nullptr;
   return a;
+}
+
+// the dependants' forces onto their parents; on a measured step with
+// Rowlinson or Lone dependants also their virial and tensor terms, summed
+// into d_sums + 48 (scalar) and + 49 (xx yy zz yz zx xy)
+cudaError_t depend_f_enqueue(mg_ctx* ctx, const Launch& L, bool measure) {
+  const DependArgs a = depend_args(ctx, measure);
+  cudaError_t e = k_depend_f(L, a, ctx->d_r, ctx->d_f);
+  if (e == cudaSuccess && a.vpart) e = k_reduce_sum(L, a.vpart, a.ndep, 7, ctx->d_sums + 48);
+  return e;
+}
+
+// cook adds those terms to En.vir and En.Pvir (sim/norm.c:1335-1338,
+// 1363-1368) after the force evaluation; a measured MD step's energies carry
+// them
+void add_depend_virial(mg_ctx* ctx, mg_energy* en) {
+  if (!ctx->d_deppart) return;
+  const double* s = ctx->h_sums + 48;
+  en->vir += s[0];
+  for (int m = 0; m < 6; m++) en->Pvir[m] += s[1 + m];
 }
 
 ThermoArgs thermo_args(mg_ctx* ctx) {
@@ -1427,7 +1452,7 @@ int md_step_enqueue(mg_ctx* ctx, bool measure) {
   Launch L = launch(ctx);
   int rc = forces_async(ctx, ctx->d_r, ctx->d_f, measure);
   if (rc) return rc;
-  CK(k_depend_f(L, depend_args(ctx), ctx->d_r, ctx->d_f));
+  CK(depend_f_enqueue(ctx, L, measure));
   CK(k_shake(L, shake_args(ctx, measure)));
   CK(k_depend_r(L, depend_args(ctx), ctx->d_r));
   if (measure) {
@@ -1524,7 +1549,7 @@ int md_steps_launched(mg_ctx* ctx, int nsteps, mg_energy* en) {
     // forces on dependants to their parents (sim/constrd.c:747), the step,
     // and dependant positions for the next force evaluation: the same
     // positions cook's depend_r makes at the start of its next step
-    if (ctx->ndep > 0) PROF("depend", k_depend_f(L, depend_args(ctx), ctx->d_r, ctx->d_f));
+    if (ctx->ndep > 0) PROF("depend", depend_f_enqueue(ctx, L, measure));
     PROF("shake", k_shake(L, shake_args(ctx, measure)));
     if (ctx->ndep > 0) PROF("depend", k_depend_r(L, depend_args(ctx), ctx->d_r));
     if (ctx->use_list) {
@@ -1638,7 +1663,7 @@ int mg_destroy(mg_ctx* ctx) {
                   ctx->d_qfix, ctx->d_adjtab, ctx->d_ag, ctx->d_aq, ctx->d_apart, ctx->d_adEq,
                   ctx->d_adLq, ctx->d_ags, ctx->d_atpart, ctx->d_aT, ctx->d_fk,
                   ctx->d_chi, ctx->d_zth, ctx->d_step, ctx->d_nh, ctx->d_vhist, ctx->d_dep_site, ctx->d_dep_first,
-                  ctx->d_dep_parent, ctx->d_dep_w, ctx->d_dep_type, ctx->d_dep_par, ctx->d_plb, ctx->d_xfirst, ctx->d_xpair,
+                  ctx->d_dep_parent, ctx->d_dep_w, ctx->d_dep_type, ctx->d_dep_par, ctx->d_deppart, ctx->d_plb, ctx->d_xfirst, ctx->d_xpair,
                   ctx->d_xq, ctx->d_za, ctx->d_vb, ctx->d_tcrows, ctx->d_zb, ctx->d_tckrows};
   for (void* b : bufs)
     if (b) cudaFree(b);
@@ -1919,6 +1944,7 @@ int mg_md_steps(mg_ctx* ctx, int nsteps, mg_energy* en) {
   if (en) {
     fill_energy(ctx, en);
     if (ctx->polar && ctx->nd > 0) add_drude_energy(ctx, en);
+    add_depend_virial(ctx, en);
     en->ekin = ctx->h_sums[17] / (ctx->h * ctx->h) / 4;
     fill_pressure(ctx, en);
   }

@@ -584,6 +584,11 @@ struct DependArgs {
   const int* mol;     // [ns] molecule of each site
   const int* type;    // [ndep] 0 Middle, 1 Rowlinson, 2 Lone (or null: all Middle)
   const double* par;  // [13 ndep] wz, x[3], y[3], tx[3], ty[3]
+  // or null; else [7 ndep] per dependant row: the virial and the virial
+  // tensor (xx yy zz yz zx xy) its redistribution adds (the out-of-plane
+  // kinds), written by the thread of the molecule's first dependant, zero
+  // in the other rows
+  double* vpart;
 };
 cudaError_t k_depend_r(const Launch& L, const DependArgs& a, double* r);
 // the dependants' forces onto their parents at positions r

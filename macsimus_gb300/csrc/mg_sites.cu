@@ -86,18 +86,31 @@ __global__ void __launch_bounds__(DEP_THREADS)
   }
 }
 
+// cook's virial tensor term of Q, F, G (sim/norm.c:1256-1262): Q (G_x F_x,
+// G_y F_y, G_z F_z, G_y F_z, G_z F_x, G_x F_y) added to v[1..6]
+__device__ __forceinline__ void ptens_add(double* v, double q, const double* F, const double* G) {
+  v[1] += q * G[0] * F[0];
+  v[2] += q * G[1] * F[1];
+  v[3] += q * G[2] * F[2];
+  v[4] += q * G[1] * F[2];
+  v[5] += q * G[2] * F[0];
+  v[6] += q * G[0] * F[1];
+}
+
 __global__ void __launch_bounds__(DEP_THREADS)
     depend_f_kernel(DependArgs a, const double* __restrict__ r, double* __restrict__ f) {
   const int k0 = blockIdx.x * DEP_THREADS + threadIdx.x;
-  if (k0 >= a.ndep || !dep_owner(a, k0)) return;
+  if (k0 >= a.ndep) return;
+  double v[7] = {0, 0, 0, 0, 0, 0, 0};  // virial, tensor
   const int m = a.mol[a.site[k0]];
-  for (int k = k0; k < a.ndep && a.mol[a.site[k]] == m; k++) {
+  const bool own = dep_owner(a, k0);
+  for (int k = k0; own && k < a.ndep && a.mol[a.site[k]] == m; k++) {
     const int typ = a.type ? a.type[k] : 0;
     const double* fd = f + 3 * (long)a.site[k];
     const double F[3] = {fd[0], fd[1], fd[2]};
     const int p0 = a.first[k];
     if (typ == 1) {
-      // Rowlinson (sim/norm.c:1304-1336): the torque of F about D0 through
+      // Rowlinson (sim/norm.c:1304-1338): the torque of F about D0 through
       // forces along l on D1 and D2
       const int i0 = a.parent[p0], i1 = a.parent[p0 + 1], i2 = a.parent[p0 + 2];
       const double* d0 = r + 3 * (long)i0;
@@ -122,10 +135,16 @@ __global__ void __launch_bounds__(DEP_THREADS)
         f1[e] += a1 * l[e];
         f2[e] += a2 * l[e];
       }
+      // the triangle's forces, and F moved from L to D0
+      ptens_add(v, a1, l, h1);
+      ptens_add(v, a2, l, h2);
+      ptens_add(v, -1.0, l, F);
+      v[0] -= vdot(l, F);
     } else if (typ == 2) {
-      // Lone (sim/norm.c:1338-1360): w F on the parents plus forces along z
+      // Lone (sim/norm.c:1338-1368): w F on the parents plus forces along z
       // that carry the torque of F about the in-plane point
       const double* q = a.par + 13 * (long)k;
+      const double* rd = r + 3 * (long)a.site[k];
       double xx[3] = {0, 0, 0}, yy[3] = {0, 0, 0}, zz[3];
       for (int c = 0; c < 3; c++) {
         const double* rp = r + 3 * (long)a.parent[p0 + c];
@@ -138,12 +157,19 @@ __global__ void __launch_bounds__(DEP_THREADS)
       const double rr = vdot(zz, zz);
       const double fx = vdot(xx, F) / sqrt(vdot(xx, xx) * rr);
       const double fy = vdot(yy, F) / sqrt(vdot(yy, yy) * rr);
+      const double fz = vdot(zz, F) / rr;
       for (int c = 0; c < 3; c++) {
         const double alpha = fx * q[7 + c] + fy * q[10 + c];
         const double w = a.w[p0 + c];
+        const double* rp = r + 3 * (long)a.parent[p0 + c];
         double* fp = f + 3 * (long)a.parent[p0 + c];
         for (int e = 0; e < 3; e++) fp[e] += w * F[e] + alpha * zz[e];
+        const double dr[3] = {rp[0] - rd[0], rp[1] - rd[1], rp[2] - rd[2]};
+        ptens_add(v, alpha, zz, dr);
       }
+      const double wr = q[0] / sqrt(rr);
+      v[0] -= wr * fz;
+      ptens_add(v, -wr, F, zz);
     } else {
       for (int p = p0; p < a.first[k + 1]; p++) {
         const double w = a.w[p];
@@ -154,6 +180,8 @@ __global__ void __launch_bounds__(DEP_THREADS)
       }
     }
   }
+  if (a.vpart)
+    for (int e = 0; e < 7; e++) a.vpart[7 * (long)k0 + e] = v[e];
 }
 
 // playback frame, sim/simils.c:1666-1686 in the same operation order:

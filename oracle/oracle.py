@@ -359,14 +359,26 @@ def depend_r(system, r):
     return r
 
 
-def depend_f(system, f, r=None):
+def depend_f(system, f, r=None, virial=False):
     """forces on the dependants added to their parents in table order
     (sim/norm.c:1276-1360, depend_f): linear f_p += w_p f_d; "Rowlinson" the
     force onto D0 and the torque about D0 through forces along l on D1, D2;
     "Lone" f_p += w_p f_d + alpha_p z with alpha_p = fx tx_p + fy ty_p (r:
     the positions, needed by the two out-of-plane kinds); the dependant
-    keeps its force, as in cook; returns a copy"""
+    keeps its force, as in cook; returns a copy.  virial=True also returns
+    the scalar virial and the virial tensor (xx yy zz yz zx xy) that the two
+    out-of-plane kinds add to cook's En.vir and En.Pvir
+    (sim/norm.c:1335-1338, 1363-1368; the tensor of Q, F, G is
+    Q (G_x F_x, G_y F_y, G_z F_z, G_y F_z, G_z F_x, G_x F_y),
+    sim/norm.c:1256-1262)"""
     f = np.array(f, dtype=np.float64, copy=True)
+    vir = 0.0
+    pv = np.zeros(6)
+
+    def tensor(q, F, G):
+        pv[:] += q * np.array([G[0] * F[0], G[1] * F[1], G[2] * F[2],
+                               G[1] * F[2], G[2] * F[0], G[0] * F[1]])
+
     for k in range(system.ndep):
         fd = f[system.dep_site[k]].copy()
         a, b = system.dep_first[k], system.dep_first[k + 1]
@@ -385,6 +397,10 @@ def depend_f(system, f, r=None):
             f[par[0]] += fd - (a1 + a2) * l
             f[par[1]] += a1 * l
             f[par[2]] += a2 * l
+            tensor(a1, l, h1)
+            tensor(a2, l, h2)
+            tensor(-1.0, l, fd)
+            vir -= l @ fd
         elif kind == 2:
             q = system.dep_par[k]
             xx = np.zeros(3)
@@ -396,12 +412,20 @@ def depend_f(system, f, r=None):
             rr = zz @ zz
             fx = (xx @ fd) / math.sqrt((xx @ xx) * rr)
             fy = (yy @ fd) / math.sqrt((yy @ yy) * rr)
+            fz = (zz @ fd) / rr
+            rd = r[system.dep_site[k]]
+            rr = math.sqrt(rr)
             for c in range(3):
                 alpha = fx * q[7 + c] + fy * q[10 + c]
                 f[par[c]] += system.dep_w[a + c] * fd + alpha * zz
+                tensor(alpha, zz, r[par[c]] - rd)
+            vir -= q[0] / rr * fz
+            tensor(-q[0] / rr, fd, zz)
         else:
             for qi in range(a, b):
                 f[system.dep_parent[qi]] += system.dep_w[qi] * fd
+    if virial:
+        return f, vir, pv
     return f
 
 

@@ -388,6 +388,10 @@ PRESSURE_CASES = {
     "press_drude216": dict(binary="cookpolpt", species=["WATD"], N=[216], L=18.6206,
                            cutoff=9.0, alpha=0.35, kn=6, h=0.001, epsc=1e-10, steps_a=4,
                            options=["-p220"], extra_def=["scf.eps=-1"]),
+    # the Rowlinson and Lone dependants' own virial and tensor terms
+    # (sim/norm.c:1335-1337, 1363-1368)
+    "press_t5r216": dict(binary="cookewpt", species=["T5R"], N=[216], L=18.6206,
+                         cutoff=9.0, alpha=0.35, kn=6, h=0.002, epsc=1e-10, steps_a=4),
 }
 
 

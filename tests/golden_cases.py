@@ -27,7 +27,7 @@ def load(case):
 DIPOLE_CASES = ["dip216eps", "dip216yb", "dip216yb8"]
 
 
-PRESSURE_CASES = ["press_spce216", "press_tip4p216", "press_drude216"]
+PRESSURE_CASES = ["press_spce216", "press_tip4p216", "press_drude216", "press_t5r216"]
 
 
 def load_pressure(case):

@@ -7,7 +7,8 @@ tensors (measurePconstraints, sim/constrd.c:115-265: the force virial plus
 the SHAKE constraint virial of sim/virc.c divided by h^2, the VERLET=3
 kinetic tensor of sim/shakev3.c), the constraint pressure Pvirc, the scalar
 virial En.vir and the pressure Pevir.  The oracle repeats that step: forces
-(+ the Drude SCF iteration, + the TIP4P dependant force redistribution) and
+(+ the Drude SCF iteration, + the dependants' force redistribution with
+the virial terms of the out-of-plane kinds) and
 leap-frog + SHAKE with the measured sums."""
 import numpy as np
 import pytest
@@ -34,7 +35,8 @@ def oracle_step(case):
         r = O.depend_r(system, r)
     f, en = orc.forces(r, measure=True, nthreads=4)
     if system.ndep:
-        f = O.depend_f(system, f)
+        f, dvir, dpvir = O.depend_f(system, f, r, virial=True)
+        en = dict(en, vir=en["vir"] + dvir, Pvir=np.asarray(en["Pvir"]) + dpvir)
     meas = np.zeros(13)
     _, _, it, ek = orc.shake_step(r, r1, f, p["h"], eps=p["epsc"], omega=om, meas=meas)
     press = O.measure_pressure(en, meas, ek, orc.L)
