@@ -298,9 +298,12 @@ def run_ours(args, rank, world, local):
     kavg = kms / max(kcnt, 1)
     achieved = algo.get(name, 0) / (kavg * 1e-3) / 1e12 if kavg > 0 else 0.0
     # the pair step's kernel: the group kernel (pair_variant 8), its half-shell
-    # form (9) or the cell kernel
-    if name == "pair_mixed" and tuned.get("pair_variant", 0) in (8, 9):
-        name = "pair_group" if tuned["pair_variant"] == 8 else "pair_half"
+    # forms (9: lanes on the home sites, 10: lanes on the neighbours; with
+    # Drude shells 10 runs 9) or the cell kernel
+    if name == "pair_mixed" and tuned.get("pair_variant", 0) in (8, 9, 10):
+        pv = tuned["pair_variant"]
+        name = {8: "pair_group", 9: "pair_half", 10: "pair_half" if system.polar
+                else "pair_half_t"}[pv]
         algo[name] = algo["pair_mixed"]
         achieved = algo[name] / (kavg * 1e-3) / 1e12 if kavg > 0 else 0.0
     traffic = None
@@ -634,7 +637,8 @@ def main():
     ap.add_argument("--equilibrate", type=int, default=400,
                     help="relax the lattice start (rigid molecules, velocity rescaling)")
     ap.add_argument("--pair-variant", type=int, default=None,
-                    help="FP32 pair kernel (mg_params.pair_variant; 8 = the group kernel), "
+                    help="FP32 pair kernel (mg_params.pair_variant; 8 = the group kernel, "
+                         "9 and 10 its half-shell forms), "
                          "instead of the autotuner's choice")
     ap.add_argument("--cells", type=int, default=None,
                     help="cells per cutoff instead of the autotuner's choice")

@@ -134,7 +134,9 @@ typedef struct {
      9 = the group kernel with Newton's third law (every pair once, over a
      half-shell stencil; forces, of the shells too, summed in 64-bit fixed
      point, 2^-32 K/A, by integer atomics, so still reproducible bit for
-     bit);
+     bit), lanes on the home sites; 10 = the same with lanes on the
+     neighbours (each lane runs one neighbour against the group's home
+     sites; with Drude shells 9 runs);
      otherwise the cell kernel with bit 0 = 8 warps per home cell (else 4),
      bit 2 = 16 warps per home cell (over bit 0), bit 1 = the erfc force
      spline in shared memory (else read through L1).  mg_autotune picks it. */
@@ -397,16 +399,16 @@ int mg_xwidom(mg_ctx *ctx, int nlist, const int *mols, const int *vtype, const d
    split (kspace_ctas_per_sm 6, 10, 16) and writes the fastest pair into
    *par, then the fastest of the 8 cell-kernel pair_variant values at that
    choice, of the group kernel (pair_variant 8) at every subdivision and,
-   on the FP32 path, of its half-shell form (pair_variant 9) at every
-   subdivision, each timed (FP32 path) with
+   on the FP32 path, of its half-shell forms (pair_variant 9 and 10) at
+   every subdivision, each timed (FP32 path) with
    kspace_serial 0 and 1, the pair chosen together.  Builds and frees its
-   own trial contexts; ms[25] (optional) gets the time per evaluation of
+   own trial contexts; ms[28] (optional) gets the time per evaluation of
    each trial (the best of three blocks of nrep evaluations; cdiv-major,
    then the 8 cell-kernel variants, the group
-   kernel at cdiv 1..3 and the half-shell group kernel at cdiv 1..3, the
+   kernel at cdiv 1..3 and the half-shell group kernel (9) at cdiv 1..3, the
    faster of the two kspace_serial settings each, then the chosen variant
-   with kspace_serial 0 and 1; -1 if that grid is not possible or the trial
-   did not run). */
+   with kspace_serial 0 and 1, then pair_variant 10 at cdiv 1..3; -1 if that
+   grid is not possible or the trial did not run). */
 int mg_autotune(const mg_topology *top, mg_params *par, const double *r, int nrep, double *ms);
 
 /* ---- adjoint ----

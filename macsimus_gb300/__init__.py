@@ -166,10 +166,10 @@ def autotune(system, L, cutoff, alpha, kappa, r, nrep=3, **kw):
     """the fastest (cells_per_cutoff, kspace_ctas_per_sm, pair_variant,
     kspace_serial) for this box and configuration (mg_autotune), with the
     timings (3x3 grid x split, the 8 cell-kernel pair variants, the group
-    kernel and its half-shell form at cdiv 1..3, the chosen variant with the
-    Ewald chain concurrent and serial)"""
+    kernel and its two half-shell forms at cdiv 1..3, the chosen variant
+    with the Ewald chain concurrent and serial)"""
     t, p, keep = describe(system, L, cutoff, alpha, kappa, **kw)
-    ms = np.full(25, -1.0)
+    ms = np.full(28, -1.0)
     rr = _arr(r, np.float64).reshape(-1)
     rc = library().mg_autotune(C.byref(t), C.byref(p), rr.ctypes.data_as(_dp), int(nrep),
                                ms.ctypes.data_as(_dp))
@@ -178,7 +178,7 @@ def autotune(system, L, cutoff, alpha, kappa, r, nrep=3, **kw):
     return dict(cells_per_cutoff=p.cells_per_cutoff, kspace_ctas_per_sm=p.kspace_ctas_per_sm,
                 pair_variant=p.pair_variant, kspace_serial=p.kspace_serial,
                 ms=ms[:9].reshape(3, 3), ms_pair=ms[9:17], ms_group=ms[17:20],
-                ms_half=ms[20:23], ms_serial=ms[23:25])
+                ms_half=ms[20:23], ms_serial=ms[23:25], ms_half_t=ms[25:28])
 
 
 def fp32_peak_tflops():

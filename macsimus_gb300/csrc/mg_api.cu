@@ -63,7 +63,7 @@ struct mg_ctx {
   // group, its grid; nprows = energy rows of the pair kernel (cell or group)
   int4* d_spans = nullptr;
   int nspans = 0, ngroup_grid = 0, nprows = 0;
-  // its half-shell form (pair_variant 9): the half stencil as z-runs and the
+  // its half-shell forms (pair_variant 9, 10): the half stencil as z-runs and the
   // 64-bit fixed-point force sums (sorted order, zero between evaluations)
   int4* d_hspans = nullptr;
   int nhspans = 0;
@@ -346,8 +346,8 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   ctx->minqq = p->minqq > 0 ? p->minqq : 1.0;
   ctx->use_list = p->skin > 0;
   ctx->pair_variant = p->pair_variant;
-  if (ctx->pair_variant < 0 || ctx->pair_variant > 9)
-    return fail(ctx, MG_ERR_ARG, "pair_variant must be 0..9");
+  if (ctx->pair_variant < 0 || ctx->pair_variant > 10)
+    return fail(ctx, MG_ERR_ARG, "pair_variant must be 0..10");
   ctx->thermostat = p->thermostat;
   if (ctx->thermostat < 0 || ctx->thermostat > 3)
     return fail(ctx, MG_ERR_ARG, "thermostat: 0 none, 1 Berendsen, 2 Bussi, 3 Nose-Hoover");
@@ -687,7 +687,7 @@ int setup(mg_ctx* ctx, const mg_topology* t, const mg_params* p) {
   CK(upload(&ctx->d_stencil, st.data(), st.size()));
   CK(upload(&ctx->d_spans, spans.data(), spans.size()));
   CK(upload(&ctx->d_hspans, hspans.data(), hspans.size()));
-  if (ctx->pair_variant == 9) {
+  if (ctx->pair_variant >= 9) {
     // centres, then (Drude builds) shells
     const size_t nfix = 3 * (size_t)ns * (t->chargepol ? 2 : 1);
     CK(dalloc(&ctx->d_facc, nfix));
@@ -1098,7 +1098,8 @@ PairArgs make_pair_args(mg_ctx* ctx, double* f_dev) {
   pa.pair_warps = (ctx->pair_variant & 4) ? 16 : ((ctx->pair_variant & 1) ? 8 : 4);
   pa.spline_smem = (ctx->pair_variant & 2) && ctx->ntab * 16 <= 200 * 1024 ? 1 : 0;
   pa.group = (ctx->pair_variant & 8) ? 1 : 0;
-  pa.newton = ctx->pair_variant == 9 ? 1 : 0;
+  // half shell: 1 lanes on the home sites, 2 lanes on the neighbours
+  pa.newton = ctx->pair_variant == 9 ? 1 : (ctx->pair_variant == 10 ? 2 : 0);
   pa.hspans = ctx->d_hspans;
   pa.nhspans = ctx->nhspans;
   pa.facc = ctx->d_facc;
@@ -3099,9 +3100,12 @@ int mg_autotune(const mg_topology* top, mg_params* par, const double* r, int nre
     // the group pair kernel (variant 8) at every cell subdivision: its
     // pruning favours other cells than the cell kernel does
     for (int a = 0; a < 3 && rc == MG_OK; a++) consider(8, cd[a], ms ? ms + 17 + a : nullptr);
-    // and its half-shell form (Newton's third law; FP32 path)
-    if (par->precision == MG_MIXED)
+    // and its half-shell forms (Newton's third law; FP32 path): lanes on the
+    // home sites, and lanes on the neighbours
+    if (par->precision == MG_MIXED) {
       for (int a = 0; a < 3 && rc == MG_OK; a++) consider(9, cd[a], ms ? ms + 20 + a : nullptr);
+      for (int a = 0; a < 3 && rc == MG_OK; a++) consider(10, cd[a], ms ? ms + 25 + a : nullptr);
+    }
   }
   if (ms) {
     ms[23] = tser[0];

@@ -153,9 +153,10 @@ struct PairArgs {
   const int4* spans;
   int nspans;
   int ngrid;                // CTAs of the group kernel (its energy rows)
-  // the group kernel with Newton's third law (pair_variant 9, no Drude
-  // shells): the half-shell z-runs, and the 64-bit fixed-point force sums
-  // (2^-32 K/A units, sorted order, kept zero between evaluations)
+  // the group kernel with Newton's third law (pair_variant 9: 1, lanes on
+  // the home sites; pair_variant 10: 2, lanes on the neighbours, shells as
+  // 1): the half-shell z-runs, and the 64-bit fixed-point force sums (2^-32
+  // K/A units, sorted order, kept zero between evaluations)
   int newton;
   const int4* hspans;
   int nhspans;

@@ -1102,6 +1102,254 @@ __global__ void __launch_bounds__(NW * 32, MEASURE ? 1 : (POLAR ? 5 : 7))
   }
 }
 
+// ------------------------------ group kernel, half shell, lanes on the
+// neighbours (pair_variant 10, no Drude shells) --
+//
+// The work items, the half-shell z-runs, the candidate pruning against the
+// cutoff sphere around the group's bounding box and the pair terms are
+// those of pair_half_mixed_kernel; the roles of the lanes are transposed.
+// The kept candidates are compacted into a ring of 64 per warp; whenever
+// 32 are queued, each lane takes one and runs it against the group's (up
+// to 8) home sites in turn, which every lane reads from shared memory
+// (broadcast).  The neighbour's force stays in the lane's registers and goes
+// into the fixed-point sums with three atomics after the 8 home sites: no
+// per-pair shuffles, one float-to-integer conversion per component and
+// neighbour.  The home sites' forces stay in 24 registers per lane and are
+// reduce-scattered over the 32 lanes once per group (lane 3 i + d ends with
+// component d of site i).  Home sites beyond the group's end are skipped by
+// a warp-uniform test.  Every rounding is explicit, as in the lane-per-home
+// kernel, so the measuring and the plain instantiation move the sites
+// identically; the integer sums make the forces bit-reproducible.
+
+// the z-ranges of half-shell span sp around cell (cx, cy, cz): column index
+// col; run [ra0, ra1] and, where the run wraps through the box, [rb0, rb1]
+__device__ __forceinline__ void half_span_runs(const PairArgs& a, int sp, int cx, int cy,
+                                               int cz, int& col, int& ra0, int& ra1, int& rb0,
+                                               int& rb1) {
+  const int4 o = a.hspans[sp];
+  int x2 = cx + o.x, y2 = cy + o.y;
+  x2 += (x2 < 0) ? a.ncx : (x2 >= a.ncx ? -a.ncx : 0);
+  y2 += (y2 < 0) ? a.ncy : (y2 >= a.ncy ? -a.ncy : 0);
+  col = (x2 * a.ncy + y2) * a.ncz;
+  int za = cz + o.z, zb = cz + o.w;
+  if (zb < 0) { za += a.ncz; zb += a.ncz; }
+  if (za >= a.ncz) { za -= a.ncz; zb -= a.ncz; }
+  rb0 = 0;
+  rb1 = -1;
+  if (za < 0) { ra0 = za + a.ncz; ra1 = a.ncz - 1; rb1 = zb; }
+  else if (zb >= a.ncz) { ra0 = za; ra1 = a.ncz - 1; rb1 = zb - a.ncz; }
+  else { ra0 = za; ra1 = zb; }
+}
+
+constexpr int HT_RING = 64;   // compacted candidates per warp (a power of two >= 63)
+// 6 CTAs per SM (80 registers, no spills): on 32768 waters with cells of
+// half the cutoff 0.305 ms, against 0.320 ms with 7 (72 registers and a
+// spill) and 0.332 ms with 8; the lane-per-home kernel takes 0.363 ms there
+#ifndef MG_HALF_T_MINB
+#define MG_HALF_T_MINB 6      // CTAs per SM the register budget is set for
+#endif
+
+template <bool MEASURE, int NW>
+__global__ void __launch_bounds__(NW * 32, MEASURE ? 1 : MG_HALF_T_MINB)
+    pair_half_t_mixed_kernel(PairArgs a, const int4* __restrict__ pj,
+                             const PairF* __restrict__ ptab_g, const float4* __restrict__ erd,
+                             const float4* __restrict__ eru, float sx, float sy, float sz,
+                             float cq, float sgrid) {
+  constexpr int NT = NW * 32;
+  extern __shared__ float4 dyn_smem[];   // the nk x nk FP32 pair table
+  __shared__ float4 sq[NW][HT_RING];     // candidate positions (w: kind | mol << 8)
+  __shared__ int sqt[NW][HT_RING];       // candidate sorted index
+  __shared__ float4 sh[NW][GROUP_SITES]; // the group's home sites
+  __shared__ double ered[MEASURE ? NT : 1];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int il = lane & 7;
+  const int nk = a.nkind, ntab = a.ntab;
+  PairFS* ptab = reinterpret_cast<PairFS*>(dyn_smem);
+  for (int t = threadIdx.x; t < 3 * nk * nk; t += NT)
+    dyn_smem[t] = reinterpret_cast<const float4*>(ptab_g + t / 3)[t % 3];
+  __syncthreads();
+  const int ncell = a.ncx * a.ncy * a.ncz;
+  const int nitems = a.gstart[ncell];
+  unsigned long long* facc = reinterpret_cast<unsigned long long*>(a.facc);
+  CSum es[9];
+
+  for (int item = blockIdx.x * NW + warp; item < nitems; item += gridDim.x * NW) {
+    const int c = a.gcell[item];
+    const int cz = c % a.ncz, cy = (c / a.ncz) % a.ncy, cx = c / (a.ncy * a.ncz);
+    const int hs = a.cell_start[c], he = a.cell_start[c + 1];
+    const int i0 = hs + GROUP_SITES * (item - a.gstart[c]);
+    const int ni = min(GROUP_SITES, he - i0);
+    const unsigned refx = (unsigned)((((unsigned long long)(2 * cx + 1)) << 31) / a.ncx),
+                   refy = (unsigned)((((unsigned long long)(2 * cy + 1)) << 31) / a.ncy),
+                   refz = (unsigned)((((unsigned long long)(2 * cz + 1)) << 31) / a.ncz);
+    // the home sites (every 8-lane group holds all of them) and their box
+    const bool vi = il < ni;
+    const int4 me = vi ? pj[i0 + il] : make_int4(0, 0, 0, 0);
+    const float xi = __fmul_rn((float)(int)((unsigned)me.x - refx), sx),
+                yi = __fmul_rn((float)(int)((unsigned)me.y - refy), sy),
+                zi = __fmul_rn((float)(int)((unsigned)me.z - refz), sz);
+    float blx = vi ? xi : 3e38f, bly = vi ? yi : 3e38f, blz = vi ? zi : 3e38f;
+    float bhx = vi ? xi : -3e38f, bhy = vi ? yi : -3e38f, bhz = vi ? zi : -3e38f;
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+      blx = fminf(blx, __shfl_xor_sync(0xffffffffu, blx, o));
+      bly = fminf(bly, __shfl_xor_sync(0xffffffffu, bly, o));
+      blz = fminf(blz, __shfl_xor_sync(0xffffffffu, blz, o));
+      bhx = fmaxf(bhx, __shfl_xor_sync(0xffffffffu, bhx, o));
+      bhy = fmaxf(bhy, __shfl_xor_sync(0xffffffffu, bhy, o));
+      bhz = fmaxf(bhz, __shfl_xor_sync(0xffffffffu, bhz, o));
+    }
+    __syncwarp();   // the previous group's readers of sh are done
+    if (lane < GROUP_SITES) sh[warp][lane] = make_float4(xi, yi, zi, __int_as_float(me.w));
+    __syncwarp();
+    float hx[GROUP_SITES], hy[GROUP_SITES], hz[GROUP_SITES];
+#pragma unroll
+    for (int i = 0; i < GROUP_SITES; i++) hx[i] = hy[i] = hz[i] = 0.f;
+
+    // cnt queued candidates from ring slot h0: lane -> one candidate
+    // against the home sites
+    auto run = [&](int h0, int cnt) {
+      const bool vt = lane < cnt;
+      const int e = vt ? (h0 + lane) & (HT_RING - 1) : h0;   // a valid slot for idle lanes
+      const float4 q = sq[warp][e];
+      const int tj = sqt[warp][e];
+      const int qw = __float_as_int(q.w);
+      const int kj = qw & 255;
+      // a candidate in the home cell pairs with the home sites before it
+      const bool inh = (unsigned)(tj - hs) < (unsigned)(he - hs);
+      const int dj = tj - i0;
+      float px = 0.f, py = 0.f, pz = 0.f;
+      float e_el = 0.f, e_lj = 0.f, e_vir = 0.f;
+      PvF pv;
+      pv.zero();
+#pragma unroll
+      for (int i = 0; i < GROUP_SITES; i++) {
+        if (i < ni) {
+          const float4 h = sh[warp][i];
+          const float dx = __fadd_rn(h.x, -q.x), dy = __fadd_rn(h.y, -q.y),
+                      dz = __fadd_rn(h.z, -q.z);
+          const float rr = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
+          const int hw = __float_as_int(h.w);
+          const bool ok = vt && rr < cq && ((hw ^ qw) >> 8) != 0 && (!inh || dj > i);
+          const PairFS P = ptab[(hw & 255) * nk + kj];
+          float flj;
+          float f = pair_force_rn(P, rr, erd, sgrid, ntab, flj);
+          f = ok ? f : 0.f;
+          hx[i] = __fmaf_rn(f, dx, hx[i]);
+          hy[i] = __fmaf_rn(f, dy, hy[i]);
+          hz[i] = __fmaf_rn(f, dz, hz[i]);
+          px = __fmaf_rn(f, dx, px);
+          py = __fmaf_rn(f, dy, py);
+          pz = __fmaf_rn(f, dz, pz);
+          if (MEASURE && ok) {
+            // energies and virial: no effect on the forces
+            const float x = __fdividef(P.Sq, rr), y = x * x * x, xt = rr - P.C2q;
+            e_lj += rr < P.C1q ? P.E4 * fmaf(y, y, -y) : (rr < P.C2q ? P.A * xt * xt : 0.f);
+            e_vir += rr * flj;
+            float e_el_p = 0.f;
+            spline_any<true, true>(erd, eru, rr, sgrid, ntab, P.qq, e_el_p);
+            e_el += e_el_p;
+            pv.add(dx, dy, dz, f);
+          }
+        }
+      }
+      if (vt) {
+        unsigned long long* fj = facc + 3 * (long)tj;
+        atomicAdd(fj, (unsigned long long)__float2ll_rn(__fmul_rn(px, -(float)FIX_SCALE)));
+        atomicAdd(fj + 1, (unsigned long long)__float2ll_rn(__fmul_rn(py, -(float)FIX_SCALE)));
+        atomicAdd(fj + 2, (unsigned long long)__float2ll_rn(__fmul_rn(pz, -(float)FIX_SCALE)));
+      }
+      if (MEASURE) {
+        es[0].add(e_el); es[1].add(e_lj); es[2].add(e_vir);
+        es[3].add(pv.p0); es[4].add(pv.p1); es[5].add(pv.p2);
+        es[6].add(pv.p3); es[7].add(pv.p4); es[8].add(pv.p5);
+      }
+      __syncwarp();   // the slots read here may be refilled next
+    };
+
+    int qh = 0, qn = 0;   // ring head and count (warp-uniform)
+    for (int sp = 0; sp < a.nhspans; sp++) {
+      int col, ra0, ra1, rb0, rb1;
+      half_span_runs(a, sp, cx, cy, cz, col, ra0, ra1, rb0, rb1);
+      for (int part = 0; part < 2; part++) {
+        const int z0 = part ? rb0 : ra0, z1 = part ? rb1 : ra1;
+        if (z1 < z0) continue;
+        // home-cell sites before the group pair with it from their own group
+        const int j0 = max(a.cell_start[col + z0], col + z0 == c ? i0 : 0),
+                  j1 = a.cell_start[col + z1 + 1];
+        for (int jb = j0; jb < j1; jb += 32) {
+          const int j = jb + lane;
+          bool keep = false;
+          float4 f4 = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (j < j1) {
+            const int4 q = pj[j];
+            f4 = make_float4(__fmul_rn((float)(int)((unsigned)q.x - refx), sx),
+                             __fmul_rn((float)(int)((unsigned)q.y - refy), sy),
+                             __fmul_rn((float)(int)((unsigned)q.z - refz), sz),
+                             __int_as_float(q.w));
+            const float ddx = fmaxf(fmaxf(blx - f4.x, f4.x - bhx), 0.f),
+                        ddy = fmaxf(fmaxf(bly - f4.y, f4.y - bhy), 0.f),
+                        ddz = fmaxf(fmaxf(blz - f4.z, f4.z - bhz), 0.f);
+            keep = fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz)) < cq;
+          }
+          const unsigned M = __ballot_sync(0xffffffffu, keep);
+          if (keep) {
+            // qn < 32 here, so the new slots never reach the queued ones
+            const int slot = (qh + qn + __popc(M & ((1u << lane) - 1u))) & (HT_RING - 1);
+            sq[warp][slot] = f4;
+            sqt[warp][slot] = j;
+          }
+          qn += __popc(M);
+          __syncwarp();
+          if (qn >= 32) {
+            run(qh, 32);
+            qh = (qh + 32) & (HT_RING - 1);
+            qn -= 32;
+          }
+        }
+      }
+    }
+    if (qn > 0) run(qh, qn);
+
+    // the home sites' sums: reduce-scatter of v[3 i + d] (24 values, 8
+    // zero) over the lanes in a fixed order; lane k ends with v[k]
+    float v[32];
+#pragma unroll
+    for (int i = 0; i < GROUP_SITES; i++) {
+      v[3 * i] = hx[i];
+      v[3 * i + 1] = hy[i];
+      v[3 * i + 2] = hz[i];
+    }
+#pragma unroll
+    for (int k = 3 * GROUP_SITES; k < 32; k++) v[k] = 0.f;
+#pragma unroll
+    for (int w = 16; w >= 1; w >>= 1) {
+      const bool up = (lane & w) != 0;
+#pragma unroll
+      for (int k = 0; k < w; k++) {
+        const float keepv = up ? v[w + k] : v[k], sendv = up ? v[k] : v[w + k];
+        v[k] = __fadd_rn(keepv, __shfl_xor_sync(0xffffffffu, sendv, w));
+      }
+    }
+    if (lane < 3 * ni)
+      atomicAdd(facc + 3 * (long)i0 + lane,
+                (unsigned long long)__float2ll_rn(__fmul_rn(v[0], (float)FIX_SCALE)));
+  }
+  if (MEASURE) {
+    // every unordered pair once; one row per CTA
+    for (int k = 0; k < 9; k++) {
+      ered[threadIdx.x] = es[k].value();
+      __syncthreads();
+      for (int w = NT / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) ered[threadIdx.x] += ered[threadIdx.x + w];
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) a.epart[blockIdx.x * NEN + k] = ered[0];
+      __syncthreads();
+    }
+  }
+}
+
 // the fixed-point sums (sorted order) into the FP64 forces (site order),
 // with shells the second half of each; the sums are cleared for the next
 // evaluation
@@ -1139,8 +1387,21 @@ cudaError_t k_pair_mixed(const Launch& L, const PairArgs& a, const int4* pj, con
       pair_half_mixed_kernel<M, P, GROUP_WARPS><<<a.ngrid, GROUP_WARPS * 32, gsm, L.s>>>(      \
           a, pj, ptab, erd, eru, sx, sy, sz, cq, sg);                                           \
   } while (0)
+#define PAIR_HALF_T(M)                                                                          \
+  do {                                                                                          \
+    if (gsm > 48 * 1024)                                                                        \
+      ge = cudaFuncSetAttribute(pair_half_t_mixed_kernel<M, GROUP_WARPS>,                      \
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm);         \
+    if (ge == cudaSuccess)                                                                      \
+      pair_half_t_mixed_kernel<M, GROUP_WARPS><<<a.ngrid, GROUP_WARPS * 32, gsm, L.s>>>(       \
+          a, pj, ptab, erd, eru, sx, sy, sz, cq, sg);                                           \
+  } while (0)
+    // lanes on the neighbours (newton 2) without shells; with shells the
+    // lane-per-home kernel
     if (polar) { if (measure) PAIR_HALF(true, true); else PAIR_HALF(false, true); }
+    else if (a.newton == 2) { if (measure) PAIR_HALF_T(true); else PAIR_HALF_T(false); }
     else { if (measure) PAIR_HALF(true, false); else PAIR_HALF(false, false); }
+#undef PAIR_HALF_T
 #undef PAIR_HALF
     if (ge != cudaSuccess) return ge;
     LAUNCHED(L);
@@ -1362,19 +1623,27 @@ __global__ void __launch_bounds__(PAIR_THREADS)
 // the FP64 positions (nearest image), the term in FP32 as in the pair
 // kernels, forces and energy summed in FP64.  Pairs beyond the cutoff are
 // skipped, as the cell traversal never meets them.
+// The force arithmetic rounds explicitly (`_rn`): the measuring
+// instantiation also uses the products for the virial, and a product the
+// compiler fuses into the force sum in one instantiation and not in the
+// other would move the sites of a measured step differently.
+__device__ __forceinline__ double excl_r2(double dx, double dy, double dz) {
+  return __fma_rn(dx, dx, __fma_rn(dy, dy, __dmul_rn(dz, dz)));
+}
+
 template <bool MEASURE>
 __device__ __forceinline__ void excl_pair(double dx, double dy, double dz, double qq, float alpha,
                                           double* fi, double* fj, double* en) {
   float fe;
-  const float e = excl_term<float>((float)(dx * dx + dy * dy + dz * dz), alpha, &fe);
-  const double fq = (double)fe * qq;
-  const double Fx = fq * dx, Fy = fq * dy, Fz = fq * dz;
-  fi[0] += Fx;
-  fi[1] += Fy;
-  fi[2] += Fz;
-  fj[0] -= Fx;
-  fj[1] -= Fy;
-  fj[2] -= Fz;
+  const float e = excl_term<float>((float)excl_r2(dx, dy, dz), alpha, &fe);
+  const double fq = __dmul_rn((double)fe, qq);
+  const double Fx = __dmul_rn(fq, dx), Fy = __dmul_rn(fq, dy), Fz = __dmul_rn(fq, dz);
+  fi[0] = __dadd_rn(fi[0], Fx);
+  fi[1] = __dadd_rn(fi[1], Fy);
+  fi[2] = __dadd_rn(fi[2], Fz);
+  fj[0] = __dadd_rn(fj[0], -Fx);
+  fj[1] = __dadd_rn(fj[1], -Fy);
+  fj[2] = __dadd_rn(fj[2], -Fz);
   if (MEASURE) {
     en[0] += (double)e * qq;
     en[1] += Fx * dx;
@@ -1407,7 +1676,7 @@ MG_BODY void excl_mixed_kernel_body(const ExclArgs& a,
       const double dx = near_img(ri[0] - rj[0], a.Lx, a.iLx),
                    dy = near_img(ri[1] - rj[1], a.Ly, a.iLy),
                    dz = near_img(ri[2] - rj[2], a.Lz, a.iLz);
-      if (!(dx * dx + dy * dy + dz * dz < a.cutoff_sq)) continue;
+      if (!(excl_r2(dx, dy, dz) < a.cutoff_sq)) continue;
       double* fi = a.f + 3 * (long)ij.x;
       double* fj = a.f + 3 * (long)ij.y;
       if (q.x != 0) excl_pair<MEASURE>(dx, dy, dz, q.x, a.alpha, fi, fj, en);

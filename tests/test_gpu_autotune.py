@@ -24,17 +24,17 @@ def test_autotune_choice_and_forces(precision):
                   [6, 10, 16].index(best["kspace_ctas_per_sm"])] == ms[ms > 0].min()
     else:
         # the group kernel or its half-shell form: its fastest subdivision
-        mg = best["ms_group"] if best["pair_variant"] == 8 else best["ms_half"]
+        mg = {8: best["ms_group"], 9: best["ms_half"], 10: best["ms_half_t"]}[best["pair_variant"]]
         assert mg[best["cells_per_cutoff"] - 1] == mg[mg > 0].min()
     if precision == "fp64":
-        assert (best["ms_half"] < 0).all()
+        assert (best["ms_half"] < 0).all() and (best["ms_half_t"] < 0).all()
     if precision == "mixed":
         # the Ewald chain beside or after the r-space chain, chosen with the variant
         assert best["kspace_serial"] in (0, 1)
         s = best["ms_serial"]
         assert s[best["kspace_serial"]] == s[s > 0].min()
     f0, _ = M.ForcePath(*args, precision=precision).forces(g["r"][0])
-    assert best["pair_variant"] in range(10)
+    assert best["pair_variant"] in range(11)
     f1, _ = M.ForcePath(*args, precision=precision, cells_per_cutoff=best["cells_per_cutoff"],
                         kspace_ctas_per_sm=best["kspace_ctas_per_sm"],
                         pair_variant=best["pair_variant"]).forces(g["r"][0])

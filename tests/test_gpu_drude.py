@@ -44,7 +44,7 @@ def test_drude_forces(precision):
         assert abs(en["lj"] - eo["lj"]) <= (1e-10 if precision == "fp64" else 1e-5) * abs(eo["lj"])
 
 
-@pytest.mark.parametrize("variant", [8, 9])
+@pytest.mark.parametrize("variant", [8, 9, 10])
 def test_drude_group_kernels(variant):
     """the group kernel (8) and its half-shell form (9: every pair once, the
     neighbour's centre and shell forces in fixed point) with Drude shells:

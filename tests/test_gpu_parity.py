@@ -106,12 +106,13 @@ def test_cell_list_is_deterministic(precision):
 
 
 @pytest.mark.parametrize("case", ["spce864", "brine532"])
-@pytest.mark.parametrize("variant", [8, 9])
+@pytest.mark.parametrize("variant", [8, 9, 10])
 def test_group_pair_kernel_matches_oracle(case, variant):
     """the group pair kernel (pair_variant 8: warps over groups of 8 home
     sites, neighbours pruned against the group's bounding box) and its
-    half-shell form (9: every pair once, forces in fixed point) give the
-    oracle's forces and energies as the cell kernel does"""
+    half-shell forms (every pair once, forces in fixed point; 9 lanes on the
+    home sites, 10 lanes on the neighbours) give the oracle's forces and
+    energies as the cell kernel does"""
     g, meta, system, ew, fc = make(case, "mixed")
     _, _, _, _, fg = make(case, "mixed", pair_variant=variant)
     orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
@@ -133,12 +134,12 @@ def test_group_pair_kernel_matches_oracle(case, variant):
 
 @pytest.mark.parametrize("cells", [2, 3])
 @pytest.mark.parametrize("polar", [False, True])
-@pytest.mark.parametrize("variant", [8, 9])
+@pytest.mark.parametrize("variant", [8, 9, 10])
 def test_group_pair_kernel_full_size(cells, polar, variant):
     """32768 waters (SPC/E, or with Drude shells displaced at random): the
-    group kernel and its half-shell form (Drude builds run the group kernel
-    for it) equal the cell kernel within the mixed rounding, for cells of a
-    half and of a third of the cutoff"""
+    group kernel and its half-shell forms (Drude builds run the lane-per-home
+    half-shell kernel for 10) equal the cell kernel within the mixed
+    rounding, for cells of a half and of a third of the cutoff"""
     from macsimus_gb300 import configs
     w = configs.workload("drude32768" if polar else "spce32768", seed=3)
     r = w["r"].copy()
@@ -156,12 +157,14 @@ def test_group_pair_kernel_full_size(cells, polar, variant):
 
 
 @pytest.mark.parametrize("cells", [1, 2, 3])
-def test_half_shell_kernel_every_pair_once(cells):
+@pytest.mark.parametrize("variant", [9, 10])
+def test_half_shell_kernel_every_pair_once(cells, variant):
     """the half-shell group kernel at every cell subdivision (the column
     (0, 0) from the home cell up, pairs inside a cell from the lower sorted
     index): the oracle's forces, LJ energy and virial, so no pair is missing
     or taken twice"""
-    g, meta, system, ew, fh = make("spce864", "mixed", pair_variant=9, cells_per_cutoff=cells)
+    g, meta, system, ew, fh = make("spce864", "mixed", pair_variant=variant,
+                                   cells_per_cutoff=cells)
     orc = O.Oracle(system, ew["L"], ew["cutoff"], ew["alpha"], ew["kappa"])
     f, en = fh.forces(g["r"][0], measure=True)
     fo, eo = orc.forces(g["r"][0], nthreads=4)
@@ -171,13 +174,17 @@ def test_half_shell_kernel_every_pair_once(cells):
     assert abs(en["vir"] - eo["vir"]) <= 2e-5 * abs(eo["vir"])
 
 
-@pytest.mark.parametrize("variant", [8, 9])
+@pytest.mark.parametrize("variant", [8, 9, 10])
 def test_group_kernel_md_is_reproducible(variant):
     """MD with the group kernel and its half-shell form: the same trajectory
     bit for bit on every run, with and without measurement (the half-shell
     kernel's fixed-point force sums do not depend on the order in which the
     atomics land)"""
-    g, meta, system, ew, _ = make("spce864", "mixed")
+    g, meta, system, ew, fq = make("spce864", "mixed", pair_variant=variant)
+    # the measuring kernels round the forces as the plain ones do
+    fa, _ = fq.forces(g["r"][0], measure=True)
+    fb, _ = fq.forces(g["r"][0], measure=False)
+    assert np.array_equal(fa, fb)
 
     def run(measure):
         _, _, _, _, fp = make("spce864", "mixed", pair_variant=variant)
