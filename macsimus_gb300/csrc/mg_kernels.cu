@@ -1116,8 +1116,8 @@ __global__ void __launch_bounds__(NW * 32, MEASURE ? 1 : (POLAR ? 5 : 7))
 // per-pair shuffles, one float-to-integer conversion per component and
 // neighbour.  The home sites' forces stay in 24 registers per lane and are
 // reduce-scattered over the 32 lanes once per group (lane 3 i + d ends with
-// component d of site i).  Home sites beyond the group's end are skipped by
-// a warp-uniform test.  Every rounding is explicit, as in the lane-per-home
+// component d of site i).  Home sites beyond the group's end are masked
+// out of the pair test.  Every rounding is explicit, as in the lane-per-home
 // kernel, so the measuring and the plain instantiation move the sites
 // identically; the integer sums make the forces bit-reproducible.
 
@@ -1142,11 +1142,11 @@ __device__ __forceinline__ void half_span_runs(const PairArgs& a, int sp, int cx
 }
 
 constexpr int HT_RING = 64;   // compacted candidates per warp (a power of two >= 63)
-// 6 CTAs per SM (80 registers, no spills): on 32768 waters with cells of
-// half the cutoff 0.305 ms, against 0.320 ms with 7 (72 registers and a
-// spill) and 0.332 ms with 8; the lane-per-home kernel takes 0.363 ms there
+// 5 CTAs per SM (96 registers): on 32768 waters with cells of half the
+// cutoff 0.283 ms, against 0.294 ms with 6 (80 registers and a spill); the
+// lane-per-home kernel takes 0.363 ms there
 #ifndef MG_HALF_T_MINB
-#define MG_HALF_T_MINB 6      // CTAs per SM the register budget is set for
+#define MG_HALF_T_MINB 5      // CTAs per SM the register budget is set for
 #endif
 
 template <bool MEASURE, int NW>
@@ -1222,15 +1222,19 @@ __global__ void __launch_bounds__(NW * 32, MEASURE ? 1 : MG_HALF_T_MINB)
       float e_el = 0.f, e_lj = 0.f, e_vir = 0.f;
       PvF pv;
       pv.zero();
+      // the home sites in turn, those beyond the group's end masked (sh
+      // holds finite positions for them): without a branch per site the
+      // compiler interleaves the sites' independent chains (0.283 ms on
+      // 32768 waters against 0.304 ms with a warp-uniform branch per site)
 #pragma unroll
       for (int i = 0; i < GROUP_SITES; i++) {
-        if (i < ni) {
+        {
           const float4 h = sh[warp][i];
           const float dx = __fadd_rn(h.x, -q.x), dy = __fadd_rn(h.y, -q.y),
                       dz = __fadd_rn(h.z, -q.z);
           const float rr = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
           const int hw = __float_as_int(h.w);
-          const bool ok = vt && rr < cq && ((hw ^ qw) >> 8) != 0 && (!inh || dj > i);
+          const bool ok = vt && i < ni && rr < cq && ((hw ^ qw) >> 8) != 0 && (!inh || dj > i);
           const PairFS P = ptab[(hw & 255) * nk + kj];
           float flj;
           float f = pair_force_rn(P, rr, erd, sgrid, ntab, flj);
