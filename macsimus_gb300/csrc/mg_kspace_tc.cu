@@ -32,11 +32,27 @@
 namespace mg {
 
 constexpr int TC_M = 128;             // charges per tile
-constexpr int TC_N = 128;             // D columns per tile
+#ifndef MG_KF_N
+#define MG_KF_N 128
+#endif
+#ifndef MG_KF_NS
+#define MG_KF_NS 2
+#endif
+// Pass-2 tile shape.  Measured on 32768 waters: 128 columns (32 k rows) in
+// two stages 0.219 ms, 64 columns in four stages (the same shared memory
+// and TMEM) 0.310 ms: the fixed cost of a tile's barrier round trips
+// outweighs the deeper pipeline.
+constexpr int TC_N = MG_KF_N;         // D columns per tile (64 or 128)
 constexpr int TC_ROWS = TC_N / 4;     // k rows per tile
+constexpr int TC_NS = MG_KF_NS;       // V stages in shared memory = TMEM buffers of TC_N columns
+static_assert(TC_N == 64 || TC_N == 128, "pass-2 tile: 64 or 128 columns");
+// tcgen05.alloc takes a power of two of at least 32 columns
+static_assert(TC_NS * TC_N <= 256 && (TC_NS * TC_N & (TC_NS * TC_N - 1)) == 0,
+              "pass-2 TMEM: a power of two of at most 256 columns");
 constexpr long TC_WAIT = 1L << 24;    // polls before a wait gives up
 constexpr int TC_EPI_WARPS = 16;      // four per TMEM lane quarter
 constexpr int TC_EPI_ROWS = TC_ROWS / (TC_EPI_WARPS / 4);   // rows per warp and tile
+constexpr int TC_EPI_LD = TC_EPI_ROWS / 4;                   // 16-column TMEM loads per warp and tile
 constexpr int TC_THREADS = 32 * (TC_EPI_WARPS + 1);
 constexpr int SK_G = 32;              // pass 1: charges per pipeline stage
 constexpr int SK_PW = 16;             // pass 1: producer warps
@@ -244,7 +260,7 @@ __device__ __forceinline__ void kf_tc_vb_body(int nrows, int ntn, int Kz, int KP
 // the callers; the row table is read from global memory)
 size_t kf_tc_smem(int KP, int nxy, int nrows) {
   (void)nrows;
-  return (size_t)1024 * (3 * KP + nxy) + 128;
+  return (size_t)1024 * (KP + nxy) + (size_t)TC_NS * 8 * TC_N * KP + 256;
 }
 
 __device__ __forceinline__ void kf_tc_body(const KfTc& a_in, const int bx_) {
@@ -252,35 +268,36 @@ __device__ __forceinline__ void kf_tc_body(const KfTc& a_in, const int bx_) {
   // registers instead of being reloaded through the reference
   const KfTc a = a_in;
   extern __shared__ __align__(1024) unsigned char smem_tc[];
-  const uint32_t zb = 1024u * a.KP;              // Z tile bytes (hi | lo); also a V tile
+  const uint32_t zb = 1024u * a.KP;              // Z tile bytes (hi | lo)
+  const uint32_t vbytes = 8u * TC_N * a.KP;      // V tile bytes (hi | lo)
   const uint32_t ab = zb + 1024u * a.nxy;        // A tile with the phase block
   unsigned char* As = smem_tc;
   const float2* XY = reinterpret_cast<const float2*>(smem_tc + zb);   // [nxy][128]
-  unsigned char* Bs = smem_tc + ab;              // two V stages of zb bytes
+  unsigned char* Bs = smem_tc + ab;              // TC_NS V stages of vbytes
   // the row table is read through L1 (every lane of a warp reads the same
   // row), which keeps nrows x 16 bytes out of shared memory: boxes up to
   // |n| <= 23 fit
-  uint64_t* bars = reinterpret_cast<uint64_t*>(Bs + 2 * (size_t)zb);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(Bs + (size_t)TC_NS * vbytes);
   uint64_t* bar_a = bars;
-  uint64_t* full = bars + 1;    // [2] V stage loaded
-  uint64_t* bfree = bars + 3;   // [2] V stage consumed
-  uint64_t* tfull = bars + 5;   // [2] TMEM buffer written
-  uint64_t* tfree = bars + 7;   // [2] TMEM buffer drained
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 9);
+  uint64_t* full = bars + 1;               // [NS] V stage loaded
+  uint64_t* bfree = full + TC_NS;          // [NS] V stage consumed
+  uint64_t* tfull = bfree + TC_NS;         // [NS] TMEM buffer written
+  uint64_t* tfree = tfull + TC_NS;         // [NS] TMEM buffer drained
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(tfree + TC_NS);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int mt = bx_;
   constexpr int PW = TC_EPI_WARPS;               // producer warp
 
   if (tid == 0) {
     tc::mbar_init(bar_a, 1);
-    for (int s = 0; s < 2; s++) {
+    for (int s = 0; s < TC_NS; s++) {
       tc::mbar_init(full + s, 1);
       tc::mbar_init(bfree + s, 1);
       tc::mbar_init(tfull + s, 1);
       tc::mbar_init(tfree + s, TC_EPI_WARPS);
     }
   }
-  if (warp == PW) tc::tmem_alloc(tslot, 2 * TC_N);
+  if (warp == PW) tc::tmem_alloc(tslot, TC_NS * TC_N);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -293,20 +310,21 @@ __device__ __forceinline__ void kf_tc_body(const KfTc& a_in, const int bx_) {
       const size_t atile_f = (size_t)2 * TC_M * (a.KP + a.nxy), vtile_f = (size_t)2 * TC_N * a.KP;
       tc::mbar_expect_tx(bar_a, ab);
       tc::bulk_g2s(As, a.za + (size_t)mt * atile_f, ab, bar_a);
-      for (int t = 0; t < 2 && t < a.ntn; t++) {
-        tc::mbar_expect_tx(full + t, zb);
-        tc::bulk_g2s(Bs + (size_t)t * zb, a.vb + (size_t)t * vtile_f, zb, full + t);
+      for (int t = 0; t < TC_NS && t < a.ntn; t++) {
+        tc::mbar_expect_tx(full + t, vbytes);
+        tc::bulk_g2s(Bs + (size_t)t * vbytes, a.vb + (size_t)t * vtile_f, vbytes, full + t);
       }
       bool ok = tc::mbar_wait(bar_a, 0, TC_WAIT);
       const uint32_t a_hi = tc::smem_u32(As), a_lo = a_hi + half;
+      // tile t: V stage and TMEM buffer s = t % NS, the (t / NS)-th use of each
       for (int t = 0; ok && t < a.ntn; t++) {
-        const int s = t & 1;
-        ok = tc::mbar_wait(full + s, (t >> 1) & 1, TC_WAIT);
-        if (ok && t >= 2) ok = tc::mbar_wait(tfree + s, ((t - 2) >> 1) & 1, TC_WAIT);
+        const int s = t % TC_NS, use = t / TC_NS;
+        ok = tc::mbar_wait(full + s, use & 1, TC_WAIT);
+        if (ok && use > 0) ok = tc::mbar_wait(tfree + s, (use - 1) & 1, TC_WAIT);
         if (!ok) break;
         tc::fence_after_sync();
         const uint32_t d = tbase + (uint32_t)(s * TC_N);
-        const uint32_t b_hi = tc::smem_u32(Bs + (size_t)s * zb), b_lo = b_hi + half;
+        const uint32_t b_hi = tc::smem_u32(Bs + (size_t)s * vbytes), b_lo = b_hi + vbytes / 2;
         for (int ks = 0; ks < a.KP / 8; ks++) {
           const uint32_t o = 256u * ks;
           tc::mma_tf32(d, tc::smem_desc(a_hi + o, 128, sbo), tc::smem_desc(b_hi + o, 128, sbo),
@@ -318,13 +336,14 @@ __device__ __forceinline__ void kf_tc_body(const KfTc& a_in, const int bx_) {
         }
         tc::mma_commit(tfull + s);
         tc::mma_commit(bfree + s);
-        // refill the stage of tile t-1 with tile t+1 once its products are done
-        if (t >= 1 && t + 1 < a.ntn) {
-          const int s1 = (t + 1) & 1;
-          ok = tc::mbar_wait(bfree + s1, ((t - 1) >> 1) & 1, TC_WAIT);
+        // refill the stage of tile t-1 with tile t-1+NS once its products are done
+        if (t >= 1 && t - 1 + TC_NS < a.ntn) {
+          const int s1 = (t - 1) % TC_NS;
+          ok = tc::mbar_wait(bfree + s1, ((t - 1) / TC_NS) & 1, TC_WAIT);
           if (!ok) break;
-          tc::mbar_expect_tx(full + s1, zb);
-          tc::bulk_g2s(Bs + (size_t)s1 * zb, a.vb + (size_t)(t + 1) * vtile_f, zb, full + s1);
+          tc::mbar_expect_tx(full + s1, vbytes);
+          tc::bulk_g2s(Bs + (size_t)s1 * vbytes, a.vb + (size_t)(t - 1 + TC_NS) * vtile_f, vbytes,
+                       full + s1);
         }
       }
       if (!ok) atomicOr(a.status, 16);
@@ -344,25 +363,26 @@ __device__ __forceinline__ void kf_tc_body(const KfTc& a_in, const int bx_) {
     // their latency hides behind the arithmetic (two register sets; the loop
     // is unrolled by two so that both stay in registers)
     auto wait_full = [&](int t) {
-      bool w = tc::mbar_wait(tfull + (t & 1), (t >> 1) & 1, TC_WAIT);
+      bool w = tc::mbar_wait(tfull + t % TC_NS, (t / TC_NS) & 1, TC_WAIT);
       w = __all_sync(0xffffffffu, w);
       if (w) tc::fence_after_sync();
       return w;
     };
-    auto issue = [&](int t, uint32_t (&v)[2][16]) {
+    auto issue = [&](int t, uint32_t (&v)[TC_EPI_LD][16]) {
       const uint32_t ta = tbase + ((uint32_t)(32 * qd) << 16) +
-                          (uint32_t)((t & 1) * TC_N + 4 * TC_EPI_ROWS * hf);
-      tc::tmem_ld16_async(ta, v[0]);
-      tc::tmem_ld16_async(ta + 16, v[1]);
+                          (uint32_t)((t % TC_NS) * TC_N + 4 * TC_EPI_ROWS * hf);
+#pragma unroll
+      for (int l = 0; l < TC_EPI_LD; l++) tc::tmem_ld16_async(ta + 16 * l, v[l]);
     };
-    auto finish = [&](int t, uint32_t (&v)[2][16]) {
+    auto finish = [&](int t, uint32_t (&v)[TC_EPI_LD][16]) {
       tc::tmem_wait(v[0]);
-      tc::tmem_regs_after_wait(v[1]);
+#pragma unroll
+      for (int l = 1; l < TC_EPI_LD; l++) tc::tmem_regs_after_wait(v[l]);
       tc::fence_before_sync();
       __syncwarp();
-      if (lane == 0) tc::mbar_arrive(tfree + (t & 1));   // the buffer may take tile t+2
+      if (lane == 0) tc::mbar_arrive(tfree + t % TC_NS);   // the buffer may take tile t+NS
     };
-    auto work = [&](int t, const uint32_t (&v)[2][16]) {
+    auto work = [&](int t, const uint32_t (&v)[TC_EPI_LD][16]) {
       float gx = 0.f, gy = 0.f, gz = 0.f;
 #pragma unroll
       for (int i = 0; i < TC_EPI_ROWS; i++) {
@@ -389,7 +409,7 @@ __device__ __forceinline__ void kf_tc_body(const KfTc& a_in, const int bx_) {
       Fy.add(gy);
       Fz.add(gz);
     };
-    uint32_t va[2][16], vb[2][16];
+    uint32_t va[TC_EPI_LD][16], vb[TC_EPI_LD][16];
     if (ok && a.ntn > 0) {
       ok = wait_full(0);
       if (ok) {
@@ -451,7 +471,7 @@ __device__ __forceinline__ void kf_tc_body(const KfTc& a_in, const int bx_) {
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if (warp == PW) tc::tmem_dealloc(tbase, 2 * TC_N);
+  if (warp == PW) tc::tmem_dealloc(tbase, TC_NS * TC_N);
 }
 
 // ------------------------------------------------------------- pass 1 --
