@@ -1379,6 +1379,7 @@ ShakeArgs shake_args(mg_ctx* ctx, bool measure) {
   sa.eps = ctx->epsc;
   sa.omega = ctx->omega;
   sa.maxit = ctx->shake_maxit;
+  sa.ffsweep = ctx->precision == MG_MIXED ? 1 : 0;
   sa.r = ctx->d_r;
   sa.r1 = ctx->d_r1;
   sa.f = ctx->d_f;

@@ -311,6 +311,9 @@ struct ShakeArgs {
   const double* mass;
   double hh, eps, omega;
   int maxit;
+  // 1: the three-site sweeps in float-float arithmetic on the FP32 pipe
+  // (mixed path); 0: FP64
+  int ffsweep;
   double* r;
   double* r1;
   const double* f;

@@ -2235,7 +2235,121 @@ __device__ __forceinline__ void meas_kin(ShakeMeas& m, double mi, double v1x, do
   m.pk[5] += (v1x * v1y + v2x * v2y) * mi;
 }
 
-template <bool NOSE, bool MEAS>
+// ---- float-float SHAKE sweeps (mixed path, three-site molecules) ----
+//
+// The sweeps of the three-site path in float-float arithmetic: every site's
+// position relative to the molecule's first site as hi + lo floats (about
+// 48 bits), the bond vector and its squared length to about 1e-14 A^2, the
+// deviation d then rounded to float (it only scales the displacements and
+// meets the tolerance test).  The FP64 sweeps run on GB300's narrow FP64
+// pipe; these run on the FP32 pipe.  Every rounding is explicit (`_rn`), so
+// the measuring and the plain instantiation sweep identically.
+
+__device__ __forceinline__ void ff_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fadd_rn(s, -a);
+  e = __fadd_rn(__fadd_rn(a, -__fadd_rn(s, -bb)), __fadd_rn(b, -bb));
+}
+__device__ __forceinline__ float ff_sel(int k, const float (&v)[3]) {
+  return k == 0 ? v[0] : (k == 1 ? v[1] : v[2]);
+}
+// (h, l) of site k += v: the hi sum's rounding error goes into lo exactly
+__device__ __forceinline__ void ff_add(int k, float (&h)[3], float (&l)[3], float v) {
+#pragma unroll
+  for (int s = 0; s < 3; s++)
+    if (s == k) {
+      float t, e;
+      ff_two_sum(h[s], v, t, e);
+      h[s] = t;
+      l[s] = __fadd_rn(l[s], e);
+    }
+}
+// component of p_i - p_j: (hi, lo), not renormalised
+__device__ __forceinline__ void ff_diff(int i, int j, const float (&h)[3], const float (&l)[3],
+                                        float& dh, float& dl) {
+  float e;
+  ff_two_sum(ff_sel(i, h), -ff_sel(j, h), dh, e);
+  dl = __fadd_rn(e, __fadd_rn(ff_sel(i, l), -ff_sel(j, l)));
+}
+
+// the SHAKE sweeps of cook (sim/constrd.c:821-839) on the three sites P
+// (updated in place); returns true if the tolerance was not met in maxit
+// sweeps; dsum: the deviations summed per constraint (measured steps)
+template <bool MEAS>
+__device__ __forceinline__ bool shake3_ff(double3 (&P)[3], const int (&ci)[3], const int (&cj)[3],
+                                          const double (&bq)[3], const double (&tol)[3],
+                                          const double (&awi)[3], const double (&awj)[3],
+                                          const double (&rx)[3], const double (&ry)[3],
+                                          const double (&rz)[3], int maxit,
+                                          double (&dsum)[3]) {
+  const double3 o = P[0];
+  float hx[3], hy[3], hz[3], lx[3], ly[3], lz[3];
+#pragma unroll
+  for (int s = 0; s < 3; s++) {
+    const double ux = P[s].x - o.x, uy = P[s].y - o.y, uz = P[s].z - o.z;
+    hx[s] = __double2float_rn(ux);
+    hy[s] = __double2float_rn(uy);
+    hz[s] = __double2float_rn(uz);
+    lx[s] = __double2float_rn(ux - (double)hx[s]);
+    ly[s] = __double2float_rn(uy - (double)hy[s]);
+    lz[s] = __double2float_rn(uz - (double)hz[s]);
+  }
+  float bqh[3], bql[3], tf[3], wi[3], wj[3], qx[3], qy[3], qz[3];
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    bqh[q] = __double2float_rn(bq[q]);
+    bql[q] = __double2float_rn(bq[q] - (double)bqh[q]);
+    tf[q] = __double2float_rn(tol[q]);
+    wi[q] = __double2float_rn(awi[q]);
+    wj[q] = __double2float_rn(awj[q]);
+    qx[q] = __double2float_rn(rx[q]);
+    qy[q] = __double2float_rn(ry[q]);
+    qz[q] = __double2float_rn(rz[q]);
+  }
+  int it = 0;
+  bool over;
+  do {
+    it++;
+    over = false;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      const int i = ci[q], j = cj[q];
+      float xh, xl, yh, yl, zh, zl;
+      ff_diff(i, j, hx, lx, xh, xl);
+      ff_diff(i, j, hy, ly, yh, yl);
+      ff_diff(i, j, hz, lz, zh, zl);
+      // squares: hi^2 exactly as p + e, plus 2 hi lo
+      const float px = __fmul_rn(xh, xh), py = __fmul_rn(yh, yh), pz = __fmul_rn(zh, zh);
+      const float ex = __fmaf_rn(__fmul_rn(2.f, xh), xl, __fmaf_rn(xh, xh, -px)),
+                  ey = __fmaf_rn(__fmul_rn(2.f, yh), yl, __fmaf_rn(yh, yh, -py)),
+                  ez = __fmaf_rn(__fmul_rn(2.f, zh), zl, __fmaf_rn(zh, zh, -pz));
+      float s1, e1, s2, e2;
+      ff_two_sum(px, py, s1, e1);
+      ff_two_sum(s1, pz, s2, e2);
+      const float E = __fadd_rn(__fadd_rn(__fadd_rn(e1, e2), __fadd_rn(ex, ey)), ez);
+      // d = bq - |p_i - p_j|^2
+      float t, te;
+      ff_two_sum(bqh[q], -s2, t, te);
+      const float d = __fadd_rn(t, __fadd_rn(te, __fadd_rn(bql[q], -E)));
+      over |= fabsf(d) > tf[q];
+      if constexpr (MEAS) dsum[q] += (double)d;
+      const float gi = __fmul_rn(d, wi[q]), gj = __fmul_rn(d, wj[q]);
+      ff_add(i, hx, lx, __fmul_rn(gi, qx[q]));
+      ff_add(i, hy, ly, __fmul_rn(gi, qy[q]));
+      ff_add(i, hz, lz, __fmul_rn(gi, qz[q]));
+      ff_add(j, hx, lx, __fmul_rn(gj, qx[q]));
+      ff_add(j, hy, ly, __fmul_rn(gj, qy[q]));
+      ff_add(j, hz, lz, __fmul_rn(gj, qz[q]));
+    }
+  } while (over && it < maxit);
+#pragma unroll
+  for (int s = 0; s < 3; s++)
+    P[s] = make_double3(o.x + ((double)hx[s] + (double)lx[s]), o.y + ((double)hy[s] + (double)ly[s]),
+                        o.z + ((double)hz[s] + (double)lz[s]));
+  return over;
+}
+
+template <bool NOSE, bool MEAS, bool DF>
 MG_BODY void shake_kernel_body(const ShakeArgs& a,
     const int bx_,
     const int by_) {
@@ -2293,8 +2407,9 @@ MG_BODY void shake_kernel_body(const ShakeArgs& a,
         rz[q] = ri.z - rj.z;
       }
       int it = 0;
-      bool over;
-      do {
+      bool over = false;
+      if constexpr (DF) over = shake3_ff<MEAS>(P, ci, cj, bq, tol, awi, awj, rx, ry, rz, a.maxit, dsum);
+      else do {
         it++;
         over = false;
 #pragma unroll
@@ -2452,24 +2567,30 @@ MG_BODY void shake_kernel_body(const ShakeArgs& a,
   }
 }
 
-template <bool NOSE, bool MEAS>
+template <bool NOSE, bool MEAS, bool DF>
 __global__ void __launch_bounds__(SH_THREADS) shake_kernel(const __grid_constant__ ShakeArgs a) {
-  shake_kernel_body<NOSE, MEAS>(a, blockIdx.x, 0);
+  shake_kernel_body<NOSE, MEAS, DF>(a, blockIdx.x, 0);
 }
 
 cudaError_t k_shake(const Launch& L, const ShakeArgs& a) {
   const int nb = cdiv(a.nmol, SH_THREADS);
-  if (a.vhist) {
-    if (a.meas_part)
-      shake_kernel<true, true><<<nb, SH_THREADS, 0, L.s>>>(a);
-    else
-      shake_kernel<true, false><<<nb, SH_THREADS, 0, L.s>>>(a);
-  } else {
-    if (a.meas_part)
-      shake_kernel<false, true><<<nb, SH_THREADS, 0, L.s>>>(a);
-    else
-      shake_kernel<false, false><<<nb, SH_THREADS, 0, L.s>>>(a);
-  }
+#define SHAKE_LAUNCH(DF)                                                  \
+  do {                                                                    \
+    if (a.vhist) {                                                        \
+      if (a.meas_part)                                                    \
+        shake_kernel<true, true, DF><<<nb, SH_THREADS, 0, L.s>>>(a);      \
+      else                                                                \
+        shake_kernel<true, false, DF><<<nb, SH_THREADS, 0, L.s>>>(a);     \
+    } else {                                                              \
+      if (a.meas_part)                                                    \
+        shake_kernel<false, true, DF><<<nb, SH_THREADS, 0, L.s>>>(a);     \
+      else                                                                \
+        shake_kernel<false, false, DF><<<nb, SH_THREADS, 0, L.s>>>(a);    \
+    }                                                                     \
+  } while (0)
+  if (a.ffsweep) SHAKE_LAUNCH(true);
+  else SHAKE_LAUNCH(false);
+#undef SHAKE_LAUNCH
   LAUNCHED(L);
   return cudaGetLastError();
 }
@@ -2576,7 +2697,8 @@ template <bool MEAS>
 __global__ void __launch_bounds__(SH_THREADS) batch_shake_kernel(const BoxStep* __restrict__ B) {
   const BoxStep& e = B[blockIdx.y];
   if ((int)blockIdx.x >= e.g_shake) return;
-  shake_kernel_body<false, MEAS>(e.sa, blockIdx.x, 0);
+  if (e.sa.ffsweep) shake_kernel_body<false, MEAS, true>(e.sa, blockIdx.x, 0);
+  else shake_kernel_body<false, MEAS, false>(e.sa, blockIdx.x, 0);
 }
 
 // sums k0..k1-1 of every box (one CTA each)
