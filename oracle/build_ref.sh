@@ -18,6 +18,9 @@ if [ ! -d "$REF/cook" ]; then
   exit 0
 fi
 mkdir -p "$OUT"
+# where the reference sources were found (read by the tests that compile
+# against cook's headers)
+echo "$REF" > "$OUT/REFERENCE_DIR"
 # module list of cook/configure.sh (base list + "elst ewald linklist")
 MODS="ground statics varfile bitfile cputime conjgrad gjlineq asksig simcg simgear \
 interpot setss intrapot sitesite norm xforces linregr constrd rhs simglob pakcp \
