@@ -47,7 +47,9 @@ enum mg_status {
 
 enum mg_precision {
   MG_FP64 = 0,   /* plain double precision everywhere */
-  MG_MIXED = 1   /* FP32 pair/k-space arithmetic, FP64 accumulation and reductions */
+  MG_MIXED = 1   /* FP32 pair/k-space arithmetic, FP64 accumulation and reductions;
+                    SHAKE sweeps of three-site molecules in float-float
+                    arithmetic (about 48 bits), their set-up and the rest FP64 */
 };
 
 /* The molecular topology and force-field tables cook builds in
